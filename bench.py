@@ -1,0 +1,291 @@
+"""Benchmark of the implicit edge-based residual path on GB300.
+
+A step is one residual evaluation of the NewtonIterate sequence
+(UpdateBCs, LSQ gradient, modified-Venkatakrishnan limiter, Roe + viscous
+edge fluxes, boundary fluxes, residual gather and norms) on the second-order
+laminar Navier-Stokes workload: a 128x96x96-node jittered Kuhn-tet box,
+1,179,648 nodes, 8,123,007 interior edges.  The metric is edge-flux
+throughput, Medges/s = interior edges / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on rank 0.  Under torchrun each rank runs an independent
+replica of the workload on its own GPU (the path does not shard; replicas
+only) and the slowest rank's time is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Edge-flux Medges/s; wall-time to 1e-10 residual drop, mixed/learned vs FP64"
+UNIT = "Medges/s"
+WORKLOADS = {
+    "ns128": dict(nx=128, ny=96, nz=96),
+    "ns64": dict(nx=64, ny=48, nz=48),
+    "ns256": dict(nx=256, ny=176, nz=176),
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        pg = td
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(steps_budget_s=15.0, threads=1, nx=40, ny=30, nz=30):
+    """The oracle (a scalar C port of the reference path) timed on the host
+    cores on a bounded sample of the same workload family."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import OracleSpace
+    from proteuscfd_gb300 import cases
+    case = cases.ns_flatplate(nx, ny, nz)
+    m = cases.build_mesh(case)
+    O = OracleSpace(m, case.param)
+    nrows = m.nnode + m.nbedge
+    q0 = cases.perturbed_state(O.qinf(), nrows, seed=1)
+    from concurrent.futures import ThreadPoolExecutor
+    done = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        while time.perf_counter() - t0 < steps_budget_s or done == 0:
+            list(ex.map(lambda _: O.full(q0), range(threads)))
+            done += threads
+    dt = time.perf_counter() - t0
+    return {"value": done * m.nedge / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d full residual evaluations of the %dx%dx%d second-order NS box (%d edges) by the "
+                      "oracle, %d thread(s), %.1f s" % (done, nx, ny, nz, m.nedge, threads, dt)}, dt, done
+
+
+def run_reference(args, rank, pg):
+    """--impl reference: the reference's CPU path (the oracle port; the
+    reference itself does not build without HDF5/MPI/METIS) on all host
+    threads, rank 0 only."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    w = WORKLOADS[args.workload]
+    # warm-up then timed steps; each step = one parallel round over all threads
+    cpu_sample(0.0, threads)
+    base, dt, done = cpu_sample(max(5.0, 2.0 * args.steps), threads)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done / threads, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "ns_flatplate %dx%dx%d (CPU sample 40x30x30)" % (w["nx"], w["ny"], w["nz"]),
+                       "sample_edges": None},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local, pg):
+    from proteuscfd_gb300 import SolutionSpace, cases
+    from proteuscfd_gb300 import _native as N
+    lib = N.load()
+    N.check(lib.pcfd_set_device(local), "pcfd_set_device")
+    w = WORKLOADS[args.workload]
+    case = cases.ns_flatplate(w["nx"], w["ny"], w["nz"])
+    t_mesh = time.perf_counter()
+    m = cases.build_mesh(case)
+    t_mesh = time.perf_counter() - t_mesh
+    S = SolutionSpace(m, case.param)
+    nrows = m.nnode + m.nbedge
+    q0 = cases.perturbed_state(S.qinf(), nrows, seed=1)
+    S.set_state(q0)
+    S.bench_residual_full(max(args.warmup, 3))
+    # timed region: K steps on the device, inputs resident in HBM
+    barrier(pg)
+    N.check(lib.pcfd_device_sync(), "sync")
+    l0 = S.launch_count()
+    with ClockSampler(local) as clk:
+        ms, norms = S.bench_residual_full(args.steps)
+    launches = S.launch_count() - l0
+    barrier(pg)
+    ms = max_over_ranks(pg, ms)
+    ms_per_step = ms / args.steps
+    value = ws * m.nedge / (ms_per_step * 1e-3) / 1e6
+
+    # per-kernel breakdown (events around each launch on the library's stream)
+    S.profile(True)
+    S.profile_reset()
+    nprof = 3
+    for _ in range(nprof):
+        S.residual_full()
+    timers = S.timers()
+    S.profile(False)
+
+    # end to end through the C ABI with host buffers: H2D of q, the step,
+    # D2H of b and the norms, every step
+    qh = np.ascontiguousarray(q0)
+    S.set_state(qh)
+    S.residual_full()
+    S.compute_residuals()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.set_state(qh)
+        S.residual_full()
+        b, _n = S.compute_residuals()
+    N.check(lib.pcfd_device_sync(), "sync")
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = max_over_ranks(pg, e2e_s)
+    h2d = qh.nbytes
+    d2h = b.nbytes + 6 * 8
+
+    # roofline of the dominant kernel, the edge-flux kernel: algorithmic bytes
+    # per launch = 40 B/edge (2 int32 ids + 4 fp64 area) + 320 B/node (q 40,
+    # xyz 24, qgrad 216, limiter 40); FP64 flops counted from the kernel source
+    ef_ms, ef_n = timers.get("edge_flux", (0.0, 0))
+    ef_avg = ef_ms / max(ef_n, 1)
+    alg_bytes = 40.0 * m.nedge + 320.0 * m.nnode
+    achieved = alg_bytes / (ef_avg * 1e-3) / 1e9 if ef_avg > 0 else None
+    peak, peak_kind = peaks()
+    tot_prof = sum(v[0] for v in timers.values() if v[1]) or 1.0
+    kernels = {k: {"ms_per_step": v[0] / nprof, "share": v[0] / tot_prof} for k, v in timers.items() if v[1]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+Venkat "
+                               "limiter K=5+Roe+viscous), Mach 0.8, Re 1e5" % (w["nx"], w["ny"], w["nz"]),
+                   "nodes": m.nnode, "edges": m.nedge, "half_edges": m.nbedge,
+                   "l2": "inputs larger than L2 (edge arrays alone %.0f MB)" % (m.nedge * 104 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "mesh_build_s": round(t_mesh, 2)},
+        "resGlobal": float(norms[0]),
+        "gpu_launches": int(launches),
+        "kernels": kernels,
+        "roofline": {"bound": "hbm", "kernel": "edge_flux", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind,
+                     "note": "FP64-pipe bound on GB300; HBM fraction reported against the measured copy peak"},
+        "clocks": clk.summary(),
+        "e2e": {"value": ws * m.nedge / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        base, _, _ = cpu_sample(12.0, 1)
+        line["cpu_baseline"] = base
+    S.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ns128", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local, pg = dist()
+    if args.impl == "reference":
+        run_reference(args, rank, pg)
+    else:
+        run_gb300(args, ws, rank, local, pg)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

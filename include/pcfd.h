@@ -1,0 +1,198 @@
+/*
+ * pcfd.h - C ABI of the GB300 (sm_103a) implementation of ProteusCFD's
+ * implicit edge-based finite-volume hot path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (PCFD_OK = 0) and never exits the process; pcfd_last_error()
+ * gives the text of the last failure on the calling thread.  All device
+ * entry points are synchronous at return and run on the handle's own CUDA
+ * stream.  Caller buffers are borrowed only for the duration of a call; the
+ * library owns its device mirrors and never frees caller memory.
+ *
+ * Each entry point names the reference interface it stands in for
+ * (file:line within ngcurrier/ProteusCFD).
+ */
+#ifndef PCFD_H_
+#define PCFD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PCFD_API __attribute__((visibility("default")))
+#else
+#define PCFD_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PCFD_OK 0
+#define PCFD_ERR_ARG 1         /* bad argument (null pointer, size out of range) */
+#define PCFD_ERR_STATE 2       /* call made in the wrong order */
+#define PCFD_ERR_CUDA 3        /* CUDA runtime error */
+#define PCFD_ERR_MESH 4        /* mesh preprocessing failed */
+#define PCFD_ERR_NOMEM 5       /* allocation failed */
+#define PCFD_ERR_UNSUPPORTED 6 /* option not available in this build */
+#define PCFD_ERR_NUMERIC 7     /* device reported a numerical failure (see pcfd_get_health) */
+
+/* ---- boundary condition types -------------------------------------------
+ * Same integer values as the reference's BCTypes enum (ucs/bc_defines.h:4),
+ * so a .bc table read by the reference can be passed through unchanged.    */
+enum pcfd_bc_type {
+  PCFD_BC_PARALLEL = 0,
+  PCFD_BC_DIRICHLET = 1,
+  PCFD_BC_NEUMANN = 2,
+  PCFD_BC_IMPERMEABLE_WALL = 3,
+  PCFD_BC_NOSLIP = 4,
+  PCFD_BC_FARFIELD_VISCOUS = 5,
+  PCFD_BC_FARFIELD = 6,
+  PCFD_BC_SONIC_INFLOW = 7,
+  PCFD_BC_SONIC_OUTFLOW = 8,
+  PCFD_BC_SYMMETRY = 9
+};
+
+/* ---- host mesh preprocessing -------------------------------------------- */
+
+/* Synthetic workload: an nx*ny*nz node box split into 6 Kuhn tets per hex.
+ * tags[f] is the boundary tag of face f (x=0, x=max, y=0, y=max, z=0, z=max). */
+typedef struct pcfd_box_params {
+  int nx, ny, nz;
+  double lx, ly, lz;  /* box extents */
+  double jitter;      /* interior-node jitter as a fraction of the local spacing */
+  uint64_t seed;      /* jitter seed */
+  double ramp_deg;    /* shear ramp angle of the y=0 wall for x > ramp_x0 (0 = none) */
+  double ramp_x0;
+  double y_ratio;     /* geometric clustering ratio toward y=0 (<= 1: uniform) */
+  int tags[6];
+} pcfd_box_params;
+
+typedef void* pcfd_mesh_t;
+
+/* Mesh arrays in the reference's layout (Mesh<T> members, ucs/mesh.h:202-203;
+ * Edges/HalfEdges, ucs/uns_base.h:13,28).  Phantom node of half-edge k is
+ * nnode + k.  All arrays are host memory. */
+typedef struct pcfd_mesh_view {
+  int nnode;               /* interior nodes */
+  int nbnode;              /* phantom (boundary) nodes = nbedge */
+  int nedge;               /* interior edges */
+  int nbedge;              /* boundary half-edges */
+  const int* edges;        /* [nedge][2] (Edges::n) */
+  const double* edge_area; /* [nedge][4] unit normal + magnitude (Edges::a) */
+  const int* bedges;       /* [nbedge][2] node, phantom id (HalfEdges::n) */
+  const double* bedge_area;/* [nbedge][4] (HalfEdges::a) */
+  const int* bfactag;      /* [nbedge] (HalfEdges::factag) */
+  const double* xyz;       /* [nnode][3] */
+  const double* vol;       /* [nnode] dual volumes */
+  const double* sw;        /* [nnode][6] weighted LSQ normal matrix (Mesh::sw) */
+  const int* ipsp;         /* [nnode+1] */
+  const int* psp;          /* [ipsp[nnode]] */
+} pcfd_mesh_view;
+
+/* Generator for the synthetic boxes (no reference counterpart: the reference
+ * reads meshes from files, ucs/mesh.tcc:2820). */
+PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p);
+/* Element-list input, the data a UGRID reader would produce
+ * (ucs/mesh.tcc:6740): triangles [ntri][3] with tags, tets [ntet][4]. */
+PCFD_API pcfd_mesh_t pcfd_mesh_from_elements(int nnode, const double* xyz, int ntri, const int* tri,
+                                             const int* tri_tag, int ntet, const int* tet);
+/* Mesh::BuildMaps + Mesh::CalcMetrics (ucs/mesh.tcc:265,1576) and
+ * ComputeNodeLSQCoefficients (ucs/gradient.tcc:115). */
+PCFD_API int pcfd_mesh_build(pcfd_mesh_t m);
+PCFD_API int pcfd_mesh_view_get(pcfd_mesh_t m, pcfd_mesh_view* v);
+PCFD_API int pcfd_mesh_stats(pcfd_mesh_t m, int* nelem_tri, int* nelem_tet, int* rewound, int* unclosed,
+                             double* max_open, double* total_vol);
+/* Mesh::ReorderMeshCuthillMcKee(1) order (ucs/mesh.tcc:2412): order[new] = old. */
+PCFD_API int pcfd_mesh_rcm_order(pcfd_mesh_t m, int* order_out);
+/* Mesh::ReorderC2nMap (ucs/mesh.tcc:224): renumber nodes; rebuild afterwards. */
+PCFD_API int pcfd_mesh_renumber(pcfd_mesh_t m, const int* order);
+PCFD_API void pcfd_mesh_destroy(pcfd_mesh_t m);
+PCFD_API const char* pcfd_mesh_last_error(void);
+
+/* ---- device solver ------------------------------------------------------- */
+
+/* The subset of Param<T> (ucs/param.h:31) the hot path reads.  Values are the
+ * reference's non-dimensional ones (velocity scale = freestream sound speed). */
+typedef struct pcfd_params {
+  double gamma;           /* Param::gamma */
+  double mach;            /* Param::velocity (= Mach number) */
+  double flowdir[3];      /* Param::flowdir */
+  double Re;              /* Param::Re */
+  double Pr, PrT;         /* Param::Pr, Param::PrT */
+  double ref_temperature; /* Param::ref_temperature [K] (Sutherland, wall T) */
+  int sorder;             /* spatial order 1 or 2 (Param::sorder) */
+  double chi;             /* MUSCL blend (Param::chi) */
+  int viscous;            /* 0 Euler, 1 laminar Navier-Stokes */
+  int limiter;            /* 0 none, 3 modified Venkatakrishnan (Param::limiter) */
+  double venkat_K;        /* limiter K; the reference hard-codes 1.0 */
+  int no_cvbc;            /* Param::no_cvbc */
+  int ntags;              /* entries in bc_type/bc_twall, indexed by factag */
+  const int* bc_type;     /* pcfd_bc_type per factag */
+  const double* bc_twall; /* BCObj::twall per factag [K]; < 0 = adiabatic */
+} pcfd_params;
+
+typedef void* pcfd_solver_t;
+
+/* Allocates device mirrors of the mesh and all fields (SolutionSpace::Init,
+ * ucs/solutionSpace.tcc:148) and initialises q to the freestream
+ * (CompressibleEqnSet::SetInitialConditions, ucs/compressible.tcc:884). */
+PCFD_API int pcfd_create(const pcfd_mesh_view* mesh, const pcfd_params* params, pcfd_solver_t* out);
+PCFD_API int pcfd_destroy(pcfd_solver_t s);
+
+/* q in the reference layout: [nnode+nbnode][nvars], nvars = 10
+ * (rho, rho u, rho v, rho w, rho E | T, P, u, v, w), ucs/compressible.tcc:11-22. */
+PCFD_API int pcfd_set_state(pcfd_solver_t s, const double* q, int nvars, int nrows);
+PCFD_API int pcfd_get_state(pcfd_solver_t s, double* q, int nvars, int nrows);
+/* freestream state Qinf (10 values), CompressibleEqnSet::UpdateQinf (ucs/compressible.tcc:827) */
+PCFD_API int pcfd_get_qinf(pcfd_solver_t s, double* qinf10);
+
+/* UpdateBCs (ucs/bc.tcc:1400): phantom states and hard-set boundary nodes. */
+PCFD_API int pcfd_update_bcs(pcfd_solver_t s);
+/* Gradient<T>::Compute (ucs/gradient.tcc:57), weighted LSQ; qgrad_out
+ * optional [nnode][9][3] in the reference layout. */
+PCFD_API int pcfd_gradient(pcfd_solver_t s, double* qgrad_out);
+/* Limiter<T>::Compute (ucs/limiters.tcc:53); l_out optional [nnode][5]. */
+PCFD_API int pcfd_limiter(pcfd_solver_t s, double* l_out);
+/* ComputeResiduals (ucs/residual.tcc:13): b (= -R) into b_out [nnode][5]
+ * (optional) and norms_out[0..5] = {resGlobal, per-equation norms}. */
+PCFD_API int pcfd_residual(pcfd_solver_t s, double* b_out, double* norms_out);
+/* UpdateBCs + gradient + limiter + residual in one call, the sequence
+ * NewtonIterate runs (ucs/solutionSpace.tcc:662-697), without copying fields
+ * back; norms_out as for pcfd_residual. */
+PCFD_API int pcfd_residual_full(pcfd_solver_t s, double* norms_out);
+
+/* Runs nsteps of pcfd_residual_full back to back on the handle's stream and
+ * returns their device time from CUDA events recorded on that stream (the
+ * reference's ResidualTimer, ucs/solutionSpace.tcc:692-701). */
+PCFD_API int pcfd_bench_residual_full(pcfd_solver_t s, int nsteps, double* ms_out, double* norms_out);
+/* Selects the CUDA device for handles created afterwards on this thread. */
+PCFD_API int pcfd_set_device(int device);
+/* Waits for all work on the current device. */
+PCFD_API int pcfd_device_sync(void);
+
+/* Per-kernel device time accumulated since the last reset, in the spirit of
+ * the reference's TimerList (ucs/timer.h:29).  Timing uses CUDA events on the
+ * handle's stream and is off unless enabled. */
+PCFD_API int pcfd_profile_enable(pcfd_solver_t s, int on);
+PCFD_API int pcfd_profile_reset(pcfd_solver_t s);
+/* name_buf receives the i-th timer's name; returns PCFD_ERR_ARG past the end */
+PCFD_API int pcfd_profile_get(pcfd_solver_t s, int i, char* name_buf, int name_len, double* ms_total,
+                              long long* launches);
+/* number of kernel launches issued by the library on this handle */
+PCFD_API long long pcfd_launch_count(pcfd_solver_t s);
+
+/* Health word the device kernels maintain (NaN fluxes kneecapped, clips,
+ * ...), replacing the reference's warnings/soft aborts (ucs/eqnset.tcc:73-88,
+ * ucs/exceptions.h:51-63).  counters[0..7]. */
+PCFD_API int pcfd_get_health(pcfd_solver_t s, long long* counters8);
+
+PCFD_API const char* pcfd_last_error(void);
+PCFD_API const char* pcfd_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCFD_H_ */

@@ -1,0 +1,40 @@
+/*
+ * CPU ORACLE - test infrastructure only (see oracle.c).  Plain-C restatement
+ * of the reference's residual path used to check the CUDA implementation.
+ */
+#ifndef PCFD_ORACLE_H_
+#define PCFD_ORACLE_H_
+
+#include "../include/pcfd.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void oracle_aux(double gamma, double* Q);
+void oracle_qinf(const pcfd_params* prm, double* Qinf);
+void oracle_init_state(const pcfd_params* prm, int nrows, double* q);
+void oracle_matvec(const double* a, const double* x, double* y, int n);
+void oracle_roe_flux(const double* QL, const double* QR, const double* avec, double vdotn, double gamma,
+                     double* flux);
+void oracle_viscous_flux(const pcfd_params* prm, const double* Q, const double* grad, const double* avec, double mut,
+                         double* flux);
+int oracle_normal_node(const pcfd_mesh_view* m, int node, const double* avec);
+int oracle_update_bcs(const pcfd_mesh_view* m, const pcfd_params* prm, double* q);
+int oracle_gradient(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, double* grad);
+int oracle_limiter(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
+                   double* l, long long* nclip);
+int oracle_residual(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
+                    const double* lim, double* b, double* norms, long long* nkneecap);
+int oracle_residual_scaled(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
+                           const double* lim, double* b, double* babs, double* norms, long long* nkneecap);
+int oracle_lu(double* a, int* p, int n);
+void oracle_lusolve(const double* a, double* b, const int* p, double* x, int n);
+void oracle_tri_area(const double* p1, const double* p2, const double* p3, double* r);
+double oracle_tet_vol(const double* p1, const double* p2, const double* p3, const double* p4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,142 @@
+"""ctypes bindings of libpcfd.so (the C ABI in include/pcfd.h).
+
+The library is loaded from the package directory; if it is absent the import
+fails loudly - there is no CPU fallback for the device path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libpcfd.so"
+
+PCFD_OK = 0
+ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "MESH", 5: "NOMEM", 6: "UNSUPPORTED", 7: "NUMERIC"}
+
+# boundary condition types: the reference's BCTypes values (ucs/bc_defines.h:4)
+BC_PARALLEL = 0
+BC_DIRICHLET = 1
+BC_NEUMANN = 2
+BC_IMPERMEABLE_WALL = 3
+BC_NOSLIP = 4
+BC_FARFIELD_VISCOUS = 5
+BC_FARFIELD = 6
+BC_SONIC_INFLOW = 7
+BC_SONIC_OUTFLOW = 8
+BC_SYMMETRY = 9
+
+
+class BoxParams(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("jitter", C.c_double), ("seed", C.c_uint64),
+        ("ramp_deg", C.c_double), ("ramp_x0", C.c_double), ("y_ratio", C.c_double),
+        ("tags", C.c_int * 6),
+    ]
+
+
+class MeshView(C.Structure):
+    _fields_ = [
+        ("nnode", C.c_int), ("nbnode", C.c_int), ("nedge", C.c_int), ("nbedge", C.c_int),
+        ("edges", C.POINTER(C.c_int)), ("edge_area", C.POINTER(C.c_double)),
+        ("bedges", C.POINTER(C.c_int)), ("bedge_area", C.POINTER(C.c_double)),
+        ("bfactag", C.POINTER(C.c_int)),
+        ("xyz", C.POINTER(C.c_double)), ("vol", C.POINTER(C.c_double)), ("sw", C.POINTER(C.c_double)),
+        ("ipsp", C.POINTER(C.c_int)), ("psp", C.POINTER(C.c_int)),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gamma", C.c_double), ("mach", C.c_double), ("flowdir", C.c_double * 3),
+        ("Re", C.c_double), ("Pr", C.c_double), ("PrT", C.c_double), ("ref_temperature", C.c_double),
+        ("sorder", C.c_int), ("chi", C.c_double), ("viscous", C.c_int), ("limiter", C.c_int),
+        ("venkat_K", C.c_double), ("no_cvbc", C.c_int), ("ntags", C.c_int),
+        ("bc_type", C.POINTER(C.c_int)), ("bc_twall", C.POINTER(C.c_double)),
+    ]
+
+
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+_LLP = C.POINTER(C.c_longlong)
+
+# name -> (restype, argtypes); every symbol include/pcfd.h declares
+PROTOTYPES = {
+    "pcfd_mesh_box_create": (_P, [C.POINTER(BoxParams)]),
+    "pcfd_mesh_from_elements": (_P, [C.c_int, _DP, C.c_int, _IP, _IP, C.c_int, _IP]),
+    "pcfd_mesh_build": (C.c_int, [_P]),
+    "pcfd_mesh_view_get": (C.c_int, [_P, C.POINTER(MeshView)]),
+    "pcfd_mesh_stats": (C.c_int, [_P, _IP, _IP, _IP, _IP, _DP, _DP]),
+    "pcfd_mesh_rcm_order": (C.c_int, [_P, _IP]),
+    "pcfd_mesh_renumber": (C.c_int, [_P, _IP]),
+    "pcfd_mesh_destroy": (None, [_P]),
+    "pcfd_mesh_last_error": (C.c_char_p, []),
+    "pcfd_create": (C.c_int, [C.POINTER(MeshView), C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "pcfd_destroy": (C.c_int, [_P]),
+    "pcfd_set_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
+    "pcfd_get_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
+    "pcfd_get_qinf": (C.c_int, [_P, _DP]),
+    "pcfd_update_bcs": (C.c_int, [_P]),
+    "pcfd_gradient": (C.c_int, [_P, _DP]),
+    "pcfd_limiter": (C.c_int, [_P, _DP]),
+    "pcfd_residual": (C.c_int, [_P, _DP, _DP]),
+    "pcfd_residual_full": (C.c_int, [_P, _DP]),
+    "pcfd_bench_residual_full": (C.c_int, [_P, C.c_int, _DP, _DP]),
+    "pcfd_set_device": (C.c_int, [C.c_int]),
+    "pcfd_device_sync": (C.c_int, []),
+    "pcfd_profile_enable": (C.c_int, [_P, C.c_int]),
+    "pcfd_profile_reset": (C.c_int, [_P]),
+    "pcfd_profile_get": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, _DP, _LLP]),
+    "pcfd_launch_count": (C.c_longlong, [_P]),
+    "pcfd_get_health": (C.c_int, [_P, _LLP]),
+    "pcfd_last_error": (C.c_char_p, []),
+    "pcfd_build_info": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path: Path | None = None) -> C.CDLL:
+    """Load libpcfd.so and attach prototypes; raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            "libpcfd.so not found at %s; build it with `python -m proteuscfd_gb300.build` "
+            "(there is no CPU fallback)" % p)
+    lib = C.CDLL(str(p))
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class PcfdError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__("%s failed: PCFD_ERR_%s (%d): %s" % (where, ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+def check(rc: int, where: str) -> None:
+    if rc != PCFD_OK:
+        msg = load().pcfd_last_error()
+        raise PcfdError(rc, where, msg.decode() if msg else "")
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_DP)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_IP)

@@ -1,0 +1,285 @@
+"""Host-side interface mirroring the reference's operator API for the hot path.
+
+The names follow the reference's classes and functions, with the device work
+behind the C ABI of libpcfd.so:
+
+=====================================  =====================================================
+this module                            reference (ngcurrier/ProteusCFD)
+=====================================  =====================================================
+``Mesh.box`` / ``Mesh.from_elements``  mesh readers + ``Mesh::BuildMaps``/``CalcMetrics``
+                                       (ucs/mesh.tcc:265,1576)
+``Param``                              ``Param<T>`` (ucs/param.h:31), hot-path subset
+``SolutionSpace.update_bcs``           ``UpdateBCs`` (ucs/bc.tcc:1400)
+``SolutionSpace.gradient``             ``Gradient<T>::Compute`` (ucs/gradient.tcc:57)
+``SolutionSpace.limiter``              ``Limiter<T>::Compute`` (ucs/limiters.tcc:53)
+``SolutionSpace.compute_residuals``    ``ComputeResiduals`` (ucs/residual.tcc:13)
+=====================================  =====================================================
+
+Errors raise ``PcfdError`` (the reference aborts through ``Abort <<``,
+ucs/exceptions.h:30-49).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+
+NEQN = 5
+NVARS = 10
+NTERMS = 9
+
+
+class Mesh:
+    """Host mesh with the reference's maps and dual metrics."""
+
+    def __init__(self, handle):
+        self._lib = N.load()
+        self._h = None
+        if not handle:
+            raise N.PcfdError(4, "mesh create", self._lib.pcfd_mesh_last_error().decode())
+        self._h = handle
+        rc = self._lib.pcfd_mesh_build(self._h)
+        if rc != 0:
+            msg = self._lib.pcfd_mesh_last_error().decode()
+            self._lib.pcfd_mesh_destroy(self._h)
+            self._h = None
+            raise N.PcfdError(rc, "pcfd_mesh_build", msg)
+        self.view = N.MeshView()
+        N.check(self._lib.pcfd_mesh_view_get(self._h, C.byref(self.view)), "pcfd_mesh_view_get")
+
+    @classmethod
+    def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5,
+            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6)):
+        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags))
+        return cls(N.load().pcfd_mesh_box_create(C.byref(p)))
+
+    @classmethod
+    def from_elements(cls, xyz, tris, tri_tags, tets):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        tris = np.ascontiguousarray(tris, dtype=np.int32)
+        tri_tags = np.ascontiguousarray(tri_tags, dtype=np.int32)
+        tets = np.ascontiguousarray(tets, dtype=np.int32)
+        h = N.load().pcfd_mesh_from_elements(len(xyz), N.dptr(xyz), len(tris), N.iptr(tris), N.iptr(tri_tags),
+                                             len(tets), N.iptr(tets))
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.pcfd_mesh_destroy(self._h)
+            self._h = None
+
+    # numpy views of the host arrays (valid while the Mesh lives)
+    def _arr(self, ptr, n, dtype):
+        return np.ctypeslib.as_array(ptr, shape=(n,)).view(dtype) if n else np.zeros(0, dtype)
+
+    @property
+    def nnode(self):
+        return self.view.nnode
+
+    @property
+    def nedge(self):
+        return self.view.nedge
+
+    @property
+    def nbedge(self):
+        return self.view.nbedge
+
+    @property
+    def edges(self):
+        return self._arr(self.view.edges, 2 * self.nedge, np.int32).reshape(-1, 2)
+
+    @property
+    def edge_area(self):
+        return self._arr(self.view.edge_area, 4 * self.nedge, np.float64).reshape(-1, 4)
+
+    @property
+    def bedges(self):
+        return self._arr(self.view.bedges, 2 * self.nbedge, np.int32).reshape(-1, 2)
+
+    @property
+    def bedge_area(self):
+        return self._arr(self.view.bedge_area, 4 * self.nbedge, np.float64).reshape(-1, 4)
+
+    @property
+    def bfactag(self):
+        return self._arr(self.view.bfactag, self.nbedge, np.int32)
+
+    @property
+    def xyz(self):
+        return self._arr(self.view.xyz, 3 * self.nnode, np.float64).reshape(-1, 3)
+
+    @property
+    def vol(self):
+        return self._arr(self.view.vol, self.nnode, np.float64)
+
+    @property
+    def sw(self):
+        return self._arr(self.view.sw, 6 * self.nnode, np.float64).reshape(-1, 6)
+
+    @property
+    def ipsp(self):
+        return self._arr(self.view.ipsp, self.nnode + 1, np.int32)
+
+    @property
+    def psp(self):
+        n = int(self.ipsp[-1])
+        return self._arr(self.view.psp, n, np.int32)
+
+    def stats(self):
+        a = [C.c_int() for _ in range(4)]
+        d = [C.c_double() for _ in range(2)]
+        N.check(self._lib.pcfd_mesh_stats(self._h, *[C.byref(x) for x in a], *[C.byref(x) for x in d]),
+                "pcfd_mesh_stats")
+        keys = ("ntri", "ntet", "rewound", "unclosed")
+        out = {k: x.value for k, x in zip(keys, a)}
+        out["max_open"] = d[0].value
+        out["total_vol"] = d[1].value
+        return out
+
+    def rcm_order(self):
+        order = np.zeros(self.nnode, dtype=np.int32)
+        N.check(self._lib.pcfd_mesh_rcm_order(self._h, N.iptr(order)), "pcfd_mesh_rcm_order")
+        return order
+
+
+@dataclass
+class Param:
+    """Hot-path subset of ``Param<T>`` (ucs/param.h:31); non-dimensional values."""
+
+    gamma: float = 1.4
+    mach: float = 0.5
+    flowdir: tuple = (1.0, 0.0, 0.0)
+    Re: float = 1.0
+    Pr: float = 0.72
+    PrT: float = 0.85
+    ref_temperature: float = 300.0
+    sorder: int = 1
+    chi: float = 0.0
+    viscous: int = 0
+    limiter: int = 0
+    venkat_K: float = 1.0
+    no_cvbc: int = 0
+    bc_type: dict = field(default_factory=dict)   # factag -> BC type
+    bc_twall: dict = field(default_factory=dict)  # factag -> wall temperature [K] (<0 adiabatic)
+
+    def to_c(self):
+        ntags = max(self.bc_type) + 1 if self.bc_type else 1
+        bct = np.zeros(ntags, dtype=np.int32)
+        btw = np.full(ntags, 1.0, dtype=np.float64)  # BCObj default twall = 1 K
+        for k, v in self.bc_type.items():
+            bct[k] = v
+        for k, v in self.bc_twall.items():
+            btw[k] = v
+        p = N.Params()
+        p.gamma, p.mach = self.gamma, self.mach
+        p.flowdir = (C.c_double * 3)(*self.flowdir)
+        p.Re, p.Pr, p.PrT, p.ref_temperature = self.Re, self.Pr, self.PrT, self.ref_temperature
+        p.sorder, p.chi, p.viscous, p.limiter = self.sorder, self.chi, self.viscous, self.limiter
+        p.venkat_K, p.no_cvbc, p.ntags = self.venkat_K, self.no_cvbc, ntags
+        p.bc_type = N.iptr(bct)
+        p.bc_twall = N.dptr(btw)
+        p._keep = (bct, btw)
+        return p
+
+
+class SolutionSpace:
+    """Device-resident solution space for one mesh (``SolutionSpace<T>``,
+    ucs/solutionSpace.h), driven through the C ABI."""
+
+    def __init__(self, mesh: Mesh, param: Param):
+        self._lib = N.load()
+        self.mesh = mesh
+        self.param = param
+        self._cp = param.to_c()
+        h = C.c_void_p()
+        N.check(self._lib.pcfd_create(C.byref(mesh.view), C.byref(self._cp), C.byref(h)), "pcfd_create")
+        self._h = h
+        self.nrows = mesh.nnode + mesh.view.nbnode
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pcfd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_state(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.nrows, NVARS)
+        N.check(self._lib.pcfd_set_state(self._h, N.dptr(q), NVARS, self.nrows), "pcfd_set_state")
+
+    def get_state(self):
+        q = np.empty((self.nrows, NVARS), dtype=np.float64)
+        N.check(self._lib.pcfd_get_state(self._h, N.dptr(q), NVARS, self.nrows), "pcfd_get_state")
+        return q
+
+    def qinf(self):
+        q = np.empty(NVARS, dtype=np.float64)
+        N.check(self._lib.pcfd_get_qinf(self._h, N.dptr(q)), "pcfd_get_qinf")
+        return q
+
+    def update_bcs(self):
+        N.check(self._lib.pcfd_update_bcs(self._h), "pcfd_update_bcs")
+
+    def gradient(self):
+        g = np.empty((self.mesh.nnode, NTERMS * 3), dtype=np.float64)
+        N.check(self._lib.pcfd_gradient(self._h, N.dptr(g)), "pcfd_gradient")
+        return g
+
+    def limiter(self):
+        lim = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        N.check(self._lib.pcfd_limiter(self._h, N.dptr(lim)), "pcfd_limiter")
+        return lim
+
+    def compute_residuals(self, want_b=True):
+        """Returns (b, norms); norms = [resGlobal, per-equation] (ComputeResiduals)."""
+        b = np.empty((self.mesh.nnode, NEQN), dtype=np.float64) if want_b else None
+        norms = np.empty(6, dtype=np.float64)
+        N.check(self._lib.pcfd_residual(self._h, N.dptr(b) if want_b else None, N.dptr(norms)), "pcfd_residual")
+        return b, norms
+
+    def residual_full(self):
+        norms = np.empty(6, dtype=np.float64)
+        N.check(self._lib.pcfd_residual_full(self._h, N.dptr(norms)), "pcfd_residual_full")
+        return norms
+
+    def bench_residual_full(self, nsteps):
+        """Device time (ms) of nsteps back-to-back residual evaluations."""
+        ms = C.c_double()
+        norms = np.empty(6, dtype=np.float64)
+        N.check(self._lib.pcfd_bench_residual_full(self._h, int(nsteps), C.byref(ms), N.dptr(norms)),
+                "pcfd_bench_residual_full")
+        return ms.value, norms
+
+    def health(self):
+        c = (C.c_longlong * 8)()
+        N.check(self._lib.pcfd_get_health(self._h, c), "pcfd_get_health")
+        return list(c)
+
+    def profile(self, on=True):
+        N.check(self._lib.pcfd_profile_enable(self._h, 1 if on else 0), "pcfd_profile_enable")
+
+    def profile_reset(self):
+        N.check(self._lib.pcfd_profile_reset(self._h), "pcfd_profile_reset")
+
+    def timers(self):
+        out = {}
+        i = 0
+        buf = C.create_string_buffer(64)
+        while True:
+            ms, n = C.c_double(), C.c_longlong()
+            if self._lib.pcfd_profile_get(self._h, i, buf, 64, C.byref(ms), C.byref(n)) != 0:
+                break
+            out[buf.value.decode()] = (ms.value, n.value)
+            i += 1
+        return out
+
+    def launch_count(self):
+        return int(self._lib.pcfd_launch_count(self._h))

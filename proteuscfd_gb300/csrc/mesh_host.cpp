@@ -1,0 +1,682 @@
+// Host-side mesh preprocessing for the edge-based median-dual finite-volume path.
+//
+// This file builds, on the host and in FP64, the integer maps and dual metrics
+// that the reference computes before its first Newton step, following the
+// reference's algorithms and traversal orders so that the resulting arrays are
+// the ones the reference's kernels would see for the same element list:
+//
+//   element-surrounding-point map ......... ucs/mesh.tcc:397   (Mesh::BuildElsp)
+//   point-surrounding-point map + dedup ... ucs/mesh.tcc:517   (Mesh::BuildPsp, cl table :541-548)
+//                                            ucs/mesh.tcc:1341  (Mesh::EliminateRepeats)
+//   interior edges and boundary half-edges  ucs/mesh.tcc:1056  (Mesh::BuildEdges)
+//   median-dual areas and volumes .......... ucs/mesh.tcc:1653  (Mesh::CalcAreasVolumes)
+//   closure check + normalisation .......... ucs/mesh.tcc:2274  (Mesh::CheckForClosure)
+//   boundary winding check ................. ucs/mesh.tcc:2336  (Mesh::FixBoundaryWindings)
+//   weighted LSQ normal matrices ........... ucs/gradient.tcc:115,461 (ComputeNodeLSQCoefficients)
+//   reverse Cuthill-McKee renumbering ...... ucs/mesh.tcc:2412  (Mesh::ReorderMeshCuthillMcKee)
+//
+// It also holds the synthetic workload generator: an Nx x Ny x Nz node box
+// split into 6 Kuhn tetrahedra per hex (all sharing the hex's (0,0,0)-(1,1,1)
+// diagonal), with seeded jitter of interior nodes, an optional sheared ramp
+// and optional geometric wall clustering.  Only tetrahedra and boundary
+// triangles occur, so only the TET/TRI rows of the reference's element tables
+// are used.
+//
+// Everything here is plain C++ with a C ABI (declared in include/pcfd.h);
+// nothing depends on CUDA.
+
+#include "../../include/pcfd.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+
+enum { ETRI = 0, ETET = 2 };
+
+struct HostMesh {
+  // geometry
+  int nnode = 0;
+  std::vector<double> xyz;          // [nnode][3]
+  // element list in reference order (boundary triangles first, then tets)
+  std::vector<int> etype;           // ETRI / ETET
+  std::vector<int> enodes;          // [nelem][4] (triangles use 3)
+  std::vector<int> efactag;         // triangles: boundary tag; tets: 0
+  // maps
+  std::vector<int> ielsp, elsp;
+  std::vector<int> ipsp, psp;
+  std::vector<int> edges;           // [nedge][2]
+  std::vector<double> ea;           // [nedge][4]
+  std::vector<int> bedges;          // [nbedge][2]  (node, phantom id)
+  std::vector<int> belem;           // [nbedge] owning boundary element
+  std::vector<int> bfactag;         // [nbedge]
+  std::vector<double> ba;           // [nbedge][4]
+  std::vector<double> vol;          // [nnode]
+  std::vector<double> sw;           // [nnode][6]
+  int nedge = 0, nbedge = 0;
+  int maps_built = 0, metrics_built = 0;
+  int rewound = 0;
+  int unclosed = 0;
+  int inverted = 0;
+  double max_open = 0.0;
+  std::string err;
+};
+
+// ---- small geometry helpers with the reference's operation order ----------
+// (ucs/geometry.h: Subtract :12, Magnitude :41, Normalize :51, CrossProduct
+//  :68, Centroid :133-215, CalcTriArea, CalcTetVol)
+inline void sub3(const double* a, const double* b, double* r) {
+  r[0] = a[0] - b[0]; r[1] = a[1] - b[1]; r[2] = a[2] - b[2];
+}
+inline void cross3(const double* v1, const double* v2, double* rv) {
+  rv[0] = v1[1] * v2[2] - v2[1] * v1[2];
+  rv[1] = v1[2] * v2[0] - v2[2] * v1[0];
+  rv[2] = v1[0] * v2[1] - v2[0] * v1[1];
+}
+inline double mag3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+inline double normalize3(const double* v, double* rv) {
+  double m = mag3(v);
+  rv[0] = v[0] / m; rv[1] = v[1] / m; rv[2] = v[2] / m;
+  return m;
+}
+inline void mid2(const double* p1, const double* p2, double* r) {
+  r[0] = (p1[0] + p2[0]); r[1] = (p1[1] + p2[1]); r[2] = (p1[2] + p2[2]);
+  r[0] *= 0.5; r[1] *= 0.5; r[2] *= 0.5;
+}
+inline void cen3(const double* p1, const double* p2, const double* p3, double* r) {
+  double frac = 1.0 / 3.0;
+  r[0] = (p1[0] + p2[0] + p3[0]); r[1] = (p1[1] + p2[1] + p3[1]); r[2] = (p1[2] + p2[2] + p3[2]);
+  r[0] *= frac; r[1] *= frac; r[2] *= frac;
+}
+inline void cen4(const double* p1, const double* p2, const double* p3, const double* p4, double* r) {
+  r[0] = (p1[0] + p2[0] + p3[0] + p4[0]);
+  r[1] = (p1[1] + p2[1] + p3[1] + p4[1]);
+  r[2] = (p1[2] + p2[2] + p3[2] + p4[2]);
+  r[0] *= 0.25; r[1] *= 0.25; r[2] *= 0.25;
+}
+inline void tri_area(const double* p1, const double* p2, const double* p3, double* r) {
+  double v1[3], v2[3];
+  sub3(p2, p1, v1); sub3(p3, p1, v2);
+  cross3(v1, v2, r);
+  r[0] = 0.5 * r[0]; r[1] = 0.5 * r[1]; r[2] = 0.5 * r[2];
+}
+inline double tet_vol(const double* p1, const double* p2, const double* p3, const double* p4) {
+  double v1[3], v2[3], v3[3], t[3];
+  sub3(p2, p1, v1); sub3(p3, p1, v2); sub3(p4, p1, v3);
+  cross3(v1, v2, t);
+  return (v3[0] * t[0] + v3[1] * t[1] + v3[2] * t[2]) / 6.0;
+}
+
+// ---- deterministic, platform-independent random numbers --------------------
+struct SplitMix64 {
+  uint64_t s;
+  explicit SplitMix64(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  // uniform in [-1, 1)
+  double sym() { return ((double)(next() >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0; }
+};
+
+// Reference element-local neighbour tables (ucs/mesh.tcc:541-548) for TRI/TET.
+const int kClTri[6] = {1, 2, 2, 0, 0, 1};
+const int kClTet[12] = {1, 2, 3, 2, 0, 3, 0, 1, 3, 0, 1, 2};
+// Tet edge orientation, edge->face and face->node tables (ucs/mesh.tcc:1696-1790)
+const int kTetEorder[12] = {0, 1, 0, 2, 0, 3, 1, 2, 1, 3, 2, 3};
+const int kTetE2f[12] = {0, 1, 2, 0, 1, 2, 0, 3, 3, 1, 2, 3};
+const int kTetFl[12] = {0, 1, 2, 0, 3, 1, 0, 2, 3, 1, 3, 2};
+
+int elem_nnodes(int t) { return t == ETRI ? 3 : 4; }
+
+// Mesh::EliminateRepeats (ucs/mesh.tcc:1341): keeps first occurrences in order.
+int eliminate_repeats(int* a, int n) {
+  if (n <= 0) return 0;
+  std::vector<char> flag(n, 1);
+  for (int i = 0; i < n; i++)
+    if (flag[i])
+      for (int j = i + 1; j < n; j++)
+        if (a[i] == a[j]) flag[j] = 0;
+  int unique = 1;
+  for (int i = 1; i < n; i++)
+    if (flag[i]) a[unique++] = a[i];
+  return unique;
+}
+
+int build_maps(HostMesh& m) {
+  const int nn = m.nnode;
+  const int ne = (int)m.etype.size();
+  // BuildElsp
+  m.ielsp.assign(nn + 1, 0);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < elem_nnodes(m.etype[e]); j++) {
+      int node = m.enodes[4 * e + j];
+      if (node < 0 || node >= nn) { m.err = "element node id out of range"; return -1; }
+      m.ielsp[node + 1]++;
+    }
+  for (int i = 1; i <= nn; i++) m.ielsp[i] += m.ielsp[i - 1];
+  m.elsp.assign(m.ielsp[nn], 0);
+  {
+    std::vector<int> fill(m.ielsp.begin(), m.ielsp.end() - 1);
+    for (int e = 0; e < ne; e++)
+      for (int j = 0; j < elem_nnodes(m.etype[e]); j++) {
+        int node = m.enodes[4 * e + j];
+        m.elsp[fill[node]++] = e;
+      }
+  }
+  // BuildPsp
+  m.ipsp.assign(nn + 1, 0);
+  m.psp.clear();
+  m.psp.reserve((size_t)nn * 16);
+  std::vector<int> tmp;
+  for (int i = 0; i < nn; i++) {
+    tmp.clear();
+    for (int k = m.ielsp[i]; k < m.ielsp[i + 1]; k++) {
+      int e = m.elsp[k];
+      const int* nodes = &m.enodes[4 * e];
+      int nl = elem_nnodes(m.etype[e]);
+      int lnode = -1;
+      for (int q = 0; q < nl; q++)
+        if (nodes[q] == i) { lnode = q; break; }
+      if (m.etype[e] == ETRI) {
+        for (int q = 0; q < 2; q++) tmp.push_back(nodes[kClTri[2 * lnode + q]]);
+      } else {
+        for (int q = 0; q < 3; q++) tmp.push_back(nodes[kClTet[3 * lnode + q]]);
+      }
+    }
+    int u = eliminate_repeats(tmp.data(), (int)tmp.size());
+    m.psp.insert(m.psp.end(), tmp.begin(), tmp.begin() + u);
+    m.ipsp[i + 1] = (int)m.psp.size();
+  }
+  // FixBoundaryWindings: every boundary triangle must face away from its tet.
+  // The generator winds them outward already; this counts any that are not
+  // and rewinds them the way the reference does (nodes 2,1,0).
+  {
+    m.rewound = 0;
+    for (int e = 0; e < ne; e++) {
+      if (m.etype[e] != ETRI) continue;
+      int* tn = &m.enodes[4 * e];
+      // find the unique tet holding all three nodes
+      int owner = -1;
+      for (int k = m.ielsp[tn[0]]; k < m.ielsp[tn[0] + 1]; k++) {
+        int t = m.elsp[k];
+        if (m.etype[t] != ETET) continue;
+        const int* q = &m.enodes[4 * t];
+        int hits = 0;
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 4; b++) hits += (tn[a] == q[b]);
+        if (hits == 3) { owner = t; break; }
+      }
+      if (owner < 0) { m.err = "boundary face without a volume element"; return -1; }
+      double bpt[3], ept[3], ne3[3], nb[3];
+      cen3(&m.xyz[3 * tn[0]], &m.xyz[3 * tn[1]], &m.xyz[3 * tn[2]], bpt);
+      const int* q = &m.enodes[4 * owner];
+      cen4(&m.xyz[3 * q[0]], &m.xyz[3 * q[1]], &m.xyz[3 * q[2]], &m.xyz[3 * q[3]], ept);
+      sub3(bpt, ept, ne3);
+      tri_area(&m.xyz[3 * tn[0]], &m.xyz[3 * tn[1]], &m.xyz[3 * tn[2]], nb);
+      normalize3(ne3, ne3);
+      normalize3(nb, nb);
+      double dot = ne3[0] * nb[0] + ne3[1] * nb[1] + ne3[2] * nb[2];
+      if (!(dot > 0.0)) {
+        std::swap(tn[0], tn[2]);
+        m.rewound++;
+      }
+    }
+  }
+  // BuildEdges: interior edges (i < psp[j]) in node-then-psp order
+  m.edges.clear();
+  for (int i = 0; i < nn; i++)
+    for (int j = m.ipsp[i]; j < m.ipsp[i + 1]; j++)
+      if (m.psp[j] > i) { m.edges.push_back(i); m.edges.push_back(m.psp[j]); }
+  m.nedge = (int)m.edges.size() / 2;
+  // boundary half-edges: one per (boundary face, face node), phantom ids from nnode
+  m.bedges.clear(); m.belem.clear(); m.bfactag.clear();
+  int jj = nn;
+  for (int e = 0; e < ne; e++) {
+    if (m.etype[e] != ETRI) continue;
+    for (int j = 0; j < 3; j++) {
+      m.bedges.push_back(m.enodes[4 * e + j]);
+      m.bedges.push_back(jj++);
+      m.belem.push_back(e);
+      m.bfactag.push_back(m.efactag[e]);
+    }
+  }
+  m.nbedge = (int)m.belem.size();
+  m.maps_built = 1;
+  return 0;
+}
+
+int calc_metrics(HostMesh& m) {
+  const int nn = m.nnode;
+  m.vol.assign(nn, 0.0);
+  // every tet must be right-handed (positive volume in the reference's
+  // CalcTetVol convention) for the dual areas to point from n[0] to n[1]
+  m.inverted = 0;
+  for (size_t e = 0; e < m.etype.size(); e++) {
+    if (m.etype[e] != ETET) continue;
+    const int* q = &m.enodes[4 * e];
+    if (!(tet_vol(&m.xyz[3 * (size_t)q[0]], &m.xyz[3 * (size_t)q[1]], &m.xyz[3 * (size_t)q[2]],
+                  &m.xyz[3 * (size_t)q[3]]) > 0.0))
+      m.inverted++;
+  }
+  if (m.inverted) {
+    m.err = "mesh has " + std::to_string(m.inverted) + " inverted or degenerate tetrahedra";
+    return -1;
+  }
+  m.ea.assign((size_t)4 * m.nedge, 0.0);
+  m.ba.assign((size_t)4 * m.nbedge, 0.0);
+  const double* X = m.xyz.data();
+  // interior edges: two dual-face triangles and four sub-volumes per
+  // surrounding element (CalcAreasVolumes, ucs/mesh.tcc:1822-1985)
+  for (int i = 0; i < m.nedge; i++) {
+    int n1 = m.edges[2 * i], n2 = m.edges[2 * i + 1];
+    for (int k = m.ielsp[n2]; k < m.ielsp[n2 + 1]; k++) {
+      int e = m.elsp[k];
+      if (m.etype[e] != ETET) continue;
+      const int* nodes = &m.enodes[4 * e];
+      int l1 = -1, l2 = -1;
+      for (int q = 0; q < 4; q++) {
+        if (nodes[q] == n1) l1 = q;
+        else if (nodes[q] == n2) l2 = q;
+      }
+      if (l1 < 0 || l2 < 0) continue;  // edge not in this element
+      int orientation = 0, eid = -1;
+      for (int j = 0; j < 6; j++) {
+        if (kTetEorder[2 * j] == l1 && kTetEorder[2 * j + 1] == l2) { eid = j; orientation = 1; break; }
+        if (kTetEorder[2 * j + 1] == l1 && kTetEorder[2 * j] == l2) { eid = j; orientation = -1; break; }
+      }
+      int face1 = kTetE2f[2 * eid], face2 = kTetE2f[2 * eid + 1];
+      double edgept[3], f1[3], f2[3], ept[3], area[3];
+      mid2(&X[3 * n1], &X[3 * n2], edgept);
+      const int* fa = &kTetFl[3 * face1];
+      cen3(&X[3 * nodes[fa[0]]], &X[3 * nodes[fa[1]]], &X[3 * nodes[fa[2]]], f1);
+      const int* fb = &kTetFl[3 * face2];
+      cen3(&X[3 * nodes[fb[0]]], &X[3 * nodes[fb[1]]], &X[3 * nodes[fb[2]]], f2);
+      cen4(&X[3 * nodes[0]], &X[3 * nodes[1]], &X[3 * nodes[2]], &X[3 * nodes[3]], ept);
+      double o = (double)orientation;
+      double* a = &m.ea[4 * i];
+      tri_area(ept, f2, edgept, area);
+      area[0] = o * area[0]; area[1] = o * area[1]; area[2] = o * area[2];
+      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+      tri_area(edgept, f1, ept, area);
+      area[0] = o * area[0]; area[1] = o * area[1]; area[2] = o * area[2];
+      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+      double tv0 = o * tet_vol(&X[3 * n1], ept, f2, edgept);
+      double tv1 = o * tet_vol(&X[3 * n1], f1, ept, edgept);
+      double tv2 = o * tet_vol(&X[3 * n2], ept, f1, edgept);
+      double tv3 = o * tet_vol(&X[3 * n2], f2, ept, edgept);
+      m.vol[n1] += tv0; m.vol[n1] += tv1;
+      m.vol[n2] += tv2; m.vol[n2] += tv3;
+    }
+  }
+  // boundary half-edges: two triangles of the boundary face's median dual
+  // (ucs/mesh.tcc:2148-2190)
+  for (int i = 0; i < m.nbedge; i++) {
+    int n1 = m.bedges[2 * i];
+    int e = m.belem[i];
+    const int* nodes = &m.enodes[4 * e];
+    int nid = -1;
+    for (int q = 0; q < 3; q++)
+      if (nodes[q] == n1) nid = q;
+    double ept[3], edgept[3], area[3];
+    cen3(&X[3 * nodes[0]], &X[3 * nodes[1]], &X[3 * nodes[2]], ept);
+    int alt = nodes[kClTri[2 * nid]];
+    mid2(&X[3 * n1], &X[3 * alt], edgept);
+    tri_area(ept, &X[3 * n1], edgept, area);
+    double* a = &m.ba[4 * i];
+    a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+    alt = nodes[kClTri[2 * nid + 1]];
+    mid2(&X[3 * n1], &X[3 * alt], edgept);
+    tri_area(edgept, &X[3 * n1], ept, area);
+    a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+  }
+  // CheckForClosure (ucs/mesh.tcc:2274): sum of signed face areas per node
+  {
+    std::vector<double> s((size_t)3 * nn, 0.0);
+    for (int i = 0; i < m.nedge; i++) {
+      int n1 = m.edges[2 * i], n2 = m.edges[2 * i + 1];
+      for (int c = 0; c < 3; c++) {
+        s[3 * n1 + c] = s[3 * n1 + c] - m.ea[4 * i + c];
+        s[3 * n2 + c] = s[3 * n2 + c] + m.ea[4 * i + c];
+      }
+    }
+    for (int i = 0; i < m.nbedge; i++) {
+      int n1 = m.bedges[2 * i];
+      for (int c = 0; c < 3; c++) s[3 * n1 + c] = s[3 * n1 + c] - m.ba[4 * i + c];
+    }
+    m.unclosed = 0;
+    m.max_open = 0.0;
+    for (int i = 0; i < nn; i++) {
+      double mg = mag3(&s[3 * i]);
+      if (mg > m.max_open) m.max_open = mg;
+      if (mg > 1.0e-10) m.unclosed++;
+    }
+  }
+  for (int i = 0; i < m.nedge; i++) m.ea[4 * i + 3] = normalize3(&m.ea[4 * i], &m.ea[4 * i]);
+  for (int i = 0; i < m.nbedge; i++) m.ba[4 * i + 3] = normalize3(&m.ba[4 * i], &m.ba[4 * i]);
+  // Weighted LSQ normal matrices (Kernel_LSQ_CoefficientsWeighted,
+  // ucs/gradient.tcc:461); the boundary variant only adds for ghost nodes,
+  // which a single partition does not have.
+  m.sw.assign((size_t)6 * nn, 0.0);
+  for (int i = 0; i < m.nedge; i++) {
+    int l = m.edges[2 * i], r = m.edges[2 * i + 1];
+    double dx[3];
+    sub3(&X[3 * l], &X[3 * r], dx);
+    double ds2 = 1.0 / (dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    double tl[6], tr[6];
+    tl[0] = dx[0] * dx[0] * ds2;
+    tl[1] = dx[0] * dx[1] * ds2;
+    tl[2] = dx[0] * dx[2] * ds2;
+    tl[3] = dx[1] * dx[1] * ds2;
+    tl[4] = dx[1] * dx[2] * ds2;
+    tl[5] = dx[2] * dx[2] * ds2;
+    dx[0] = -dx[0]; dx[1] = -dx[1]; dx[2] = -dx[2];
+    tr[0] = tl[0];
+    tr[1] = (dx[0] * dx[1]) * ds2;
+    tr[2] = (dx[0] * dx[2]) * ds2;
+    tr[3] = tl[3];
+    tr[4] = (dx[1] * dx[2]) * ds2;
+    tr[5] = tl[5];
+    // DriverScatter adds the right side first, then the left
+    for (int c = 0; c < 6; c++) m.sw[6 * r + c] += tr[c];
+    for (int c = 0; c < 6; c++) m.sw[6 * l + c] += tl[c];
+  }
+  m.metrics_built = 1;
+  return 0;
+}
+
+// Reverse Cuthill-McKee renumbering of the nodes following
+// Mesh::ReorderMeshCuthillMcKee (ucs/mesh.tcc:2412-2490): breadth-first from
+// the lowest-degree unvisited node, neighbours queued by ascending degree,
+// then the order reversed.  Ties between equal degrees keep psp order
+// (std::stable_sort); the reference's std::sort is unstable, so equal-degree
+// ties are the one place this ordering is not pinned to the reference.
+int rcm_order(const HostMesh& m, std::vector<int>& order) {
+  const int nn = m.nnode;
+  std::vector<int> deg(nn);
+  for (int i = 0; i < nn; i++) deg[i] = m.ipsp[i + 1] - m.ipsp[i];
+  std::vector<char> seen(nn, 0);
+  order.clear();
+  order.reserve(nn);
+  std::vector<int> nb;
+  int start_scan = 0;
+  while ((int)order.size() < nn) {
+    int root = -1, best = 1 << 30;
+    for (int i = start_scan; i < nn; i++)
+      if (!seen[i] && deg[i] < best) { best = deg[i]; root = i; }
+    seen[root] = 1;
+    size_t head = order.size();
+    order.push_back(root);
+    while (head < order.size()) {
+      int v = order[head++];
+      nb.clear();
+      for (int j = m.ipsp[v]; j < m.ipsp[v + 1]; j++)
+        if (!seen[m.psp[j]]) nb.push_back(m.psp[j]);
+      std::stable_sort(nb.begin(), nb.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+      for (int w : nb)
+        if (!seen[w]) { seen[w] = 1; order.push_back(w); }
+    }
+    while (start_scan < nn && seen[start_scan]) start_scan++;
+  }
+  std::reverse(order.begin(), order.end());
+  return 0;
+}
+
+thread_local std::string g_last_mesh_error;
+
+}  // namespace
+
+extern "C" {
+
+PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p) {
+  if (!p || p->nx < 2 || p->ny < 2 || p->nz < 2) {
+    g_last_mesh_error = "pcfd_mesh_box_create: need nx, ny, nz >= 2";
+    return nullptr;
+  }
+  const long long nnode_ll = (long long)p->nx * p->ny * p->nz;
+  if (nnode_ll > 400000000LL) {
+    g_last_mesh_error = "pcfd_mesh_box_create: box too large";
+    return nullptr;
+  }
+  HostMesh* m = new (std::nothrow) HostMesh();
+  if (!m) return nullptr;
+  const int nx = p->nx, ny = p->ny, nz = p->nz;
+  m->nnode = (int)nnode_ll;
+  auto id = [&](int i, int j, int k) { return i + nx * (j + ny * k); };
+  // 1-D node coordinates per axis; y may be geometrically clustered toward y=0
+  std::vector<double> cx(nx), cy(ny), cz(nz);
+  for (int i = 0; i < nx; i++) cx[i] = p->lx * (double)i / (double)(nx - 1);
+  for (int k = 0; k < nz; k++) cz[k] = p->lz * (double)k / (double)(nz - 1);
+  if (p->y_ratio > 1.0) {
+    double h0 = (p->y_ratio - 1.0) / (std::pow(p->y_ratio, (double)(ny - 1)) - 1.0);
+    double y = 0.0, h = h0;
+    for (int j = 0; j < ny; j++) {
+      cy[j] = p->ly * y;
+      y += h;
+      h *= p->y_ratio;
+    }
+    cy[ny - 1] = p->ly;
+  } else {
+    for (int j = 0; j < ny; j++) cy[j] = p->ly * (double)j / (double)(ny - 1);
+  }
+  auto local_h = [](const std::vector<double>& c, int i) {
+    int n = (int)c.size();
+    double hl = i > 0 ? c[i] - c[i - 1] : 1e300;
+    double hr = i < n - 1 ? c[i + 1] - c[i] : 1e300;
+    return std::min(hl, hr);
+  };
+  m->xyz.resize((size_t)3 * m->nnode);
+  SplitMix64 rng(p->seed);
+  const double tanr = std::tan(p->ramp_deg * 3.14159265358979323846 / 180.0);
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        double x = cx[i], y = cy[j], z = cz[k];
+        bool interior = i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1;
+        if (interior && p->jitter > 0.0) {
+          x += p->jitter * local_h(cx, i) * rng.sym();
+          y += p->jitter * local_h(cy, j) * rng.sym();
+          z += p->jitter * local_h(cz, k) * rng.sym();
+        }
+        if (p->ramp_deg != 0.0 && x > p->ramp_x0) {
+          // shear y so the bottom wall ramps up by ramp_deg and the top stays flat
+          y = y + tanr * (x - p->ramp_x0) * (p->ly - y) / p->ly;
+        }
+        size_t n = (size_t)id(i, j, k);
+        m->xyz[3 * n + 0] = x;
+        m->xyz[3 * n + 1] = y;
+        m->xyz[3 * n + 2] = z;
+      }
+  // boundary triangles: two per boundary quad, split along the diagonal the
+  // Kuhn tets use (the one through the hex corner (0,0,0) or (1,1,1)),
+  // wound so the normal points out of the box.
+  auto push_tri = [&](int a, int b, int c, int tag, const double* out) {
+    double n[3];
+    tri_area(&m->xyz[3 * (size_t)a], &m->xyz[3 * (size_t)b], &m->xyz[3 * (size_t)c], n);
+    if (n[0] * out[0] + n[1] * out[1] + n[2] * out[2] < 0.0) std::swap(a, c);
+    m->etype.push_back(ETRI);
+    m->enodes.push_back(a); m->enodes.push_back(b); m->enodes.push_back(c); m->enodes.push_back(-1);
+    m->efactag.push_back(tag);
+  };
+  // face order: x=0, x=max, y=0, y=max, z=0, z=max
+  for (int f = 0; f < 6; f++) {
+    int axis = f / 2, side = f % 2;
+    double out[3] = {0, 0, 0};
+    out[axis] = side ? 1.0 : -1.0;
+    int tag = p->tags[f];
+    int na = axis == 0 ? ny : nx;  // first in-face axis extent
+    int nb = axis == 2 ? ny : nz;  // second in-face axis extent
+    for (int b = 0; b < nb - 1; b++)
+      for (int a = 0; a < na - 1; a++) {
+        int c[2][2][2];
+        int ci, cj, ck;
+        if (axis == 0) { ci = side ? nx - 2 : 0; cj = a; ck = b; }
+        else if (axis == 1) { ci = a; cj = side ? ny - 2 : 0; ck = b; }
+        else { ci = a; cj = b; ck = side ? nz - 2 : 0; }
+        for (int u = 0; u < 2; u++)
+          for (int v = 0; v < 2; v++)
+            for (int w = 0; w < 2; w++) c[u][v][w] = id(ci + u, cj + v, ck + w);
+        // the four face corners in cyclic order and the diagonal endpoints
+        int q0, q1, q2, q3;  // q0 and q2 are the diagonal
+        if (axis == 0) {
+          int s = side;
+          // face corners (s, v, w)
+          if (!s) { q0 = c[0][0][0]; q1 = c[0][1][0]; q2 = c[0][1][1]; q3 = c[0][0][1]; }
+          else { q0 = c[1][0][0]; q1 = c[1][1][0]; q2 = c[1][1][1]; q3 = c[1][0][1]; }
+        } else if (axis == 1) {
+          int s = side;
+          if (!s) { q0 = c[0][0][0]; q1 = c[1][0][0]; q2 = c[1][0][1]; q3 = c[0][0][1]; }
+          else { q0 = c[0][1][0]; q1 = c[1][1][0]; q2 = c[1][1][1]; q3 = c[0][1][1]; }
+        } else {
+          int s = side;
+          if (!s) { q0 = c[0][0][0]; q1 = c[1][0][0]; q2 = c[1][1][0]; q3 = c[0][1][0]; }
+          else { q0 = c[0][0][1]; q1 = c[1][0][1]; q2 = c[1][1][1]; q3 = c[0][1][1]; }
+        }
+        push_tri(q0, q1, q2, tag, out);
+        push_tri(q0, q2, q3, tag, out);
+      }
+  }
+  // Kuhn tets: for each permutation (s0,s1,s2) of the axes, the path
+  // c000 -> +e_s0 -> +e_s1 -> c111; odd permutations are flipped so every tet
+  // is right-handed (positive reference volume).
+  const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  const int parity[6] = {0, 1, 1, 0, 0, 1};
+  for (int k = 0; k < nz - 1; k++)
+    for (int j = 0; j < ny - 1; j++)
+      for (int i = 0; i < nx - 1; i++)
+        for (int t = 0; t < 6; t++) {
+          int off[3] = {0, 0, 0};
+          int v[4];
+          v[0] = id(i, j, k);
+          off[perms[t][0]] = 1;
+          v[1] = id(i + off[0], j + off[1], k + off[2]);
+          off[perms[t][1]] = 1;
+          v[2] = id(i + off[0], j + off[1], k + off[2]);
+          v[3] = id(i + 1, j + 1, k + 1);
+          if (parity[t]) std::swap(v[1], v[2]);
+          m->etype.push_back(ETET);
+          for (int q = 0; q < 4; q++) m->enodes.push_back(v[q]);
+          m->efactag.push_back(0);
+        }
+  return (pcfd_mesh_t)m;
+}
+
+PCFD_API pcfd_mesh_t pcfd_mesh_from_elements(int nnode, const double* xyz, int ntri, const int* tri,
+                                             const int* tri_tag, int ntet, const int* tet) {
+  if (nnode <= 0 || !xyz || ntri < 0 || ntet <= 0 || !tet || (ntri > 0 && (!tri || !tri_tag))) {
+    g_last_mesh_error = "pcfd_mesh_from_elements: bad arguments";
+    return nullptr;
+  }
+  HostMesh* m = new (std::nothrow) HostMesh();
+  if (!m) return nullptr;
+  m->nnode = nnode;
+  m->xyz.assign(xyz, xyz + (size_t)3 * nnode);
+  for (int e = 0; e < ntri; e++) {
+    m->etype.push_back(ETRI);
+    for (int q = 0; q < 3; q++) m->enodes.push_back(tri[3 * e + q]);
+    m->enodes.push_back(-1);
+    m->efactag.push_back(tri_tag[e]);
+  }
+  for (int e = 0; e < ntet; e++) {
+    m->etype.push_back(ETET);
+    for (int q = 0; q < 4; q++) m->enodes.push_back(tet[4 * e + q]);
+    m->efactag.push_back(0);
+  }
+  return (pcfd_mesh_t)m;
+}
+
+PCFD_API int pcfd_mesh_build(pcfd_mesh_t h) {
+  if (!h) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  if (build_maps(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  if (calc_metrics(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_mesh_view_get(pcfd_mesh_t h, pcfd_mesh_view* v) {
+  if (!h || !v) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  if (!m->maps_built || !m->metrics_built) return PCFD_ERR_STATE;
+  std::memset(v, 0, sizeof(*v));
+  v->nnode = m->nnode;
+  v->nbnode = m->nbedge;
+  v->nedge = m->nedge;
+  v->nbedge = m->nbedge;
+  v->edges = m->edges.data();
+  v->edge_area = m->ea.data();
+  v->bedges = m->bedges.data();
+  v->bedge_area = m->ba.data();
+  v->bfactag = m->bfactag.data();
+  v->xyz = m->xyz.data();
+  v->vol = m->vol.data();
+  v->sw = m->sw.data();
+  v->ipsp = m->ipsp.data();
+  v->psp = m->psp.data();
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_mesh_stats(pcfd_mesh_t h, int* nelem_tri, int* nelem_tet, int* rewound, int* unclosed,
+                             double* max_open, double* total_vol) {
+  if (!h) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  int nt = 0, nk = 0;
+  for (int t : m->etype) (t == ETRI ? nt : nk)++;
+  if (nelem_tri) *nelem_tri = nt;
+  if (nelem_tet) *nelem_tet = nk;
+  if (rewound) *rewound = m->rewound;
+  if (unclosed) *unclosed = m->unclosed;
+  if (max_open) *max_open = m->max_open;
+  if (total_vol) {
+    double s = 0.0;
+    for (double x : m->vol) s += x;
+    *total_vol = s;
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_mesh_rcm_order(pcfd_mesh_t h, int* order_out) {
+  if (!h || !order_out) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  if (!m->maps_built) return PCFD_ERR_STATE;
+  std::vector<int> order;
+  rcm_order(*m, order);
+  std::memcpy(order_out, order.data(), sizeof(int) * order.size());
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_mesh_renumber(pcfd_mesh_t h, const int* order) {
+  // order[new] = old; renumbers nodes and element connectivity, then the
+  // maps and metrics must be rebuilt with pcfd_mesh_build.
+  if (!h || !order) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  const int nn = m->nnode;
+  std::vector<int> old2new(nn, -1);
+  for (int i = 0; i < nn; i++) {
+    int o = order[i];
+    if (o < 0 || o >= nn || old2new[o] >= 0) return PCFD_ERR_ARG;
+    old2new[o] = i;
+  }
+  std::vector<double> x2((size_t)3 * nn);
+  for (int i = 0; i < nn; i++)
+    for (int c = 0; c < 3; c++) x2[3 * (size_t)i + c] = m->xyz[3 * (size_t)order[i] + c];
+  m->xyz.swap(x2);
+  for (size_t e = 0; e < m->etype.size(); e++)
+    for (int q = 0; q < elem_nnodes(m->etype[e]); q++) m->enodes[4 * e + q] = old2new[m->enodes[4 * e + q]];
+  m->maps_built = m->metrics_built = 0;
+  return PCFD_OK;
+}
+
+PCFD_API void pcfd_mesh_destroy(pcfd_mesh_t h) { delete (HostMesh*)h; }
+
+PCFD_API const char* pcfd_mesh_last_error(void) { return g_last_mesh_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,1271 @@
+// Device solver for the edge-based implicit finite-volume path on sm_103a:
+// C ABI (include/pcfd.h), device-resident mesh and fields, and the kernels
+// for boundary conditions, LSQ gradient, limiter and residual.
+//
+// Design (GB300-first, one GPU):
+//  * Every field lives in HBM for the life of the handle; host copies happen
+//    only in set/get calls.
+//  * The edge loops of the reference (Driver/Bdriver, ucs/driver.tcc:6,70)
+//    become (a) one edge kernel that evaluates each edge's flux once and
+//    stores it, and (b) a node kernel that gathers, for every node, its
+//    incident edge fluxes in ascending edge order - the order in which the
+//    reference's sequential scatter adds them - so the sum is deterministic
+//    and free of atomics.
+//  * Node-centred passes (gradient, limiter) gather over a node->edge CSR in
+//    the same ascending edge order; the static per-edge-end LSQ weights and
+//    edge half-vectors are computed once at set-up, because the mesh does
+//    not move.
+//  * FP64 throughout the residual path.
+#include "../../include/pcfd.h"
+#include "flux_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace pcfd;
+
+// 32-byte aligned edge area record (unit normal + magnitude), one 256-bit load
+struct __align__(32) D4 {
+  double x, y, z, w;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return set_err(PCFD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+enum HealthSlot { H_KNEECAP = 0, H_LIMCLIP = 1, H_RHOCLIP = 2, H_ECLIP = 3, H_PCLIP = 4, H_NANDQ = 5, H_BADBC = 6 };
+
+// Kernel timers, one per launch site (TimerList analogue)
+enum TimerId { T_BC = 0, T_GRAD, T_LIMITER, T_EDGEFLUX, T_BEDGEFLUX, T_GATHER, T_NORM, T_SETUP, T_COUNT };
+const char* kTimerNames[T_COUNT] = {"bc_update", "lsq_gradient", "venkat_limiter", "edge_flux",
+                                    "bedge_flux", "residual_gather", "norm_reduce", "setup"};
+
+struct Solver {
+  // sizes
+  int nnode = 0, nbnode = 0, nedge = 0, nbedge = 0, ntot = 0;
+  int nbgroup = 0;  // boundary nodes
+  pcfd_params prm{};
+  std::vector<int> bc_type;
+  std::vector<double> bc_twall;
+  double qinf[NVARS];
+  int bc_sequential = 0;  // 1: a no-slip normal node is itself hard-set; run BCs in order
+
+  cudaStream_t stream = nullptr;
+  // mesh
+  int2* d_en = nullptr;         // [nedge] edge nodes
+  D4* d_ea = nullptr;      // [nedge] unit normal + area
+  double* d_eh = nullptr;       // [nedge][3] 0.5 (xR - xL)
+  int2* d_bn = nullptr;         // [nbedge]
+  D4* d_ba = nullptr;      // [nbedge]
+  int* d_bbc = nullptr;         // [nbedge] bc type
+  double* d_btw = nullptr;      // [nbedge] non-dimensional wall temperature
+  int* d_bnrm = nullptr;        // [nbedge] no-slip normal node (or -1)
+  double* d_xyz = nullptr;      // [nnode][3]
+  double* d_vol = nullptr;      // [nnode]
+  int* d_nptr = nullptr;        // [nnode+1] node -> incident edges
+  int* d_nedg = nullptr;        // [2 nedge] signed edge id (~e when the node is the left node)
+  int* d_nnbr = nullptr;        // [2 nedge] neighbour node of that entry
+  double* d_lsq = nullptr;      // [2 nedge][3] LSQ weights per edge end
+  int* d_bptr = nullptr;        // [nnode+1] node -> boundary half-edges (bedge order)
+  int* d_bhe = nullptr;         // [nbedge]
+  int* d_bgnode = nullptr;      // [nbgroup] boundary nodes
+  int* d_bgptr = nullptr;       // [nbgroup+1] -> d_bghe
+  int* d_bghe = nullptr;        // [nbedge]
+  // fields
+  double* d_q = nullptr;        // [ntot][10]
+  double* d_grad = nullptr;     // [nnode][27]
+  double* d_lim = nullptr;      // [nnode][5]
+  double* d_b = nullptr;        // [nnode][5]
+  double* d_ef = nullptr;       // [nedge][5] edge flux scratch
+  double* d_bf = nullptr;       // [nbedge][5] half-edge flux scratch
+  double* d_part = nullptr;     // [kNormBlocks][6] norm partial sums (scratch)
+  double* d_norms = nullptr;    // [6]
+  unsigned long long* d_health = nullptr;  // [8]
+  int have_grad = 0, have_lim = 0;
+
+  // profiling
+  int profile = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double t_ms[T_COUNT] = {0};
+  long long t_n[T_COUNT] = {0};
+  long long launches = 0;
+};
+
+constexpr int kNormBlocks = 304;  // 2 x 152 SMs
+constexpr int kNormThreads = 256;
+
+template <class F>
+int launch(Solver* s, int timer, F&& f) {
+  if (s->profile) cudaEventRecord(s->ev0, s->stream);
+  f();
+  s->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  if (s->profile) {
+    cudaEventRecord(s->ev1, s->stream);
+    cudaEventSynchronize(s->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->t_ms[timer] += ms;
+    s->t_n[timer]++;
+  }
+  return PCFD_OK;
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// -------------------------------------------------------------------------
+// set-up kernels
+// -------------------------------------------------------------------------
+
+// ComputeLSQCoefficients (ucs/gradient.tcc:141) for every (node, edge) entry
+// of the node->edge CSR, with the inverse-distance weighting of
+// Kernel_LSQ_Gradient (:251): grad_i += -we(s_i, w (x_i - x_j)) w (q_j - q_i).
+// The stored triple is -we * w.
+__global__ void k_lsq_weights(int nnode, const int* __restrict__ nptr, const int* __restrict__ nnbr,
+                              const double* __restrict__ xyz, const double* __restrict__ sw,
+                              double* __restrict__ lsq) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  const double* s = &sw[6 * i];
+  double s11 = s[0], s12 = s[1], s13 = s[2], s22 = s[3], s23 = s[4], s33 = s[5];
+  double r11 = s11, r12 = s12, r13 = s13;
+  double r12_r11 = (r11 == 0.0) ? 0.0 : r12 / r11;
+  double r22 = s22 - r12 * r12_r11;
+  double r23 = s23 - r12_r11 * r13;
+  double r13_r11 = (r11 == 0.0) ? 0.0 : r13 / r11;
+  double r23_r22 = (r22 == 0.0) ? 0.0 : r23 / r22;
+  double r33 = s33 - r13 * r13_r11 - r23 * r23_r22;
+  double xi0 = xyz[3 * i], xi1 = xyz[3 * i + 1], xi2 = xyz[3 * i + 2];
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    int j = nnbr[k];
+    double dx0 = xi0 - xyz[3 * j], dx1 = xi1 - xyz[3 * j + 1], dx2 = xi2 - xyz[3 * j + 2];
+    double d2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+    double weight = 1.0 / sqrt(d2);
+    dx0 *= weight; dx1 *= weight; dx2 *= weight;
+    double dykdx = (dx1 - r12_r11 * dx0);
+    double we2 = (r33 == 0.0) ? 0.0 : (dx2 - r13_r11 * dx0 - r23_r22 * dykdx) / r33;
+    double we1 = (r22 == 0.0) ? 0.0 : (dykdx - r23 * we2) / r22;
+    double we0 = (r11 == 0.0) ? 0.0 : (dx0 - r12 * we1 - r13 * we2) / r11;
+    lsq[3 * (size_t)k + 0] = -we0 * weight;
+    lsq[3 * (size_t)k + 1] = -we1 * weight;
+    lsq[3 * (size_t)k + 2] = -we2 * weight;
+  }
+}
+
+__global__ void k_edge_half(int nedge, const int2* __restrict__ en, const double* __restrict__ xyz,
+                            double* __restrict__ eh) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  int2 n = en[e];
+  for (int c = 0; c < 3; c++) eh[3 * (size_t)e + c] = 0.5 * (xyz[3 * n.y + c] - xyz[3 * n.x + c]);
+}
+
+__global__ void k_fill_state(int nrows, const double* __restrict__ qinf, double* __restrict__ q) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  for (int j = 0; j < NVARS; j++) q[(size_t)i * NVARS + j] = qinf[j];
+}
+
+// -------------------------------------------------------------------------
+// boundary conditions (UpdateBCs, ucs/bc.tcc:1400)
+// -------------------------------------------------------------------------
+
+struct BcConst {
+  double gamma;
+  int no_cvbc;
+  double qinf[NVARS];
+};
+
+// GetFarfieldBoundaryVariables (ucs/compressible.tcc:1246), static grid
+__device__ void bc_farfield(const BcConst& k, const double* QL, double* QR, const D4 a) {
+  const double gamma = k.gamma;
+  const double* Qinf = k.qinf;
+  for (int subit = 0; subit < 10; subit++) {
+    double t0 = (QL[0] + QR[0]) / 2.0, t1 = (QL[1] + QR[1]) / 2.0, t2 = (QL[2] + QR[2]) / 2.0,
+           t3 = (QL[3] + QR[3]) / 2.0, t4 = (QL[4] + QR[4]) / 2.0;
+    double it0 = 1.0 / t0;
+    double theta = t1 * it0 * a.x + t2 * it0 * a.y + t3 * it0 * a.z;
+    double rhoi = QL[0];
+    double iri = 1.0 / QL[0];
+    double ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
+    double pi = QL[6];
+    double rhoinf = Qinf[0];
+    double uinf = Qinf[1] / Qinf[0], vinf = Qinf[2] / Qinf[0], winf = Qinf[3] / Qinf[0];
+    double pinf = Qinf[6];
+    double tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
+    double pavg = (gamma - 1.0) * (t4 - t0 * (0.5 * (tu * tu + tv * tv + tw * tw)));
+    double rhoavg = t0;
+    double c2avg = gamma * (pavg / rhoavg);
+    double cavg = sqrt(c2avg);
+    double mach = fabs(theta / cavg);
+    if (theta == 0.0) {
+      return;
+    } else if (theta > 0.0 && mach >= 1.0) {
+      for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
+    } else if (theta < 0.0 && mach >= 1.0) {
+      for (int i = 0; i < NEQN; i++) QR[i] = Qinf[i];
+    } else if (theta > 0.0 && mach < 1.0) {
+      double pb = pinf;
+      double rhob = rhoi + (pb - pi) / c2avg;
+      double t = (pb - pi) / (rhoavg * cavg);
+      double ub = ui - a.x * t, vb = vi - a.y * t, wb = wi - a.z * t;
+      QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
+      QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
+    } else if (theta < 0.0 && mach < 1.0) {
+      double pb = 0.5 * (pinf + pi + rhoavg * cavg * (a.x * (uinf - ui) + a.y * (vinf - vi) + a.z * (winf - wi)));
+      double rhob = rhoinf + (pb - pinf) / c2avg;
+      double t = (pb - pinf) / (rhoavg * cavg);
+      double ub = uinf + a.x * t, vb = vinf + a.y * t, wb = winf + a.z * t;
+      QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
+      QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
+    } else {
+      return;
+    }
+  }
+}
+
+// GetInviscidWallBoundaryVariables (ucs/compressible.tcc:1375), static grid
+__device__ void bc_inviscid_wall(const BcConst& k, const double* QL, double* QR, const D4 a) {
+  const double gamma = k.gamma;
+  const double rhoi = QL[0];
+  const double iri = 1.0 / rhoi;
+  const double ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
+  const double pi = QL[6];
+  if (k.no_cvbc) {
+    double dot = QL[1] * a.x + QL[2] * a.y + QL[3] * a.z;
+    for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
+    QR[1] = QL[1] - 2.0 * dot * a.x;
+    QR[2] = QL[2] - 2.0 * dot * a.y;
+    QR[3] = QL[3] - 2.0 * dot * a.z;
+    return;
+  }
+  const double thetaL = ui * a.x + vi * a.y + wi * a.z;
+  for (int subit = 0; subit < 10; subit++) {
+    double t0 = (QL[0] + QR[0]) / 2.0, t1 = (QL[1] + QR[1]) / 2.0, t2 = (QL[2] + QR[2]) / 2.0,
+           t3 = (QL[3] + QR[3]) / 2.0, t4 = (QL[4] + QR[4]) / 2.0;
+    double it0 = 1.0 / t0;
+    double tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
+    double rhoavg = t0;
+    double pavg = (gamma - 1.0) * (t4 - t0 * (0.5 * (tu * tu + tv * tv + tw * tw)));
+    double c2avg = gamma * (pavg / rhoavg);
+    double cavg = sqrt(c2avg);
+    double pb = pi + rhoavg * cavg * thetaL;
+    double rhob = rhoi + (pb - pi) / c2avg;
+    double t = (pb - pi) / (rhoavg * cavg);
+    double ub = ui - a.x * t, vb = vi - a.y * t, wb = wi - a.z * t;
+    QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
+    QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
+  }
+}
+
+// One boundary half-edge of CalculateBoundaryVariables (ucs/bc.tcc:1059).
+// Returns 0 on an unknown BC type.
+__device__ int apply_bc(const BcConst& k, int bct, double* QL, double* QR, const D4 a, double Tw,
+                        const double* nQ) {
+  switch (bct) {
+    case PCFD_BC_SONIC_INFLOW:
+    case PCFD_BC_DIRICHLET:
+      for (int i = 0; i < NVARS; i++) QR[i] = QL[i] = k.qinf[i];
+      break;
+    case PCFD_BC_SONIC_OUTFLOW:
+    case PCFD_BC_NEUMANN:
+      for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
+      break;
+    case PCFD_BC_FARFIELD:
+      bc_farfield(k, QL, QR, a);
+      break;
+    case PCFD_BC_IMPERMEABLE_WALL:
+    case PCFD_BC_SYMMETRY:
+      bc_inviscid_wall(k, QL, QR, a);
+      break;
+    case PCFD_BC_NOSLIP:
+      // GetViscousWallBoundaryVariables (ucs/compressible.tcc:1545), static wall
+      if (Tw < 0.0) {
+        QR[0] = QL[0] = nQ[0];
+        QR[4] = QL[4] = nQ[4];
+      } else {
+        double gm1 = k.gamma - 1.0;
+        double rhoEt = (Tw * QL[0] / (k.gamma * gm1) + 0.5 * QR[0] * 0.0);
+        QR[0] = QL[0];
+        QR[4] = QL[4] = rhoEt;
+      }
+      QR[1] = QL[1] = QL[0] * 0.0;
+      QR[2] = QL[2] = QL[0] * 0.0;
+      QR[3] = QL[3] = QL[0] * 0.0;
+      break;
+    default:
+      return 0;
+  }
+  aux_vars(k.gamma, QR);
+  aux_vars(k.gamma, QL);
+  return 1;
+}
+
+// One thread per boundary node; its half-edges in bedge order.
+__global__ void k_bc_nodes(int ngroup, const int* __restrict__ gnode, const int* __restrict__ gptr,
+                           const int* __restrict__ ghe, const int2* __restrict__ bn, const D4* __restrict__ ba,
+                           const int* __restrict__ bbc, const double* __restrict__ btw, const int* __restrict__ bnrm,
+                           BcConst k, double* __restrict__ q, unsigned long long* health) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroup) return;
+  int node = gnode[g];
+  double QL[NVARS];
+  for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)node * NVARS + j];
+  for (int p = gptr[g]; p < gptr[g + 1]; p++) {
+    int he = ghe[p];
+    int ph = bn[he].y;
+    double QR[NVARS];
+    for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)ph * NVARS + j];
+    double nQ[NVARS] = {0};
+    int bct = bbc[he];
+    if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+      for (int j = 0; j < NVARS; j++) nQ[j] = q[(size_t)bnrm[he] * NVARS + j];
+    if (!apply_bc(k, bct, QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
+    for (int j = 0; j < NVARS; j++) q[(size_t)ph * NVARS + j] = QR[j];
+  }
+  for (int j = 0; j < NVARS; j++) q[(size_t)node * NVARS + j] = QL[j];
+}
+
+// Exact reference order when a no-slip normal node is itself hard-set by a
+// boundary condition: a single thread walks the half-edges in bedge order.
+__global__ void k_bc_sequential(int nbedge, const int2* __restrict__ bn, const D4* __restrict__ ba,
+                                const int* __restrict__ bbc, const double* __restrict__ btw,
+                                const int* __restrict__ bnrm, BcConst k, double* __restrict__ q,
+                                unsigned long long* health) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int he = 0; he < nbedge; he++) {
+    int2 n = bn[he];
+    double* QL = &q[(size_t)n.x * NVARS];
+    double* QR = &q[(size_t)n.y * NVARS];
+    double nQ[NVARS] = {0};
+    int bct = bbc[he];
+    if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+      for (int j = 0; j < NVARS; j++) nQ[j] = q[(size_t)bnrm[he] * NVARS + j];
+    if (!apply_bc(k, bct, QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
+  }
+}
+
+// -------------------------------------------------------------------------
+// weighted LSQ gradient (Gradient::Compute, ucs/gradient.tcc:57)
+// -------------------------------------------------------------------------
+
+__constant__ int c_gradlist[NTERMS] = {0, 1, 2, 3, 4, 5, 7, 8, 9};
+
+__global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restrict__ nptr,
+                                                  const int* __restrict__ nnbr, const double* __restrict__ lsq,
+                                                  const double* __restrict__ q, const int* __restrict__ bptr,
+                                                  const int* __restrict__ bhe, const int* __restrict__ bbc,
+                                                  const D4* __restrict__ ba, double* __restrict__ grad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double qi[NTERMS];
+  for (int t = 0; t < NTERMS; t++) qi[t] = q[(size_t)i * NVARS + c_gradlist[t]];
+  double g[NTERMS * 3];
+  for (int t = 0; t < NTERMS * 3; t++) g[t] = 0.0;
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    int j = nnbr[k];
+    double c0 = lsq[3 * (size_t)k], c1 = lsq[3 * (size_t)k + 1], c2 = lsq[3 * (size_t)k + 2];
+    const double* qj = &q[(size_t)j * NVARS];
+#pragma unroll
+    for (int t = 0; t < NTERMS; t++) {
+      double dq = qj[c_gradlist[t]] - qi[t];
+      g[3 * t + 0] += c0 * dq;
+      g[3 * t + 1] += c1 * dq;
+      g[3 * t + 2] += c2 * dq;
+    }
+  }
+  // Bkernel_Symmetry_Fix (ucs/gradient.tcc:545), in half-edge order
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    int he = bhe[p];
+    if (bbc[he] != PCFD_BC_SYMMETRY) continue;
+    D4 a = ba[he];
+#pragma unroll
+    for (int t = 0; t < NTERMS; t++) {
+      double dot = g[3 * t] * a.x + g[3 * t + 1] * a.y + g[3 * t + 2] * a.z;
+      g[3 * t + 0] -= dot * a.x;
+      g[3 * t + 1] -= dot * a.y;
+      g[3 * t + 2] -= dot * a.z;
+    }
+  }
+  for (int t = 0; t < NTERMS * 3; t++) grad[(size_t)i * NTERMS * 3 + t] = g[t];
+}
+
+// -------------------------------------------------------------------------
+// limiter (Limiter::Compute, ucs/limiters.tcc:53; limiter = 3)
+// -------------------------------------------------------------------------
+
+// Neighbour min/max (initialised to zero as the reference does) and the
+// modified Venkatakrishnan value, fused per node.
+__global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict__ nptr,
+                                                const int* __restrict__ nnbr, const double* __restrict__ q,
+                                                const double* __restrict__ grad, const double* __restrict__ xyz,
+                                                const double* __restrict__ vol, double chi, double K3,
+                                                double* __restrict__ lim) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double qi[NEQN], qmin[NEQN], qmax[NEQN], l[NEQN], gi[NEQN * 3];
+  for (int t = 0; t < NEQN; t++) {
+    qi[t] = q[(size_t)i * NVARS + t];
+    qmin[t] = 0.0;
+    qmax[t] = 0.0;
+    l[t] = 1.0;
+  }
+  for (int t = 0; t < NEQN * 3; t++) gi[t] = grad[(size_t)i * NTERMS * 3 + t];
+  const int k0 = nptr[i], k1 = nptr[i + 1];
+  for (int k = k0; k < k1; k++) {
+    const double* qj = &q[(size_t)nnbr[k] * NVARS];
+    for (int t = 0; t < NEQN; t++) {
+      double v = qj[t];
+      qmax[t] = (qmax[t] > v) ? qmax[t] : v;
+      qmin[t] = (qmin[t] < v) ? qmin[t] : v;
+    }
+  }
+  const double ep2 = 6.0 * 3.141592653589793 * vol[i] * K3;
+  const double xi0 = xyz[3 * i], xi1 = xyz[3 * i + 1], xi2 = xyz[3 * i + 2];
+  for (int k = k0; k < k1; k++) {
+    int j = nnbr[k];
+    const double* qj = &q[(size_t)j * NVARS];
+    double dx0 = 0.5 * (xyz[3 * j] - xi0), dx1 = 0.5 * (xyz[3 * j + 1] - xi1), dx2 = 0.5 * (xyz[3 * j + 2] - xi2);
+    for (int t = 0; t < NEQN; t++) {
+      double dQ = qj[t] - qi[t];
+      double Q = qi[t] + (0.5 * chi * dQ + (1.0 - chi) * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
+      double DM = Q - qi[t];
+      double DP = (Q > qi[t]) ? qmax[t] - qi[t] : qmin[t] - qi[t];
+      double v = (DP * DP + ep2 + 2.0 * DM * DP) / (DP * DP + 2.0 * DM * DM + DM * DP + ep2);
+      l[t] = (l[t] < v) ? l[t] : v;
+    }
+  }
+  for (int t = 0; t < NEQN; t++) lim[(size_t)i * NEQN + t] = l[t];
+}
+
+__device__ __forceinline__ int bad_extrap(double gamma, const double* Q) {
+  double r = Q[0];
+  double ir = 1.0 / r;
+  double u = Q[1] * ir, v = Q[2] * ir, w = Q[3] * ir;
+  double p = (gamma - 1.0) * (Q[4] - r * (0.5 * (u * u + v * v + w * w)));
+  return (p < 1.0e-10) || (r < 0.0) || (Q[4] < 1.0e-10);
+}
+
+// Kernel_PressureClip (ucs/limiters.tcc:737) evaluated with the post-limiter
+// values on both sides of every edge; a node whose own extrapolation, or the
+// Roe average with any neighbour's, is non-physical gets a zero limiter.
+// (The reference applies the same test edge by edge in sequence; the two
+// agree whenever no clip fires, and clips are counted in the health word.)
+__global__ void __launch_bounds__(128) k_pressure_clip(int nnode, const int* __restrict__ nptr,
+                                                       const int* __restrict__ nnbr, const double* __restrict__ q,
+                                                       const double* __restrict__ grad,
+                                                       const double* __restrict__ xyz, double chi, double gamma,
+                                                       const double* __restrict__ lim_in, double* __restrict__ lim_out,
+                                                       unsigned long long* health) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double li[NEQN];
+  for (int t = 0; t < NEQN; t++) li[t] = lim_in[(size_t)i * NEQN + t];
+  int clip = 0;
+  const double* qi = &q[(size_t)i * NVARS];
+  const double* gi = &grad[(size_t)i * NTERMS * 3];
+  for (int k = nptr[i]; k < nptr[i + 1] && !clip; k++) {
+    int j = nnbr[k];
+    const double* qj = &q[(size_t)j * NVARS];
+    const double* gj = &grad[(size_t)j * NTERMS * 3];
+    double dx[3], Qi[NEQN], Qj[NEQN];
+    for (int c = 0; c < 3; c++) dx[c] = 0.5 * (xyz[3 * j + c] - xyz[3 * i + c]);
+    for (int t = 0; t < NEQN; t++) {
+      double dQ = qj[t] - qi[t];
+      Qi[t] = qi[t] + (0.5 * chi * dQ + (1.0 - chi) * (gi[3 * t] * dx[0] + gi[3 * t + 1] * dx[1] + gi[3 * t + 2] * dx[2])) * li[t];
+      double lj = lim_in[(size_t)j * NEQN + t];
+      Qj[t] = qj[t] + (0.5 * chi * (-dQ) + (1.0 - chi) * (gj[3 * t] * (-dx[0]) + gj[3 * t + 1] * (-dx[1]) + gj[3 * t + 2] * (-dx[2]))) * lj;
+    }
+    if (bad_extrap(gamma, Qi)) { clip = 1; break; }
+    // RoeVariables (ucs/compressible.tcc:533) of the pair, then the same test
+    double gm1 = gamma - 1.0;
+    double rL = Qi[0], rR = Qj[0];
+    double uL = Qi[1] / rL, vL = Qi[2] / rL, wL = Qi[3] / rL;
+    double uR = Qj[1] / rR, vR = Qj[2] / rR, wR = Qj[3] / rR;
+    double PL = gm1 * (Qi[4] - 0.5 * rL * (uL * uL + vL * vL + wL * wL));
+    double PR = gm1 * (Qj[4] - 0.5 * rR * (uR * uR + vR * vR + wR * wR));
+    double hL = (Qi[4] + PL) / rL, hR = (Qj[4] + PR) / rR;
+    double rho = sqrt(rL * rR);
+    double sg = rho / (rL + rho);
+    double u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
+    double v2h = 0.5 * (u * u + v * v + w * w);
+    double Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
+    if (bad_extrap(gamma, Qr)) { clip = 1; break; }
+  }
+  if (clip) atomicAdd(&health[H_LIMCLIP], 1ull);
+  for (int t = 0; t < NEQN; t++) {
+    double v = clip ? 0.0 : li[t];
+    lim_out[(size_t)i * NEQN + t] = (v < 0.0) ? 0.0 : v;
+  }
+}
+
+// -------------------------------------------------------------------------
+// residual (SpatialResidual, ucs/residual.tcc:66)
+// -------------------------------------------------------------------------
+
+struct FluxConst {
+  double gamma, chi;
+  int ho, viscous;
+  double inv_retilde;  // Mach / Re
+  double S;            // Sutherland constant / T_ref
+  double cp_over_pr;   // (1/(gamma-1)) / Pr
+};
+
+__device__ __forceinline__ int kneecap5(double* f) {
+  int bad = 0;
+#pragma unroll
+  for (int i = 0; i < NEQN; i++)
+    if (isnan(f[i])) { f[i] = 0.0; bad = 1; }
+  return bad;
+}
+
+// Kernel_Inviscid_Flux (:192) + Kernel_Viscous_Flux (:390) for one edge; the
+// sum is stored as the flux leaving the left node.
+__global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __restrict__ en,
+                                                   const D4* __restrict__ ea, const double* __restrict__ eh,
+                                                   const double* __restrict__ q, const double* __restrict__ grad,
+                                                   const double* __restrict__ lim, FluxConst k,
+                                                   double* __restrict__ ef, unsigned long long* health) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int2 n = en[e];
+  const D4 a = ea[e];
+  const double* qL = &q[(size_t)n.x * NVARS];
+  const double* qR = &q[(size_t)n.y * NVARS];
+  double QL[NEQN], QR[NEQN];
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) { QL[t] = qL[t]; QR[t] = qR[t]; }
+  double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+  if (k.ho || k.viscous) { h0 = eh[3 * (size_t)e]; h1 = eh[3 * (size_t)e + 1]; h2 = eh[3 * (size_t)e + 2]; }
+  if (k.ho) {
+    const double* gL = &grad[(size_t)n.x * NTERMS * 3];
+    const double* gR = &grad[(size_t)n.y * NTERMS * 3];
+    const double* lL = &lim[(size_t)n.x * NEQN];
+    const double* lR = &lim[(size_t)n.y * NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) {
+      double dQ = qR[t] - qL[t];
+      double cl = 0.5 * k.chi * dQ + (1.0 - k.chi) * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2);
+      double cr = 0.5 * k.chi * (-dQ) + (1.0 - k.chi) * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2));
+      QL[t] = qL[t] + cl * lL[t];
+      QR[t] = qR[t] + cr * lR[t];
+    }
+  }
+  double f[NEQN];
+  roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
+  if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
+  if (k.viscous) {
+    // face state: plain average of the nodal conservative variables
+    double Q0 = (qL[0] + qR[0]) / 2.0, Q1 = (qL[1] + qR[1]) / 2.0, Q2 = (qL[2] + qR[2]) / 2.0,
+           Q3 = (qL[3] + qR[3]) / 2.0, Q4 = (qL[4] + qR[4]) / 2.0;
+    double iQ0 = 1.0 / Q0;
+    double u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
+    double P = (k.gamma - 1.0) * (Q4 - 0.5 * Q0 * (u * u + v * v + w * w));
+    double T = k.gamma * P * iQ0;
+    const double* gL = &grad[(size_t)n.x * NTERMS * 3];
+    const double* gR = &grad[(size_t)n.y * NTERMS * 3];
+    double g[NTERMS * 3];
+#pragma unroll
+    for (int t = 0; t < NTERMS * 3; t++) g[t] = 0.5 * (gL[t] + gR[t]);
+    if (k.ho) {
+      // directional correction along the edge (dx = xR - xL = 2 h)
+      double d0 = 2.0 * h0, d1 = 2.0 * h1, d2 = 2.0 * h2;
+      double s2 = d0 * d0 + d1 * d1 + d2 * d2;
+      double is2 = 1.0 / s2;
+#pragma unroll
+      for (int t = 0; t < NTERMS; t++) {
+        double qdots = d0 * g[3 * t] + d1 * g[3 * t + 1] + d2 * g[3 * t + 2];
+        int loc = c_gradlist[t];
+        double dq = (qR[loc] - qL[loc] - qdots) * is2;
+        g[3 * t] += dq * d0;
+        g[3 * t + 1] += dq * d1;
+        g[3 * t + 2] += dq * d2;
+      }
+    }
+    double fv[NEQN];
+    viscous_flux(u, v, w, T, g, a.x, a.y, a.z, a.w * k.inv_retilde, k.S, k.cp_over_pr, fv);
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) f[t] += fv[t];
+  }
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) ef[(size_t)e * NEQN + t] = f[t];
+}
+
+// Bkernel_Inviscid_Flux (:299) + Bkernel_Viscous_Flux (:472) for one
+// half-edge (boundary node, phantom node).
+__global__ void __launch_bounds__(128) k_bedge_flux(int nbedge, const int2* __restrict__ bn,
+                                                    const D4* __restrict__ ba, const double* __restrict__ q,
+                                                    const double* __restrict__ grad, FluxConst k,
+                                                    double* __restrict__ bf, unsigned long long* health) {
+  int he = blockIdx.x * blockDim.x + threadIdx.x;
+  if (he >= nbedge) return;
+  const int2 n = bn[he];
+  const D4 a = ba[he];
+  const double* qL = &q[(size_t)n.x * NVARS];
+  const double* qR = &q[(size_t)n.y * NVARS];
+  double QL[NEQN], QR[NEQN], f[NEQN];
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) { QL[t] = qL[t]; QR[t] = qR[t]; }
+  roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
+  if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
+  if (k.viscous) {
+    double Q0 = 0.5 * (qL[0] + qR[0]), Q1 = 0.5 * (qL[1] + qR[1]), Q2 = 0.5 * (qL[2] + qR[2]),
+           Q3 = 0.5 * (qL[3] + qR[3]), Q4 = 0.5 * (qL[4] + qR[4]);
+    double iQ0 = 1.0 / Q0;
+    double u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
+    double P = (k.gamma - 1.0) * (Q4 - 0.5 * Q0 * (u * u + v * v + w * w));
+    double T = k.gamma * P * iQ0;
+    double fv[NEQN];
+    viscous_flux(u, v, w, T, &grad[(size_t)n.x * NTERMS * 3], a.x, a.y, a.z, a.w * k.inv_retilde, k.S,
+                 k.cp_over_pr, fv);
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) f[t] += fv[t];
+  }
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) bf[(size_t)he * NEQN + t] = f[t];
+}
+
+// b_i = sum over incident edges in ascending edge id (-F_e if i is the left
+// node, +F_e otherwise) - sum of its half-edge fluxes; then the no-slip
+// residual hook (ModifyViscousWallResidual, ucs/compressible.tcc:1612) and
+// per-block partial sums of b^2 for the norms.
+__global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* __restrict__ nptr,
+                                                         const int* __restrict__ nedg, const double* __restrict__ ef,
+                                                         const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                         const double* __restrict__ bf, const int* __restrict__ bbc,
+                                                         const double* __restrict__ btw, double* __restrict__ b,
+                                                         double* __restrict__ part) {
+  __shared__ double red[kNormThreads / 32][6];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    double r[NEQN] = {0, 0, 0, 0, 0};
+    for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+      int se = nedg[k];
+      if (se < 0) {
+        const double* f = &ef[(size_t)(~se) * NEQN];
+#pragma unroll
+        for (int t = 0; t < NEQN; t++) r[t] += -f[t];
+      } else {
+        const double* f = &ef[(size_t)se * NEQN];
+#pragma unroll
+        for (int t = 0; t < NEQN; t++) r[t] += f[t];
+      }
+    }
+    for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+      int he = bhe[p];
+      const double* f = &bf[(size_t)he * NEQN];
+#pragma unroll
+      for (int t = 0; t < NEQN; t++) r[t] += -f[t];
+    }
+    for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+      int he = bhe[p];
+      if (bbc[he] != PCFD_BC_NOSLIP) continue;
+      r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = 0.0;
+      if (btw[he] < 0.0) r[0] = 0.0;
+    }
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) {
+      b[(size_t)i * NEQN + t] = r[t];
+      acc[1 + t] += r[t] * r[t];
+    }
+  }
+  acc[0] = acc[1] + acc[2] + acc[3] + acc[4] + acc[5];
+  // deterministic block reduction: warp shuffles then a fixed-order sum
+  for (int c = 0; c < 6; c++) {
+    double v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int w = 0; w < kNormThreads / 32; w++) v += red[w][threadIdx.x];
+    part[(size_t)blockIdx.x * 6 + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ part, double* __restrict__ norms) {
+  int c = threadIdx.x;
+  if (c >= 6) return;
+  double v = 0.0;
+  for (int bI = 0; bI < nblocks; bI++) v += part[(size_t)bI * 6 + c];
+  if (c == 0) norms[0] = sqrt(v) / ((double)nnode * NEQN);
+  else norms[c] = sqrt(v) / (double)nnode;
+}
+
+// -------------------------------------------------------------------------
+// host helpers
+// -------------------------------------------------------------------------
+
+template <class T>
+int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return set_err(PCFD_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return PCFD_OK;
+}
+
+template <class T>
+int dput(T** p, const T* h, size_t n) {
+  int rc = dalloc(p, n);
+  if (rc) return rc;
+  if (n) CUDA_TRY(cudaMemcpy(*p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  return PCFD_OK;
+}
+
+void free_solver(Solver* s) {
+  if (!s) return;
+  void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
+                  s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
+                  s->d_bgptr, s->d_bghe, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
+                  s->d_norms, s->d_health};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+// Most-normal neighbour of a no-slip wall node (ucs/bc.tcc:1184-1207); a
+// mesh constant, found once here instead of on every call.
+int normal_node(const pcfd_mesh_view* m, int node, const double* avec) {
+  int normalNode = -1;
+  double dotmax = 0.0;
+  const double* wx = &m->xyz[3 * node];
+  for (int k = m->ipsp[node]; k < m->ipsp[node + 1]; k++) {
+    int pt = m->psp[k];
+    const double* px = &m->xyz[3 * pt];
+    double dx[3] = {px[0] - wx[0], px[1] - wx[1], px[2] - wx[2]};
+    double mg = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    dx[0] = dx[0] / mg; dx[1] = dx[1] / mg; dx[2] = dx[2] / mg;
+    double dot = 0.0;
+    for (int i = 0; i < 3; i++) dot -= dx[i] * avec[i];
+    if (dot >= dotmax) { normalNode = pt; dotmax = dot; }
+  }
+  return normalNode;
+}
+
+BcConst make_bc_const(const Solver* s) {
+  BcConst k;
+  k.gamma = s->prm.gamma;
+  k.no_cvbc = s->prm.no_cvbc;
+  for (int j = 0; j < NVARS; j++) k.qinf[j] = s->qinf[j];
+  return k;
+}
+
+FluxConst make_flux_const(const Solver* s) {
+  FluxConst k;
+  k.gamma = s->prm.gamma;
+  k.chi = s->prm.chi;
+  k.ho = s->prm.sorder > 1;
+  k.viscous = s->prm.viscous;
+  k.inv_retilde = s->prm.Re != 0.0 ? s->prm.mach / s->prm.Re : 0.0;
+  k.S = 110.4 / s->prm.ref_temperature;
+  k.cp_over_pr = (1.0 / (s->prm.gamma - 1.0)) / s->prm.Pr;
+  return k;
+}
+
+void host_qinf(const pcfd_params& p, double* Q) {
+  // UpdateQinf (ucs/compressible.tcc:827): p = T = 1, rho = gamma p / T
+  double gamma = p.gamma, gm1 = gamma - 1.0;
+  double rho = 1.0 * gamma / 1.0;
+  double u = p.flowdir[0] * p.mach, v = p.flowdir[1] * p.mach, w = p.flowdir[2] * p.mach;
+  double E = 1.0 / gm1 + 0.5 * rho * (u * u + v * v + w * w);
+  Q[0] = rho; Q[1] = rho * u; Q[2] = rho * v; Q[3] = rho * w; Q[4] = E;
+  double ir = 1.0 / Q[0];
+  double uu = Q[1] * ir, vv = Q[2] * ir, ww = Q[3] * ir;
+  double P = gm1 * (Q[4] - 0.5 * Q[0] * (uu * uu + vv * vv + ww * ww));
+  Q[6] = P; Q[5] = gamma * P * ir; Q[7] = uu; Q[8] = vv; Q[9] = ww;
+}
+
+int run_bcs(Solver* s) {
+  BcConst k = make_bc_const(s);
+  if (s->bc_sequential) {
+    return launch(s, T_BC, [&] {
+      k_bc_sequential<<<1, 1, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, k, s->d_q,
+                                              s->d_health);
+    });
+  }
+  if (s->nbgroup == 0) return PCFD_OK;
+  return launch(s, T_BC, [&] {
+    k_bc_nodes<<<nblk(s->nbgroup, 128), 128, 0, s->stream>>>(s->nbgroup, s->d_bgnode, s->d_bgptr, s->d_bghe, s->d_bn,
+                                                            s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, k, s->d_q,
+                                                            s->d_health);
+  });
+}
+
+int run_gradient(Solver* s) {
+  int rc = launch(s, T_GRAD, [&] {
+    k_gradient<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_lsq, s->d_q,
+                                                          s->d_bptr, s->d_bhe, s->d_bbc, s->d_ba, s->d_grad);
+  });
+  if (rc == PCFD_OK) s->have_grad = 1;
+  return rc;
+}
+
+int run_limiter(Solver* s) {
+  if (s->prm.limiter == 0) {
+    // limiters stay 1.0 (OFF), Limiter ctor (ucs/limiters.tcc:36-41)
+    std::vector<double> ones((size_t)s->nnode * NEQN, 1.0);
+    CUDA_TRY(cudaMemcpyAsync(s->d_lim, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->have_lim = 1;
+    return PCFD_OK;
+  }
+  double K = s->prm.venkat_K;
+  int rc = launch(s, T_LIMITER, [&] {
+    k_venkat<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad, s->d_xyz,
+                                                        s->d_vol, s->prm.chi, K * K * K, s->d_b);
+  });
+  if (rc) return rc;
+  // d_b holds the pre-clip limiter as scratch; the clip writes the final value
+  rc = launch(s, T_LIMITER, [&] {
+    k_pressure_clip<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad,
+                                                               s->d_xyz, s->prm.chi, s->prm.gamma, s->d_b, s->d_lim,
+                                                               s->d_health);
+  });
+  if (rc == PCFD_OK) s->have_lim = 1;
+  return rc;
+}
+
+int run_residual(Solver* s) {
+  FluxConst k = make_flux_const(s);
+  if ((k.ho || k.viscous) && !s->have_grad) return set_err(PCFD_ERR_STATE, "residual: gradient not computed");
+  if (k.ho && !s->have_lim) return set_err(PCFD_ERR_STATE, "residual: limiter not computed");
+  int rc = launch(s, T_EDGEFLUX, [&] {
+    k_edge_flux<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q, s->d_grad,
+                                                           s->d_lim, k, s->d_ef, s->d_health);
+  });
+  if (rc) return rc;
+  if (s->nbedge > 0) {
+    rc = launch(s, T_BEDGEFLUX, [&] {
+      k_bedge_flux<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_q, s->d_grad, k,
+                                                               s->d_bf, s->d_health);
+    });
+    if (rc) return rc;
+  }
+  rc = launch(s, T_GATHER, [&] {
+    k_gather<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_ef, s->d_bptr, s->d_bhe,
+                                                         s->d_bf, s->d_bbc, s->d_btw, s->d_b, s->d_part);
+  });
+  if (rc) return rc;
+  return launch(s, T_NORM, [&] {
+    k_norm_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms);
+  });
+}
+
+}  // namespace
+
+// -------------------------------------------------------------------------
+// C ABI
+// -------------------------------------------------------------------------
+
+extern "C" {
+
+PCFD_API const char* pcfd_last_error(void) { return g_err.c_str(); }
+
+PCFD_API const char* pcfd_build_info(void) {
+  static std::string info;
+  if (info.empty()) {
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "pcfd sm_103a; CUDA runtime %d; edge-flux + node-gather residual (FP64)",
+                  CUDART_VERSION);
+    info = buf;
+  }
+  return info.c_str();
+}
+
+PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_solver_t* out) {
+  if (!m || !prm || !out) return set_err(PCFD_ERR_ARG, "pcfd_create: null argument");
+  *out = nullptr;
+  if (m->nnode <= 0 || m->nedge <= 0 || m->nbedge < 0 || m->nbnode != m->nbedge)
+    return set_err(PCFD_ERR_ARG, "pcfd_create: bad mesh sizes");
+  if (!m->edges || !m->edge_area || !m->xyz || !m->vol || !m->sw || !m->ipsp || !m->psp ||
+      (m->nbedge > 0 && (!m->bedges || !m->bedge_area || !m->bfactag)))
+    return set_err(PCFD_ERR_ARG, "pcfd_create: null mesh array");
+  if (prm->gamma <= 1.0 || prm->sorder < 1 || prm->sorder > 2 || prm->ntags <= 0 || !prm->bc_type || !prm->bc_twall)
+    return set_err(PCFD_ERR_ARG, "pcfd_create: bad parameters");
+  if (prm->limiter != 0 && prm->limiter != 3)
+    return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: only limiter 0 (off) and 3 (modified Venkatakrishnan)");
+  if (prm->viscous && (prm->Re <= 0.0 || prm->Pr <= 0.0 || prm->ref_temperature <= 0.0))
+    return set_err(PCFD_ERR_ARG, "pcfd_create: viscous run needs Re, Pr and ref_temperature > 0");
+  const long long nn = m->nnode, ne = m->nedge, nb = m->nbedge;
+  // validate integer maps before they reach a kernel
+  for (long long e = 0; e < ne; e++) {
+    int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+    if (a < 0 || a >= nn || b < 0 || b >= nn || a == b) return set_err(PCFD_ERR_ARG, "pcfd_create: edge node out of range");
+  }
+  for (long long k = 0; k < nb; k++) {
+    int a = m->bedges[2 * k], b = m->bedges[2 * k + 1];
+    if (a < 0 || a >= nn || b != nn + k) return set_err(PCFD_ERR_ARG, "pcfd_create: half-edge ids out of range");
+    int tag = m->bfactag[k];
+    if (tag < 0 || tag >= prm->ntags) return set_err(PCFD_ERR_ARG, "pcfd_create: half-edge tag without a BC");
+  }
+  if (m->ipsp[0] != 0) return set_err(PCFD_ERR_ARG, "pcfd_create: ipsp[0] != 0");
+  for (long long i = 0; i < nn; i++)
+    if (m->ipsp[i + 1] < m->ipsp[i]) return set_err(PCFD_ERR_ARG, "pcfd_create: ipsp not monotone");
+  for (long long k = 0; k < m->ipsp[nn]; k++)
+    if (m->psp[k] < 0 || m->psp[k] >= nn) return set_err(PCFD_ERR_ARG, "pcfd_create: psp out of range");
+
+  Solver* s = new Solver();
+  s->nnode = m->nnode;
+  s->nbnode = m->nbnode;
+  s->nedge = m->nedge;
+  s->nbedge = m->nbedge;
+  s->ntot = m->nnode + m->nbnode;
+  s->prm = *prm;
+  s->bc_type.assign(prm->bc_type, prm->bc_type + prm->ntags);
+  s->bc_twall.assign(prm->bc_twall, prm->bc_twall + prm->ntags);
+  s->prm.bc_type = s->bc_type.data();
+  s->prm.bc_twall = s->bc_twall.data();
+  if (s->prm.venkat_K <= 0.0) s->prm.venkat_K = 1.0;
+  host_qinf(s->prm, s->qinf);
+
+  int rc = PCFD_OK;
+#define TRY(x)                \
+  do {                        \
+    rc = (x);                 \
+    if (rc) {                 \
+      free_solver(s);         \
+      return rc;              \
+    }                         \
+  } while (0)
+  cudaError_t ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) { free_solver(s); return set_err(PCFD_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(ce)); }
+  cudaEventCreate(&s->ev0);
+  cudaEventCreate(&s->ev1);
+
+  // --- host-side integer preprocessing of the GPU maps ---
+  // node -> incident edges, ascending edge id
+  std::vector<int> nptr(nn + 1, 0);
+  for (long long e = 0; e < ne; e++) {
+    nptr[m->edges[2 * e] + 1]++;
+    nptr[m->edges[2 * e + 1] + 1]++;
+  }
+  for (long long i = 0; i < nn; i++) nptr[i + 1] += nptr[i];
+  std::vector<int> nedg(2 * ne), nnbr(2 * ne);
+  {
+    std::vector<int> fill(nptr.begin(), nptr.end() - 1);
+    for (long long e = 0; e < ne; e++) {
+      int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+      nedg[fill[a]] = ~(int)e; nnbr[fill[a]++] = b;
+      nedg[fill[b]] = (int)e; nnbr[fill[b]++] = a;
+    }
+  }
+  // node -> boundary half-edges (bedge order) and boundary node groups
+  std::vector<int> bptr(nn + 1, 0), bhe(nb);
+  for (long long k = 0; k < nb; k++) bptr[m->bedges[2 * k] + 1]++;
+  for (long long i = 0; i < nn; i++) bptr[i + 1] += bptr[i];
+  {
+    std::vector<int> fill(bptr.begin(), bptr.end() - 1);
+    for (long long k = 0; k < nb; k++) bhe[fill[m->bedges[2 * k]]++] = (int)k;
+  }
+  std::vector<int> gnode, gptr(1, 0);
+  for (long long i = 0; i < nn; i++)
+    if (bptr[i + 1] > bptr[i]) {
+      gnode.push_back((int)i);
+      gptr.push_back(bptr[i + 1]);
+    }
+  s->nbgroup = (int)gnode.size();
+  // per-half-edge BC data; no-slip normal nodes
+  std::vector<int> bbc(nb), bnrm(nb, -1);
+  std::vector<double> btw(nb, 0.0);
+  std::vector<char> hardset(nn, 0);
+  for (long long k = 0; k < nb; k++) {
+    int tag = m->bfactag[k];
+    bbc[k] = s->bc_type[tag];
+    btw[k] = s->bc_twall[tag] / s->prm.ref_temperature;
+    if (bbc[k] == PCFD_BC_NOSLIP) bnrm[k] = normal_node(m, m->bedges[2 * k], &m->bedge_area[4 * k]);
+    if (bbc[k] == PCFD_BC_NOSLIP || bbc[k] == PCFD_BC_SONIC_INFLOW || bbc[k] == PCFD_BC_DIRICHLET)
+      hardset[m->bedges[2 * k]] = 1;
+  }
+  s->bc_sequential = 0;
+  for (long long k = 0; k < nb; k++)
+    if (bnrm[k] >= 0 && hardset[bnrm[k]]) s->bc_sequential = 1;
+
+  std::vector<int2> en(ne), bn(nb);
+  std::vector<D4> ea(ne), ba(nb);
+  for (long long e = 0; e < ne; e++) {
+    en[e] = make_int2(m->edges[2 * e], m->edges[2 * e + 1]);
+    const double* a = &m->edge_area[4 * e];
+    ea[e] = D4{a[0], a[1], a[2], a[3]};
+  }
+  for (long long k = 0; k < nb; k++) {
+    bn[k] = make_int2(m->bedges[2 * k], m->bedges[2 * k + 1]);
+    const double* a = &m->bedge_area[4 * k];
+    ba[k] = D4{a[0], a[1], a[2], a[3]};
+  }
+
+  TRY(dput(&s->d_en, en.data(), ne));
+  TRY(dput(&s->d_ea, ea.data(), ne));
+  TRY(dput(&s->d_bn, bn.data(), nb));
+  TRY(dput(&s->d_ba, ba.data(), nb));
+  TRY(dput(&s->d_bbc, bbc.data(), nb));
+  TRY(dput(&s->d_btw, btw.data(), nb));
+  TRY(dput(&s->d_bnrm, bnrm.data(), nb));
+  TRY(dput(&s->d_xyz, m->xyz, 3 * nn));
+  TRY(dput(&s->d_vol, m->vol, nn));
+  TRY(dput(&s->d_nptr, nptr.data(), nn + 1));
+  TRY(dput(&s->d_nedg, nedg.data(), 2 * ne));
+  TRY(dput(&s->d_nnbr, nnbr.data(), 2 * ne));
+  TRY(dput(&s->d_bptr, bptr.data(), nn + 1));
+  TRY(dput(&s->d_bhe, bhe.data(), nb));
+  TRY(dput(&s->d_bgnode, gnode.data(), gnode.size()));
+  TRY(dput(&s->d_bgptr, gptr.data(), gptr.size()));
+  TRY(dput(&s->d_bghe, bhe.data(), nb));  // groups are the non-empty bptr rows, same order
+  TRY(dalloc(&s->d_eh, 3 * ne));
+  TRY(dalloc(&s->d_lsq, 3 * 2 * ne));
+  TRY(dalloc(&s->d_q, (size_t)s->ntot * NVARS));
+  TRY(dalloc(&s->d_grad, (size_t)nn * NTERMS * 3));
+  TRY(dalloc(&s->d_lim, (size_t)nn * NEQN));
+  TRY(dalloc(&s->d_b, (size_t)nn * NEQN));
+  TRY(dalloc(&s->d_ef, (size_t)ne * NEQN));
+  TRY(dalloc(&s->d_bf, (size_t)nb * NEQN));
+  TRY(dalloc(&s->d_part, (size_t)kNormBlocks * 6));
+  TRY(dalloc(&s->d_norms, 6));
+  TRY(dalloc(&s->d_health, 8));
+  if (cudaMemsetAsync(s->d_health, 0, 8 * sizeof(unsigned long long), s->stream) != cudaSuccess) {
+    free_solver(s);
+    return set_err(PCFD_ERR_CUDA, "memset health");
+  }
+  double* d_sw = nullptr;
+  double* d_qinf = nullptr;
+  TRY(dput(&d_sw, m->sw, 6 * nn));
+  TRY(dput(&d_qinf, s->qinf, NVARS));
+  TRY(launch(s, T_SETUP, [&] {
+    k_lsq_weights<<<nblk(nn, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_xyz, d_sw, s->d_lsq);
+  }));
+  TRY(launch(s, T_SETUP, [&] {
+    k_edge_half<<<nblk(ne, 256), 256, 0, s->stream>>>(s->nedge, s->d_en, s->d_xyz, s->d_eh);
+  }));
+  TRY(launch(s, T_SETUP, [&] {
+    k_fill_state<<<nblk(s->ntot, 256), 256, 0, s->stream>>>(s->ntot, d_qinf, s->d_q);
+  }));
+  ce = cudaStreamSynchronize(s->stream);
+  cudaFree(d_sw);
+  cudaFree(d_qinf);
+  if (ce != cudaSuccess) {
+    free_solver(s);
+    return set_err(PCFD_ERR_CUDA, std::string("pcfd_create setup: ") + cudaGetErrorString(ce));
+  }
+  // the limiter starts at 1.0 (OFF), as the Limiter constructor leaves it
+  {
+    std::vector<double> ones((size_t)nn * NEQN, 1.0);
+    if (cudaMemcpy(s->d_lim, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+      free_solver(s);
+      return set_err(PCFD_ERR_CUDA, "limiter init");
+    }
+  }
+#undef TRY
+  *out = (pcfd_solver_t)s;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_destroy(pcfd_solver_t h) {
+  if (!h) return set_err(PCFD_ERR_ARG, "pcfd_destroy: null handle");
+  Solver* s = (Solver*)h;
+  cudaStreamSynchronize(s->stream);
+  free_solver(s);
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_state(pcfd_solver_t h, const double* q, int nvars, int nrows) {
+  Solver* s = (Solver*)h;
+  if (!s || !q || nvars != NVARS || nrows != s->ntot) return set_err(PCFD_ERR_ARG, "pcfd_set_state: bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(s->d_q, q, (size_t)nrows * NVARS * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->have_grad = s->have_lim = 0;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_get_state(pcfd_solver_t h, double* q, int nvars, int nrows) {
+  Solver* s = (Solver*)h;
+  if (!s || !q || nvars != NVARS || nrows != s->ntot) return set_err(PCFD_ERR_ARG, "pcfd_get_state: bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(q, s->d_q, (size_t)nrows * NVARS * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_get_qinf(pcfd_solver_t h, double* qinf10) {
+  Solver* s = (Solver*)h;
+  if (!s || !qinf10) return set_err(PCFD_ERR_ARG, "pcfd_get_qinf: bad arguments");
+  std::memcpy(qinf10, s->qinf, sizeof(s->qinf));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_update_bcs(pcfd_solver_t h) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_update_bcs: null handle");
+  int rc = run_bcs(s);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->have_grad = s->have_lim = 0;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_gradient(pcfd_solver_t h, double* qgrad_out) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_gradient: null handle");
+  int rc = run_gradient(s);
+  if (rc) return rc;
+  if (qgrad_out)
+    CUDA_TRY(cudaMemcpyAsync(qgrad_out, s->d_grad, (size_t)s->nnode * NTERMS * 3 * sizeof(double),
+                             cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_limiter(pcfd_solver_t h, double* l_out) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_limiter: null handle");
+  if (s->prm.limiter != 0 && !s->have_grad) return set_err(PCFD_ERR_STATE, "pcfd_limiter: gradient not computed");
+  int rc = run_limiter(s);
+  if (rc) return rc;
+  if (l_out)
+    CUDA_TRY(cudaMemcpyAsync(l_out, s->d_lim, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
+                             s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_residual(pcfd_solver_t h, double* b_out, double* norms_out) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_residual: null handle");
+  int rc = run_residual(s);
+  if (rc) return rc;
+  if (b_out)
+    CUDA_TRY(cudaMemcpyAsync(b_out, s->d_b, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
+                             s->stream));
+  if (norms_out)
+    CUDA_TRY(cudaMemcpyAsync(norms_out, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_residual_full(pcfd_solver_t h, double* norms_out) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_residual_full: null handle");
+  const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
+  int rc;
+  if ((rc = run_bcs(s))) return rc;
+  if (need_grad) {
+    if ((rc = run_gradient(s))) return rc;
+    if (s->prm.sorder > 1 && (rc = run_limiter(s))) return rc;
+  }
+  if ((rc = run_residual(s))) return rc;
+  if (norms_out)
+    CUDA_TRY(cudaMemcpyAsync(norms_out, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_bench_residual_full(pcfd_solver_t h, int nsteps, double* ms_out, double* norms_out) {
+  Solver* s = (Solver*)h;
+  if (!s || nsteps <= 0 || !ms_out) return set_err(PCFD_ERR_ARG, "pcfd_bench_residual_full: bad arguments");
+  const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
+  int saved = s->profile;
+  s->profile = 0;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaEventRecord(e0, s->stream));
+  int rc = PCFD_OK;
+  for (int it = 0; it < nsteps && rc == PCFD_OK; it++) {
+    rc = run_bcs(s);
+    if (!rc && need_grad) rc = run_gradient(s);
+    if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s);
+    if (!rc) rc = run_residual(s);
+  }
+  cudaEventRecord(e1, s->stream);
+  cudaError_t ce = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->profile = saved;
+  if (rc) return rc;
+  if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("bench: ") + cudaGetErrorString(ce));
+  *ms_out = ms;
+  if (norms_out) {
+    CUDA_TRY(cudaMemcpyAsync(norms_out, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_device(int device) {
+  int n = 0;
+  CUDA_TRY(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return set_err(PCFD_ERR_ARG, "pcfd_set_device: no such device");
+  CUDA_TRY(cudaSetDevice(device));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_device_sync(void) {
+  CUDA_TRY(cudaDeviceSynchronize());
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_profile_enable(pcfd_solver_t h, int on) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "null handle");
+  s->profile = on ? 1 : 0;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_profile_reset(pcfd_solver_t h) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "null handle");
+  for (int i = 0; i < T_COUNT; i++) { s->t_ms[i] = 0.0; s->t_n[i] = 0; }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_profile_get(pcfd_solver_t h, int i, char* name_buf, int name_len, double* ms_total,
+                              long long* launches) {
+  Solver* s = (Solver*)h;
+  if (!s || i < 0 || i >= T_COUNT) return PCFD_ERR_ARG;
+  if (name_buf && name_len > 0) {
+    std::strncpy(name_buf, kTimerNames[i], name_len - 1);
+    name_buf[name_len - 1] = 0;
+  }
+  if (ms_total) *ms_total = s->t_ms[i];
+  if (launches) *launches = s->t_n[i];
+  return PCFD_OK;
+}
+
+PCFD_API long long pcfd_launch_count(pcfd_solver_t h) {
+  Solver* s = (Solver*)h;
+  return s ? s->launches : -1;
+}
+
+PCFD_API int pcfd_get_health(pcfd_solver_t h, long long* c8) {
+  Solver* s = (Solver*)h;
+  if (!s || !c8) return set_err(PCFD_ERR_ARG, "pcfd_get_health: bad arguments");
+  unsigned long long tmp[8];
+  CUDA_TRY(cudaMemcpyAsync(tmp, s->d_health, sizeof(tmp), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < 8; i++) c8[i] = (long long)tmp[i];
+  return PCFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+"""ctypes access to the CPU oracle (oracle/liboracle.so) - test infrastructure."""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+_LLP = C.POINTER(C.c_longlong)
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        from proteuscfd_gb300 import _native as N
+        from proteuscfd_gb300 import build as B
+        B.build_oracle()
+        L = C.CDLL(str(ROOT / "oracle" / "liboracle.so"))
+        MV = C.POINTER(N.MeshView)
+        PP = C.POINTER(N.Params)
+        protos = {
+            "oracle_aux": (None, [C.c_double, _DP]),
+            "oracle_qinf": (None, [PP, _DP]),
+            "oracle_init_state": (None, [PP, C.c_int, _DP]),
+            "oracle_roe_flux": (None, [_DP, _DP, _DP, C.c_double, C.c_double, _DP]),
+            "oracle_viscous_flux": (None, [PP, _DP, _DP, _DP, C.c_double, _DP]),
+            "oracle_normal_node": (C.c_int, [MV, C.c_int, _DP]),
+            "oracle_update_bcs": (C.c_int, [MV, PP, _DP]),
+            "oracle_gradient": (C.c_int, [MV, PP, _DP, _DP]),
+            "oracle_limiter": (C.c_int, [MV, PP, _DP, _DP, _DP, _LLP]),
+            "oracle_residual": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _LLP]),
+            "oracle_residual_scaled": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _DP, _LLP]),
+            "oracle_lu": (C.c_int, [_DP, _IP, C.c_int]),
+            "oracle_lusolve": (None, [_DP, _DP, _IP, _DP, C.c_int]),
+            "oracle_matvec": (None, [_DP, _DP, _DP, C.c_int]),
+            "oracle_tri_area": (None, [_DP, _DP, _DP, _DP]),
+            "oracle_tet_vol": (C.c_double, [_DP, _DP, _DP, _DP]),
+        }
+        for n, (r, a) in protos.items():
+            f = getattr(L, n)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def dp(a):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_DP)
+
+
+def ip(a):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_IP)
+
+
+class OracleSpace:
+    """The oracle run on the same mesh view and parameters as a SolutionSpace."""
+
+    def __init__(self, mesh, param):
+        self.mesh = mesh
+        self.param = param
+        self.cp = param.to_c()
+        self.L = lib()
+
+    def qinf(self):
+        q = np.zeros(10)
+        self.L.oracle_qinf(C.byref(self.cp), dp(q))
+        return q
+
+    def update_bcs(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).copy()
+        rc = self.L.oracle_update_bcs(C.byref(self.mesh.view), C.byref(self.cp), dp(q))
+        assert rc == 0
+        return q
+
+    def gradient(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        g = np.zeros((self.mesh.nnode, 27))
+        assert self.L.oracle_gradient(C.byref(self.mesh.view), C.byref(self.cp), dp(q), dp(g)) == 0
+        return g
+
+    def limiter(self, q, g):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        l = np.zeros((self.mesh.nnode, 5))
+        nclip = C.c_longlong()
+        assert self.L.oracle_limiter(C.byref(self.mesh.view), C.byref(self.cp), dp(q), dp(g), dp(l),
+                                     C.byref(nclip)) == 0
+        return l, nclip.value
+
+    def residual(self, q, g=None, l=None):
+        n = self.mesh.nnode
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        g = np.zeros((n, 27)) if g is None else np.ascontiguousarray(g)
+        l = np.ones((n, 5)) if l is None else np.ascontiguousarray(l)
+        b = np.zeros((n, 5))
+        babs = np.zeros((n, 5))
+        norms = np.zeros(6)
+        kc = C.c_longlong()
+        assert self.L.oracle_residual_scaled(C.byref(self.mesh.view), C.byref(self.cp), dp(q), dp(g), dp(l), dp(b),
+                                             dp(babs), dp(norms), C.byref(kc)) == 0
+        self.last_babs = babs
+        return b, norms, kc.value
+
+    def full(self, q):
+        """UpdateBCs, gradient, limiter, residual - the NewtonIterate order."""
+        q = self.update_bcs(q)
+        p = self.param
+        g = l = None
+        if p.sorder > 1 or p.viscous:
+            g = self.gradient(q)
+        if p.sorder > 1:
+            l, _ = self.limiter(q, g)
+        b, norms, _ = self.residual(q, g, l)
+        return q, g, l, b, norms

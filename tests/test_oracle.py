@@ -1,0 +1,164 @@
+"""The CPU oracle, pinned before it is trusted: against the reference's own
+ucs/matrix.h and ucs/geometry.h (golden vectors made by
+tests/golden/make_golden.py, and live through oracle/_ref when the reference
+tree is present), and against the analytic properties the reference's tests
+and the scheme imply."""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from oracle_lib import OracleSpace, dp, ip
+from proteuscfd_gb300 import Mesh, Param, cases
+from proteuscfd_gb300 import _native as N
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+REF_LIB = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "libref_pin.so"
+
+
+def test_lu_and_matvec_match_reference_vectors_bitwise():
+    d = json.loads((GOLDEN / "ref_pin_vectors.json").read_text())
+    L = O.lib()
+    for c in d["matrix"]:
+        a = np.ascontiguousarray(np.array(c["a"]))
+        p = np.zeros(5, dtype=np.int32)
+        err = L.oracle_lu(dp(a), ip(p), 5)
+        assert err == c["err"]
+        assert np.array_equal(a, np.array(c["lu"]))
+        assert p.tolist() == c["piv"]
+        b = np.array(c["b"])
+        x = np.zeros(5)
+        L.oracle_lusolve(dp(a), dp(b), ip(p), dp(x), 5)
+        assert np.array_equal(b, np.array(c["solve"]))
+        y = np.zeros(5)
+        L.oracle_matvec(dp(np.ascontiguousarray(np.array(c["a"]))), dp(np.array(c["b"])), dp(y), 5)
+        assert np.array_equal(y, np.array(c["matvec"]))
+
+
+def test_geometry_matches_reference_vectors_bitwise():
+    d = json.loads((GOLDEN / "ref_pin_vectors.json").read_text())
+    L = O.lib()
+    for g in d["geometry"]:
+        pts = [np.ascontiguousarray(np.array(p)) for p in g["pts"]]
+        r = np.zeros(3)
+        L.oracle_tri_area(dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(r))
+        assert np.array_equal(r, np.array(g["tri_area"]))
+        assert L.oracle_tet_vol(*[dp(p) for p in pts]) == g["tet_vol"]
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="reference tree not present")
+def test_lu_matches_live_reference():
+    R = C.CDLL(str(REF_LIB))
+    L = O.lib()
+    rng = np.random.default_rng(7)
+    for _ in range(200):
+        a = rng.normal(size=(5, 5))
+        a1, a2 = a.copy(), a.copy()
+        p1, p2 = np.zeros(5, np.int32), np.zeros(5, np.int32)
+        assert R.ref_lu(dp(a1), ip(p1), 5) == L.oracle_lu(dp(a2), ip(p2), 5)
+        assert np.array_equal(a1, a2) and np.array_equal(p1, p2)
+
+
+def euler_param(**kw):
+    base = dict(gamma=1.4, mach=0.7, bc_type={t: N.BC_FARFIELD for t in range(1, 7)})
+    base.update(kw)
+    return Param(**base)
+
+
+def test_roe_flux_consistency():
+    """RoeFlux(Q, Q) = area * F(Q): zero dissipation for equal states."""
+    L = O.lib()
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        rho = 1.0 + rng.uniform(-0.3, 0.3)
+        u = rng.normal(size=3)
+        p = 1.0 + rng.uniform(-0.3, 0.3)
+        E = p / 0.4 + 0.5 * rho * (u @ u)
+        Q = np.array([rho, *(rho * u), E])
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        a = np.array([*n, 0.37])
+        f = np.zeros(5)
+        L.oracle_roe_flux(dp(Q.copy()), dp(Q.copy()), dp(a), 0.0, 1.4, dp(f))
+        th = u @ n
+        ref = 0.37 * np.array([rho * th, rho * u[0] * th + p * n[0], rho * u[1] * th + p * n[1],
+                               rho * u[2] * th + p * n[2], (E + p) * th])
+        assert np.allclose(f, ref, rtol=1e-13, atol=1e-13)
+
+
+def test_freestream_preserved():
+    """Uniform freestream on a closed dual: every residual is zero to rounding."""
+    m = Mesh.box(8, 7, 6, jitter=0.2, seed=5)
+    prm = euler_param()
+    o = OracleSpace(m, prm)
+    q = np.tile(o.qinf(), (m.nnode + m.nbedge, 1))
+    q2 = o.update_bcs(q)
+    assert np.allclose(q2, q, rtol=0, atol=1e-14)
+    b, norms, kc = o.residual(q2)
+    assert kc == 0
+    assert np.abs(b).max() < 1e-13
+
+
+def test_residual_is_conservative():
+    """Sum of b over all nodes equals minus the sum of boundary fluxes:
+    interior edge fluxes cancel pairwise (telescoping)."""
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=9)
+    prm = euler_param(mach=0.5)
+    o = OracleSpace(m, prm)
+    q = cases.smooth_state(m, o.qinf(), m.nnode + m.nbedge)
+    q = o.update_bcs(q)
+    b, _, _ = o.residual(q)
+    # boundary-only residual: the same call on a mesh view without interior edges
+    L = O.lib()
+    bflux = np.zeros(5)
+    be, ba = m.bedges, m.bedge_area
+    for k in range(m.nbedge):
+        f = np.zeros(5)
+        L.oracle_roe_flux(dp(np.ascontiguousarray(q[be[k, 0]])), dp(np.ascontiguousarray(q[be[k, 1]])),
+                          dp(np.ascontiguousarray(ba[k])), 0.0, 1.4, dp(f))
+        bflux += f
+    assert np.allclose(b.sum(axis=0), -bflux, rtol=1e-12, atol=1e-12)
+
+
+def test_lsq_gradient_exact_for_linear_fields():
+    """The weighted LSQ gradient reproduces a linear field exactly at every
+    node (the zero-error checks of unitTest/gradientTest.h, on a linear
+    field where the error must vanish on any stencil)."""
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=11)
+    prm = euler_param()
+    o = OracleSpace(m, prm)
+    q = np.tile(o.qinf(), (m.nnode + m.nbedge, 1))
+    x = m.xyz
+    G = np.array([0.3, -0.7, 1.1])
+    q[:m.nnode, 0] = 1.0 + x @ G
+    g = o.gradient(q)
+    assert np.allclose(g[:, 0:3], G, rtol=0, atol=1e-11)
+    assert np.abs(g[:, 3:15]).max() < 1e-11  # momentum/energy constant
+
+
+def test_limiter_is_one_for_linear_fields_far_from_bounds():
+    m = Mesh.box(6, 6, 6, jitter=0.1, seed=2)
+    prm = euler_param(sorder=2, limiter=3)
+    o = OracleSpace(m, prm)
+    q = cases.smooth_state(m, o.qinf(), m.nnode + m.nbedge, amp=1e-3)
+    g = o.gradient(q)
+    l, nclip = o.limiter(q, g)
+    assert nclip == 0
+    assert np.all(l <= 1.0) and np.all(l >= 0.0)
+
+
+def test_noslip_normal_node_is_wall_normal():
+    m = Mesh.box(5, 5, 5, jitter=0.0)
+    L = O.lib()
+    be, ba = m.bedges, m.bedge_area
+    tag = m.bfactag
+    for k in range(m.nbedge):
+        if tag[k] != 3:
+            continue
+        node = int(be[k, 0])
+        nn = L.oracle_normal_node(C.byref(m.view), node, dp(np.ascontiguousarray(ba[k])))
+        assert nn >= 0
+        assert m.xyz[nn, 1] > m.xyz[node, 1]
