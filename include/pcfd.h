@@ -128,6 +128,10 @@ typedef struct pcfd_params {
   int limiter;            /* 0 none, 3 modified Venkatakrishnan (Param::limiter) */
   double venkat_K;        /* limiter K; the reference hard-codes 1.0 */
   int no_cvbc;            /* Param::no_cvbc */
+  int jac_boundary_eval;  /* Param::boundaryJacEval: 0 re-derive the phantom state from each
+                           * perturbed interior state (reference default), 1 keep it frozen;
+                           * 3 re-derive it for the base state too, so the boundary
+                           * condition's sub-iteration drift cancels (no reference counterpart) */
   int ntags;              /* entries in bc_type/bc_twall, indexed by factag */
   const int* bc_type;     /* pcfd_bc_type per factag */
   const double* bc_twall; /* BCObj::twall per factag [K]; < 0 = adiabatic */
@@ -162,6 +166,70 @@ PCFD_API int pcfd_residual(pcfd_solver_t s, double* b_out, double* norms_out);
  * NewtonIterate runs (ucs/solutionSpace.tcc:662-697), without copying fields
  * back; norms_out as for pcfd_residual. */
 PCFD_API int pcfd_residual_full(pcfd_solver_t s, double* norms_out);
+
+/* ComputeTimesteps (ucs/timestep.tcc:7), local time stepping: dt_i = CFL
+ * vol_i / sum(max eigenvalue * area).  dt_out [nnode] and dtmin optional. */
+PCFD_API int pcfd_timestep(pcfd_solver_t s, double cfl, double* dt_out, double* dtmin);
+/* Storage precision of the off-diagonal Jacobian blocks: 0 FP64, 1 FP32,
+ * 2 BF16 (FP64 accumulation in every product; the diagonal stays FP64).
+ * The reference stores everything in FP64 (CRSMatrix<T>, ucs/crsmatrix.h:10). */
+PCFD_API int pcfd_set_jacobian_precision(pcfd_solver_t s, int precision);
+/* ComputeJacobians (ucs/jacobian.tcc:13): finite-difference Roe blocks
+ * (Kernel_NumJac :254, Bkernel_NumJac :459), analytic viscous blocks
+ * (:734), diagonal column sums (:437), vol/dtau with the last time step
+ * (ContributeTemporalTerms :214), no-slip row changes (ucs/bc.tcc:748), and
+ * the diagonal LU of CRSMatrix::PrepareSGS (ucs/crsmatrix.tcc:840).  Applies
+ * the boundary conditions to the state first, as the reference's boundary
+ * kernel does. */
+PCFD_API int pcfd_jacobian(pcfd_solver_t s);
+/* The assembled matrix in the reference layout: blocks [nblocks][5][5],
+ * row-major, diagonal first in each row (before its LU). */
+PCFD_API int pcfd_get_jacobian(pcfd_solver_t s, double* blocks, long long nblocks);
+PCFD_API long long pcfd_nblocks(pcfd_solver_t s);
+/* CRS row pointers ia [nnode+1], column ids ja [nblocks] and the number of
+ * colours of the Gauss-Seidel sweeps; any pointer may be null. */
+PCFD_API int pcfd_crs_structure(pcfd_solver_t s, int* ia, int* ja, int* ncolor);
+/* The colouring of the Gauss-Seidel sweeps: rows of colour c are
+ * rows[color_ptr[c] .. color_ptr[c+1]); color_ptr has ncolor+1 entries, rows
+ * nnode.  No reference counterpart (the reference sweeps rows in order). */
+PCFD_API int pcfd_coloring(pcfd_solver_t s, int* color_ptr, int* rows);
+/* CRS::SGS (ucs/crs.tcc:62) with x = 0 and b = the last residual: nsweeps
+ * multicolour symmetric block Gauss-Seidel sweeps.  x_out [nnode][5] and
+ * dnorm (|norm change of x over the last sweep|, the reference's return
+ * value) optional. */
+PCFD_API int pcfd_sgs(pcfd_solver_t s, int nsweeps, double* x_out, double* dnorm);
+/* NaN/Inf zeroing and CompressibleEqnSet::ApplyDQ (ucs/compressible.tcc:929)
+ * of x (x_in [nnode][5] if given, else the last linear solution); dqnorm =
+ * ParallelL2Norm of x (ucs/solutionSpace.tcc:817). */
+PCFD_API int pcfd_apply_dq(pcfd_solver_t s, const double* x_in, double* dqnorm);
+
+typedef struct pcfd_newton_opts {
+  int iter;             /* outer iteration number, from 1 (SolutionSpace::iter) */
+  double cfl;           /* Param::cfl */
+  double cfl_start;     /* Param::cflStart (ramp start; <= 0: no ramp) */
+  int cfl_ramp_steps;   /* Param::cflRampingSteps */
+  int nsgs;             /* Param::nSgs: SGS sweeps, or FGMRES preconditioner sweeps */
+  int jac_update_freq;  /* Param::jacobianFreq */
+  int jac_precision;    /* 0 FP64, 1 FP32, 2 BF16 off-diagonal storage */
+  int linear_solver;    /* 0 block SGS (the reference's), 1 FGMRES preconditioned by SGS */
+  int fgmres_m;         /* Krylov dimension per restart (FGMRES) */
+  int fgmres_restarts;  /* restarts (FGMRES) */
+  double fgmres_rtol;   /* relative tolerance (FGMRES) */
+} pcfd_newton_opts;
+
+typedef struct pcfd_newton_report {
+  double res[6];  /* resGlobal and per-equation residual norms before the update */
+  double dqnorm;  /* update norm */
+  double dtmin;   /* smallest local time step */
+  double lin_res; /* SGS: norm change of the last sweep; FGMRES: final relative residual */
+  int lin_iters;  /* sweeps or Krylov iterations */
+  double cfl;     /* CFL used */
+} pcfd_newton_report;
+
+/* One outer iteration in the reference's order: PreTimeAdvance (Jacobian,
+ * time step; ucs/solutionSpace.tcc:573) then NewtonIterate (:640: boundary
+ * conditions, gradient, limiter, residual, linear solve, update). */
+PCFD_API int pcfd_newton_step(pcfd_solver_t s, const pcfd_newton_opts* opts, pcfd_newton_report* report);
 
 /* Runs nsteps of pcfd_residual_full back to back on the handle's stream and
  * returns their device time from CUDA events recorded on that stream (the

@@ -858,3 +858,393 @@ double oracle_tet_vol(const double* p1, const double* p2, const double* p3, cons
   t[2] = v1[0] * v2[1] - v2[0] * v1[1];
   return (v3[0] * t[0] + v3[1] * t[1] + v3[2] * t[2]) / 6.0;
 }
+
+/* ---------------------------------------------------------------------- */
+/* implicit part: time step, Jacobian, SGS, update                         */
+/* ---------------------------------------------------------------------- */
+
+/* MaxEigenvalue, ucs/compressible.tcc:799, on the face-averaged state */
+static double max_eigenvalue(const pcfd_params* prm, const double* QL, const double* QR, const double* avec) {
+  double t[NVARS];
+  for (int i = 0; i < NEQN; i++) t[i] = 0.5 * (QL[i] + QR[i]);
+  oracle_aux(prm->gamma, t);
+  double gm1 = prm->gamma - 1.0;
+  double rho = t[0], u = t[1] / rho, v = t[2] / rho, w = t[3] / rho;
+  double v2h = 0.5 * (u * u + v * v + w * w);
+  double P = gm1 * (t[4] - rho * v2h);
+  double c = sqrt(prm->gamma * P / rho);
+  double theta = u * avec[0] + v * avec[1] + w * avec[2];
+  double e4 = fabs(theta + c), e5 = fabs(theta - c);
+  return dmax(e4, e5);
+}
+
+/* ComputeTimesteps with local time stepping, ucs/timestep.tcc:7,80,115 */
+double oracle_timestep(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, double cfl, double* dt) {
+  const int nn = m->nnode;
+  for (int i = 0; i < nn; i++) dt[i] = 0.0;
+  for (int e = 0; e < m->nedge; e++) {
+    int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+    const double* avec = &m->edge_area[4 * e];
+    double s = max_eigenvalue(prm, &q[(size_t)a * NVARS], &q[(size_t)b * NVARS], avec) * avec[3];
+    dt[b] += s;
+    dt[a] += s;
+  }
+  for (int k = 0; k < m->nbedge; k++) {
+    int a = m->bedges[2 * k], b = m->bedges[2 * k + 1];
+    const double* avec = &m->bedge_area[4 * k];
+    dt[a] += max_eigenvalue(prm, &q[(size_t)a * NVARS], &q[(size_t)b * NVARS], avec) * avec[3];
+  }
+  double dtmin = 0.0;
+  for (int i = 0; i < nn; i++) {
+    dt[i] = cfl * (m->vol[i] / dt[i]);
+    dtmin = (i == 0) ? dt[i] : dmin(dtmin, dt[i]);
+  }
+  return dtmin;
+}
+
+/* CRSMatrix::Init, ucs/crsmatrix.tcc:48: diagonal first, then psp order */
+void oracle_crs_init(const pcfd_mesh_view* m, int* ia, int* ja) {
+  const int nn = m->nnode;
+  ia[0] = 0;
+  for (int i = 0; i < nn; i++) ia[i + 1] = ia[i] + (m->ipsp[i + 1] - m->ipsp[i]) + 1;
+  for (int i = 0; i < nn; i++) {
+    int c = ia[i];
+    ja[c++] = i;
+    for (int k = m->ipsp[i]; k < m->ipsp[i + 1]; k++) ja[c++] = m->psp[k];
+  }
+}
+
+/* CRSMatrix::GetIndex, ucs/crsmatrix.tcc:740 (linear row search) */
+static int crs_index(const int* ia, const int* ja, int row, int col) {
+  if (row == col) return ia[row];
+  for (int k = ia[row] + 1; k < ia[row + 1]; k++)
+    if (ja[k] == col) return k;
+  return -1;
+}
+
+static void numflux(const double* QL, const double* QR, const double* avec, double gamma, double* f) {
+  oracle_roe_flux(QL, QR, avec, 0.0, gamma, f);
+  kneecap(f);
+}
+
+/* CompressibleEqnSet::ViscousJacobian, ucs/compressible.tcc:1633 */
+static void viscous_jacobian(const pcfd_params* prm, const double* QL, const double* QR, const double* dx, double s2,
+                             const double* avec, double* aL, double* aR) {
+  double Qavg[NVARS];
+  for (int i = 0; i < NEQN; i++) Qavg[i] = 0.5 * (QL[i] + QR[i]);
+  oracle_aux(prm->gamma, Qavg);
+  double mu = viscosity(prm, Qavg);
+  double tmut = mu;
+  double ReTilde = prm->Re / prm->mach;
+  double RK = avec[3] / ReTilde;
+  double RKT = RK * tmut;
+  double rhoL = QL[0], uL = QL[1] / rhoL, vL = QL[2] / rhoL, wL = QL[3] / rhoL, PL = QL[6];
+  double rhoR = QR[0], uR = QR[1] / rhoR, vR = QR[2] / rhoR, wR = QR[3] / rhoR, PR = QR[6];
+  double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+  double DxL[3], DxR[3];
+  for (int i = 0; i < 3; i++) {
+    DxL[i] = -dx[i] / (rhoL * s2);
+    DxR[i] = dx[i] / (rhoR * s2);
+  }
+  double c43 = 4.0 / 3.0, mc23 = -2.0 / 3.0;
+  double gamma = prm->gamma, gm1 = gamma - 1.0;
+  double cp = 1.0 / gm1;
+  double k = mu / prm->Pr * cp;
+  double c1 = -(k + 0.0);
+  for (int side = 1; side >= 0; side--) {
+    const double* D = side ? DxR : DxL;
+    double* A = side ? aR : aL;
+    double rho = side ? rhoR : rhoL, P = side ? PR : PL;
+    double us = side ? uR : uL, vs = side ? vR : vL, ws = side ? wR : wL;
+    double dux = -u * D[0], duy = -u * D[1], duz = -u * D[2];
+    double dvx = -v * D[0], dvy = -v * D[1], dvz = -v * D[2];
+    double dwx = -w * D[0], dwy = -w * D[1], dwz = -w * D[2];
+    double dfact = -2.0 / 3.0 * (dux + dvy + dwz);
+    double dtxx = (2.0 * dux + dfact), dtyy = (2.0 * dvy + dfact), dtzz = (2.0 * dwz + dfact);
+    double dtxy = duy + dvx, dtxz = duz + dwx, dtyz = dvz + dwy;
+    double dtxn = dtxx * avec[0] + dtxy * avec[1] + dtxz * avec[2];
+    double dtyn = dtxy * avec[0] + dtyy * avec[1] + dtyz * avec[2];
+    double dtzn = dtxz * avec[0] + dtyz * avec[1] + dtzz * avec[2];
+    double r2u = (c43 * D[0] * avec[0] + D[1] * avec[1] + D[2] * avec[2]);
+    double r2v = (mc23 * D[1] * avec[0] + D[0] * avec[1]);
+    double r2w = (mc23 * D[2] * avec[0] + D[0] * avec[2]);
+    double r3u = (mc23 * D[0] * avec[1] + D[1] * avec[0]);
+    double r3v = (D[0] * avec[0] + c43 * D[1] * avec[1] + D[2] * avec[2]);
+    double r3w = (mc23 * D[2] * avec[1] + D[1] * avec[2]);
+    double r4u = (mc23 * D[0] * avec[2] + D[2] * avec[0]);
+    double r4v = (mc23 * D[1] * avec[2] + D[2] * avec[1]);
+    double r4w = (D[0] * avec[0] + D[1] * avec[1] + c43 * D[2] * avec[2]);
+    A[0] = A[1] = A[2] = A[3] = A[4] = 0.0;
+    A[5] = -RKT * (dtxn); A[6] = -RKT * r2u; A[7] = -RKT * r2v; A[8] = -RKT * r2w; A[9] = 0.0;
+    A[10] = -RKT * (dtyn); A[11] = -RKT * r3u; A[12] = -RKT * r3v; A[13] = -RKT * r3w; A[14] = 0.0;
+    A[15] = -RKT * (dtzn); A[16] = -RKT * r4u; A[17] = -RKT * r4v; A[18] = -RKT * r4w; A[19] = 0.0;
+    double v2 = (us * us + vs * vs + ws * ws);
+    double dT_dP = gamma / rho;
+    double dP_dr = +gm1 * 0.5 * v2, dP_dru = -gm1 * us, dP_drv = -gm1 * vs, dP_drw = -gm1 * ws, dP_dret = +gm1;
+    double Tn = (D[0] * avec[0] + D[1] * avec[1] + D[2] * avec[2]) * dT_dP * c1;
+    A[20] = -RKT * (dtxn * u + dtyn * v + dtzn * w) + RK * Tn * (dP_dr - P / rho);
+    A[21] = -RKT * (r2u * u + r3u * v + r4u * w) + RK * Tn * dP_dru;
+    A[22] = -RKT * (r2v * u + r3v * v + r4v * w) + RK * Tn * dP_drv;
+    A[23] = -RKT * (r2w * u + r3w * v + r4w * w) + RK * Tn * dP_drw;
+    A[24] = RK * Tn * dP_dret;
+  }
+  for (int i = 0; i < 25; i++) aL[i] = -aL[i];
+}
+
+/* One half-edge of CalculateBoundaryVariables on (QL, QR) in place */
+static int apply_bc_one(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* Qinf, int eid,
+                        double* QL, double* QR) {
+  const double* avec = &m->bedge_area[4 * eid];
+  int bct = bc_of(prm, m->bfactag[eid]);
+  const double gamma = prm->gamma;
+  switch (bct) {
+    case PCFD_BC_SONIC_INFLOW:
+    case PCFD_BC_DIRICHLET:
+      for (int i = 0; i < NVARS; i++) QR[i] = QL[i] = Qinf[i];
+      break;
+    case PCFD_BC_SONIC_OUTFLOW:
+    case PCFD_BC_NEUMANN:
+      for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
+      break;
+    case PCFD_BC_FARFIELD:
+      bc_farfield(gamma, QL, QR, Qinf, avec, 0.0);
+      break;
+    case PCFD_BC_IMPERMEABLE_WALL:
+    case PCFD_BC_SYMMETRY:
+      bc_inviscid_wall(gamma, prm->no_cvbc, QL, QR, avec, 0.0);
+      break;
+    case PCFD_BC_NOSLIP: {
+      int nn = oracle_normal_node(m, m->bedges[2 * eid], avec);
+      double nQ[NVARS];
+      memcpy(nQ, &q[(size_t)nn * NVARS], sizeof(nQ));
+      double Tw = prm->bc_twall[m->bfactag[eid]] / prm->ref_temperature;
+      bc_viscous_wall(gamma, QL, QR, nQ, Tw);
+      break;
+    }
+    default:
+      return -1;
+  }
+  oracle_aux(gamma, QR);
+  oracle_aux(gamma, QL);
+  return 0;
+}
+
+/* LU in place of every diagonal block (PrepareSGS, ucs/crsmatrix.tcc:840) */
+void oracle_prepare_sgs(int nnode, const int* ia, double* M, int* pv) {
+  for (int i = 0; i < nnode; i++) oracle_lu(&M[(size_t)ia[i] * 25], &pv[(size_t)i * 5], 5);
+}
+
+/* ComputeJacobians (ucs/jacobian.tcc:13) for the ideal gas, steady:
+ * Kernel_NumJac, Bkernel_NumJac (jacobianBoundaryEval = 0, which applies the
+ * boundary conditions to the stored state as it goes), Kernel_Viscous_Jac,
+ * Kernel_Diag_NumJac, ContributeTemporalTerms with dt, then the no-slip row
+ * changes.  M [nblocks][25] in the reference layout; q is modified as the
+ * reference modifies it. */
+int oracle_jacobian(const pcfd_mesh_view* m, const pcfd_params* prm, double* q, const double* dt, const int* ia,
+                    const int* ja, double* M) {
+  const int nn = m->nnode;
+  const double gamma = prm->gamma;
+  const double h = 1.0e-8;
+  memset(M, 0, sizeof(double) * (size_t)ia[nn] * 25);
+  double Qinf[NVARS];
+  oracle_qinf(prm, Qinf);
+  /* Kernel_NumJac, :254 */
+  for (int e = 0; e < m->nedge; e++) {
+    int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+    const double* avec = &m->edge_area[4 * e];
+    const double* QL = &q[(size_t)a * NVARS];
+    const double* QR = &q[(size_t)b * NVARS];
+    double fS[NEQN], fL[NEQN], fR[NEQN], QPL[NVARS], QPR[NVARS], tL[25], tR[25];
+    numflux(QL, QR, avec, gamma, fS);
+    for (int i = 0; i < NEQN; i++) {
+      memcpy(QPL, QL, sizeof(QPL));
+      memcpy(QPR, QR, sizeof(QPR));
+      QPL[i] += h;
+      QPR[i] += h;
+      oracle_aux(gamma, QPL);
+      oracle_aux(gamma, QPR);
+      numflux(QPL, QR, avec, gamma, fL);
+      numflux(QL, QPR, avec, gamma, fR);
+      for (int j = 0; j < NEQN; j++) tL[j * NEQN + i] = (fS[j] - fL[j]) / h;
+      for (int j = 0; j < NEQN; j++) tR[j * NEQN + i] = (fR[j] - fS[j]) / h;
+    }
+    double* pR = &M[(size_t)crs_index(ia, ja, a, b) * 25];
+    double* pL = &M[(size_t)crs_index(ia, ja, b, a) * 25];
+    for (int t = 0; t < 25; t++) pR[t] += tR[t];
+    for (int t = 0; t < 25; t++) pL[t] += tL[t];
+  }
+  /* Bkernel_NumJac, :459 */
+  for (int eid = 0; eid < m->nbedge; eid++) {
+    int a = m->bedges[2 * eid], b = m->bedges[2 * eid + 1];
+    const double* avec = &m->bedge_area[4 * eid];
+    double* QL = &q[(size_t)a * NVARS];
+    double* QR = &q[(size_t)b * NVARS];
+    if (apply_bc_one(m, prm, q, Qinf, eid, QL, QR)) return -1;
+    double fS[NEQN], fL[NEQN], QPL[NVARS], QPR[NVARS], tL[25];
+    const int beval = prm->jac_boundary_eval;
+    if (beval == 3) {
+      /* build extension: base state through the same boundary map */
+      double QBL[NVARS], QBR[NVARS];
+      memcpy(QBL, QL, sizeof(QBL));
+      memcpy(QBR, QR, sizeof(QBR));
+      apply_bc_one(m, prm, q, Qinf, eid, QBL, QBR);
+      numflux(QBL, QBR, avec, gamma, fS);
+    } else {
+      numflux(QL, QR, avec, gamma, fS);
+    }
+    for (int i = 0; i < NEQN; i++) {
+      memcpy(QPL, QL, sizeof(QPL));
+      memcpy(QPR, QR, sizeof(QPR));
+      QPL[i] += h;
+      QPR[i] += h;
+      oracle_aux(gamma, QPL);
+      oracle_aux(gamma, QPR);
+      if (beval != 1) {
+        memcpy(QPR, QR, sizeof(QPR));
+        oracle_aux(gamma, QPR);
+        apply_bc_one(m, prm, q, Qinf, eid, QPL, QPR);
+        numflux(QPL, QPR, avec, gamma, fL);
+      } else {
+        numflux(QPL, QR, avec, gamma, fL);
+      }
+      for (int j = 0; j < NEQN; j++) tL[j * NEQN + i] = (fL[j] - fS[j]) / h;
+    }
+    double* d = &M[(size_t)ia[a] * 25];
+    for (int t = 0; t < 25; t++) d[t] += tL[t];
+  }
+  /* Kernel_Viscous_Jac, :734 */
+  if (prm->viscous) {
+    for (int e = 0; e < m->nedge; e++) {
+      int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+      const double* xL = &m->xyz[3 * a];
+      const double* xR = &m->xyz[3 * b];
+      double dx[3], s2 = 0.0, aL[25], aR[25];
+      for (int i = 0; i < 3; i++) { dx[i] = (xR[i] - xL[i]); s2 += dx[i] * dx[i]; }
+      viscous_jacobian(prm, &q[(size_t)a * NVARS], &q[(size_t)b * NVARS], dx, s2, &m->edge_area[4 * e], aL, aR);
+      double* pR = &M[(size_t)crs_index(ia, ja, a, b) * 25];
+      double* pL = &M[(size_t)crs_index(ia, ja, b, a) * 25];
+      for (int t = 0; t < 25; t++) pR[t] += aR[t];
+      for (int t = 0; t < 25; t++) pL[t] += aL[t];
+    }
+  }
+  /* Kernel_Diag_NumJac, :437 */
+  for (int e = 0; e < m->nedge; e++) {
+    int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+    const double* jacL = &M[(size_t)crs_index(ia, ja, b, a) * 25];
+    const double* jacR = &M[(size_t)crs_index(ia, ja, a, b) * 25];
+    double* dR = &M[(size_t)ia[b] * 25];
+    double* dL = &M[(size_t)ia[a] * 25];
+    for (int t = 0; t < 25; t++) dR[t] += -jacR[t];
+    for (int t = 0; t < 25; t++) dL[t] += -jacL[t];
+  }
+  /* ContributeTemporalTerms, ucs/jacobian.tcc:214 -> ucs/eqnset.tcc:195 */
+  for (int i = 0; i < nn; i++) {
+    double* d = &M[(size_t)ia[i] * 25];
+    for (int r = 0; r < NEQN; r++) d[r * NEQN + r] += 1.0 * m->vol[i] / dt[i];
+  }
+  /* Bkernel_BC_Jac_Modify -> ModifyViscousWallJacobian */
+  for (int eid = 0; eid < m->nbedge; eid++) {
+    if (bc_of(prm, m->bfactag[eid]) != PCFD_BC_NOSLIP) continue;
+    int a = m->bedges[2 * eid];
+    double Tw = prm->bc_twall[m->bfactag[eid]] / prm->ref_temperature;
+    int rows[5], nr = 0;
+    rows[nr++] = 1; rows[nr++] = 2; rows[nr++] = 3;
+    if (Tw < 0.0) { rows[nr++] = 0; rows[nr++] = 4; }
+    else rows[nr++] = 4;
+    for (int rr = 0; rr < nr; rr++) {
+      int sr = rows[rr];
+      for (int k = ia[a]; k < ia[a + 1]; k++)
+        for (int c = 0; c < NEQN; c++) M[(size_t)k * 25 + sr * NEQN + c] = 0.0;
+      M[(size_t)ia[a] * 25 + sr * NEQN + sr] = 1.0;
+    }
+    if (Tw < 0.0) {
+      int nnrm = oracle_normal_node(m, a, &m->bedge_area[4 * eid]);
+      double* off = &M[(size_t)crs_index(ia, ja, a, nnrm) * 25];
+      off[0] = -1.0;
+      off[24] = -1.0;
+    } else {
+      M[(size_t)ia[a] * 25 + 4 * NEQN + 0] = -(Tw / (gamma * (gamma - 1.0)) + 0.5 * 0.0);
+    }
+  }
+  return 0;
+}
+
+/* One block Gauss-Seidel row update (the body of the loops in CRS::SGS) */
+static void sgs_row(int node, const int* ia, const int* ja, const double* M, const int* pv, const double* b,
+                    double* x) {
+  double rhs[NEQN], vout[NEQN], tmp[NEQN];
+  memcpy(rhs, &b[(size_t)node * NEQN], sizeof(rhs));
+  for (int k = ia[node] + 1; k < ia[node + 1]; k++) {
+    oracle_matvec(&M[(size_t)k * 25], &x[(size_t)ja[k] * NEQN], vout, NEQN);
+    for (int c = 0; c < NEQN; c++) rhs[c] -= vout[c];
+  }
+  oracle_lusolve(&M[(size_t)ia[node] * 25], rhs, &pv[(size_t)node * NEQN], tmp, NEQN);
+  memcpy(&x[(size_t)node * NEQN], rhs, sizeof(rhs));
+}
+
+/* CRS::SGS, ucs/crs.tcc:62: nSgs x (forward then backward lexicographic
+ * sweeps); M's diagonal must hold its LU (oracle_prepare_sgs).  Returns
+ * |norm(x) after the last sweep - after the one before|. */
+double oracle_sgs(int nnode, const int* ia, const int* ja, const double* M, const int* pv, const double* b, double* x,
+                  int nsweeps) {
+  double xOld = 0.0, xNorm = 0.0;
+  for (int s = 0; s < nsweeps; s++) {
+    for (int i = 0; i < nnode; i++) sgs_row(i, ia, ja, M, pv, b, x);
+    for (int i = nnode - 1; i >= 0; i--) sgs_row(i, ia, ja, M, pv, b, x);
+    xOld = xNorm;
+    double t = 0.0;
+    for (size_t k = 0; k < (size_t)nnode * NEQN; k++) t += x[k] * x[k];
+    xNorm = sqrt(t) / (double)((size_t)nnode * NEQN);
+  }
+  return fabs(xOld - xNorm);
+}
+
+/* The same sweeps over rows grouped by colour (rows[cptr[c]..cptr[c+1]]),
+ * colours forward then backward: the order the GPU uses.  Test helper. */
+void oracle_sgs_colored(int nnode, const int* ia, const int* ja, const double* M, const int* pv, const double* b,
+                        double* x, int nsweeps, int ncolor, const int* cptr, const int* rows) {
+  (void)nnode;
+  for (int s = 0; s < nsweeps; s++) {
+    for (int c = 0; c < ncolor; c++)
+      for (int k = cptr[c]; k < cptr[c + 1]; k++) sgs_row(rows[k], ia, ja, M, pv, b, x);
+    for (int c = ncolor - 1; c >= 0; c--)
+      for (int k = cptr[c]; k < cptr[c + 1]; k++) sgs_row(rows[k], ia, ja, M, pv, b, x);
+  }
+}
+
+/* NaN/Inf update zeroing and CompressibleEqnSet::ApplyDQ
+ * (ucs/solutionSpace.tcc:774-804, ucs/compressible.tcc:929); returns the
+ * update norm sqrt(sum x^2)/(nnode*5). */
+double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* x, double* q) {
+  const int nn = m->nnode;
+  const double gm1 = prm->gamma - 1.0;
+  for (int j = 0; j < nn; j++) {
+    int zero = 0;
+    for (int k = 0; k < NEQN; k++)
+      if (isnan(x[(size_t)j * NEQN + k]) || isinf(x[(size_t)j * NEQN + k])) { x[(size_t)j * NEQN + k] = 0.0; zero = 1; }
+    if (zero)
+      for (int k = 0; k < NEQN; k++) x[(size_t)j * NEQN + k] = 0.0;
+  }
+  for (int j = 0; j < nn; j++) {
+    double* dQ = &x[(size_t)j * NEQN];
+    double* Q = &q[(size_t)j * NVARS];
+    double minP = 1.0e-10, minRho = 1.0e-10, minE = 1.0e-10;
+    if (Q[0] + dQ[0] < 0.0) Q[0] = minRho; else Q[0] += dQ[0];
+    if (Q[4] + dQ[4] < 0.0) Q[4] = minE; else Q[4] += dQ[4];
+    double rho = Q[0], u = Q[1] / rho, v = Q[2] / rho, w = Q[3] / rho, E = Q[4];
+    double v2 = u * u + v * v + w * w;
+    if (E < 0.5 * rho * v2) {
+      double v2mod = 2.0 * (E - minP / gm1);
+      double frac = 0.0;
+      if (v2mod > 0.0) frac = sqrt(v2mod / v2);
+      u *= frac; v *= frac; w *= frac;
+      Q[1] = rho * u; Q[2] = rho * v; Q[3] = rho * w;
+    } else {
+      Q[1] += dQ[1]; Q[2] += dQ[2]; Q[3] += dQ[3];
+    }
+    oracle_aux(prm->gamma, Q);
+  }
+  double t = 0.0;
+  for (size_t k = 0; k < (size_t)nn * NEQN; k++) t += x[k] * x[k];
+  return sqrt(t) / (double)((size_t)nn * NEQN);
+}

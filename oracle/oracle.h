@@ -33,6 +33,17 @@ void oracle_lusolve(const double* a, double* b, const int* p, double* x, int n);
 void oracle_tri_area(const double* p1, const double* p2, const double* p3, double* r);
 double oracle_tet_vol(const double* p1, const double* p2, const double* p3, const double* p4);
 
+double oracle_timestep(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, double cfl, double* dt);
+void oracle_crs_init(const pcfd_mesh_view* m, int* ia, int* ja);
+void oracle_prepare_sgs(int nnode, const int* ia, double* M, int* pv);
+int oracle_jacobian(const pcfd_mesh_view* m, const pcfd_params* prm, double* q, const double* dt, const int* ia,
+                    const int* ja, double* M);
+double oracle_sgs(int nnode, const int* ia, const int* ja, const double* M, const int* pv, const double* b, double* x,
+                  int nsweeps);
+void oracle_sgs_colored(int nnode, const int* ia, const int* ja, const double* M, const int* pv, const double* b,
+                        double* x, int nsweeps, int ncolor, const int* cptr, const int* rows);
+double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* x, double* q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,8 +54,23 @@ class Params(C.Structure):
         ("gamma", C.c_double), ("mach", C.c_double), ("flowdir", C.c_double * 3),
         ("Re", C.c_double), ("Pr", C.c_double), ("PrT", C.c_double), ("ref_temperature", C.c_double),
         ("sorder", C.c_int), ("chi", C.c_double), ("viscous", C.c_int), ("limiter", C.c_int),
-        ("venkat_K", C.c_double), ("no_cvbc", C.c_int), ("ntags", C.c_int),
+        ("venkat_K", C.c_double), ("no_cvbc", C.c_int), ("jac_boundary_eval", C.c_int), ("ntags", C.c_int),
         ("bc_type", C.POINTER(C.c_int)), ("bc_twall", C.POINTER(C.c_double)),
+    ]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [
+        ("iter", C.c_int), ("cfl", C.c_double), ("cfl_start", C.c_double), ("cfl_ramp_steps", C.c_int),
+        ("nsgs", C.c_int), ("jac_update_freq", C.c_int), ("jac_precision", C.c_int), ("linear_solver", C.c_int),
+        ("fgmres_m", C.c_int), ("fgmres_restarts", C.c_int), ("fgmres_rtol", C.c_double),
+    ]
+
+
+class NewtonReport(C.Structure):
+    _fields_ = [
+        ("res", C.c_double * 6), ("dqnorm", C.c_double), ("dtmin", C.c_double), ("lin_res", C.c_double),
+        ("lin_iters", C.c_int), ("cfl", C.c_double),
     ]
 
 
@@ -86,6 +101,16 @@ PROTOTYPES = {
     "pcfd_residual": (C.c_int, [_P, _DP, _DP]),
     "pcfd_residual_full": (C.c_int, [_P, _DP]),
     "pcfd_bench_residual_full": (C.c_int, [_P, C.c_int, _DP, _DP]),
+    "pcfd_timestep": (C.c_int, [_P, C.c_double, _DP, _DP]),
+    "pcfd_set_jacobian_precision": (C.c_int, [_P, C.c_int]),
+    "pcfd_jacobian": (C.c_int, [_P]),
+    "pcfd_get_jacobian": (C.c_int, [_P, _DP, C.c_longlong]),
+    "pcfd_nblocks": (C.c_longlong, [_P]),
+    "pcfd_crs_structure": (C.c_int, [_P, _IP, _IP, _IP]),
+    "pcfd_sgs": (C.c_int, [_P, C.c_int, _DP, _DP]),
+    "pcfd_coloring": (C.c_int, [_P, _IP, _IP]),
+    "pcfd_apply_dq": (C.c_int, [_P, _DP, _DP]),
+    "pcfd_newton_step": (C.c_int, [_P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
     "pcfd_set_device": (C.c_int, [C.c_int]),
     "pcfd_device_sync": (C.c_int, []),
     "pcfd_profile_enable": (C.c_int, [_P, C.c_int]),

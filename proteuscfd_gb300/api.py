@@ -13,6 +13,13 @@ this module                            reference (ngcurrier/ProteusCFD)
 ``SolutionSpace.gradient``             ``Gradient<T>::Compute`` (ucs/gradient.tcc:57)
 ``SolutionSpace.limiter``              ``Limiter<T>::Compute`` (ucs/limiters.tcc:53)
 ``SolutionSpace.compute_residuals``    ``ComputeResiduals`` (ucs/residual.tcc:13)
+``SolutionSpace.compute_timesteps``    ``ComputeTimesteps`` (ucs/timestep.tcc:7)
+``SolutionSpace.compute_jacobians``    ``ComputeJacobians`` (ucs/jacobian.tcc:13)
+``SolutionSpace.sgs``                  ``CRS::SGS`` (ucs/crs.tcc:62)
+``SolutionSpace.apply_dq``             ``CompressibleEqnSet::ApplyDQ`` (ucs/compressible.tcc:929)
+``SolutionSpace.newton_iterate``       ``PreTimeAdvance`` + ``NewtonIterate``
+                                       (ucs/solutionSpace.tcc:573,640)
+``solve``                              ``Solve`` (ucs/solve.tcc:24)
 =====================================  =====================================================
 
 Errors raise ``PcfdError`` (the reference aborts through ``Abort <<``,
@@ -162,6 +169,7 @@ class Param:
     limiter: int = 0
     venkat_K: float = 1.0
     no_cvbc: int = 0
+    jac_boundary_eval: int = 0
     bc_type: dict = field(default_factory=dict)   # factag -> BC type
     bc_twall: dict = field(default_factory=dict)  # factag -> wall temperature [K] (<0 adiabatic)
 
@@ -179,6 +187,7 @@ class Param:
         p.Re, p.Pr, p.PrT, p.ref_temperature = self.Re, self.Pr, self.PrT, self.ref_temperature
         p.sorder, p.chi, p.viscous, p.limiter = self.sorder, self.chi, self.viscous, self.limiter
         p.venkat_K, p.no_cvbc, p.ntags = self.venkat_K, self.no_cvbc, ntags
+        p.jac_boundary_eval = self.jac_boundary_eval
         p.bc_type = N.iptr(bct)
         p.bc_twall = N.dptr(btw)
         p._keep = (bct, btw)
@@ -258,6 +267,64 @@ class SolutionSpace:
                 "pcfd_bench_residual_full")
         return ms.value, norms
 
+    def compute_timesteps(self, cfl):
+        dt = np.empty(self.mesh.nnode, dtype=np.float64)
+        dtmin = C.c_double()
+        N.check(self._lib.pcfd_timestep(self._h, float(cfl), N.dptr(dt), C.byref(dtmin)), "pcfd_timestep")
+        return dt, dtmin.value
+
+    def set_jacobian_precision(self, prec):
+        """0 FP64, 1 FP32, 2 BF16 storage of the off-diagonal blocks."""
+        N.check(self._lib.pcfd_set_jacobian_precision(self._h, int(prec)), "pcfd_set_jacobian_precision")
+
+    def compute_jacobians(self):
+        N.check(self._lib.pcfd_jacobian(self._h), "pcfd_jacobian")
+
+    def nblocks(self):
+        return int(self._lib.pcfd_nblocks(self._h))
+
+    def get_jacobian(self):
+        nb = self.nblocks()
+        M = np.empty((nb, 25), dtype=np.float64)
+        N.check(self._lib.pcfd_get_jacobian(self._h, N.dptr(M), nb), "pcfd_get_jacobian")
+        return M
+
+    def crs_structure(self):
+        ia = np.empty(self.mesh.nnode + 1, dtype=np.int32)
+        ja = np.empty(self.nblocks(), dtype=np.int32)
+        nc = C.c_int()
+        N.check(self._lib.pcfd_crs_structure(self._h, N.iptr(ia), N.iptr(ja), C.byref(nc)), "pcfd_crs_structure")
+        return ia, ja, nc.value
+
+    def coloring(self):
+        _, _, nc = self.crs_structure()
+        cptr = np.empty(nc + 1, dtype=np.int32)
+        rows = np.empty(self.mesh.nnode, dtype=np.int32)
+        N.check(self._lib.pcfd_coloring(self._h, N.iptr(cptr), N.iptr(rows)), "pcfd_coloring")
+        return cptr, rows
+
+    def sgs(self, nsweeps):
+        x = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        dn = C.c_double()
+        N.check(self._lib.pcfd_sgs(self._h, int(nsweeps), N.dptr(x), C.byref(dn)), "pcfd_sgs")
+        return x, dn.value
+
+    def apply_dq(self, x=None):
+        dn = C.c_double()
+        xp = N.dptr(np.ascontiguousarray(x, dtype=np.float64)) if x is not None else None
+        N.check(self._lib.pcfd_apply_dq(self._h, xp, C.byref(dn)), "pcfd_apply_dq")
+        return dn.value
+
+    def newton_iterate(self, it, cfl=5.0, nsgs=10, cfl_start=0.0, cfl_ramp_steps=0, jac_precision=0,
+                       linear_solver=0, fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-2, jac_update_freq=1):
+        o = N.NewtonOpts(int(it), float(cfl), float(cfl_start), int(cfl_ramp_steps), int(nsgs), int(jac_update_freq),
+                         int(jac_precision), int(linear_solver), int(fgmres_m), int(fgmres_restarts),
+                         float(fgmres_rtol))
+        r = N.NewtonReport()
+        N.check(self._lib.pcfd_newton_step(self._h, C.byref(o), C.byref(r)), "pcfd_newton_step")
+        return {"res": list(r.res), "dqnorm": r.dqnorm, "dtmin": r.dtmin, "lin_res": r.lin_res,
+                "lin_iters": r.lin_iters, "cfl": r.cfl}
+
     def health(self):
         c = (C.c_longlong * 8)()
         N.check(self._lib.pcfd_get_health(self._h, c), "pcfd_get_health")
@@ -283,3 +350,20 @@ class SolutionSpace:
 
     def launch_count(self):
         return int(self._lib.pcfd_launch_count(self._h))
+
+
+def solve(space: SolutionSpace, nsteps: int, drop: float = 0.0, **opts):
+    """Outer iterations (``Solve``, ucs/solve.tcc:24).  Runs ``nsteps``
+    iterations, or stops early once resGlobal has dropped by ``drop``
+    relative to the first iteration (the reference itself never stops
+    early).  Returns the per-iteration reports."""
+    hist = []
+    r0 = None
+    for it in range(1, nsteps + 1):
+        rep = space.newton_iterate(it, **opts)
+        hist.append(rep)
+        if r0 is None:
+            r0 = rep["res"][0]
+        if drop > 0.0 and r0 > 0.0 and rep["res"][0] <= drop * r0:
+            break
+    return hist

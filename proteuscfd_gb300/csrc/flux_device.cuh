@@ -20,15 +20,21 @@ __device__ __forceinline__ double entropy_fix(double eig, double eigL, double ei
   double eps = dmax(eig - eigL, eigR - eig);
   eps = dmax(0.0, eps);
   double a = fabs(eig);
-  return (a < eps) ? 0.5 * (eig * eig / eps + eps) : a;
+  if (a < eps) a = 0.5 * (eig * eig / eps + eps);
+  return a;
 }
 
 // Roe flux with the reference's eigen-decomposition: RoeVariables (:533),
 // Eigensystem (:580), entropy fix, |A| dQ = T |L| Tinv dQ, and
 // 0.5 area (F_L + F_R - |A| dQ) (RoeFlux, :93).  avec = (nx, ny, nz, area);
 // static grid (vdotn = 0).
-__device__ __forceinline__ void roe_flux(const double* QL, const double* QR, const double nx, const double ny,
-                                         const double nz, const double area, const double gamma, double* flux) {
+// Returns a mask of non-physical states in the sense of BadExtrapolation
+// (ucs/compressible.tcc:1056: p < 1e-10, rho < 0 or rho E < 1e-10):
+// bit 0 = left state, bit 1 = right state, bit 2 = Roe-averaged state.  The
+// limiter's pressure clip (ucs/limiters.tcc:737) applies exactly these
+// three tests to the same extrapolated states.
+__device__ __forceinline__ int roe_flux(const double* QL, const double* QR, const double nx, const double ny,
+                                        const double nz, const double area, const double gamma, double* flux) {
   const double gm1 = gamma - 1.0;
   const double rL = QL[0], irL = 1.0 / rL;
   const double uL = QL[1] * irL, vL = QL[2] * irL, wL = QL[3] * irL, EL = QL[4];
@@ -47,13 +53,13 @@ __device__ __forceinline__ void roe_flux(const double* QL, const double* QR, con
   const double w = wL + sigma * (wR - wL);
   const double h = hL + sigma * (hR - hL);
   double v2h = 0.5 * (u * u + v * v + w * w);
-  const double rE = rho / gamma * (h + gm1 * v2h);
+  const double rE = rho * (1.0 / gamma) * (h + gm1 * v2h);
   const double irho = 1.0 / rho;
   const double P = gm1 * (rE - rho * v2h);
   const double c2 = gamma * P * irho;
   const double c = sqrt(c2);
   const double ic = 1.0 / c;
-  const double ic2 = 1.0 / c2;
+  const double ic2 = ic * ic;
   const double thetaf = u * nx + v * ny + w * nz;
 
   // entropy-fixed |eigenvalues|
@@ -85,7 +91,7 @@ __device__ __forceinline__ void roe_flux(const double* QL, const double* QR, con
 
   // dr = T dv (columns of the right eigenvector matrix)
   const double rc = rho * ic;
-  const double cg = c / gm1;
+  const double cg = c * (1.0 / gm1);
   const double dr0 = nx * dv0 + ny * dv1 + nz * dv2 + rc * dv3 + rc * dv4;
   const double dr1 = (u * nx) * dv0 + (u * ny - rho * nz) * dv1 + (u * nz + rho * ny) * dv2 +
                      rho * (u * ic + nx) * dv3 + rho * (u * ic - nx) * dv4;
@@ -105,6 +111,8 @@ __device__ __forceinline__ void roe_flux(const double* QL, const double* QR, con
   flux[2] = ha * ((vL * rtL + PL * ny) + (vR * rtR + PR * ny) - dr2);
   flux[3] = ha * ((wL * rtL + PL * nz) + (wR * rtR + PR * nz) - dr3);
   flux[4] = ha * (hL * rtL + hR * rtR - dr4);
+  return ((rL < 0.0 || EL < 1.0e-10 || PL < 1.0e-10) ? 1 : 0) | ((rR < 0.0 || ER < 1.0e-10 || PR < 1.0e-10) ? 2 : 0) |
+         ((P < 1.0e-10 || rE < 1.0e-10) ? 4 : 0);
 }
 
 // ComputeAuxiliaryVariables (ucs/compressible.tcc:1230) on a 10-wide record

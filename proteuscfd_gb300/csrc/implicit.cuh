@@ -1,0 +1,611 @@
+// Implicit part of the path on sm_103a: Jacobian assembly into device block
+// CRS, block LU of the diagonal, block Gauss-Seidel sweeps, the Newton
+// update and the local time step.  Included by solver.cu inside its
+// anonymous namespace (it uses the Solver state and the residual kernels).
+//
+// Block CRS layout: the reference's (CRSMatrix::Init, ucs/crsmatrix.tcc:48):
+// row i = diagonal block first, then its psp neighbours in psp order; blocks
+// are 5x5 row-major.  Off-diagonal blocks are stored in the Jacobian
+// precision T (double, float or bfloat16); the diagonal is kept in FP64 in a
+// separate array, before (d_diag) and after (d_dlu + pivots) its LU.
+#pragma once
+
+// (cuda_bf16.h is included by solver.cu at file scope)
+
+template <class T>
+__device__ __forceinline__ T to_store(double v);
+template <>
+__device__ __forceinline__ double to_store<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float to_store<float>(double v) { return (float)v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_store<__nv_bfloat16>(double v) { return __double2bfloat16(v); }
+
+__device__ __forceinline__ double ld_blk(const double* p) { return *p; }
+__device__ __forceinline__ double ld_blk(const float* p) { return (double)*p; }
+__device__ __forceinline__ double ld_blk(const __nv_bfloat16* p) { return (double)__bfloat162float(*p); }
+__device__ __forceinline__ float ld_blkf(const double* p) { return (float)*p; }
+__device__ __forceinline__ float ld_blkf(const float* p) { return *p; }
+__device__ __forceinline__ float ld_blkf(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+// NumericalFlux with the NaN kneecap (ucs/eqnset.tcc:55-90), Roe flux
+__device__ __forceinline__ void numflux(const double* QL, const double* QR, const D4& a, double gamma, double* f,
+                                        unsigned long long* health) {
+  roe_flux(QL, QR, a.x, a.y, a.z, a.w, gamma, f);
+  if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
+}
+
+// CompressibleEqnSet::ViscousJacobian (ucs/compressible.tcc:1633), laminar.
+// QL/QR are the nodal 10-wide records (their stored pressure is used, as
+// GetPressure reads it); aL/aR are the left/right blocks with the sign the
+// reference scatters them with.
+__device__ void viscous_jacobian(const double* QL, const double* QR, const double* dx, double s2, const D4& a,
+                                 double gamma, double Pr, double inv_retilde, double S, double* aL, double* aR) {
+  double Q0 = 0.5 * (QL[0] + QR[0]), Q1 = 0.5 * (QL[1] + QR[1]), Q2 = 0.5 * (QL[2] + QR[2]),
+         Q3 = 0.5 * (QL[3] + QR[3]), Q4 = 0.5 * (QL[4] + QR[4]);
+  double gm1 = gamma - 1.0;
+  double iQ0 = 1.0 / Q0;
+  double ua = Q1 * iQ0, va = Q2 * iQ0, wa = Q3 * iQ0;
+  double Pa = gm1 * (Q4 - 0.5 * Q0 * (ua * ua + va * va + wa * wa));
+  double Ta = gamma * Pa * iQ0;
+  double mu = sutherland(Ta, S);
+  double RK = a.w * inv_retilde;
+  double RKT = RK * mu;
+  double rhoL = QL[0], uL = QL[1] / rhoL, vL = QL[2] / rhoL, wL = QL[3] / rhoL, PL = QL[6];
+  double rhoR = QR[0], uR = QR[1] / rhoR, vR = QR[2] / rhoR, wR = QR[3] / rhoR, PR = QR[6];
+  double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+  double DxL[3], DxR[3];
+  for (int i = 0; i < 3; i++) {
+    DxL[i] = -dx[i] / (rhoL * s2);
+    DxR[i] = dx[i] / (rhoR * s2);
+  }
+  const double c43 = 4.0 / 3.0, mc23 = -2.0 / 3.0;
+  double cp = 1.0 / gm1;
+  double c1 = -(mu / Pr * cp);
+  for (int side = 0; side < 2; side++) {
+    const double* D = side ? DxR : DxL;
+    double* A = side ? aR : aL;
+    double rho = side ? rhoR : rhoL, P = side ? PR : PL;
+    double us = side ? uR : uL, vs = side ? vR : vL, ws = side ? wR : wL;
+    double dux = -u * D[0], duy = -u * D[1], duz = -u * D[2];
+    double dvx = -v * D[0], dvy = -v * D[1], dvz = -v * D[2];
+    double dwx = -w * D[0], dwy = -w * D[1], dwz = -w * D[2];
+    double dfact = -2.0 / 3.0 * (dux + dvy + dwz);
+    double dtxx = (2.0 * dux + dfact), dtyy = (2.0 * dvy + dfact), dtzz = (2.0 * dwz + dfact);
+    double dtxy = duy + dvx, dtxz = duz + dwx, dtyz = dvz + dwy;
+    double dtxn = dtxx * a.x + dtxy * a.y + dtxz * a.z;
+    double dtyn = dtxy * a.x + dtyy * a.y + dtyz * a.z;
+    double dtzn = dtxz * a.x + dtyz * a.y + dtzz * a.z;
+    double r2u = (c43 * D[0] * a.x + D[1] * a.y + D[2] * a.z);
+    double r2v = (mc23 * D[1] * a.x + D[0] * a.y);
+    double r2w = (mc23 * D[2] * a.x + D[0] * a.z);
+    double r3u = (mc23 * D[0] * a.y + D[1] * a.x);
+    double r3v = (D[0] * a.x + c43 * D[1] * a.y + D[2] * a.z);
+    double r3w = (mc23 * D[2] * a.y + D[1] * a.z);
+    double r4u = (mc23 * D[0] * a.z + D[2] * a.x);
+    double r4v = (mc23 * D[1] * a.z + D[2] * a.y);
+    double r4w = (D[0] * a.x + D[1] * a.y + c43 * D[2] * a.z);
+    A[0] = A[1] = A[2] = A[3] = A[4] = 0.0;
+    A[5] = -RKT * dtxn; A[6] = -RKT * r2u; A[7] = -RKT * r2v; A[8] = -RKT * r2w; A[9] = 0.0;
+    A[10] = -RKT * dtyn; A[11] = -RKT * r3u; A[12] = -RKT * r3v; A[13] = -RKT * r3w; A[14] = 0.0;
+    A[15] = -RKT * dtzn; A[16] = -RKT * r4u; A[17] = -RKT * r4v; A[18] = -RKT * r4w; A[19] = 0.0;
+    double v2 = (us * us + vs * vs + ws * ws);
+    double dT_dP = gamma / rho;
+    double dP_dr = +gm1 * 0.5 * v2, dP_dru = -gm1 * us, dP_drv = -gm1 * vs, dP_drw = -gm1 * ws, dP_dret = +gm1;
+    double Tn = (D[0] * a.x + D[1] * a.y + D[2] * a.z) * dT_dP * c1;
+    A[20] = -RKT * (dtxn * u + dtyn * v + dtzn * w) + RK * Tn * (dP_dr - P / rho);
+    A[21] = -RKT * (r2u * u + r3u * v + r4u * w) + RK * Tn * dP_dru;
+    A[22] = -RKT * (r2v * u + r3v * v + r4v * w) + RK * Tn * dP_drv;
+    A[23] = -RKT * (r2w * u + r3w * v + r4w * w) + RK * Tn * dP_drw;
+    A[24] = RK * Tn * dP_dret;
+  }
+  for (int i = 0; i < 25; i++) aL[i] = -aL[i];
+}
+
+struct JacConst {
+  double gamma, Pr, inv_retilde, S;
+  int viscous;
+};
+
+// Kernel_NumJac (ucs/jacobian.tcc:254): one-sided finite differences of the
+// Roe flux (h = 1e-8, 11 flux evaluations per edge) into A(R,L) and A(L,R),
+// plus Kernel_Viscous_Jac (:734) when viscous.
+template <class T>
+__global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restrict__ en, const D4* __restrict__ ea,
+                                                  const double* __restrict__ eh, const double* __restrict__ q,
+                                                  const int* __restrict__ pos_lr, const int* __restrict__ pos_rl,
+                                                  JacConst k, T* __restrict__ M, unsigned long long* health) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int2 n = en[e];
+  const D4 a = ea[e];
+  double QL[NVARS], QR[NVARS];
+#pragma unroll
+  for (int t = 0; t < NVARS; t++) { QL[t] = q[(size_t)n.x * NVARS + t]; QR[t] = q[(size_t)n.y * NVARS + t]; }
+  const double h = 1.0e-8;
+  const double ih = 1.0 / h;
+  double fS[NEQN];
+  numflux(QL, QR, a, k.gamma, fS, health);
+  double tL[25], tR[25];
+  for (int i = 0; i < NEQN; i++) {
+    double QP[NEQN], fP[NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) QP[t] = QL[t];
+    QP[i] += h;
+    numflux(QP, QR, a, k.gamma, fP, health);
+#pragma unroll
+    for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = (fS[j] - fP[j]) * ih;
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) QP[t] = QR[t];
+    QP[i] += h;
+    numflux(QL, QP, a, k.gamma, fP, health);
+#pragma unroll
+    for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = (fP[j] - fS[j]) * ih;
+  }
+  if (k.viscous) {
+    double dx[3] = {2.0 * eh[3 * (size_t)e], 2.0 * eh[3 * (size_t)e + 1], 2.0 * eh[3 * (size_t)e + 2]};
+    double s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    double vL[25], vR[25];
+    viscous_jacobian(QL, QR, dx, s2, a, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
+#pragma unroll
+    for (int t = 0; t < 25; t++) { tL[t] += vL[t]; tR[t] += vR[t]; }
+  }
+  T* bl = &M[(size_t)pos_rl[e] * 25];  // A(R, L)
+  T* br = &M[(size_t)pos_lr[e] * 25];  // A(L, R)
+#pragma unroll
+  for (int t = 0; t < 25; t++) { bl[t] = to_store<T>(tL[t]); br[t] = to_store<T>(tR[t]); }
+}
+
+// Bkernel_NumJac (ucs/jacobian.tcc:459) with jacobianBoundaryEval = 0: the
+// phantom state is re-derived from each perturbed interior state through
+// the boundary condition, and the difference quotient goes to the diagonal.
+// The state itself went through UpdateBCs just before (the reference applies
+// the boundary conditions to the stored state inside this kernel).
+__global__ void __launch_bounds__(128) k_jac_bedge(int nbedge, const int2* __restrict__ bn, const D4* __restrict__ ba,
+                                                   const int* __restrict__ bbc, const double* __restrict__ btw,
+                                                   const int* __restrict__ bnrm, BcConst bk, int beval,
+                                                   const double* __restrict__ q, double* __restrict__ bblk,
+                                                   unsigned long long* health) {
+  int he = blockIdx.x * blockDim.x + threadIdx.x;
+  if (he >= nbedge) return;
+  const int2 n = bn[he];
+  const D4 a = ba[he];
+  double QL[NVARS], QR[NVARS], nQ[NVARS];
+  for (int t = 0; t < NVARS; t++) { QL[t] = q[(size_t)n.x * NVARS + t]; QR[t] = q[(size_t)n.y * NVARS + t]; }
+  const int bct = bbc[he];
+  for (int t = 0; t < NVARS; t++) nQ[t] = 0.0;
+  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+    for (int t = 0; t < NVARS; t++) nQ[t] = q[(size_t)bnrm[he] * NVARS + t];
+  const double h = 1.0e-8;
+  const double ih = 1.0 / h;
+  double fS[NEQN];
+  if (beval == 3) {
+    // base state through the same boundary-condition map as the perturbed ones
+    double QBL[NVARS], QBR[NVARS];
+    for (int t = 0; t < NVARS; t++) { QBL[t] = QL[t]; QBR[t] = QR[t]; }
+    apply_bc(bk, bct, QBL, QBR, a, btw[he], nQ);
+    numflux(QBL, QBR, a, bk.gamma, fS, health);
+  } else {
+    numflux(QL, QR, a, bk.gamma, fS, health);
+  }
+  double* out = &bblk[(size_t)he * 25];
+  for (int i = 0; i < NEQN; i++) {
+    double QPL[NVARS], QPR[NVARS], fL[NEQN];
+    for (int t = 0; t < NVARS; t++) { QPL[t] = QL[t]; QPR[t] = QR[t]; }
+    QPL[i] += h;
+    aux_vars(bk.gamma, QPL);
+    aux_vars(bk.gamma, QPR);
+    if (beval != 1) apply_bc(bk, bct, QPL, QPR, a, btw[he], nQ);
+    numflux(QPL, QPR, a, bk.gamma, fL, health);
+    for (int j = 0; j < NEQN; j++) out[j * 5 + i] = (fL[j] - fS[j]) * ih;
+  }
+}
+
+// Diagonal blocks: boundary contributions in half-edge order, minus the
+// column of off-diagonal blocks in edge order (Kernel_Diag_NumJac,
+// ucs/jacobian.tcc:437), plus vol/dtau on the diagonal
+// (EqnSet::ContributeTemporalTerms, ucs/eqnset.tcc:195, steady: cnp1 = 1).
+template <class T>
+__global__ void __launch_bounds__(128) k_jac_diag(int nnode, const int* __restrict__ nptr, const int* __restrict__ nedg,
+                                                  const int* __restrict__ pos_lr, const int* __restrict__ pos_rl,
+                                                  const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                  const double* __restrict__ bblk, const T* __restrict__ M,
+                                                  const double* __restrict__ vol, const double* __restrict__ dt,
+                                                  double* __restrict__ diag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double D[25];
+#pragma unroll
+  for (int t = 0; t < 25; t++) D[t] = 0.0;
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    const double* B = &bblk[(size_t)bhe[p] * 25];
+#pragma unroll
+    for (int t = 0; t < 25; t++) D[t] += B[t];
+  }
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    int se = nedg[k];
+    // column block A(j, i): i is the left node -> A(R, L); else A(L, R)
+    const T* A = (se < 0) ? &M[(size_t)pos_rl[~se] * 25] : &M[(size_t)pos_lr[se] * 25];
+#pragma unroll
+    for (int t = 0; t < 25; t++) D[t] += -ld_blk(&A[t]);
+  }
+  double vd = 1.0 * vol[i] / dt[i];
+#pragma unroll
+  for (int r = 0; r < NEQN; r++) D[r * 5 + r] += vd;
+#pragma unroll
+  for (int t = 0; t < 25; t++) diag[(size_t)i * 25 + t] = D[t];
+}
+
+// LU (ucs/matrix.h:111) in place with row pivots, on a 5x5 block.
+__device__ __forceinline__ int lu5(double* a, int* p) {
+  int bad = 0, row = 0;
+  for (int i = 0; i < 5; i++) p[i] = i;
+  for (int i = 0; i < 5; i++) {
+    double large = 0.0;
+    for (int j = i; j < 5; j++)
+      if (fabs(a[p[j] * 5 + i]) > fabs(large)) { large = a[p[j] * 5 + i]; row = j; }
+    if (large == 0.0 || fabs(large) < 1.0e-15) bad = 1;
+    int t = p[i]; p[i] = p[row]; p[row] = t;
+    large = 1.0 / large;
+    for (int j = i + 1; j < 5; j++) a[p[j] * 5 + i] *= large;
+    for (int j = i + 1; j < 5; j++)
+      for (int kk = i + 1; kk < 5; kk++) a[p[j] * 5 + kk] -= a[p[j] * 5 + i] * a[p[i] * 5 + kk];
+  }
+  return bad;
+}
+
+// No-slip row modifications (Bkernel_BC_Jac_Modify, ucs/bc.tcc:748 ->
+// ModifyViscousWallJacobian, ucs/compressible.tcc:1577) on the node's own
+// row, then PrepareSGS's LU of the diagonal (ucs/crsmatrix.tcc:840).
+template <class T>
+__global__ void __launch_bounds__(128) k_jac_finish(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
+                                                    const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                    const int* __restrict__ bbc, const double* __restrict__ btw,
+                                                    const int* __restrict__ bnrm, double gamma, T* __restrict__ M,
+                                                    double* __restrict__ diag, double* __restrict__ dlu,
+                                                    int* __restrict__ piv, unsigned long long* health) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double D[25];
+#pragma unroll
+  for (int t = 0; t < 25; t++) D[t] = diag[(size_t)i * 25 + t];
+  bool mod = false;
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    int he = bhe[p];
+    if (bbc[he] != PCFD_BC_NOSLIP) continue;
+    mod = true;
+    double Tw = btw[he];
+    int rows[5];
+    int nr = 0;
+    rows[nr++] = 1; rows[nr++] = 2; rows[nr++] = 3;
+    if (Tw < 0.0) { rows[nr++] = 0; rows[nr++] = 4; }
+    else rows[nr++] = 4;
+    for (int rr = 0; rr < nr; rr++) {
+      int sr = rows[rr];
+      for (int b = ia[i] + 1; b < ia[i + 1]; b++)
+        for (int c = 0; c < 5; c++) M[(size_t)b * 25 + sr * 5 + c] = to_store<T>(0.0);
+      for (int c = 0; c < 5; c++) D[sr * 5 + c] = 0.0;
+      D[sr * 5 + sr] = 1.0;
+    }
+    if (Tw < 0.0) {
+      int nn = bnrm[he];
+      for (int b = ia[i] + 1; b < ia[i + 1]; b++)
+        if (ja[b] == nn) {
+          M[(size_t)b * 25 + 0] = to_store<T>(-1.0);
+          M[(size_t)b * 25 + 24] = to_store<T>(-1.0);
+        }
+    } else {
+      D[4 * 5 + 0] = -(Tw / (gamma * (gamma - 1.0)) + 0.5 * 0.0);
+    }
+  }
+  if (mod)
+    for (int t = 0; t < 25; t++) diag[(size_t)i * 25 + t] = D[t];
+  int pv[5];
+  if (lu5(D, pv)) atomicAdd(&health[H_BADLU], 1ull);
+  // store reciprocals of the U diagonal for the solves
+#pragma unroll
+  for (int r = 0; r < 5; r++) D[pv[r] * 5 + r] = 1.0 / D[pv[r] * 5 + r];
+#pragma unroll
+  for (int t = 0; t < 25; t++) dlu[(size_t)i * 25 + t] = D[t];
+#pragma unroll
+  for (int r = 0; r < 5; r++) piv[(size_t)i * 5 + r] = pv[r];
+}
+
+// LuSolve (ucs/matrix.h:238) with the U-diagonal reciprocals stored by
+// k_jac_finish; b is overwritten with the solution.
+__device__ __forceinline__ void lusolve5(const double* a, double* b, const int* p) {
+  double x[5];
+  for (int i = 0; i < 5; i++) {
+    double sum = 0.0;
+    for (int j = 0; j < i; j++) sum += a[p[i] * 5 + j] * x[j];
+    x[i] = b[p[i]] - sum;
+  }
+  for (int i = 4; i >= 0; i--) {
+    double sum = 0.0;
+    for (int j = 4; j > i; j--) sum += a[p[i] * 5 + j] * b[j];
+    b[i] = (x[i] - sum) * a[p[i] * 5 + i];
+  }
+}
+
+// One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62),
+// a warp per block row: lanes 0..29 take (block, sub-row) pairs of six
+// blocks at a time, partial products are summed through shared memory, and
+// lane 0 solves the 5x5 diagonal system.
+template <class T>
+__global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restrict__ rows, const int* __restrict__ ia,
+                                                   const int* __restrict__ ja, const T* __restrict__ M,
+                                                   const double* __restrict__ dlu, const int* __restrict__ piv,
+                                                   const double* __restrict__ b, double* __restrict__ x) {
+  __shared__ double part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x * 8 + w;
+  if (gw >= nrows) return;
+  const int i = rows[gw];
+  const int b0 = ia[i] + 1, b1 = ia[i + 1];
+  const int r = lane % 5, kb = lane / 5;  // lanes 30, 31 idle
+  double acc = 0.0;
+  if (lane < 30) {
+    for (int blk = b0 + kb; blk < b1; blk += 6) {
+      const T* A = &M[(size_t)blk * 25 + r * 5];
+      const double* xj = &x[(size_t)ja[blk] * 5];
+#pragma unroll
+      for (int c = 0; c < 5; c++) acc += ld_blk(&A[c]) * xj[c];
+    }
+  }
+  part[w][lane] = acc;
+  __syncwarp();
+  if (lane == 0) {
+    double rhs[5];
+    for (int rr = 0; rr < 5; rr++) {
+      double s = 0.0;
+      for (int m = 0; m < 6; m++) s += part[w][rr + 5 * m];
+      rhs[rr] = b[(size_t)i * 5 + rr] - s;
+    }
+    int p[5];
+    for (int rr = 0; rr < 5; rr++) p[rr] = piv[(size_t)i * 5 + rr];
+    lusolve5(&dlu[(size_t)i * 25], rhs, p);
+    for (int rr = 0; rr < 5; rr++) x[(size_t)i * 5 + rr] = rhs[rr];
+  }
+}
+
+// Block sparse matrix-vector product y = A x (CRS MatVecMultiply,
+// ucs/crs.tcc:484) with the FP64 diagonal, warp per block row.
+template <class T>
+__global__ void __launch_bounds__(256) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
+                                              const T* __restrict__ M, const double* __restrict__ diag,
+                                              const double* __restrict__ x, double* __restrict__ y) {
+  __shared__ double part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w;
+  if (i >= nnode) return;
+  const int b0 = ia[i] + 1, b1 = ia[i + 1];
+  const int r = lane % 5, kb = lane / 5;
+  double acc = 0.0;
+  if (lane < 30) {
+    for (int blk = b0 + kb; blk < b1; blk += 6) {
+      const T* A = &M[(size_t)blk * 25 + r * 5];
+      const double* xj = &x[(size_t)ja[blk] * 5];
+#pragma unroll
+      for (int c = 0; c < 5; c++) acc += ld_blk(&A[c]) * xj[c];
+    }
+    if (kb == 0) {
+      const double* D = &diag[(size_t)i * 25 + r * 5];
+      const double* xi = &x[(size_t)i * 5];
+      for (int c = 0; c < 5; c++) acc += D[c] * xi[c];
+    }
+  }
+  part[w][lane] = acc;
+  __syncwarp();
+  if (lane < 5) {
+    double s = 0.0;
+    for (int m = 0; m < 6; m++) s += part[w][lane + 5 * m];
+    y[(size_t)i * 5 + lane] = s;
+  }
+}
+
+// Newton update (NewtonIterate, ucs/solutionSpace.tcc:772-818): NaN/Inf
+// updates are zeroed per node, CompressibleEqnSet::ApplyDQ
+// (ucs/compressible.tcc:929) clips density, energy and pressure, the
+// auxiliary variables are recomputed, and b-style partial sums of dq^2 are
+// formed for the update norm.
+__global__ void __launch_bounds__(kNormThreads) k_apply_dq(int nnode, double gamma, double* __restrict__ x,
+                                                            double* __restrict__ q, double* __restrict__ part,
+                                                            unsigned long long* health) {
+  __shared__ double red[kNormThreads / 32];
+  double acc = 0.0;
+  const double gm1 = gamma - 1.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    double dQ[5];
+    bool zero = false;
+    for (int k = 0; k < 5; k++) {
+      dQ[k] = x[(size_t)i * 5 + k];
+      if (isnan(dQ[k]) || isinf(dQ[k])) zero = true;
+    }
+    if (zero) {
+      for (int k = 0; k < 5; k++) { dQ[k] = 0.0; x[(size_t)i * 5 + k] = 0.0; }
+      atomicAdd(&health[H_NANDQ], 1ull);
+    }
+    double* Q = &q[(size_t)i * NVARS];
+    const double minP = 1.0e-10, minRho = 1.0e-10, minE = 1.0e-10;
+    if (Q[0] + dQ[0] < 0.0) { Q[0] = minRho; atomicAdd(&health[H_RHOCLIP], 1ull); }
+    else Q[0] += dQ[0];
+    if (Q[4] + dQ[4] < 0.0) { Q[4] = minE; atomicAdd(&health[H_ECLIP], 1ull); }
+    else Q[4] += dQ[4];
+    double rho = Q[0];
+    double u = Q[1] / rho, v = Q[2] / rho, w = Q[3] / rho;
+    double E = Q[4];
+    double v2 = u * u + v * v + w * w;
+    if (E < 0.5 * rho * v2) {
+      atomicAdd(&health[H_PCLIP], 1ull);
+      double v2mod = 2.0 * (E - minP / gm1);
+      double frac = 0.0;
+      if (v2mod > 0.0) frac = sqrt(v2mod / v2);
+      u *= frac; v *= frac; w *= frac;
+      Q[1] = rho * u; Q[2] = rho * v; Q[3] = rho * w;
+    } else {
+      Q[1] += dQ[1]; Q[2] += dQ[2]; Q[3] += dQ[3];
+    }
+    aux_vars(gamma, Q);
+    for (int k = 0; k < 5; k++) acc += dQ[k] * dQ[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int k = 0; k < kNormThreads / 32; k++) v += red[k];
+    part[blockIdx.x] = v;
+  }
+}
+
+// Sum of squares of a vector in fixed order (deterministic), per block.
+__global__ void __launch_bounds__(kNormThreads) k_sumsq(long long n, const double* __restrict__ v,
+                                                         double* __restrict__ part) {
+  __shared__ double red[kNormThreads / 32];
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += v[i] * v[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < kNormThreads / 32; k++) s += red[k];
+    part[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_sum_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < nblocks; i++) s += part[i];
+  *out = s;
+}
+
+// MaxEigenvalue (ucs/compressible.tcc:799) of the face-averaged state
+__device__ __forceinline__ double max_eig(const double* QL, const double* QR, const D4& a, double gamma, double half) {
+  double Q0 = half * (QL[0] + QR[0]), Q1 = half * (QL[1] + QR[1]), Q2 = half * (QL[2] + QR[2]),
+         Q3 = half * (QL[3] + QR[3]), Q4 = half * (QL[4] + QR[4]);
+  double gm1 = gamma - 1.0;
+  double ir = 1.0 / Q0;
+  double u = Q1 * ir, v = Q2 * ir, w = Q3 * ir;
+  double v2h = 0.5 * (u * u + v * v + w * w);
+  double P = gm1 * (Q4 - Q0 * v2h);
+  double c = sqrt(gamma * P * ir);
+  double theta = u * a.x + v * a.y + w * a.z;
+  double e4 = fabs(theta + c), e5 = fabs(theta - c);
+  return e4 > e5 ? e4 : e5;
+}
+
+// ComputeTimesteps (ucs/timestep.tcc:7) with local time stepping:
+// dt_i = CFL vol_i / sum(max eigenvalue * area) over the node's faces.
+__global__ void __launch_bounds__(128) k_timestep(int nnode, const int* __restrict__ nptr, const int* __restrict__ nedg,
+                                                  const int* __restrict__ nnbr, const D4* __restrict__ ea,
+                                                  const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                  const int2* __restrict__ bn, const D4* __restrict__ ba,
+                                                  const double* __restrict__ q, const double* __restrict__ vol,
+                                                  double gamma, double cfl, double* __restrict__ dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double s = 0.0;
+  const double* qi = &q[(size_t)i * NVARS];
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    int se = nedg[k];
+    int e = se < 0 ? ~se : se;
+    const double* qj = &q[(size_t)nnbr[k] * NVARS];
+    // the reference averages left and right in edge orientation
+    s += (se < 0 ? max_eig(qi, qj, ea[e], gamma, 0.5) : max_eig(qj, qi, ea[e], gamma, 0.5)) * ea[e].w;
+  }
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    int he = bhe[p];
+    s += max_eig(qi, &q[(size_t)bn[he].y * NVARS], ba[he], gamma, 0.5) * ba[he].w;
+  }
+  dt[i] = cfl * (vol[i] / s);
+}
+
+__global__ void __launch_bounds__(kNormThreads) k_min_part(int n, const double* __restrict__ v,
+                                                            double* __restrict__ part) {
+  __shared__ double red[kNormThreads / 32];
+  double m = 1.0e300;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = fmin(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 1.0e300;
+    for (int k = 0; k < kNormThreads / 32; k++) r = fmin(r, red[k]);
+    part[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_min_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double r = 1.0e300;
+  for (int i = 0; i < nblocks; i++) r = fmin(r, part[i]);
+  *out = r;
+}
+
+// ---- FGMRES vector kernels (deterministic reductions) ----------------------
+
+// part[block][k] = partial sums of (w, V_k) for k < nv; V_k = V + k*n
+__global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const double* __restrict__ V,
+                                                        const double* __restrict__ w, double* __restrict__ part,
+                                                        int part_stride) {
+  __shared__ double red[kNormThreads / 32];
+  for (int k = 0; k < nv; k++) {
+    const double* v = V + (size_t)k * n;
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+      acc += w[i] * v[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sacc = 0.0;
+      for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q];
+      part[(size_t)blockIdx.x * part_stride + k] = sacc;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_mdot_final(int nblocks, int nv, int part_stride, const double* __restrict__ part,
+                             double* __restrict__ out) {
+  int k = threadIdx.x;
+  if (k >= nv) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; b++) s += part[(size_t)b * part_stride + k];
+  out[k] = s;
+}
+
+// w -= sum_k h[k] V_k   (h on the device)
+__global__ void k_orth_update(long long n, int nv, const double* __restrict__ V, const double* __restrict__ h,
+                              double* __restrict__ w) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = w[i];
+    for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
+    w[i] = v;
+  }
+}
+
+// y = a * x
+__global__ void k_scale_copy(long long n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
+
+// x += sum_k c[k] Z_k
+__global__ void k_combine(long long n, int nv, const double* __restrict__ Z, const double* __restrict__ c,
+                          double* __restrict__ x) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = x[i];
+    for (int k = 0; k < nv; k++) v += c[k] * Z[(size_t)k * n + i];
+    x[i] = v;
+  }
+}
+
+// r = b - r   (r holds A x on entry)
+__global__ void k_residual_vec(long long n, const double* __restrict__ b, double* __restrict__ r) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    r[i] = b[i] - r[i];
+}

@@ -19,6 +19,7 @@
 #include "../../include/pcfd.h"
 #include "flux_device.cuh"
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,12 +52,26 @@ int set_err(int code, const std::string& msg) {
       return set_err(PCFD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-enum HealthSlot { H_KNEECAP = 0, H_LIMCLIP = 1, H_RHOCLIP = 2, H_ECLIP = 3, H_PCLIP = 4, H_NANDQ = 5, H_BADBC = 6 };
+enum HealthSlot {
+  H_KNEECAP = 0,  // NaN flux components zeroed (ucs/eqnset.tcc:73-88)
+  H_LIMCLIP = 1,  // nodes whose limiter the pressure clip zeroed
+  H_RHOCLIP = 2,  // ApplyDQ density clips
+  H_ECLIP = 3,    // ApplyDQ energy clips
+  H_PCLIP = 4,    // ApplyDQ pressure clips
+  H_NANDQ = 5,    // nodes whose NaN/Inf update was zeroed
+  H_BADBC = 6,    // half-edges with an unknown boundary condition type
+  H_BADLU = 7     // ill-conditioned diagonal blocks in the LU
+};
 
 // Kernel timers, one per launch site (TimerList analogue)
-enum TimerId { T_BC = 0, T_GRAD, T_LIMITER, T_EDGEFLUX, T_BEDGEFLUX, T_GATHER, T_NORM, T_SETUP, T_COUNT };
-const char* kTimerNames[T_COUNT] = {"bc_update", "lsq_gradient", "venkat_limiter", "edge_flux",
-                                    "bedge_flux", "residual_gather", "norm_reduce", "setup"};
+enum TimerId {
+  T_BC = 0, T_GRAD, T_LIMITER, T_EDGEFLUX, T_CLIP, T_BEDGEFLUX, T_GATHER, T_NORM, T_SETUP,
+  T_JAC_EDGE, T_JAC_BEDGE, T_JAC_DIAG, T_JAC_FINISH, T_SGS, T_SPMV, T_KRYLOV, T_UPDATE, T_TIMESTEP, T_COUNT
+};
+const char* kTimerNames[T_COUNT] = {"bc_update", "lsq_gradient", "venkat_limiter", "edge_flux", "pressure_clip",
+                                    "bedge_flux", "residual_gather", "norm_reduce", "setup", "jac_edge",
+                                    "jac_bedge", "jac_diag", "jac_finish_lu", "sgs_sweep", "spmv",
+                                    "krylov_vec", "apply_dq", "timestep"};
 
 struct Solver {
   // sizes
@@ -99,7 +114,39 @@ struct Solver {
   double* d_part = nullptr;     // [kNormBlocks][6] norm partial sums (scratch)
   double* d_norms = nullptr;    // [6]
   unsigned long long* d_health = nullptr;  // [8]
+  double* d_limraw = nullptr;   // [nnode][5] limiter before the clamp to zero
+  int* d_clipflag = nullptr;    // [nnode] bit 0 clip, bit 1 negative raw limiter
+  int* d_clipany = nullptr;     // [1]
+  int* d_bind = nullptr;        // half-edges of nodes without hard-set BCs
+  int nbind = 0;
   int have_grad = 0, have_lim = 0;
+  int lim_clipped = 0;  // 1: d_lim already went through the explicit pressure clip
+
+  // implicit system (block CRS in the reference layout)
+  long long nblocks = 0;
+  int* d_ia = nullptr;          // [nnode+1]
+  int* d_ja = nullptr;          // [nblocks]
+  int* d_pos_lr = nullptr;      // [nedge] block index of A(L,R)
+  int* d_pos_rl = nullptr;      // [nedge] block index of A(R,L)
+  int jac_prec = -1;            // 0 FP64, 1 FP32, 2 BF16 off-diagonal storage
+  void* d_M = nullptr;          // [nblocks][25] off-diagonal blocks (diagonal slots unused)
+  double* d_diag = nullptr;     // [nnode][25] diagonal blocks before the LU
+  double* d_dlu = nullptr;      // [nnode][25] LU of the diagonal, U reciprocals on its diagonal
+  int* d_piv = nullptr;         // [nnode][5]
+  double* d_bblk = nullptr;     // [nbedge][25] boundary contributions to the diagonal
+  double* d_dt = nullptr;       // [nnode] local pseudo time step
+  double* d_x = nullptr;        // [nnode][5] linear solution (dq)
+  double* d_scal = nullptr;     // [16] scalar results
+  int have_dt = 0, have_jac = 0;
+  int ncolor = 0;
+  std::vector<int> color_ptr;   // [ncolor+1] into d_color_rows
+  int* d_color_rows = nullptr;  // [nnode]
+  // FGMRES work space (allocated on first use)
+  int fg_m = 0;
+  double* d_V = nullptr;        // [m+1][nnode*5]
+  double* d_Z = nullptr;        // [m][nnode*5]
+  double* d_w = nullptr;        // [nnode*5]
+  double* d_dots = nullptr;     // [kNormBlocks][m+2] partial dot products
 
   // profiling
   int profile = 0;
@@ -345,6 +392,27 @@ __global__ void k_bc_nodes(int ngroup, const int* __restrict__ gnode, const int*
   for (int j = 0; j < NVARS; j++) q[(size_t)node * NVARS + j] = QL[j];
 }
 
+// Half-edges of boundary nodes that no condition hard-sets (far field, walls,
+// symmetry, outflow): each writes only its own phantom state, so every
+// half-edge is independent.  The node's stored auxiliary variables are left
+// as they are (the reference recomputes them from unchanged conservative
+// values).
+__global__ void k_bc_halfedges(int n, const int* __restrict__ list, const int2* __restrict__ bn,
+                               const D4* __restrict__ ba, const int* __restrict__ bbc,
+                               const double* __restrict__ btw, BcConst k, double* __restrict__ q,
+                               unsigned long long* health) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  int he = list[t];
+  int2 nd = bn[he];
+  double QL[NVARS], QR[NVARS];
+  for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)nd.x * NVARS + j];
+  for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)nd.y * NVARS + j];
+  double nQ[NVARS] = {0};
+  if (!apply_bc(k, bbc[he], QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
+  for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = QR[j];
+}
+
 // Exact reference order when a no-slip normal node is itself hard-set by a
 // boundary condition: a single thread walks the half-edges in bedge order.
 __global__ void k_bc_sequential(int nbedge, const int2* __restrict__ bn, const D4* __restrict__ ba,
@@ -419,7 +487,8 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
                                                 const int* __restrict__ nnbr, const double* __restrict__ q,
                                                 const double* __restrict__ grad, const double* __restrict__ xyz,
                                                 const double* __restrict__ vol, double chi, double K3,
-                                                double* __restrict__ lim) {
+                                                double* __restrict__ limraw, double* __restrict__ lim,
+                                                int* __restrict__ clipflag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnode) return;
   double qi[NEQN], qmin[NEQN], qmax[NEQN], l[NEQN], gi[NEQN * 3];
@@ -441,20 +510,37 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
   }
   const double ep2 = 6.0 * 3.141592653589793 * vol[i] * K3;
   const double xi0 = xyz[3 * i], xi1 = xyz[3 * i + 1], xi2 = xyz[3 * i + 2];
+  // The limiter is min(1, min_k num_k / den_k) with every den_k > 0
+  // (den = (DP + DM/2)^2 + 7/4 DM^2 + eps^2).  The running minimum is kept
+  // as a fraction and compared by cross-multiplication, so only one FP64
+  // division per equation remains instead of one per edge and equation.
+  double bn[NEQN], bd[NEQN];
+  for (int t = 0; t < NEQN; t++) { bn[t] = l[t]; bd[t] = 1.0; }
   for (int k = k0; k < k1; k++) {
     int j = nnbr[k];
     const double* qj = &q[(size_t)j * NVARS];
     double dx0 = 0.5 * (xyz[3 * j] - xi0), dx1 = 0.5 * (xyz[3 * j + 1] - xi1), dx2 = 0.5 * (xyz[3 * j + 2] - xi2);
+#pragma unroll
     for (int t = 0; t < NEQN; t++) {
       double dQ = qj[t] - qi[t];
       double Q = qi[t] + (0.5 * chi * dQ + (1.0 - chi) * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
       double DM = Q - qi[t];
       double DP = (Q > qi[t]) ? qmax[t] - qi[t] : qmin[t] - qi[t];
-      double v = (DP * DP + ep2 + 2.0 * DM * DP) / (DP * DP + 2.0 * DM * DM + DM * DP + ep2);
-      l[t] = (l[t] < v) ? l[t] : v;
+      double num = DP * DP + ep2 + 2.0 * DM * DP;
+      double den = DP * DP + 2.0 * DM * DM + DM * DP + ep2;
+      if (num * bd[t] < bn[t] * den) { bn[t] = num; bd[t] = den; }
     }
   }
-  for (int t = 0; t < NEQN; t++) lim[(size_t)i * NEQN + t] = l[t];
+  // raw values (possibly negative) feed the pressure clip; the clamp to
+  // zero comes after it (ucs/limiters.tcc:110-124)
+  int neg = 0;
+  for (int t = 0; t < NEQN; t++) {
+    double v = (bd[t] == 1.0) ? bn[t] : bn[t] / bd[t];
+    limraw[(size_t)i * NEQN + t] = v;
+    if (v < 0.0) neg = 1;
+    if (lim) lim[(size_t)i * NEQN + t] = (v < 0.0) ? 0.0 : v;
+  }
+  clipflag[i] = neg ? 2 : 0;
 }
 
 __device__ __forceinline__ int bad_extrap(double gamma, const double* Q) {
@@ -463,6 +549,37 @@ __device__ __forceinline__ int bad_extrap(double gamma, const double* Q) {
   double u = Q[1] * ir, v = Q[2] * ir, w = Q[3] * ir;
   double p = (gamma - 1.0) * (Q[4] - r * (0.5 * (u * u + v * v + w * w)));
   return (p < 1.0e-10) || (r < 0.0) || (Q[4] < 1.0e-10);
+}
+
+// Extrapolated states of one edge with the given limiters and the three
+// BadExtrapolation tests of Kernel_PressureClip (ucs/limiters.tcc:737):
+// bit 0 left, bit 1 right, bit 2 Roe average.
+__device__ int clip_check(const double* qL, const double* qR, const double* gL, const double* gR,
+                          const double* lL, const double* lR, double h0, double h1, double h2, double chi,
+                          double gamma) {
+  double Qi[NEQN], Qj[NEQN];
+  for (int t = 0; t < NEQN; t++) {
+    double dQ = qR[t] - qL[t];
+    Qi[t] = qL[t] + (0.5 * chi * dQ + (1.0 - chi) * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2)) * lL[t];
+    Qj[t] = qR[t] + (0.5 * chi * (-dQ) + (1.0 - chi) * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2))) * lR[t];
+  }
+  int m = 0;
+  if (bad_extrap(gamma, Qi)) m |= 1;
+  if (bad_extrap(gamma, Qj)) m |= 2;
+  double gm1 = gamma - 1.0;
+  double rL = Qi[0], rR = Qj[0];
+  double uL = Qi[1] / rL, vL = Qi[2] / rL, wL = Qi[3] / rL;
+  double uR = Qj[1] / rR, vR = Qj[2] / rR, wR = Qj[3] / rR;
+  double PL = gm1 * (Qi[4] - 0.5 * rL * (uL * uL + vL * vL + wL * wL));
+  double PR = gm1 * (Qj[4] - 0.5 * rR * (uR * uR + vR * vR + wR * wR));
+  double hL = (Qi[4] + PL) / rL, hR = (Qj[4] + PR) / rR;
+  double rho = sqrt(rL * rR);
+  double sg = rho / (rL + rho);
+  double u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
+  double v2h = 0.5 * (u * u + v * v + w * w);
+  double Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
+  if (bad_extrap(gamma, Qr)) m |= 4;
+  return m;
 }
 
 // Kernel_PressureClip (ucs/limiters.tcc:737) evaluated with the post-limiter
@@ -525,6 +642,7 @@ __global__ void __launch_bounds__(128) k_pressure_clip(int nnode, const int* __r
 struct FluxConst {
   double gamma, chi;
   int ho, viscous;
+  int clip;            // second order with a limiter: the pressure clip applies
   double inv_retilde;  // Mach / Re
   double S;            // Sutherland constant / T_ref
   double cp_over_pr;   // (1/(gamma-1)) / Pr
@@ -540,14 +658,25 @@ __device__ __forceinline__ int kneecap5(double* f) {
 
 // Kernel_Inviscid_Flux (:192) + Kernel_Viscous_Flux (:390) for one edge; the
 // sum is stored as the flux leaving the left node.
+// MODE 0: plain evaluation.  MODE 1: also flags the nodes whose extrapolated
+// or Roe-averaged states are non-physical - the pressure clip of the limiter
+// (ucs/limiters.tcc:737) tests exactly these states, so when nothing is
+// flagged the clip is a no-op and the fluxes already stand.  MODE 2:
+// re-evaluates only edges touching a flagged node, after their limiters were
+// zeroed; it returns at once when nothing was flagged.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __restrict__ en,
                                                    const D4* __restrict__ ea, const double* __restrict__ eh,
                                                    const double* __restrict__ q, const double* __restrict__ grad,
                                                    const double* __restrict__ lim, FluxConst k,
-                                                   double* __restrict__ ef, unsigned long long* health) {
+                                                   double* __restrict__ ef, unsigned long long* health,
+                                                   int* __restrict__ clipflag, int* __restrict__ clipany,
+                                                   const double* __restrict__ limraw) {
+  if (MODE == 2 && *(volatile int*)clipany == 0) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nedge) return;
   const int2 n = en[e];
+  if (MODE == 2 && !((clipflag[n.x] | clipflag[n.y]) & 1)) return;
   const D4 a = ea[e];
   const double* qL = &q[(size_t)n.x * NVARS];
   const double* qR = &q[(size_t)n.y * NVARS];
@@ -571,7 +700,18 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
     }
   }
   double f[NEQN];
-  roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
+  int bad = roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
+  if (MODE == 1 && k.clip && ((clipflag[n.x] | clipflag[n.y]) & 2)) {
+    // an endpoint had negative raw limiter values, which the clip sees
+    // before they are clamped: test the states it would build
+    bad = clip_check(qL, qR, &grad[(size_t)n.x * NTERMS * 3], &grad[(size_t)n.y * NTERMS * 3],
+                     &limraw[(size_t)n.x * NEQN], &limraw[(size_t)n.y * NEQN], h0, h1, h2, k.chi, k.gamma);
+  }
+  if (MODE == 1 && k.clip && bad) {
+    if (bad & 5) atomicOr(&clipflag[n.x], 1);
+    if (bad & 6) atomicOr(&clipflag[n.y], 1);
+    atomicOr(clipany, 1);
+  }
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
   if (k.viscous) {
     // face state: plain average of the nodal conservative variables
@@ -608,6 +748,19 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
   }
 #pragma unroll
   for (int t = 0; t < NEQN; t++) ef[(size_t)e * NEQN + t] = f[t];
+}
+
+// Zeroes the limiter of every flagged node (the pressure clip); returns at
+// once when nothing was flagged.
+__global__ void k_clip_apply(int nnode, const int* __restrict__ clipflag, const int* __restrict__ clipany,
+                             double* __restrict__ lim, unsigned long long* health) {
+  if (*(volatile const int*)clipany == 0) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    if (clipflag[i] & 1) {
+      for (int t = 0; t < NEQN; t++) lim[(size_t)i * NEQN + t] = 0.0;
+      atomicAdd(&health[H_LIMCLIP], 1ull);
+    }
+  }
 }
 
 // Bkernel_Inviscid_Flux (:299) + Bkernel_Viscous_Flux (:472) for one
@@ -653,10 +806,13 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
                                                          const int* __restrict__ bptr, const int* __restrict__ bhe,
                                                          const double* __restrict__ bf, const int* __restrict__ bbc,
                                                          const double* __restrict__ btw, double* __restrict__ b,
-                                                         double* __restrict__ part) {
+                                                         double* __restrict__ part, int* __restrict__ clipflag,
+                                                         const int* __restrict__ clipany) {
   __shared__ double red[kNormThreads / 32][6];
   double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int any = *(volatile const int*)clipany;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    if (any && (clipflag[i] & 1)) clipflag[i] &= ~1;
     double r[NEQN] = {0, 0, 0, 0, 0};
     for (int k = nptr[i]; k < nptr[i + 1]; k++) {
       int se = nedg[k];
@@ -703,14 +859,18 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
   }
 }
 
-__global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ part, double* __restrict__ norms) {
+__global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ part, double* __restrict__ norms,
+                             int* __restrict__ clipany) {
   int c = threadIdx.x;
+  if (c == 0) *clipany = 0;
   if (c >= 6) return;
   double v = 0.0;
   for (int bI = 0; bI < nblocks; bI++) v += part[(size_t)bI * 6 + c];
   if (c == 0) norms[0] = sqrt(v) / ((double)nnode * NEQN);
   else norms[c] = sqrt(v) / (double)nnode;
 }
+
+#include "implicit.cuh"
 
 // -------------------------------------------------------------------------
 // host helpers
@@ -737,7 +897,9 @@ void free_solver(Solver* s) {
   void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
                   s->d_bgptr, s->d_bghe, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
-                  s->d_norms, s->d_health};
+                  s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
+                  s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_piv,
+                  s->d_bblk, s->d_dt, s->d_x, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -779,6 +941,7 @@ FluxConst make_flux_const(const Solver* s) {
   k.chi = s->prm.chi;
   k.ho = s->prm.sorder > 1;
   k.viscous = s->prm.viscous;
+  k.clip = k.ho && s->prm.limiter != 0;
   k.inv_retilde = s->prm.Re != 0.0 ? s->prm.mach / s->prm.Re : 0.0;
   k.S = 110.4 / s->prm.ref_temperature;
   k.cp_over_pr = (1.0 / (s->prm.gamma - 1.0)) / s->prm.Pr;
@@ -806,6 +969,14 @@ int run_bcs(Solver* s) {
                                               s->d_health);
     });
   }
+  int rc = PCFD_OK;
+  if (s->nbind > 0) {
+    rc = launch(s, T_BC, [&] {
+      k_bc_halfedges<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba, s->d_bbc,
+                                                                 s->d_btw, k, s->d_q, s->d_health);
+    });
+    if (rc) return rc;
+  }
   if (s->nbgroup == 0) return PCFD_OK;
   return launch(s, T_BC, [&] {
     k_bc_nodes<<<nblk(s->nbgroup, 128), 128, 0, s->stream>>>(s->nbgroup, s->d_bgnode, s->d_bgptr, s->d_bghe, s->d_bn,
@@ -823,7 +994,7 @@ int run_gradient(Solver* s) {
   return rc;
 }
 
-int run_limiter(Solver* s) {
+int run_limiter(Solver* s, bool clip) {
   if (s->prm.limiter == 0) {
     // limiters stay 1.0 (OFF), Limiter ctor (ucs/limiters.tcc:36-41)
     std::vector<double> ones((size_t)s->nnode * NEQN, 1.0);
@@ -835,16 +1006,26 @@ int run_limiter(Solver* s) {
   double K = s->prm.venkat_K;
   int rc = launch(s, T_LIMITER, [&] {
     k_venkat<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad, s->d_xyz,
-                                                        s->d_vol, s->prm.chi, K * K * K, s->d_b);
+                                                        s->d_vol, s->prm.chi, K * K * K, s->d_limraw,
+                                                        clip ? nullptr : s->d_lim, s->d_clipflag);
   });
   if (rc) return rc;
+  if (!clip) {
+    // the clip is folded into the residual's edge pass (k_edge_flux<1>)
+    s->have_lim = 1;
+    s->lim_clipped = 0;
+    return PCFD_OK;
+  }
   // d_b holds the pre-clip limiter as scratch; the clip writes the final value
   rc = launch(s, T_LIMITER, [&] {
     k_pressure_clip<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad,
-                                                               s->d_xyz, s->prm.chi, s->prm.gamma, s->d_b, s->d_lim,
-                                                               s->d_health);
+                                                               s->d_xyz, s->prm.chi, s->prm.gamma, s->d_limraw,
+                                                               s->d_lim, s->d_health);
   });
-  if (rc == PCFD_OK) s->have_lim = 1;
+  if (rc == PCFD_OK) {
+    s->have_lim = 1;
+    s->lim_clipped = 1;
+  }
   return rc;
 }
 
@@ -852,11 +1033,25 @@ int run_residual(Solver* s) {
   FluxConst k = make_flux_const(s);
   if ((k.ho || k.viscous) && !s->have_grad) return set_err(PCFD_ERR_STATE, "residual: gradient not computed");
   if (k.ho && !s->have_lim) return set_err(PCFD_ERR_STATE, "residual: limiter not computed");
+  if (s->lim_clipped) k.clip = 0;  // the explicit clip already ran
   int rc = launch(s, T_EDGEFLUX, [&] {
-    k_edge_flux<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q, s->d_grad,
-                                                           s->d_lim, k, s->d_ef, s->d_health);
+    k_edge_flux<1><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
+                                                              s->d_grad, s->d_lim, k, s->d_ef, s->d_health,
+                                                              s->d_clipflag, s->d_clipany, s->d_limraw);
   });
   if (rc) return rc;
+  if (k.clip) {
+    rc = launch(s, T_CLIP, [&] {
+      k_clip_apply<<<kNormBlocks, 256, 0, s->stream>>>(s->nnode, s->d_clipflag, s->d_clipany, s->d_lim, s->d_health);
+    });
+    if (rc) return rc;
+    rc = launch(s, T_CLIP, [&] {
+      k_edge_flux<2><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
+                                                                s->d_grad, s->d_lim, k, s->d_ef, s->d_health,
+                                                                s->d_clipflag, s->d_clipany, s->d_limraw);
+    });
+    if (rc) return rc;
+  }
   if (s->nbedge > 0) {
     rc = launch(s, T_BEDGEFLUX, [&] {
       k_bedge_flux<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_q, s->d_grad, k,
@@ -866,12 +1061,327 @@ int run_residual(Solver* s) {
   }
   rc = launch(s, T_GATHER, [&] {
     k_gather<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_ef, s->d_bptr, s->d_bhe,
-                                                         s->d_bf, s->d_bbc, s->d_btw, s->d_b, s->d_part);
+                                                         s->d_bf, s->d_bbc, s->d_btw, s->d_b, s->d_part,
+                                                         s->d_clipflag, s->d_clipany);
   });
   if (rc) return rc;
   return launch(s, T_NORM, [&] {
-    k_norm_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms);
+    k_norm_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms, s->d_clipany);
   });
+}
+
+
+// ---- implicit system runners ---------------------------------------------
+
+size_t prec_bytes(int prec) { return prec == 0 ? 8 : (prec == 1 ? 4 : 2); }
+
+int ensure_matrix(Solver* s, int prec) {
+  if (prec < 0 || prec > 2) return set_err(PCFD_ERR_ARG, "Jacobian precision must be 0 (FP64), 1 (FP32) or 2 (BF16)");
+  if (s->d_M && s->jac_prec == prec) return PCFD_OK;
+  if (s->d_M) { cudaFree(s->d_M); s->d_M = nullptr; }
+  size_t bytes = (size_t)s->nblocks * 25 * prec_bytes(prec);
+  cudaError_t e = cudaMalloc(&s->d_M, bytes);
+  if (e != cudaSuccess) return set_err(PCFD_ERR_NOMEM, std::string("matrix: ") + cudaGetErrorString(e));
+  CUDA_TRY(cudaMemsetAsync(s->d_M, 0, bytes, s->stream));
+  s->jac_prec = prec;
+  s->have_jac = 0;
+  return PCFD_OK;
+}
+
+// Param::UpdateCFL (ucs/param.tcc:696), prescribed ramp
+double ramp_cfl(int iter, double cfl_start, double cfl, int ramp_steps) {
+  if (ramp_steps > 0 && iter < ramp_steps) return (cfl - cfl_start) / (double)ramp_steps * (double)iter + cfl_start;
+  return cfl;
+}
+
+int run_timestep(Solver* s, double cfl) {
+  int rc = launch(s, T_TIMESTEP, [&] {
+    k_timestep<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_ea,
+                                                          s->d_bptr, s->d_bhe, s->d_bn, s->d_ba, s->d_q, s->d_vol,
+                                                          s->prm.gamma, cfl, s->d_dt);
+  });
+  if (rc) return rc;
+  rc = launch(s, T_TIMESTEP, [&] { k_min_part<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_dt, s->d_part); });
+  if (rc) return rc;
+  rc = launch(s, T_TIMESTEP, [&] { k_min_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->d_part, s->d_scal + 0); });
+  if (rc == PCFD_OK) s->have_dt = 1;
+  return rc;
+}
+
+JacConst make_jac_const(const Solver* s) {
+  JacConst k;
+  k.gamma = s->prm.gamma;
+  k.Pr = s->prm.Pr;
+  k.inv_retilde = s->prm.Re != 0.0 ? s->prm.mach / s->prm.Re : 0.0;
+  k.S = 110.4 / s->prm.ref_temperature;
+  k.viscous = s->prm.viscous;
+  return k;
+}
+
+template <class T>
+int run_jacobian_t(Solver* s) {
+  T* M = (T*)s->d_M;
+  JacConst jk = make_jac_const(s);
+  BcConst bk = make_bc_const(s);
+  int rc = launch(s, T_JAC_EDGE, [&] {
+    k_jac_edge<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
+                                                             s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
+  });
+  if (rc) return rc;
+  if (s->nbedge > 0) {
+    rc = launch(s, T_JAC_BEDGE, [&] {
+      k_jac_bedge<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
+                                                              s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_q,
+                                                              s->d_bblk, s->d_health);
+    });
+    if (rc) return rc;
+  }
+  rc = launch(s, T_JAC_DIAG, [&] {
+    k_jac_diag<T><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_pos_lr,
+                                                             s->d_pos_rl, s->d_bptr, s->d_bhe, s->d_bblk, M,
+                                                             s->d_vol, s->d_dt, s->d_diag);
+  });
+  if (rc) return rc;
+  rc = launch(s, T_JAC_FINISH, [&] {
+    k_jac_finish<T><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, s->d_bptr, s->d_bhe,
+                                                               s->d_bbc, s->d_btw, s->d_bnrm, s->prm.gamma, M,
+                                                               s->d_diag, s->d_dlu, s->d_piv, s->d_health);
+  });
+  if (rc == PCFD_OK) s->have_jac = 1;
+  return rc;
+}
+
+// ComputeJacobians (ucs/jacobian.tcc:13) including the boundary-condition
+// application its boundary kernel performs on the stored state.
+int run_jacobian(Solver* s) {
+  if (!s->have_dt) return set_err(PCFD_ERR_STATE, "jacobian: no time step computed yet (pcfd_timestep)");
+  if (!s->d_M) {
+    int rc = ensure_matrix(s, 0);
+    if (rc) return rc;
+  }
+  int rc = run_bcs(s);
+  if (rc) return rc;
+  s->have_grad = s->have_lim = 0;
+  switch (s->jac_prec) {
+    case 0: return run_jacobian_t<double>(s);
+    case 1: return run_jacobian_t<float>(s);
+    default: return run_jacobian_t<__nv_bfloat16>(s);
+  }
+}
+
+int run_sumsq(Solver* s, const double* v, long long n, double* out_dev) {
+  int rc = launch(s, T_KRYLOV, [&] { k_sumsq<<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, v, s->d_part); });
+  if (rc) return rc;
+  return launch(s, T_KRYLOV, [&] { k_sum_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->d_part, out_dev); });
+}
+
+// nsweeps of multicolour block symmetric Gauss-Seidel on A x = b from the
+// current x (CRS::SGS, ucs/crs.tcc:62).  The reference sweeps rows in index
+// order; here rows of one colour (no two adjacent) update together and the
+// colours are swept forward then backward, the GPU form of the same
+// smoother.  Returns |norm(x_last) - norm(x_previous)| as the reference does.
+template <class T>
+int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
+  const T* M = (const T*)s->d_M;
+  const double cnt = (double)s->nnode * NEQN;
+  double prev = 0.0, cur = 0.0;
+  for (int sw = 0; sw < nsweeps; sw++) {
+    for (int dir = 0; dir < 2; dir++) {
+      for (int cc = 0; cc < s->ncolor; cc++) {
+        int c = dir == 0 ? cc : s->ncolor - 1 - cc;
+        int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
+        if (nr == 0) continue;
+        int rc = launch(s, T_SGS, [&] {
+          k_sgs_color<T><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M, s->d_dlu,
+                                                            s->d_piv, b, x);
+        });
+        if (rc) return rc;
+      }
+    }
+    if (dnorm && sw >= nsweeps - 2) {
+      int rc = run_sumsq(s, x, (long long)s->nnode * NEQN, s->d_scal + 2);
+      if (rc) return rc;
+      double v;
+      CUDA_TRY(cudaMemcpyAsync(&v, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+      CUDA_TRY(cudaStreamSynchronize(s->stream));
+      prev = cur;
+      cur = std::sqrt(v) / cnt;
+    }
+  }
+  if (dnorm) *dnorm = std::fabs((nsweeps >= 2 ? prev : 0.0) - cur);
+  return PCFD_OK;
+}
+
+int run_sgs(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "sgs: no Jacobian assembled");
+  switch (s->jac_prec) {
+    case 0: return run_sgs_t<double>(s, nsweeps, b, x, dnorm);
+    case 1: return run_sgs_t<float>(s, nsweeps, b, x, dnorm);
+    default: return run_sgs_t<__nv_bfloat16>(s, nsweeps, b, x, dnorm);
+  }
+}
+
+int run_apply_dq(Solver* s, double* dqnorm) {
+  int rc = launch(s, T_UPDATE, [&] {
+    k_apply_dq<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->prm.gamma, s->d_x, s->d_q, s->d_part,
+                                                           s->d_health);
+  });
+  if (rc) return rc;
+  rc = launch(s, T_UPDATE, [&] { k_sum_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->d_part, s->d_scal + 3); });
+  if (rc) return rc;
+  s->have_grad = s->have_lim = 0;
+  if (dqnorm) {
+    double v;
+    CUDA_TRY(cudaMemcpyAsync(&v, s->d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *dqnorm = std::sqrt(v) / ((double)s->nnode * NEQN);
+  }
+  return PCFD_OK;
+}
+
+
+// ---- FGMRES -----------------------------------------------------------------
+
+template <class T>
+int run_spmv_t(Solver* s, const double* x, double* y) {
+  return launch(s, T_SPMV, [&] {
+    k_spmv<T><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M, s->d_diag, x, y);
+  });
+}
+
+int run_spmv(Solver* s, const double* x, double* y) {
+  switch (s->jac_prec) {
+    case 0: return run_spmv_t<double>(s, x, y);
+    case 1: return run_spmv_t<float>(s, x, y);
+    default: return run_spmv_t<__nv_bfloat16>(s, x, y);
+  }
+}
+
+int ensure_krylov(Solver* s, int m) {
+  if (s->fg_m >= m && s->d_V) return PCFD_OK;
+  if (s->d_V) cudaFree(s->d_V);
+  if (s->d_Z) cudaFree(s->d_Z);
+  if (s->d_w) cudaFree(s->d_w);
+  if (s->d_dots) cudaFree(s->d_dots);
+  s->d_V = s->d_Z = s->d_w = s->d_dots = nullptr;
+  const size_t n = (size_t)s->nnode * NEQN;
+  int rc;
+  if ((rc = dalloc(&s->d_V, n * (m + 1)))) return rc;
+  if ((rc = dalloc(&s->d_Z, n * m))) return rc;
+  if ((rc = dalloc(&s->d_w, n))) return rc;
+  if ((rc = dalloc(&s->d_dots, (size_t)kNormBlocks * (m + 2) + 2 * (m + 2)))) return rc;
+  s->fg_m = m;
+  return PCFD_OK;
+}
+
+// dots[k] = (w, V_k), k < nv, copied to the host
+int run_mdot(Solver* s, const double* V, int nv, const double* w, double* host_out) {
+  const long long n = (long long)s->nnode * NEQN;
+  const int stride = s->fg_m + 2;
+  double* part = s->d_dots;
+  double* res = s->d_dots + (size_t)kNormBlocks * stride;
+  int rc = launch(s, T_KRYLOV, [&] { k_mdot<<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride); });
+  if (rc) return rc;
+  rc = launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res); });
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(host_out, res, nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+// Restarted flexible GMRES, right-preconditioned by nsgs block-SGS sweeps,
+// classical Gram-Schmidt with one re-orthogonalisation (batched dot
+// products), Givens rotations on the host.  FGMRES has no counterpart on the
+// reference's Newton path: its CRS::GMRES (ucs/crs.tcc:176) is a fixed-
+// preconditioner restarted GMRES used by the design modes only.
+int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters) {
+  const int m = std::max(1, std::min(o->fgmres_m > 0 ? o->fgmres_m : 30, 60));
+  const int restarts = std::max(1, o->fgmres_restarts);
+  const double rtol = o->fgmres_rtol > 0.0 ? o->fgmres_rtol : 1e-3;
+  int rc = ensure_krylov(s, m);
+  if (rc) return rc;
+  const long long n = (long long)s->nnode * NEQN;
+  double* V = s->d_V;
+  double* Z = s->d_Z;
+  double* w = s->d_w;
+  double* hdev = s->d_dots + (size_t)kNormBlocks * (s->fg_m + 2) + (s->fg_m + 2);
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), hcol(m + 2), y(m);
+  double beta0 = -1.0;
+  int total = 0;
+  double rel = 1.0;
+  for (int rs = 0; rs < restarts; rs++) {
+    // r = b - A x  (x is zero on the first pass)
+    if (rs == 0) {
+      CUDA_TRY(cudaMemcpyAsync(w, s->d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+    } else {
+      if ((rc = run_spmv(s, s->d_x, w))) return rc;
+      if ((rc = launch(s, T_KRYLOV, [&] { k_residual_vec<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_b, w); }))) return rc;
+    }
+    double bb;
+    if ((rc = run_mdot(s, w, 1, w, &bb))) return rc;
+    double beta = std::sqrt(bb);
+    if (beta0 < 0.0) beta0 = beta;
+    if (beta == 0.0 || beta0 == 0.0) { rel = 0.0; break; }
+    if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<<<kNormBlocks, 256, 0, s->stream>>>(n, 1.0 / beta, w, V); }))) return rc;
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    for (; j < m; j++) {
+      double* zj = Z + (size_t)j * n;
+      CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(double), s->stream));
+      if ((rc = run_sgs(s, std::max(1, o->nsgs), V + (size_t)j * n, zj, nullptr))) return rc;
+      if ((rc = run_spmv(s, zj, w))) return rc;
+      // CGS2
+      for (int k = 0; k <= j + 1; k++) hcol[k] = 0.0;
+      for (int pass = 0; pass < 2; pass++) {
+        std::vector<double> d(j + 1);
+        if ((rc = run_mdot(s, V, j + 1, w, d.data()))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(hdev, d.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, hdev, w); })))
+          return rc;
+        for (int k = 0; k <= j; k++) hcol[k] += d[k];
+      }
+      double ww;
+      if ((rc = run_mdot(s, w, 1, w, &ww))) return rc;
+      double hn = std::sqrt(ww);
+      hcol[j + 1] = hn;
+      if (hn > 0.0) {
+        double* vn = V + (size_t)(j + 1) * n;
+        if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<<<kNormBlocks, 256, 0, s->stream>>>(n, 1.0 / hn, w, vn); })))
+          return rc;
+      }
+      // apply previous rotations, then a new one
+      for (int k = 0; k < j; k++) {
+        double t = cs[k] * hcol[k] + sn[k] * hcol[k + 1];
+        hcol[k + 1] = -sn[k] * hcol[k] + cs[k] * hcol[k + 1];
+        hcol[k] = t;
+      }
+      double den = std::sqrt(hcol[j] * hcol[j] + hcol[j + 1] * hcol[j + 1]);
+      cs[j] = den > 0.0 ? hcol[j] / den : 1.0;
+      sn[j] = den > 0.0 ? hcol[j + 1] / den : 0.0;
+      hcol[j] = den;
+      hcol[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      for (int k = 0; k <= j; k++) H[(size_t)k * m + j] = hcol[k];
+      total++;
+      rel = std::fabs(g[j + 1]) / beta0;
+      if (rel < rtol || hn == 0.0) { j++; break; }
+    }
+    // back substitution and x += Z y
+    for (int k = j - 1; k >= 0; k--) {
+      double t = g[k];
+      for (int q = k + 1; q < j; q++) t -= H[(size_t)k * m + q] * y[q];
+      y[k] = t / H[(size_t)k * m + k];
+    }
+    CUDA_TRY(cudaMemcpyAsync(hdev, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    if ((rc = launch(s, T_KRYLOV, [&] { k_combine<<<kNormBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
+      return rc;
+    if (rel < rtol) break;
+  }
+  if (relres) *relres = rel;
+  if (iters) *iters = total;
+  return PCFD_OK;
 }
 
 }  // namespace
@@ -905,6 +1415,8 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     return set_err(PCFD_ERR_ARG, "pcfd_create: null mesh array");
   if (prm->gamma <= 1.0 || prm->sorder < 1 || prm->sorder > 2 || prm->ntags <= 0 || !prm->bc_type || !prm->bc_twall)
     return set_err(PCFD_ERR_ARG, "pcfd_create: bad parameters");
+  if (prm->jac_boundary_eval < 0 || prm->jac_boundary_eval > 3)
+    return set_err(PCFD_ERR_ARG, "pcfd_create: jac_boundary_eval must be 0, 1, 2 or 3");
   if (prm->limiter != 0 && prm->limiter != 3)
     return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: only limiter 0 (off) and 3 (modified Venkatakrishnan)");
   if (prm->viscous && (prm->Re <= 0.0 || prm->Pr <= 0.0 || prm->ref_temperature <= 0.0))
@@ -980,7 +1492,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     std::vector<int> fill(bptr.begin(), bptr.end() - 1);
     for (long long k = 0; k < nb; k++) bhe[fill[m->bedges[2 * k]]++] = (int)k;
   }
-  std::vector<int> gnode, gptr(1, 0);
+  std::vector<int> gnode, gptr(1, 0), bghe_list;
   for (long long i = 0; i < nn; i++)
     if (bptr[i + 1] > bptr[i]) {
       gnode.push_back((int)i);
@@ -1002,6 +1514,27 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   s->bc_sequential = 0;
   for (long long k = 0; k < nb; k++)
     if (bnrm[k] >= 0 && hardset[bnrm[k]]) s->bc_sequential = 1;
+  // nodes no condition hard-sets get one thread per half-edge; the rest keep
+  // their half-edges in order on one thread
+  std::vector<int> bind;
+  {
+    std::vector<int> gnode2, gptr2(1, 0), ghe2;
+    for (size_t g = 0; g < gnode.size(); g++) {
+      int node = gnode[g];
+      if (!hardset[node]) {
+        for (int p = gptr[g]; p < gptr[g + 1]; p++) bind.push_back(bhe[p]);
+      } else {
+        gnode2.push_back(node);
+        for (int p = gptr[g]; p < gptr[g + 1]; p++) ghe2.push_back(bhe[p]);
+        gptr2.push_back((int)ghe2.size());
+      }
+    }
+    gnode.swap(gnode2);
+    gptr.swap(gptr2);
+    bghe_list.swap(ghe2);
+  }
+  s->nbgroup = (int)gnode.size();
+  s->nbind = (int)bind.size();
 
   std::vector<int2> en(ne), bn(nb);
   std::vector<D4> ea(ne), ba(nb);
@@ -1032,7 +1565,16 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dput(&s->d_bhe, bhe.data(), nb));
   TRY(dput(&s->d_bgnode, gnode.data(), gnode.size()));
   TRY(dput(&s->d_bgptr, gptr.data(), gptr.size()));
-  TRY(dput(&s->d_bghe, bhe.data(), nb));  // groups are the non-empty bptr rows, same order
+  TRY(dput(&s->d_bghe, bghe_list.data(), bghe_list.size()));
+  TRY(dput(&s->d_bind, bind.data(), bind.size()));
+  TRY(dalloc(&s->d_clipflag, (size_t)nn));
+  TRY(dalloc(&s->d_limraw, (size_t)nn * NEQN));
+  TRY(dalloc(&s->d_clipany, 1));
+  if (cudaMemsetAsync(s->d_clipflag, 0, sizeof(int) * (size_t)nn, s->stream) != cudaSuccess ||
+      cudaMemsetAsync(s->d_clipany, 0, sizeof(int), s->stream) != cudaSuccess) {
+    free_solver(s);
+    return set_err(PCFD_ERR_CUDA, "memset clip flags");
+  }
   TRY(dalloc(&s->d_eh, 3 * ne));
   TRY(dalloc(&s->d_lsq, 3 * 2 * ne));
   TRY(dalloc(&s->d_q, (size_t)s->ntot * NVARS));
@@ -1075,6 +1617,73 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
       free_solver(s);
       return set_err(PCFD_ERR_CUDA, "limiter init");
     }
+  }
+  // --- implicit system structure: block CRS exactly as CRSMatrix::Init
+  // (ucs/crsmatrix.tcc:48), the block of each edge located once here instead
+  // of by GetPointer's row search on every access (:740), and a greedy
+  // colouring of the node graph for the Gauss-Seidel sweeps
+  {
+    std::vector<int> ia(nn + 1), ja;
+    ia[0] = 0;
+    for (long long i = 0; i < nn; i++) ia[i + 1] = ia[i] + (m->ipsp[i + 1] - m->ipsp[i]) + 1;
+    s->nblocks = ia[nn];
+    ja.resize(s->nblocks);
+    for (long long i = 0; i < nn; i++) {
+      int c = ia[i];
+      ja[c++] = (int)i;
+      for (int k = m->ipsp[i]; k < m->ipsp[i + 1]; k++) ja[c++] = m->psp[k];
+    }
+    std::vector<int> pos_lr(ne), pos_rl(ne);
+    auto find = [&](int row, int col) {
+      for (int b = ia[row] + 1; b < ia[row + 1]; b++)
+        if (ja[b] == col) return b;
+      return -1;
+    };
+    for (long long e = 0; e < ne; e++) {
+      int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+      pos_lr[e] = find(a, b);
+      pos_rl[e] = find(b, a);
+      if (pos_lr[e] < 0 || pos_rl[e] < 0) {
+        free_solver(s);
+        return set_err(PCFD_ERR_ARG, "pcfd_create: edge missing from psp (maps inconsistent)");
+      }
+    }
+    // colouring: smallest colour not used by an already coloured neighbour
+    std::vector<int> color(nn, -1);
+    int ncol = 0;
+    std::vector<int> mark(64, -1);
+    for (long long i = 0; i < nn; i++) {
+      for (int k = m->ipsp[i]; k < m->ipsp[i + 1]; k++) {
+        int c = color[m->psp[k]];
+        if (c >= 0) {
+          if (c >= (int)mark.size()) mark.resize(c + 1, -1);
+          mark[c] = (int)i;
+        }
+      }
+      int c = 0;
+      while (c < (int)mark.size() && mark[c] == (int)i) c++;
+      if (c >= (int)mark.size()) mark.resize(c + 1, -1);
+      color[i] = c;
+      ncol = std::max(ncol, c + 1);
+    }
+    s->ncolor = ncol;
+    s->color_ptr.assign(ncol + 1, 0);
+    for (long long i = 0; i < nn; i++) s->color_ptr[color[i] + 1]++;
+    for (int c = 0; c < ncol; c++) s->color_ptr[c + 1] += s->color_ptr[c];
+    std::vector<int> rows(nn), fill(s->color_ptr.begin(), s->color_ptr.end() - 1);
+    for (long long i = 0; i < nn; i++) rows[fill[color[i]]++] = (int)i;
+    TRY(dput(&s->d_ia, ia.data(), ia.size()));
+    TRY(dput(&s->d_ja, ja.data(), ja.size()));
+    TRY(dput(&s->d_pos_lr, pos_lr.data(), pos_lr.size()));
+    TRY(dput(&s->d_pos_rl, pos_rl.data(), pos_rl.size()));
+    TRY(dput(&s->d_color_rows, rows.data(), rows.size()));
+    TRY(dalloc(&s->d_diag, (size_t)nn * 25));
+    TRY(dalloc(&s->d_dlu, (size_t)nn * 25));
+    TRY(dalloc(&s->d_piv, (size_t)nn * 5));
+    TRY(dalloc(&s->d_bblk, (size_t)std::max<long long>(nb, 1) * 25));
+    TRY(dalloc(&s->d_dt, (size_t)nn));
+    TRY(dalloc(&s->d_x, (size_t)nn * NEQN));
+    TRY(dalloc(&s->d_scal, 16));
   }
 #undef TRY
   *out = (pcfd_solver_t)s;
@@ -1139,7 +1748,7 @@ PCFD_API int pcfd_limiter(pcfd_solver_t h, double* l_out) {
   Solver* s = (Solver*)h;
   if (!s) return set_err(PCFD_ERR_ARG, "pcfd_limiter: null handle");
   if (s->prm.limiter != 0 && !s->have_grad) return set_err(PCFD_ERR_STATE, "pcfd_limiter: gradient not computed");
-  int rc = run_limiter(s);
+  int rc = run_limiter(s, true);
   if (rc) return rc;
   if (l_out)
     CUDA_TRY(cudaMemcpyAsync(l_out, s->d_lim, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1170,7 +1779,7 @@ PCFD_API int pcfd_residual_full(pcfd_solver_t h, double* norms_out) {
   if ((rc = run_bcs(s))) return rc;
   if (need_grad) {
     if ((rc = run_gradient(s))) return rc;
-    if (s->prm.sorder > 1 && (rc = run_limiter(s))) return rc;
+    if (s->prm.sorder > 1 && (rc = run_limiter(s, false))) return rc;
   }
   if ((rc = run_residual(s))) return rc;
   if (norms_out)
@@ -1193,7 +1802,7 @@ PCFD_API int pcfd_bench_residual_full(pcfd_solver_t h, int nsteps, double* ms_ou
   for (int it = 0; it < nsteps && rc == PCFD_OK; it++) {
     rc = run_bcs(s);
     if (!rc && need_grad) rc = run_gradient(s);
-    if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s);
+    if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s, false);
     if (!rc) rc = run_residual(s);
   }
   cudaEventRecord(e1, s->stream);
@@ -1223,6 +1832,164 @@ PCFD_API int pcfd_set_device(int device) {
 
 PCFD_API int pcfd_device_sync(void) {
   CUDA_TRY(cudaDeviceSynchronize());
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_timestep(pcfd_solver_t h, double cfl, double* dt_out, double* dtmin) {
+  Solver* s = (Solver*)h;
+  if (!s || !(cfl > 0.0)) return set_err(PCFD_ERR_ARG, "pcfd_timestep: bad arguments");
+  int rc = run_timestep(s, cfl);
+  if (rc) return rc;
+  if (dt_out)
+    CUDA_TRY(cudaMemcpyAsync(dt_out, s->d_dt, (size_t)s->nnode * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (dtmin) CUDA_TRY(cudaMemcpyAsync(dtmin, s->d_scal + 0, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_jacobian_precision(pcfd_solver_t h, int precision) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_set_jacobian_precision: null handle");
+  int rc = ensure_matrix(s, precision);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_jacobian(pcfd_solver_t h) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_jacobian: null handle");
+  int rc = run_jacobian(s);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_get_jacobian(pcfd_solver_t h, double* blocks, long long nblocks) {
+  Solver* s = (Solver*)h;
+  if (!s || !blocks || nblocks != s->nblocks) return set_err(PCFD_ERR_ARG, "pcfd_get_jacobian: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_get_jacobian: no Jacobian assembled");
+  const size_t nv = (size_t)s->nblocks * 25;
+  std::vector<double> out(nv);
+  std::vector<char> raw(nv * prec_bytes(s->jac_prec));
+  CUDA_TRY(cudaMemcpyAsync(raw.data(), s->d_M, raw.size(), cudaMemcpyDeviceToHost, s->stream));
+  std::vector<double> diag((size_t)s->nnode * 25);
+  std::vector<int> ia(s->nnode + 1);
+  CUDA_TRY(cudaMemcpyAsync(diag.data(), s->d_diag, diag.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(ia.data(), s->d_ia, ia.size() * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  for (size_t i = 0; i < nv; i++) {
+    if (s->jac_prec == 0) out[i] = ((double*)raw.data())[i];
+    else if (s->jac_prec == 1) out[i] = ((float*)raw.data())[i];
+    else {
+      uint16_t b = ((uint16_t*)raw.data())[i];
+      uint32_t u = (uint32_t)b << 16;
+      float f;
+      std::memcpy(&f, &u, 4);
+      out[i] = f;
+    }
+  }
+  for (int i = 0; i < s->nnode; i++)
+    for (int t = 0; t < 25; t++) out[(size_t)ia[i] * 25 + t] = diag[(size_t)i * 25 + t];
+  std::memcpy(blocks, out.data(), nv * sizeof(double));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_crs_structure(pcfd_solver_t h, int* ia, int* ja, int* ncolor) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_crs_structure: null handle");
+  if (ia) CUDA_TRY(cudaMemcpy(ia, s->d_ia, (size_t)(s->nnode + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (ja) CUDA_TRY(cudaMemcpy(ja, s->d_ja, (size_t)s->nblocks * sizeof(int), cudaMemcpyDeviceToHost));
+  if (ncolor) *ncolor = s->ncolor;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_coloring(pcfd_solver_t h, int* color_ptr, int* rows) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_coloring: null handle");
+  if (color_ptr) std::memcpy(color_ptr, s->color_ptr.data(), s->color_ptr.size() * sizeof(int));
+  if (rows) CUDA_TRY(cudaMemcpy(rows, s->d_color_rows, (size_t)s->nnode * sizeof(int), cudaMemcpyDeviceToHost));
+  return PCFD_OK;
+}
+
+PCFD_API long long pcfd_nblocks(pcfd_solver_t h) {
+  Solver* s = (Solver*)h;
+  return s ? s->nblocks : -1;
+}
+
+PCFD_API int pcfd_sgs(pcfd_solver_t h, int nsweeps, double* x_out, double* dnorm) {
+  Solver* s = (Solver*)h;
+  if (!s || nsweeps < 0) return set_err(PCFD_ERR_ARG, "pcfd_sgs: bad arguments");
+  CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));
+  int rc = run_sgs(s, nsweeps, s->d_b, s->d_x, dnorm);
+  if (rc) return rc;
+  if (x_out)
+    CUDA_TRY(cudaMemcpyAsync(x_out, s->d_x, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
+                             s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_apply_dq(pcfd_solver_t h, const double* x_in, double* dqnorm) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "pcfd_apply_dq: null handle");
+  if (x_in)
+    CUDA_TRY(cudaMemcpyAsync(s->d_x, x_in, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyHostToDevice,
+                             s->stream));
+  int rc = run_apply_dq(s, dqnorm);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_newton_report* rep) {
+  Solver* s = (Solver*)h;
+  if (!s || !o || o->iter < 1 || o->nsgs < 0 || !(o->cfl > 0.0))
+    return set_err(PCFD_ERR_ARG, "pcfd_newton_step: bad arguments");
+  if (o->linear_solver != 0 && o->linear_solver != 1)
+    return set_err(PCFD_ERR_ARG, "pcfd_newton_step: linear_solver must be 0 (SGS) or 1 (FGMRES)");
+  int rc;
+  if (o->jac_precision != s->jac_prec && (rc = ensure_matrix(s, o->jac_precision))) return rc;
+  const double cfl = ramp_cfl(o->iter, o->cfl_start > 0.0 ? o->cfl_start : o->cfl, o->cfl, o->cfl_ramp_steps);
+  // SolutionSpace::PreIterate (ucs/solutionSpace.tcc:510): a time step exists
+  // before the first Jacobian
+  if (!s->have_dt && (rc = run_timestep(s, cfl))) return rc;
+  // PreTimeAdvance (:573): Jacobian with the time step of the previous
+  // iteration, then this iteration's CFL and time steps
+  const int jf = o->jac_update_freq > 0 ? o->jac_update_freq : 1;
+  if (o->nsgs > 0 && (o->iter % jf == 0 || o->iter == 1 || !s->have_jac) && (rc = run_jacobian(s))) return rc;
+  if ((rc = run_timestep(s, cfl))) return rc;
+  // NewtonIterate (:640)
+  if ((rc = run_bcs(s))) return rc;
+  const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
+  if (need_grad && (rc = run_gradient(s))) return rc;
+  if (need_grad && s->prm.sorder > 1 && (rc = run_limiter(s, false))) return rc;
+  if ((rc = run_residual(s))) return rc;
+  double lin = 0.0;
+  int lin_it = 0;
+  CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));
+  if (o->nsgs > 0) {
+    if (o->linear_solver == 0) {
+      if ((rc = run_sgs(s, o->nsgs, s->d_b, s->d_x, &lin))) return rc;
+      lin_it = o->nsgs;
+    } else {
+      if ((rc = run_fgmres(s, o, &lin, &lin_it))) return rc;
+    }
+  }
+  double dqn = 0.0;
+  if ((rc = run_apply_dq(s, &dqn))) return rc;
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    CUDA_TRY(cudaMemcpyAsync(rep->res, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(&rep->dtmin, s->d_scal + 0, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    rep->dqnorm = dqn;
+    rep->lin_res = lin;
+    rep->lin_iters = lin_it;
+    rep->cfl = cfl;
+  } else {
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
   return PCFD_OK;
 }
 

@@ -33,6 +33,13 @@ def lib():
             "oracle_residual": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _LLP]),
             "oracle_residual_scaled": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _DP, _LLP]),
             "oracle_lu": (C.c_int, [_DP, _IP, C.c_int]),
+            "oracle_timestep": (C.c_double, [MV, PP, _DP, C.c_double, _DP]),
+            "oracle_crs_init": (None, [MV, _IP, _IP]),
+            "oracle_prepare_sgs": (None, [C.c_int, _IP, _DP, _IP]),
+            "oracle_jacobian": (C.c_int, [MV, PP, _DP, _DP, _IP, _IP, _DP]),
+            "oracle_sgs": (C.c_double, [C.c_int, _IP, _IP, _DP, _IP, _DP, _DP, C.c_int]),
+            "oracle_sgs_colored": (None, [C.c_int, _IP, _IP, _DP, _IP, _DP, _DP, C.c_int, C.c_int, _IP, _IP]),
+            "oracle_apply_dq": (C.c_double, [MV, PP, _DP, _DP]),
             "oracle_lusolve": (None, [_DP, _DP, _IP, _DP, C.c_int]),
             "oracle_matvec": (None, [_DP, _DP, _DP, C.c_int]),
             "oracle_tri_area": (None, [_DP, _DP, _DP, _DP]),
@@ -115,3 +122,87 @@ class OracleSpace:
             l, _ = self.limiter(q, g)
         b, norms, _ = self.residual(q, g, l)
         return q, g, l, b, norms
+
+
+class OracleImplicit(OracleSpace):
+    """The reference's implicit iteration on the CPU: time step, FD Jacobian,
+    diagonal LU, lexicographic block SGS, ApplyDQ (test infrastructure)."""
+
+    def __init__(self, mesh, param):
+        super().__init__(mesh, param)
+        n = mesh.nnode
+        self.ia = np.zeros(n + 1, dtype=np.int32)
+        self.ja = np.zeros(n + 2 * mesh.nedge, dtype=np.int32)
+        self.L.oracle_crs_init(C.byref(mesh.view), ip(self.ia), ip(self.ja))
+        self.dt = None
+
+    def timestep(self, q, cfl):
+        dt = np.zeros(self.mesh.nnode)
+        dtmin = self.L.oracle_timestep(C.byref(self.mesh.view), C.byref(self.cp), dp(np.ascontiguousarray(q)),
+                                       float(cfl), dp(dt))
+        return dt, dtmin
+
+    def jacobian(self, q, dt):
+        """Returns (M, q) - the reference's Jacobian modifies the state."""
+        q = np.ascontiguousarray(q, dtype=np.float64).copy()
+        M = np.zeros((len(self.ja), 25))
+        assert self.L.oracle_jacobian(C.byref(self.mesh.view), C.byref(self.cp), dp(q), dp(np.ascontiguousarray(dt)),
+                                      ip(self.ia), ip(self.ja), dp(M)) == 0
+        return M, q
+
+    def lu(self, M):
+        M = M.copy()
+        pv = np.zeros(self.mesh.nnode * 5, dtype=np.int32)
+        self.L.oracle_prepare_sgs(self.mesh.nnode, ip(self.ia), dp(M), ip(pv))
+        return M, pv
+
+    def sgs(self, Mlu, pv, b, nsweeps):
+        x = np.zeros((self.mesh.nnode, 5))
+        d = self.L.oracle_sgs(self.mesh.nnode, ip(self.ia), ip(self.ja), dp(Mlu), ip(pv),
+                              dp(np.ascontiguousarray(b)), dp(x), int(nsweeps))
+        return x, d
+
+    def sgs_colored(self, Mlu, pv, b, nsweeps, cptr, rows):
+        x = np.zeros((self.mesh.nnode, 5))
+        self.L.oracle_sgs_colored(self.mesh.nnode, ip(self.ia), ip(self.ja), dp(Mlu), ip(pv),
+                                  dp(np.ascontiguousarray(b)), dp(x), int(nsweeps), len(cptr) - 1,
+                                  ip(np.ascontiguousarray(cptr, dtype=np.int32)),
+                                  ip(np.ascontiguousarray(rows, dtype=np.int32)))
+        return x
+
+    def apply_dq(self, x, q):
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        q = np.ascontiguousarray(q, dtype=np.float64).copy()
+        dn = self.L.oracle_apply_dq(C.byref(self.mesh.view), C.byref(self.cp), dp(x), dp(q))
+        return q, dn
+
+    def newton(self, q, nsteps, cfl=5.0, nsgs=10, cfl_start=0.0, cfl_ramp_steps=0, coloring=None):
+        """Solve's loop with PreIterate, PreTimeAdvance and NewtonIterate in
+        the reference's order; returns the final q and the resGlobal history."""
+        def ramp(it):
+            cs = cfl_start if cfl_start > 0 else cfl
+            if cfl_ramp_steps > 0 and it < cfl_ramp_steps:
+                return (cfl - cs) / cfl_ramp_steps * it + cs
+            return cfl
+        q = np.ascontiguousarray(q, dtype=np.float64).copy()
+        dt, _ = self.timestep(q, ramp(1))
+        hist = []
+        for it in range(1, nsteps + 1):
+            M, q = self.jacobian(q, dt)
+            dt, _ = self.timestep(q, ramp(it))
+            q = self.update_bcs(q)
+            p = self.param
+            g = l = None
+            if p.sorder > 1 or p.viscous:
+                g = self.gradient(q)
+            if p.sorder > 1:
+                l, _ = self.limiter(q, g)
+            b, norms, _ = self.residual(q, g, l)
+            hist.append(norms[0])
+            Mlu, pv = self.lu(M)
+            if coloring is None:
+                x, _ = self.sgs(Mlu, pv, b, nsgs)
+            else:
+                x = self.sgs_colored(Mlu, pv, b, nsgs, *coloring)
+            q, _ = self.apply_dq(x, q)
+        return q, hist

@@ -1,0 +1,141 @@
+"""Implicit part on the GPU against the oracle, through the C ABI: local
+time step, finite-difference Jacobian in block CRS, the multicolour block
+Gauss-Seidel kernel, and whole Newton iterations."""
+import numpy as np
+import pytest
+
+from oracle_lib import OracleImplicit
+from parity import assert_field_close
+from proteuscfd_gb300 import SolutionSpace, cases
+from proteuscfd_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def euler_case(beval=1):
+    c = cases.euler_ramp(14, 9, 7, seed=4)
+    c.param.jac_boundary_eval = beval
+    return c
+
+
+def ns_case(beval=0):
+    c = cases.ns_flatplate(11, 9, 7, seed=5, venkat_K=1.0)
+    c.param.jac_boundary_eval = beval
+    return c
+
+
+CASES = [euler_case(0), euler_case(1), ns_case(0), ns_case(3)]
+IDS = ["euler_beval0", "euler_beval1", "ns_beval0", "ns_beval3"]
+
+
+def setup(case, seed=1):
+    m = cases.build_mesh(case)
+    S = SolutionSpace(m, case.param)
+    O = OracleImplicit(m, case.param)
+    q0 = cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, seed)
+    return m, S, O, q0
+
+
+@pytest.mark.parametrize("case", CASES[::2], ids=IDS[::2])
+def test_timestep_parity(case):
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    dt, dtmin = S.compute_timesteps(7.5)
+    dto, dtmino = O.timestep(q0, 7.5)
+    assert np.allclose(dt, dto, rtol=1e-13, atol=0)
+    assert abs(dtmin - dtmino) <= 1e-13 * dtmino
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_jacobian_parity_fp64(case):
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    S.update_bcs()
+    q1 = S.get_state()
+    dt, _ = S.compute_timesteps(5.0)
+    S.compute_jacobians()
+    Mg = S.get_jacobian()
+    ia, ja, nc = S.crs_structure()
+    assert np.array_equal(ia, O.ia) and np.array_equal(ja, O.ja)
+    qo = O.update_bcs(q0)
+    dto, _ = O.timestep(qo, 5.0)
+    Mo, qo2 = O.jacobian(qo, dto)
+    # the state after the Jacobian's boundary pass matches
+    assert_field_close(S.get_state(), qo2, 1e-12, "state after Jacobian BC pass")
+    # finite differences with h = 1e-8 turn flux rounding into ~1e-8
+    # relative noise, so blocks agree to 1e-6 of their own magnitude
+    scale = np.abs(Mo).max(axis=1, keepdims=True) + 1e-300
+    err = (np.abs(Mg - Mo) / scale).max()
+    assert err < 1e-6, err
+    assert S.health()[7] == 0
+
+
+def test_jacobian_storage_precisions():
+    case = ns_case(3)
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    S.compute_timesteps(5.0)
+    out = {}
+    for prec in (0, 1, 2):
+        S.set_state(q0)
+        S.set_jacobian_precision(prec)
+        S.compute_jacobians()
+        out[prec] = S.get_jacobian()
+    ref = out[0]
+    scale = np.abs(ref).max(axis=1, keepdims=True) + 1e-300
+    assert (np.abs(out[1] - ref) / scale).max() < 1e-6    # FP32 storage
+    assert (np.abs(out[2] - ref) / scale).max() < 1e-2    # BF16 storage
+
+
+@pytest.mark.parametrize("case", [CASES[1], CASES[3]], ids=[IDS[1], IDS[3]])
+def test_sgs_kernel_matches_colored_oracle(case):
+    """The GPU sweep kernel is the oracle's row update in the GPU's colour
+    order (same arithmetic, different order from the reference's
+    lexicographic sweep)."""
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    S.compute_timesteps(5.0)
+    S.compute_jacobians()
+    S.residual_full()
+    b = S.compute_residuals()[0]
+    x, _ = S.sgs(4)
+    M = S.get_jacobian()
+    Mlu, pv = O.lu(M)
+    cptr, rows = S.coloring()
+    xo = O.sgs_colored(Mlu, pv, b, 4, cptr, rows)
+    assert_field_close(x, xo, 1e-11, "SGS solution")
+    # and it is a good approximate solve of the same system
+    xl, _ = O.sgs(Mlu, pv, b, 4)
+    assert np.linalg.norm(x - xl) < 0.5 * np.linalg.norm(xl)
+
+
+@pytest.mark.parametrize("case", [CASES[1], CASES[3]], ids=[IDS[1], IDS[3]])
+def test_newton_iterates_match_oracle(case):
+    """Three outer iterations on the GPU against the oracle's iteration with
+    the same colour order; FD Jacobian noise (~1e-8) bounds the agreement."""
+    m, S, O, q0 = setup(case)
+    # start from a state the boundary conditions have already been applied
+    # to, as after any earlier iteration
+    q0 = O.update_bcs(q0)
+    S.set_state(q0)
+    hist = []
+    for it in range(1, 4):
+        rep = S.newton_iterate(it, cfl=5.0, nsgs=6)
+        hist.append(rep["res"][0])
+    qg = S.get_state()
+    qo, ho = O.newton(q0, 3, cfl=5.0, nsgs=6, coloring=S.coloring())
+    assert np.allclose(hist, ho, rtol=1e-9, atol=0), (hist, ho)
+    n = m.nnode
+    assert_field_close(qg[:n, :5], qo[:n, :5], 1e-7, "q after 3 Newton iterations")
+
+
+def test_fgmres_reduces_linear_residual():
+    case = ns_case(3)
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    for prec in (0, 1):
+        S.set_state(q0)
+        rep = S.newton_iterate(1, cfl=20.0, nsgs=1, linear_solver=1, fgmres_m=20, fgmres_restarts=2,
+                               fgmres_rtol=1e-6, jac_precision=prec)
+        assert rep["lin_res"] < 1e-6, rep
+        assert np.isfinite(rep["dqnorm"]) and rep["dqnorm"] > 0
