@@ -189,17 +189,32 @@ def run_gb300(args, ws, rank, local, pg):
     S = SolutionSpace(m, case.param)
     nrows = m.nnode + m.nbedge
     q0 = cases.perturbed_state(S.qinf(), nrows, seed=1)
-    S.set_state(q0)
-    S.bench_residual_full(max(args.warmup, 3))
-    # timed region: K steps on the device, inputs resident in HBM
-    barrier(pg)
-    N.check(lib.pcfd_device_sync(), "sync")
-    l0 = S.launch_count()
-    with ClockSampler(local) as clk:
-        ms, norms = S.bench_residual_full(args.steps)
-    launches = S.launch_count() - l0
-    barrier(pg)
-    ms = max_over_ranks(pg, ms)
+
+    def timed(arith):
+        """K device-timed steps of the residual in the given arithmetic."""
+        S.set_residual_arithmetic(arith)
+        S.set_state(q0)
+        S.bench_residual_full(max(args.warmup, 3))
+        barrier(pg)
+        N.check(lib.pcfd_device_sync(), "sync")
+        l0 = S.launch_count()
+        with ClockSampler(local) as clk:
+            ms, norms = S.bench_residual_full(args.steps)
+        launches = S.launch_count() - l0
+        barrier(pg)
+        return max_over_ranks(pg, ms), norms, launches, clk
+
+    # reference precision first, then the double-float kernels; the headline
+    # uses double-float only when its norms agree with FP64 to 1e-10
+    arith_names = {0: "f64", 1: "df64 (FP32 pair, ~48-bit significand)"}
+    ms64, norms64, launches64, clk64 = timed(0)
+    results = {0: (ms64, norms64, launches64, clk64)}
+    if args.arith in ("df", "best"):
+        results[1] = timed(1)
+    df_ok = 1 in results and abs(results[1][1][0] - norms64[0]) <= 1e-10 * abs(norms64[0])
+    use = 1 if (args.arith == "df" or (args.arith == "best" and df_ok)) else 0
+    ms, norms, launches, clk = results[use]
+    S.set_residual_arithmetic(use)
     ms_per_step = ms / args.steps
     value = ws * m.nedge / (ms_per_step * 1e-3) / 1e6
 
@@ -217,12 +232,12 @@ def run_gb300(args, ws, rank, local, pg):
     qh = np.ascontiguousarray(q0)
     S.set_state(qh)
     S.residual_full()
-    S.compute_residuals()
+    S.get_residual()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         S.set_state(qh)
         S.residual_full()
-        b, _n = S.compute_residuals()
+        b = S.get_residual()
     N.check(lib.pcfd_device_sync(), "sync")
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(pg, e2e_s)
@@ -243,13 +258,20 @@ def run_gb300(args, ws, rank, local, pg):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
+        "dtype": arith_names[use], "data": "synthetic",
         "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+Venkat "
                                "limiter K=5+Roe+viscous), Mach 0.8, Re 1e5" % (w["nx"], w["ny"], w["nz"]),
                    "nodes": m.nnode, "edges": m.nedge, "half_edges": m.nbedge,
                    "l2": "inputs larger than L2 (edge arrays alone %.0f MB)" % (m.nedge * 104 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "mesh_build_s": round(t_mesh, 2)},
         "resGlobal": float(norms[0]),
+        "arithmetic": {"used": arith_names[use],
+                       "f64": {"value": ws * m.nedge / (ms64 / args.steps * 1e-3) / 1e6, "ms_per_step": ms64 / args.steps,
+                               "resGlobal": float(norms64[0])},
+                       "df64": ({"value": ws * m.nedge / (results[1][0] / args.steps * 1e-3) / 1e6,
+                                 "ms_per_step": results[1][0] / args.steps, "resGlobal": float(results[1][1][0]),
+                                 "resGlobal_rel_diff_vs_f64": abs(results[1][1][0] - norms64[0]) / abs(norms64[0])}
+                                if 1 in results else None)},
         "gpu_launches": int(launches),
         "kernels": kernels,
         "roofline": {"bound": "hbm", "kernel": "edge_flux", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -276,6 +298,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ns128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--arith", default="best", choices=["f64", "df", "best"],
+                    help="residual arithmetic: FP64, double-float, or double-float when it agrees with FP64")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local, pg = dist()

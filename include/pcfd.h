@@ -162,6 +162,8 @@ PCFD_API int pcfd_limiter(pcfd_solver_t s, double* l_out);
 /* ComputeResiduals (ucs/residual.tcc:13): b (= -R) into b_out [nnode][5]
  * (optional) and norms_out[0..5] = {resGlobal, per-equation norms}. */
 PCFD_API int pcfd_residual(pcfd_solver_t s, double* b_out, double* norms_out);
+/* b (= -R) of the last residual evaluation, [nnode][5], without recomputing. */
+PCFD_API int pcfd_get_residual(pcfd_solver_t s, double* b_out);
 /* UpdateBCs + gradient + limiter + residual in one call, the sequence
  * NewtonIterate runs (ucs/solutionSpace.tcc:662-697), without copying fields
  * back; norms_out as for pcfd_residual. */
@@ -230,6 +232,15 @@ typedef struct pcfd_newton_report {
  * time step; ucs/solutionSpace.tcc:573) then NewtonIterate (:640: boundary
  * conditions, gradient, limiter, residual, linear solve, update). */
 PCFD_API int pcfd_newton_step(pcfd_solver_t s, const pcfd_newton_opts* opts, pcfd_newton_report* report);
+
+/* Arithmetic of the composite residual calls (pcfd_residual_full,
+ * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1
+ * double-float - the same kernels with every FP64 operation replaced by a
+ * pair of FP32 numbers (about 48 significant bits), which GB300 executes on
+ * its FP32 pipes at many times its FP64 rate.  Boundary conditions, the
+ * state, b and the norms stay FP64.  The single-stage calls (pcfd_gradient,
+ * pcfd_limiter, pcfd_residual) always use FP64.  No reference counterpart. */
+PCFD_API int pcfd_set_residual_arithmetic(pcfd_solver_t s, int mode);
 
 /* Runs nsteps of pcfd_residual_full back to back on the handle's stream and
  * returns their device time from CUDA events recorded on that stream (the

@@ -100,6 +100,7 @@ PROTOTYPES = {
     "pcfd_limiter": (C.c_int, [_P, _DP]),
     "pcfd_residual": (C.c_int, [_P, _DP, _DP]),
     "pcfd_residual_full": (C.c_int, [_P, _DP]),
+    "pcfd_get_residual": (C.c_int, [_P, _DP]),
     "pcfd_bench_residual_full": (C.c_int, [_P, C.c_int, _DP, _DP]),
     "pcfd_timestep": (C.c_int, [_P, C.c_double, _DP, _DP]),
     "pcfd_set_jacobian_precision": (C.c_int, [_P, C.c_int]),
@@ -112,6 +113,7 @@ PROTOTYPES = {
     "pcfd_apply_dq": (C.c_int, [_P, _DP, _DP]),
     "pcfd_newton_step": (C.c_int, [_P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
     "pcfd_set_device": (C.c_int, [C.c_int]),
+    "pcfd_set_residual_arithmetic": (C.c_int, [_P, C.c_int]),
     "pcfd_device_sync": (C.c_int, []),
     "pcfd_profile_enable": (C.c_int, [_P, C.c_int]),
     "pcfd_profile_reset": (C.c_int, [_P]),

@@ -254,6 +254,11 @@ class SolutionSpace:
         N.check(self._lib.pcfd_residual(self._h, N.dptr(b) if want_b else None, N.dptr(norms)), "pcfd_residual")
         return b, norms
 
+    def get_residual(self):
+        b = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        N.check(self._lib.pcfd_get_residual(self._h, N.dptr(b)), "pcfd_get_residual")
+        return b
+
     def residual_full(self):
         norms = np.empty(6, dtype=np.float64)
         N.check(self._lib.pcfd_residual_full(self._h, N.dptr(norms)), "pcfd_residual_full")
@@ -266,6 +271,10 @@ class SolutionSpace:
         N.check(self._lib.pcfd_bench_residual_full(self._h, int(nsteps), C.byref(ms), N.dptr(norms)),
                 "pcfd_bench_residual_full")
         return ms.value, norms
+
+    def set_residual_arithmetic(self, mode):
+        """0 FP64, 1 double-float on the FP32 pipes (composite calls only)."""
+        N.check(self._lib.pcfd_set_residual_arithmetic(self._h, int(mode)), "pcfd_set_residual_arithmetic")
 
     def compute_timesteps(self, cfl):
         dt = np.empty(self.mesh.nnode, dtype=np.float64)

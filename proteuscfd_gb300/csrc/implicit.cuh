@@ -31,7 +31,7 @@ __device__ __forceinline__ float ld_blkf(const __nv_bfloat16* p) { return __bflo
 // NumericalFlux with the NaN kneecap (ucs/eqnset.tcc:55-90), Roe flux
 __device__ __forceinline__ void numflux(const double* QL, const double* QR, const D4& a, double gamma, double* f,
                                         unsigned long long* health) {
-  roe_flux(QL, QR, a.x, a.y, a.z, a.w, gamma, f);
+  roe_flux(QL, QR, a.x, a.y, a.z, a.w, gamma, gamma - 1.0, 1.0 / gamma, 1.0 / (gamma - 1.0), f);
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
 }
 

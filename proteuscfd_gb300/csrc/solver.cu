@@ -35,6 +35,19 @@ using namespace pcfd;
 struct __align__(32) D4 {
   double x, y, z, w;
 };
+struct __align__(32) DF4 {
+  dfl x, y, z, w;
+};
+template <class S>
+struct V4;
+template <>
+struct V4<double> {
+  using type = D4;
+};
+template <>
+struct V4<dfl> {
+  using type = DF4;
+};
 
 namespace {
 
@@ -121,6 +134,15 @@ struct Solver {
   int nbind = 0;
   int have_grad = 0, have_lim = 0;
   int lim_clipped = 0;  // 1: d_lim already went through the explicit pressure clip
+  int grad_arith = 0, lim_arith = 0;
+
+  // residual arithmetic of the composite calls: 0 FP64, 1 double-float on the
+  // FP32 pipes; the double-float copies of the residual-path arrays
+  int arith = 0;
+  int f_q_valid = 0;
+  dfl *f_q = nullptr, *f_grad = nullptr, *f_lim = nullptr, *f_limraw = nullptr, *f_eh = nullptr, *f_lsq = nullptr,
+      *f_ef = nullptr, *f_bf = nullptr;
+  DF4 *f_ea = nullptr, *f_ba = nullptr;
 
   // implicit system (block CRS in the reference layout)
   long long nblocks = 0;
@@ -434,28 +456,31 @@ __global__ void k_bc_sequential(int nbedge, const int2* __restrict__ bn, const D
 
 // -------------------------------------------------------------------------
 // weighted LSQ gradient (Gradient::Compute, ucs/gradient.tcc:57)
+// Residual-path kernels are templated on the scalar type S: double (the
+// reference precision) or dfl (double-float on the FP32 pipes).
 // -------------------------------------------------------------------------
 
 __constant__ int c_gradlist[NTERMS] = {0, 1, 2, 3, 4, 5, 7, 8, 9};
 
+template <class S>
 __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restrict__ nptr,
-                                                  const int* __restrict__ nnbr, const double* __restrict__ lsq,
-                                                  const double* __restrict__ q, const int* __restrict__ bptr,
+                                                  const int* __restrict__ nnbr, const S* __restrict__ lsq,
+                                                  const S* __restrict__ q, const int* __restrict__ bptr,
                                                   const int* __restrict__ bhe, const int* __restrict__ bbc,
-                                                  const D4* __restrict__ ba, double* __restrict__ grad) {
+                                                  const typename V4<S>::type* __restrict__ ba, S* __restrict__ grad) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnode) return;
-  double qi[NTERMS];
+  S qi[NTERMS];
   for (int t = 0; t < NTERMS; t++) qi[t] = q[(size_t)i * NVARS + c_gradlist[t]];
-  double g[NTERMS * 3];
-  for (int t = 0; t < NTERMS * 3; t++) g[t] = 0.0;
+  S g[NTERMS * 3];
+  for (int t = 0; t < NTERMS * 3; t++) g[t] = Sc<S>::c(0.0);
   for (int k = nptr[i]; k < nptr[i + 1]; k++) {
     int j = nnbr[k];
-    double c0 = lsq[3 * (size_t)k], c1 = lsq[3 * (size_t)k + 1], c2 = lsq[3 * (size_t)k + 2];
-    const double* qj = &q[(size_t)j * NVARS];
+    S c0 = lsq[3 * (size_t)k], c1 = lsq[3 * (size_t)k + 1], c2 = lsq[3 * (size_t)k + 2];
+    const S* qj = &q[(size_t)j * NVARS];
 #pragma unroll
     for (int t = 0; t < NTERMS; t++) {
-      double dq = qj[c_gradlist[t]] - qi[t];
+      S dq = qj[c_gradlist[t]] - qi[t];
       g[3 * t + 0] += c0 * dq;
       g[3 * t + 1] += c1 * dq;
       g[3 * t + 2] += c2 * dq;
@@ -465,10 +490,10 @@ __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restri
   for (int p = bptr[i]; p < bptr[i + 1]; p++) {
     int he = bhe[p];
     if (bbc[he] != PCFD_BC_SYMMETRY) continue;
-    D4 a = ba[he];
+    typename V4<S>::type a = ba[he];
 #pragma unroll
     for (int t = 0; t < NTERMS; t++) {
-      double dot = g[3 * t] * a.x + g[3 * t + 1] * a.y + g[3 * t + 2] * a.z;
+      S dot = g[3 * t] * a.x + g[3 * t + 1] * a.y + g[3 * t + 2] * a.z;
       g[3 * t + 0] -= dot * a.x;
       g[3 * t + 1] -= dot * a.y;
       g[3 * t + 2] -= dot * a.z;
@@ -482,52 +507,58 @@ __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restri
 // -------------------------------------------------------------------------
 
 // Neighbour min/max (initialised to zero as the reference does) and the
-// modified Venkatakrishnan value, fused per node.
+// modified Venkatakrishnan value, fused per node.  The half-edge vector of
+// each incident edge gives dx = 0.5 (x_j - x_i) (its sign flips when the node
+// is the edge's right end).
+template <class S>
 __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict__ nptr,
-                                                const int* __restrict__ nnbr, const double* __restrict__ q,
-                                                const double* __restrict__ grad, const double* __restrict__ xyz,
-                                                const double* __restrict__ vol, double chi, double K3,
-                                                double* __restrict__ limraw, double* __restrict__ lim,
+                                                const int* __restrict__ nedg, const int* __restrict__ nnbr,
+                                                const S* __restrict__ q, const S* __restrict__ grad,
+                                                const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
+                                                double K3, S* __restrict__ limraw, S* __restrict__ lim,
                                                 int* __restrict__ clipflag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnode) return;
-  double qi[NEQN], qmin[NEQN], qmax[NEQN], l[NEQN], gi[NEQN * 3];
+  const S zero = Sc<S>::c(0.0);
+  const S chi = Sc<S>::from(chi_d), hchi = Sc<S>::c(0.5) * chi, omc = Sc<S>::c(1.0) - chi;
+  S qi[NEQN], qmin[NEQN], qmax[NEQN], gi[NEQN * 3];
   for (int t = 0; t < NEQN; t++) {
     qi[t] = q[(size_t)i * NVARS + t];
-    qmin[t] = 0.0;
-    qmax[t] = 0.0;
-    l[t] = 1.0;
+    qmin[t] = zero;
+    qmax[t] = zero;
   }
   for (int t = 0; t < NEQN * 3; t++) gi[t] = grad[(size_t)i * NTERMS * 3 + t];
   const int k0 = nptr[i], k1 = nptr[i + 1];
   for (int k = k0; k < k1; k++) {
-    const double* qj = &q[(size_t)nnbr[k] * NVARS];
+    const S* qj = &q[(size_t)nnbr[k] * NVARS];
     for (int t = 0; t < NEQN; t++) {
-      double v = qj[t];
+      S v = qj[t];
       qmax[t] = (qmax[t] > v) ? qmax[t] : v;
       qmin[t] = (qmin[t] < v) ? qmin[t] : v;
     }
   }
-  const double ep2 = 6.0 * 3.141592653589793 * vol[i] * K3;
-  const double xi0 = xyz[3 * i], xi1 = xyz[3 * i + 1], xi2 = xyz[3 * i + 2];
+  const S ep2 = Sc<S>::from(6.0 * 3.141592653589793 * vol[i] * K3);
   // The limiter is min(1, min_k num_k / den_k) with every den_k > 0
   // (den = (DP + DM/2)^2 + 7/4 DM^2 + eps^2).  The running minimum is kept
-  // as a fraction and compared by cross-multiplication, so only one FP64
+  // as a fraction and compared by cross-multiplication, so only one
   // division per equation remains instead of one per edge and equation.
-  double bn[NEQN], bd[NEQN];
-  for (int t = 0; t < NEQN; t++) { bn[t] = l[t]; bd[t] = 1.0; }
+  const S one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
+  S bn[NEQN], bd[NEQN];
+  for (int t = 0; t < NEQN; t++) { bn[t] = one; bd[t] = one; }
   for (int k = k0; k < k1; k++) {
-    int j = nnbr[k];
-    const double* qj = &q[(size_t)j * NVARS];
-    double dx0 = 0.5 * (xyz[3 * j] - xi0), dx1 = 0.5 * (xyz[3 * j + 1] - xi1), dx2 = 0.5 * (xyz[3 * j + 2] - xi2);
+    int se = nedg[k];
+    const S* qj = &q[(size_t)nnbr[k] * NVARS];
+    const S* hv = &eh[3 * (size_t)(se < 0 ? ~se : se)];
+    S dx0 = hv[0], dx1 = hv[1], dx2 = hv[2];
+    if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      double dQ = qj[t] - qi[t];
-      double Q = qi[t] + (0.5 * chi * dQ + (1.0 - chi) * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
-      double DM = Q - qi[t];
-      double DP = (Q > qi[t]) ? qmax[t] - qi[t] : qmin[t] - qi[t];
-      double num = DP * DP + ep2 + 2.0 * DM * DP;
-      double den = DP * DP + 2.0 * DM * DM + DM * DP + ep2;
+      S dQ = qj[t] - qi[t];
+      S Q = qi[t] + (hchi * dQ + omc * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
+      S DM = Q - qi[t];
+      S DP = (Q > qi[t]) ? qmax[t] - qi[t] : qmin[t] - qi[t];
+      S num = DP * DP + ep2 + two * DM * DP;
+      S den = DP * DP + two * DM * DM + DM * DP + ep2;
       if (num * bd[t] < bn[t] * den) { bn[t] = num; bd[t] = den; }
     }
   }
@@ -535,51 +566,63 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
   // zero comes after it (ucs/limiters.tcc:110-124)
   int neg = 0;
   for (int t = 0; t < NEQN; t++) {
-    double v = (bd[t] == 1.0) ? bn[t] : bn[t] / bd[t];
+    S v = (bd[t] == one) ? bn[t] : bn[t] / bd[t];
     limraw[(size_t)i * NEQN + t] = v;
-    if (v < 0.0) neg = 1;
-    if (lim) lim[(size_t)i * NEQN + t] = (v < 0.0) ? 0.0 : v;
+    if (v < zero) neg = 1;
+    if (lim) lim[(size_t)i * NEQN + t] = (v < zero) ? zero : v;
   }
   clipflag[i] = neg ? 2 : 0;
 }
 
-__device__ __forceinline__ int bad_extrap(double gamma, const double* Q) {
+// BadExtrapolation (ucs/compressible.tcc:1056)
+template <class S>
+__device__ __forceinline__ int bad_extrap(S gamma, const S* Q) {
+  S r = Q[0];
+  S ir = Sc<S>::c(1.0) / r;
+  S u = Q[1] * ir, v = Q[2] * ir, w = Q[3] * ir;
+  S p = (gamma - Sc<S>::c(1.0)) * (Q[4] - r * (Sc<S>::c(0.5) * (u * u + v * v + w * w)));
+  const S tiny = Sc<S>::c(1.0e-10);
+  return (p < tiny) || (r < Sc<S>::c(0.0)) || (Q[4] < tiny);
+}
+
+// Extrapolated states of one edge with the given limiters and the three
+// BadExtrapolation tests of Kernel_PressureClip (ucs/limiters.tcc:737):
+// bit 0 left, bit 1 right, bit 2 Roe average.  h = 0.5 (x_R - x_L).
+template <class S>
+__device__ int clip_check(const S* qL, const S* qR, const S* gL, const S* gR, const S* lL, const S* lR, S h0, S h1,
+                          S h2, S chi, S gamma) {
+  const S hchi = Sc<S>::c(0.5) * chi, omc = Sc<S>::c(1.0) - chi;
+  S Qi[NEQN], Qj[NEQN];
+  for (int t = 0; t < NEQN; t++) {
+    S dQ = qR[t] - qL[t];
+    Qi[t] = qL[t] + (hchi * dQ + omc * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2)) * lL[t];
+    Qj[t] = qR[t] + (hchi * (-dQ) + omc * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2))) * lR[t];
+  }
+  int m = 0;
+  if (bad_extrap(gamma, Qi)) m |= 1;
+  if (bad_extrap(gamma, Qj)) m |= 2;
+  const S gm1 = gamma - Sc<S>::c(1.0), half = Sc<S>::c(0.5);
+  S rL = Qi[0], rR = Qj[0];
+  S uL = Qi[1] / rL, vL = Qi[2] / rL, wL = Qi[3] / rL;
+  S uR = Qj[1] / rR, vR = Qj[2] / rR, wR = Qj[3] / rR;
+  S PL = gm1 * (Qi[4] - half * rL * (uL * uL + vL * vL + wL * wL));
+  S PR = gm1 * (Qj[4] - half * rR * (uR * uR + vR * vR + wR * wR));
+  S hL = (Qi[4] + PL) / rL, hR = (Qj[4] + PR) / rR;
+  S rho = sqrt(rL * rR);
+  S sg = rho / (rL + rho);
+  S u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
+  S v2h = half * (u * u + v * v + w * w);
+  S Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
+  if (bad_extrap(gamma, Qr)) m |= 4;
+  return m;
+}
+
+__device__ __forceinline__ int bad_extrap_d(double gamma, const double* Q) {
   double r = Q[0];
   double ir = 1.0 / r;
   double u = Q[1] * ir, v = Q[2] * ir, w = Q[3] * ir;
   double p = (gamma - 1.0) * (Q[4] - r * (0.5 * (u * u + v * v + w * w)));
   return (p < 1.0e-10) || (r < 0.0) || (Q[4] < 1.0e-10);
-}
-
-// Extrapolated states of one edge with the given limiters and the three
-// BadExtrapolation tests of Kernel_PressureClip (ucs/limiters.tcc:737):
-// bit 0 left, bit 1 right, bit 2 Roe average.
-__device__ int clip_check(const double* qL, const double* qR, const double* gL, const double* gR,
-                          const double* lL, const double* lR, double h0, double h1, double h2, double chi,
-                          double gamma) {
-  double Qi[NEQN], Qj[NEQN];
-  for (int t = 0; t < NEQN; t++) {
-    double dQ = qR[t] - qL[t];
-    Qi[t] = qL[t] + (0.5 * chi * dQ + (1.0 - chi) * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2)) * lL[t];
-    Qj[t] = qR[t] + (0.5 * chi * (-dQ) + (1.0 - chi) * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2))) * lR[t];
-  }
-  int m = 0;
-  if (bad_extrap(gamma, Qi)) m |= 1;
-  if (bad_extrap(gamma, Qj)) m |= 2;
-  double gm1 = gamma - 1.0;
-  double rL = Qi[0], rR = Qj[0];
-  double uL = Qi[1] / rL, vL = Qi[2] / rL, wL = Qi[3] / rL;
-  double uR = Qj[1] / rR, vR = Qj[2] / rR, wR = Qj[3] / rR;
-  double PL = gm1 * (Qi[4] - 0.5 * rL * (uL * uL + vL * vL + wL * wL));
-  double PR = gm1 * (Qj[4] - 0.5 * rR * (uR * uR + vR * vR + wR * wR));
-  double hL = (Qi[4] + PL) / rL, hR = (Qj[4] + PR) / rR;
-  double rho = sqrt(rL * rR);
-  double sg = rho / (rL + rho);
-  double u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
-  double v2h = 0.5 * (u * u + v * v + w * w);
-  double Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
-  if (bad_extrap(gamma, Qr)) m |= 4;
-  return m;
 }
 
 // Kernel_PressureClip (ucs/limiters.tcc:737) evaluated with the post-limiter
@@ -612,7 +655,7 @@ __global__ void __launch_bounds__(128) k_pressure_clip(int nnode, const int* __r
       double lj = lim_in[(size_t)j * NEQN + t];
       Qj[t] = qj[t] + (0.5 * chi * (-dQ) + (1.0 - chi) * (gj[3 * t] * (-dx[0]) + gj[3 * t + 1] * (-dx[1]) + gj[3 * t + 2] * (-dx[2]))) * lj;
     }
-    if (bad_extrap(gamma, Qi)) { clip = 1; break; }
+    if (bad_extrap_d(gamma, Qi)) { clip = 1; break; }
     // RoeVariables (ucs/compressible.tcc:533) of the pair, then the same test
     double gm1 = gamma - 1.0;
     double rL = Qi[0], rR = Qj[0];
@@ -626,7 +669,7 @@ __global__ void __launch_bounds__(128) k_pressure_clip(int nnode, const int* __r
     double u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
     double v2h = 0.5 * (u * u + v * v + w * w);
     double Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
-    if (bad_extrap(gamma, Qr)) { clip = 1; break; }
+    if (bad_extrap_d(gamma, Qr)) { clip = 1; break; }
   }
   if (clip) atomicAdd(&health[H_LIMCLIP], 1ull);
   for (int t = 0; t < NEQN; t++) {
@@ -648,11 +691,30 @@ struct FluxConst {
   double cp_over_pr;   // (1/(gamma-1)) / Pr
 };
 
-__device__ __forceinline__ int kneecap5(double* f) {
+// the constants in the working scalar type, converted once per thread
+template <class S>
+struct FluxK {
+  S gamma, gm1, igamma, igm1, chi, hchi, omc, inv_retilde, Sc_, cp_over_pr;
+  __device__ __forceinline__ explicit FluxK(const FluxConst& k) {
+    gamma = Sc<S>::from(k.gamma);
+    gm1 = Sc<S>::from(k.gamma - 1.0);
+    igamma = Sc<S>::from(1.0 / k.gamma);
+    igm1 = Sc<S>::from(1.0 / (k.gamma - 1.0));
+    chi = Sc<S>::from(k.chi);
+    hchi = Sc<S>::from(0.5 * k.chi);
+    omc = Sc<S>::from(1.0 - k.chi);
+    inv_retilde = Sc<S>::from(k.inv_retilde);
+    Sc_ = Sc<S>::from(k.S);
+    cp_over_pr = Sc<S>::from(k.cp_over_pr);
+  }
+};
+
+template <class S>
+__device__ __forceinline__ int kneecap5(S* f) {
   int bad = 0;
 #pragma unroll
   for (int i = 0; i < NEQN; i++)
-    if (isnan(f[i])) { f[i] = 0.0; bad = 1; }
+    if (isnan(f[i])) { f[i] = Sc<S>::c(0.0); bad = 1; }
   return bad;
 }
 
@@ -664,85 +726,88 @@ __device__ __forceinline__ int kneecap5(double* f) {
 // flagged the clip is a no-op and the fluxes already stand.  MODE 2:
 // re-evaluates only edges touching a flagged node, after their limiters were
 // zeroed; it returns at once when nothing was flagged.
-template <int MODE>
+template <class S, int MODE>
 __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __restrict__ en,
-                                                   const D4* __restrict__ ea, const double* __restrict__ eh,
-                                                   const double* __restrict__ q, const double* __restrict__ grad,
-                                                   const double* __restrict__ lim, FluxConst k,
-                                                   double* __restrict__ ef, unsigned long long* health,
+                                                   const typename V4<S>::type* __restrict__ ea,
+                                                   const S* __restrict__ eh, const S* __restrict__ q,
+                                                   const S* __restrict__ grad, const S* __restrict__ lim, FluxConst kd,
+                                                   S* __restrict__ ef, unsigned long long* health,
                                                    int* __restrict__ clipflag, int* __restrict__ clipany,
-                                                   const double* __restrict__ limraw) {
+                                                   const S* __restrict__ limraw) {
   if (MODE == 2 && *(volatile int*)clipany == 0) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nedge) return;
   const int2 n = en[e];
   if (MODE == 2 && !((clipflag[n.x] | clipflag[n.y]) & 1)) return;
-  const D4 a = ea[e];
-  const double* qL = &q[(size_t)n.x * NVARS];
-  const double* qR = &q[(size_t)n.y * NVARS];
-  double QL[NEQN], QR[NEQN];
+  const FluxK<S> k(kd);
+  const typename V4<S>::type a = ea[e];
+  const S* qL = &q[(size_t)n.x * NVARS];
+  const S* qR = &q[(size_t)n.y * NVARS];
+  S QL[NEQN], QR[NEQN];
 #pragma unroll
   for (int t = 0; t < NEQN; t++) { QL[t] = qL[t]; QR[t] = qR[t]; }
-  double h0 = 0.0, h1 = 0.0, h2 = 0.0;
-  if (k.ho || k.viscous) { h0 = eh[3 * (size_t)e]; h1 = eh[3 * (size_t)e + 1]; h2 = eh[3 * (size_t)e + 2]; }
-  if (k.ho) {
-    const double* gL = &grad[(size_t)n.x * NTERMS * 3];
-    const double* gR = &grad[(size_t)n.y * NTERMS * 3];
-    const double* lL = &lim[(size_t)n.x * NEQN];
-    const double* lR = &lim[(size_t)n.y * NEQN];
+  S h0 = Sc<S>::c(0.0), h1 = h0, h2 = h0;
+  if (kd.ho || kd.viscous) { h0 = eh[3 * (size_t)e]; h1 = eh[3 * (size_t)e + 1]; h2 = eh[3 * (size_t)e + 2]; }
+  if (kd.ho) {
+    const S* gL = &grad[(size_t)n.x * NTERMS * 3];
+    const S* gR = &grad[(size_t)n.y * NTERMS * 3];
+    const S* lL = &lim[(size_t)n.x * NEQN];
+    const S* lR = &lim[(size_t)n.y * NEQN];
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      double dQ = qR[t] - qL[t];
-      double cl = 0.5 * k.chi * dQ + (1.0 - k.chi) * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2);
-      double cr = 0.5 * k.chi * (-dQ) + (1.0 - k.chi) * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2));
+      S dQ = qR[t] - qL[t];
+      S cl = k.hchi * dQ + k.omc * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2);
+      S cr = k.hchi * (-dQ) + k.omc * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2));
       QL[t] = qL[t] + cl * lL[t];
       QR[t] = qR[t] + cr * lR[t];
     }
   }
-  double f[NEQN];
-  int bad = roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
-  if (MODE == 1 && k.clip && ((clipflag[n.x] | clipflag[n.y]) & 2)) {
+  S f[NEQN];
+  int bad = roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, k.gm1, k.igamma, k.igm1, f);
+  if (MODE == 1 && kd.clip && ((clipflag[n.x] | clipflag[n.y]) & 2)) {
     // an endpoint had negative raw limiter values, which the clip sees
     // before they are clamped: test the states it would build
     bad = clip_check(qL, qR, &grad[(size_t)n.x * NTERMS * 3], &grad[(size_t)n.y * NTERMS * 3],
                      &limraw[(size_t)n.x * NEQN], &limraw[(size_t)n.y * NEQN], h0, h1, h2, k.chi, k.gamma);
   }
-  if (MODE == 1 && k.clip && bad) {
+  if (MODE == 1 && kd.clip && bad) {
     if (bad & 5) atomicOr(&clipflag[n.x], 1);
     if (bad & 6) atomicOr(&clipflag[n.y], 1);
     atomicOr(clipany, 1);
   }
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
-  if (k.viscous) {
+  if (kd.viscous) {
     // face state: plain average of the nodal conservative variables
-    double Q0 = (qL[0] + qR[0]) / 2.0, Q1 = (qL[1] + qR[1]) / 2.0, Q2 = (qL[2] + qR[2]) / 2.0,
-           Q3 = (qL[3] + qR[3]) / 2.0, Q4 = (qL[4] + qR[4]) / 2.0;
-    double iQ0 = 1.0 / Q0;
-    double u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
-    double P = (k.gamma - 1.0) * (Q4 - 0.5 * Q0 * (u * u + v * v + w * w));
-    double T = k.gamma * P * iQ0;
-    const double* gL = &grad[(size_t)n.x * NTERMS * 3];
-    const double* gR = &grad[(size_t)n.y * NTERMS * 3];
-    double g[NTERMS * 3];
+    const S half = Sc<S>::c(0.5);
+    S Q0 = (qL[0] + qR[0]) * half, Q1 = (qL[1] + qR[1]) * half, Q2 = (qL[2] + qR[2]) * half,
+      Q3 = (qL[3] + qR[3]) * half, Q4 = (qL[4] + qR[4]) * half;
+    S iQ0 = Sc<S>::c(1.0) / Q0;
+    S u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
+    S P = k.gm1 * (Q4 - half * Q0 * (u * u + v * v + w * w));
+    S T = k.gamma * P * iQ0;
+    const S* gL = &grad[(size_t)n.x * NTERMS * 3];
+    const S* gR = &grad[(size_t)n.y * NTERMS * 3];
+    S g[NTERMS * 3];
 #pragma unroll
-    for (int t = 0; t < NTERMS * 3; t++) g[t] = 0.5 * (gL[t] + gR[t]);
-    if (k.ho) {
+    for (int t = 0; t < NTERMS * 3; t++) g[t] = half * (gL[t] + gR[t]);
+    if (kd.ho) {
       // directional correction along the edge (dx = xR - xL = 2 h)
-      double d0 = 2.0 * h0, d1 = 2.0 * h1, d2 = 2.0 * h2;
-      double s2 = d0 * d0 + d1 * d1 + d2 * d2;
-      double is2 = 1.0 / s2;
+      const S two = Sc<S>::c(2.0);
+      S d0 = two * h0, d1 = two * h1, d2 = two * h2;
+      S s2 = d0 * d0 + d1 * d1 + d2 * d2;
+      S is2 = Sc<S>::c(1.0) / s2;
 #pragma unroll
       for (int t = 0; t < NTERMS; t++) {
-        double qdots = d0 * g[3 * t] + d1 * g[3 * t + 1] + d2 * g[3 * t + 2];
+        S qdots = d0 * g[3 * t] + d1 * g[3 * t + 1] + d2 * g[3 * t + 2];
         int loc = c_gradlist[t];
-        double dq = (qR[loc] - qL[loc] - qdots) * is2;
+        S dq = (qR[loc] - qL[loc] - qdots) * is2;
         g[3 * t] += dq * d0;
         g[3 * t + 1] += dq * d1;
         g[3 * t + 2] += dq * d2;
       }
     }
-    double fv[NEQN];
-    viscous_flux(u, v, w, T, g, a.x, a.y, a.z, a.w * k.inv_retilde, k.S, k.cp_over_pr, fv);
+    S fv[NEQN];
+    viscous_flux(u, v, w, T, g, a.x, a.y, a.z, a.w * k.inv_retilde, k.Sc_, k.cp_over_pr, fv);
 #pragma unroll
     for (int t = 0; t < NEQN; t++) f[t] += fv[t];
   }
@@ -752,12 +817,13 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
 
 // Zeroes the limiter of every flagged node (the pressure clip); returns at
 // once when nothing was flagged.
+template <class S>
 __global__ void k_clip_apply(int nnode, const int* __restrict__ clipflag, const int* __restrict__ clipany,
-                             double* __restrict__ lim, unsigned long long* health) {
+                             S* __restrict__ lim, unsigned long long* health) {
   if (*(volatile const int*)clipany == 0) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
     if (clipflag[i] & 1) {
-      for (int t = 0; t < NEQN; t++) lim[(size_t)i * NEQN + t] = 0.0;
+      for (int t = 0; t < NEQN; t++) lim[(size_t)i * NEQN + t] = Sc<S>::c(0.0);
       atomicAdd(&health[H_LIMCLIP], 1ull);
     }
   }
@@ -765,30 +831,33 @@ __global__ void k_clip_apply(int nnode, const int* __restrict__ clipflag, const 
 
 // Bkernel_Inviscid_Flux (:299) + Bkernel_Viscous_Flux (:472) for one
 // half-edge (boundary node, phantom node).
+template <class S>
 __global__ void __launch_bounds__(128) k_bedge_flux(int nbedge, const int2* __restrict__ bn,
-                                                    const D4* __restrict__ ba, const double* __restrict__ q,
-                                                    const double* __restrict__ grad, FluxConst k,
-                                                    double* __restrict__ bf, unsigned long long* health) {
+                                                    const typename V4<S>::type* __restrict__ ba,
+                                                    const S* __restrict__ q, const S* __restrict__ grad, FluxConst kd,
+                                                    S* __restrict__ bf, unsigned long long* health) {
   int he = blockIdx.x * blockDim.x + threadIdx.x;
   if (he >= nbedge) return;
+  const FluxK<S> k(kd);
   const int2 n = bn[he];
-  const D4 a = ba[he];
-  const double* qL = &q[(size_t)n.x * NVARS];
-  const double* qR = &q[(size_t)n.y * NVARS];
-  double QL[NEQN], QR[NEQN], f[NEQN];
+  const typename V4<S>::type a = ba[he];
+  const S* qL = &q[(size_t)n.x * NVARS];
+  const S* qR = &q[(size_t)n.y * NVARS];
+  S QL[NEQN], QR[NEQN], f[NEQN];
 #pragma unroll
   for (int t = 0; t < NEQN; t++) { QL[t] = qL[t]; QR[t] = qR[t]; }
-  roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, f);
+  roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, k.gm1, k.igamma, k.igm1, f);
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
-  if (k.viscous) {
-    double Q0 = 0.5 * (qL[0] + qR[0]), Q1 = 0.5 * (qL[1] + qR[1]), Q2 = 0.5 * (qL[2] + qR[2]),
-           Q3 = 0.5 * (qL[3] + qR[3]), Q4 = 0.5 * (qL[4] + qR[4]);
-    double iQ0 = 1.0 / Q0;
-    double u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
-    double P = (k.gamma - 1.0) * (Q4 - 0.5 * Q0 * (u * u + v * v + w * w));
-    double T = k.gamma * P * iQ0;
-    double fv[NEQN];
-    viscous_flux(u, v, w, T, &grad[(size_t)n.x * NTERMS * 3], a.x, a.y, a.z, a.w * k.inv_retilde, k.S,
+  if (kd.viscous) {
+    const S half = Sc<S>::c(0.5);
+    S Q0 = half * (qL[0] + qR[0]), Q1 = half * (qL[1] + qR[1]), Q2 = half * (qL[2] + qR[2]),
+      Q3 = half * (qL[3] + qR[3]), Q4 = half * (qL[4] + qR[4]);
+    S iQ0 = Sc<S>::c(1.0) / Q0;
+    S u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
+    S P = k.gm1 * (Q4 - half * Q0 * (u * u + v * v + w * w));
+    S T = k.gamma * P * iQ0;
+    S fv[NEQN];
+    viscous_flux(u, v, w, T, &grad[(size_t)n.x * NTERMS * 3], a.x, a.y, a.z, a.w * k.inv_retilde, k.Sc_,
                  k.cp_over_pr, fv);
 #pragma unroll
     for (int t = 0; t < NEQN; t++) f[t] += fv[t];
@@ -800,11 +869,13 @@ __global__ void __launch_bounds__(128) k_bedge_flux(int nbedge, const int2* __re
 // b_i = sum over incident edges in ascending edge id (-F_e if i is the left
 // node, +F_e otherwise) - sum of its half-edge fluxes; then the no-slip
 // residual hook (ModifyViscousWallResidual, ucs/compressible.tcc:1612) and
-// per-block partial sums of b^2 for the norms.
+// per-block partial sums of b^2 for the norms.  The sum runs in S and b is
+// stored in FP64.
+template <class S>
 __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* __restrict__ nptr,
-                                                         const int* __restrict__ nedg, const double* __restrict__ ef,
+                                                         const int* __restrict__ nedg, const S* __restrict__ ef,
                                                          const int* __restrict__ bptr, const int* __restrict__ bhe,
-                                                         const double* __restrict__ bf, const int* __restrict__ bbc,
+                                                         const S* __restrict__ bf, const int* __restrict__ bbc,
                                                          const double* __restrict__ btw, double* __restrict__ b,
                                                          double* __restrict__ part, int* __restrict__ clipflag,
                                                          const int* __restrict__ clipany) {
@@ -813,35 +884,40 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
   const int any = *(volatile const int*)clipany;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
     if (any && (clipflag[i] & 1)) clipflag[i] &= ~1;
-    double r[NEQN] = {0, 0, 0, 0, 0};
+    S r[NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) r[t] = Sc<S>::c(0.0);
     for (int k = nptr[i]; k < nptr[i + 1]; k++) {
       int se = nedg[k];
       if (se < 0) {
-        const double* f = &ef[(size_t)(~se) * NEQN];
+        const S* f = &ef[(size_t)(~se) * NEQN];
 #pragma unroll
         for (int t = 0; t < NEQN; t++) r[t] += -f[t];
       } else {
-        const double* f = &ef[(size_t)se * NEQN];
+        const S* f = &ef[(size_t)se * NEQN];
 #pragma unroll
         for (int t = 0; t < NEQN; t++) r[t] += f[t];
       }
     }
     for (int p = bptr[i]; p < bptr[i + 1]; p++) {
       int he = bhe[p];
-      const double* f = &bf[(size_t)he * NEQN];
+      const S* f = &bf[(size_t)he * NEQN];
 #pragma unroll
       for (int t = 0; t < NEQN; t++) r[t] += -f[t];
     }
+    double rd[NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) rd[t] = Sc<S>::to(r[t]);
     for (int p = bptr[i]; p < bptr[i + 1]; p++) {
       int he = bhe[p];
       if (bbc[he] != PCFD_BC_NOSLIP) continue;
-      r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = 0.0;
-      if (btw[he] < 0.0) r[0] = 0.0;
+      rd[1] = 0.0; rd[2] = 0.0; rd[3] = 0.0; rd[4] = 0.0;
+      if (btw[he] < 0.0) rd[0] = 0.0;
     }
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      b[(size_t)i * NEQN + t] = r[t];
-      acc[1 + t] += r[t] * r[t];
+      b[(size_t)i * NEQN + t] = rd[t];
+      acc[1 + t] += rd[t] * rd[t];
     }
   }
   acc[0] = acc[1] + acc[2] + acc[3] + acc[4] + acc[5];
@@ -868,6 +944,16 @@ __global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ 
   for (int bI = 0; bI < nblocks; bI++) v += part[(size_t)bI * 6 + c];
   if (c == 0) norms[0] = sqrt(v) / ((double)nnode * NEQN);
   else norms[c] = sqrt(v) / (double)nnode;
+}
+
+// FP64 -> double-float copies (state each evaluation; static geometry once)
+__global__ void k_to_df(long long n, const double* __restrict__ in, dfl* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = to_df(in[i]);
+}
+__global__ void k_to_dbl(long long n, const dfl* __restrict__ in, double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = to_dbl(in[i]);
 }
 
 #include "implicit.cuh"
@@ -899,7 +985,8 @@ void free_solver(Solver* s) {
                   s->d_bgptr, s->d_bghe, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_piv,
-                  s->d_bblk, s->d_dt, s->d_x, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots};
+                  s->d_bblk, s->d_dt, s->d_x, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
+                  s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -962,6 +1049,7 @@ void host_qinf(const pcfd_params& p, double* Q) {
 }
 
 int run_bcs(Solver* s) {
+  s->f_q_valid = 0;
   BcConst k = make_bc_const(s);
   if (s->bc_sequential) {
     return launch(s, T_BC, [&] {
@@ -985,38 +1073,116 @@ int run_bcs(Solver* s) {
   });
 }
 
-int run_gradient(Solver* s) {
-  int rc = launch(s, T_GRAD, [&] {
-    k_gradient<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_lsq, s->d_q,
-                                                          s->d_bptr, s->d_bhe, s->d_bbc, s->d_ba, s->d_grad);
-  });
-  if (rc == PCFD_OK) s->have_grad = 1;
+// The residual-path buffers in the working scalar type: the FP64 arrays,
+// or their double-float copies (allocated on first use).
+template <class S>
+struct RBuf {
+  S *q, *grad, *lim, *limraw, *eh, *lsq, *ef, *bf;
+  typename V4<S>::type *ea, *ba;
+};
+RBuf<double> rbuf_d(Solver* s) {
+  return {s->d_q, s->d_grad, s->d_lim, s->d_limraw, s->d_eh, s->d_lsq, s->d_ef, s->d_bf, s->d_ea, s->d_ba};
+}
+RBuf<dfl> rbuf_f(Solver* s) {
+  return {s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
+}
+
+int to_df_launch(Solver* s, const double* in, dfl* out, long long n) {
+  return launch(s, T_SETUP, [&] { k_to_df<<<kNormBlocks, 256, 0, s->stream>>>(n, in, out); });
+}
+
+// double-float copies of the static geometry and buffers for the state
+int ensure_df(Solver* s) {
+  if (s->f_q) return PCFD_OK;
+  int rc;
+  const long long nn = s->nnode, ne = s->nedge, nb = s->nbedge;
+  if ((rc = dalloc(&s->f_q, (size_t)s->ntot * NVARS))) return rc;
+  if ((rc = dalloc(&s->f_grad, (size_t)nn * NTERMS * 3))) return rc;
+  if ((rc = dalloc(&s->f_lim, (size_t)nn * NEQN))) return rc;
+  if ((rc = dalloc(&s->f_limraw, (size_t)nn * NEQN))) return rc;
+  if ((rc = dalloc(&s->f_eh, (size_t)ne * 3))) return rc;
+  if ((rc = dalloc(&s->f_lsq, (size_t)ne * 6))) return rc;
+  if ((rc = dalloc(&s->f_ef, (size_t)ne * NEQN))) return rc;
+  if ((rc = dalloc(&s->f_bf, (size_t)std::max<long long>(nb, 1) * NEQN))) return rc;
+  if ((rc = dalloc(&s->f_ea, (size_t)ne))) return rc;
+  if ((rc = dalloc(&s->f_ba, (size_t)std::max<long long>(nb, 1)))) return rc;
+  if ((rc = to_df_launch(s, s->d_eh, s->f_eh, ne * 3))) return rc;
+  if ((rc = to_df_launch(s, s->d_lsq, s->f_lsq, ne * 6))) return rc;
+  if ((rc = to_df_launch(s, (const double*)s->d_ea, (dfl*)s->f_ea, ne * 4))) return rc;
+  if (nb > 0 && (rc = to_df_launch(s, (const double*)s->d_ba, (dfl*)s->f_ba, nb * 4))) return rc;
+  return PCFD_OK;
+}
+
+// the state in the working scalar type (converted once per change of q)
+int prep_state(Solver* s, int arith) {
+  if (arith == 0) return PCFD_OK;
+  int rc = ensure_df(s);
+  if (rc) return rc;
+  if (s->f_q_valid) return PCFD_OK;
+  rc = to_df_launch(s, s->d_q, s->f_q, (long long)s->ntot * NVARS);
+  if (rc == PCFD_OK) s->f_q_valid = 1;
   return rc;
 }
 
-int run_limiter(Solver* s, bool clip) {
+template <class S>
+int run_gradient_t(Solver* s, RBuf<S> r) {
+  return launch(s, T_GRAD, [&] {
+    k_gradient<S><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, r.lsq, r.q, s->d_bptr,
+                                                             s->d_bhe, s->d_bbc, r.ba, r.grad);
+  });
+}
+
+int run_gradient(Solver* s, int arith = 0) {
+  int rc = prep_state(s, arith);
+  if (rc) return rc;
+  rc = arith ? run_gradient_t(s, rbuf_f(s)) : run_gradient_t(s, rbuf_d(s));
+  if (rc == PCFD_OK) {
+    s->have_grad = 1;
+    s->grad_arith = arith;
+  }
+  return rc;
+}
+
+template <class S>
+int run_venkat_t(Solver* s, RBuf<S> r, bool clip) {
+  double K = s->prm.venkat_K;
+  return launch(s, T_LIMITER, [&] {
+    k_venkat<S><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.q, r.grad,
+                                                           r.eh, s->d_vol, s->prm.chi, K * K * K, r.limraw,
+                                                           clip ? nullptr : r.lim, s->d_clipflag);
+  });
+}
+
+// Limiter<T>::Compute.  clip = true runs the explicit pressure-clip kernel
+// (FP64 only); clip = false folds the clip into the residual's edge pass.
+int run_limiter(Solver* s, bool clip, int arith = 0) {
+  if (clip) arith = 0;
   if (s->prm.limiter == 0) {
     // limiters stay 1.0 (OFF), Limiter ctor (ucs/limiters.tcc:36-41)
     std::vector<double> ones((size_t)s->nnode * NEQN, 1.0);
     CUDA_TRY(cudaMemcpyAsync(s->d_lim, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    if (arith) {
+      int rc = ensure_df(s);
+      if (rc) return rc;
+      rc = to_df_launch(s, s->d_lim, s->f_lim, (long long)s->nnode * NEQN);
+      if (rc) return rc;
+    }
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->have_lim = 1;
-    return PCFD_OK;
-  }
-  double K = s->prm.venkat_K;
-  int rc = launch(s, T_LIMITER, [&] {
-    k_venkat<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad, s->d_xyz,
-                                                        s->d_vol, s->prm.chi, K * K * K, s->d_limraw,
-                                                        clip ? nullptr : s->d_lim, s->d_clipflag);
-  });
-  if (rc) return rc;
-  if (!clip) {
-    // the clip is folded into the residual's edge pass (k_edge_flux<1>)
-    s->have_lim = 1;
+    s->lim_arith = arith;
     s->lim_clipped = 0;
     return PCFD_OK;
   }
-  // d_b holds the pre-clip limiter as scratch; the clip writes the final value
+  if (!s->have_grad || s->grad_arith != arith) return set_err(PCFD_ERR_STATE, "limiter: gradient not computed");
+  int rc = arith ? run_venkat_t(s, rbuf_f(s), clip) : run_venkat_t(s, rbuf_d(s), clip);
+  if (rc) return rc;
+  if (!clip) {
+    // the clip is folded into the residual's edge pass (k_edge_flux<S, 1>)
+    s->have_lim = 1;
+    s->lim_arith = arith;
+    s->lim_clipped = 0;
+    return PCFD_OK;
+  }
   rc = launch(s, T_LIMITER, [&] {
     k_pressure_clip<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nnbr, s->d_q, s->d_grad,
                                                                s->d_xyz, s->prm.chi, s->prm.gamma, s->d_limraw,
@@ -1024,50 +1190,59 @@ int run_limiter(Solver* s, bool clip) {
   });
   if (rc == PCFD_OK) {
     s->have_lim = 1;
+    s->lim_arith = 0;
     s->lim_clipped = 1;
   }
   return rc;
 }
 
-int run_residual(Solver* s) {
-  FluxConst k = make_flux_const(s);
-  if ((k.ho || k.viscous) && !s->have_grad) return set_err(PCFD_ERR_STATE, "residual: gradient not computed");
-  if (k.ho && !s->have_lim) return set_err(PCFD_ERR_STATE, "residual: limiter not computed");
-  if (s->lim_clipped) k.clip = 0;  // the explicit clip already ran
+template <class S>
+int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
   int rc = launch(s, T_EDGEFLUX, [&] {
-    k_edge_flux<1><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
-                                                              s->d_grad, s->d_lim, k, s->d_ef, s->d_health,
-                                                              s->d_clipflag, s->d_clipany, s->d_limraw);
+    k_edge_flux<S, 1><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k,
+                                                                 r.ef, s->d_health, s->d_clipflag, s->d_clipany,
+                                                                 r.limraw);
   });
   if (rc) return rc;
   if (k.clip) {
     rc = launch(s, T_CLIP, [&] {
-      k_clip_apply<<<kNormBlocks, 256, 0, s->stream>>>(s->nnode, s->d_clipflag, s->d_clipany, s->d_lim, s->d_health);
+      k_clip_apply<S><<<kNormBlocks, 256, 0, s->stream>>>(s->nnode, s->d_clipflag, s->d_clipany, r.lim, s->d_health);
     });
     if (rc) return rc;
     rc = launch(s, T_CLIP, [&] {
-      k_edge_flux<2><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
-                                                                s->d_grad, s->d_lim, k, s->d_ef, s->d_health,
-                                                                s->d_clipflag, s->d_clipany, s->d_limraw);
+      k_edge_flux<S, 2><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim,
+                                                                   k, r.ef, s->d_health, s->d_clipflag, s->d_clipany,
+                                                                   r.limraw);
     });
     if (rc) return rc;
   }
   if (s->nbedge > 0) {
     rc = launch(s, T_BEDGEFLUX, [&] {
-      k_bedge_flux<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_q, s->d_grad, k,
-                                                               s->d_bf, s->d_health);
+      k_bedge_flux<S><<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, r.ba, r.q, r.grad, k, r.bf,
+                                                                  s->d_health);
     });
     if (rc) return rc;
   }
   rc = launch(s, T_GATHER, [&] {
-    k_gather<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_ef, s->d_bptr, s->d_bhe,
-                                                         s->d_bf, s->d_bbc, s->d_btw, s->d_b, s->d_part,
-                                                         s->d_clipflag, s->d_clipany);
+    k_gather<S><<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, r.ef, s->d_bptr, s->d_bhe,
+                                                            r.bf, s->d_bbc, s->d_btw, s->d_b, s->d_part, s->d_clipflag,
+                                                            s->d_clipany);
   });
   if (rc) return rc;
   return launch(s, T_NORM, [&] {
     k_norm_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms, s->d_clipany);
   });
+}
+
+int run_residual(Solver* s, int arith = 0) {
+  FluxConst k = make_flux_const(s);
+  if ((k.ho || k.viscous) && (!s->have_grad || s->grad_arith != arith))
+    return set_err(PCFD_ERR_STATE, "residual: gradient not computed");
+  if (k.ho && (!s->have_lim || s->lim_arith != arith)) return set_err(PCFD_ERR_STATE, "residual: limiter not computed");
+  if (s->lim_clipped) k.clip = 0;  // the explicit clip already ran
+  int rc = prep_state(s, arith);
+  if (rc) return rc;
+  return arith ? run_residual_t(s, rbuf_f(s), k) : run_residual_t(s, rbuf_d(s), k);
 }
 
 
@@ -1222,6 +1397,7 @@ int run_sgs(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
 }
 
 int run_apply_dq(Solver* s, double* dqnorm) {
+  s->f_q_valid = 0;
   int rc = launch(s, T_UPDATE, [&] {
     k_apply_dq<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->prm.gamma, s->d_x, s->d_q, s->d_part,
                                                            s->d_health);
@@ -1704,6 +1880,7 @@ PCFD_API int pcfd_set_state(pcfd_solver_t h, const double* q, int nvars, int nro
   CUDA_TRY(cudaMemcpyAsync(s->d_q, q, (size_t)nrows * NVARS * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   s->have_grad = s->have_lim = 0;
+  s->f_q_valid = 0;
   return PCFD_OK;
 }
 
@@ -1771,6 +1948,14 @@ PCFD_API int pcfd_residual(pcfd_solver_t h, double* b_out, double* norms_out) {
   return PCFD_OK;
 }
 
+PCFD_API int pcfd_get_residual(pcfd_solver_t h, double* b_out) {
+  Solver* s = (Solver*)h;
+  if (!s || !b_out) return set_err(PCFD_ERR_ARG, "pcfd_get_residual: bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(b_out, s->d_b, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
 PCFD_API int pcfd_residual_full(pcfd_solver_t h, double* norms_out) {
   Solver* s = (Solver*)h;
   if (!s) return set_err(PCFD_ERR_ARG, "pcfd_residual_full: null handle");
@@ -1778,10 +1963,10 @@ PCFD_API int pcfd_residual_full(pcfd_solver_t h, double* norms_out) {
   int rc;
   if ((rc = run_bcs(s))) return rc;
   if (need_grad) {
-    if ((rc = run_gradient(s))) return rc;
-    if (s->prm.sorder > 1 && (rc = run_limiter(s, false))) return rc;
+    if ((rc = run_gradient(s, s->arith))) return rc;
+    if (s->prm.sorder > 1 && (rc = run_limiter(s, false, s->arith))) return rc;
   }
-  if ((rc = run_residual(s))) return rc;
+  if ((rc = run_residual(s, s->arith))) return rc;
   if (norms_out)
     CUDA_TRY(cudaMemcpyAsync(norms_out, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -1801,9 +1986,9 @@ PCFD_API int pcfd_bench_residual_full(pcfd_solver_t h, int nsteps, double* ms_ou
   int rc = PCFD_OK;
   for (int it = 0; it < nsteps && rc == PCFD_OK; it++) {
     rc = run_bcs(s);
-    if (!rc && need_grad) rc = run_gradient(s);
-    if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s, false);
-    if (!rc) rc = run_residual(s);
+    if (!rc && need_grad) rc = run_gradient(s, s->arith);
+    if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s, false, s->arith);
+    if (!rc) rc = run_residual(s, s->arith);
   }
   cudaEventRecord(e1, s->stream);
   cudaError_t ce = cudaEventSynchronize(e1);
@@ -1819,6 +2004,19 @@ PCFD_API int pcfd_bench_residual_full(pcfd_solver_t h, int nsteps, double* ms_ou
     CUDA_TRY(cudaMemcpyAsync(norms_out, s->d_norms, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
   }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_residual_arithmetic(pcfd_solver_t h, int mode) {
+  Solver* s = (Solver*)h;
+  if (!s || (mode != 0 && mode != 1)) return set_err(PCFD_ERR_ARG, "pcfd_set_residual_arithmetic: mode must be 0 or 1");
+  if (mode == 1) {
+    int rc = ensure_df(s);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
+  s->arith = mode;
+  s->have_grad = s->have_lim = 0;
   return PCFD_OK;
 }
 
@@ -1962,9 +2160,9 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   // NewtonIterate (:640)
   if ((rc = run_bcs(s))) return rc;
   const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
-  if (need_grad && (rc = run_gradient(s))) return rc;
-  if (need_grad && s->prm.sorder > 1 && (rc = run_limiter(s, false))) return rc;
-  if ((rc = run_residual(s))) return rc;
+  if (need_grad && (rc = run_gradient(s, s->arith))) return rc;
+  if (need_grad && s->prm.sorder > 1 && (rc = run_limiter(s, false, s->arith))) return rc;
+  if ((rc = run_residual(s, s->arith))) return rc;
   double lin = 0.0;
   int lin_it = 0;
   CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));

@@ -153,3 +153,53 @@ def test_pressure_clip_matches_oracle(seed):
     assert_residual_close(bg2, bo, O.last_babs)
     assert np.allclose(ng2, no, rtol=1e-12, atol=0)
     assert S.health()[1] > 0
+
+
+@pytest.mark.parametrize("case", SMALL, ids=lambda c: c.name + "_K%g" % c.param.venkat_K)
+@pytest.mark.parametrize("state", ["smooth", "perturbed"])
+def test_double_float_residual_matches_oracle(case, state):
+    """The double-float kernels (FP32 pipes, ~48-bit significands) meet the
+    same 1e-12 residual parity bar as the FP64 kernels."""
+    m, S, O, q0 = run_both(case, state, seed=13)
+    S.set_residual_arithmetic(1)
+    S.set_state(q0)
+    norms = S.residual_full()
+    b = S.get_residual()
+    _, _, _, bo, no = O.full(q0)
+    assert_residual_close(b, bo, O.last_babs)
+    assert np.allclose(norms, no, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_double_float_pressure_clip(seed):
+    case = cases.ns_flatplate(12, 10, 8, seed=5, venkat_K=1.0)
+    m = cases.build_mesh(case)
+    S = SolutionSpace(m, case.param)
+    O = OracleSpace(m, case.param)
+    q0 = low_pressure_state(m, S.qinf(), seed)
+    S.set_residual_arithmetic(1)
+    S.set_state(q0)
+    ng = S.residual_full()
+    bg = S.get_residual()
+    _, _, _, bo, no = O.full(q0)
+    assert_residual_close(bg, bo, O.last_babs)
+    assert np.allclose(ng, no, rtol=1e-12, atol=0)
+    assert S.health()[1] > 0
+
+
+def test_double_float_full_size_freestream():
+    case = cases.ns_flatplate(128, 96, 96)
+    p = case.param
+    p.bc_type = {1: N.BC_FARFIELD, 2: N.BC_FARFIELD, 3: N.BC_FARFIELD, 4: N.BC_FARFIELD,
+                 5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY}
+    m = cases.build_mesh(case)
+    S = SolutionSpace(m, p)
+    S.set_residual_arithmetic(1)
+    q = np.tile(S.qinf(), (m.nnode + m.nbedge, 1))
+    S.set_state(q)
+    S.residual_full()
+    b = S.get_residual()
+    area = np.zeros(m.nnode)
+    np.add.at(area, m.edges[:, 0], m.edge_area[:, 3])
+    np.add.at(area, m.edges[:, 1], m.edge_area[:, 3])
+    assert (np.abs(b) / (area[:, None] * 5.0)).max() < 1e-12
