@@ -267,6 +267,22 @@ PCFD_API long long pcfd_launch_count(pcfd_solver_t s);
  * ucs/exceptions.h:51-63).  counters[0..7]. */
 PCFD_API int pcfd_get_health(pcfd_solver_t s, long long* counters8);
 
+/* Residual norms of a caller-provided device array, with no device
+ * allocation at all - for callers that cannot let a library allocate GPU
+ * memory: applications that hand out every byte from their own pool or fixed
+ * per-tenant budget, or solver loops that must not allocate once running.
+ * This entry point has no counterpart in the reference.
+ * b: device pointer to [nnode][5] doubles; norms: device pointer to 6
+ * doubles, written as pcfd_residual's norms_out (resGlobal, then the five
+ * per-equation norms); stream: a cudaStream_t, or null for the default
+ * stream; synchronous at return.  The only scratch is one fixed array inside
+ * the library (768 KiB per GPU, held until the process exits), which limits
+ * nnode to 33,554,432; larger inputs return PCFD_ERR_ARG.  The first call on
+ * each device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race on it and must be serialised by the caller. */
+PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, double* norms, void* stream);
+
 PCFD_API const char* pcfd_last_error(void);
 PCFD_API const char* pcfd_build_info(void);
 

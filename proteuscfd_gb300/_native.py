@@ -120,6 +120,7 @@ PROTOTYPES = {
     "pcfd_profile_get": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, _DP, _LLP]),
     "pcfd_launch_count": (C.c_longlong, [_P]),
     "pcfd_get_health": (C.c_int, [_P, _LLP]),
+    "pcfd_residual_norms_noalloc": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]),
     "pcfd_last_error": (C.c_char_p, []),
     "pcfd_build_info": (C.c_char_p, []),
 }

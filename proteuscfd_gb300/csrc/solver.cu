@@ -1566,6 +1566,9 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters)
 // C ABI
 // -------------------------------------------------------------------------
 
+// lets the library's other translation units report through pcfd_last_error
+void pcfd_set_last_error(const std::string& msg) { g_err = msg; }
+
 extern "C" {
 
 PCFD_API const char* pcfd_last_error(void) { return g_err.c_str(); }
