@@ -217,6 +217,9 @@ typedef struct pcfd_newton_opts {
   int fgmres_m;         /* Krylov dimension per restart (FGMRES) */
   int fgmres_restarts;  /* restarts (FGMRES) */
   double fgmres_rtol;   /* relative tolerance (FGMRES) */
+  int limiter_refresh;  /* Param::limiterRefresh: recompute the limiter every n iterations (<= 0: 1) */
+  int limiter_freeze;   /* Param::limiterFreeze: keep the limiter fixed from this iteration on (<= 0: never) */
+  int first_order_steps;/* Param::nFirstOrderSteps: first-order fluxes up to this iteration */
 } pcfd_newton_opts;
 
 typedef struct pcfd_newton_report {

@@ -64,6 +64,7 @@ class NewtonOpts(C.Structure):
         ("iter", C.c_int), ("cfl", C.c_double), ("cfl_start", C.c_double), ("cfl_ramp_steps", C.c_int),
         ("nsgs", C.c_int), ("jac_update_freq", C.c_int), ("jac_precision", C.c_int), ("linear_solver", C.c_int),
         ("fgmres_m", C.c_int), ("fgmres_restarts", C.c_int), ("fgmres_rtol", C.c_double),
+        ("limiter_refresh", C.c_int), ("limiter_freeze", C.c_int), ("first_order_steps", C.c_int),
     ]
 
 

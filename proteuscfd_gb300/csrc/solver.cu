@@ -135,6 +135,7 @@ struct Solver {
   int have_grad = 0, have_lim = 0;
   int lim_clipped = 0;  // 1: d_lim already went through the explicit pressure clip
   int grad_arith = 0, lim_arith = 0;
+  int lim_fresh = 0;    // the limiter was computed since the last residual (its clip is pending)
 
   // residual arithmetic of the composite calls: 0 FP64, 1 double-float on the
   // FP32 pipes; the double-float copies of the residual-path arrays
@@ -1181,6 +1182,7 @@ int run_limiter(Solver* s, bool clip, int arith = 0) {
     s->have_lim = 1;
     s->lim_arith = arith;
     s->lim_clipped = 0;
+    s->lim_fresh = 1;
     return PCFD_OK;
   }
   rc = launch(s, T_LIMITER, [&] {
@@ -1234,15 +1236,19 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
   });
 }
 
-int run_residual(Solver* s, int arith = 0) {
+int run_residual(Solver* s, int arith = 0, bool first_order = false) {
   FluxConst k = make_flux_const(s);
+  if (first_order) k.ho = 0;
+  k.clip = k.ho && s->prm.limiter != 0 && s->lim_fresh;
   if ((k.ho || k.viscous) && (!s->have_grad || s->grad_arith != arith))
     return set_err(PCFD_ERR_STATE, "residual: gradient not computed");
   if (k.ho && (!s->have_lim || s->lim_arith != arith)) return set_err(PCFD_ERR_STATE, "residual: limiter not computed");
   if (s->lim_clipped) k.clip = 0;  // the explicit clip already ran
   int rc = prep_state(s, arith);
   if (rc) return rc;
-  return arith ? run_residual_t(s, rbuf_f(s), k) : run_residual_t(s, rbuf_d(s), k);
+  rc = arith ? run_residual_t(s, rbuf_f(s), k) : run_residual_t(s, rbuf_d(s), k);
+  s->lim_fresh = 0;  // the pressure clip belongs to the limiter evaluation it follows
+  return rc;
 }
 
 
@@ -1336,7 +1342,9 @@ int run_jacobian(Solver* s) {
   }
   int rc = run_bcs(s);
   if (rc) return rc;
-  s->have_grad = s->have_lim = 0;
+  // the gradient no longer matches the state; the limiter field keeps its
+  // values, as the reference's does between evaluations
+  s->have_grad = 0;
   switch (s->jac_prec) {
     case 0: return run_jacobian_t<double>(s);
     case 1: return run_jacobian_t<float>(s);
@@ -1405,7 +1413,7 @@ int run_apply_dq(Solver* s, double* dqnorm) {
   if (rc) return rc;
   rc = launch(s, T_UPDATE, [&] { k_sum_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->d_part, s->d_scal + 3); });
   if (rc) return rc;
-  s->have_grad = s->have_lim = 0;
+  s->have_grad = 0;
   if (dqnorm) {
     double v;
     CUDA_TRY(cudaMemcpyAsync(&v, s->d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -2160,12 +2168,21 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   const int jf = o->jac_update_freq > 0 ? o->jac_update_freq : 1;
   if (o->nsgs > 0 && (o->iter % jf == 0 || o->iter == 1 || !s->have_jac) && (rc = run_jacobian(s))) return rc;
   if ((rc = run_timestep(s, cfl))) return rc;
-  // NewtonIterate (:640)
+  // NewtonIterate (:640): gradient when second order is active or viscous;
+  // the limiter every limiter_refresh iterations until limiter_freeze, the
+  // frozen values otherwise (:671-690)
   if ((rc = run_bcs(s))) return rc;
-  const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
-  if (need_grad && (rc = run_gradient(s, s->arith))) return rc;
-  if (need_grad && s->prm.sorder > 1 && (rc = run_limiter(s, false, s->arith))) return rc;
-  if ((rc = run_residual(s, s->arith))) return rc;
+  const bool ho_now = s->prm.sorder > 1 && o->iter > o->first_order_steps;
+  if ((ho_now || s->prm.viscous) && (rc = run_gradient(s, s->arith))) return rc;
+  if (ho_now) {
+    const int refresh = o->limiter_refresh > 0 ? o->limiter_refresh : 1;
+    const bool frozen = o->limiter_freeze > 0 && o->iter >= o->limiter_freeze;
+    const bool recompute = (o->iter % refresh == 0 && !frozen) || !s->have_lim || s->lim_arith != s->arith;
+    if (s->prm.limiter == 0 || recompute) {
+      if ((rc = run_limiter(s, false, s->arith))) return rc;
+    }
+  }
+  if ((rc = run_residual(s, s->arith, !ho_now))) return rc;
   double lin = 0.0;
   int lin_it = 0;
   CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));
