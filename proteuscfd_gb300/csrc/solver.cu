@@ -265,48 +265,50 @@ struct BcConst {
   double qinf[NVARS];
 };
 
-// GetFarfieldBoundaryVariables (ucs/compressible.tcc:1246), static grid
-__device__ void bc_farfield(const BcConst& k, const double* QL, double* QR, const D4 a) {
-  const double gamma = k.gamma;
-  const double* Qinf = k.qinf;
+// GetFarfieldBoundaryVariables (ucs/compressible.tcc:1246), static grid;
+// S = double, or dfl for the double-float residual arithmetic.  qinf and
+// the stored pressure pi come in as S.
+template <class S>
+__device__ void bc_farfield(S gamma, const S* Qinf, const S* QL, S pi, S* QR, const S ax, const S ay, const S az) {
+  const S half = Sc<S>::c(0.5), one = Sc<S>::c(1.0), zero = Sc<S>::c(0.0);
+  const S gm1 = gamma - one;
   for (int subit = 0; subit < 10; subit++) {
-    double t0 = (QL[0] + QR[0]) / 2.0, t1 = (QL[1] + QR[1]) / 2.0, t2 = (QL[2] + QR[2]) / 2.0,
-           t3 = (QL[3] + QR[3]) / 2.0, t4 = (QL[4] + QR[4]) / 2.0;
-    double it0 = 1.0 / t0;
-    double theta = t1 * it0 * a.x + t2 * it0 * a.y + t3 * it0 * a.z;
-    double rhoi = QL[0];
-    double iri = 1.0 / QL[0];
-    double ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
-    double pi = QL[6];
-    double rhoinf = Qinf[0];
-    double uinf = Qinf[1] / Qinf[0], vinf = Qinf[2] / Qinf[0], winf = Qinf[3] / Qinf[0];
-    double pinf = Qinf[6];
-    double tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
-    double pavg = (gamma - 1.0) * (t4 - t0 * (0.5 * (tu * tu + tv * tv + tw * tw)));
-    double rhoavg = t0;
-    double c2avg = gamma * (pavg / rhoavg);
-    double cavg = sqrt(c2avg);
-    double mach = fabs(theta / cavg);
-    if (theta == 0.0) {
+    S t0 = (QL[0] + QR[0]) * half, t1 = (QL[1] + QR[1]) * half, t2 = (QL[2] + QR[2]) * half,
+      t3 = (QL[3] + QR[3]) * half, t4 = (QL[4] + QR[4]) * half;
+    S it0 = one / t0;
+    S theta = t1 * it0 * ax + t2 * it0 * ay + t3 * it0 * az;
+    S rhoi = QL[0];
+    S iri = one / QL[0];
+    S ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
+    S rhoinf = Qinf[0];
+    S uinf = Qinf[1] / Qinf[0], vinf = Qinf[2] / Qinf[0], winf = Qinf[3] / Qinf[0];
+    S pinf = Qinf[6];
+    S tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
+    S pavg = gm1 * (t4 - t0 * (half * (tu * tu + tv * tv + tw * tw)));
+    S rhoavg = t0;
+    S c2avg = gamma * (pavg / rhoavg);
+    S cavg = sqrt(c2avg);
+    S mach = fabs(theta / cavg);
+    if (theta == zero) {
       return;
-    } else if (theta > 0.0 && mach >= 1.0) {
+    } else if (theta > zero && mach >= one) {
       for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
-    } else if (theta < 0.0 && mach >= 1.0) {
+    } else if (theta < zero && mach >= one) {
       for (int i = 0; i < NEQN; i++) QR[i] = Qinf[i];
-    } else if (theta > 0.0 && mach < 1.0) {
-      double pb = pinf;
-      double rhob = rhoi + (pb - pi) / c2avg;
-      double t = (pb - pi) / (rhoavg * cavg);
-      double ub = ui - a.x * t, vb = vi - a.y * t, wb = wi - a.z * t;
+    } else if (theta > zero && mach < one) {
+      S pb = pinf;
+      S rhob = rhoi + (pb - pi) / c2avg;
+      S t = (pb - pi) / (rhoavg * cavg);
+      S ub = ui - ax * t, vb = vi - ay * t, wb = wi - az * t;
       QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
-      QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
-    } else if (theta < 0.0 && mach < 1.0) {
-      double pb = 0.5 * (pinf + pi + rhoavg * cavg * (a.x * (uinf - ui) + a.y * (vinf - vi) + a.z * (winf - wi)));
-      double rhob = rhoinf + (pb - pinf) / c2avg;
-      double t = (pb - pinf) / (rhoavg * cavg);
-      double ub = uinf + a.x * t, vb = vinf + a.y * t, wb = winf + a.z * t;
+      QR[4] = pb / gm1 + half * rhob * (ub * ub + vb * vb + wb * wb);
+    } else if (theta < zero && mach < one) {
+      S pb = half * (pinf + pi + rhoavg * cavg * (ax * (uinf - ui) + ay * (vinf - vi) + az * (winf - wi)));
+      S rhob = rhoinf + (pb - pinf) / c2avg;
+      S t = (pb - pinf) / (rhoavg * cavg);
+      S ub = uinf + ax * t, vb = vinf + ay * t, wb = winf + az * t;
       QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
-      QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
+      QR[4] = pb / gm1 + half * rhob * (ub * ub + vb * vb + wb * wb);
     } else {
       return;
     }
@@ -314,37 +316,47 @@ __device__ void bc_farfield(const BcConst& k, const double* QL, double* QR, cons
 }
 
 // GetInviscidWallBoundaryVariables (ucs/compressible.tcc:1375), static grid
-__device__ void bc_inviscid_wall(const BcConst& k, const double* QL, double* QR, const D4 a) {
-  const double gamma = k.gamma;
-  const double rhoi = QL[0];
-  const double iri = 1.0 / rhoi;
-  const double ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
-  const double pi = QL[6];
-  if (k.no_cvbc) {
-    double dot = QL[1] * a.x + QL[2] * a.y + QL[3] * a.z;
+template <class S>
+__device__ void bc_inviscid_wall(S gamma, int no_cvbc, const S* QL, S pi, S* QR, const S ax, const S ay,
+                                 const S az) {
+  const S half = Sc<S>::c(0.5), one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
+  const S gm1 = gamma - one;
+  const S rhoi = QL[0];
+  const S iri = one / rhoi;
+  const S ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
+  if (no_cvbc) {
+    S dot = QL[1] * ax + QL[2] * ay + QL[3] * az;
     for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
-    QR[1] = QL[1] - 2.0 * dot * a.x;
-    QR[2] = QL[2] - 2.0 * dot * a.y;
-    QR[3] = QL[3] - 2.0 * dot * a.z;
+    QR[1] = QL[1] - two * dot * ax;
+    QR[2] = QL[2] - two * dot * ay;
+    QR[3] = QL[3] - two * dot * az;
     return;
   }
-  const double thetaL = ui * a.x + vi * a.y + wi * a.z;
+  const S thetaL = ui * ax + vi * ay + wi * az;
   for (int subit = 0; subit < 10; subit++) {
-    double t0 = (QL[0] + QR[0]) / 2.0, t1 = (QL[1] + QR[1]) / 2.0, t2 = (QL[2] + QR[2]) / 2.0,
-           t3 = (QL[3] + QR[3]) / 2.0, t4 = (QL[4] + QR[4]) / 2.0;
-    double it0 = 1.0 / t0;
-    double tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
-    double rhoavg = t0;
-    double pavg = (gamma - 1.0) * (t4 - t0 * (0.5 * (tu * tu + tv * tv + tw * tw)));
-    double c2avg = gamma * (pavg / rhoavg);
-    double cavg = sqrt(c2avg);
-    double pb = pi + rhoavg * cavg * thetaL;
-    double rhob = rhoi + (pb - pi) / c2avg;
-    double t = (pb - pi) / (rhoavg * cavg);
-    double ub = ui - a.x * t, vb = vi - a.y * t, wb = wi - a.z * t;
+    S t0 = (QL[0] + QR[0]) * half, t1 = (QL[1] + QR[1]) * half, t2 = (QL[2] + QR[2]) * half,
+      t3 = (QL[3] + QR[3]) * half, t4 = (QL[4] + QR[4]) * half;
+    S it0 = one / t0;
+    S tu = t1 * it0, tv = t2 * it0, tw = t3 * it0;
+    S rhoavg = t0;
+    S pavg = gm1 * (t4 - t0 * (half * (tu * tu + tv * tv + tw * tw)));
+    S c2avg = gamma * (pavg / rhoavg);
+    S cavg = sqrt(c2avg);
+    S pb = pi + rhoavg * cavg * thetaL;
+    S rhob = rhoi + (pb - pi) / c2avg;
+    S t = (pb - pi) / (rhoavg * cavg);
+    S ub = ui - ax * t, vb = vi - ay * t, wb = wi - az * t;
     QR[0] = rhob; QR[1] = rhob * ub; QR[2] = rhob * vb; QR[3] = rhob * wb;
-    QR[4] = pb / (gamma - 1.0) + 0.5 * rhob * (ub * ub + vb * vb + wb * wb);
+    QR[4] = pb / gm1 + half * rhob * (ub * ub + vb * vb + wb * wb);
   }
+}
+
+// FP64 entry points used by the ordered kernels and the boundary Jacobian
+__device__ void bc_farfield(const BcConst& k, const double* QL, double* QR, const D4 a) {
+  bc_farfield<double>(k.gamma, k.qinf, QL, QL[6], QR, a.x, a.y, a.z);
+}
+__device__ void bc_inviscid_wall(const BcConst& k, const double* QL, double* QR, const D4 a) {
+  bc_inviscid_wall<double>(k.gamma, k.no_cvbc, QL, QL[6], QR, a.x, a.y, a.z);
 }
 
 // One boundary half-edge of CalculateBoundaryVariables (ucs/bc.tcc:1059).
@@ -434,6 +446,40 @@ __global__ void k_bc_halfedges(int n, const int* __restrict__ list, const int2* 
   double nQ[NVARS] = {0};
   if (!apply_bc(k, bbc[he], QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
   for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = QR[j];
+}
+
+// The same for the double-float residual arithmetic: far-field and wall
+// sub-iterations in double-float, the phantom state written back in FP64.
+__global__ void k_bc_halfedges_df(int n, const int* __restrict__ list, const int2* __restrict__ bn,
+                                  const D4* __restrict__ ba, const int* __restrict__ bbc, BcConst k,
+                                  double* __restrict__ q, unsigned long long* health) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  int he = list[t];
+  int2 nd = bn[he];
+  const int bct = bbc[he];
+  if (bct != PCFD_BC_FARFIELD && bct != PCFD_BC_IMPERMEABLE_WALL && bct != PCFD_BC_SYMMETRY) {
+    // outflow / Neumann: a copy, done in FP64
+    double QL[NVARS], QR[NVARS], nQ[NVARS] = {0};
+    for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)nd.x * NVARS + j];
+    for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)nd.y * NVARS + j];
+    if (!apply_bc(k, bct, QL, QR, ba[he], 0.0, nQ)) atomicAdd(&health[H_BADBC], 1ull);
+    for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = QR[j];
+    return;
+  }
+  dfl QL[NEQN], QR[NEQN], Qinf[NVARS];
+  for (int j = 0; j < NEQN; j++) QL[j] = to_df(q[(size_t)nd.x * NVARS + j]);
+  for (int j = 0; j < NEQN; j++) QR[j] = to_df(q[(size_t)nd.y * NVARS + j]);
+  for (int j = 0; j < NVARS; j++) Qinf[j] = to_df(k.qinf[j]);
+  const dfl pi = to_df(q[(size_t)nd.x * NVARS + 6]);
+  const D4 a = ba[he];
+  const dfl ax = to_df(a.x), ay = to_df(a.y), az = to_df(a.z), gamma = to_df(k.gamma);
+  if (bct == PCFD_BC_FARFIELD) bc_farfield<dfl>(gamma, Qinf, QL, pi, QR, ax, ay, az);
+  else bc_inviscid_wall<dfl>(gamma, k.no_cvbc, QL, pi, QR, ax, ay, az);
+  double Q[NVARS];
+  for (int j = 0; j < NEQN; j++) Q[j] = to_dbl(QR[j]);
+  aux_vars(k.gamma, Q);
+  for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = Q[j];
 }
 
 // Exact reference order when a no-slip normal node is itself hard-set by a
@@ -683,6 +729,12 @@ __global__ void __launch_bounds__(128) k_pressure_clip(int nnode, const int* __r
 // residual (SpatialResidual, ucs/residual.tcc:66)
 // -------------------------------------------------------------------------
 
+// the flux constants in one scalar type
+template <class S>
+struct FluxK {
+  S gamma, gm1, igamma, igm1, chi, hchi, omc, inv_retilde, Sc_, cp_over_pr;
+};
+
 struct FluxConst {
   double gamma, chi;
   int ho, viscous;
@@ -690,25 +742,16 @@ struct FluxConst {
   double inv_retilde;  // Mach / Re
   double S;            // Sutherland constant / T_ref
   double cp_over_pr;   // (1/(gamma-1)) / Pr
+  FluxK<double> kd;    // derived constants, FP64
+  FluxK<dfl> kf;       // the same split into double-float on the host
 };
 
-// the constants in the working scalar type, converted once per thread
 template <class S>
-struct FluxK {
-  S gamma, gm1, igamma, igm1, chi, hchi, omc, inv_retilde, Sc_, cp_over_pr;
-  __device__ __forceinline__ explicit FluxK(const FluxConst& k) {
-    gamma = Sc<S>::from(k.gamma);
-    gm1 = Sc<S>::from(k.gamma - 1.0);
-    igamma = Sc<S>::from(1.0 / k.gamma);
-    igm1 = Sc<S>::from(1.0 / (k.gamma - 1.0));
-    chi = Sc<S>::from(k.chi);
-    hchi = Sc<S>::from(0.5 * k.chi);
-    omc = Sc<S>::from(1.0 - k.chi);
-    inv_retilde = Sc<S>::from(k.inv_retilde);
-    Sc_ = Sc<S>::from(k.S);
-    cp_over_pr = Sc<S>::from(k.cp_over_pr);
-  }
-};
+__device__ __forceinline__ const FluxK<S>& flux_k(const FluxConst& k);
+template <>
+__device__ __forceinline__ const FluxK<double>& flux_k<double>(const FluxConst& k) { return k.kd; }
+template <>
+__device__ __forceinline__ const FluxK<dfl>& flux_k<dfl>(const FluxConst& k) { return k.kf; }
 
 template <class S>
 __device__ __forceinline__ int kneecap5(S* f) {
@@ -740,7 +783,7 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
   if (e >= nedge) return;
   const int2 n = en[e];
   if (MODE == 2 && !((clipflag[n.x] | clipflag[n.y]) & 1)) return;
-  const FluxK<S> k(kd);
+  const FluxK<S>& k = flux_k<S>(kd);
   const typename V4<S>::type a = ea[e];
   const S* qL = &q[(size_t)n.x * NVARS];
   const S* qR = &q[(size_t)n.y * NVARS];
@@ -839,7 +882,7 @@ __global__ void __launch_bounds__(128) k_bedge_flux(int nbedge, const int2* __re
                                                     S* __restrict__ bf, unsigned long long* health) {
   int he = blockIdx.x * blockDim.x + threadIdx.x;
   if (he >= nbedge) return;
-  const FluxK<S> k(kd);
+  const FluxK<S>& k = flux_k<S>(kd);
   const int2 n = bn[he];
   const typename V4<S>::type a = ba[he];
   const S* qL = &q[(size_t)n.x * NVARS];
@@ -1033,6 +1076,17 @@ FluxConst make_flux_const(const Solver* s) {
   k.inv_retilde = s->prm.Re != 0.0 ? s->prm.mach / s->prm.Re : 0.0;
   k.S = 110.4 / s->prm.ref_temperature;
   k.cp_over_pr = (1.0 / (s->prm.gamma - 1.0)) / s->prm.Pr;
+  const double g = k.gamma;
+  const double vals[10] = {g, g - 1.0, 1.0 / g, 1.0 / (g - 1.0), k.chi, 0.5 * k.chi, 1.0 - k.chi,
+                           k.inv_retilde, k.S, k.cp_over_pr};
+  double* dd = &k.kd.gamma;
+  dfl* ff = &k.kf.gamma;
+  for (int i = 0; i < 10; i++) {
+    dd[i] = vals[i];
+    float hi = (float)vals[i];
+    ff[i].hi = hi;
+    ff[i].lo = (float)(vals[i] - (double)hi);
+  }
   return k;
 }
 
@@ -1049,7 +1103,7 @@ void host_qinf(const pcfd_params& p, double* Q) {
   Q[6] = P; Q[5] = gamma * P * ir; Q[7] = uu; Q[8] = vv; Q[9] = ww;
 }
 
-int run_bcs(Solver* s) {
+int run_bcs(Solver* s, int arith = 0) {
   s->f_q_valid = 0;
   BcConst k = make_bc_const(s);
   if (s->bc_sequential) {
@@ -1061,8 +1115,12 @@ int run_bcs(Solver* s) {
   int rc = PCFD_OK;
   if (s->nbind > 0) {
     rc = launch(s, T_BC, [&] {
-      k_bc_halfedges<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba, s->d_bbc,
-                                                                 s->d_btw, k, s->d_q, s->d_health);
+      if (arith)
+        k_bc_halfedges_df<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba,
+                                                                      s->d_bbc, k, s->d_q, s->d_health);
+      else
+        k_bc_halfedges<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba, s->d_bbc,
+                                                                   s->d_btw, k, s->d_q, s->d_health);
     });
     if (rc) return rc;
   }
@@ -1972,7 +2030,7 @@ PCFD_API int pcfd_residual_full(pcfd_solver_t h, double* norms_out) {
   if (!s) return set_err(PCFD_ERR_ARG, "pcfd_residual_full: null handle");
   const bool need_grad = s->prm.sorder > 1 || s->prm.viscous;
   int rc;
-  if ((rc = run_bcs(s))) return rc;
+  if ((rc = run_bcs(s, s->arith))) return rc;
   if (need_grad) {
     if ((rc = run_gradient(s, s->arith))) return rc;
     if (s->prm.sorder > 1 && (rc = run_limiter(s, false, s->arith))) return rc;
@@ -1996,7 +2054,7 @@ PCFD_API int pcfd_bench_residual_full(pcfd_solver_t h, int nsteps, double* ms_ou
   CUDA_TRY(cudaEventRecord(e0, s->stream));
   int rc = PCFD_OK;
   for (int it = 0; it < nsteps && rc == PCFD_OK; it++) {
-    rc = run_bcs(s);
+    rc = run_bcs(s, s->arith);
     if (!rc && need_grad) rc = run_gradient(s, s->arith);
     if (!rc && need_grad && s->prm.sorder > 1) rc = run_limiter(s, false, s->arith);
     if (!rc) rc = run_residual(s, s->arith);
@@ -2171,7 +2229,7 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   // NewtonIterate (:640): gradient when second order is active or viscous;
   // the limiter every limiter_refresh iterations until limiter_freeze, the
   // frozen values otherwise (:671-690)
-  if ((rc = run_bcs(s))) return rc;
+  if ((rc = run_bcs(s, s->arith))) return rc;
   const bool ho_now = s->prm.sorder > 1 && o->iter > o->first_order_steps;
   if ((ho_now || s->prm.viscous) && (rc = run_gradient(s, s->arith))) return rc;
   if (ho_now) {
