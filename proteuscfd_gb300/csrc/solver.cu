@@ -116,7 +116,10 @@ struct Solver {
   int* d_bhe = nullptr;         // [nbedge]
   int* d_bgnode = nullptr;      // [nbgroup] boundary nodes
   int* d_bgptr = nullptr;       // [nbgroup+1] -> d_bghe
-  int* d_bghe = nullptr;        // [nbedge]
+  int* d_bghe = nullptr;        // [nbgslot] half-edges of the hard-set nodes, bedge order per node
+  int nbgslot = 0;
+  int* d_bgslot = nullptr;      // [nbgslot] -> group
+  double* d_bgqr = nullptr;     // [nbgslot][NVARS] new phantom states
   // fields
   double* d_q = nullptr;        // [ntot][10]
   double* d_grad = nullptr;     // [nnode][27]
@@ -402,29 +405,120 @@ __device__ int apply_bc(const BcConst& k, int bct, double* QL, double* QR, const
   return 1;
 }
 
-// One thread per boundary node; its half-edges in bedge order.
-__global__ void k_bc_nodes(int ngroup, const int* __restrict__ gnode, const int* __restrict__ gptr,
-                           const int* __restrict__ ghe, const int2* __restrict__ bn, const D4* __restrict__ ba,
-                           const int* __restrict__ bbc, const double* __restrict__ btw, const int* __restrict__ bnrm,
-                           BcConst k, double* __restrict__ q, unsigned long long* health) {
-  int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ngroup) return;
-  int node = gnode[g];
+// Nodes that a condition hard-sets (no-slip, Dirichlet, sonic inflow) see
+// their half-edges in bedge order: a half-edge's phantom state depends on
+// the node state left by the hard-set half-edges before it.  The work is
+// split so that every half-edge still gets its own thread:
+//   k_bc_group_halfedges  one thread per half-edge of a hard-set node; it
+//                         replays the node-state changes of the earlier
+//                         hard-set half-edges of its node (cheap assignments)
+//                         and then runs its own condition, writing the new
+//                         phantom state to a scratch row;
+//   k_bc_group_nodes      one thread per hard-set node; it replays all its
+//                         half-edges' node-state changes, writes the node,
+//                         then moves its phantoms from scratch into q.
+// Reads of q in the first kernel therefore all see the state before the
+// update, as in the reference's sequential loop (ucs/bc.tcc:1400).
+
+__device__ __forceinline__ bool hardsets(int bct) {
+  return bct == PCFD_BC_NOSLIP || bct == PCFD_BC_SONIC_INFLOW || bct == PCFD_BC_DIRICHLET;
+}
+
+// The node-state half of apply_bc for the hard-setting conditions; qr0 is
+// the phantom density before the update (it enters the isothermal wall's
+// energy multiplied by the zero wall velocity).
+__device__ void hardset_node(const BcConst& k, int bct, double* QL, double Tw, const double* nQ, double qr0) {
+  if (bct == PCFD_BC_NOSLIP) {
+    if (Tw < 0.0) {
+      QL[0] = nQ[0];
+      QL[4] = nQ[4];
+    } else {
+      double gm1 = k.gamma - 1.0;
+      QL[4] = (Tw * QL[0] / (k.gamma * gm1) + 0.5 * qr0 * 0.0);
+    }
+    QL[1] = QL[0] * 0.0;
+    QL[2] = QL[0] * 0.0;
+    QL[3] = QL[0] * 0.0;
+  } else {
+    for (int i = 0; i < NVARS; i++) QL[i] = k.qinf[i];
+  }
+}
+
+// Node state seen by slot p1 of a group whose slots start at p0.  Each
+// half-edge ends with a recompute of the node's auxiliary variables, which
+// depend only on its conservative values, so one recompute at the end
+// stands for all of them.
+__device__ void replay_group(const BcConst& k, int p0, int p1, const int* __restrict__ ghe,
+                             const int2* __restrict__ bn, const int* __restrict__ bbc,
+                             const double* __restrict__ btw, const int* __restrict__ bnrm,
+                             const double* __restrict__ q, double* QL) {
+  for (int p = p0; p < p1; p++) {
+    const int he = ghe[p];
+    const int bct = bbc[he];
+    if (!hardsets(bct)) continue;
+    double nQ[NVARS] = {0};
+    if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+      for (int j = 0; j < NVARS; j++) nQ[j] = q[(size_t)bnrm[he] * NVARS + j];
+    hardset_node(k, bct, QL, btw[he], nQ, q[(size_t)bn[he].y * NVARS]);
+  }
+  if (p1 > p0) aux_vars(k.gamma, QL);
+}
+
+template <bool DF>
+__global__ void k_bc_group_halfedges(int nslot, const int* __restrict__ slot_group, const int* __restrict__ gnode,
+                                     const int* __restrict__ gptr, const int* __restrict__ ghe,
+                                     const int2* __restrict__ bn, const D4* __restrict__ ba,
+                                     const int* __restrict__ bbc, const double* __restrict__ btw,
+                                     const int* __restrict__ bnrm, BcConst k, const double* __restrict__ q,
+                                     double* __restrict__ qr_out, unsigned long long* health) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nslot) return;
+  const int g = slot_group[t];
+  const int node = gnode[g];
   double QL[NVARS];
   for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)node * NVARS + j];
-  for (int p = gptr[g]; p < gptr[g + 1]; p++) {
-    int he = ghe[p];
-    int ph = bn[he].y;
-    double QR[NVARS];
-    for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)ph * NVARS + j];
+  replay_group(k, gptr[g], t, ghe, bn, bbc, btw, bnrm, q, QL);
+  const int he = ghe[t];
+  const int ph = bn[he].y;
+  const int bct = bbc[he];
+  double QR[NVARS];
+  for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)ph * NVARS + j];
+  if (DF && (bct == PCFD_BC_FARFIELD || bct == PCFD_BC_IMPERMEABLE_WALL || bct == PCFD_BC_SYMMETRY)) {
+    dfl L[NEQN], R[NEQN], Qinf[NVARS];
+    for (int j = 0; j < NEQN; j++) L[j] = to_df(QL[j]);
+    for (int j = 0; j < NEQN; j++) R[j] = to_df(QR[j]);
+    for (int j = 0; j < NVARS; j++) Qinf[j] = to_df(k.qinf[j]);
+    const D4 a = ba[he];
+    const dfl ax = to_df(a.x), ay = to_df(a.y), az = to_df(a.z), gamma = to_df(k.gamma);
+    if (bct == PCFD_BC_FARFIELD) bc_farfield<dfl>(gamma, Qinf, L, to_df(QL[6]), R, ax, ay, az);
+    else bc_inviscid_wall<dfl>(gamma, k.no_cvbc, L, to_df(QL[6]), R, ax, ay, az);
+    for (int j = 0; j < NEQN; j++) QR[j] = to_dbl(R[j]);
+    aux_vars(k.gamma, QR);
+  } else {
     double nQ[NVARS] = {0};
-    int bct = bbc[he];
     if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
       for (int j = 0; j < NVARS; j++) nQ[j] = q[(size_t)bnrm[he] * NVARS + j];
     if (!apply_bc(k, bct, QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
-    for (int j = 0; j < NVARS; j++) q[(size_t)ph * NVARS + j] = QR[j];
   }
+  for (int j = 0; j < NVARS; j++) qr_out[(size_t)t * NVARS + j] = QR[j];
+}
+
+__global__ void k_bc_group_nodes(int ngroup, const int* __restrict__ gnode, const int* __restrict__ gptr,
+                                 const int* __restrict__ ghe, const int2* __restrict__ bn,
+                                 const int* __restrict__ bbc, const double* __restrict__ btw,
+                                 const int* __restrict__ bnrm, BcConst k, const double* __restrict__ qr_in,
+                                 double* __restrict__ q) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroup) return;
+  const int node = gnode[g];
+  double QL[NVARS];
+  for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)node * NVARS + j];
+  replay_group(k, gptr[g], gptr[g + 1], ghe, bn, bbc, btw, bnrm, q, QL);
   for (int j = 0; j < NVARS; j++) q[(size_t)node * NVARS + j] = QL[j];
+  for (int p = gptr[g]; p < gptr[g + 1]; p++) {
+    const int ph = bn[ghe[p]].y;
+    for (int j = 0; j < NVARS; j++) q[(size_t)ph * NVARS + j] = qr_in[(size_t)p * NVARS + j];
+  }
 }
 
 // Half-edges of boundary nodes that no condition hard-sets (far field, walls,
@@ -995,11 +1089,6 @@ __global__ void k_to_df(long long n, const double* __restrict__ in, dfl* __restr
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = to_df(in[i]);
 }
-__global__ void k_to_dbl(long long n, const dfl* __restrict__ in, double* __restrict__ out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = to_dbl(in[i]);
-}
-
 #include "implicit.cuh"
 
 // -------------------------------------------------------------------------
@@ -1026,7 +1115,7 @@ void free_solver(Solver* s) {
   if (!s) return;
   void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
-                  s->d_bgptr, s->d_bghe, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
+                  s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_piv,
                   s->d_bblk, s->d_dt, s->d_x, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
@@ -1125,12 +1214,24 @@ int run_bcs(Solver* s, int arith = 0) {
     if (rc) return rc;
   }
   if (s->nbgroup == 0) return PCFD_OK;
+  rc = launch(s, T_BC, [&] {
+    if (arith)
+      k_bc_group_halfedges<true><<<nblk(s->nbgslot, 128), 128, 0, s->stream>>>(
+          s->nbgslot, s->d_bgslot, s->d_bgnode, s->d_bgptr, s->d_bghe, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
+          s->d_bnrm, k, s->d_q, s->d_bgqr, s->d_health);
+    else
+      k_bc_group_halfedges<false><<<nblk(s->nbgslot, 128), 128, 0, s->stream>>>(
+          s->nbgslot, s->d_bgslot, s->d_bgnode, s->d_bgptr, s->d_bghe, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
+          s->d_bnrm, k, s->d_q, s->d_bgqr, s->d_health);
+  });
+  if (rc) return rc;
   return launch(s, T_BC, [&] {
-    k_bc_nodes<<<nblk(s->nbgroup, 128), 128, 0, s->stream>>>(s->nbgroup, s->d_bgnode, s->d_bgptr, s->d_bghe, s->d_bn,
-                                                            s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, k, s->d_q,
-                                                            s->d_health);
+    k_bc_group_nodes<<<nblk(s->nbgroup, 128), 128, 0, s->stream>>>(s->nbgroup, s->d_bgnode, s->d_bgptr, s->d_bghe,
+                                                                   s->d_bn, s->d_bbc, s->d_btw, s->d_bnrm, k,
+                                                                   s->d_bgqr, s->d_q);
   });
 }
+
 
 // The residual-path buffers in the working scalar type: the FP64 arrays,
 // or their double-float copies (allocated on first use).
@@ -1811,6 +1912,14 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dput(&s->d_bgnode, gnode.data(), gnode.size()));
   TRY(dput(&s->d_bgptr, gptr.data(), gptr.size()));
   TRY(dput(&s->d_bghe, bghe_list.data(), bghe_list.size()));
+  {
+    std::vector<int> slot(bghe_list.size());
+    for (size_t g = 0; g < gnode.size(); g++)
+      for (int p = gptr[g]; p < gptr[g + 1]; p++) slot[p] = (int)g;
+    s->nbgslot = (int)slot.size();
+    TRY(dput(&s->d_bgslot, slot.data(), slot.size()));
+    TRY(dalloc(&s->d_bgqr, std::max<size_t>(slot.size(), 1) * NVARS));
+  }
   TRY(dput(&s->d_bind, bind.data(), bind.size()));
   TRY(dalloc(&s->d_clipflag, (size_t)nn));
   TRY(dalloc(&s->d_limraw, (size_t)nn * NEQN));
