@@ -213,7 +213,9 @@ typedef struct pcfd_newton_opts {
   int nsgs;             /* Param::nSgs: SGS sweeps, or FGMRES preconditioner sweeps */
   int jac_update_freq;  /* Param::jacobianFreq */
   int jac_precision;    /* 0 FP64, 1 FP32, 2 BF16 off-diagonal storage */
-  int linear_solver;    /* 0 block SGS (the reference's), 1 FGMRES preconditioned by SGS */
+  int linear_solver;    /* 0 block SGS (the reference's), 1 FGMRES preconditioned by SGS,
+                           2 FGMRES preconditioned by SGS plus the learned correction
+                           (pcfd_lp_*), with plain SGS-preconditioned FGMRES as the fallback */
   int fgmres_m;         /* Krylov dimension per restart (FGMRES) */
   int fgmres_restarts;  /* restarts (FGMRES) */
   double fgmres_rtol;   /* relative tolerance (FGMRES) */
@@ -229,6 +231,7 @@ typedef struct pcfd_newton_report {
   double lin_res; /* SGS: norm change of the last sweep; FGMRES: final relative residual */
   int lin_iters;  /* sweeps or Krylov iterations */
   double cfl;     /* CFL used */
+  int lp_fallbacks; /* linear_solver 2: restarts that fell back to SGS-only preconditioning */
 } pcfd_newton_report;
 
 /* One outer iteration in the reference's order: PreTimeAdvance (Jacobian,
@@ -236,13 +239,66 @@ typedef struct pcfd_newton_report {
  * conditions, gradient, limiter, residual, linear solve, update). */
 PCFD_API int pcfd_newton_step(pcfd_solver_t s, const pcfd_newton_opts* opts, pcfd_newton_report* report);
 
+/* ---- learned right preconditioner -------------------------------------
+ * No reference counterpart: it sits where CRS<T>::PrecondBackSolve sits
+ * (ucs/crs.tcc:591).  For a Krylov vector v the preconditioner returns
+ *   z = y + sigma * N(x),   y = nsgs block-SGS sweeps on v,
+ *   sigma = RMS of y over all nodes and equations,
+ * where N is an edge message-passing network applied to the node features x
+ * (PCFD_LP_NIN per node: y/sigma (5), the state as rho/rho_inf - 1,
+ * u/c_inf, v/c_inf, w/c_inf, p/p_inf - 1 (5), log(vol/mean vol) (1)) and
+ * the edge features (unit face normal oriented away from the node (3), edge
+ * length / mean edge length (1)).  Network: encoder 11 -> 64 (ReLU); three
+ * layers h' = ReLU(Ws h + Wm m + b) with m_i = (1/deg_i) sum_j
+ * (We e_ij + ce) * h_j (channel-wise gate); decoder 64 -> 5.  Matrices are
+ * BF16, biases and accumulation FP32; the 64x128 layer products run on the
+ * tensor cores.  Parameters are one FP32 array of PCFD_LP_NPARAM values in
+ * the order: Win[64][11], bin[64], then per layer We[64][4], ce[64],
+ * Ws[64][64], Wm[64][64], b[64], then Wout[5][64], bout[5]. */
+#define PCFD_LP_NIN 11
+#define PCFD_LP_HIDDEN 64
+#define PCFD_LP_NEDGE 4
+#define PCFD_LP_NOUT 5
+#define PCFD_LP_LAYERS 3
+#define PCFD_LP_NPARAM 26821
+
+/* Allocates the network on the handle with seeded initial parameters
+ * (decoder zero, so the preconditioner starts as plain SGS). */
+PCFD_API int pcfd_lp_init(pcfd_solver_t s, unsigned long long seed);
+PCFD_API int pcfd_lp_get_params(pcfd_solver_t s, float* params);
+PCFD_API int pcfd_lp_set_params(pcfd_solver_t s, const float* params);
+/* Network output for host features x [nnode][PCFD_LP_NIN] -> out [nnode][5]. */
+PCFD_API int pcfd_lp_forward(pcfd_solver_t s, const float* x, float* out);
+/* Loss sum((out - t)^2) / (5 nnode) and its gradient with respect to the
+ * parameters, for host features x and targets t [nnode][5]. */
+PCFD_API int pcfd_lp_loss_grad(pcfd_solver_t s, const float* x, const float* t, float* grad, double* loss);
+/* Node features of a base-preconditioned vector y [nnode][5] (host) with
+ * the handle's current state; sigma_out receives sigma. */
+PCFD_API int pcfd_lp_features(pcfd_solver_t s, const double* y, float* x, double* sigma_out);
+/* Training pairs from the current linear system (the Jacobian and residual
+ * of the last pcfd_newton_step), stored on the device as the features of
+ * y = SGS(r) and the target (x - y)/sigma for pairs (r, x) with A x = r:
+ * (b, dq) with dq solved to the relative tolerance rtol by SGS-preconditioned
+ * FGMRES(30), and, for the first krylov_pairs directions z_j of that solve,
+ * (A z_j, z_j) - exact pairs drawn from the vectors the Krylov solver itself
+ * preconditions. */
+PCFD_API int pcfd_lp_collect(pcfd_solver_t s, int nsgs, double rtol, int krylov_pairs, int* nsamples_out);
+PCFD_API int pcfd_lp_clear_samples(pcfd_solver_t s);
+/* Adam over the stored pairs (one pair per step, epochs passes).
+ * loss_first/loss_last: mean loss of the first and last pass. */
+PCFD_API int pcfd_lp_train(pcfd_solver_t s, int epochs, double lr, double* loss_first, double* loss_last);
+/* Applies the preconditioner to v [nnode][5] (host) -> z (host). */
+PCFD_API int pcfd_lp_apply(pcfd_solver_t s, int nsgs, const double* v, double* z);
+
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1
  * double-float - the same kernels with every FP64 operation replaced by a
  * pair of FP32 numbers (about 48 significant bits), which GB300 executes on
- * its FP32 pipes at many times its FP64 rate.  Boundary conditions, the
- * state, b and the norms stay FP64.  The single-stage calls (pcfd_gradient,
- * pcfd_limiter, pcfd_residual) always use FP64.  No reference counterpart. */
+ * its FP32 pipes at many times its FP64 rate.  The state, b and the norms
+ * stay FP64.  Mode 1 also evaluates the interior fluxes of the
+ * finite-difference Jacobian in double-float (about 1e-6 relative error in
+ * its coefficients).  The single-stage calls (pcfd_gradient, pcfd_limiter,
+ * pcfd_residual) always use FP64.  No reference counterpart. */
 PCFD_API int pcfd_set_residual_arithmetic(pcfd_solver_t s, int mode);
 
 /* Runs nsteps of pcfd_residual_full back to back on the handle's stream and

@@ -44,6 +44,17 @@ void oracle_sgs_colored(int nnode, const int* ia, const int* ja, const double* M
                         double* x, int nsweeps, int ncolor, const int* cptr, const int* rows);
 double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* x, double* q);
 
+/* learned preconditioner network (learned.c) */
+double oracle_bf16(double v);
+int oracle_lp_nparam(void);
+void oracle_lp_graph(const pcfd_mesh_view* m, int* nptr, int* nbr, float* ef);
+double oracle_lp_features(int nnode, const double* y, const double* q, const double* vol, const double* qinf,
+                          double gamma, float* x);
+void oracle_lp_forward(int n, const int* nptr, const int* nbr, const float* ef, const float* x, const float* w,
+                       int emulate, double* out);
+double oracle_lp_loss_grad(int n, const int* nptr, const int* nbr, const float* ef, const float* x, const float* t,
+                           const float* w, int emulate, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,14 @@ BC_SONIC_INFLOW = 7
 BC_SONIC_OUTFLOW = 8
 BC_SYMMETRY = 9
 
+# learned preconditioner network sizes (PCFD_LP_* in include/pcfd.h)
+LP_NIN = 11
+LP_HIDDEN = 64
+LP_NEDGE = 4
+LP_NOUT = 5
+LP_LAYERS = 3
+LP_NPARAM = 26821
+
 
 class BoxParams(C.Structure):
     _fields_ = [
@@ -71,7 +79,7 @@ class NewtonOpts(C.Structure):
 class NewtonReport(C.Structure):
     _fields_ = [
         ("res", C.c_double * 6), ("dqnorm", C.c_double), ("dtmin", C.c_double), ("lin_res", C.c_double),
-        ("lin_iters", C.c_int), ("cfl", C.c_double),
+        ("lin_iters", C.c_int), ("cfl", C.c_double), ("lp_fallbacks", C.c_int),
     ]
 
 
@@ -79,6 +87,7 @@ _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 _LLP = C.POINTER(C.c_longlong)
+_FP = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes); every symbol include/pcfd.h declares
 PROTOTYPES = {
@@ -115,6 +124,16 @@ PROTOTYPES = {
     "pcfd_newton_step": (C.c_int, [_P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
     "pcfd_set_device": (C.c_int, [C.c_int]),
     "pcfd_set_residual_arithmetic": (C.c_int, [_P, C.c_int]),
+    "pcfd_lp_init": (C.c_int, [_P, C.c_ulonglong]),
+    "pcfd_lp_get_params": (C.c_int, [_P, _FP]),
+    "pcfd_lp_set_params": (C.c_int, [_P, _FP]),
+    "pcfd_lp_forward": (C.c_int, [_P, _FP, _FP]),
+    "pcfd_lp_loss_grad": (C.c_int, [_P, _FP, _FP, _FP, _DP]),
+    "pcfd_lp_features": (C.c_int, [_P, _DP, _FP, _DP]),
+    "pcfd_lp_collect": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, _IP]),
+    "pcfd_lp_clear_samples": (C.c_int, [_P]),
+    "pcfd_lp_train": (C.c_int, [_P, C.c_int, C.c_double, _DP, _DP]),
+    "pcfd_lp_apply": (C.c_int, [_P, C.c_int, _DP, _DP]),
     "pcfd_device_sync": (C.c_int, []),
     "pcfd_profile_enable": (C.c_int, [_P, C.c_int]),
     "pcfd_profile_reset": (C.c_int, [_P]),
@@ -159,6 +178,11 @@ def check(rc: int, where: str) -> None:
     if rc != PCFD_OK:
         msg = load().pcfd_last_error()
         raise PcfdError(rc, where, msg.decode() if msg else "")
+
+
+def fptr(a):
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_FP)
 
 
 def dptr(a: np.ndarray):

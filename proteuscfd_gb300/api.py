@@ -276,6 +276,63 @@ class SolutionSpace:
         """0 FP64, 1 double-float on the FP32 pipes (composite calls only)."""
         N.check(self._lib.pcfd_set_residual_arithmetic(self._h, int(mode)), "pcfd_set_residual_arithmetic")
 
+    # ---- learned right preconditioner (pcfd_lp_*; no reference counterpart,
+    # it sits where CRS<T>::PrecondBackSolve sits, ucs/crs.tcc:591) --------
+    def lp_init(self, seed=1):
+        N.check(self._lib.pcfd_lp_init(self._h, int(seed)), "pcfd_lp_init")
+
+    def lp_get_params(self):
+        w = np.empty(N.LP_NPARAM, dtype=np.float32)
+        N.check(self._lib.pcfd_lp_get_params(self._h, N.fptr(w)), "pcfd_lp_get_params")
+        return w
+
+    def lp_set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == N.LP_NPARAM
+        N.check(self._lib.pcfd_lp_set_params(self._h, N.fptr(w)), "pcfd_lp_set_params")
+
+    def lp_forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        assert x.shape == (self.mesh.nnode, N.LP_NIN)
+        out = np.empty((self.mesh.nnode, N.LP_NOUT), dtype=np.float32)
+        N.check(self._lib.pcfd_lp_forward(self._h, N.fptr(x), N.fptr(out)), "pcfd_lp_forward")
+        return out
+
+    def lp_loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(N.LP_NPARAM, dtype=np.float32)
+        loss = C.c_double()
+        N.check(self._lib.pcfd_lp_loss_grad(self._h, N.fptr(x), N.fptr(t), N.fptr(g), C.byref(loss)), "pcfd_lp_loss_grad")
+        return loss.value, g
+
+    def lp_features(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        x = np.empty((self.mesh.nnode, N.LP_NIN), dtype=np.float32)
+        sg = C.c_double()
+        N.check(self._lib.pcfd_lp_features(self._h, N.dptr(y), N.fptr(x), C.byref(sg)), "pcfd_lp_features")
+        return x, sg.value
+
+    def lp_apply(self, v, nsgs=1):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        z = np.empty((self.mesh.nnode, 5), dtype=np.float64)
+        N.check(self._lib.pcfd_lp_apply(self._h, int(nsgs), N.dptr(v), N.dptr(z)), "pcfd_lp_apply")
+        return z
+
+    def lp_collect(self, nsgs=1, rtol=1e-6, krylov_pairs=0):
+        ns = C.c_int()
+        N.check(self._lib.pcfd_lp_collect(self._h, int(nsgs), float(rtol), int(krylov_pairs), C.byref(ns)),
+                "pcfd_lp_collect")
+        return ns.value
+
+    def lp_clear_samples(self):
+        N.check(self._lib.pcfd_lp_clear_samples(self._h), "pcfd_lp_clear_samples")
+
+    def lp_train(self, epochs, lr=1e-3):
+        a, b = C.c_double(), C.c_double()
+        N.check(self._lib.pcfd_lp_train(self._h, int(epochs), float(lr), C.byref(a), C.byref(b)), "pcfd_lp_train")
+        return a.value, b.value
+
     def compute_timesteps(self, cfl):
         dt = np.empty(self.mesh.nnode, dtype=np.float64)
         dtmin = C.c_double()
@@ -333,7 +390,7 @@ class SolutionSpace:
         r = N.NewtonReport()
         N.check(self._lib.pcfd_newton_step(self._h, C.byref(o), C.byref(r)), "pcfd_newton_step")
         return {"res": list(r.res), "dqnorm": r.dqnorm, "dtmin": r.dtmin, "lin_res": r.lin_res,
-                "lin_iters": r.lin_iters, "cfl": r.cfl}
+                "lin_iters": r.lin_iters, "cfl": r.cfl, "lp_fallbacks": r.lp_fallbacks}
 
     def health(self):
         c = (C.c_longlong * 8)()

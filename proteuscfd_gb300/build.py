@@ -86,10 +86,11 @@ def build_library(verbose: bool = False) -> Path:
 
 def build_oracle(verbose: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure)."""
-    srcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "oracle.h", ROOT / "include" / "pcfd.h"]
+    csrcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "learned.c"]
+    srcs = csrcs + [ORACLE_DIR / "oracle.h", ROOT / "include" / "pcfd.h"]
     if _stale(ORACLE_LIB, srcs + [Path(__file__)]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run_all([["gcc", "-O2", "-std=c11", "-fPIC", "-shared", str(ORACLE_DIR / "oracle.c"), "-o", str(tmp), "-lm"]])
+        _run_all([["gcc", "-O2", "-std=c11", "-fPIC", "-shared"] + [str(c) for c in csrcs] + ["-o", str(tmp), "-lm"]])
         os.replace(tmp, ORACLE_LIB)
         if verbose:
             print("built", ORACLE_LIB)

@@ -156,6 +156,70 @@ __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restr
   for (int t = 0; t < 25; t++) { bl[t] = to_store<T>(tL[t]); br[t] = to_store<T>(tR[t]); }
 }
 
+// The same differences with the eleven Roe flux evaluations in double-float
+// (the residual's alternative arithmetic, on the FP32 pipes).  A flux
+// carries ~2^-48 relative error there, so the quotient over h = 1e-8 has
+// ~1e-6 relative error: the Jacobian is only the Newton iteration matrix,
+// the residual (evaluated separately) decides the converged answer.  The
+// analytic viscous blocks stay FP64.
+template <class T>
+__global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __restrict__ en,
+                                                     const D4* __restrict__ ea, const double* __restrict__ eh,
+                                                     const double* __restrict__ q, const int* __restrict__ pos_lr,
+                                                     const int* __restrict__ pos_rl, JacConst k, T* __restrict__ M,
+                                                     unsigned long long* health) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int2 n = en[e];
+  const D4 a = ea[e];
+  dfl QL[NEQN], QR[NEQN];
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) {
+    QL[t] = to_df(q[(size_t)n.x * NVARS + t]);
+    QR[t] = to_df(q[(size_t)n.y * NVARS + t]);
+  }
+  const dfl nx = to_df(a.x), ny = to_df(a.y), nz = to_df(a.z), ar = to_df(a.w);
+  const dfl g = to_df(k.gamma), gm1 = to_df(k.gamma - 1.0), ig = to_df(1.0 / k.gamma), igm1 = to_df(1.0 / (k.gamma - 1.0));
+  const dfl h = to_df(1.0e-8);
+  const double ih = 1.0 / 1.0e-8;
+  dfl fS[NEQN];
+  roe_flux<dfl>(QL, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fS);
+  if (kneecap5(fS)) atomicAdd(&health[H_KNEECAP], 1ull);
+  double tL[25], tR[25];
+  for (int i = 0; i < NEQN; i++) {
+    dfl QP[NEQN], fP[NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) QP[t] = QL[t];
+    QP[i] = QP[i] + h;
+    roe_flux<dfl>(QP, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
+    if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
+#pragma unroll
+    for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = to_dbl(fS[j] - fP[j]) * ih;
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) QP[t] = QR[t];
+    QP[i] = QP[i] + h;
+    roe_flux<dfl>(QL, QP, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
+    if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
+#pragma unroll
+    for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = to_dbl(fP[j] - fS[j]) * ih;
+  }
+  if (k.viscous) {
+    double QLd[NVARS], QRd[NVARS];
+#pragma unroll
+    for (int t = 0; t < NVARS; t++) { QLd[t] = q[(size_t)n.x * NVARS + t]; QRd[t] = q[(size_t)n.y * NVARS + t]; }
+    double dx[3] = {2.0 * eh[3 * (size_t)e], 2.0 * eh[3 * (size_t)e + 1], 2.0 * eh[3 * (size_t)e + 2]};
+    double s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    double vL[25], vR[25];
+    viscous_jacobian(QLd, QRd, dx, s2, a, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
+#pragma unroll
+    for (int t = 0; t < 25; t++) { tL[t] += vL[t]; tR[t] += vR[t]; }
+  }
+  T* bl = &M[(size_t)pos_rl[e] * 25];  // A(R, L)
+  T* br = &M[(size_t)pos_lr[e] * 25];  // A(L, R)
+#pragma unroll
+  for (int t = 0; t < 25; t++) { bl[t] = to_store<T>(tL[t]); br[t] = to_store<T>(tR[t]); }
+}
+
 // Bkernel_NumJac (ucs/jacobian.tcc:459) with jacobianBoundaryEval = 0: the
 // phantom state is re-derived from each perturbed interior state through
 // the boundary condition, and the difference quotient goes to the diagonal.
@@ -327,80 +391,112 @@ __device__ __forceinline__ void lusolve5(const double* a, double* b, const int* 
   }
 }
 
-// One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62),
-// a warp per block row: lanes 0..29 take (block, sub-row) pairs of six
-// blocks at a time, partial products are summed through shared memory, and
-// lane 0 solves the 5x5 diagonal system.
+// Arithmetic of the off-diagonal products: FP64 for the FP64 matrix, FP32
+// for the FP32 and BF16 storage (whose coefficients carry FP32 or coarser
+// rounding already); the diagonal blocks and the LU stay FP64.
+template <class T>
+struct OffAcc {
+  typedef float type;
+};
+template <>
+struct OffAcc<double> {
+  typedef double type;
+};
+__device__ __forceinline__ double off_val(double a) { return a; }
+__device__ __forceinline__ float off_val(float a) { return a; }
+__device__ __forceinline__ float off_val(__nv_bfloat16 a) { return __bfloat162float(a); }
+__device__ __forceinline__ double off_x(double x, double) { return x; }
+__device__ __forceinline__ float off_x(double x, float) { return (float)x; }
+
+// Sum over lanes 5r .. 5r+4 of v, left in lane 5r (r = 0..4).
+template <class A>
+__device__ __forceinline__ A sum5(A v) {
+  const unsigned full = 0xffffffffu;
+  return v + __shfl_down_sync(full, v, 1) + __shfl_down_sync(full, v, 2) + __shfl_down_sync(full, v, 3) +
+         __shfl_down_sync(full, v, 4);
+}
+
+// Off-diagonal part of block row i of A x.  The row's blocks are contiguous
+// in CRS order, 25 coefficients each (row-major), so lane l < 25 takes
+// coefficient (l / 5, l % 5) of every block: each warp load reads 25
+// consecutive coefficients.  The row's column indices come in with one
+// coalesced load (lane b holds block b's), and the coefficient and x loads
+// of eight blocks are issued before any of them is used, so a row costs
+// about three memory latencies however many blocks it has.  Lane 5r
+// receives row r's sum.
+template <class T>
+__device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane, const int* __restrict__ ia,
+                                                                const int* __restrict__ ja, const T* __restrict__ M,
+                                                                const double* __restrict__ x) {
+  typedef typename OffAcc<T>::type A;
+  const unsigned full = 0xffffffffu;
+  const int b0 = ia[i] + 1, nb = ia[i + 1] - b0;
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  A acc = A(0);
+  for (int base = 0; base < nb; base += 32) {
+    const int jl = base + lane < nb ? ja[b0 + base + lane] : 0;
+    const int nk = min(32, nb - base);
+    for (int k0 = 0; k0 < nk; k0 += 8) {
+      A av[8], xv[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int k = k0 + u;
+        const int j = __shfl_sync(full, jl, k & 31);
+        const bool ok = active && k < nk;
+        av[u] = ok ? off_val(M[(size_t)(b0 + base + k) * 25 + lane]) : A(0);
+        xv[u] = ok ? off_x(x[(size_t)j * 5 + c], A(0)) : A(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) acc = fma(av[u], xv[u], acc);
+    }
+  }
+  return sum5(acc);
+}
+
+// One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62), a
+// warp per block row: rhs = b_i - sum_j A_ij x_j over the off-diagonal
+// blocks, then lane 0 solves the 5x5 diagonal system with its FP64 LU.
 template <class T>
 __global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restrict__ rows, const int* __restrict__ ia,
                                                    const int* __restrict__ ja, const T* __restrict__ M,
                                                    const double* __restrict__ dlu, const int* __restrict__ piv,
                                                    const double* __restrict__ b, double* __restrict__ x) {
-  __shared__ double part[8][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gw = blockIdx.x * 8 + w;
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (gw >= nrows) return;
   const int i = rows[gw];
-  const int b0 = ia[i] + 1, b1 = ia[i + 1];
-  const int r = lane % 5, kb = lane / 5;  // lanes 30, 31 idle
-  double acc = 0.0;
-  if (lane < 30) {
-    for (int blk = b0 + kb; blk < b1; blk += 6) {
-      const T* A = &M[(size_t)blk * 25 + r * 5];
-      const double* xj = &x[(size_t)ja[blk] * 5];
+  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, x);
+  double rhs[5];
 #pragma unroll
-      for (int c = 0; c < 5; c++) acc += ld_blk(&A[c]) * xj[c];
-    }
-  }
-  part[w][lane] = acc;
-  __syncwarp();
+  for (int r = 0; r < 5; r++) rhs[r] = __shfl_sync(0xffffffffu, s, 5 * r);
   if (lane == 0) {
-    double rhs[5];
-    for (int rr = 0; rr < 5; rr++) {
-      double s = 0.0;
-      for (int m = 0; m < 6; m++) s += part[w][rr + 5 * m];
-      rhs[rr] = b[(size_t)i * 5 + rr] - s;
-    }
     int p[5];
-    for (int rr = 0; rr < 5; rr++) p[rr] = piv[(size_t)i * 5 + rr];
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      rhs[r] = b[(size_t)i * 5 + r] - rhs[r];
+      p[r] = piv[(size_t)i * 5 + r];
+    }
     lusolve5(&dlu[(size_t)i * 25], rhs, p);
-    for (int rr = 0; rr < 5; rr++) x[(size_t)i * 5 + rr] = rhs[rr];
+#pragma unroll
+    for (int r = 0; r < 5; r++) x[(size_t)i * 5 + r] = rhs[r];
   }
 }
 
 // Block sparse matrix-vector product y = A x (CRS MatVecMultiply,
-// ucs/crs.tcc:484) with the FP64 diagonal, warp per block row.
+// ucs/crs.tcc:484), warp per block row, with the FP64 diagonal.
 template <class T>
 __global__ void __launch_bounds__(256) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
                                               const T* __restrict__ M, const double* __restrict__ diag,
                                               const double* __restrict__ x, double* __restrict__ y) {
-  __shared__ double part[8][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + w;
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= nnode) return;
-  const int b0 = ia[i] + 1, b1 = ia[i + 1];
-  const int r = lane % 5, kb = lane / 5;
-  double acc = 0.0;
-  if (lane < 30) {
-    for (int blk = b0 + kb; blk < b1; blk += 6) {
-      const T* A = &M[(size_t)blk * 25 + r * 5];
-      const double* xj = &x[(size_t)ja[blk] * 5];
-#pragma unroll
-      for (int c = 0; c < 5; c++) acc += ld_blk(&A[c]) * xj[c];
-    }
-    if (kb == 0) {
-      const double* D = &diag[(size_t)i * 25 + r * 5];
-      const double* xi = &x[(size_t)i * 5];
-      for (int c = 0; c < 5; c++) acc += D[c] * xi[c];
-    }
-  }
-  part[w][lane] = acc;
-  __syncwarp();
-  if (lane < 5) {
-    double s = 0.0;
-    for (int m = 0; m < 6; m++) s += part[w][lane + 5 * m];
-    y[(size_t)i * 5 + lane] = s;
-  }
+  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, x);
+  double d = 0.0;
+  if (lane < 25) d = diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5];
+  d = sum5(d);
+  if (lane < 25 && lane % 5 == 0) y[(size_t)i * 5 + lane / 5] = s + d;
 }
 
 // Newton update (NewtonIterate, ucs/solutionSpace.tcc:772-818): NaN/Inf

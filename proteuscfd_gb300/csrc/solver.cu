@@ -18,6 +18,7 @@
 //  * FP64 throughout the residual path.
 #include "../../include/pcfd.h"
 #include "flux_device.cuh"
+#include "umma.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -79,12 +80,16 @@ enum HealthSlot {
 // Kernel timers, one per launch site (TimerList analogue)
 enum TimerId {
   T_BC = 0, T_GRAD, T_LIMITER, T_EDGEFLUX, T_CLIP, T_BEDGEFLUX, T_GATHER, T_NORM, T_SETUP,
-  T_JAC_EDGE, T_JAC_BEDGE, T_JAC_DIAG, T_JAC_FINISH, T_SGS, T_SPMV, T_KRYLOV, T_UPDATE, T_TIMESTEP, T_COUNT
+  T_JAC_EDGE, T_JAC_BEDGE, T_JAC_DIAG, T_JAC_FINISH, T_SGS, T_SPMV, T_KRYLOV, T_UPDATE, T_TIMESTEP, T_LP_FWD,
+  T_LP_BWD, T_COUNT
 };
 const char* kTimerNames[T_COUNT] = {"bc_update", "lsq_gradient", "venkat_limiter", "edge_flux", "pressure_clip",
                                     "bedge_flux", "residual_gather", "norm_reduce", "setup", "jac_edge",
                                     "jac_bedge", "jac_diag", "jac_finish_lu", "sgs_sweep", "spmv",
-                                    "krylov_vec", "apply_dq", "timestep"};
+                                    "krylov_vec", "apply_dq", "timestep", "learned_forward",
+                                    "learned_backward"};
+
+struct Learned;
 
 struct Solver {
   // sizes
@@ -176,6 +181,9 @@ struct Solver {
 
   // profiling
   int profile = 0;
+  // learned preconditioner (pcfd_lp_*), with the mesh means its features use
+  Learned* lp = nullptr;
+  double lp_lmean = 1.0, lp_vmean = 1.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double t_ms[T_COUNT] = {0};
   long long t_n[T_COUNT] = {0};
@@ -1090,6 +1098,7 @@ __global__ void k_to_df(long long n, const double* __restrict__ in, dfl* __restr
     out[i] = to_df(in[i]);
 }
 #include "implicit.cuh"
+#include "learned.cuh"
 
 // -------------------------------------------------------------------------
 // host helpers
@@ -1111,8 +1120,11 @@ int dput(T** p, const T* h, size_t n) {
   return PCFD_OK;
 }
 
+void free_learned(Learned* lp);
+
 void free_solver(Solver* s) {
   if (!s) return;
+  free_learned(s->lp);
   void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
@@ -1464,8 +1476,12 @@ int run_jacobian_t(Solver* s) {
   JacConst jk = make_jac_const(s);
   BcConst bk = make_bc_const(s);
   int rc = launch(s, T_JAC_EDGE, [&] {
-    k_jac_edge<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
-                                                             s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
+    if (s->arith)
+      k_jac_edge_df<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
+                                                                  s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
+    else
+      k_jac_edge<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
+                                                               s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
   });
   if (rc) return rc;
   if (s->nbedge > 0) {
@@ -1637,9 +1653,19 @@ int run_mdot(Solver* s, const double* V, int nv, const double* w, double* host_o
 // products), Givens rotations on the host.  FGMRES has no counterpart on the
 // reference's Newton path: its CRS::GMRES (ucs/crs.tcc:176) is a fixed-
 // preconditioner restarted GMRES used by the design modes only.
-int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters) {
+int lp_precondition(Solver* s, int nsgs, const double* v, double* z);
+
+// Restarted right-preconditioned flexible GMRES (Saad 1993) with classical
+// Gram-Schmidt applied twice; the reference's GMRES (ucs/crs.tcc:176) is the
+// non-flexible form.  Preconditioner: nsgs block-SGS sweeps, or with use_lp
+// the learned correction on top of them; a cycle in which the learned
+// preconditioner reduces the residual by less than 10 % switches the rest of
+// the solve to plain SGS and adds one cycle (counted in *fallbacks).
+int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp = false,
+               int* fallbacks = nullptr) {
   const int m = std::max(1, std::min(o->fgmres_m > 0 ? o->fgmres_m : 30, 60));
-  const int restarts = std::max(1, o->fgmres_restarts);
+  int restarts = std::max(1, o->fgmres_restarts);
+  if (fallbacks) *fallbacks = 0;
   const double rtol = o->fgmres_rtol > 0.0 ? o->fgmres_rtol : 1e-3;
   int rc = ensure_krylov(s, m);
   if (rc) return rc;
@@ -1672,7 +1698,11 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters)
     for (; j < m; j++) {
       double* zj = Z + (size_t)j * n;
       CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(double), s->stream));
-      if ((rc = run_sgs(s, std::max(1, o->nsgs), V + (size_t)j * n, zj, nullptr))) return rc;
+      if (use_lp) {
+        if ((rc = lp_precondition(s, std::max(1, o->nsgs), V + (size_t)j * n, zj))) return rc;
+      } else if ((rc = run_sgs(s, std::max(1, o->nsgs), V + (size_t)j * n, zj, nullptr))) {
+        return rc;
+      }
       if ((rc = run_spmv(s, zj, w))) return rc;
       // CGS2
       for (int k = 0; k <= j + 1; k++) hcol[k] = 0.0;
@@ -1721,9 +1751,269 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters)
     if ((rc = launch(s, T_KRYLOV, [&] { k_combine<<<kNormBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
       return rc;
     if (rel < rtol) break;
+    if (use_lp && rel > 0.9 * beta / beta0) {
+      use_lp = false;
+      restarts++;
+      if (fallbacks) (*fallbacks)++;
+    }
   }
   if (relres) *relres = rel;
   if (iters) *iters = total;
+  return PCFD_OK;
+}
+
+// -------------------------------------------------------------------------
+// learned right preconditioner (kernels in learned.cuh)
+// -------------------------------------------------------------------------
+
+struct Learned {
+  int n = 0;
+  long long nnz = 0;
+  float4* ef = nullptr;           // [nnz] oriented edge features
+  float* invdeg = nullptr;        // [n]
+  float* w = nullptr;             // [NPARAM] FP32 master parameters
+  float* g = nullptr;             // [NPARAM + 1] gradient, then the loss sum
+  float *m1 = nullptr, *m2 = nullptr;  // Adam moments
+  int adam_t = 0;
+  __nv_bfloat16 *img_fwd = nullptr, *img_bwd = nullptr;  // [NL][LP_IMG]
+  float* x = nullptr;             // [n][NIN]
+  __nv_bfloat16* h = nullptr;     // [NL+1][n][H]
+  __nv_bfloat16* m = nullptr;     // [NL][n][H]
+  float *out = nullptr, *t = nullptr;        // [n][NOUT]
+  float *dh = nullptr, *dhs = nullptr, *dm = nullptr;  // [n][H]
+  __nv_bfloat16* dz = nullptr;    // [n][H]
+  float* part = nullptr;          // per-block gradient partials
+  size_t part_len = 0;
+  double *y = nullptr, *sigma = nullptr, *vbuf = nullptr;  // [n][5], [1], [n][5]
+  int* err = nullptr;
+  int grid_red = 0;               // blocks of the grid-stride backward kernels
+  int npb = 0;                    // nodes per block of the weight-gradient kernels
+  std::vector<float*> sx, st;     // stored training pairs
+};
+
+void free_learned(Learned* lp) {
+  if (!lp) return;
+  void* ptrs[] = {lp->ef, lp->invdeg, lp->w, lp->g, lp->m1, lp->m2, lp->img_fwd, lp->img_bwd, lp->x, lp->h, lp->m,
+                  lp->out, lp->t, lp->dh, lp->dhs, lp->dm, lp->dz, lp->part, lp->y, lp->sigma, lp->vbuf, lp->err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (float* p : lp->sx) cudaFree(p);
+  for (float* p : lp->st) cudaFree(p);
+  delete lp;
+}
+
+// seeded initial parameters: Kaiming-uniform matrices, unit gates, zero
+// decoder (the preconditioner starts as its SGS base)
+void lp_initial_params(unsigned long long seed, std::vector<float>& w) {
+  w.assign(LP_NPARAM, 0.f);
+  unsigned long long st = seed;
+  auto uni = [&](double a) {
+    st += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = st;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)(a * (2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0));
+  };
+  for (int i = 0; i < LP_H * LP_NIN; i++) w[LP_OFF_WIN + i] = uni(std::sqrt(6.0 / LP_NIN));
+  for (int l = 0; l < LP_NL; l++) {
+    float* wl = &w[LP_OFF_L0 + l * LP_L_SIZE];
+    for (int i = 0; i < LP_H * LP_NE; i++) wl[LP_L_WE + i] = uni(0.1);
+    for (int i = 0; i < LP_H; i++) wl[LP_L_CE + i] = 1.f;
+    for (int i = 0; i < LP_H * LP_H; i++) wl[LP_L_WS + i] = uni(std::sqrt(6.0 / (2 * LP_H)));
+    for (int i = 0; i < LP_H * LP_H; i++) wl[LP_L_WM + i] = uni(std::sqrt(6.0 / (2 * LP_H)));
+  }
+}
+
+int lp_pack(Solver* s) {
+  Learned* lp = s->lp;
+  return launch(s, T_LP_BWD, [&] {
+    k_lp_pack<<<nblk(LP_NL * LP_IMG, 256), 256, 0, s->stream>>>(lp->w, lp->img_fwd, lp->img_bwd);
+  });
+}
+
+int lp_check_err(Solver* s) {
+  int e = 0;
+  CUDA_TRY(cudaMemcpyAsync(&e, s->lp->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (e) {
+    CUDA_TRY(cudaMemsetAsync(s->lp->err, 0, sizeof(int), s->stream));
+    return set_err(PCFD_ERR_NUMERIC, "learned preconditioner: tensor-core wait expired");
+  }
+  return PCFD_OK;
+}
+
+// Forward pass from the features in lp->x.  train: store h, m and out for
+// the backward pass; otherwise write z = y + sigma * out.
+int lp_forward(Solver* s, bool train, double* z) {
+  Learned* lp = s->lp;
+  const int n = lp->n;
+  const size_t nh = (size_t)n * LP_H;
+  int rc = launch(s, T_LP_FWD, [&] {
+    k_lp_encode<<<nblk((long long)n * (LP_H / 2), 256), 256, 0, s->stream>>>(n, lp->x, lp->w, lp->h);
+  });
+  if (rc) return rc;
+  const int tiles = nblk(n, LP_TILE);
+  for (int l = 0; l < LP_NL; l++) {
+    const float* wl = lp->w + LP_OFF_L0 + l * LP_L_SIZE;
+    const __nv_bfloat16* hin = lp->h + (train ? l : (l & 1)) * nh;
+    __nv_bfloat16* hout = lp->h + (train ? l + 1 : ((l + 1) & 1)) * nh;
+    __nv_bfloat16* mout = train ? lp->m + l * nh : nullptr;
+    const __nv_bfloat16* img = lp->img_fwd + (size_t)l * LP_IMG;
+    rc = launch(s, T_LP_FWD, [&] {
+      if (l < LP_NL - 1)
+        k_lp_layer<false><<<tiles, LP_THREADS, LP_SMEM, s->stream>>>(
+            n, s->d_nptr, s->d_nnbr, lp->ef, lp->invdeg, hin, wl, img, hout, mout, lp->w, nullptr, nullptr, nullptr,
+            nullptr, lp->err);
+      else
+        k_lp_layer<true><<<tiles, LP_THREADS, LP_SMEM, s->stream>>>(
+            n, s->d_nptr, s->d_nnbr, lp->ef, lp->invdeg, hin, wl, img, train ? hout : nullptr, mout, lp->w,
+            train ? lp->out : nullptr, lp->y, lp->sigma, train ? nullptr : z, lp->err);
+    });
+    if (rc) return rc;
+  }
+  return PCFD_OK;
+}
+
+// gradient of the loss against lp->t into lp->g (after lp_forward(train))
+int lp_backward(Solver* s) {
+  Learned* lp = s->lp;
+  const int n = lp->n;
+  const size_t nh = (size_t)n * LP_H;
+  const int tiles = nblk(n, LP_TILE);
+  const int gr = lp->grid_red;
+  const int nwb = nblk(n, lp->npb);
+  auto reduce = [&](int nb, int len, float* dst) {
+    return launch(s, T_LP_BWD, [&] { k_lp_reduce<<<nblk(len, 256), 256, 0, s->stream>>>(nb, len, lp->part, dst); });
+  };
+  int rc = launch(s, T_LP_BWD, [&] {
+    k_lp_dec_bwd<<<gr, 256, 0, s->stream>>>(n, lp->out, lp->t, lp->h + LP_NL * nh, lp->w, lp->dh, lp->part);
+  });
+  if (rc || (rc = reduce(gr, LP_DEC_LEN, lp->g + LP_OFF_WOUT))) return rc;
+  for (int l = LP_NL - 1; l >= 0; l--) {
+    const float* wl = lp->w + LP_OFF_L0 + l * LP_L_SIZE;
+    float* gl = lp->g + LP_OFF_L0 + l * LP_L_SIZE;
+    rc = launch(s, T_LP_BWD, [&] {
+      k_lp_layer_bwd<<<tiles, LP_THREADS, LP_SMEM, s->stream>>>(n, lp->dh, lp->h + (l + 1) * nh,
+                                                               lp->img_bwd + (size_t)l * LP_IMG, lp->dz, lp->dhs,
+                                                               lp->dm, lp->err);
+    });
+    if (rc) return rc;
+    rc = launch(s, T_LP_BWD, [&] {
+      k_lp_wgrad<<<nwb, 256, 0, s->stream>>>(n, lp->npb, lp->dz, lp->h + l * nh, lp->m + l * nh, lp->part);
+    });
+    if (rc || (rc = reduce(nwb, LP_WG_LEN, gl + LP_L_WS))) return rc;
+    rc = launch(s, T_LP_BWD, [&] {
+      k_lp_gather_bwd<<<gr, 256, 0, s->stream>>>(n, s->d_nptr, s->d_nnbr, lp->ef, lp->invdeg, lp->h + l * nh, wl,
+                                                lp->dhs, lp->dm, lp->dh, lp->part);
+    });
+    if (rc || (rc = reduce(gr, LP_GB_LEN, gl + LP_L_WE))) return rc;
+  }
+  rc = launch(s, T_LP_BWD, [&] {
+    k_lp_enc_bwd<<<nwb, 256, 0, s->stream>>>(n, lp->npb, lp->dh, lp->h, lp->x, lp->part);
+  });
+  if (rc || (rc = reduce(nwb, LP_EB_LEN, lp->g + LP_OFF_WIN))) return rc;
+  return PCFD_OK;
+}
+
+// sigma of lp->y, then the node features into lp->x
+int lp_features(Solver* s) {
+  Learned* lp = s->lp;
+  int rc = launch(s, T_LP_FWD, [&] {
+    k_sumsq<<<kNormBlocks, kNormThreads, 0, s->stream>>>((long long)lp->n * NEQN, lp->y, s->d_part);
+  });
+  if (rc) return rc;
+  rc = launch(s, T_LP_FWD, [&] {
+    k_lp_sigma<<<1, 256, 0, s->stream>>>(kNormBlocks, s->d_part, (double)lp->n * NEQN, lp->sigma);
+  });
+  if (rc) return rc;
+  double qinf[NVARS];
+  host_qinf(s->prm, qinf);
+  const double cinf = std::sqrt(s->prm.gamma * qinf[6] / qinf[0]);
+  return launch(s, T_LP_FWD, [&] {
+    k_lp_features<<<nblk(lp->n, 256), 256, 0, s->stream>>>(lp->n, lp->y, lp->sigma, s->d_q, s->d_vol, qinf[0],
+                                                          qinf[6], cinf, s->lp_vmean, lp->x);
+  });
+}
+
+// z = y + sigma N(x(y)),  y = nsgs SGS sweeps on v
+int lp_precondition(Solver* s, int nsgs, const double* v, double* z) {
+  Learned* lp = s->lp;
+  if (!lp) return set_err(PCFD_ERR_STATE, "learned preconditioner: pcfd_lp_init not called");
+  CUDA_TRY(cudaMemsetAsync(lp->y, 0, (size_t)lp->n * NEQN * sizeof(double), s->stream));
+  int rc = run_sgs(s, nsgs, v, lp->y, nullptr);
+  if (rc || (rc = lp_features(s))) return rc;
+  return lp_forward(s, false, z);
+}
+
+int lp_adam_step(Solver* s, double lr) {
+  Learned* lp = s->lp;
+  lp->adam_t++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - std::pow(b1, (float)lp->adam_t), bc2 = 1.f - std::pow(b2, (float)lp->adam_t);
+  int rc = launch(s, T_LP_BWD, [&] {
+    k_lp_adam<<<nblk(LP_NPARAM, 256), 256, 0, s->stream>>>(LP_NPARAM, lp->w, lp->g, lp->m1, lp->m2, (float)lr,
+                                                          b1, b2, 1e-8f, bc1, bc2);
+  });
+  if (rc) return rc;
+  return lp_pack(s);
+}
+
+int lp_alloc(Solver* s) {
+  Learned* lp = new Learned();
+  s->lp = lp;
+  const int n = s->nnode;
+  lp->n = n;
+  lp->nnz = 2LL * s->nedge;
+  lp->grid_red = std::min(nblk(n, 8), 4 * 152);
+  lp->npb = std::max(256, nblk(n, 1216));
+  const int nwb = nblk(n, lp->npb);
+  lp->part_len = std::max({(size_t)lp->grid_red * LP_DEC_LEN, (size_t)lp->grid_red * LP_GB_LEN,
+                           (size_t)nwb * LP_WG_LEN, (size_t)nwb * LP_EB_LEN});
+  const size_t nh = (size_t)n * LP_H;
+  int rc;
+  if ((rc = dalloc(&lp->ef, std::max<long long>(lp->nnz, 1)))) return rc;
+  if ((rc = dalloc(&lp->invdeg, n))) return rc;
+  if ((rc = dalloc(&lp->w, LP_NPARAM))) return rc;
+  if ((rc = dalloc(&lp->g, LP_NPARAM + 1))) return rc;
+  if ((rc = dalloc(&lp->m1, LP_NPARAM))) return rc;
+  if ((rc = dalloc(&lp->m2, LP_NPARAM))) return rc;
+  if ((rc = dalloc(&lp->img_fwd, (size_t)LP_NL * LP_IMG))) return rc;
+  if ((rc = dalloc(&lp->img_bwd, (size_t)LP_NL * LP_IMG))) return rc;
+  if ((rc = dalloc(&lp->x, (size_t)n * LP_NIN))) return rc;
+  if ((rc = dalloc(&lp->h, (LP_NL + 1) * nh))) return rc;
+  if ((rc = dalloc(&lp->m, LP_NL * nh))) return rc;
+  if ((rc = dalloc(&lp->out, (size_t)n * LP_NOUT))) return rc;
+  if ((rc = dalloc(&lp->t, (size_t)n * LP_NOUT))) return rc;
+  if ((rc = dalloc(&lp->dh, nh))) return rc;
+  if ((rc = dalloc(&lp->dhs, nh))) return rc;
+  if ((rc = dalloc(&lp->dm, nh))) return rc;
+  if ((rc = dalloc(&lp->dz, nh))) return rc;
+  if ((rc = dalloc(&lp->part, lp->part_len))) return rc;
+  if ((rc = dalloc(&lp->y, (size_t)n * NEQN))) return rc;
+  if ((rc = dalloc(&lp->vbuf, (size_t)n * NEQN))) return rc;
+  if ((rc = dalloc(&lp->sigma, 1))) return rc;
+  if ((rc = dalloc(&lp->err, 1))) return rc;
+  CUDA_TRY(cudaMemsetAsync(lp->err, 0, sizeof(int), s->stream));
+  CUDA_TRY(cudaMemsetAsync(lp->h, 0, (LP_NL + 1) * nh * sizeof(__nv_bfloat16), s->stream));
+  CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
+  CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
+  CUDA_TRY(cudaFuncSetAttribute(k_lp_layer_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
+  return launch(s, T_SETUP, [&] {
+    k_lp_graph<<<nblk(n, 256), 256, 0, s->stream>>>(n, s->d_nptr, s->d_nedg, s->d_en, s->d_ea, s->d_xyz,
+                                                    s->lp_lmean, lp->ef, lp->invdeg);
+  });
+}
+
+int lp_set_params(Solver* s, const float* w) {
+  Learned* lp = s->lp;
+  CUDA_TRY(cudaMemcpyAsync(lp->w, w, LP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemsetAsync(lp->m1, 0, LP_NPARAM * sizeof(float), s->stream));
+  CUDA_TRY(cudaMemsetAsync(lp->m2, 0, LP_NPARAM * sizeof(float), s->stream));
+  lp->adam_t = 0;
+  int rc = lp_pack(s);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
   return PCFD_OK;
 }
 
@@ -1904,6 +2194,20 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dput(&s->d_bnrm, bnrm.data(), nb));
   TRY(dput(&s->d_xyz, m->xyz, 3 * nn));
   TRY(dput(&s->d_vol, m->vol, nn));
+  {
+    // mean edge length and mean dual volume, summed in index order (the
+    // learned preconditioner's feature scales)
+    double ls = 0.0, vs = 0.0;
+    for (long long e = 0; e < ne; e++) {
+      const double* a = &m->xyz[3 * m->edges[2 * e]];
+      const double* b = &m->xyz[3 * m->edges[2 * e + 1]];
+      const double dx = b[0] - a[0], dy = b[1] - a[1], dz = b[2] - a[2];
+      ls += std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    for (long long i = 0; i < nn; i++) vs += m->vol[i];
+    s->lp_lmean = ne > 0 ? ls / ne : 1.0;
+    s->lp_vmean = nn > 0 ? vs / nn : 1.0;
+  }
   TRY(dput(&s->d_nptr, nptr.data(), nn + 1));
   TRY(dput(&s->d_nedg, nedg.data(), 2 * ne));
   TRY(dput(&s->d_nnbr, nnbr.data(), 2 * ne));
@@ -2322,8 +2626,10 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   Solver* s = (Solver*)h;
   if (!s || !o || o->iter < 1 || o->nsgs < 0 || !(o->cfl > 0.0))
     return set_err(PCFD_ERR_ARG, "pcfd_newton_step: bad arguments");
-  if (o->linear_solver != 0 && o->linear_solver != 1)
-    return set_err(PCFD_ERR_ARG, "pcfd_newton_step: linear_solver must be 0 (SGS) or 1 (FGMRES)");
+  if (o->linear_solver < 0 || o->linear_solver > 2)
+    return set_err(PCFD_ERR_ARG, "pcfd_newton_step: linear_solver must be 0 (SGS), 1 (FGMRES) or 2 (learned)");
+  if (o->linear_solver == 2 && !s->lp)
+    return set_err(PCFD_ERR_STATE, "pcfd_newton_step: linear_solver 2 needs pcfd_lp_init");
   int rc;
   if (o->jac_precision != s->jac_prec && (rc = ensure_matrix(s, o->jac_precision))) return rc;
   const double cfl = ramp_cfl(o->iter, o->cfl_start > 0.0 ? o->cfl_start : o->cfl, o->cfl, o->cfl_ramp_steps);
@@ -2351,14 +2657,15 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   }
   if ((rc = run_residual(s, s->arith, !ho_now))) return rc;
   double lin = 0.0;
-  int lin_it = 0;
+  int lin_it = 0, fallbacks = 0;
   CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));
   if (o->nsgs > 0) {
     if (o->linear_solver == 0) {
       if ((rc = run_sgs(s, o->nsgs, s->d_b, s->d_x, &lin))) return rc;
       lin_it = o->nsgs;
     } else {
-      if ((rc = run_fgmres(s, o, &lin, &lin_it))) return rc;
+      if ((rc = run_fgmres(s, o, &lin, &lin_it, o->linear_solver == 2, &fallbacks))) return rc;
+      if (o->linear_solver == 2 && (rc = lp_check_err(s))) return rc;
     }
   }
   double dqn = 0.0;
@@ -2372,8 +2679,206 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
     rep->lin_res = lin;
     rep->lin_iters = lin_it;
     rep->cfl = cfl;
+    rep->lp_fallbacks = fallbacks;
   } else {
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
+  return PCFD_OK;
+}
+
+// ---- learned right preconditioner --------------------------------------
+
+PCFD_API int pcfd_lp_init(pcfd_solver_t h, unsigned long long seed) {
+  Solver* s = (Solver*)h;
+  if (!s) return set_err(PCFD_ERR_ARG, "null handle");
+  free_learned(s->lp);
+  s->lp = nullptr;
+  int rc = lp_alloc(s);
+  if (rc) {
+    free_learned(s->lp);
+    s->lp = nullptr;
+    return rc;
+  }
+  std::vector<float> w;
+  lp_initial_params(seed, w);
+  return lp_set_params(s, w.data());
+}
+
+static Learned* lp_of(pcfd_solver_t h, const char* fn) {
+  Solver* s = (Solver*)h;
+  if (!s) {
+    set_err(PCFD_ERR_ARG, std::string(fn) + ": null handle");
+    return nullptr;
+  }
+  if (!s->lp) set_err(PCFD_ERR_STATE, std::string(fn) + ": pcfd_lp_init not called");
+  return s->lp;
+}
+
+PCFD_API int pcfd_lp_get_params(pcfd_solver_t h, float* w) {
+  Learned* lp = lp_of(h, "pcfd_lp_get_params");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!w) return set_err(PCFD_ERR_ARG, "pcfd_lp_get_params: null pointer");
+  Solver* s = (Solver*)h;
+  CUDA_TRY(cudaMemcpyAsync(w, lp->w, LP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_lp_set_params(pcfd_solver_t h, const float* w) {
+  Learned* lp = lp_of(h, "pcfd_lp_set_params");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!w) return set_err(PCFD_ERR_ARG, "pcfd_lp_set_params: null pointer");
+  return lp_set_params((Solver*)h, w);
+}
+
+PCFD_API int pcfd_lp_forward(pcfd_solver_t h, const float* x, float* out) {
+  Learned* lp = lp_of(h, "pcfd_lp_forward");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!x || !out) return set_err(PCFD_ERR_ARG, "pcfd_lp_forward: null pointer");
+  Solver* s = (Solver*)h;
+  CUDA_TRY(cudaMemcpyAsync(lp->x, x, (size_t)lp->n * LP_NIN * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  int rc = lp_forward(s, true, nullptr);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(out, lp->out, (size_t)lp->n * LP_NOUT * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  return lp_check_err(s);
+}
+
+PCFD_API int pcfd_lp_loss_grad(pcfd_solver_t h, const float* x, const float* t, float* grad, double* loss) {
+  Learned* lp = lp_of(h, "pcfd_lp_loss_grad");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!x || !t) return set_err(PCFD_ERR_ARG, "pcfd_lp_loss_grad: null pointer");
+  Solver* s = (Solver*)h;
+  CUDA_TRY(cudaMemcpyAsync(lp->x, x, (size_t)lp->n * LP_NIN * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(lp->t, t, (size_t)lp->n * LP_NOUT * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  int rc = lp_forward(s, true, nullptr);
+  if (rc || (rc = lp_backward(s))) return rc;
+  std::vector<float> g(LP_NPARAM + 1);
+  CUDA_TRY(cudaMemcpyAsync(g.data(), lp->g, (LP_NPARAM + 1) * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  if ((rc = lp_check_err(s))) return rc;
+  if (grad) std::memcpy(grad, g.data(), LP_NPARAM * sizeof(float));
+  if (loss) *loss = (double)g[LP_NPARAM] / (5.0 * lp->n);
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_lp_features(pcfd_solver_t h, const double* y, float* x, double* sigma_out) {
+  Learned* lp = lp_of(h, "pcfd_lp_features");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!y || !x) return set_err(PCFD_ERR_ARG, "pcfd_lp_features: null pointer");
+  Solver* s = (Solver*)h;
+  CUDA_TRY(cudaMemcpyAsync(lp->y, y, (size_t)lp->n * NEQN * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc = lp_features(s);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(x, lp->x, (size_t)lp->n * LP_NIN * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  double sg = 0.0;
+  CUDA_TRY(cudaMemcpyAsync(&sg, lp->sigma, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (sigma_out) *sigma_out = sg;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_lp_apply(pcfd_solver_t h, int nsgs, const double* v, double* z) {
+  Learned* lp = lp_of(h, "pcfd_lp_apply");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  if (!v || !z || nsgs < 1) return set_err(PCFD_ERR_ARG, "pcfd_lp_apply: bad arguments");
+  Solver* s = (Solver*)h;
+  const size_t bytes = (size_t)lp->n * NEQN * sizeof(double);
+  CUDA_TRY(cudaMemcpyAsync(lp->vbuf, v, bytes, cudaMemcpyHostToDevice, s->stream));
+  int rc = lp_precondition(s, nsgs, lp->vbuf, s->d_x);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(z, s->d_x, bytes, cudaMemcpyDeviceToHost, s->stream));
+  return lp_check_err(s);
+}
+
+// store the features of lp->y and the target (xt - y)/sigma as a new pair
+int lp_store_pair(Solver* s, const double* xt) {
+  Learned* lp = s->lp;
+  const size_t n5 = (size_t)lp->n * NEQN;
+  int rc = lp_features(s);
+  if (rc) return rc;
+  float *sx = nullptr, *st = nullptr;
+  if ((rc = dalloc(&sx, (size_t)lp->n * LP_NIN))) return rc;
+  if ((rc = dalloc(&st, n5))) {
+    cudaFree(sx);
+    return rc;
+  }
+  lp->sx.push_back(sx);
+  lp->st.push_back(st);
+  CUDA_TRY(cudaMemcpyAsync(sx, lp->x, (size_t)lp->n * LP_NIN * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
+  return launch(s, T_LP_BWD, [&] {
+    k_lp_target<<<kNormBlocks, 256, 0, s->stream>>>((long long)n5, xt, lp->y, lp->sigma, st);
+  });
+}
+
+PCFD_API int pcfd_lp_collect(pcfd_solver_t h, int nsgs, double rtol, int krylov_pairs, int* nsamples_out) {
+  Learned* lp = lp_of(h, "pcfd_lp_collect");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  Solver* s = (Solver*)h;
+  if (nsgs < 1 || !(rtol > 0.0) || krylov_pairs < 0)
+    return set_err(PCFD_ERR_ARG, "pcfd_lp_collect: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_lp_collect: no linear system (run pcfd_newton_step first)");
+  const size_t n5 = (size_t)lp->n * NEQN;
+  // dq: A dq = b to rtol by SGS-preconditioned FGMRES(30)
+  pcfd_newton_opts o = {};
+  o.nsgs = 1;
+  o.fgmres_m = 30;
+  o.fgmres_restarts = 50;
+  o.fgmres_rtol = rtol;
+  CUDA_TRY(cudaMemsetAsync(s->d_x, 0, n5 * sizeof(double), s->stream));
+  double rel = 1.0;
+  int it = 0;
+  int rc = run_fgmres(s, &o, &rel, &it);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemsetAsync(lp->y, 0, n5 * sizeof(double), s->stream));
+  if ((rc = run_sgs(s, nsgs, s->d_b, lp->y, nullptr)) || (rc = lp_store_pair(s, s->d_x))) return rc;
+  // (A z_j, z_j) for the directions of the last FGMRES cycle
+  const int nk = std::min(std::min(krylov_pairs, it), s->fg_m);
+  for (int j = 0; j < nk; j++) {
+    const double* zj = s->d_Z + (size_t)j * n5;
+    if ((rc = run_spmv(s, zj, lp->vbuf))) return rc;
+    CUDA_TRY(cudaMemsetAsync(lp->y, 0, n5 * sizeof(double), s->stream));
+    if ((rc = run_sgs(s, nsgs, lp->vbuf, lp->y, nullptr)) || (rc = lp_store_pair(s, zj))) return rc;
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (nsamples_out) *nsamples_out = (int)lp->sx.size();
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_lp_clear_samples(pcfd_solver_t h) {
+  Learned* lp = lp_of(h, "pcfd_lp_clear_samples");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  CUDA_TRY(cudaStreamSynchronize(((Solver*)h)->stream));
+  for (float* p : lp->sx) cudaFree(p);
+  for (float* p : lp->st) cudaFree(p);
+  lp->sx.clear();
+  lp->st.clear();
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_lp_train(pcfd_solver_t h, int epochs, double lr, double* loss_first, double* loss_last) {
+  Learned* lp = lp_of(h, "pcfd_lp_train");
+  if (!lp) return h ? PCFD_ERR_STATE : PCFD_ERR_ARG;
+  Solver* s = (Solver*)h;
+  if (epochs < 1 || !(lr > 0.0)) return set_err(PCFD_ERR_ARG, "pcfd_lp_train: bad arguments");
+  if (lp->sx.empty()) return set_err(PCFD_ERR_STATE, "pcfd_lp_train: no training pairs (pcfd_lp_collect)");
+  const int ns = (int)lp->sx.size();
+  std::vector<float> lsum(ns);
+  for (int e = 0; e < epochs; e++) {
+    double tot = 0.0;
+    for (int k = 0; k < ns; k++) {
+      CUDA_TRY(cudaMemcpyAsync(lp->x, lp->sx[k], (size_t)lp->n * LP_NIN * sizeof(float), cudaMemcpyDeviceToDevice,
+                               s->stream));
+      CUDA_TRY(cudaMemcpyAsync(lp->t, lp->st[k], (size_t)lp->n * LP_NOUT * sizeof(float), cudaMemcpyDeviceToDevice,
+                               s->stream));
+      int rc = lp_forward(s, true, nullptr);
+      if (rc || (rc = lp_backward(s))) return rc;
+      CUDA_TRY(cudaMemcpyAsync(&lsum[k], lp->g + LP_NPARAM, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+      if ((rc = lp_adam_step(s, lr))) return rc;
+    }
+    int rc = lp_check_err(s);
+    if (rc) return rc;
+    for (int k = 0; k < ns; k++) tot += (double)lsum[k] / (5.0 * lp->n);
+    if (e == 0 && loss_first) *loss_first = tot / ns;
+    if (e == epochs - 1 && loss_last) *loss_last = tot / ns;
   }
   return PCFD_OK;
 }

@@ -8,6 +8,7 @@ ROOT = Path(__file__).resolve().parent.parent
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 _LLP = C.POINTER(C.c_longlong)
+_FP = C.POINTER(C.c_float)
 _lib = None
 
 
@@ -44,6 +45,12 @@ def lib():
             "oracle_matvec": (None, [_DP, _DP, _DP, C.c_int]),
             "oracle_tri_area": (None, [_DP, _DP, _DP, _DP]),
             "oracle_tet_vol": (C.c_double, [_DP, _DP, _DP, _DP]),
+            "oracle_bf16": (C.c_double, [C.c_double]),
+            "oracle_lp_nparam": (C.c_int, []),
+            "oracle_lp_graph": (None, [MV, _IP, _IP, _FP]),
+            "oracle_lp_features": (C.c_double, [C.c_int, _DP, _DP, _DP, _DP, C.c_double, _FP]),
+            "oracle_lp_forward": (None, [C.c_int, _IP, _IP, _FP, _FP, _FP, C.c_int, _DP]),
+            "oracle_lp_loss_grad": (C.c_double, [C.c_int, _IP, _IP, _FP, _FP, _FP, _FP, C.c_int, _DP]),
         }
         for n, (r, a) in protos.items():
             f = getattr(L, n)
@@ -61,6 +68,64 @@ def dp(a):
 def ip(a):
     assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(_IP)
+
+
+def fp(a):
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_FP)
+
+
+class OracleNet:
+    """The learned preconditioner's network on the oracle (CPU, double)."""
+
+    def __init__(self, mesh):
+        self.L = lib()
+        self.n = mesh.nnode
+        nnz = 2 * mesh.nedge
+        self.nptr = np.zeros(self.n + 1, np.int32)
+        self.nbr = np.zeros(nnz, np.int32)
+        self.ef = np.zeros((nnz, 4), np.float32)
+        self.L.oracle_lp_graph(C.byref(mesh.view), ip(self.nptr), ip(self.nbr), fp(self.ef))
+
+    def forward(self, x, w, emulate=1):
+        x = np.ascontiguousarray(x, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        out = np.zeros((self.n, 5))
+        self.L.oracle_lp_forward(self.n, ip(self.nptr), ip(self.nbr), fp(self.ef), fp(x), fp(w), emulate, dp(out))
+        return out
+
+    def loss_grad(self, x, t, w, emulate=1):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        g = np.zeros(self.L.oracle_lp_nparam())
+        loss = self.L.oracle_lp_loss_grad(self.n, ip(self.nptr), ip(self.nbr), fp(self.ef), fp(x), fp(t), fp(w),
+                                          emulate, dp(g))
+        return loss, g
+
+
+def lp_features(y, q, vol, qinf, gamma):
+    n = vol.shape[0]
+    x = np.zeros((n, 11), np.float32)
+    y = np.ascontiguousarray(y, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    vol = np.ascontiguousarray(vol, np.float64)
+    qinf = np.ascontiguousarray(qinf, np.float64)
+    sigma = lib().oracle_lp_features(n, dp(y), dp(q), dp(vol), dp(qinf), gamma, fp(x))
+    return x, sigma
+
+
+def lp_random_params(seed, scale=1.0):
+    """Seeded parameters with every block non-zero (for checks of the backward pass)."""
+    rng = np.random.default_rng(seed)
+    nin, h, ne, nout, nl = 11, 64, 4, 5, 3
+    parts = [rng.uniform(-1, 1, h * nin) * np.sqrt(3.0 / nin), rng.uniform(-0.1, 0.1, h)]
+    for _ in range(nl):
+        parts += [rng.uniform(-0.5, 0.5, h * ne), 1.0 + rng.uniform(-0.1, 0.1, h),
+                  rng.uniform(-1, 1, h * h) * np.sqrt(3.0 / h), rng.uniform(-1, 1, h * h) * np.sqrt(3.0 / h),
+                  rng.uniform(-0.1, 0.1, h)]
+    parts += [rng.uniform(-1, 1, nout * h) * np.sqrt(3.0 / h), rng.uniform(-0.1, 0.1, nout)]
+    return (np.concatenate(parts) * scale).astype(np.float32)
 
 
 class OracleSpace:

@@ -1,0 +1,137 @@
+"""Learned right preconditioner on the GPU, through the C ABI: the network's
+forward pass (tensor-core layer products) and its gradient against the CPU
+oracle, the node features, the preconditioner's base case, training, and
+FGMRES with the learned preconditioner against FGMRES with plain SGS."""
+import numpy as np
+import pytest
+
+from oracle_lib import OracleNet, lp_features, lp_random_params
+from proteuscfd_gb300 import SolutionSpace, cases
+from proteuscfd_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+# BF16 activations: one BF16 rounding step (2^-8 relative) can flip between
+# the tensor-core and the sequential FP32 sums, so outputs agree to ~1e-3
+# in the L2 sense; gradients (BF16 dz operand) to ~1e-2.
+FWD_RTOL = 1e-2
+GRAD_RTOL = 3e-2
+
+
+def make(case_dims=(16, 12, 10), seed=2):
+    c = cases.ns_flatplate(*case_dims, seed=seed)
+    c.param.jac_boundary_eval = 3
+    m = cases.build_mesh(c)
+    S = SolutionSpace(m, c.param)
+    q0 = cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 1)
+    S.set_state(q0)
+    return c, m, S, q0
+
+
+@pytest.fixture(scope="module")
+def small():
+    c, m, S, q0 = make()
+    S.lp_init(7)
+    return c, m, S, q0, OracleNet(m)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
+
+
+def test_params_roundtrip(small):
+    _, _, S, _, _ = small
+    w = S.lp_get_params()
+    assert w.shape == (N.LP_NPARAM,)
+    # decoder starts at zero, gates at one
+    assert np.all(w[26496:] == 0)
+    assert np.all(w[768 + 256:768 + 320] == 1.0)
+    w2 = lp_random_params(11)
+    S.lp_set_params(w2)
+    assert np.array_equal(S.lp_get_params(), w2)
+
+
+@pytest.mark.parametrize("dims", [(17, 12, 10), (23, 17, 9)])
+def test_forward_parity(dims):
+    c, m, S, _ = make(dims)
+    S.lp_init(3)
+    net = OracleNet(m)
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (m.nnode, N.LP_NIN)).astype(np.float32)
+    w = lp_random_params(9)
+    S.lp_set_params(w)
+    out = S.lp_forward(x)
+    ref = net.forward(x, w, emulate=1)
+    assert m.nnode % 128 != 0  # a partial last tile is covered
+    assert rel(out, ref) < FWD_RTOL, rel(out, ref)
+    # against the unrounded network the BF16 error is larger but bounded
+    assert rel(out, net.forward(x, w, emulate=0)) < 5e-2
+
+
+def test_gradient_parity(small):
+    _, m, S, _, net = small
+    rng = np.random.default_rng(6)
+    x = rng.uniform(-1, 1, (m.nnode, N.LP_NIN)).astype(np.float32)
+    t = rng.uniform(-1, 1, (m.nnode, 5)).astype(np.float32)
+    w = lp_random_params(12)
+    S.lp_set_params(w)
+    loss, g = S.lp_loss_grad(x, t)
+    loss_ref, g_ref = net.loss_grad(x, t, w, emulate=1)
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    blocks = {"Win": (0, 704), "bin": (704, 768), "Wout": (26496, 26816), "bout": (26816, 26821)}
+    for l in range(3):
+        b = 768 + l * 8576
+        blocks.update({"We%d" % l: (b, b + 256), "ce%d" % l: (b + 256, b + 320), "Ws%d" % l: (b + 320, b + 4416),
+                       "Wm%d" % l: (b + 4416, b + 8512), "b%d" % l: (b + 8512, b + 8576)})
+    for name, (a, e) in blocks.items():
+        assert rel(g[a:e], g_ref[a:e]) < GRAD_RTOL, (name, rel(g[a:e], g_ref[a:e]))
+
+
+def test_features_parity(small):
+    c, m, S, q0, _ = small
+    rng = np.random.default_rng(8)
+    y = rng.normal(size=(m.nnode, 5)) * 1e-3
+    x, sigma = S.lp_features(y)
+    q = S.get_state()
+    xr, sr = lp_features(y, q[:m.nnode], np.asarray(m.vol), S.qinf(), c.param.gamma)
+    assert abs(sigma - sr) <= 1e-12 * sr
+    assert np.abs(x - xr).max() <= 1e-6 * max(1.0, np.abs(xr).max())
+
+
+def test_initial_preconditioner_is_sgs(small):
+    """With the zero decoder of the initial parameters z = SGS(v) exactly."""
+    _, m, S, _, _ = small
+    S.lp_init(7)
+    S.newton_iterate(1, cfl=5.0, nsgs=2)
+    v = S.get_residual()
+    z = S.lp_apply(v, nsgs=2)
+    x_sgs, _ = S.sgs(2)
+    assert np.array_equal(z, x_sgs)
+
+
+def test_training_and_learned_fgmres():
+    """Pairs from the solver's own Newton systems; training lowers the loss;
+    FGMRES with the learned preconditioner converges, and the Krylov
+    iterations it needs on later systems are compared with plain SGS."""
+    c, m, S, _ = make((20, 14, 12), seed=3)
+    S.lp_init(1)
+    opts = dict(cfl=20.0, cfl_start=1.0, cfl_ramp_steps=10, nsgs=1, linear_solver=1, fgmres_m=30,
+                fgmres_restarts=2, fgmres_rtol=1e-2, jac_precision=1)
+    for it in range(1, 13):
+        S.newton_iterate(it, **opts)
+        if it >= 3:
+            S.lp_collect(nsgs=1, rtol=1e-6, krylov_pairs=10)
+    l0, l1 = S.lp_train(epochs=30, lr=2e-3)
+    assert np.isfinite(l1) and l1 < 0.8 * l0, (l0, l1)
+    # continue the run with both preconditioners on the same systems
+    it_sgs, it_lp = [], []
+    for it in range(13, 19):
+        st = S.get_state()
+        r1 = S.newton_iterate(it, **opts)
+        S.set_state(st)
+        r2 = S.newton_iterate(it, **dict(opts, linear_solver=2))
+        it_sgs.append(r1["lin_iters"])
+        it_lp.append(r2["lin_iters"])
+        assert r2["lin_res"] < 1e-2 or r2["lp_fallbacks"] > 0
+        assert np.isfinite(r2["res"][0])
+    print("krylov iterations sgs", it_sgs, "learned", it_lp)
