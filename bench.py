@@ -176,6 +176,125 @@ def run_reference(args, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+# Newton settings of the convergence study.  "fp64" is the reference's plain
+# method: FP64 residual and Jacobian, 10 block-SGS sweeps per step.  "mixed":
+# double-float residual and Jacobian fluxes, FP32 Jacobian storage,
+# FGMRES(30) right-preconditioned by one SGS sweep.  "mixed_learned": the
+# same with the learned correction on top of the SGS sweep.
+CONV_COMMON = dict(cfl_start=1.0, limiter_freeze=60, first_order_steps=20)
+CONV_ARMS = {
+    "fp64": dict(arith=0, opts=dict(CONV_COMMON, cfl=50.0, cfl_ramp_steps=40, nsgs=10, linear_solver=0,
+                                    jac_precision=0)),
+    "mixed": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=1,
+                                     fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1)),
+    "mixed_learned": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=2,
+                                             fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1)),
+}
+
+
+def train_learned(dims, seed, iters, epochs, lr, krylov_pairs=5):
+    """Training pairs from the mixed solver's own systems on a mesh with
+    another seed; returns the parameters and the training record."""
+    from proteuscfd_gb300 import SolutionSpace, cases
+    case = cases.ns_flatplate(*dims, seed=seed)
+    case.param.jac_boundary_eval = 3
+    m = cases.build_mesh(case)
+    S = SolutionSpace(m, case.param)
+    S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, seed))
+    S.set_residual_arithmetic(1)
+    S.lp_init(1)
+    t0 = time.perf_counter()
+    npairs = 0
+    for it in range(1, iters + 1):
+        S.newton_iterate(it, **CONV_ARMS["mixed"]["opts"])
+        if it >= 3 and it % 3 == 0:
+            npairs = S.lp_collect(nsgs=1, rtol=1e-6, krylov_pairs=krylov_pairs)
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    l0, l1 = S.lp_train(epochs=epochs, lr=lr)
+    t_train = time.perf_counter() - t0
+    w = S.lp_get_params()
+    S.close()
+    return w, {"mesh": "%dx%dx%d" % dims, "seed": seed, "pairs": npairs, "epochs": epochs, "lr": lr,
+               "loss_first_epoch": l0, "loss_last_epoch": l1, "collect_s": round(t_collect, 2),
+               "train_s": round(t_train, 2)}
+
+
+def converge_study(args):
+    """Wall time to a 1e-10 drop of resGlobal on one GPU, per arm, with the
+    final-field and wall-force differences against the FP64 arm."""
+    from proteuscfd_gb300 import SolutionSpace, cases
+    from proteuscfd_gb300 import _native as N
+    w = WORKLOADS[args.converge_workload]
+    dims = (w["nx"], w["ny"], w["nz"])
+    out = {"workload": "ns_flatplate %dx%dx%d (mesh seed 2, state seed 1), second order, Mach 0.8, Re 1e5" % dims,
+           "target_drop": 1e-10, "time_cap_s": args.converge_cap}
+    lp_w = None
+    if "mixed_learned" in args.converge_arms:
+        # same resolution, unseen mesh and state seed
+        lp_w, out["learned_training"] = train_learned(dims, 7, 45, 40, 1e-3)
+    finals = {}
+    for name in args.converge_arms:
+        arm = CONV_ARMS[name]
+        case = cases.ns_flatplate(*dims)
+        case.param.jac_boundary_eval = 3
+        m = cases.build_mesh(case)
+        S = SolutionSpace(m, case.param)
+        S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 1))
+        S.set_residual_arithmetic(arm["arith"])
+        if arm["opts"]["linear_solver"] == 2:
+            S.lp_init(1)
+            S.lp_set_params(lp_w)
+        N.check(N.load().pcfd_device_sync(), "sync")
+        hist, t_at, lin, fb = [], {}, 0, 0
+        t0 = time.perf_counter()
+        for it in range(1, args.converge_iters + 1):
+            rep = S.newton_iterate(it, **arm["opts"])
+            r = rep["res"][0]
+            hist.append(r)
+            lin += rep["lin_iters"]
+            fb += rep["lp_fallbacks"]
+            el = time.perf_counter() - t0
+            for d in (1e-2, 1e-4, 1e-6, 1e-8, 1e-10):
+                if d not in t_at and r <= d * hist[0]:
+                    t_at[d] = [it, round(el, 3)]
+            if not np.isfinite(r) or r <= 1e-10 * hist[0] or el > args.converge_cap:
+                break
+        wall = time.perf_counter() - t0
+        q = S.get_state()
+        finals[name] = (q[:m.nnode, :5].copy(), wall_force(m, case, q))
+        rec = {"iters": len(hist), "wall_s": round(wall, 3), "drop": hist[-1] / hist[0],
+               "reached_1e-10": 1e-10 in t_at, "s_to_drop": {str(k): v for k, v in t_at.items()},
+               "linear_iters_per_step": lin / len(hist), "health": S.health()}
+        if fb:
+            rec["sgs_fallbacks"] = fb
+        out[name] = rec
+        S.close()
+    if "fp64" in finals:
+        qref, fref = finals["fp64"]
+        for name, (qa, fa) in finals.items():
+            if name == "fp64":
+                continue
+            out[name]["field_rel_l2_vs_fp64"] = float(np.linalg.norm(qa - qref) / np.linalg.norm(qref))
+            out[name]["wall_force_rel_err_vs_fp64"] = float(np.linalg.norm(fa - fref) / np.linalg.norm(fref))
+            if out[name]["reached_1e-10"] and out["fp64"]["reached_1e-10"]:
+                out[name]["speedup_vs_fp64"] = out["fp64"]["s_to_drop"]["1e-10"][1] / out[name]["s_to_drop"]["1e-10"][1]
+    return out
+
+
+def wall_force(m, case, q):
+    """Pressure force on the no-slip wall: sum over its boundary half-edges of
+    p(node) times the outward dual-face area vector."""
+    from proteuscfd_gb300 import _native as N
+    be = np.asarray(m.bedges).reshape(-1, 2)
+    ba = np.asarray(m.bedge_area).reshape(-1, 4)
+    tags = np.asarray(m.bfactag)
+    wall = [t for t, b in case.param.bc_type.items() if b == N.BC_NOSLIP]
+    sel = np.isin(tags, wall)
+    p = q[be[sel, 0], 6]
+    return (p[:, None] * ba[sel, :3] * ba[sel, 3:4]).sum(axis=0)
+
+
 def run_gb300(args, ws, rank, local, pg):
     from proteuscfd_gb300 import SolutionSpace, cases
     from proteuscfd_gb300 import _native as N
@@ -291,6 +410,8 @@ def run_gb300(args, ws, rank, local, pg):
         base, _, _ = cpu_sample(12.0, 1)
         line["cpu_baseline"] = base
     S.close()
+    if rank == 0 and ws == 1 and args.converge_arms:
+        line["convergence"] = converge_study(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -305,11 +426,24 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--arith", default="best", choices=["f64", "df", "best", "dfonly"],
                     help="residual arithmetic: FP64, double-float, or double-float when it agrees with FP64")
+    ap.add_argument("--converge", default="fp64,mixed,mixed_learned",
+                    help="comma-separated arms of the time-to-1e-10 study on one GPU ('' to skip)")
+    ap.add_argument("--converge-workload", default="ns64", choices=sorted(WORKLOADS))
+    ap.add_argument("--converge-cap", type=float, default=60.0, help="wall-time cap per arm, seconds")
+    ap.add_argument("--converge-iters", type=int, default=3000, help="Newton iteration cap per arm")
+    ap.add_argument("--converge-only", action="store_true", help="run only the convergence study")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.converge_arms = [a for a in args.converge.split(",") if a]
+    for a in args.converge_arms:
+        if a not in CONV_ARMS:
+            ap.error("unknown convergence arm %r" % a)
     ws, rank, local, pg = dist()
     if args.impl == "reference":
         run_reference(args, rank, pg)
+    elif args.converge_only:
+        if rank == 0:
+            print(json.dumps({"convergence": converge_study(args)}), flush=True)
     else:
         run_gb300(args, ws, rank, local, pg)
     if pg:

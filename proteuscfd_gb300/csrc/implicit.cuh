@@ -391,9 +391,34 @@ __device__ __forceinline__ void lusolve5(const double* a, double* b, const int* 
   }
 }
 
-// Arithmetic of the off-diagonal products: FP64 for the FP64 matrix, FP32
+// Explicit inverse of each LU-factored diagonal block, column c = LuSolve of
+// the unit vector e_c, so that a sweep's diagonal solve is one 25-lane
+// product instead of a serial substitution on one lane (FP64 runs at 2
+// operations per clock per SM on GB300).  Same values as LuSolve in exact
+// arithmetic; the rounding differs at the level of cond(D) * 1e-16.
+__global__ void k_diag_inverse(int nnode, const double* __restrict__ dlu, const int* __restrict__ piv,
+                               double* __restrict__ dinv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  double a[25];
+  int p[5];
+#pragma unroll
+  for (int t = 0; t < 25; t++) a[t] = dlu[(size_t)i * 25 + t];
+#pragma unroll
+  for (int r = 0; r < 5; r++) p[r] = piv[(size_t)i * 5 + r];
+  for (int c = 0; c < 5; c++) {
+    double b[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    b[c] = 1.0;
+    lusolve5(a, b, p);
+    for (int r = 0; r < 5; r++) dinv[(size_t)i * 25 + r * 5 + c] = b[r];
+  }
+}
+
+// Arithmetic of the off-diagonal products: FP64 for the FP64 matrix; FP32
 // for the FP32 and BF16 storage (whose coefficients carry FP32 or coarser
-// rounding already); the diagonal blocks and the LU stay FP64.
+// rounding already), reading an FP32 copy of x, so that no per-coefficient
+// FP64 instruction (a double-to-float conversion runs on the FP64 pipe) is
+// left.  The diagonal blocks and the LU stay FP64.
 template <class T>
 struct OffAcc {
   typedef float type;
@@ -405,8 +430,6 @@ struct OffAcc<double> {
 __device__ __forceinline__ double off_val(double a) { return a; }
 __device__ __forceinline__ float off_val(float a) { return a; }
 __device__ __forceinline__ float off_val(__nv_bfloat16 a) { return __bfloat162float(a); }
-__device__ __forceinline__ double off_x(double x, double) { return x; }
-__device__ __forceinline__ float off_x(double x, float) { return (float)x; }
 
 // Sum over lanes 5r .. 5r+4 of v, left in lane 5r (r = 0..4).
 template <class A>
@@ -421,13 +444,12 @@ __device__ __forceinline__ A sum5(A v) {
 // coefficient (l / 5, l % 5) of every block: each warp load reads 25
 // consecutive coefficients.  The row's column indices come in with one
 // coalesced load (lane b holds block b's), and the coefficient and x loads
-// of eight blocks are issued before any of them is used, so a row costs
-// about three memory latencies however many blocks it has.  Lane 5r
-// receives row r's sum.
+// of eight blocks are issued before any of them is used.  xa is x in the
+// accumulation type.  Lane 5r receives row r's sum.
 template <class T>
 __device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane, const int* __restrict__ ia,
                                                                 const int* __restrict__ ja, const T* __restrict__ M,
-                                                                const double* __restrict__ x) {
+                                                                const typename OffAcc<T>::type* __restrict__ xa) {
   typedef typename OffAcc<T>::type A;
   const unsigned full = 0xffffffffu;
   const int b0 = ia[i] + 1, nb = ia[i + 1] - b0;
@@ -445,7 +467,7 @@ __device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane,
         const int j = __shfl_sync(full, jl, k & 31);
         const bool ok = active && k < nk;
         av[u] = ok ? off_val(M[(size_t)(b0 + base + k) * 25 + lane]) : A(0);
-        xv[u] = ok ? off_x(x[(size_t)j * 5 + c], A(0)) : A(0);
+        xv[u] = ok ? xa[(size_t)j * 5 + c] : A(0);
       }
 #pragma unroll
       for (int u = 0; u < 8; u++) acc = fma(av[u], xv[u], acc);
@@ -454,32 +476,35 @@ __device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane,
   return sum5(acc);
 }
 
+// FP32 copy of an FP64 vector (once per product or sweep)
+__global__ void k_to_f32(long long n, const double* __restrict__ x, float* __restrict__ xf) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    xf[i] = (float)x[i];
+}
+
 // One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62), a
 // warp per block row: rhs = b_i - sum_j A_ij x_j over the off-diagonal
-// blocks, then lane 0 solves the 5x5 diagonal system with its FP64 LU.
+// blocks, then lane 0 solves the 5x5 diagonal system with its FP64 LU and
+// writes x_i (and its FP32 copy when the products read one).
 template <class T>
 __global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restrict__ rows, const int* __restrict__ ia,
                                                    const int* __restrict__ ja, const T* __restrict__ M,
-                                                   const double* __restrict__ dlu, const int* __restrict__ piv,
-                                                   const double* __restrict__ b, double* __restrict__ x) {
+                                                   const double* __restrict__ dinv, const double* __restrict__ b,
+                                                   double* __restrict__ x, typename OffAcc<T>::type* __restrict__ xa) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (gw >= nrows) return;
   const int i = rows[gw];
-  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, x);
-  double rhs[5];
-#pragma unroll
-  for (int r = 0; r < 5; r++) rhs[r] = __shfl_sync(0xffffffffu, s, 5 * r);
-  if (lane == 0) {
-    int p[5];
-#pragma unroll
-    for (int r = 0; r < 5; r++) {
-      rhs[r] = b[(size_t)i * 5 + r] - rhs[r];
-      p[r] = piv[(size_t)i * 5 + r];
-    }
-    lusolve5(&dlu[(size_t)i * 25], rhs, p);
-#pragma unroll
-    for (int r = 0; r < 5; r++) x[(size_t)i * 5 + r] = rhs[r];
+  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, xa);
+  // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
+  const int r = lane / 5, c = lane % 5;
+  const double rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : 0.0;
+  const double rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
+  double v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : 0.0;
+  v = sum5(v);
+  if (lane < 25 && c == 0) {
+    x[(size_t)i * 5 + r] = v;
+    if ((const void*)xa != (const void*)x) xa[(size_t)i * 5 + r] = (typename OffAcc<T>::type)v;
   }
 }
 
@@ -488,11 +513,13 @@ __global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restr
 template <class T>
 __global__ void __launch_bounds__(256) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
                                               const T* __restrict__ M, const double* __restrict__ diag,
-                                              const double* __restrict__ x, double* __restrict__ y) {
+                                              const double* __restrict__ x,
+                                              const typename OffAcc<T>::type* __restrict__ xa,
+                                              double* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= nnode) return;
-  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, x);
+  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, xa);
   double d = 0.0;
   if (lane < 25) d = diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5];
   d = sum5(d);
@@ -647,19 +674,31 @@ __global__ void k_min_final(int nblocks, const double* __restrict__ part, double
 __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const double* __restrict__ V,
                                                         const double* __restrict__ w, double* __restrict__ part,
                                                         int part_stride) {
-  __shared__ double red[kNormThreads / 32];
-  for (int k = 0; k < nv; k++) {
-    const double* v = V + (size_t)k * n;
-    double acc = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-      acc += w[i] * v[i];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  // eight vectors per pass over w: w is read nv/8 times, each V_k once
+  __shared__ double red[kNormThreads / 32][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k0 = 0; k0 < nv; k0 += 8) {
+    const int nk = min(8, nv - k0);
+    double acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) acc[u] = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+      const double wi = w[i];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (u < nk) acc[u] = fma(wi, V[(size_t)(k0 + u) * n + i], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      double a = acc[u];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0) red[wid][u] = a;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < nk) {
       double sacc = 0.0;
-      for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q];
-      part[(size_t)blockIdx.x * part_stride + k] = sacc;
+      for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q][threadIdx.x];
+      part[(size_t)blockIdx.x * part_stride + k0 + threadIdx.x] = sacc;
     }
     __syncthreads();
   }

@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 using namespace pcfd;
@@ -163,10 +164,12 @@ struct Solver {
   void* d_M = nullptr;          // [nblocks][25] off-diagonal blocks (diagonal slots unused)
   double* d_diag = nullptr;     // [nnode][25] diagonal blocks before the LU
   double* d_dlu = nullptr;      // [nnode][25] LU of the diagonal, U reciprocals on its diagonal
+  double* d_dinv = nullptr;     // [nnode][25] inverse of the diagonal block (from the LU)
   int* d_piv = nullptr;         // [nnode][5]
   double* d_bblk = nullptr;     // [nbedge][25] boundary contributions to the diagonal
   double* d_dt = nullptr;       // [nnode] local pseudo time step
   double* d_x = nullptr;        // [nnode][5] linear solution (dq)
+  float* d_xf = nullptr;        // [nnode][5] FP32 copy of the vector the FP32/BF16 products read
   double* d_scal = nullptr;     // [16] scalar results
   int have_dt = 0, have_jac = 0;
   int ncolor = 0;
@@ -1129,8 +1132,8 @@ void free_solver(Solver* s) {
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
-                  s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_piv,
-                  s->d_bblk, s->d_dt, s->d_x, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
+                  s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
+                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
                   s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1431,6 +1434,10 @@ int ensure_matrix(Solver* s, int prec) {
   if (prec < 0 || prec > 2) return set_err(PCFD_ERR_ARG, "Jacobian precision must be 0 (FP64), 1 (FP32) or 2 (BF16)");
   if (s->d_M && s->jac_prec == prec) return PCFD_OK;
   if (s->d_M) { cudaFree(s->d_M); s->d_M = nullptr; }
+  if (!s->d_xf) {
+    int rc = dalloc(&s->d_xf, (size_t)s->nnode * NEQN);
+    if (rc) return rc;
+  }
   size_t bytes = (size_t)s->nblocks * 25 * prec_bytes(prec);
   cudaError_t e = cudaMalloc(&s->d_M, bytes);
   if (e != cudaSuccess) return set_err(PCFD_ERR_NOMEM, std::string("matrix: ") + cudaGetErrorString(e));
@@ -1503,6 +1510,10 @@ int run_jacobian_t(Solver* s) {
                                                                s->d_bbc, s->d_btw, s->d_bnrm, s->prm.gamma, M,
                                                                s->d_diag, s->d_dlu, s->d_piv, s->d_health);
   });
+  if (rc) return rc;
+  rc = launch(s, T_JAC_FINISH, [&] {
+    k_diag_inverse<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_dlu, s->d_piv, s->d_dinv);
+  });
   if (rc == PCFD_OK) s->have_jac = 1;
   return rc;
 }
@@ -1543,6 +1554,15 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
   const T* M = (const T*)s->d_M;
   const double cnt = (double)s->nnode * NEQN;
   double prev = 0.0, cur = 0.0;
+  typedef typename OffAcc<T>::type A;
+  A* xa = (A*)x;
+  if (!std::is_same<T, double>::value) {
+    int rc = launch(s, T_SGS, [&] {
+      k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>((long long)s->nnode * NEQN, x, s->d_xf);
+    });
+    if (rc) return rc;
+    xa = (A*)s->d_xf;
+  }
   for (int sw = 0; sw < nsweeps; sw++) {
     for (int dir = 0; dir < 2; dir++) {
       for (int cc = 0; cc < s->ncolor; cc++) {
@@ -1550,8 +1570,8 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
         int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
         if (nr == 0) continue;
         int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M, s->d_dlu,
-                                                            s->d_piv, b, x);
+          k_sgs_color<T><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
+                                                            s->d_dinv, b, x, xa);
         });
         if (rc) return rc;
       }
@@ -1603,8 +1623,18 @@ int run_apply_dq(Solver* s, double* dqnorm) {
 
 template <class T>
 int run_spmv_t(Solver* s, const double* x, double* y) {
+  typedef typename OffAcc<T>::type A;
+  const A* xa = (const A*)x;
+  if (!std::is_same<T, double>::value) {
+    int rc = launch(s, T_SPMV, [&] {
+      k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>((long long)s->nnode * NEQN, x, s->d_xf);
+    });
+    if (rc) return rc;
+    xa = (const A*)s->d_xf;
+  }
   return launch(s, T_SPMV, [&] {
-    k_spmv<T><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M, s->d_diag, x, y);
+    k_spmv<T><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M, s->d_diag, x,
+                                                        xa, y);
   });
 }
 
@@ -1628,22 +1658,33 @@ int ensure_krylov(Solver* s, int m) {
   if ((rc = dalloc(&s->d_V, n * (m + 1)))) return rc;
   if ((rc = dalloc(&s->d_Z, n * m))) return rc;
   if ((rc = dalloc(&s->d_w, n))) return rc;
-  if ((rc = dalloc(&s->d_dots, (size_t)kNormBlocks * (m + 2) + 2 * (m + 2)))) return rc;
+  // partials [kNormBlocks][m+2], then four result slots of m+2 each
+  if ((rc = dalloc(&s->d_dots, (size_t)kNormBlocks * (m + 2) + 4 * (m + 2)))) return rc;
   s->fg_m = m;
   return PCFD_OK;
 }
 
-// dots[k] = (w, V_k), k < nv, copied to the host
-int run_mdot(Solver* s, const double* V, int nv, const double* w, double* host_out) {
+// result slot `slot` (0..3) of the Krylov dot buffer, m+2 doubles
+double* krylov_slot(Solver* s, int slot) {
+  return s->d_dots + (size_t)kNormBlocks * (s->fg_m + 2) + (size_t)slot * (s->fg_m + 2);
+}
+
+// dots[k] = (w, V_k), k < nv, into result slot `slot` on the device
+int run_mdot_dev(Solver* s, const double* V, int nv, const double* w, int slot) {
   const long long n = (long long)s->nnode * NEQN;
   const int stride = s->fg_m + 2;
   double* part = s->d_dots;
-  double* res = s->d_dots + (size_t)kNormBlocks * stride;
+  double* res = krylov_slot(s, slot);
   int rc = launch(s, T_KRYLOV, [&] { k_mdot<<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride); });
   if (rc) return rc;
-  rc = launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res); });
+  return launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res); });
+}
+
+// the same, copied to the host
+int run_mdot(Solver* s, const double* V, int nv, const double* w, double* host_out) {
+  int rc = run_mdot_dev(s, V, nv, w, 0);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpyAsync(host_out, res, nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(host_out, krylov_slot(s, 0), nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   return PCFD_OK;
 }
@@ -1673,7 +1714,7 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters,
   double* V = s->d_V;
   double* Z = s->d_Z;
   double* w = s->d_w;
-  double* hdev = s->d_dots + (size_t)kNormBlocks * (s->fg_m + 2) + (s->fg_m + 2);
+  double* hdev = krylov_slot(s, 3);
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), hcol(m + 2), y(m);
   double beta0 = -1.0;
   int total = 0;
@@ -1704,18 +1745,23 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters,
         return rc;
       }
       if ((rc = run_spmv(s, zj, w))) return rc;
-      // CGS2
-      for (int k = 0; k <= j + 1; k++) hcol[k] = 0.0;
+      // CGS2 with the coefficients kept on the device (slots 1, 2) and the
+      // norm of the result (slot 0); one host synchronisation per iteration
       for (int pass = 0; pass < 2; pass++) {
-        std::vector<double> d(j + 1);
-        if ((rc = run_mdot(s, V, j + 1, w, d.data()))) return rc;
-        CUDA_TRY(cudaMemcpyAsync(hdev, d.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, hdev, w); })))
+        if ((rc = run_mdot_dev(s, V, j + 1, w, 1 + pass))) return rc;
+        double* dv = krylov_slot(s, 1 + pass);
+        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, dv, w); })))
           return rc;
-        for (int k = 0; k <= j; k++) hcol[k] += d[k];
       }
-      double ww;
-      if ((rc = run_mdot(s, w, 1, w, &ww))) return rc;
+      if ((rc = run_mdot_dev(s, w, 1, w, 0))) return rc;
+      std::vector<double> dd(3 * (size_t)(s->fg_m + 2));
+      CUDA_TRY(cudaMemcpyAsync(dd.data(), krylov_slot(s, 0), dd.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                               s->stream));
+      CUDA_TRY(cudaStreamSynchronize(s->stream));
+      const size_t st = s->fg_m + 2;
+      for (int k = 0; k <= j + 1; k++) hcol[k] = 0.0;
+      for (int k = 0; k <= j; k++) hcol[k] = dd[st + k] + dd[2 * st + k];
+      const double ww = dd[0];
       double hn = std::sqrt(ww);
       hcol[j + 1] = hn;
       if (hn > 0.0) {
@@ -2337,6 +2383,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     TRY(dput(&s->d_color_rows, rows.data(), rows.size()));
     TRY(dalloc(&s->d_diag, (size_t)nn * 25));
     TRY(dalloc(&s->d_dlu, (size_t)nn * 25));
+    TRY(dalloc(&s->d_dinv, (size_t)nn * 25));
     TRY(dalloc(&s->d_piv, (size_t)nn * 5));
     TRY(dalloc(&s->d_bblk, (size_t)std::max<long long>(nb, 1) * 25));
     TRY(dalloc(&s->d_dt, (size_t)nn));
