@@ -228,7 +228,8 @@ def converge_study(args):
     w = WORKLOADS[args.converge_workload]
     dims = (w["nx"], w["ny"], w["nz"])
     out = {"workload": "ns_flatplate %dx%dx%d (mesh seed 2, state seed 1), second order, Mach 0.8, Re 1e5" % dims,
-           "target_drop": 1e-10, "time_cap_s": args.converge_cap}
+           "target_drop": 1e-10, "time_cap_s": args.converge_cap,
+           "limiter_freeze": args.converge_limiter_freeze}
     lp_w = None
     if "mixed_learned" in args.converge_arms:
         # same resolution, unseen mesh and state seed
@@ -245,11 +246,12 @@ def converge_study(args):
         if arm["opts"]["linear_solver"] == 2:
             S.lp_init(1)
             S.lp_set_params(lp_w)
+        opts = dict(arm["opts"], limiter_freeze=args.converge_limiter_freeze)
         N.check(N.load().pcfd_device_sync(), "sync")
         hist, t_at, lin, fb = [], {}, 0, 0
         t0 = time.perf_counter()
         for it in range(1, args.converge_iters + 1):
-            rep = S.newton_iterate(it, **arm["opts"])
+            rep = S.newton_iterate(it, **opts)
             r = rep["res"][0]
             hist.append(r)
             lin += rep["lin_iters"]
@@ -367,12 +369,14 @@ def run_gb300(args, ws, rank, local, pg):
     h2d = qh.nbytes
     d2h = b.nbytes + 6 * 8
 
-    # roofline of the dominant kernel, the edge-flux kernel: algorithmic bytes
-    # per launch = 40 B/edge (2 int32 ids + 4 fp64 area) + 320 B/node (q 40,
-    # xyz 24, qgrad 216, limiter 40); FP64 flops counted from the kernel source
+    # roofline of the dominant kernel, the inviscid edge-flux kernel
+    # (MUSCL + Roe + clip test): algorithmic bytes per launch = 104 B/edge
+    # (2 int32 ids 8, area vector 32, edge half-vector 24, flux written 40)
+    # + 200 B/node (conservative q 40, the 15 gradient terms of the
+    # conservative variables 120, limiter 40), each array once per launch
     ef_ms, ef_n = timers.get("edge_flux", (0.0, 0))
     ef_avg = ef_ms / max(ef_n, 1)
-    alg_bytes = 40.0 * m.nedge + 320.0 * m.nnode
+    alg_bytes = 104.0 * m.nedge + 200.0 * m.nnode
     achieved = alg_bytes / (ef_avg * 1e-3) / 1e9 if ef_avg > 0 else None
     peak, peak_kind = peaks()
     tot_prof = sum(v[0] for v in timers.values() if v[1]) or 1.0
@@ -432,6 +436,8 @@ def main():
     ap.add_argument("--converge-cap", type=float, default=60.0, help="wall-time cap per arm, seconds")
     ap.add_argument("--converge-iters", type=int, default=3000, help="Newton iteration cap per arm")
     ap.add_argument("--converge-only", action="store_true", help="run only the convergence study")
+    ap.add_argument("--converge-limiter-freeze", type=int, default=60,
+                    help="Newton iteration from which the limiter is frozen (0: recomputed every iteration)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.converge_arms = [a for a in args.converge.split(",") if a]

@@ -476,6 +476,12 @@ __device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane,
   return sum5(acc);
 }
 
+// FP64 copy of an FP32 vector
+__global__ void k_f32_to_f64(long long n, const float* __restrict__ x, double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
 // FP32 copy of an FP64 vector (once per product or sweep)
 __global__ void k_to_f32(long long n, const double* __restrict__ x, float* __restrict__ xf) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -484,23 +490,25 @@ __global__ void k_to_f32(long long n, const double* __restrict__ x, float* __res
 
 // One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62), a
 // warp per block row: rhs = b_i - sum_j A_ij x_j over the off-diagonal
-// blocks, then lane 0 solves the 5x5 diagonal system with its FP64 LU and
-// writes x_i (and its FP32 copy when the products read one).
-template <class T>
+// blocks, then x_i = D_i^-1 rhs as a 25-lane product with the stored
+// inverse.  K is the vector type (FP64, or FP32 inside the FP32 Krylov
+// solver); xa is x in the products' accumulation type (x itself, or its
+// FP32 copy, which the sweep keeps current).
+template <class T, class K>
 __global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restrict__ rows, const int* __restrict__ ia,
                                                    const int* __restrict__ ja, const T* __restrict__ M,
-                                                   const double* __restrict__ dinv, const double* __restrict__ b,
-                                                   double* __restrict__ x, typename OffAcc<T>::type* __restrict__ xa) {
+                                                   const K* __restrict__ dinv, const K* __restrict__ b,
+                                                   K* __restrict__ x, typename OffAcc<T>::type* __restrict__ xa) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (gw >= nrows) return;
   const int i = rows[gw];
-  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, xa);
+  const K s = (K)row_offdiag<T>(i, lane, ia, ja, M, xa);
   // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
   const int r = lane / 5, c = lane % 5;
-  const double rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : 0.0;
-  const double rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
-  double v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : 0.0;
+  const K rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : K(0);
+  const K rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
+  K v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : K(0);
   v = sum5(v);
   if (lane < 25 && c == 0) {
     x[(size_t)i * 5 + r] = v;
@@ -509,21 +517,29 @@ __global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restr
 }
 
 // Block sparse matrix-vector product y = A x (CRS MatVecMultiply,
-// ucs/crs.tcc:484), warp per block row, with the FP64 diagonal.
-template <class T>
+// ucs/crs.tcc:484), warp per block row, diagonal in the vector type.
+template <class T, class K>
 __global__ void __launch_bounds__(256) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
-                                              const T* __restrict__ M, const double* __restrict__ diag,
-                                              const double* __restrict__ x,
-                                              const typename OffAcc<T>::type* __restrict__ xa,
-                                              double* __restrict__ y) {
+                                              const T* __restrict__ M, const K* __restrict__ diag,
+                                              const K* __restrict__ x,
+                                              const typename OffAcc<T>::type* __restrict__ xa, K* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= nnode) return;
-  const double s = (double)row_offdiag<T>(i, lane, ia, ja, M, xa);
-  double d = 0.0;
+  const K s = (K)row_offdiag<T>(i, lane, ia, ja, M, xa);
+  K d = K(0);
   if (lane < 25) d = diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5];
   d = sum5(d);
   if (lane < 25 && lane % 5 == 0) y[(size_t)i * 5 + lane / 5] = s + d;
+}
+
+// FP32 copies of the diagonal blocks and their inverses (FP32 Krylov solver)
+__global__ void k_diag_f32(long long n25, const double* __restrict__ diag, const double* __restrict__ dinv,
+                           float* __restrict__ diagf, float* __restrict__ dinvf) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n25; k += (long long)gridDim.x * blockDim.x) {
+    diagf[k] = (float)diag[k];
+    dinvf[k] = (float)dinv[k];
+  }
 }
 
 // Newton update (NewtonIterate, ucs/solutionSpace.tcc:772-818): NaN/Inf
@@ -671,28 +687,30 @@ __global__ void k_min_final(int nblocks, const double* __restrict__ part, double
 // ---- FGMRES vector kernels (deterministic reductions) ----------------------
 
 // part[block][k] = partial sums of (w, V_k) for k < nv; V_k = V + k*n
-__global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const double* __restrict__ V,
-                                                        const double* __restrict__ w, double* __restrict__ part,
+template <class K>
+__global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const K* __restrict__ V,
+                                                        const K* __restrict__ w, double* __restrict__ part,
                                                         int part_stride) {
-  // eight vectors per pass over w: w is read nv/8 times, each V_k once
+  // eight vectors per pass over w: w is read nv/8 times, each V_k once;
+  // per-thread sums in the vector type, block sums in FP64
   __shared__ double red[kNormThreads / 32][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k0 = 0; k0 < nv; k0 += 8) {
     const int nk = min(8, nv - k0);
-    double acc[8];
+    K acc[8];
 #pragma unroll
-    for (int u = 0; u < 8; u++) acc[u] = 0.0;
+    for (int u = 0; u < 8; u++) acc[u] = K(0);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-      const double wi = w[i];
+      const K wi = w[i];
 #pragma unroll
       for (int u = 0; u < 8; u++)
         if (u < nk) acc[u] = fma(wi, V[(size_t)(k0 + u) * n + i], acc[u]);
     }
 #pragma unroll
     for (int u = 0; u < 8; u++) {
-      double a = acc[u];
+      K a = acc[u];
       for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-      if (lane == 0) red[wid][u] = a;
+      if (lane == 0) red[wid][u] = (double)a;
     }
     __syncthreads();
     if (threadIdx.x < nk) {
@@ -704,39 +722,51 @@ __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, cons
   }
 }
 
+// final sums; also an FP32 copy for the FP32 Krylov kernels
 __global__ void k_mdot_final(int nblocks, int nv, int part_stride, const double* __restrict__ part,
-                             double* __restrict__ out) {
+                             double* __restrict__ out, float* __restrict__ outf) {
   int k = threadIdx.x;
   if (k >= nv) return;
   double s = 0.0;
   for (int b = 0; b < nblocks; b++) s += part[(size_t)b * part_stride + k];
   out[k] = s;
+  outf[k] = (float)s;
 }
 
-// w -= sum_k h[k] V_k   (h on the device)
-__global__ void k_orth_update(long long n, int nv, const double* __restrict__ V, const double* __restrict__ h,
-                              double* __restrict__ w) {
+// w -= sum_k h[k] V_k   (h on the device, in the vector type)
+template <class K>
+__global__ void k_orth_update(long long n, int nv, const K* __restrict__ V, const K* __restrict__ h,
+                              K* __restrict__ w) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double v = w[i];
+    K v = w[i];
     for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
     w[i] = v;
   }
 }
 
 // y = a * x
-__global__ void k_scale_copy(long long n, double a, const double* __restrict__ x, double* __restrict__ y) {
+template <class K>
+__global__ void k_scale_copy(long long n, K a, const K* __restrict__ x, K* __restrict__ y) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     y[i] = a * x[i];
 }
 
-// x += sum_k c[k] Z_k
-__global__ void k_combine(long long n, int nv, const double* __restrict__ Z, const double* __restrict__ c,
+// x += sum_k c[k] Z_k  (x FP64; the sum in the vector type)
+template <class K>
+__global__ void k_combine(long long n, int nv, const K* __restrict__ Z, const K* __restrict__ c,
                           double* __restrict__ x) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double v = x[i];
+    K v = K(0);
     for (int k = 0; k < nv; k++) v += c[k] * Z[(size_t)k * n + i];
-    x[i] = v;
+    x[i] += (double)v;
   }
+}
+
+// FP32 vector from an FP64 one, or b - r into FP32 (r = A x on entry)
+__global__ void k_residual_vec_f32(long long n, const double* __restrict__ b, const double* __restrict__ r,
+                                   float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)(b[i] - (r ? r[i] : 0.0));
 }
 
 // r = b - r   (r holds A x on entry)

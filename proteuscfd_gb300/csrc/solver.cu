@@ -82,13 +82,13 @@ enum HealthSlot {
 enum TimerId {
   T_BC = 0, T_GRAD, T_LIMITER, T_EDGEFLUX, T_CLIP, T_BEDGEFLUX, T_GATHER, T_NORM, T_SETUP,
   T_JAC_EDGE, T_JAC_BEDGE, T_JAC_DIAG, T_JAC_FINISH, T_SGS, T_SPMV, T_KRYLOV, T_UPDATE, T_TIMESTEP, T_LP_FWD,
-  T_LP_BWD, T_COUNT
+  T_LP_BWD, T_EDGEVISC, T_COUNT
 };
 const char* kTimerNames[T_COUNT] = {"bc_update", "lsq_gradient", "venkat_limiter", "edge_flux", "pressure_clip",
                                     "bedge_flux", "residual_gather", "norm_reduce", "setup", "jac_edge",
                                     "jac_bedge", "jac_diag", "jac_finish_lu", "sgs_sweep", "spmv",
                                     "krylov_vec", "apply_dq", "timestep", "learned_forward",
-                                    "learned_backward"};
+                                    "learned_backward", "edge_viscous"};
 
 struct Learned;
 
@@ -165,6 +165,10 @@ struct Solver {
   double* d_diag = nullptr;     // [nnode][25] diagonal blocks before the LU
   double* d_dlu = nullptr;      // [nnode][25] LU of the diagonal, U reciprocals on its diagonal
   double* d_dinv = nullptr;     // [nnode][25] inverse of the diagonal block (from the LU)
+  float* d_diagf = nullptr;     // [nnode][25] FP32 copies of diag and dinv (FP32 Krylov solver)
+  float* d_dinvf = nullptr;
+  double* d_wd = nullptr;       // [nnode][5] FP64 scratch of the Krylov solver
+  float* d_dotsf = nullptr;     // FP32 copies of the Krylov dot results
   int* d_piv = nullptr;         // [nnode][5]
   double* d_bblk = nullptr;     // [nbedge][25] boundary contributions to the diagonal
   double* d_dt = nullptr;       // [nnode] local pseudo time step
@@ -867,8 +871,8 @@ __device__ __forceinline__ int kneecap5(S* f) {
   return bad;
 }
 
-// Kernel_Inviscid_Flux (:192) + Kernel_Viscous_Flux (:390) for one edge; the
-// sum is stored as the flux leaving the left node.
+// Kernel_Inviscid_Flux (:192) for one edge, stored as the flux leaving the
+// left node (k_edge_visc adds the viscous part).
 // MODE 0: plain evaluation.  MODE 1: also flags the nodes whose extrapolated
 // or Roe-averaged states are non-physical - the pressure clip of the limiter
 // (ucs/limiters.tcc:737) tests exactly these states, so when nothing is
@@ -925,7 +929,27 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
     atomicOr(clipany, 1);
   }
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
-  if (kd.viscous) {
+#pragma unroll
+  for (int t = 0; t < NEQN; t++) ef[(size_t)e * NEQN + t] = f[t];
+}
+
+// Kernel_Viscous_Flux (:390) for one edge, added to the stored inviscid
+// flux.  A separate pass keeps each of the two kernels' code and register
+// footprint small (the double-float forms are long).
+template <class S>
+__global__ void __launch_bounds__(128) k_edge_visc(int nedge, const int2* __restrict__ en,
+                                                   const typename V4<S>::type* __restrict__ ea,
+                                                   const S* __restrict__ eh, const S* __restrict__ q,
+                                                   const S* __restrict__ grad, FluxConst kd, S* __restrict__ ef) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int2 n = en[e];
+  const FluxK<S>& k = flux_k<S>(kd);
+  const typename V4<S>::type a = ea[e];
+  const S* qL = &q[(size_t)n.x * NVARS];
+  const S* qR = &q[(size_t)n.y * NVARS];
+  const S h0 = eh[3 * (size_t)e], h1 = eh[3 * (size_t)e + 1], h2 = eh[3 * (size_t)e + 2];
+  {
     // face state: plain average of the nodal conservative variables
     const S half = Sc<S>::c(0.5);
     S Q0 = (qL[0] + qR[0]) * half, Q1 = (qL[1] + qR[1]) * half, Q2 = (qL[2] + qR[2]) * half,
@@ -958,10 +982,8 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
     S fv[NEQN];
     viscous_flux(u, v, w, T, g, a.x, a.y, a.z, a.w * k.inv_retilde, k.Sc_, k.cp_over_pr, fv);
 #pragma unroll
-    for (int t = 0; t < NEQN; t++) f[t] += fv[t];
+    for (int t = 0; t < NEQN; t++) ef[(size_t)e * NEQN + t] += fv[t];
   }
-#pragma unroll
-  for (int t = 0; t < NEQN; t++) ef[(size_t)e * NEQN + t] = f[t];
 }
 
 // Zeroes the limiter of every flagged node (the pressure clip); returns at
@@ -1133,7 +1155,7 @@ void free_solver(Solver* s) {
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
-                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
+                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
                   s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1392,6 +1414,12 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
     });
     if (rc) return rc;
   }
+  if (k.viscous) {
+    rc = launch(s, T_EDGEVISC, [&] {
+      k_edge_visc<S><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, k, r.ef);
+    });
+    if (rc) return rc;
+  }
   if (s->nbedge > 0) {
     rc = launch(s, T_BEDGEFLUX, [&] {
       k_bedge_flux<S><<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, r.ba, r.q, r.grad, k, r.bf,
@@ -1436,6 +1464,8 @@ int ensure_matrix(Solver* s, int prec) {
   if (s->d_M) { cudaFree(s->d_M); s->d_M = nullptr; }
   if (!s->d_xf) {
     int rc = dalloc(&s->d_xf, (size_t)s->nnode * NEQN);
+    if (!rc) rc = dalloc(&s->d_diagf, (size_t)s->nnode * 25);
+    if (!rc) rc = dalloc(&s->d_dinvf, (size_t)s->nnode * 25);
     if (rc) return rc;
   }
   size_t bytes = (size_t)s->nblocks * 25 * prec_bytes(prec);
@@ -1514,6 +1544,11 @@ int run_jacobian_t(Solver* s) {
   rc = launch(s, T_JAC_FINISH, [&] {
     k_diag_inverse<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_dlu, s->d_piv, s->d_dinv);
   });
+  if (rc == PCFD_OK && !std::is_same<T, double>::value)
+    rc = launch(s, T_JAC_FINISH, [&] {
+      k_diag_f32<<<kNormBlocks, 256, 0, s->stream>>>((long long)s->nnode * 25, s->d_diag, s->d_dinv, s->d_diagf,
+                                                     s->d_dinvf);
+    });
   if (rc == PCFD_OK) s->have_jac = 1;
   return rc;
 }
@@ -1570,8 +1605,8 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
         int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
         if (nr == 0) continue;
         int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
-                                                            s->d_dinv, b, x, xa);
+          k_sgs_color<T, double><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja,
+                                                                    M, s->d_dinv, b, x, xa);
         });
         if (rc) return rc;
       }
@@ -1597,6 +1632,33 @@ int run_sgs(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
     case 1: return run_sgs_t<float>(s, nsweeps, b, x, dnorm);
     default: return run_sgs_t<__nv_bfloat16>(s, nsweeps, b, x, dnorm);
   }
+}
+
+// nsweeps of the same sweep on FP32 vectors (the FP32 Krylov solver's
+// preconditioner; FP32 or BF16 matrix storage)
+template <class T>
+int run_sgs_f_t(Solver* s, int nsweeps, const float* b, float* x) {
+  const T* M = (const T*)s->d_M;
+  for (int sw = 0; sw < nsweeps; sw++)
+    for (int dir = 0; dir < 2; dir++)
+      for (int cc = 0; cc < s->ncolor; cc++) {
+        int c = dir == 0 ? cc : s->ncolor - 1 - cc;
+        int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
+        if (nr == 0) continue;
+        int rc = launch(s, T_SGS, [&] {
+          k_sgs_color<T, float><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
+                                                                   s->d_dinvf, b, x, x);
+        });
+        if (rc) return rc;
+      }
+  return PCFD_OK;
+}
+
+int run_sgs_f(Solver* s, int nsweeps, const float* b, float* x) {
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "sgs: no Jacobian assembled");
+  if (s->jac_prec == 1) return run_sgs_f_t<float>(s, nsweeps, b, x);
+  if (s->jac_prec == 2) return run_sgs_f_t<__nv_bfloat16>(s, nsweeps, b, x);
+  return set_err(PCFD_ERR_STATE, "FP32 sweep needs FP32 or BF16 matrix storage");
 }
 
 int run_apply_dq(Solver* s, double* dqnorm) {
@@ -1633,9 +1695,22 @@ int run_spmv_t(Solver* s, const double* x, double* y) {
     xa = (const A*)s->d_xf;
   }
   return launch(s, T_SPMV, [&] {
-    k_spmv<T><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M, s->d_diag, x,
-                                                        xa, y);
+    k_spmv<T, double><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
+                                                                s->d_diag, x, xa, y);
   });
+}
+
+template <class T>
+int run_spmv_f_t(Solver* s, const float* x, float* y) {
+  return launch(s, T_SPMV, [&] {
+    k_spmv<T, float><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
+                                                               s->d_diagf, x, x, y);
+  });
+}
+
+int run_spmv_f(Solver* s, const float* x, float* y) {
+  if (s->jac_prec == 1) return run_spmv_f_t<float>(s, x, y);
+  return run_spmv_f_t<__nv_bfloat16>(s, x, y);
 }
 
 int run_spmv(Solver* s, const double* x, double* y) {
@@ -1660,6 +1735,10 @@ int ensure_krylov(Solver* s, int m) {
   if ((rc = dalloc(&s->d_w, n))) return rc;
   // partials [kNormBlocks][m+2], then four result slots of m+2 each
   if ((rc = dalloc(&s->d_dots, (size_t)kNormBlocks * (m + 2) + 4 * (m + 2)))) return rc;
+  if (s->d_dotsf) cudaFree(s->d_dotsf);
+  s->d_dotsf = nullptr;
+  if ((rc = dalloc(&s->d_dotsf, 4 * (size_t)(m + 2)))) return rc;
+  if (!s->d_wd && (rc = dalloc(&s->d_wd, n))) return rc;
   s->fg_m = m;
   return PCFD_OK;
 }
@@ -1669,31 +1748,32 @@ double* krylov_slot(Solver* s, int slot) {
   return s->d_dots + (size_t)kNormBlocks * (s->fg_m + 2) + (size_t)slot * (s->fg_m + 2);
 }
 
-// dots[k] = (w, V_k), k < nv, into result slot `slot` on the device
-int run_mdot_dev(Solver* s, const double* V, int nv, const double* w, int slot) {
+float* krylov_slot_f(Solver* s, int slot) { return s->d_dotsf + (size_t)slot * (s->fg_m + 2); }
+template <class K>
+K* krylov_coef(Solver* s, int slot);
+template <>
+double* krylov_coef<double>(Solver* s, int slot) { return krylov_slot(s, slot); }
+template <>
+float* krylov_coef<float>(Solver* s, int slot) { return krylov_slot_f(s, slot); }
+
+// dots[k] = (w, V_k), k < nv, into result slot `slot` on the device (FP64,
+// with an FP32 copy)
+template <class K>
+int run_mdot_dev(Solver* s, const K* V, int nv, const K* w, int slot) {
   const long long n = (long long)s->nnode * NEQN;
   const int stride = s->fg_m + 2;
   double* part = s->d_dots;
   double* res = krylov_slot(s, slot);
-  int rc = launch(s, T_KRYLOV, [&] { k_mdot<<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride); });
+  float* resf = krylov_slot_f(s, slot);
+  int rc = launch(s, T_KRYLOV, [&] {
+    k_mdot<K><<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride);
+  });
   if (rc) return rc;
-  return launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res); });
+  return launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res, resf); });
 }
 
-// the same, copied to the host
-int run_mdot(Solver* s, const double* V, int nv, const double* w, double* host_out) {
-  int rc = run_mdot_dev(s, V, nv, w, 0);
-  if (rc) return rc;
-  CUDA_TRY(cudaMemcpyAsync(host_out, krylov_slot(s, 0), nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-  CUDA_TRY(cudaStreamSynchronize(s->stream));
-  return PCFD_OK;
-}
 
-// Restarted flexible GMRES, right-preconditioned by nsgs block-SGS sweeps,
-// classical Gram-Schmidt with one re-orthogonalisation (batched dot
-// products), Givens rotations on the host.  FGMRES has no counterpart on the
-// reference's Newton path: its CRS::GMRES (ucs/crs.tcc:176) is a fixed-
-// preconditioner restarted GMRES used by the design modes only.
+// learned preconditioner (defined with the network's host code below)
 int lp_precondition(Solver* s, int nsgs, const double* v, double* z);
 
 // Restarted right-preconditioned flexible GMRES (Saad 1993) with classical
@@ -1702,8 +1782,51 @@ int lp_precondition(Solver* s, int nsgs, const double* v, double* z);
 // the learned correction on top of them; a cycle in which the learned
 // preconditioner reduces the residual by less than 10 % switches the rest of
 // the solve to plain SGS and adds one cycle (counted in *fallbacks).
-int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp = false,
-               int* fallbacks = nullptr) {
+int lp_precondition_f(Solver* s, int nsgs, const float* v, float* z);
+
+// preconditioner and product in the Krylov vector type
+int krylov_prec(Solver* s, int nsgs, bool use_lp, const double* v, double* z) {
+  return use_lp ? lp_precondition(s, nsgs, v, z) : run_sgs(s, nsgs, v, z, nullptr);
+}
+int krylov_prec(Solver* s, int nsgs, bool use_lp, const float* v, float* z) {
+  return use_lp ? lp_precondition_f(s, nsgs, v, z) : run_sgs_f(s, nsgs, v, z);
+}
+int krylov_spmv(Solver* s, const double* x, double* y) { return run_spmv(s, x, y); }
+int krylov_spmv(Solver* s, const float* x, float* y) { return run_spmv_f(s, x, y); }
+
+// r0 = b - A x into the Krylov vector w (x = 0 on the first cycle)
+int krylov_residual(Solver* s, bool first, double* w) {
+  const long long n = (long long)s->nnode * NEQN;
+  if (first) {
+    CUDA_TRY(cudaMemcpyAsync(w, s->d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+    return PCFD_OK;
+  }
+  int rc = run_spmv(s, s->d_x, w);
+  if (rc) return rc;
+  return launch(s, T_KRYLOV, [&] { k_residual_vec<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_b, w); });
+}
+int krylov_residual(Solver* s, bool first, float* w) {
+  const long long n = (long long)s->nnode * NEQN;
+  if (!first) {
+    int rc = run_spmv(s, s->d_x, s->d_wd);
+    if (rc) return rc;
+  }
+  const double* r = first ? nullptr : s->d_wd;
+  return launch(s, T_KRYLOV, [&] { k_residual_vec_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_b, r, w); });
+}
+
+// Restarted right-preconditioned flexible GMRES (Saad 1993) with classical
+// Gram-Schmidt applied twice; the reference's GMRES (ucs/crs.tcc:176) is the
+// non-flexible form.  K is the Krylov vector type: FP64 with the FP64
+// matrix, FP32 with FP32 or BF16 storage - the linear solve is then a
+// defect correction whose rounding the FP64 residual of each restart and of
+// the next Newton step wins back; the update x stays FP64.  Preconditioner:
+// nsgs block-SGS sweeps, or with use_lp the learned correction on top of
+// them; a cycle in which the learned preconditioner reduces the residual by
+// less than 10 % switches the rest of the solve to plain SGS and adds one
+// cycle (counted in *fallbacks).
+template <class K>
+int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp, int* fallbacks) {
   const int m = std::max(1, std::min(o->fgmres_m > 0 ? o->fgmres_m : 30, 60));
   int restarts = std::max(1, o->fgmres_restarts);
   if (fallbacks) *fallbacks = 0;
@@ -1711,62 +1834,55 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters,
   int rc = ensure_krylov(s, m);
   if (rc) return rc;
   const long long n = (long long)s->nnode * NEQN;
-  double* V = s->d_V;
-  double* Z = s->d_Z;
-  double* w = s->d_w;
-  double* hdev = krylov_slot(s, 3);
+  K* V = (K*)s->d_V;
+  K* Z = (K*)s->d_Z;
+  K* w = (K*)s->d_w;
+  K* hdev = krylov_coef<K>(s, 3);
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), hcol(m + 2), y(m);
+  std::vector<K> yk(m);
   double beta0 = -1.0;
   int total = 0;
   double rel = 1.0;
+  const size_t st = s->fg_m + 2;
+  std::vector<double> dd(3 * st);
   for (int rs = 0; rs < restarts; rs++) {
-    // r = b - A x  (x is zero on the first pass)
-    if (rs == 0) {
-      CUDA_TRY(cudaMemcpyAsync(w, s->d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
-    } else {
-      if ((rc = run_spmv(s, s->d_x, w))) return rc;
-      if ((rc = launch(s, T_KRYLOV, [&] { k_residual_vec<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_b, w); }))) return rc;
-    }
+    if ((rc = krylov_residual(s, rs == 0, w))) return rc;
+    if ((rc = run_mdot_dev<K>(s, w, 1, w, 0))) return rc;
     double bb;
-    if ((rc = run_mdot(s, w, 1, w, &bb))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(&bb, krylov_slot(s, 0), sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
     double beta = std::sqrt(bb);
     if (beta0 < 0.0) beta0 = beta;
     if (beta == 0.0 || beta0 == 0.0) { rel = 0.0; break; }
-    if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<<<kNormBlocks, 256, 0, s->stream>>>(n, 1.0 / beta, w, V); }))) return rc;
+    if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kNormBlocks, 256, 0, s->stream>>>(n, K(1.0 / beta), w, V); })))
+      return rc;
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
     for (; j < m; j++) {
-      double* zj = Z + (size_t)j * n;
-      CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(double), s->stream));
-      if (use_lp) {
-        if ((rc = lp_precondition(s, std::max(1, o->nsgs), V + (size_t)j * n, zj))) return rc;
-      } else if ((rc = run_sgs(s, std::max(1, o->nsgs), V + (size_t)j * n, zj, nullptr))) {
-        return rc;
-      }
-      if ((rc = run_spmv(s, zj, w))) return rc;
+      K* zj = Z + (size_t)j * n;
+      CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(K), s->stream));
+      if ((rc = krylov_prec(s, std::max(1, o->nsgs), use_lp, V + (size_t)j * n, zj))) return rc;
+      if ((rc = krylov_spmv(s, zj, w))) return rc;
       // CGS2 with the coefficients kept on the device (slots 1, 2) and the
       // norm of the result (slot 0); one host synchronisation per iteration
       for (int pass = 0; pass < 2; pass++) {
-        if ((rc = run_mdot_dev(s, V, j + 1, w, 1 + pass))) return rc;
-        double* dv = krylov_slot(s, 1 + pass);
-        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, dv, w); })))
+        if ((rc = run_mdot_dev<K>(s, V, j + 1, w, 1 + pass))) return rc;
+        K* dv = krylov_coef<K>(s, 1 + pass);
+        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<K><<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, dv, w); })))
           return rc;
       }
-      if ((rc = run_mdot_dev(s, w, 1, w, 0))) return rc;
-      std::vector<double> dd(3 * (size_t)(s->fg_m + 2));
+      if ((rc = run_mdot_dev<K>(s, w, 1, w, 0))) return rc;
       CUDA_TRY(cudaMemcpyAsync(dd.data(), krylov_slot(s, 0), dd.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                s->stream));
       CUDA_TRY(cudaStreamSynchronize(s->stream));
-      const size_t st = s->fg_m + 2;
       for (int k = 0; k <= j + 1; k++) hcol[k] = 0.0;
       for (int k = 0; k <= j; k++) hcol[k] = dd[st + k] + dd[2 * st + k];
-      const double ww = dd[0];
-      double hn = std::sqrt(ww);
+      double hn = std::sqrt(dd[0]);
       hcol[j + 1] = hn;
       if (hn > 0.0) {
-        double* vn = V + (size_t)(j + 1) * n;
-        if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<<<kNormBlocks, 256, 0, s->stream>>>(n, 1.0 / hn, w, vn); })))
+        K* vn = V + (size_t)(j + 1) * n;
+        if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kNormBlocks, 256, 0, s->stream>>>(n, K(1.0 / hn), w, vn); })))
           return rc;
       }
       // apply previous rotations, then a new one
@@ -1793,8 +1909,9 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters,
       for (int q = k + 1; q < j; q++) t -= H[(size_t)k * m + q] * y[q];
       y[k] = t / H[(size_t)k * m + k];
     }
-    CUDA_TRY(cudaMemcpyAsync(hdev, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    if ((rc = launch(s, T_KRYLOV, [&] { k_combine<<<kNormBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
+    for (int k = 0; k < j; k++) yk[k] = (K)y[k];
+    CUDA_TRY(cudaMemcpyAsync(hdev, yk.data(), j * sizeof(K), cudaMemcpyHostToDevice, s->stream));
+    if ((rc = launch(s, T_KRYLOV, [&] { k_combine<K><<<kNormBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
       return rc;
     if (rel < rtol) break;
     if (use_lp && rel > 0.9 * beta / beta0) {
@@ -1803,9 +1920,17 @@ int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters,
       if (fallbacks) (*fallbacks)++;
     }
   }
+  // the host copy of y must outlive the asynchronous copy above
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
   if (relres) *relres = rel;
   if (iters) *iters = total;
   return PCFD_OK;
+}
+
+int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp = false,
+               int* fallbacks = nullptr) {
+  if (s->jac_prec == 0) return run_fgmres_t<double>(s, o, relres, iters, use_lp, fallbacks);
+  return run_fgmres_t<float>(s, o, relres, iters, use_lp, fallbacks);
 }
 
 // -------------------------------------------------------------------------
@@ -1990,6 +2115,16 @@ int lp_precondition(Solver* s, int nsgs, const double* v, double* z) {
   int rc = run_sgs(s, nsgs, v, lp->y, nullptr);
   if (rc || (rc = lp_features(s))) return rc;
   return lp_forward(s, false, z);
+}
+
+// the same on FP32 Krylov vectors (through FP64 copies)
+int lp_precondition_f(Solver* s, int nsgs, const float* v, float* z) {
+  Learned* lp = s->lp;
+  if (!lp) return set_err(PCFD_ERR_STATE, "learned preconditioner: pcfd_lp_init not called");
+  const long long n = (long long)lp->n * NEQN;
+  int rc = launch(s, T_KRYLOV, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, v, lp->vbuf); });
+  if (rc || (rc = lp_precondition(s, nsgs, lp->vbuf, s->d_wd))) return rc;
+  return launch(s, T_KRYLOV, [&] { k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_wd, z); });
 }
 
 int lp_adam_step(Solver* s, double lr) {
@@ -2881,6 +3016,13 @@ PCFD_API int pcfd_lp_collect(pcfd_solver_t h, int nsgs, double rtol, int krylov_
   const int nk = std::min(std::min(krylov_pairs, it), s->fg_m);
   for (int j = 0; j < nk; j++) {
     const double* zj = s->d_Z + (size_t)j * n5;
+    if (s->jac_prec != 0) {
+      // FP32 Krylov directions: an FP64 copy
+      const float* zf = (const float*)s->d_Z + (size_t)j * n5;
+      rc = launch(s, T_KRYLOV, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>((long long)n5, zf, s->d_wd); });
+      if (rc) return rc;
+      zj = s->d_wd;
+    }
     if ((rc = run_spmv(s, zj, lp->vbuf))) return rc;
     CUDA_TRY(cudaMemsetAsync(lp->y, 0, n5 * sizeof(double), s->stream));
     if ((rc = run_sgs(s, nsgs, lp->vbuf, lp->y, nullptr)) || (rc = lp_store_pair(s, zj))) return rc;
