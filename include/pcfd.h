@@ -159,6 +159,12 @@ PCFD_API int pcfd_update_bcs(pcfd_solver_t s);
 PCFD_API int pcfd_gradient(pcfd_solver_t s, double* qgrad_out);
 /* Limiter<T>::Compute (ucs/limiters.tcc:53); l_out optional [nnode][5]. */
 PCFD_API int pcfd_limiter(pcfd_solver_t s, double* l_out);
+/* The limiter values the next residual uses, [nnode][5] (Limiter<T>::l,
+ * ucs/limiters.h), without recomputing them. */
+PCFD_API int pcfd_get_limiter(pcfd_solver_t s, double* l_out);
+/* Installs limiter values [nnode][5] as final (no pressure-clip pass); with
+ * pcfd_newton_opts.limiter_freeze they stay fixed. */
+PCFD_API int pcfd_set_limiter(pcfd_solver_t s, const double* l);
 /* ComputeResiduals (ucs/residual.tcc:13): b (= -R) into b_out [nnode][5]
  * (optional) and norms_out[0..5] = {resGlobal, per-equation norms}. */
 PCFD_API int pcfd_residual(pcfd_solver_t s, double* b_out, double* norms_out);

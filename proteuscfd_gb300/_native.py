@@ -124,6 +124,8 @@ PROTOTYPES = {
     "pcfd_newton_step": (C.c_int, [_P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
     "pcfd_set_device": (C.c_int, [C.c_int]),
     "pcfd_set_residual_arithmetic": (C.c_int, [_P, C.c_int]),
+    "pcfd_get_limiter": (C.c_int, [_P, _DP]),
+    "pcfd_set_limiter": (C.c_int, [_P, _DP]),
     "pcfd_lp_init": (C.c_int, [_P, C.c_ulonglong]),
     "pcfd_lp_get_params": (C.c_int, [_P, _FP]),
     "pcfd_lp_set_params": (C.c_int, [_P, _FP]),

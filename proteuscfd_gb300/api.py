@@ -276,6 +276,17 @@ class SolutionSpace:
         """0 FP64, 1 double-float on the FP32 pipes (composite calls only)."""
         N.check(self._lib.pcfd_set_residual_arithmetic(self._h, int(mode)), "pcfd_set_residual_arithmetic")
 
+    def get_limiter(self):
+        """Limiter<T>::l as the next residual uses it (no recomputation)."""
+        lim = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        N.check(self._lib.pcfd_get_limiter(self._h, N.dptr(lim)), "pcfd_get_limiter")
+        return lim
+
+    def set_limiter(self, lim):
+        lim = np.ascontiguousarray(lim, dtype=np.float64)
+        assert lim.shape == (self.mesh.nnode, NEQN)
+        N.check(self._lib.pcfd_set_limiter(self._h, N.dptr(lim)), "pcfd_set_limiter")
+
     # ---- learned right preconditioner (pcfd_lp_*; no reference counterpart,
     # it sits where CRS<T>::PrecondBackSolve sits, ucs/crs.tcc:591) --------
     def lp_init(self, seed=1):

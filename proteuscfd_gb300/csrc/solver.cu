@@ -1118,6 +1118,10 @@ __global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ 
 }
 
 // FP64 -> double-float copies (state each evaluation; static geometry once)
+__global__ void k_df_to_f64(long long n, const dfl* __restrict__ in, double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = to_dbl(in[i]);
+}
 __global__ void k_to_df(long long n, const double* __restrict__ in, dfl* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = to_df(in[i]);
@@ -2595,6 +2599,37 @@ PCFD_API int pcfd_limiter(pcfd_solver_t h, double* l_out) {
     CUDA_TRY(cudaMemcpyAsync(l_out, s->d_lim, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
                              s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_get_limiter(pcfd_solver_t h, double* l_out) {
+  Solver* s = (Solver*)h;
+  if (!s || !l_out) return set_err(PCFD_ERR_ARG, "pcfd_get_limiter: bad arguments");
+  if (!s->have_lim) return set_err(PCFD_ERR_STATE, "pcfd_get_limiter: no limiter computed");
+  const long long n = (long long)s->nnode * NEQN;
+  if (s->lim_arith) {
+    int rc = launch(s, T_SETUP, [&] { k_df_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, s->f_lim, s->d_lim); });
+    if (rc) return rc;
+  }
+  CUDA_TRY(cudaMemcpyAsync(l_out, s->d_lim, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_limiter(pcfd_solver_t h, const double* l) {
+  Solver* s = (Solver*)h;
+  if (!s || !l) return set_err(PCFD_ERR_ARG, "pcfd_set_limiter: bad arguments");
+  const long long n = (long long)s->nnode * NEQN;
+  CUDA_TRY(cudaMemcpyAsync(s->d_lim, l, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  if (s->arith) {
+    int rc = ensure_df(s);
+    if (rc || (rc = to_df_launch(s, s->d_lim, s->f_lim, n))) return rc;
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->have_lim = 1;
+  s->lim_arith = s->arith;
+  s->lim_clipped = 1;  // final values: no pressure-clip pass follows
+  s->lim_fresh = 0;
   return PCFD_OK;
 }
 

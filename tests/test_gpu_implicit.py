@@ -96,6 +96,26 @@ def test_jacobian_storage_precisions():
     assert row_block_error(out[2], ref, O.ia) < 1e-2    # BF16 storage
 
 
+@pytest.mark.parametrize("arith", [0, 1])
+def test_limiter_get_set_roundtrip(arith):
+    case = ns_case(3)
+    m, S, O, q0 = setup(case)
+    S.set_state(q0)
+    S.set_residual_arithmetic(arith)
+    S.newton_iterate(1, cfl=5.0, nsgs=2)
+    lim = S.get_limiter()
+    assert lim.shape == (m.nnode, 5) and np.all(lim >= 0.0) and np.all(lim <= 1.0)
+    lim2 = np.clip(lim * 0.5 + 0.25, 0.0, 1.0)
+    S.set_limiter(lim2)
+    # the double-float arithmetic holds the limiter as an FP32 pair (~48 bits)
+    rtol = 0.0 if arith == 0 else 2.0 ** -46
+    assert np.allclose(S.get_limiter(), lim2, rtol=rtol, atol=0.0)
+    # a frozen limiter is what the next residual uses
+    r1 = S.newton_iterate(2, cfl=5.0, nsgs=2, limiter_freeze=1)
+    assert np.isfinite(r1["res"][0])
+    assert np.allclose(S.get_limiter(), lim2, rtol=rtol, atol=0.0)
+
+
 def test_jacobian_double_float_fluxes():
     """Residual arithmetic 1 evaluates the finite-difference fluxes in
     double-float: flux rounding ~2^-48 over h = 1e-8 leaves ~1e-6 relative
