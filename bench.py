@@ -314,6 +314,44 @@ def converge_study(args):
     return out
 
 
+def chemistry_study(args):
+    """Finite-rate chemistry of the reacting workload: the 5-species air
+    mechanism's production rates on 2,007,040 nodes (the reacting box's node
+    count), inputs resident in HBM, device time by CUDA events; the host-API
+    form with its copies; the oracle on a host sample."""
+    import torch
+    sys.path.insert(0, str(ROOT / "tests"))
+    from chem_cases import mechanism, states
+    from oracle_lib import chem_rates
+    from proteuscfd_gb300.chem import ChemModel, model_struct
+    spec = mechanism()
+    n = 2007040
+    rho, T = states(n, seed=5, tmin=300.0, tmax=8000.0)
+    c = ChemModel(spec)
+    d_rho = torch.from_numpy(rho).cuda()
+    d_T = torch.from_numpy(T).cuda()
+    d_w = torch.empty_like(d_rho)
+    for _ in range(3):
+        c.production_rates_dev(n, d_rho.data_ptr(), d_T.data_ptr(), d_w.data_ptr())
+    ms = [c.production_rates_dev(n, d_rho.data_ptr(), d_T.data_ptr(), d_w.data_ptr()) for _ in range(args.steps)]
+    ms_avg = float(np.mean(ms))
+    t0 = time.perf_counter()
+    k = 3
+    for _ in range(k):
+        c.production_rates(rho, T)
+    e2e = (time.perf_counter() - t0) / k
+    ns = 20000
+    t0 = time.perf_counter()
+    chem_rates(model_struct(spec), rho[:ns], T[:ns])
+    tcpu = time.perf_counter() - t0
+    c.close()
+    return {"workload": "5-species air, 6 reactions (chemModels/5speciesAir.rxn), %d nodes, T 300-8000 K" % n,
+            "mnodes_per_s": n / (ms_avg * 1e-3) / 1e6, "ms": ms_avg,
+            "e2e_mnodes_per_s": n / e2e / 1e6,
+            "cpu_baseline": {"mnodes_per_s": ns / tcpu / 1e6, "cores": 1, "kind": "port",
+                             "sample": "%d nodes by the oracle, 1 thread" % ns}}
+
+
 def wall_force(m, case, q):
     """Pressure force on the no-slip wall: sum over its boundary half-edges of
     p(node) times the outward dual-face area vector."""
@@ -444,6 +482,8 @@ def run_gb300(args, ws, rank, local, pg):
         base, _, _ = cpu_sample(12.0, 1)
         line["cpu_baseline"] = base
     S.close()
+    if rank == 0 and ws == 1 and not args.no_chemistry:
+        line["chemistry"] = chemistry_study(args)
     if rank == 0 and ws == 1 and args.converge_arms:
         line["convergence"] = converge_study(args)
     if rank == 0:
@@ -466,6 +506,7 @@ def main():
     ap.add_argument("--converge-cap", type=float, default=60.0, help="wall-time cap per arm, seconds")
     ap.add_argument("--converge-iters", type=int, default=3000, help="Newton iteration cap per arm")
     ap.add_argument("--converge-only", action="store_true", help="run only the convergence study")
+    ap.add_argument("--no-chemistry", action="store_true", help="skip the finite-rate chemistry measurement")
     ap.add_argument("--converge-limiter-freeze", type=int, default=60,
                     help="Newton iteration from which the limiter is frozen (0: recomputed every iteration)")
     args = ap.parse_args()

@@ -296,6 +296,52 @@ PCFD_API int pcfd_lp_train(pcfd_solver_t s, int epochs, double lr, double* loss_
 /* Applies the preconditioner to v [nnode][5] (host) -> z (host). */
 PCFD_API int pcfd_lp_apply(pcfd_solver_t s, int nsgs, const double* v, double* z);
 
+/* ---- finite-rate chemistry (reacting air) ------------------------------
+ * Mass production rates of a finite-rate mechanism per node, the per-node
+ * chemistry of the reacting equation set: ChemModel<T>::
+ * GetMassProductionRates (ucs/chem.tcc:575) with Reaction<T>::
+ * GetForwardReactionRate / GetEquilibriumReactionRate /
+ * GetBackwardReactionRate / GetMassProductionRate (ucs/reaction.tcc:608,
+ * 629,683,763) and the NASA-7 curve selection of Species<T>::GetThermoCoeff
+ * (ucs/species.tcc:96).  Backward rates come from the equilibrium constant
+ * of the Gibbs energies.  Units are the reference's: densities kg/m^3,
+ * temperature K, rates kg/(m^3 s), molecular weights kg/mol, EA as each
+ * rate form expects it (J/mol, or K for the Gupta form). */
+#define PCFD_CHEM_MAX_SPECIES 16
+#define PCFD_CHEM_MAX_REACTIONS 32
+#define PCFD_CHEM_MAX_LOCAL 16
+
+typedef struct pcfd_chem_reaction {
+  int type;          /* Reaction::rxnType: 0 Arrhenius, 1 ModArrhenius, 2 GuptaModArrhenius, 3 Power */
+  double A, EA, n;   /* forward-rate coefficients (SI) */
+  int third_bodies;  /* thirdBodiesPresent */
+  int nlocal;        /* the reaction's species: reactants, products, then listed third bodies */
+  int global[PCFD_CHEM_MAX_LOCAL];      /* index in the model's species list */
+  double nup[PCFD_CHEM_MAX_LOCAL];      /* Nup: reactant stoichiometric coefficients */
+  double nupp[PCFD_CHEM_MAX_LOCAL];     /* Nupp: product stoichiometric coefficients */
+  double tbeff[PCFD_CHEM_MAX_LOCAL];    /* TBEff: third-body efficiencies */
+} pcfd_chem_reaction;
+
+typedef struct pcfd_chem_model {
+  int nspecies;
+  double mw[PCFD_CHEM_MAX_SPECIES];          /* Species::MW, kg/mol */
+  double nasa_lo[PCFD_CHEM_MAX_SPECIES][7];  /* NASA-7 coefficients used up to 1000 K (and below 200 K) */
+  double nasa_hi[PCFD_CHEM_MAX_SPECIES][7];  /* above 1000 K (and above 6000 K) */
+  int nreactions;
+  pcfd_chem_reaction rx[PCFD_CHEM_MAX_REACTIONS];
+} pcfd_chem_model;
+
+typedef struct pcfd_chem_s* pcfd_chem_t;
+
+PCFD_API int pcfd_chem_create(const pcfd_chem_model* model, pcfd_chem_t* out);
+PCFD_API int pcfd_chem_destroy(pcfd_chem_t c);
+/* host arrays: rhoi [n][nspecies], T [n], wdot [n][nspecies] */
+PCFD_API int pcfd_chem_production_rates(pcfd_chem_t c, long long n, const double* rhoi, const double* T, double* wdot);
+/* the same on device arrays, on the handle's stream; ms_out (optional)
+ * receives the kernel's device time */
+PCFD_API int pcfd_chem_production_rates_dev(pcfd_chem_t c, long long n, const double* rhoi, const double* T,
+                                            double* wdot, double* ms_out);
+
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1
  * double-float - the same kernels with every FP64 operation replaced by a

@@ -55,6 +55,12 @@ void oracle_lp_forward(int n, const int* nptr, const int* nbr, const float* ef, 
 double oracle_lp_loss_grad(int n, const int* nptr, const int* nbr, const float* ef, const float* x, const float* t,
                            const float* w, int emulate, double* grad);
 
+/* finite-rate chemistry (chem.c) */
+double oracle_chem_kf(const pcfd_chem_reaction* r, double T);
+double oracle_chem_kc(const pcfd_chem_model* m, const pcfd_chem_reaction* r, double T);
+void oracle_chem_rates(const pcfd_chem_model* m, const double* rhoi, double T, double* wdot);
+void oracle_chem_rates_n(const pcfd_chem_model* m, long long n, const double* rhoi, const double* T, double* wdot);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,27 @@ class NewtonReport(C.Structure):
     ]
 
 
+CHEM_MAX_SPECIES = 16
+CHEM_MAX_REACTIONS = 32
+CHEM_MAX_LOCAL = 16
+
+
+class ChemReaction(C.Structure):
+    _fields_ = [
+        ("type", C.c_int), ("A", C.c_double), ("EA", C.c_double), ("n", C.c_double), ("third_bodies", C.c_int),
+        ("nlocal", C.c_int), ("global_", C.c_int * CHEM_MAX_LOCAL), ("nup", C.c_double * CHEM_MAX_LOCAL),
+        ("nupp", C.c_double * CHEM_MAX_LOCAL), ("tbeff", C.c_double * CHEM_MAX_LOCAL),
+    ]
+
+
+class ChemModelC(C.Structure):
+    _fields_ = [
+        ("nspecies", C.c_int), ("mw", C.c_double * CHEM_MAX_SPECIES),
+        ("nasa_lo", (C.c_double * 7) * CHEM_MAX_SPECIES), ("nasa_hi", (C.c_double * 7) * CHEM_MAX_SPECIES),
+        ("nreactions", C.c_int), ("rx", ChemReaction * CHEM_MAX_REACTIONS),
+    ]
+
+
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
@@ -125,6 +146,10 @@ PROTOTYPES = {
     "pcfd_set_device": (C.c_int, [C.c_int]),
     "pcfd_set_residual_arithmetic": (C.c_int, [_P, C.c_int]),
     "pcfd_get_limiter": (C.c_int, [_P, _DP]),
+    "pcfd_chem_create": (C.c_int, [C.POINTER(ChemModelC), C.POINTER(_P)]),
+    "pcfd_chem_destroy": (C.c_int, [_P]),
+    "pcfd_chem_production_rates": (C.c_int, [_P, C.c_longlong, _DP, _DP, _DP]),
+    "pcfd_chem_production_rates_dev": (C.c_int, [_P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, _DP]),
     "pcfd_set_limiter": (C.c_int, [_P, _DP]),
     "pcfd_lp_init": (C.c_int, [_P, C.c_ulonglong]),
     "pcfd_lp_get_params": (C.c_int, [_P, _FP]),

@@ -1,0 +1,88 @@
+"""Finite-rate chemistry on the GPU: the mass production rates of a reacting
+air mechanism per node (ChemModel<T>::GetMassProductionRates,
+ucs/chem.tcc:575), through the C ABI (pcfd_chem_*)."""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+
+from . import _native as N
+
+
+def model_struct(spec: dict) -> "N.ChemModelC":
+    """pcfd_chem_model from a mechanism description: {"species": [{"MW" (kg/mol),
+    "lo", "hi" (NASA-7)}], "reactions": [{"type", "A", "EA", "n",
+    "third_bodies", "global", "nup", "nupp", "tbeff"}]}."""
+    m = N.ChemModelC()
+    sp = spec["species"]
+    rx = spec["reactions"]
+    if not 0 < len(sp) <= N.CHEM_MAX_SPECIES or len(rx) > N.CHEM_MAX_REACTIONS:
+        raise ValueError("mechanism too large")
+    m.nspecies = len(sp)
+    for k, s in enumerate(sp):
+        m.mw[k] = s["MW"]
+        for i in range(7):
+            m.nasa_lo[k][i] = s["lo"][i]
+            m.nasa_hi[k][i] = s["hi"][i]
+    m.nreactions = len(rx)
+    for j, r in enumerate(rx):
+        c = m.rx[j]
+        c.type, c.A, c.EA, c.n, c.third_bodies = r["type"], r["A"], r["EA"], r["n"], r["third_bodies"]
+        c.nlocal = len(r["global"])
+        if c.nlocal > N.CHEM_MAX_LOCAL:
+            raise ValueError("reaction with too many species")
+        for l in range(c.nlocal):
+            c.global_[l] = r["global"][l]
+            c.nup[l] = r["nup"][l]
+            c.nupp[l] = r["nupp"][l]
+            c.tbeff[l] = r["tbeff"][l]
+    return m
+
+
+def load_mechanism(path) -> dict:
+    return json.loads(Path(path).read_text())
+
+
+class ChemModel:
+    """Handle of a mechanism on the GPU."""
+
+    def __init__(self, spec: dict):
+        self._lib = N.load()
+        self.spec = spec
+        self.nspecies = len(spec["species"])
+        self._m = model_struct(spec)
+        h = C.c_void_p()
+        N.check(self._lib.pcfd_chem_create(C.byref(self._m), C.byref(h)), "pcfd_chem_create")
+        self._h = h
+
+    def production_rates(self, rhoi, T):
+        """rhoi [n][nspecies] kg/m^3, T [n] K -> wdot [n][nspecies] kg/(m^3 s)."""
+        rhoi = np.ascontiguousarray(rhoi, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        n = T.shape[0]
+        assert rhoi.shape == (n, self.nspecies)
+        w = np.empty_like(rhoi)
+        N.check(self._lib.pcfd_chem_production_rates(self._h, n, N.dptr(rhoi), N.dptr(T), N.dptr(w)),
+                "pcfd_chem_production_rates")
+        return w
+
+    def production_rates_dev(self, n, rhoi_ptr, T_ptr, wdot_ptr):
+        """Device pointers; returns the kernel's device time in ms."""
+        ms = C.c_double()
+        N.check(self._lib.pcfd_chem_production_rates_dev(self._h, int(n), rhoi_ptr, T_ptr, wdot_ptr, C.byref(ms)),
+                "pcfd_chem_production_rates_dev")
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pcfd_chem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

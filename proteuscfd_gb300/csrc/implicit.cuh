@@ -439,41 +439,65 @@ __device__ __forceinline__ A sum5(A v) {
          __shfl_down_sync(full, v, 4);
 }
 
-// Off-diagonal part of block row i of A x.  The row's blocks are contiguous
+// Off-diagonal part of a block row of A x.  The row's blocks are contiguous
 // in CRS order, 25 coefficients each (row-major), so lane l < 25 takes
 // coefficient (l / 5, l % 5) of every block: each warp load reads 25
 // consecutive coefficients.  The row's column indices come in with one
-// coalesced load (lane b holds block b's), and the coefficient and x loads
-// of eight blocks are issued before any of them is used.  xa is x in the
-// accumulation type.  Lane 5r receives row r's sum.
+// coalesced load (lane b holds block b's).  A row is handled in two phases
+// so that a warp can overlap rows: row_issue starts the coefficient and x
+// loads of the first 16 blocks (8 in FP64), row_finish consumes them (and walks any
+// further blocks).  Lane 5r receives row r's sum.
+// blocks whose loads are issued together: 16 in FP32, 8 in FP64 (registers)
 template <class T>
-__device__ __forceinline__ typename OffAcc<T>::type row_offdiag(int i, int lane, const int* __restrict__ ia,
-                                                                const int* __restrict__ ja, const T* __restrict__ M,
-                                                                const typename OffAcc<T>::type* __restrict__ xa) {
+struct RowBatch {
+  static constexpr int n = sizeof(typename OffAcc<T>::type) == 8 ? 8 : 16;
+};
+
+template <class T>
+__device__ __forceinline__ void row_issue(int b0, int nb, int jl, int lane, const T* __restrict__ M,
+                                          const typename OffAcc<T>::type* __restrict__ xa,
+                                          typename OffAcc<T>::type (&av)[RowBatch<T>::n],
+                                          typename OffAcc<T>::type (&xv)[RowBatch<T>::n]) {
+  constexpr int kRowBatch = RowBatch<T>::n;
   typedef typename OffAcc<T>::type A;
-  const unsigned full = 0xffffffffu;
-  const int b0 = ia[i] + 1, nb = ia[i + 1] - b0;
   const int c = lane % 5;
   const bool active = lane < 25;
+#pragma unroll
+  for (int u = 0; u < kRowBatch; u++) {
+    const int j = __shfl_sync(0xffffffffu, jl, u);
+    const bool ok = active && u < nb;
+    av[u] = ok ? off_val(M[(size_t)(b0 + u) * 25 + lane]) : A(0);
+    xv[u] = ok ? xa[(size_t)j * 5 + c] : A(0);
+  }
+}
+
+template <class T>
+__device__ __forceinline__ typename OffAcc<T>::type row_finish(int b0, int nb, int jl, int lane,
+                                                               const int* __restrict__ ja, const T* __restrict__ M,
+                                                               const typename OffAcc<T>::type* __restrict__ xa,
+                                                               const typename OffAcc<T>::type (&av)[RowBatch<T>::n],
+                                                               const typename OffAcc<T>::type (&xv)[RowBatch<T>::n]) {
+  typedef typename OffAcc<T>::type A;
+  constexpr int kRowBatch = RowBatch<T>::n;
   A acc = A(0);
-  for (int base = 0; base < nb; base += 32) {
-    const int jl = base + lane < nb ? ja[b0 + base + lane] : 0;
-    const int nk = min(32, nb - base);
-    for (int k0 = 0; k0 < nk; k0 += 8) {
-      A av[8], xv[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int k = k0 + u;
-        const int j = __shfl_sync(full, jl, k & 31);
-        const bool ok = active && k < nk;
-        av[u] = ok ? off_val(M[(size_t)(b0 + base + k) * 25 + lane]) : A(0);
-        xv[u] = ok ? xa[(size_t)j * 5 + c] : A(0);
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) acc = fma(av[u], xv[u], acc);
-    }
+  for (int u = 0; u < kRowBatch; u++) acc = fma(av[u], xv[u], acc);
+  // blocks past the first batch
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  for (int k = kRowBatch; k < nb; k++) {
+    const int j = k < 32 ? __shfl_sync(0xffffffffu, jl, k & 31) : ja[b0 + k];
+    if (active) acc = fma(off_val(M[(size_t)(b0 + k) * 25 + lane]), xa[(size_t)j * 5 + c], acc);
   }
   return sum5(acc);
+}
+
+// the next row's block range and column indices
+__device__ __forceinline__ void row_meta(const int* __restrict__ ia, const int* __restrict__ ja, int i, int lane,
+                                         int& b0, int& nb, int& jl) {
+  b0 = ia[i] + 1;
+  nb = ia[i + 1] - b0;
+  jl = lane < nb ? ja[b0 + lane] : 0;
 }
 
 // FP64 copy of an FP32 vector
@@ -488,49 +512,89 @@ __global__ void k_to_f32(long long n, const double* __restrict__ x, float* __res
     xf[i] = (float)x[i];
 }
 
-// One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62), a
-// warp per block row: rhs = b_i - sum_j A_ij x_j over the off-diagonal
-// blocks, then x_i = D_i^-1 rhs as a 25-lane product with the stored
-// inverse.  K is the vector type (FP64, or FP32 inside the FP32 Krylov
-// solver); xa is x in the products' accumulation type (x itself, or its
-// FP32 copy, which the sweep keeps current).
+// One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62):
+// warps stride over the colour's rows; for each, rhs = b_i - sum_j A_ij x_j
+// over the off-diagonal blocks, then x_i = D_i^-1 rhs as a 25-lane product
+// with the stored inverse.  While a row's coefficients are in flight the warp
+// already loads the next row's id, block range and column indices, so a row
+// costs about one memory latency instead of four.  K is the vector type
+// (FP64, or FP32 inside the FP32 Krylov solver); xa is x in the products'
+// accumulation type (x itself, or its FP32 copy, which the sweep keeps
+// current).  Rows of one colour share no block, so no row reads an x this
+// launch writes.
 template <class T, class K>
-__global__ void __launch_bounds__(256) k_sgs_color(int nrows, const int* __restrict__ rows, const int* __restrict__ ia,
-                                                   const int* __restrict__ ja, const T* __restrict__ M,
-                                                   const K* __restrict__ dinv, const K* __restrict__ b,
-                                                   K* __restrict__ x, typename OffAcc<T>::type* __restrict__ xa) {
+__global__ void __launch_bounds__(256, 3) k_sgs_color(int nrows, const int* __restrict__ rows,
+                                                      const int* __restrict__ ia, const int* __restrict__ ja,
+                                                      const T* __restrict__ M, const K* __restrict__ dinv,
+                                                      const K* __restrict__ b, K* __restrict__ x,
+                                                      typename OffAcc<T>::type* __restrict__ xa) {
+  typedef typename OffAcc<T>::type A;
   const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (gw >= nrows) return;
-  const int i = rows[gw];
-  const K s = (K)row_offdiag<T>(i, lane, ia, ja, M, xa);
-  // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
+  const int W = gridDim.x * 8;
+  int g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (g >= nrows) return;
+  int i = rows[g];
+  int b0, nb, jl;
+  row_meta(ia, ja, i, lane, b0, nb, jl);
+  int in = g + W < nrows ? rows[g + W] : -1;
   const int r = lane / 5, c = lane % 5;
-  const K rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : K(0);
-  const K rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
-  K v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : K(0);
-  v = sum5(v);
-  if (lane < 25 && c == 0) {
-    x[(size_t)i * 5 + r] = v;
-    if ((const void*)xa != (const void*)x) xa[(size_t)i * 5 + r] = (typename OffAcc<T>::type)v;
+  while (true) {
+    A av[RowBatch<T>::n], xv[RowBatch<T>::n];
+    row_issue<T>(b0, nb, jl, lane, M, xa, av, xv);
+    const int inn = g + 2 * W < nrows ? rows[g + 2 * W] : -1;
+    int b0n = 0, nbn = 0, jln = 0;
+    if (in >= 0) row_meta(ia, ja, in, lane, b0n, nbn, jln);
+    const K s = (K)row_finish<T>(b0, nb, jl, lane, ja, M, xa, av, xv);
+    // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
+    const K rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : K(0);
+    const K rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
+    K v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : K(0);
+    v = sum5(v);
+    if (lane < 25 && c == 0) {
+      x[(size_t)i * 5 + r] = v;
+      if ((const void*)xa != (const void*)x) xa[(size_t)i * 5 + r] = (A)v;
+    }
+    if (in < 0) break;
+    g += W;
+    i = in;
+    in = inn;
+    b0 = b0n;
+    nb = nbn;
+    jl = jln;
   }
 }
 
 // Block sparse matrix-vector product y = A x (CRS MatVecMultiply,
-// ucs/crs.tcc:484), warp per block row, diagonal in the vector type.
+// ucs/crs.tcc:484), warps striding over the rows with the same overlap of
+// the next row's indices, diagonal in the vector type.
 template <class T, class K>
-__global__ void __launch_bounds__(256) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
-                                              const T* __restrict__ M, const K* __restrict__ diag,
-                                              const K* __restrict__ x,
-                                              const typename OffAcc<T>::type* __restrict__ xa, K* __restrict__ y) {
+__global__ void __launch_bounds__(256, 3) k_spmv(int nnode, const int* __restrict__ ia, const int* __restrict__ ja,
+                                                 const T* __restrict__ M, const K* __restrict__ diag,
+                                                 const K* __restrict__ x,
+                                                 const typename OffAcc<T>::type* __restrict__ xa, K* __restrict__ y) {
+  typedef typename OffAcc<T>::type A;
   const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int W = gridDim.x * 8;
+  int i = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= nnode) return;
-  const K s = (K)row_offdiag<T>(i, lane, ia, ja, M, xa);
-  K d = K(0);
-  if (lane < 25) d = diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5];
-  d = sum5(d);
-  if (lane < 25 && lane % 5 == 0) y[(size_t)i * 5 + lane / 5] = s + d;
+  int b0, nb, jl;
+  row_meta(ia, ja, i, lane, b0, nb, jl);
+  while (true) {
+    A av[RowBatch<T>::n], xv[RowBatch<T>::n];
+    row_issue<T>(b0, nb, jl, lane, M, xa, av, xv);
+    K d = lane < 25 ? diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5] : K(0);
+    const int in = i + W;
+    int b0n = 0, nbn = 0, jln = 0;
+    if (in < nnode) row_meta(ia, ja, in, lane, b0n, nbn, jln);
+    const K s = (K)row_finish<T>(b0, nb, jl, lane, ja, M, xa, av, xv);
+    d = sum5(d);
+    if (lane < 25 && lane % 5 == 0) y[(size_t)i * 5 + lane / 5] = s + d;
+    if (in >= nnode) break;
+    i = in;
+    b0 = b0n;
+    nb = nbn;
+    jl = jln;
+  }
 }
 
 // FP32 copies of the diagonal blocks and their inverses (FP32 Krylov solver)

@@ -220,6 +220,10 @@ int launch(Solver* s, int timer, F&& f) {
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
+// Blocks of the row kernels (8 warps each, warps striding over rows): three
+// resident blocks per SM on 152 SMs, fewer when there are fewer rows.
+inline int row_grid(long long nrows) { return std::max(1, std::min(nblk(nrows, 8), 3 * 152)); }
+
 // -------------------------------------------------------------------------
 // set-up kernels
 // -------------------------------------------------------------------------
@@ -1609,7 +1613,7 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
         int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
         if (nr == 0) continue;
         int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T, double><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja,
+          k_sgs_color<T, double><<<row_grid(nr), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja,
                                                                     M, s->d_dinv, b, x, xa);
         });
         if (rc) return rc;
@@ -1650,7 +1654,7 @@ int run_sgs_f_t(Solver* s, int nsweeps, const float* b, float* x) {
         int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
         if (nr == 0) continue;
         int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T, float><<<nblk(nr, 8), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
+          k_sgs_color<T, float><<<row_grid(nr), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
                                                                    s->d_dinvf, b, x, x);
         });
         if (rc) return rc;
@@ -1699,7 +1703,7 @@ int run_spmv_t(Solver* s, const double* x, double* y) {
     xa = (const A*)s->d_xf;
   }
   return launch(s, T_SPMV, [&] {
-    k_spmv<T, double><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
+    k_spmv<T, double><<<row_grid(s->nnode), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
                                                                 s->d_diag, x, xa, y);
   });
 }
@@ -1707,7 +1711,7 @@ int run_spmv_t(Solver* s, const double* x, double* y) {
 template <class T>
 int run_spmv_f_t(Solver* s, const float* x, float* y) {
   return launch(s, T_SPMV, [&] {
-    k_spmv<T, float><<<nblk(s->nnode, 8), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
+    k_spmv<T, float><<<row_grid(s->nnode), 256, 0, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const T*)s->d_M,
                                                                s->d_diagf, x, x, y);
   });
 }

@@ -1,0 +1,41 @@
+"""Shared inputs of the chemistry tests: the 5-species air mechanism and
+seeded thermochemical states."""
+from pathlib import Path
+
+import numpy as np
+
+from proteuscfd_gb300.chem import load_mechanism
+
+FIXTURE = Path(__file__).resolve().parent / "golden" / "chem_5species_air.json"
+# atoms of N and O per molecule, by species name
+ATOMS = {"N": (1, 0), "O": (0, 1), "N2": (2, 0), "O2": (0, 2), "NO": (1, 1)}
+
+
+def mechanism():
+    return load_mechanism(FIXTURE)
+
+
+def states(n, seed=1, tmin=150.0, tmax=9000.0):
+    """Densities log-uniform over 1e-8..1e-1 kg/m^3 per species and
+    temperatures spanning both curve fits and both pinned ranges."""
+    rng = np.random.default_rng(seed)
+    spec = mechanism()
+    ns = len(spec["species"])
+    rho = 10.0 ** rng.uniform(-8, -1, size=(n, ns))
+    T = rng.uniform(tmin, tmax, size=n)
+    T[: min(n, 8)] = [150.0, 199.0, 200.0, 999.0, 1000.0, 1001.0, 6000.0, 7500.0][: min(n, 8)]
+    return rho, T
+
+
+def conservation(spec, w):
+    """Relative mass and element imbalance of production rates w [n][ns]."""
+    mw = np.array([s["MW"] for s in spec["species"]])
+    names = [s["name"] for s in spec["species"]]
+    scale = np.abs(w).sum(axis=1) + 1e-300
+    mass = np.abs(w.sum(axis=1)) / scale
+    mol = w / mw
+    elem = []
+    for e in range(2):
+        a = np.array([ATOMS[nm][e] for nm in names])
+        elem.append(np.abs((mol * a).sum(axis=1)) / ((np.abs(mol) * a).sum(axis=1) + 1e-300))
+    return mass.max(), max(x.max() for x in elem)

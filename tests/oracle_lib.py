@@ -46,6 +46,9 @@ def lib():
             "oracle_tri_area": (None, [_DP, _DP, _DP, _DP]),
             "oracle_tet_vol": (C.c_double, [_DP, _DP, _DP, _DP]),
             "oracle_bf16": (C.c_double, [C.c_double]),
+            "oracle_chem_rates_n": (None, [C.POINTER(N.ChemModelC), C.c_longlong, _DP, _DP, _DP]),
+            "oracle_chem_kf": (C.c_double, [C.POINTER(N.ChemReaction), C.c_double]),
+            "oracle_chem_kc": (C.c_double, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemReaction), C.c_double]),
             "oracle_lp_nparam": (C.c_int, []),
             "oracle_lp_graph": (None, [MV, _IP, _IP, _FP]),
             "oracle_lp_features": (C.c_double, [C.c_int, _DP, _DP, _DP, _DP, C.c_double, _FP]),
@@ -271,3 +274,12 @@ class OracleImplicit(OracleSpace):
                 x = self.sgs_colored(Mlu, pv, b, nsgs, *coloring)
             q, _ = self.apply_dq(x, q)
         return q, hist
+
+
+def chem_rates(model_struct, rhoi, T):
+    """Oracle production rates for a pcfd_chem_model ctypes structure."""
+    rhoi = np.ascontiguousarray(rhoi, np.float64)
+    T = np.ascontiguousarray(T, np.float64)
+    w = np.zeros_like(rhoi)
+    lib().oracle_chem_rates_n(C.byref(model_struct), T.shape[0], dp(rhoi), dp(T), dp(w))
+    return w

@@ -1,0 +1,63 @@
+"""The finite-rate chemistry restatement on the CPU oracle: the mechanism
+fixture against the reference's own files, and conservation properties of
+the production rates (test infrastructure checks; no GPU)."""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from chem_cases import FIXTURE, conservation, mechanism, states
+from oracle_lib import chem_rates
+from proteuscfd_gb300.chem import model_struct
+
+REF = Path("/root/reference")
+
+
+def test_fixture_shape():
+    spec = mechanism()
+    assert [s["name"] for s in spec["species"]] == ["O2", "O", "N", "N2", "NO"]
+    assert len(spec["reactions"]) == 6
+    # O2 + M <==> 2O + M with the file's third-body efficiencies
+    r = spec["reactions"][0]
+    assert r["type"] == 2 and r["third_bodies"] == 1
+    assert r["species"] == ["O2", "O", "N", "N2", "NO"] and r["tbeff"] == [9.0, 25.0, 1.0, 2.0, 1.0]
+    assert r["nup"][:2] == [1.0, 0.0] and r["nupp"][:2] == [0.0, 2.0]
+    # N2 + N <==> 2N + N merges N on the right
+    r = spec["reactions"][2]
+    assert r["species"] == ["N2", "N"] and r["nup"] == [1.0, 1.0] and r["nupp"] == [0.0, 3.0]
+
+
+@pytest.mark.skipif(not (REF / "chemdata" / "chemDB.py").exists(), reason="reference tree absent")
+def test_fixture_regenerates_from_reference(tmp_path):
+    out = subprocess.run([sys.executable, str(FIXTURE.parent / "make_chem_fixture.py"), str(REF)],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert json.loads(FIXTURE.read_text()) == mechanism()
+
+
+def test_oracle_conserves_mass_and_elements():
+    spec = mechanism()
+    m = model_struct(spec)
+    rho, T = states(4000, seed=2)
+    w = chem_rates(m, rho, T)
+    assert np.all(np.isfinite(w))
+    mass, elem = conservation(spec, w)
+    # atoms are conserved exactly; mass only to the rounding of the database's
+    # molecular weights (2 MW(N) - MW(N2) = 8e-8 kg/mol in the Burcat data)
+    assert elem < 1e-12
+    assert mass < 1e-5
+
+
+def test_oracle_dissociation_direction():
+    """Pure O2 at 6000 K dissociates; pure O at 300 K recombines."""
+    spec = mechanism()
+    m = model_struct(spec)
+    rho = np.zeros((2, 5))
+    rho[0, 0] = 1e-2   # O2
+    rho[1, 1] = 1e-2   # O
+    w = chem_rates(m, rho, np.array([6000.0, 300.0]))
+    assert w[0, 0] < 0 and w[0, 1] > 0
+    assert w[1, 1] < 0 and w[1, 0] > 0
