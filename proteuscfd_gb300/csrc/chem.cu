@@ -46,6 +46,17 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 __device__ __forceinline__ bool whole(double v) { return v == floor(v); }
 
+// x^a: small whole exponents (the stoichiometric coefficients of the
+// mechanisms, 0..3) by multiplication, which FP64 pow would spend ~20
+// operations on; anything else through pow
+__device__ __forceinline__ double stoich_pow(double x, double a) {
+  if (a == 0.0) return 1.0;
+  if (a == 1.0) return x;
+  if (a == 2.0) return x * x;
+  if (a == 3.0) return x * x * x;
+  return pow(x, whole(a) ? (double)(int)a : a);
+}
+
 __device__ __forceinline__ const double* thermo_coeff(const pcfd_chem_model& m, int s, double T) {
   if (T < 200.0) return m.nasa_lo[s];
   if (T > 6000.0) return m.nasa_hi[s];
@@ -113,8 +124,8 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
     for (int l = 0; l < r.nlocal; l++) {
       const double x = X[r.global[l]];
       const double a = r.nup[l], b = r.nupp[l];
-      form *= pow(x, whole(a) ? (double)(int)a : a);
-      dest *= pow(x, whole(b) ? (double)(int)b : b);
+      form *= stoich_pow(x, a);
+      dest *= stoich_pow(x, b);
     }
     double Mc = 1.0;
     if (r.third_bodies) {
