@@ -679,10 +679,9 @@ __global__ void __launch_bounds__(kNormThreads) k_sumsq(long long n, const doubl
 }
 
 __global__ void k_sum_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double s = 0.0;
-  for (int i = 0; i < nblocks; i++) s += part[i];
-  *out = s;
+  if (threadIdx.x >= 32) return;
+  const double s = warp_col_sum(part, nblocks, 1, 0, threadIdx.x);
+  if (threadIdx.x == 0) *out = s;
 }
 
 // MaxEigenvalue (ucs/compressible.tcc:799) of the face-averaged state
@@ -742,10 +741,11 @@ __global__ void __launch_bounds__(kNormThreads) k_min_part(int n, const double* 
 }
 
 __global__ void k_min_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (threadIdx.x >= 32) return;
   double r = 1.0e300;
-  for (int i = 0; i < nblocks; i++) r = fmin(r, part[i]);
-  *out = r;
+  for (int i = threadIdx.x; i < nblocks; i += 32) r = fmin(r, part[i]);
+  for (int o = 16; o > 0; o >>= 1) r = fmin(r, __shfl_xor_sync(0xffffffffu, r, o));
+  if (threadIdx.x == 0) *out = r;
 }
 
 // ---- FGMRES vector kernels (deterministic reductions) ----------------------
@@ -754,10 +754,12 @@ __global__ void k_min_final(int nblocks, const double* __restrict__ part, double
 template <class K>
 __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const K* __restrict__ V,
                                                         const K* __restrict__ w, double* __restrict__ part,
-                                                        int part_stride) {
+                                                        int part_stride, unsigned int* __restrict__ done,
+                                                        double* __restrict__ out, float* __restrict__ outf) {
   // eight vectors per pass over w: w is read nv/8 times, each V_k once;
   // per-thread sums in the vector type, block sums in FP64
   __shared__ double red[kNormThreads / 32][8];
+  __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k0 = 0; k0 < nv; k0 += 8) {
     const int nk = min(8, nv - k0);
@@ -784,17 +786,22 @@ __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, cons
     }
     __syncthreads();
   }
-}
-
-// final sums; also an FP32 copy for the FP32 Krylov kernels
-__global__ void k_mdot_final(int nblocks, int nv, int part_stride, const double* __restrict__ part,
-                             double* __restrict__ out, float* __restrict__ outf) {
-  int k = threadIdx.x;
-  if (k >= nv) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; b++) s += part[(size_t)b * part_stride + k];
-  out[k] = s;
-  outf[k] = (float)s;
+  // the last block to finish sums the partials (a warp per dot product, in
+  // a fixed order) and re-arms the counter
+  __threadfence();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int k = wid; k < nv; k += kNormThreads / 32) {
+      const double sum = warp_col_sum(part, (int)gridDim.x, part_stride, k, lane);
+      if (lane == 0) {
+        out[k] = sum;
+        outf[k] = (float)sum;
+      }
+    }
+    if (threadIdx.x == 0) *done = 0u;
+  }
 }
 
 // w -= sum_k h[k] V_k   (h on the device, in the vector type)

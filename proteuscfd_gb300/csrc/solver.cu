@@ -169,6 +169,7 @@ struct Solver {
   float* d_dinvf = nullptr;
   double* d_wd = nullptr;       // [nnode][5] FP64 scratch of the Krylov solver
   float* d_dotsf = nullptr;     // FP32 copies of the Krylov dot results
+  unsigned int* d_mdot_done = nullptr;  // blocks finished in k_mdot (re-armed by its last block)
   int* d_piv = nullptr;         // [nnode][5]
   double* d_bblk = nullptr;     // [nbedge][25] boundary contributions to the diagonal
   double* d_dt = nullptr;       // [nnode] local pseudo time step
@@ -1110,15 +1111,25 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
   }
 }
 
+// Sum of column k of nb per-block partials (row stride st) by one warp in a
+// fixed order: lane l adds rows l, l+32, ... in turn, then a butterfly;
+// lane 0's value is the result.  Reads bypass L1 (the partials come from
+// other blocks of the same launch in k_mdot).
+__device__ __forceinline__ double warp_col_sum(const double* part, int nb, int st, int k, int lane) {
+  double v = 0.0;
+  for (int b = lane; b < nb; b += 32) v += __ldcg(&part[(size_t)b * st + k]);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// a warp per norm, each summing the per-block partials in a fixed order
 __global__ void k_norm_final(int nblocks, int nnode, const double* __restrict__ part, double* __restrict__ norms,
                              int* __restrict__ clipany) {
-  int c = threadIdx.x;
-  if (c == 0) *clipany = 0;
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  if (threadIdx.x == 0) *clipany = 0;
   if (c >= 6) return;
-  double v = 0.0;
-  for (int bI = 0; bI < nblocks; bI++) v += part[(size_t)bI * 6 + c];
-  if (c == 0) norms[0] = sqrt(v) / ((double)nnode * NEQN);
-  else norms[c] = sqrt(v) / (double)nnode;
+  const double v = warp_col_sum(part, nblocks, 6, c, lane);
+  if (lane == 0) norms[c] = c == 0 ? sqrt(v) / ((double)nnode * NEQN) : sqrt(v) / (double)nnode;
 }
 
 // FP64 -> double-float copies (state each evaluation; static geometry once)
@@ -1163,7 +1174,7 @@ void free_solver(Solver* s) {
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
-                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
+                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_mdot_done, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
                   s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1442,7 +1453,7 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
   });
   if (rc) return rc;
   return launch(s, T_NORM, [&] {
-    k_norm_final<<<1, 32, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms, s->d_clipany);
+    k_norm_final<<<1, 192, 0, s->stream>>>(kNormBlocks, s->nnode, s->d_part, s->d_norms, s->d_clipany);
   });
 }
 
@@ -1747,6 +1758,10 @@ int ensure_krylov(Solver* s, int m) {
   s->d_dotsf = nullptr;
   if ((rc = dalloc(&s->d_dotsf, 4 * (size_t)(m + 2)))) return rc;
   if (!s->d_wd && (rc = dalloc(&s->d_wd, n))) return rc;
+  if (!s->d_mdot_done) {
+    if ((rc = dalloc(&s->d_mdot_done, 1))) return rc;
+    CUDA_TRY(cudaMemsetAsync(s->d_mdot_done, 0, sizeof(unsigned int), s->stream));
+  }
   s->fg_m = m;
   return PCFD_OK;
 }
@@ -1773,11 +1788,9 @@ int run_mdot_dev(Solver* s, const K* V, int nv, const K* w, int slot) {
   double* part = s->d_dots;
   double* res = krylov_slot(s, slot);
   float* resf = krylov_slot_f(s, slot);
-  int rc = launch(s, T_KRYLOV, [&] {
-    k_mdot<K><<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride);
+  return launch(s, T_KRYLOV, [&] {
+    k_mdot<K><<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride, s->d_mdot_done, res, resf);
   });
-  if (rc) return rc;
-  return launch(s, T_KRYLOV, [&] { k_mdot_final<<<1, 64, 0, s->stream>>>(kNormBlocks, nv, stride, part, res, resf); });
 }
 
 
