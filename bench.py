@@ -180,7 +180,9 @@ def run_reference(args, rank, pg):
 # method: FP64 residual and Jacobian, 10 block-SGS sweeps per step.  "mixed":
 # double-float residual and Jacobian fluxes, FP32 Jacobian storage,
 # FGMRES(30) right-preconditioned by one SGS sweep.  "mixed_learned": the
-# same with the learned correction on top of the SGS sweep.
+# same with the learned correction on top of the SGS sweep for the first
+# three Krylov directions of each cycle (the directions closest to the
+# right-hand sides the network is trained on).
 CONV_COMMON = dict(cfl_start=1.0, limiter_freeze=60, first_order_steps=20)
 CONV_ARMS = {
     "fp64": dict(arith=0, opts=dict(CONV_COMMON, cfl=50.0, cfl_ramp_steps=40, nsgs=10, linear_solver=0,
@@ -188,11 +190,12 @@ CONV_ARMS = {
     "mixed": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=1,
                                      fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1)),
     "mixed_learned": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=2,
-                                             fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1)),
+                                             fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1,
+                                             lp_directions=3)),
 }
 
 
-def train_learned(dims, seed, iters, epochs, lr, krylov_pairs=5):
+def train_learned(dims, seed, iters, epochs, lr, krylov_pairs=0):
     """Training pairs from the mixed solver's own systems on a mesh with
     another seed; returns the parameters and the training record."""
     from proteuscfd_gb300 import SolutionSpace, cases
@@ -233,7 +236,7 @@ def converge_study(args):
     lp_w = None
     if "mixed_learned" in args.converge_arms:
         # same resolution, unseen mesh and state seed
-        lp_w, out["learned_training"] = train_learned(dims, 7, 45, 40, 1e-3)
+        lp_w, out["learned_training"] = train_learned(dims, 7, 60, 150, 2e-3)
     finals = {}
     for name in args.converge_arms:
         arm = CONV_ARMS[name]

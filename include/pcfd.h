@@ -228,6 +228,8 @@ typedef struct pcfd_newton_opts {
   int limiter_refresh;  /* Param::limiterRefresh: recompute the limiter every n iterations (<= 0: 1) */
   int limiter_freeze;   /* Param::limiterFreeze: keep the limiter fixed from this iteration on (<= 0: never) */
   int first_order_steps;/* Param::nFirstOrderSteps: first-order fluxes up to this iteration */
+  int lp_directions;    /* linear_solver 2: the learned correction applies to the first lp_directions
+                           Krylov directions of each cycle, plain SGS to the rest (<= 0: all) */
 } pcfd_newton_opts;
 
 typedef struct pcfd_newton_report {

@@ -73,6 +73,7 @@ class NewtonOpts(C.Structure):
         ("nsgs", C.c_int), ("jac_update_freq", C.c_int), ("jac_precision", C.c_int), ("linear_solver", C.c_int),
         ("fgmres_m", C.c_int), ("fgmres_restarts", C.c_int), ("fgmres_rtol", C.c_double),
         ("limiter_refresh", C.c_int), ("limiter_freeze", C.c_int), ("first_order_steps", C.c_int),
+        ("lp_directions", C.c_int),
     ]
 
 

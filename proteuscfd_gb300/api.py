@@ -394,10 +394,11 @@ class SolutionSpace:
 
     def newton_iterate(self, it, cfl=5.0, nsgs=10, cfl_start=0.0, cfl_ramp_steps=0, jac_precision=0,
                        linear_solver=0, fgmres_m=30, fgmres_restarts=1, fgmres_rtol=1e-2, jac_update_freq=1,
-                       limiter_refresh=1, limiter_freeze=0, first_order_steps=0):
+                       limiter_refresh=1, limiter_freeze=0, first_order_steps=0, lp_directions=0):
         o = N.NewtonOpts(int(it), float(cfl), float(cfl_start), int(cfl_ramp_steps), int(nsgs), int(jac_update_freq),
                          int(jac_precision), int(linear_solver), int(fgmres_m), int(fgmres_restarts),
-                         float(fgmres_rtol), int(limiter_refresh), int(limiter_freeze), int(first_order_steps))
+                         float(fgmres_rtol), int(limiter_refresh), int(limiter_freeze), int(first_order_steps),
+                         int(lp_directions))
         r = N.NewtonReport()
         N.check(self._lib.pcfd_newton_step(self._h, C.byref(o), C.byref(r)), "pcfd_newton_step")
         return {"res": list(r.res), "dqnorm": r.dqnorm, "dtmin": r.dtmin, "lin_res": r.lin_res,

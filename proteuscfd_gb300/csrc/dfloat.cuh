@@ -112,6 +112,12 @@ struct Sc<double> {
   static __device__ __forceinline__ double to(double x) { return x; }
 };
 template <>
+struct Sc<float> {
+  static __device__ __forceinline__ float c(double x) { return (float)x; }
+  static __device__ __forceinline__ float from(double x) { return (float)x; }
+  static __device__ __forceinline__ double to(float x) { return (double)x; }
+};
+template <>
 struct Sc<dfl> {
   // for literal arguments the casts fold at compile time
   static __device__ __forceinline__ dfl c(double x) {

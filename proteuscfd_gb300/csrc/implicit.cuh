@@ -35,64 +35,67 @@ __device__ __forceinline__ void numflux(const double* QL, const double* QR, cons
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
 }
 
-// CompressibleEqnSet::ViscousJacobian (ucs/compressible.tcc:1633), laminar.
+// CompressibleEqnSet::ViscousJacobian (ucs/compressible.tcc:1633), laminar,
+// in the scalar type R (FP64; FP32 when the blocks are stored in FP32 or BF16).
 // QL/QR are the nodal 10-wide records (their stored pressure is used, as
 // GetPressure reads it); aL/aR are the left/right blocks with the sign the
 // reference scatters them with.
-__device__ void viscous_jacobian(const double* QL, const double* QR, const double* dx, double s2, const D4& a,
-                                 double gamma, double Pr, double inv_retilde, double S, double* aL, double* aR) {
-  double Q0 = 0.5 * (QL[0] + QR[0]), Q1 = 0.5 * (QL[1] + QR[1]), Q2 = 0.5 * (QL[2] + QR[2]),
-         Q3 = 0.5 * (QL[3] + QR[3]), Q4 = 0.5 * (QL[4] + QR[4]);
-  double gm1 = gamma - 1.0;
-  double iQ0 = 1.0 / Q0;
-  double ua = Q1 * iQ0, va = Q2 * iQ0, wa = Q3 * iQ0;
-  double Pa = gm1 * (Q4 - 0.5 * Q0 * (ua * ua + va * va + wa * wa));
-  double Ta = gamma * Pa * iQ0;
-  double mu = sutherland(Ta, S);
-  double RK = a.w * inv_retilde;
-  double RKT = RK * mu;
-  double rhoL = QL[0], uL = QL[1] / rhoL, vL = QL[2] / rhoL, wL = QL[3] / rhoL, PL = QL[6];
-  double rhoR = QR[0], uR = QR[1] / rhoR, vR = QR[2] / rhoR, wR = QR[3] / rhoR, PR = QR[6];
-  double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
-  double DxL[3], DxR[3];
+template <class R>
+__device__ void viscous_jacobian(const R* QL, const R* QR, const R* dx, R s2, R ax, R ay, R az, R aw, R gamma, R Pr,
+                                 R inv_retilde, R S, R* aL, R* aR) {
+  const R half = R(0.5), one = R(1.0), two = R(2.0);
+  R Q0 = half * (QL[0] + QR[0]), Q1 = half * (QL[1] + QR[1]), Q2 = half * (QL[2] + QR[2]),
+         Q3 = half * (QL[3] + QR[3]), Q4 = half * (QL[4] + QR[4]);
+  R gm1 = gamma - one;
+  R iQ0 = one / Q0;
+  R ua = Q1 * iQ0, va = Q2 * iQ0, wa = Q3 * iQ0;
+  R Pa = gm1 * (Q4 - half * Q0 * (ua * ua + va * va + wa * wa));
+  R Ta = gamma * Pa * iQ0;
+  R mu = sutherland(Ta, S);
+  R RK = aw * inv_retilde;
+  R RKT = RK * mu;
+  R rhoL = QL[0], uL = QL[1] / rhoL, vL = QL[2] / rhoL, wL = QL[3] / rhoL, PL = QL[6];
+  R rhoR = QR[0], uR = QR[1] / rhoR, vR = QR[2] / rhoR, wR = QR[3] / rhoR, PR = QR[6];
+  R u = half * (uL + uR), v = half * (vL + vR), w = half * (wL + wR);
+  R DxL[3], DxR[3];
   for (int i = 0; i < 3; i++) {
     DxL[i] = -dx[i] / (rhoL * s2);
     DxR[i] = dx[i] / (rhoR * s2);
   }
-  const double c43 = 4.0 / 3.0, mc23 = -2.0 / 3.0;
-  double cp = 1.0 / gm1;
-  double c1 = -(mu / Pr * cp);
+  const R c43 = R(4.0 / 3.0), mc23 = R(-2.0 / 3.0);
+  R cp = one / gm1;
+  R c1 = -(mu / Pr * cp);
   for (int side = 0; side < 2; side++) {
-    const double* D = side ? DxR : DxL;
-    double* A = side ? aR : aL;
-    double rho = side ? rhoR : rhoL, P = side ? PR : PL;
-    double us = side ? uR : uL, vs = side ? vR : vL, ws = side ? wR : wL;
-    double dux = -u * D[0], duy = -u * D[1], duz = -u * D[2];
-    double dvx = -v * D[0], dvy = -v * D[1], dvz = -v * D[2];
-    double dwx = -w * D[0], dwy = -w * D[1], dwz = -w * D[2];
-    double dfact = -2.0 / 3.0 * (dux + dvy + dwz);
-    double dtxx = (2.0 * dux + dfact), dtyy = (2.0 * dvy + dfact), dtzz = (2.0 * dwz + dfact);
-    double dtxy = duy + dvx, dtxz = duz + dwx, dtyz = dvz + dwy;
-    double dtxn = dtxx * a.x + dtxy * a.y + dtxz * a.z;
-    double dtyn = dtxy * a.x + dtyy * a.y + dtyz * a.z;
-    double dtzn = dtxz * a.x + dtyz * a.y + dtzz * a.z;
-    double r2u = (c43 * D[0] * a.x + D[1] * a.y + D[2] * a.z);
-    double r2v = (mc23 * D[1] * a.x + D[0] * a.y);
-    double r2w = (mc23 * D[2] * a.x + D[0] * a.z);
-    double r3u = (mc23 * D[0] * a.y + D[1] * a.x);
-    double r3v = (D[0] * a.x + c43 * D[1] * a.y + D[2] * a.z);
-    double r3w = (mc23 * D[2] * a.y + D[1] * a.z);
-    double r4u = (mc23 * D[0] * a.z + D[2] * a.x);
-    double r4v = (mc23 * D[1] * a.z + D[2] * a.y);
-    double r4w = (D[0] * a.x + D[1] * a.y + c43 * D[2] * a.z);
-    A[0] = A[1] = A[2] = A[3] = A[4] = 0.0;
-    A[5] = -RKT * dtxn; A[6] = -RKT * r2u; A[7] = -RKT * r2v; A[8] = -RKT * r2w; A[9] = 0.0;
-    A[10] = -RKT * dtyn; A[11] = -RKT * r3u; A[12] = -RKT * r3v; A[13] = -RKT * r3w; A[14] = 0.0;
-    A[15] = -RKT * dtzn; A[16] = -RKT * r4u; A[17] = -RKT * r4v; A[18] = -RKT * r4w; A[19] = 0.0;
-    double v2 = (us * us + vs * vs + ws * ws);
-    double dT_dP = gamma / rho;
-    double dP_dr = +gm1 * 0.5 * v2, dP_dru = -gm1 * us, dP_drv = -gm1 * vs, dP_drw = -gm1 * ws, dP_dret = +gm1;
-    double Tn = (D[0] * a.x + D[1] * a.y + D[2] * a.z) * dT_dP * c1;
+    const R* D = side ? DxR : DxL;
+    R* A = side ? aR : aL;
+    R rho = side ? rhoR : rhoL, P = side ? PR : PL;
+    R us = side ? uR : uL, vs = side ? vR : vL, ws = side ? wR : wL;
+    R dux = -u * D[0], duy = -u * D[1], duz = -u * D[2];
+    R dvx = -v * D[0], dvy = -v * D[1], dvz = -v * D[2];
+    R dwx = -w * D[0], dwy = -w * D[1], dwz = -w * D[2];
+    R dfact = R(-2.0 / 3.0) * (dux + dvy + dwz);
+    R dtxx = (two * dux + dfact), dtyy = (two * dvy + dfact), dtzz = (two * dwz + dfact);
+    R dtxy = duy + dvx, dtxz = duz + dwx, dtyz = dvz + dwy;
+    R dtxn = dtxx * ax + dtxy * ay + dtxz * az;
+    R dtyn = dtxy * ax + dtyy * ay + dtyz * az;
+    R dtzn = dtxz * ax + dtyz * ay + dtzz * az;
+    R r2u = (c43 * D[0] * ax + D[1] * ay + D[2] * az);
+    R r2v = (mc23 * D[1] * ax + D[0] * ay);
+    R r2w = (mc23 * D[2] * ax + D[0] * az);
+    R r3u = (mc23 * D[0] * ay + D[1] * ax);
+    R r3v = (D[0] * ax + c43 * D[1] * ay + D[2] * az);
+    R r3w = (mc23 * D[2] * ay + D[1] * az);
+    R r4u = (mc23 * D[0] * az + D[2] * ax);
+    R r4v = (mc23 * D[1] * az + D[2] * ay);
+    R r4w = (D[0] * ax + D[1] * ay + c43 * D[2] * az);
+    A[0] = A[1] = A[2] = A[3] = A[4] = R(0);
+    A[5] = -RKT * dtxn; A[6] = -RKT * r2u; A[7] = -RKT * r2v; A[8] = -RKT * r2w; A[9] = R(0);
+    A[10] = -RKT * dtyn; A[11] = -RKT * r3u; A[12] = -RKT * r3v; A[13] = -RKT * r3w; A[14] = R(0);
+    A[15] = -RKT * dtzn; A[16] = -RKT * r4u; A[17] = -RKT * r4v; A[18] = -RKT * r4w; A[19] = R(0);
+    R v2 = (us * us + vs * vs + ws * ws);
+    R dT_dP = gamma / rho;
+    R dP_dr = +gm1 * half * v2, dP_dru = -gm1 * us, dP_drv = -gm1 * vs, dP_drw = -gm1 * ws, dP_dret = +gm1;
+    R Tn = (D[0] * ax + D[1] * ay + D[2] * az) * dT_dP * c1;
     A[20] = -RKT * (dtxn * u + dtyn * v + dtzn * w) + RK * Tn * (dP_dr - P / rho);
     A[21] = -RKT * (r2u * u + r3u * v + r4u * w) + RK * Tn * dP_dru;
     A[22] = -RKT * (r2v * u + r3v * v + r4v * w) + RK * Tn * dP_drv;
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restr
     double dx[3] = {2.0 * eh[3 * (size_t)e], 2.0 * eh[3 * (size_t)e + 1], 2.0 * eh[3 * (size_t)e + 2]};
     double s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
     double vL[25], vR[25];
-    viscous_jacobian(QL, QR, dx, s2, a, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
+    viscous_jacobian<double>(QL, QR, dx, s2, a.x, a.y, a.z, a.w, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
 #pragma unroll
     for (int t = 0; t < 25; t++) { tL[t] += vL[t]; tR[t] += vR[t]; }
   }
@@ -162,12 +165,24 @@ __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restr
 // ~1e-6 relative error: the Jacobian is only the Newton iteration matrix,
 // the residual (evaluated separately) decides the converged answer.  The
 // analytic viscous blocks stay FP64.
+// difference quotient of two double-float fluxes in the block type's
+// arithmetic (h = 1e-8, whose reciprocal 1e8 is exact in FP32)
+__device__ __forceinline__ double df_quot(dfl d, double) { return to_dbl(d) * 1.0e8; }
+__device__ __forceinline__ float df_quot(dfl d, float) { return __fmul_rn(__fadd_rn(d.hi, d.lo), 1.0e8f); }
+__device__ __forceinline__ __nv_bfloat16 store_blk(__nv_bfloat16*, float v) { return __float2bfloat16(v); }
+__device__ __forceinline__ float store_blk(float*, float v) { return v; }
+__device__ __forceinline__ double store_blk(double*, double v) { return v; }
+
 template <class T>
 __global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __restrict__ en,
                                                      const D4* __restrict__ ea, const double* __restrict__ eh,
                                                      const double* __restrict__ q, const int* __restrict__ pos_lr,
                                                      const int* __restrict__ pos_rl, JacConst k, T* __restrict__ M,
                                                      unsigned long long* health) {
+  // FP64 blocks keep FP64 quotients and viscous blocks; FP32 and BF16
+  // blocks get them in FP32, so no FP64 instruction is spent on a value
+  // that is rounded to FP32 or coarser anyway
+  typedef typename std::conditional<std::is_same<T, double>::value, double, float>::type VR;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nedge) return;
   const int2 n = en[e];
@@ -181,11 +196,10 @@ __global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __re
   const dfl nx = to_df(a.x), ny = to_df(a.y), nz = to_df(a.z), ar = to_df(a.w);
   const dfl g = to_df(k.gamma), gm1 = to_df(k.gamma - 1.0), ig = to_df(1.0 / k.gamma), igm1 = to_df(1.0 / (k.gamma - 1.0));
   const dfl h = to_df(1.0e-8);
-  const double ih = 1.0 / 1.0e-8;
   dfl fS[NEQN];
   roe_flux<dfl>(QL, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fS);
   if (kneecap5(fS)) atomicAdd(&health[H_KNEECAP], 1ull);
-  double tL[25], tR[25];
+  VR tL[25], tR[25];
   for (int i = 0; i < NEQN; i++) {
     dfl QP[NEQN], fP[NEQN];
 #pragma unroll
@@ -194,30 +208,34 @@ __global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __re
     roe_flux<dfl>(QP, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
     if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
-    for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = to_dbl(fS[j] - fP[j]) * ih;
+    for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = df_quot(fS[j] - fP[j], VR(0));
 #pragma unroll
     for (int t = 0; t < NEQN; t++) QP[t] = QR[t];
     QP[i] = QP[i] + h;
     roe_flux<dfl>(QL, QP, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
     if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
-    for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = to_dbl(fP[j] - fS[j]) * ih;
+    for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = df_quot(fP[j] - fS[j], VR(0));
   }
   if (k.viscous) {
-    double QLd[NVARS], QRd[NVARS];
+    VR QLv[NVARS], QRv[NVARS];
 #pragma unroll
-    for (int t = 0; t < NVARS; t++) { QLd[t] = q[(size_t)n.x * NVARS + t]; QRd[t] = q[(size_t)n.y * NVARS + t]; }
-    double dx[3] = {2.0 * eh[3 * (size_t)e], 2.0 * eh[3 * (size_t)e + 1], 2.0 * eh[3 * (size_t)e + 2]};
-    double s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-    double vL[25], vR[25];
-    viscous_jacobian(QLd, QRd, dx, s2, a, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
+    for (int t = 0; t < NVARS; t++) {
+      QLv[t] = (VR)q[(size_t)n.x * NVARS + t];
+      QRv[t] = (VR)q[(size_t)n.y * NVARS + t];
+    }
+    VR dx[3] = {(VR)(2.0 * eh[3 * (size_t)e]), (VR)(2.0 * eh[3 * (size_t)e + 1]), (VR)(2.0 * eh[3 * (size_t)e + 2])};
+    VR s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    VR vL[25], vR[25];
+    viscous_jacobian<VR>(QLv, QRv, dx, s2, (VR)a.x, (VR)a.y, (VR)a.z, (VR)a.w, (VR)k.gamma, (VR)k.Pr,
+                         (VR)k.inv_retilde, (VR)k.S, vL, vR);
 #pragma unroll
     for (int t = 0; t < 25; t++) { tL[t] += vL[t]; tR[t] += vR[t]; }
   }
   T* bl = &M[(size_t)pos_rl[e] * 25];  // A(R, L)
   T* br = &M[(size_t)pos_lr[e] * 25];  // A(L, R)
 #pragma unroll
-  for (int t = 0; t < 25; t++) { bl[t] = to_store<T>(tL[t]); br[t] = to_store<T>(tR[t]); }
+  for (int t = 0; t < 25; t++) { bl[t] = store_blk(bl, tL[t]); br[t] = store_blk(br, tR[t]); }
 }
 
 // Bkernel_NumJac (ucs/jacobian.tcc:459) with jacobianBoundaryEval = 0: the
@@ -262,6 +280,114 @@ __global__ void __launch_bounds__(128) k_jac_bedge(int nbedge, const int2* __res
     if (beval != 1) apply_bc(bk, bct, QPL, QPR, a, btw[he], nQ);
     numflux(QPL, QPR, a, bk.gamma, fL, health);
     for (int j = 0; j < NEQN; j++) out[j * 5 + i] = (fL[j] - fS[j]) * ih;
+  }
+}
+
+// The boundary-condition map and auxiliary variables in double-float, for
+// the double-float form of the boundary Jacobian below (the same operations
+// as apply_bc and aux_vars).
+__device__ __forceinline__ void aux_vars_df(dfl gamma, dfl* Q) {
+  const dfl one = Sc<dfl>::c(1.0), half = Sc<dfl>::c(0.5);
+  const dfl gm1 = gamma - one;
+  const dfl ir = one / Q[0];
+  const dfl u = Q[1] * ir, v = Q[2] * ir, w = Q[3] * ir;
+  const dfl P = gm1 * (Q[4] - half * Q[0] * (u * u + v * v + w * w));
+  Q[6] = P;
+  Q[5] = gamma * P * ir;
+  Q[7] = u;
+  Q[8] = v;
+  Q[9] = w;
+}
+
+__device__ int apply_bc_df(int bct, dfl gamma, int no_cvbc, const dfl* qinf, dfl* QL, dfl* QR, dfl ax, dfl ay, dfl az,
+                           dfl Tw, const dfl* nQ) {
+  const dfl zero = Sc<dfl>::c(0.0), one = Sc<dfl>::c(1.0);
+  switch (bct) {
+    case PCFD_BC_SONIC_INFLOW:
+    case PCFD_BC_DIRICHLET:
+      for (int i = 0; i < NVARS; i++) QR[i] = QL[i] = qinf[i];
+      break;
+    case PCFD_BC_SONIC_OUTFLOW:
+    case PCFD_BC_NEUMANN:
+      for (int i = 0; i < NEQN; i++) QR[i] = QL[i];
+      break;
+    case PCFD_BC_FARFIELD:
+      bc_farfield<dfl>(gamma, qinf, QL, QL[6], QR, ax, ay, az);
+      break;
+    case PCFD_BC_IMPERMEABLE_WALL:
+    case PCFD_BC_SYMMETRY:
+      bc_inviscid_wall<dfl>(gamma, no_cvbc, QL, QL[6], QR, ax, ay, az);
+      break;
+    case PCFD_BC_NOSLIP:
+      if (Tw < zero) {
+        QR[0] = QL[0] = nQ[0];
+        QR[4] = QL[4] = nQ[4];
+      } else {
+        const dfl gm1 = gamma - one;
+        const dfl rhoEt = Tw * QL[0] / (gamma * gm1) + Sc<dfl>::c(0.5) * QR[0] * zero;
+        QR[0] = QL[0];
+        QR[4] = QL[4] = rhoEt;
+      }
+      QR[1] = QL[1] = QL[0] * zero;
+      QR[2] = QL[2] = QL[0] * zero;
+      QR[3] = QL[3] = QL[0] * zero;
+      break;
+    default:
+      return 0;
+  }
+  aux_vars_df(gamma, QR);
+  aux_vars_df(gamma, QL);
+  return 1;
+}
+
+// Bkernel_NumJac in double-float: the six boundary-condition maps with their
+// ten far-field or wall sub-iterations and the six Roe fluxes of a
+// half-edge on the FP32 pipes; the difference quotients (FP64 diagonal
+// contributions) carry ~1e-6 relative error, as in k_jac_edge_df.
+__global__ void __launch_bounds__(128) k_jac_bedge_df(int nbedge, const int2* __restrict__ bn,
+                                                      const D4* __restrict__ ba, const int* __restrict__ bbc,
+                                                      const double* __restrict__ btw, const int* __restrict__ bnrm,
+                                                      BcConst bk, int beval, const double* __restrict__ q,
+                                                      double* __restrict__ bblk, unsigned long long* health) {
+  int he = blockIdx.x * blockDim.x + threadIdx.x;
+  if (he >= nbedge) return;
+  const int2 n = bn[he];
+  const D4 a = ba[he];
+  dfl QL[NVARS], QR[NVARS], nQ[NVARS], qinf[NVARS];
+  for (int t = 0; t < NVARS; t++) {
+    QL[t] = to_df(q[(size_t)n.x * NVARS + t]);
+    QR[t] = to_df(q[(size_t)n.y * NVARS + t]);
+    qinf[t] = to_df(bk.qinf[t]);
+    nQ[t] = Sc<dfl>::c(0.0);
+  }
+  const int bct = bbc[he];
+  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+    for (int t = 0; t < NVARS; t++) nQ[t] = to_df(q[(size_t)bnrm[he] * NVARS + t]);
+  const dfl gamma = to_df(bk.gamma), gm1 = to_df(bk.gamma - 1.0), ig = to_df(1.0 / bk.gamma),
+            igm1 = to_df(1.0 / (bk.gamma - 1.0));
+  const dfl ax = to_df(a.x), ay = to_df(a.y), az = to_df(a.z), aw = to_df(a.w), Tw = to_df(btw[he]);
+  const dfl h = to_df(1.0e-8);
+  dfl fS[NEQN];
+  if (beval == 3) {
+    dfl QBL[NVARS], QBR[NVARS];
+    for (int t = 0; t < NVARS; t++) { QBL[t] = QL[t]; QBR[t] = QR[t]; }
+    apply_bc_df(bct, gamma, bk.no_cvbc, qinf, QBL, QBR, ax, ay, az, Tw, nQ);
+    roe_flux<dfl>(QBL, QBR, ax, ay, az, aw, gamma, gm1, ig, igm1, fS);
+  } else {
+    roe_flux<dfl>(QL, QR, ax, ay, az, aw, gamma, gm1, ig, igm1, fS);
+  }
+  if (kneecap5(fS)) atomicAdd(&health[H_KNEECAP], 1ull);
+  double* out = &bblk[(size_t)he * 25];
+  for (int i = 0; i < NEQN; i++) {
+    dfl QPL[NVARS], QPR[NVARS], fL[NEQN];
+    for (int t = 0; t < NVARS; t++) { QPL[t] = QL[t]; QPR[t] = QR[t]; }
+    QPL[i] = QPL[i] + h;
+    aux_vars_df(gamma, QPL);
+    aux_vars_df(gamma, QPR);
+    if (beval != 1) apply_bc_df(bct, gamma, bk.no_cvbc, qinf, QPL, QPR, ax, ay, az, Tw, nQ);
+    roe_flux<dfl>(QPL, QPR, ax, ay, az, aw, gamma, gm1, ig, igm1, fL);
+    if (kneecap5(fL)) atomicAdd(&health[H_KNEECAP], 1ull);
+    for (int j = 0; j < NEQN; j++) out[j * 5 + i] = to_dbl(fL[j] - fS[j]) * 1.0e8;
   }
 }
 

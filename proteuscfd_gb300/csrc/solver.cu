@@ -1542,9 +1542,14 @@ int run_jacobian_t(Solver* s) {
   if (rc) return rc;
   if (s->nbedge > 0) {
     rc = launch(s, T_JAC_BEDGE, [&] {
-      k_jac_bedge<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
-                                                              s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_q,
-                                                              s->d_bblk, s->d_health);
+      if (s->arith)
+        k_jac_bedge_df<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc,
+                                                                   s->d_btw, s->d_bnrm, bk, s->prm.jac_boundary_eval,
+                                                                   s->d_q, s->d_bblk, s->d_health);
+      else
+        k_jac_bedge<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
+                                                                s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_q,
+                                                                s->d_bblk, s->d_health);
     });
     if (rc) return rc;
   }
@@ -1883,7 +1888,8 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
     for (; j < m; j++) {
       K* zj = Z + (size_t)j * n;
       CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(K), s->stream));
-      if ((rc = krylov_prec(s, std::max(1, o->nsgs), use_lp, V + (size_t)j * n, zj))) return rc;
+      const bool lp_here = use_lp && (o->lp_directions <= 0 || j < o->lp_directions);
+      if ((rc = krylov_prec(s, std::max(1, o->nsgs), lp_here, V + (size_t)j * n, zj))) return rc;
       if ((rc = krylov_spmv(s, zj, w))) return rc;
       // CGS2 with the coefficients kept on the device (slots 1, 2) and the
       // norm of the result (slot 0); one host synchronisation per iteration

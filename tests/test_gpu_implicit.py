@@ -131,6 +131,11 @@ def test_jacobian_double_float_fluxes():
         S.compute_jacobians()
         out[arith] = S.get_jacobian()
     assert row_block_error(out[1], out[0], O.ia) < 2e-5
+    # FP32 storage: quotients and viscous blocks formed in FP32
+    S.set_state(q0)
+    S.set_jacobian_precision(1)
+    S.compute_jacobians()
+    assert row_block_error(S.get_jacobian(), out[0], O.ia) < 5e-5
     assert S.health()[0] == 0
 
 

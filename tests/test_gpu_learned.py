@@ -110,28 +110,36 @@ def test_initial_preconditioner_is_sgs(small):
 
 
 def test_training_and_learned_fgmres():
-    """Pairs from the solver's own Newton systems; training lowers the loss;
-    FGMRES with the learned preconditioner converges, and the Krylov
-    iterations it needs on later systems are compared with plain SGS."""
-    c, m, S, _ = make((20, 14, 12), seed=3)
+    """Pairs (b, dq) from the solver's own Newton systems; training lowers
+    the loss; on later systems the learned correction on the first Krylov
+    directions leaves a smaller FGMRES residual after the same number of
+    iterations than plain SGS (the gain is printed), and applied to every
+    direction it falls back to SGS cycles when it does not help."""
+    c, m, S, _ = make((24, 18, 14), seed=3)
+    S.set_residual_arithmetic(1)
     S.lp_init(1)
-    opts = dict(cfl=20.0, cfl_start=1.0, cfl_ramp_steps=10, nsgs=1, linear_solver=1, fgmres_m=30,
-                fgmres_restarts=2, fgmres_rtol=1e-2, jac_precision=1)
-    for it in range(1, 13):
+    opts = dict(cfl=50.0, cfl_start=1.0, cfl_ramp_steps=20, nsgs=1, linear_solver=1, fgmres_m=30,
+                fgmres_restarts=1, fgmres_rtol=1e-3, jac_precision=1, first_order_steps=10, limiter_freeze=40)
+    for it in range(1, 41):
         S.newton_iterate(it, **opts)
-        if it >= 3:
-            S.lp_collect(nsgs=1, rtol=1e-6, krylov_pairs=10)
-    l0, l1 = S.lp_train(epochs=30, lr=2e-3)
-    assert np.isfinite(l1) and l1 < 0.8 * l0, (l0, l1)
-    # continue the run with both preconditioners on the same systems
-    it_sgs, it_lp = [], []
-    for it in range(13, 19):
+        if it >= 3 and it % 2 == 0:
+            S.lp_collect(nsgs=1, rtol=1e-6)
+    l0, l1 = S.lp_train(epochs=150, lr=2e-3)
+    assert np.isfinite(l1) and l1 < 0.5 * l0, (l0, l1)
+    fixed = dict(opts, fgmres_m=10, fgmres_rtol=1e-12)
+    r_sgs, r_lp, fb_all = [], [], 0
+    for it in range(41, 49):
         st = S.get_state()
-        r1 = S.newton_iterate(it, **opts)
+        r_sgs.append(S.newton_iterate(it, **fixed)["lin_res"])
         S.set_state(st)
-        r2 = S.newton_iterate(it, **dict(opts, linear_solver=2))
-        it_sgs.append(r1["lin_iters"])
-        it_lp.append(r2["lin_iters"])
-        assert r2["lin_res"] < 1e-2 or r2["lp_fallbacks"] > 0
-        assert np.isfinite(r2["res"][0])
-    print("krylov iterations sgs", it_sgs, "learned", it_lp)
+        r_lp.append(S.newton_iterate(it, **dict(fixed, linear_solver=2, lp_directions=3))["lin_res"])
+        S.set_state(st)
+        r = S.newton_iterate(it, **dict(opts, linear_solver=2))
+        fb_all += r["lp_fallbacks"]
+        assert np.isfinite(r["res"][0])
+        S.set_state(st)
+        S.newton_iterate(it, **opts)
+    gain = np.exp(np.mean(np.log(r_sgs)) - np.mean(np.log(r_lp)))
+    print("FGMRES(10) residual: sgs %.3e, learned %.3e (%.2fx lower); fallbacks with every direction: %d"
+          % (np.exp(np.mean(np.log(r_sgs))), np.exp(np.mean(np.log(r_lp))), gain, fb_all))
+    assert gain > 1.0, (r_sgs, r_lp)
