@@ -237,7 +237,7 @@ def converge_study(args):
     if "mixed_learned" in args.converge_arms:
         # same resolution, unseen mesh and state seed
         lp_w, out["learned_training"] = train_learned(dims, 7, 60, 150, 2e-3)
-    finals = {}
+    finals, frozen_lim = {}, None
     for name in args.converge_arms:
         arm = CONV_ARMS[name]
         case = cases.ns_flatplate(*dims)
@@ -268,16 +268,19 @@ def converge_study(args):
         wall = time.perf_counter() - t0
         q = S.get_state()
         finals[name] = (q[:m.nnode, :5].copy(), wall_force(m, case, q))
-        if name == "fp64":
+        if name == "fp64" and len(hist) > opts["first_order_steps"]:
             frozen_lim = S.get_limiter()
         rec = {"iters": len(hist), "wall_s": round(wall, 3), "drop": hist[-1] / hist[0],
                "reached_1e-10": 1e-10 in t_at, "s_to_drop": {str(k): v for k, v in t_at.items()},
                "linear_iters_per_step": lin / len(hist), "health": S.health()}
         if fb:
             rec["sgs_fallbacks"] = fb
+        if not np.isfinite(hist[-1]):
+            rec["stopped"] = "non-finite residual"
+            rec["res_history"] = [float(v) for v in hist[-10:]]
         out[name] = rec
         S.close()
-    if "fp64" in finals and "mixed" in finals:
+    if "fp64" in finals and "mixed" in finals and frozen_lim is not None:
         # The frozen limiter makes the converged field depend on the state at
         # the freeze, which differs between arms.  This check solves the
         # mixed arm's equations with the FP64 arm's frozen limiter from the

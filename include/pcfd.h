@@ -125,8 +125,8 @@ typedef struct pcfd_params {
   int sorder;             /* spatial order 1 or 2 (Param::sorder) */
   double chi;             /* MUSCL blend (Param::chi) */
   int viscous;            /* 0 Euler, 1 laminar Navier-Stokes */
-  int limiter;            /* 0 none, 3 modified Venkatakrishnan (Param::limiter) */
-  double venkat_K;        /* limiter K; the reference hard-codes 1.0 */
+  int limiter;            /* Param::limiter: 0 none, 1 Barth, 2 Venkatakrishnan, 3 modified Venkatakrishnan */
+  double venkat_K;        /* modified Venkatakrishnan K; the reference hard-codes 1.0 */
   int no_cvbc;            /* Param::no_cvbc */
   int jac_boundary_eval;  /* Param::boundaryJacEval: 0 re-derive the phantom state from each
                            * perturbed interior state (reference default), 1 keep it frozen;

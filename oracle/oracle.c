@@ -559,7 +559,7 @@ int oracle_limiter(const pcfd_mesh_view* m, const pcfd_params* prm, const double
   for (size_t i = 0; i < (size_t)nn * NEQN; i++) l[i] = 1.0;
   if (nclip) *nclip = 0;
   if (prm->limiter == 0) return 0;
-  if (prm->limiter != 3) return -1;
+  if (prm->limiter < 1 || prm->limiter > 3) return -1;
   double* qmin = (double*)calloc((size_t)nn * NEQN, sizeof(double));
   double* qmax = (double*)calloc((size_t)nn * NEQN, sizeof(double));
   /* Kernel_FindMinMax, :135 (initialised to zero, quirk kept) */
@@ -576,6 +576,45 @@ int oracle_limiter(const pcfd_mesh_view* m, const pcfd_params* prm, const double
       qmin[b * NEQN + i] = dmin(qmin[b * NEQN + i], qa[i]);
     }
   }
+  if (prm->limiter == 1 || prm->limiter == 2) {
+    /* Kernel_Barth, :194, and Kernel_Venkat, :372: the ratio of the allowed
+     * to the extrapolated change, clamped to [0, 1] (Barth) or passed
+     * through (t^2 + 2t)/(t^2 + t + 2) (Venkatakrishnan) */
+    const double ones1[NEQN] = {1, 1, 1, 1, 1};
+    for (int e = 0; e < m->nedge; e++) {
+      int a = m->edges[2 * e], b = m->edges[2 * e + 1];
+      const double* qL = &q[(size_t)a * NVARS];
+      const double* qR = &q[(size_t)b * NVARS];
+      const double* xL = &m->xyz[3 * a];
+      const double* xR = &m->xyz[3 * b];
+      double QL[NEQN], QR[NEQN], dx[3], dQ[NEQN];
+      for (int i = 0; i < NEQN; i++) dQ[i] = qR[i] - qL[i];
+      dx[0] = 0.5 * (xR[0] - xL[0]); dx[1] = 0.5 * (xR[1] - xL[1]); dx[2] = 0.5 * (xR[2] - xL[2]);
+      extrapolate(chi, QL, qL, dQ, &grad[(size_t)a * NTERMS * 3], dx, ones1);
+      dx[0] = -dx[0]; dx[1] = -dx[1]; dx[2] = -dx[2];
+      for (int i = 0; i < NEQN; i++) dQ[i] = -dQ[i];
+      extrapolate(chi, QR, qR, dQ, &grad[(size_t)b * NTERMS * 3], dx, ones1);
+      for (int side = 0; side < 2; side++) {
+        const int nd = side ? b : a;
+        const double* qs = side ? qR : qL;
+        const double* Qs = side ? QR : QL;
+        for (int j = 0; j < NEQN; j++) {
+          double temp = 1.0;
+          if (Qs[j] > qs[j]) temp = (qmax[nd * NEQN + j] - qs[j]) / (Qs[j] - qs[j]);
+          else if (Qs[j] < qs[j]) temp = (qmin[nd * NEQN + j] - qs[j]) / (Qs[j] - qs[j]);
+          if (prm->limiter == 1) {
+            temp = dmax(0.0, temp);
+            temp = dmin(1.0, temp);
+          } else {
+            temp = (temp * temp + 2.0 * temp) / (temp * temp + temp + 2.0);
+          }
+          l[nd * NEQN + j] = dmin(l[nd * NEQN + j], temp);
+        }
+      }
+    }
+    goto clip;
+  }
+  {
   /* Kernel_VenkatMod, :534 */
   const double Pi = 3.141592653589793;
   const double K = prm->venkat_K;
@@ -614,6 +653,8 @@ int oracle_limiter(const pcfd_mesh_view* m, const pcfd_params* prm, const double
       l[b * NEQN + j] = dmin(l[b * NEQN + j], t);
     }
   }
+  }
+clip:;
   /* Kernel_PressureClip, :737: sequential over edges as in the reference */
   long long clips = 0;
   for (int e = 0; e < m->nedge; e++) {

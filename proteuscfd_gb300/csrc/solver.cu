@@ -664,14 +664,16 @@ __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restri
 }
 
 // -------------------------------------------------------------------------
-// limiter (Limiter::Compute, ucs/limiters.tcc:53; limiter = 3)
+// limiter (Limiter::Compute, ucs/limiters.tcc:53; limiter = 1, 2, 3)
 // -------------------------------------------------------------------------
 
 // Neighbour min/max (initialised to zero as the reference does) and the
-// modified Venkatakrishnan value, fused per node.  The half-edge vector of
-// each incident edge gives dx = 0.5 (x_j - x_i) (its sign flips when the node
-// is the edge's right end).
-template <class S>
+// limiter value, fused per node: LIM 1 Barth (Kernel_Barth,
+// ucs/limiters.tcc:194), 2 Venkatakrishnan (Kernel_Venkat, :372), 3 modified
+// Venkatakrishnan (Kernel_VenkatMod, :534).  The half-edge vector of each
+// incident edge gives dx = 0.5 (x_j - x_i) (its sign flips when the node is
+// the edge's right end).
+template <class S, int LIM>
 __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict__ nptr,
                                                 const int* __restrict__ nedg, const int* __restrict__ nnbr,
                                                 const S* __restrict__ q, const S* __restrict__ grad,
@@ -698,12 +700,50 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
       qmin[t] = (qmin[t] < v) ? qmin[t] : v;
     }
   }
+  const S one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
+  if (LIM != 3) {
+    // t = (allowed change) / (extrapolated change), 1 where the extrapolation
+    // leaves the value unchanged; Barth clamps t to [0, 1], Venkatakrishnan
+    // maps it through (t^2 + 2t) / (t^2 + t + 2) (positive denominator).
+    S lm[NEQN];
+    for (int t = 0; t < NEQN; t++) lm[t] = one;
+    for (int k = k0; k < k1; k++) {
+      int se = nedg[k];
+      const S* qj = &q[(size_t)nnbr[k] * NVARS];
+      const S* hv = &eh[3 * (size_t)(se < 0 ? ~se : se)];
+      S dx0 = hv[0], dx1 = hv[1], dx2 = hv[2];
+      if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
+#pragma unroll
+      for (int t = 0; t < NEQN; t++) {
+        S dQ = qj[t] - qi[t];
+        S Q = qi[t] + (hchi * dQ + omc * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
+        S r = one;
+        if (Q > qi[t]) r = (qmax[t] - qi[t]) / (Q - qi[t]);
+        else if (Q < qi[t]) r = (qmin[t] - qi[t]) / (Q - qi[t]);
+        if (LIM == 1) {
+          r = (r > zero) ? r : zero;
+          r = (r < one) ? r : one;
+        } else {
+          r = (r * r + two * r) / (r * r + r + two);
+        }
+        if (r < lm[t]) lm[t] = r;
+      }
+    }
+    int neg = 0;
+    for (int t = 0; t < NEQN; t++) {
+      S v = lm[t];
+      limraw[(size_t)i * NEQN + t] = v;
+      if (v < zero) neg = 1;
+      if (lim) lim[(size_t)i * NEQN + t] = (v < zero) ? zero : v;
+    }
+    clipflag[i] = neg ? 2 : 0;
+    return;
+  }
   const S ep2 = Sc<S>::from(6.0 * 3.141592653589793 * vol[i] * K3);
   // The limiter is min(1, min_k num_k / den_k) with every den_k > 0
   // (den = (DP + DM/2)^2 + 7/4 DM^2 + eps^2).  The running minimum is kept
   // as a fraction and compared by cross-multiplication, so only one
   // division per equation remains instead of one per edge and equation.
-  const S one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
   S bn[NEQN], bd[NEQN];
   for (int t = 0; t < NEQN; t++) { bn[t] = one; bd[t] = one; }
   for (int k = k0; k < k1; k++) {
@@ -1362,10 +1402,11 @@ int run_gradient(Solver* s, int arith = 0) {
 template <class S>
 int run_venkat_t(Solver* s, RBuf<S> r, bool clip) {
   double K = s->prm.venkat_K;
+  auto kern = s->prm.limiter == 1 ? k_venkat<S, 1> : s->prm.limiter == 2 ? k_venkat<S, 2> : k_venkat<S, 3>;
   return launch(s, T_LIMITER, [&] {
-    k_venkat<S><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.q, r.grad,
-                                                           r.eh, s->d_vol, s->prm.chi, K * K * K, r.limraw,
-                                                           clip ? nullptr : r.lim, s->d_clipflag);
+    kern<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.q, r.grad, r.eh,
+                                                     s->d_vol, s->prm.chi, K * K * K, r.limraw,
+                                                     clip ? nullptr : r.lim, s->d_clipflag);
   });
 }
 
@@ -2261,8 +2302,9 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     return set_err(PCFD_ERR_ARG, "pcfd_create: bad parameters");
   if (prm->jac_boundary_eval < 0 || prm->jac_boundary_eval > 3)
     return set_err(PCFD_ERR_ARG, "pcfd_create: jac_boundary_eval must be 0, 1, 2 or 3");
-  if (prm->limiter != 0 && prm->limiter != 3)
-    return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: only limiter 0 (off) and 3 (modified Venkatakrishnan)");
+  if (prm->limiter < 0 || prm->limiter > 3)
+    return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: limiter must be 0 (off), 1 (Barth), 2 (Venkatakrishnan) or 3 "
+                                         "(modified Venkatakrishnan)");
   if (prm->viscous && (prm->Re <= 0.0 || prm->Pr <= 0.0 || prm->ref_temperature <= 0.0))
     return set_err(PCFD_ERR_ARG, "pcfd_create: viscous run needs Re, Pr and ref_temperature > 0");
   const long long nn = m->nnode, ne = m->nedge, nb = m->nbedge;

@@ -203,3 +203,31 @@ def test_double_float_full_size_freestream():
     np.add.at(area, m.edges[:, 0], m.edge_area[:, 3])
     np.add.at(area, m.edges[:, 1], m.edge_area[:, 3])
     assert (np.abs(b) / (area[:, None] * 5.0)).max() < 1e-12
+
+
+@pytest.mark.parametrize("kind", [1, 2], ids=["barth", "venkat"])
+@pytest.mark.parametrize("arith", [0, 1], ids=["fp64", "df"])
+def test_barth_and_venkat_limiters(kind, arith):
+    """Barth (Kernel_Barth, ucs/limiters.tcc:194) and Venkatakrishnan
+    (Kernel_Venkat, :372) limiters and the residual that uses them, against
+    the oracle; the Venkatakrishnan case has negative raw values, so the
+    pressure clip folded into the edge pass and the clamp to zero run too."""
+    case = cases.ns_flatplate(12, 10, 8, seed=5, venkat_K=1.0)
+    case.param.limiter = kind
+    m, S, O, q0 = run_both(case, "perturbed", seed=11)
+    S.set_residual_arithmetic(arith)
+    S.set_state(q0)
+    norms = S.residual_full()
+    q, g, l, bo, no = O.full(q0)
+    if arith == 0:
+        b = S.compute_residuals()[0]
+        assert_residual_close(b, bo, O.last_babs)
+        assert np.allclose(norms, no, rtol=1e-12, atol=0)
+        S.set_state(q0)
+        S.update_bcs()
+        S.gradient()
+        assert np.abs(S.limiter() - O.limiter(q, g)[0]).max() <= 1e-12
+    else:
+        assert np.allclose(norms, no, rtol=1e-10, atol=0), (norms, no)
+    if kind == 1:
+        assert np.all((l >= 0) & (l <= 1))

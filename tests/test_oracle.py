@@ -162,3 +162,54 @@ def test_noslip_normal_node_is_wall_normal():
         nn = L.oracle_normal_node(C.byref(m.view), node, dp(np.ascontiguousarray(ba[k])))
         assert nn >= 0
         assert m.xyz[nn, 1] > m.xyz[node, 1]
+
+
+def _limiter_loop(m, q, g, chi, kind):
+    """Per-edge restatement of Kernel_Barth (ucs/limiters.tcc:194) and
+    Kernel_Venkat (:372) over the zero-initialised neighbour bounds."""
+    n = m.nnode
+    qmin = np.zeros((n, 5))
+    qmax = np.zeros((n, 5))
+    for a, b in m.edges:
+        qmax[a] = np.maximum(qmax[a], q[b, :5]); qmin[a] = np.minimum(qmin[a], q[b, :5])
+        qmax[b] = np.maximum(qmax[b], q[a, :5]); qmin[b] = np.minimum(qmin[b], q[a, :5])
+    lim = np.ones((n, 5))
+    gr = g.reshape(n, 9, 3)[:, :5]
+    for a, b in m.edges:
+        dx = 0.5 * (m.xyz[b] - m.xyz[a])
+        for nd, other, h in ((a, b, dx), (b, a, -dx)):
+            dq = q[other, :5] - q[nd, :5]
+            Q = q[nd, :5] + (0.5 * chi * dq + (1.0 - chi) * (gr[nd] @ h))
+            for j in range(5):
+                t = 1.0
+                if Q[j] > q[nd, j]:
+                    t = (qmax[nd, j] - q[nd, j]) / (Q[j] - q[nd, j])
+                elif Q[j] < q[nd, j]:
+                    t = (qmin[nd, j] - q[nd, j]) / (Q[j] - q[nd, j])
+                t = min(1.0, max(0.0, t)) if kind == 1 else (t * t + 2 * t) / (t * t + t + 2)
+                lim[nd, j] = min(lim[nd, j], t)
+    return lim
+
+
+@pytest.mark.parametrize("kind", [1, 2])
+def test_barth_and_venkat_limiters(kind):
+    """The oracle's Barth (1) and Venkatakrishnan (2) limiters against a
+    per-edge loop, and their uniform-flow values: the extrapolation leaves a
+    uniform field unchanged, so t = 1 gives 1 for Barth and 3/4 for the
+    reference's Venkatakrishnan form, which is applied without a guard."""
+    m = Mesh.box(6, 5, 5, jitter=0.15, seed=3)
+    prm = euler_param(sorder=2, limiter=kind)
+    o = OracleSpace(m, prm)
+    q = cases.perturbed_state(o.qinf(), m.nnode + m.nbedge, 4)
+    g = o.gradient(q)
+    l, nclip = o.limiter(q, g)
+    assert nclip == 0
+    # the clamp to zero follows the (here idle) pressure clip
+    ref = np.maximum(_limiter_loop(m, q, g, prm.chi, kind), 0.0)
+    assert np.abs(l - ref).max() <= 1e-12
+    if kind == 1:
+        assert np.all((l >= 0) & (l <= 1))
+    qu = np.tile(o.qinf(), (m.nnode + m.nbedge, 1))
+    lu, nclip = o.limiter(qu, o.gradient(qu))
+    assert nclip == 0
+    assert np.allclose(lu, 1.0 if kind == 1 else 0.75, rtol=0, atol=1e-15)
