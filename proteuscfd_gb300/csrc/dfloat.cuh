@@ -80,6 +80,9 @@ __device__ __forceinline__ dfl operator/(dfl a, dfl b) {
   float rr = __fadd_rn(d.hi, __fadd_rn(__fsub_rn(d.lo, pe), a.lo));
   return fast_two_sum(q1, __fmul_rn(rr, r));
 }
+// 2a, exact (both parts scale by a power of two)
+__device__ __forceinline__ dfl twice(dfl a) { return mkdf(2.0f * a.hi, 2.0f * a.lo); }
+__device__ __forceinline__ double twice(double a) { return 2.0 * a; }
 __device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { return a = a + b; }
 __device__ __forceinline__ dfl& operator-=(dfl& a, dfl b) { return a = a - b; }
 __device__ __forceinline__ dfl& operator*=(dfl& a, dfl b) { return a = a * b; }
@@ -89,6 +92,16 @@ __device__ __forceinline__ bool operator<=(dfl a, dfl b) { return !(b < a); }
 __device__ __forceinline__ bool operator>=(dfl a, dfl b) { return !(a < b); }
 __device__ __forceinline__ bool operator==(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
 
+// hardware reciprocal approximation (PTX rcp.approx, at most 1 ulp off)
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// s = sqrt(hi) in FP32, then one Newton correction (a - s^2) / (2 s) whose
+// residual a - s^2 is formed exactly; the correction is about 2^-24 of the
+// result, so an FP32 approximation of 1 / (2 s) is enough for it
 __device__ __forceinline__ dfl sqrt(dfl a) {
   if (!(a.hi > 0.0f)) return mkdf(__fsqrt_rn(a.hi), 0.0f);
   float s = __fsqrt_rn(a.hi);
@@ -97,7 +110,7 @@ __device__ __forceinline__ dfl sqrt(dfl a) {
   dfl d = two_sum(a.hi, -p);
   float r = __fadd_rn(__fsub_rn(d.lo, pe), a.lo);
   r = __fadd_rn(d.hi, r);
-  return fast_two_sum(s, __fmul_rn(r, __fdiv_rn(0.5f, s)));
+  return fast_two_sum(s, __fmul_rn(r, __fmul_rn(0.5f, rcp_approx(s))));
 }
 __device__ __forceinline__ dfl fabs(dfl a) { return (a.hi < 0.0f) ? -a : a; }
 __device__ __forceinline__ bool isnan(dfl a) { return ::isnan(a.hi) || ::isnan(a.lo); }

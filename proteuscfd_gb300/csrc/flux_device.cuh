@@ -30,9 +30,9 @@ __device__ __forceinline__ S entropy_fix(S eig, S eigL, S eigR) {
   return a;
 }
 
-// Roe flux with the reference's eigen-decomposition: RoeVariables (:533),
-// Eigensystem (:580), entropy fix, |A| dQ = T |L| Tinv dQ, and
-// 0.5 area (F_L + F_R - |A| dQ) (RoeFlux, :93).  (nx, ny, nz, area) is the
+// Roe flux with the reference's eigensystem: RoeVariables (:533),
+// Eigensystem (:580), entropy fix, |A| dQ = T |L| Tinv dQ (evaluated in
+// projector form, below), and 0.5 area (F_L + F_R - |A| dQ) (RoeFlux, :93).  (nx, ny, nz, area) is the
 // edge's unit normal and area; static grid (vdotn = 0).
 // Returns a mask of non-physical states in the sense of BadExtrapolation
 // (ucs/compressible.tcc:1056: p < 1e-10, rho < 0 or rho E < 1e-10):
@@ -62,12 +62,10 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
   const S h = hL + sigma * (hR - hL);
   S v2h = half * (u * u + v * v + w * w);
   const S rE = rho * igamma * (h + gm1 * v2h);
-  const S irho = one / rho;
   const S P = gm1 * (rE - rho * v2h);
-  const S c2 = gamma * P * irho;
+  const S c2 = gm1 * (h - v2h);  // = gamma P / rho with P and rE above
   const S c = sqrt(c2);
-  const S ic = one / c;
-  const S ic2 = ic * ic;
+  const S ic2 = one / c2;
   const S thetaf = u * nx + v * ny + w * nz;
 
   // entropy-fixed |eigenvalues|
@@ -81,34 +79,25 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
 
   const S d0 = QR[0] - QL[0], d1 = QR[1] - QL[1], d2 = QR[2] - QL[2], d3 = QR[3] - QL[3], d4 = QR[4] - QL[4];
 
-  // dv = Tinv dQ (rows of the left eigenvector matrix)
-  const S gv = gm1 * v2h, gu = gm1 * u, gvv = gm1 * v, gw = gm1 * w;
-  S dv0 = (nx - nz * v * irho + ny * w * irho - nx * ic2 * gv) * d0 + (nx * ic2 * gu) * d1 +
-          (nz * irho + nx * ic2 * gvv) * d2 + (-ny * irho + nx * ic2 * gw) * d3 + (-nx * ic2 * gm1) * d4;
-  S dv1 = (ny + nz * u * irho - nx * w * irho - ny * ic2 * gv) * d0 + (-nz * irho + ny * ic2 * gu) * d1 +
-          (ny * ic2 * gvv) * d2 + (nx * irho + ny * ic2 * gw) * d3 + (-ny * ic2 * gm1) * d4;
-  S dv2 = (nz - ny * u * irho + nx * v * irho - nz * ic2 * gv) * d0 + (ny * irho + nz * ic2 * gu) * d1 +
-          (-nx * irho + nz * ic2 * gvv) * d2 + (nz * ic2 * gw) * d3 + (-nz * ic2 * gm1) * d4;
-  const S hr = half * irho;
-  S dv3 = (-hr * (thetaf - gv * ic)) * d0 + (hr * (nx - gu * ic)) * d1 + (hr * (ny - gvv * ic)) * d2 +
-          (hr * (nz - gw * ic)) * d3 + (hr * (gm1 * ic)) * d4;
-  S dv4 = (hr * (thetaf + gv * ic)) * d0 + (-hr * (nx + gu * ic)) * d1 + (-hr * (ny + gvv * ic)) * d2 +
-          (-hr * (nz + gw * ic)) * d3 + (hr * (gm1 * ic)) * d4;
-  dv0 *= l0; dv1 *= l0; dv2 *= l0; dv3 *= l3; dv4 *= l4;
-
-  // dr = T dv (columns of the right eigenvector matrix)
-  const S rc = rho * ic;
-  const S cg = c * igm1;
-  const S dr0 = nx * dv0 + ny * dv1 + nz * dv2 + rc * dv3 + rc * dv4;
-  const S dr1 = (u * nx) * dv0 + (u * ny - rho * nz) * dv1 + (u * nz + rho * ny) * dv2 + rho * (u * ic + nx) * dv3 +
-                rho * (u * ic - nx) * dv4;
-  const S dr2 = (v * nx + rho * nz) * dv0 + (v * ny) * dv1 + (v * nz - rho * nx) * dv2 + rho * (v * ic + ny) * dv3 +
-                rho * (v * ic - ny) * dv4;
-  const S dr3 = (w * nx - rho * ny) * dv0 + (w * ny + rho * nx) * dv1 + (w * nz) * dv2 + rho * (w * ic + nz) * dv3 +
-                rho * (w * ic - nz) * dv4;
-  const S dr4 = (v2h * nx + rho * (v * nz - w * ny)) * dv0 + (v2h * ny + rho * (w * nx - u * nz)) * dv1 +
-                (v2h * nz + rho * (u * ny - v * nx)) * dv2 + rho * (v2h * ic + thetaf + cg) * dv3 +
-                rho * (v2h * ic - thetaf + cg) * dv4;
+  // |A| dQ = T |L| Tinv dQ.  The three entropy/shear columns of T share the
+  // eigenvalue l0, so the product is l0 dQ + (l3 - l0) P+ dQ + (l4 - l0) P- dQ
+  // with P+/- the projectors on the two acoustic eigenvectors
+  // r+/- = (1, u +/- c n, h +/- c theta): the same value as the reference's
+  // two 5x5 products (any basis of the l0 eigenspace gives it), in about a
+  // third of the operations.  P+/- dQ = a+/- r+/- with
+  // a+/- = (dp +/- c rho dVn) / (2 c^2), where rho dVn = n.d(rho u) - theta d(rho)
+  // and dp = (gamma - 1)(d(rho E) - u.d(rho u) + |u|^2/2 d(rho)) at the Roe state.
+  const S rdvn = (nx * d1 + ny * d2 + nz * d3) - thetaf * d0;
+  const S dp = gm1 * (d4 - (u * d1 + v * d2 + w * d3) + v2h * d0);
+  const S hic2 = half * ic2;
+  const S ap3 = (l3 - l0) * ((dp + c * rdvn) * hic2);
+  const S ap4 = (l4 - l0) * ((dp - c * rdvn) * hic2);
+  const S sp = ap3 + ap4, sm = c * (ap3 - ap4);
+  const S dr0 = l0 * d0 + sp;
+  const S dr1 = l0 * d1 + (u * sp + nx * sm);
+  const S dr2 = l0 * d2 + (v * sp + ny * sm);
+  const S dr3 = l0 * d3 + (w * sp + nz * sm);
+  const S dr4 = l0 * d4 + (h * sp + thetaf * sm);
 
   // physical fluxes (Flux, :686)
   const S rtL = rL * thetaL, rtR = rR * thetaR;

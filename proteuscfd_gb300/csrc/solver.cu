@@ -667,39 +667,23 @@ __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restri
 // limiter (Limiter::Compute, ucs/limiters.tcc:53; limiter = 1, 2, 3)
 // -------------------------------------------------------------------------
 
-// Neighbour min/max (initialised to zero as the reference does) and the
-// limiter value, fused per node: LIM 1 Barth (Kernel_Barth,
+// The limiter of node i from its state qi, its gradient gi (first NEQN
+// terms) and the neighbour bounds qmin/qmax (Kernel_FindMinMax, :135,
+// initialised to zero as the reference does): LIM 1 Barth (Kernel_Barth,
 // ucs/limiters.tcc:194), 2 Venkatakrishnan (Kernel_Venkat, :372), 3 modified
 // Venkatakrishnan (Kernel_VenkatMod, :534).  The half-edge vector of each
 // incident edge gives dx = 0.5 (x_j - x_i) (its sign flips when the node is
-// the edge's right end).
-template <class S, int LIM>
-__global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict__ nptr,
-                                                const int* __restrict__ nedg, const int* __restrict__ nnbr,
-                                                const S* __restrict__ q, const S* __restrict__ grad,
-                                                const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
-                                                double K3, S* __restrict__ limraw, S* __restrict__ lim,
-                                                int* __restrict__ clipflag) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nnode) return;
+// the edge's right end).  Writes the raw value, the clamped value (lim may
+// be null) and the clip flag.  CHI0: chi = 0, so the extrapolation is
+// q + grad.dx exactly and the 0.5 chi dQ term is skipped (bit-identical).
+template <class S, int LIM, bool CHI0>
+__device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __restrict__ nedg,
+                                           const int* __restrict__ nnbr, const S* __restrict__ q,
+                                           const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
+                                           double K3, const S* qi, const S* gi, const S* qmin, const S* qmax,
+                                           S* __restrict__ limraw, S* __restrict__ lim, int* __restrict__ clipflag) {
   const S zero = Sc<S>::c(0.0);
   const S chi = Sc<S>::from(chi_d), hchi = Sc<S>::c(0.5) * chi, omc = Sc<S>::c(1.0) - chi;
-  S qi[NEQN], qmin[NEQN], qmax[NEQN], gi[NEQN * 3];
-  for (int t = 0; t < NEQN; t++) {
-    qi[t] = q[(size_t)i * NVARS + t];
-    qmin[t] = zero;
-    qmax[t] = zero;
-  }
-  for (int t = 0; t < NEQN * 3; t++) gi[t] = grad[(size_t)i * NTERMS * 3 + t];
-  const int k0 = nptr[i], k1 = nptr[i + 1];
-  for (int k = k0; k < k1; k++) {
-    const S* qj = &q[(size_t)nnbr[k] * NVARS];
-    for (int t = 0; t < NEQN; t++) {
-      S v = qj[t];
-      qmax[t] = (qmax[t] > v) ? qmax[t] : v;
-      qmin[t] = (qmin[t] < v) ? qmin[t] : v;
-    }
-  }
   const S one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
   if (LIM != 3) {
     // t = (allowed change) / (extrapolated change), 1 where the extrapolation
@@ -715,8 +699,8 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
       if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
 #pragma unroll
       for (int t = 0; t < NEQN; t++) {
-        S dQ = qj[t] - qi[t];
-        S Q = qi[t] + (hchi * dQ + omc * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
+        S gdx = gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2;
+        S Q = CHI0 ? qi[t] + gdx : qi[t] + (hchi * (qj[t] - qi[t]) + omc * gdx);
         S r = one;
         if (Q > qi[t]) r = (qmax[t] - qi[t]) / (Q - qi[t]);
         else if (Q < qi[t]) r = (qmin[t] - qi[t]) / (Q - qi[t]);
@@ -744,8 +728,21 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
   // (den = (DP + DM/2)^2 + 7/4 DM^2 + eps^2).  The running minimum is kept
   // as a fraction and compared by cross-multiplication, so only one
   // division per equation remains instead of one per edge and equation.
-  S bn[NEQN], bd[NEQN];
-  for (int t = 0; t < NEQN; t++) { bn[t] = one; bd[t] = one; }
+  // DP takes one of two values per equation (qmax - q or qmin - q, by the
+  // sign of DM); both and their squares are formed once, outside the
+  // neighbour loop.  FP64 keeps the reference's expression order
+  // (ucs/limiters.tcc:617); double-float forms DM as the extrapolation's
+  // correction itself and adds eps^2 to DP^2 first.
+  constexpr bool F64 = std::is_same<S, double>::value;
+  S dpp[NEQN], dpm[NEQN], bp[NEQN], bm[NEQN], bn[NEQN], bd[NEQN];
+  for (int t = 0; t < NEQN; t++) {
+    dpp[t] = qmax[t] - qi[t];
+    dpm[t] = qmin[t] - qi[t];
+    bp[t] = F64 ? dpp[t] * dpp[t] : dpp[t] * dpp[t] + ep2;
+    bm[t] = F64 ? dpm[t] * dpm[t] : dpm[t] * dpm[t] + ep2;
+    bn[t] = one;
+    bd[t] = one;
+  }
   for (int k = k0; k < k1; k++) {
     int se = nedg[k];
     const S* qj = &q[(size_t)nnbr[k] * NVARS];
@@ -754,12 +751,27 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
     if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      S dQ = qj[t] - qi[t];
-      S Q = qi[t] + (hchi * dQ + omc * (gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2));
-      S DM = Q - qi[t];
-      S DP = (Q > qi[t]) ? qmax[t] - qi[t] : qmin[t] - qi[t];
-      S num = DP * DP + ep2 + two * DM * DP;
-      S den = DP * DP + two * DM * DM + DM * DP + ep2;
+      S gdx = gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2;
+      S corr = CHI0 ? gdx : hchi * (qj[t] - qi[t]) + omc * gdx;
+      S num, den;
+      if (F64) {
+        S Q = qi[t] + corr;
+        S DM = Q - qi[t];
+        bool pos = Q > qi[t];
+        S DP = pos ? dpp[t] : dpm[t];
+        S P2 = pos ? bp[t] : bm[t];
+        S mp = DM * DP;
+        num = P2 + ep2 + twice(mp);
+        den = P2 + twice(DM * DM) + mp + ep2;
+      } else {
+        S DM = corr;
+        bool pos = DM > zero;
+        S DP = pos ? dpp[t] : dpm[t];
+        S P2 = pos ? bp[t] : bm[t];
+        S mp = DM * DP;
+        num = P2 + twice(mp);
+        den = P2 + twice(DM * DM) + mp;
+      }
       if (num * bd[t] < bn[t] * den) { bn[t] = num; bd[t] = den; }
     }
   }
@@ -773,6 +785,37 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
     if (lim) lim[(size_t)i * NEQN + t] = (v < zero) ? zero : v;
   }
   clipflag[i] = neg ? 2 : 0;
+}
+
+// Standalone limiter (Limiter<T>::Compute after a separate gradient): the
+// neighbour bounds, then limit_node.
+template <class S, int LIM, bool CHI0>
+__global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict__ nptr,
+                                                const int* __restrict__ nedg, const int* __restrict__ nnbr,
+                                                const S* __restrict__ q, const S* __restrict__ grad,
+                                                const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
+                                                double K3, S* __restrict__ limraw, S* __restrict__ lim,
+                                                int* __restrict__ clipflag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  const S zero = Sc<S>::c(0.0);
+  S qi[NEQN], qmin[NEQN], qmax[NEQN], gi[NEQN * 3];
+  for (int t = 0; t < NEQN; t++) {
+    qi[t] = q[(size_t)i * NVARS + t];
+    qmin[t] = zero;
+    qmax[t] = zero;
+  }
+  for (int t = 0; t < NEQN * 3; t++) gi[t] = grad[(size_t)i * NTERMS * 3 + t];
+  const int k0 = nptr[i], k1 = nptr[i + 1];
+  for (int k = k0; k < k1; k++) {
+    const S* qj = &q[(size_t)nnbr[k] * NVARS];
+    for (int t = 0; t < NEQN; t++) {
+      S v = qj[t];
+      qmax[t] = (qmax[t] > v) ? qmax[t] : v;
+      qmin[t] = (qmin[t] < v) ? qmin[t] : v;
+    }
+  }
+  limit_node<S, LIM, CHI0>(i, k0, k1, nedg, nnbr, q, eh, vol, chi_d, K3, qi, gi, qmin, qmax, limraw, lim, clipflag);
 }
 
 // BadExtrapolation (ucs/compressible.tcc:1056)
@@ -923,8 +966,9 @@ __device__ __forceinline__ int kneecap5(S* f) {
 // (ucs/limiters.tcc:737) tests exactly these states, so when nothing is
 // flagged the clip is a no-op and the fluxes already stand.  MODE 2:
 // re-evaluates only edges touching a flagged node, after their limiters were
-// zeroed; it returns at once when nothing was flagged.
-template <class S, int MODE>
+// zeroed; it returns at once when nothing was flagged.  CHI0: chi = 0, so
+// the MUSCL correction is grad.dx alone (bit-identical to the general form).
+template <class S, int MODE, bool CHI0>
 __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __restrict__ en,
                                                    const typename V4<S>::type* __restrict__ ea,
                                                    const S* __restrict__ eh, const S* __restrict__ q,
@@ -953,9 +997,17 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
     const S* lR = &lim[(size_t)n.y * NEQN];
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      S dQ = qR[t] - qL[t];
-      S cl = k.hchi * dQ + k.omc * (gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2);
-      S cr = k.hchi * (-dQ) + k.omc * (gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2));
+      S gl = gL[3 * t] * h0 + gL[3 * t + 1] * h1 + gL[3 * t + 2] * h2;
+      S gr = gR[3 * t] * (-h0) + gR[3 * t + 1] * (-h1) + gR[3 * t + 2] * (-h2);
+      S cl, cr;
+      if (CHI0) {
+        cl = gl;
+        cr = gr;
+      } else {
+        S dQ = qR[t] - qL[t];
+        cl = k.hchi * dQ + k.omc * gl;
+        cr = k.hchi * (-dQ) + k.omc * gr;
+      }
       QL[t] = qL[t] + cl * lL[t];
       QR[t] = qR[t] + cr * lR[t];
     }
@@ -1402,7 +1454,10 @@ int run_gradient(Solver* s, int arith = 0) {
 template <class S>
 int run_venkat_t(Solver* s, RBuf<S> r, bool clip) {
   double K = s->prm.venkat_K;
-  auto kern = s->prm.limiter == 1 ? k_venkat<S, 1> : s->prm.limiter == 2 ? k_venkat<S, 2> : k_venkat<S, 3>;
+  const bool c0 = s->prm.chi == 0.0;
+  auto kern = s->prm.limiter == 1 ? (c0 ? k_venkat<S, 1, true> : k_venkat<S, 1, false>)
+              : s->prm.limiter == 2 ? (c0 ? k_venkat<S, 2, true> : k_venkat<S, 2, false>)
+                                    : (c0 ? k_venkat<S, 3, true> : k_venkat<S, 3, false>);
   return launch(s, T_LIMITER, [&] {
     kern<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.q, r.grad, r.eh,
                                                      s->d_vol, s->prm.chi, K * K * K, r.limraw,
@@ -1456,10 +1511,12 @@ int run_limiter(Solver* s, bool clip, int arith = 0) {
 
 template <class S>
 int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
+  const bool c0 = s->prm.chi == 0.0;
+  auto flux1 = c0 ? k_edge_flux<S, 1, true> : k_edge_flux<S, 1, false>;
+  auto flux2 = c0 ? k_edge_flux<S, 2, true> : k_edge_flux<S, 2, false>;
   int rc = launch(s, T_EDGEFLUX, [&] {
-    k_edge_flux<S, 1><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k,
-                                                                 r.ef, s->d_health, s->d_clipflag, s->d_clipany,
-                                                                 r.limraw);
+    flux1<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k, r.ef,
+                                                      s->d_health, s->d_clipflag, s->d_clipany, r.limraw);
   });
   if (rc) return rc;
   if (k.clip) {
@@ -1468,9 +1525,8 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
     });
     if (rc) return rc;
     rc = launch(s, T_CLIP, [&] {
-      k_edge_flux<S, 2><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim,
-                                                                   k, r.ef, s->d_health, s->d_clipflag, s->d_clipany,
-                                                                   r.limraw);
+      flux2<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k, r.ef,
+                                                        s->d_health, s->d_clipflag, s->d_clipany, r.limraw);
     });
     if (rc) return rc;
   }
@@ -2928,15 +2984,11 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   // frozen values otherwise (:671-690)
   if ((rc = run_bcs(s, s->arith))) return rc;
   const bool ho_now = s->prm.sorder > 1 && o->iter > o->first_order_steps;
+  const int refresh = o->limiter_refresh > 0 ? o->limiter_refresh : 1;
+  const bool frozen = o->limiter_freeze > 0 && o->iter >= o->limiter_freeze;
+  const bool recompute = (o->iter % refresh == 0 && !frozen) || !s->have_lim || s->lim_arith != s->arith;
   if ((ho_now || s->prm.viscous) && (rc = run_gradient(s, s->arith))) return rc;
-  if (ho_now) {
-    const int refresh = o->limiter_refresh > 0 ? o->limiter_refresh : 1;
-    const bool frozen = o->limiter_freeze > 0 && o->iter >= o->limiter_freeze;
-    const bool recompute = (o->iter % refresh == 0 && !frozen) || !s->have_lim || s->lim_arith != s->arith;
-    if (s->prm.limiter == 0 || recompute) {
-      if ((rc = run_limiter(s, false, s->arith))) return rc;
-    }
-  }
+  if (ho_now && (s->prm.limiter == 0 || recompute) && (rc = run_limiter(s, false, s->arith))) return rc;
   if ((rc = run_residual(s, s->arith, !ho_now))) return rc;
   double lin = 0.0;
   int lin_it = 0, fallbacks = 0;

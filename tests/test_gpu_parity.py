@@ -231,3 +231,28 @@ def test_barth_and_venkat_limiters(kind, arith):
         assert np.allclose(norms, no, rtol=1e-10, atol=0), (norms, no)
     if kind == 1:
         assert np.all((l >= 0) & (l <= 1))
+
+
+@pytest.mark.parametrize("limiter", [3, 1], ids=["venkat_mod", "barth"])
+@pytest.mark.parametrize("arith", [0, 1], ids=["fp64", "df"])
+def test_muscl_with_nonzero_chi(limiter, arith):
+    """The general MUSCL extrapolation q + (chi/2 dQ + (1 - chi) grad.dx) in
+    the limiter and the edge flux (the chi = 0 kernels skip the dQ term),
+    against the oracle with chi = 1/3."""
+    case = cases.ns_flatplate(12, 10, 8, seed=5, venkat_K=1.0)
+    case.param.chi = 1.0 / 3.0
+    case.param.limiter = limiter
+    m, S, O, q0 = run_both(case, "perturbed", seed=13)
+    S.set_residual_arithmetic(arith)
+    S.set_state(q0)
+    norms = S.residual_full()
+    q, g, l, bo, no = O.full(q0)
+    if arith == 0:
+        assert_residual_close(S.compute_residuals()[0], bo, O.last_babs)
+        assert np.allclose(norms, no, rtol=1e-12, atol=0)
+        S.set_state(q0)
+        S.update_bcs()
+        S.gradient()
+        assert np.abs(S.limiter() - O.limiter(q, g)[0]).max() <= 1e-12
+    else:
+        assert np.allclose(norms, no, rtol=1e-10, atol=0), (norms, no)
