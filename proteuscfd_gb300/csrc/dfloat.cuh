@@ -80,9 +80,12 @@ __device__ __forceinline__ dfl operator/(dfl a, dfl b) {
   float rr = __fadd_rn(d.hi, __fadd_rn(__fsub_rn(d.lo, pe), a.lo));
   return fast_two_sum(q1, __fmul_rn(rr, r));
 }
-// 2a, exact (both parts scale by a power of two)
+// 2a and a/2, exact (both parts scale by a power of two); the same values
+// as a multiplication by the constant, without its error terms
 __device__ __forceinline__ dfl twice(dfl a) { return mkdf(2.0f * a.hi, 2.0f * a.lo); }
 __device__ __forceinline__ double twice(double a) { return 2.0 * a; }
+__device__ __forceinline__ dfl halve(dfl a) { return mkdf(0.5f * a.hi, 0.5f * a.lo); }
+__device__ __forceinline__ double halve(double a) { return 0.5 * a; }
 __device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { return a = a + b; }
 __device__ __forceinline__ dfl& operator-=(dfl& a, dfl b) { return a = a - b; }
 __device__ __forceinline__ dfl& operator*=(dfl& a, dfl b) { return a = a * b; }

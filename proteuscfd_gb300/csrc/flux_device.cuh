@@ -26,7 +26,7 @@ __device__ __forceinline__ S entropy_fix(S eig, S eigL, S eigR) {
   S eps = smax(eig - eigL, eigR - eig);
   eps = smax(Sc<S>::c(0.0), eps);
   S a = fabs(eig);
-  if (a < eps) a = Sc<S>::c(0.5) * (eig * eig / eps + eps);
+  if (a < eps) a = halve(eig * eig / eps + eps);
   return a;
 }
 
@@ -42,15 +42,14 @@ __device__ __forceinline__ S entropy_fix(S eig, S eigL, S eigR) {
 template <class S>
 __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, const S ny, const S nz, const S area,
                                         const S gamma, const S gm1, const S igamma, const S igm1, S* flux) {
-  const S half = Sc<S>::c(0.5);
   const S one = Sc<S>::c(1.0);
   const S rL = QL[0], irL = one / rL;
   const S uL = QL[1] * irL, vL = QL[2] * irL, wL = QL[3] * irL, EL = QL[4];
-  const S PL = gm1 * (EL - half * rL * (uL * uL + vL * vL + wL * wL));
+  const S PL = gm1 * (EL - halve(rL) * (uL * uL + vL * vL + wL * wL));
   const S hL = (EL + PL) * irL;
   const S rR = QR[0], irR = one / rR;
   const S uR = QR[1] * irR, vR = QR[2] * irR, wR = QR[3] * irR, ER = QR[4];
-  const S PR = gm1 * (ER - half * rR * (uR * uR + vR * vR + wR * wR));
+  const S PR = gm1 * (ER - halve(rR) * (uR * uR + vR * vR + wR * wR));
   const S hR = (ER + PR) * irR;
 
   // Roe-averaged state
@@ -60,7 +59,7 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
   const S v = vL + sigma * (vR - vL);
   const S w = wL + sigma * (wR - wL);
   const S h = hL + sigma * (hR - hL);
-  S v2h = half * (u * u + v * v + w * w);
+  S v2h = halve(u * u + v * v + w * w);
   const S rE = rho * igamma * (h + gm1 * v2h);
   const S P = gm1 * (rE - rho * v2h);
   const S c2 = gm1 * (h - v2h);  // = gamma P / rho with P and rE above
@@ -89,7 +88,7 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
   // and dp = (gamma - 1)(d(rho E) - u.d(rho u) + |u|^2/2 d(rho)) at the Roe state.
   const S rdvn = (nx * d1 + ny * d2 + nz * d3) - thetaf * d0;
   const S dp = gm1 * (d4 - (u * d1 + v * d2 + w * d3) + v2h * d0);
-  const S hic2 = half * ic2;
+  const S hic2 = halve(ic2);
   const S ap3 = (l3 - l0) * ((dp + c * rdvn) * hic2);
   const S ap4 = (l4 - l0) * ((dp - c * rdvn) * hic2);
   const S sp = ap3 + ap4, sm = c * (ap3 - ap4);
@@ -101,7 +100,7 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
 
   // physical fluxes (Flux, :686)
   const S rtL = rL * thetaL, rtR = rR * thetaR;
-  const S ha = half * area;
+  const S ha = halve(area);
   flux[0] = ha * (rtL + rtR - dr0);
   flux[1] = ha * ((uL * rtL + PL * nx) + (uR * rtR + PR * nx) - dr1);
   flux[2] = ha * ((vL * rtL + PL * ny) + (vR * rtR + PR * ny) - dr2);
@@ -145,7 +144,7 @@ __device__ __forceinline__ void viscous_flux(const S u, const S v, const S w, co
   const S two = Sc<S>::c(2.0);
   const S mu = sutherland(T, Sconst);
   const S fact = Sc<S>::c(-2.0 / 3.0) * (ux + vy + wz);
-  const S tauxx = two * ux + fact, tauyy = two * vy + fact, tauzz = two * wz + fact;
+  const S tauxx = twice(ux) + fact, tauyy = twice(vy) + fact, tauzz = twice(wz) + fact;
   const S tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
   const S RKT = rk * mu;
   const S c1 = -(mu * cp_over_pr);

@@ -737,9 +737,10 @@ __global__ void k_diag_f32(long long n25, const double* __restrict__ diag, const
 // (ucs/compressible.tcc:929) clips density, energy and pressure, the
 // auxiliary variables are recomputed, and b-style partial sums of dq^2 are
 // formed for the update norm.
+// fq, when given, is the double-float copy of q, updated with each row.
 __global__ void __launch_bounds__(kNormThreads) k_apply_dq(int nnode, double gamma, double* __restrict__ x,
-                                                            double* __restrict__ q, double* __restrict__ part,
-                                                            unsigned long long* health) {
+                                                            double* __restrict__ q, dfl* __restrict__ fq,
+                                                            double* __restrict__ part, unsigned long long* health) {
   __shared__ double red[kNormThreads / 32];
   double acc = 0.0;
   const double gm1 = gamma - 1.0;
@@ -775,6 +776,8 @@ __global__ void __launch_bounds__(kNormThreads) k_apply_dq(int nnode, double gam
       Q[1] += dQ[1]; Q[2] += dQ[2]; Q[3] += dQ[3];
     }
     aux_vars(gamma, Q);
+    if (fq)
+      for (int j = 0; j < NVARS; j++) fq[(size_t)i * NVARS + j] = to_df(Q[j]);
     for (int k = 0; k < 5; k++) acc += dQ[k] * dQ[k];
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);

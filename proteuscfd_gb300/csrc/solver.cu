@@ -440,6 +440,14 @@ __device__ int apply_bc(const BcConst& k, int bct, double* QL, double* QR, const
 // Reads of q in the first kernel therefore all see the state before the
 // update, as in the reference's sequential loop (ucs/bc.tcc:1400).
 
+// Writes one state row; fq, when given, is the double-float copy of q the
+// residual reads, kept current row by row instead of converted again whole.
+__device__ __forceinline__ void store_row(double* __restrict__ q, dfl* __restrict__ fq, int row, const double* Q) {
+  for (int j = 0; j < NVARS; j++) q[(size_t)row * NVARS + j] = Q[j];
+  if (fq)
+    for (int j = 0; j < NVARS; j++) fq[(size_t)row * NVARS + j] = to_df(Q[j]);
+}
+
 __device__ __forceinline__ bool hardsets(int bct) {
   return bct == PCFD_BC_NOSLIP || bct == PCFD_BC_SONIC_INFLOW || bct == PCFD_BC_DIRICHLET;
 }
@@ -527,18 +535,15 @@ __global__ void k_bc_group_nodes(int ngroup, const int* __restrict__ gnode, cons
                                  const int* __restrict__ ghe, const int2* __restrict__ bn,
                                  const int* __restrict__ bbc, const double* __restrict__ btw,
                                  const int* __restrict__ bnrm, BcConst k, const double* __restrict__ qr_in,
-                                 double* __restrict__ q) {
+                                 double* __restrict__ q, dfl* __restrict__ fq) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngroup) return;
   const int node = gnode[g];
   double QL[NVARS];
   for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)node * NVARS + j];
   replay_group(k, gptr[g], gptr[g + 1], ghe, bn, bbc, btw, bnrm, q, QL);
-  for (int j = 0; j < NVARS; j++) q[(size_t)node * NVARS + j] = QL[j];
-  for (int p = gptr[g]; p < gptr[g + 1]; p++) {
-    const int ph = bn[ghe[p]].y;
-    for (int j = 0; j < NVARS; j++) q[(size_t)ph * NVARS + j] = qr_in[(size_t)p * NVARS + j];
-  }
+  store_row(q, fq, node, QL);
+  for (int p = gptr[g]; p < gptr[g + 1]; p++) store_row(q, fq, bn[ghe[p]].y, &qr_in[(size_t)p * NVARS]);
 }
 
 // Half-edges of boundary nodes that no condition hard-sets (far field, walls,
@@ -549,7 +554,7 @@ __global__ void k_bc_group_nodes(int ngroup, const int* __restrict__ gnode, cons
 __global__ void k_bc_halfedges(int n, const int* __restrict__ list, const int2* __restrict__ bn,
                                const D4* __restrict__ ba, const int* __restrict__ bbc,
                                const double* __restrict__ btw, BcConst k, double* __restrict__ q,
-                               unsigned long long* health) {
+                               dfl* __restrict__ fq, unsigned long long* health) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   int he = list[t];
@@ -559,14 +564,14 @@ __global__ void k_bc_halfedges(int n, const int* __restrict__ list, const int2* 
   for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)nd.y * NVARS + j];
   double nQ[NVARS] = {0};
   if (!apply_bc(k, bbc[he], QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
-  for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = QR[j];
+  store_row(q, fq, nd.y, QR);
 }
 
 // The same for the double-float residual arithmetic: far-field and wall
 // sub-iterations in double-float, the phantom state written back in FP64.
 __global__ void k_bc_halfedges_df(int n, const int* __restrict__ list, const int2* __restrict__ bn,
                                   const D4* __restrict__ ba, const int* __restrict__ bbc, BcConst k,
-                                  double* __restrict__ q, unsigned long long* health) {
+                                  double* __restrict__ q, dfl* __restrict__ fq, unsigned long long* health) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   int he = list[t];
@@ -578,7 +583,7 @@ __global__ void k_bc_halfedges_df(int n, const int* __restrict__ list, const int
     for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)nd.x * NVARS + j];
     for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)nd.y * NVARS + j];
     if (!apply_bc(k, bct, QL, QR, ba[he], 0.0, nQ)) atomicAdd(&health[H_BADBC], 1ull);
-    for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = QR[j];
+    store_row(q, fq, nd.y, QR);
     return;
   }
   dfl QL[NEQN], QR[NEQN], Qinf[NVARS];
@@ -593,7 +598,7 @@ __global__ void k_bc_halfedges_df(int n, const int* __restrict__ list, const int
   double Q[NVARS];
   for (int j = 0; j < NEQN; j++) Q[j] = to_dbl(QR[j]);
   aux_vars(k.gamma, Q);
-  for (int j = 0; j < NVARS; j++) q[(size_t)nd.y * NVARS + j] = Q[j];
+  store_row(q, fq, nd.y, Q);
 }
 
 // Exact reference order when a no-slip normal node is itself hard-set by a
@@ -1048,22 +1053,20 @@ __global__ void __launch_bounds__(128) k_edge_visc(int nedge, const int2* __rest
   const S h0 = eh[3 * (size_t)e], h1 = eh[3 * (size_t)e + 1], h2 = eh[3 * (size_t)e + 2];
   {
     // face state: plain average of the nodal conservative variables
-    const S half = Sc<S>::c(0.5);
-    S Q0 = (qL[0] + qR[0]) * half, Q1 = (qL[1] + qR[1]) * half, Q2 = (qL[2] + qR[2]) * half,
-      Q3 = (qL[3] + qR[3]) * half, Q4 = (qL[4] + qR[4]) * half;
+    S Q0 = halve(qL[0] + qR[0]), Q1 = halve(qL[1] + qR[1]), Q2 = halve(qL[2] + qR[2]), Q3 = halve(qL[3] + qR[3]),
+      Q4 = halve(qL[4] + qR[4]);
     S iQ0 = Sc<S>::c(1.0) / Q0;
     S u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
-    S P = k.gm1 * (Q4 - half * Q0 * (u * u + v * v + w * w));
+    S P = k.gm1 * (Q4 - halve(Q0) * (u * u + v * v + w * w));
     S T = k.gamma * P * iQ0;
     const S* gL = &grad[(size_t)n.x * NTERMS * 3];
     const S* gR = &grad[(size_t)n.y * NTERMS * 3];
     S g[NTERMS * 3];
 #pragma unroll
-    for (int t = 0; t < NTERMS * 3; t++) g[t] = half * (gL[t] + gR[t]);
+    for (int t = 0; t < NTERMS * 3; t++) g[t] = halve(gL[t] + gR[t]);
     if (kd.ho) {
       // directional correction along the edge (dx = xR - xL = 2 h)
-      const S two = Sc<S>::c(2.0);
-      S d0 = two * h0, d1 = two * h1, d2 = two * h2;
+      S d0 = twice(h0), d1 = twice(h1), d2 = twice(h2);
       S s2 = d0 * d0 + d1 * d1 + d2 * d2;
       S is2 = Sc<S>::c(1.0) / s2;
 #pragma unroll
@@ -1117,12 +1120,11 @@ __global__ void __launch_bounds__(128) k_bedge_flux(int nbedge, const int2* __re
   roe_flux(QL, QR, a.x, a.y, a.z, a.w, k.gamma, k.gm1, k.igamma, k.igm1, f);
   if (kneecap5(f)) atomicAdd(&health[H_KNEECAP], 1ull);
   if (kd.viscous) {
-    const S half = Sc<S>::c(0.5);
-    S Q0 = half * (qL[0] + qR[0]), Q1 = half * (qL[1] + qR[1]), Q2 = half * (qL[2] + qR[2]),
-      Q3 = half * (qL[3] + qR[3]), Q4 = half * (qL[4] + qR[4]);
+    S Q0 = halve(qL[0] + qR[0]), Q1 = halve(qL[1] + qR[1]), Q2 = halve(qL[2] + qR[2]), Q3 = halve(qL[3] + qR[3]),
+      Q4 = halve(qL[4] + qR[4]);
     S iQ0 = Sc<S>::c(1.0) / Q0;
     S u = Q1 * iQ0, v = Q2 * iQ0, w = Q3 * iQ0;
-    S P = k.gm1 * (Q4 - half * Q0 * (u * u + v * v + w * w));
+    S P = k.gm1 * (Q4 - halve(Q0) * (u * u + v * v + w * w));
     S T = k.gamma * P * iQ0;
     S fv[NEQN];
     viscous_flux(u, v, w, T, &grad[(size_t)n.x * NTERMS * 3], a.x, a.y, a.z, a.w * k.inv_retilde, k.Sc_,
@@ -1341,7 +1343,10 @@ void host_qinf(const pcfd_params& p, double* Q) {
 }
 
 int run_bcs(Solver* s, int arith = 0) {
-  s->f_q_valid = 0;
+  // a valid double-float copy of q is updated with the rows the conditions
+  // write (the sequential walk invalidates it instead)
+  dfl* fq = (s->f_q_valid && !s->bc_sequential) ? s->f_q : nullptr;
+  if (!fq) s->f_q_valid = 0;
   BcConst k = make_bc_const(s);
   if (s->bc_sequential) {
     return launch(s, T_BC, [&] {
@@ -1354,10 +1359,10 @@ int run_bcs(Solver* s, int arith = 0) {
     rc = launch(s, T_BC, [&] {
       if (arith)
         k_bc_halfedges_df<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba,
-                                                                      s->d_bbc, k, s->d_q, s->d_health);
+                                                                      s->d_bbc, k, s->d_q, fq, s->d_health);
       else
         k_bc_halfedges<<<nblk(s->nbind, 128), 128, 0, s->stream>>>(s->nbind, s->d_bind, s->d_bn, s->d_ba, s->d_bbc,
-                                                                   s->d_btw, k, s->d_q, s->d_health);
+                                                                   s->d_btw, k, s->d_q, fq, s->d_health);
     });
     if (rc) return rc;
   }
@@ -1376,7 +1381,7 @@ int run_bcs(Solver* s, int arith = 0) {
   return launch(s, T_BC, [&] {
     k_bc_group_nodes<<<nblk(s->nbgroup, 128), 128, 0, s->stream>>>(s->nbgroup, s->d_bgnode, s->d_bgptr, s->d_bghe,
                                                                    s->d_bn, s->d_bbc, s->d_btw, s->d_bnrm, k,
-                                                                   s->d_bgqr, s->d_q);
+                                                                   s->d_bgqr, s->d_q, fq);
   });
 }
 
@@ -1783,9 +1788,10 @@ int run_sgs_f(Solver* s, int nsweeps, const float* b, float* x) {
 }
 
 int run_apply_dq(Solver* s, double* dqnorm) {
-  s->f_q_valid = 0;
+  // a valid double-float copy of q is updated row by row
+  dfl* fq = s->f_q_valid ? s->f_q : nullptr;
   int rc = launch(s, T_UPDATE, [&] {
-    k_apply_dq<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->prm.gamma, s->d_x, s->d_q, s->d_part,
+    k_apply_dq<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->prm.gamma, s->d_x, s->d_q, fq, s->d_part,
                                                            s->d_health);
   });
   if (rc) return rc;
