@@ -206,6 +206,15 @@ PCFD_API int pcfd_coloring(pcfd_solver_t s, int* color_ptr, int* rows);
  * dnorm (|norm change of x over the last sweep|, the reference's return
  * value) optional. */
 PCFD_API int pcfd_sgs(pcfd_solver_t s, int nsweeps, double* x_out, double* dnorm);
+/* CRSMatrix::MatVecMultiply (ucs/crs.tcc:484): y = A x with the assembled
+ * matrix, x and y host arrays [nnode][5].  vec_precision 0 multiplies FP64
+ * vectors (the FGMRES solver of an FP64 system); 1 FP32 vectors (the FP32
+ * Krylov solver, FP32 or BF16 matrix storage only), returned widened. */
+PCFD_API int pcfd_matvec(pcfd_solver_t s, const double* x, double* y, int vec_precision);
+/* CRS::SGS (ucs/crs.tcc:62) with x = 0 and the right-hand side b (host,
+ * [nnode][5]): nsweeps sweeps into x_out.  vec_precision as pcfd_matvec:
+ * 1 runs the FP32 Krylov solver's preconditioner sweep. */
+PCFD_API int pcfd_sgs_rhs(pcfd_solver_t s, int nsweeps, const double* b, double* x_out, int vec_precision);
 /* NaN/Inf zeroing and CompressibleEqnSet::ApplyDQ (ucs/compressible.tcc:929)
  * of x (x_in [nnode][5] if given, else the last linear solution); dqnorm =
  * ParallelL2Norm of x (ucs/solutionSpace.tcc:817). */

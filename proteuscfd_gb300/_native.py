@@ -141,6 +141,8 @@ PROTOTYPES = {
     "pcfd_nblocks": (C.c_longlong, [_P]),
     "pcfd_crs_structure": (C.c_int, [_P, _IP, _IP, _IP]),
     "pcfd_sgs": (C.c_int, [_P, C.c_int, _DP, _DP]),
+    "pcfd_matvec": (C.c_int, [_P, _DP, _DP, C.c_int]),
+    "pcfd_sgs_rhs": (C.c_int, [_P, C.c_int, _DP, _DP, C.c_int]),
     "pcfd_coloring": (C.c_int, [_P, _IP, _IP]),
     "pcfd_apply_dq": (C.c_int, [_P, _DP, _DP]),
     "pcfd_newton_step": (C.c_int, [_P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),

@@ -386,6 +386,23 @@ class SolutionSpace:
         N.check(self._lib.pcfd_sgs(self._h, int(nsweeps), N.dptr(x), C.byref(dn)), "pcfd_sgs")
         return x, dn.value
 
+    def matvec(self, x, fp32=False):
+        """y = A x with the assembled matrix (FP64 vectors, or FP32 vectors
+        through the FP32 Krylov solver's product)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        N.check(self._lib.pcfd_matvec(self._h, N.dptr(x), N.dptr(y), 1 if fp32 else 0), "pcfd_matvec")
+        return y
+
+    def sgs_rhs(self, b, nsweeps, fp32=False):
+        """nsweeps SGS sweeps from x = 0 for the right-hand side b (FP64
+        vectors, or the FP32 Krylov preconditioner's sweep)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        N.check(self._lib.pcfd_sgs_rhs(self._h, int(nsweeps), N.dptr(b), N.dptr(x), 1 if fp32 else 0),
+                "pcfd_sgs_rhs")
+        return x
+
     def apply_dq(self, x=None):
         dn = C.c_double()
         xp = N.dptr(np.ascontiguousarray(x, dtype=np.float64)) if x is not None else None

@@ -30,10 +30,41 @@ __device__ __forceinline__ S entropy_fix(S eig, S eigL, S eigR) {
   return a;
 }
 
+// Primitive quantities of one side of a Roe flux (the per-state part of
+// RoeVariables, Eigensystem and Flux).  A finite-difference Jacobian that
+// perturbs one side reuses the other side's record.
+template <class S>
+struct RoeSide {
+  S r, ir, u, v, w, E, P, h, c, th;
+};
+
+template <class S>
+__device__ __forceinline__ RoeSide<S> roe_side(const S* Q, const S nx, const S ny, const S nz, const S gamma,
+                                               const S gm1) {
+  RoeSide<S> o;
+  o.r = Q[0];
+  o.ir = Sc<S>::c(1.0) / o.r;
+  o.u = Q[1] * o.ir;
+  o.v = Q[2] * o.ir;
+  o.w = Q[3] * o.ir;
+  o.E = Q[4];
+  o.P = gm1 * (o.E - halve(o.r) * (o.u * o.u + o.v * o.v + o.w * o.w));
+  o.h = (o.E + o.P) * o.ir;
+  o.c = sqrt(gamma * o.P * o.ir);
+  o.th = o.u * nx + o.v * ny + o.w * nz;
+  return o;
+}
+
+template <class S>
+__device__ __forceinline__ int roe_core(const RoeSide<S>& L, const RoeSide<S>& R, const S* QL, const S* QR,
+                                        const S nx, const S ny, const S nz, const S area, const S gamma, const S gm1,
+                                        const S igamma, S* flux);
+
 // Roe flux with the reference's eigensystem: RoeVariables (:533),
 // Eigensystem (:580), entropy fix, |A| dQ = T |L| Tinv dQ (evaluated in
-// projector form, below), and 0.5 area (F_L + F_R - |A| dQ) (RoeFlux, :93).  (nx, ny, nz, area) is the
-// edge's unit normal and area; static grid (vdotn = 0).
+// projector form, in roe_core), and 0.5 area (F_L + F_R - |A| dQ)
+// (RoeFlux, :93).  (nx, ny, nz, area) is the edge's unit normal and area;
+// static grid (vdotn = 0).
 // Returns a mask of non-physical states in the sense of BadExtrapolation
 // (ucs/compressible.tcc:1056: p < 1e-10, rho < 0 or rho E < 1e-10):
 // bit 0 = left state, bit 1 = right state, bit 2 = Roe-averaged state.  The
@@ -42,15 +73,17 @@ __device__ __forceinline__ S entropy_fix(S eig, S eigL, S eigR) {
 template <class S>
 __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, const S ny, const S nz, const S area,
                                         const S gamma, const S gm1, const S igamma, const S igm1, S* flux) {
+  return roe_core(roe_side(QL, nx, ny, nz, gamma, gm1), roe_side(QR, nx, ny, nz, gamma, gm1), QL, QR, nx, ny, nz,
+                  area, gamma, gm1, igamma, flux);
+}
+
+template <class S>
+__device__ __forceinline__ int roe_core(const RoeSide<S>& L, const RoeSide<S>& R, const S* QL, const S* QR,
+                                        const S nx, const S ny, const S nz, const S area, const S gamma, const S gm1,
+                                        const S igamma, S* flux) {
   const S one = Sc<S>::c(1.0);
-  const S rL = QL[0], irL = one / rL;
-  const S uL = QL[1] * irL, vL = QL[2] * irL, wL = QL[3] * irL, EL = QL[4];
-  const S PL = gm1 * (EL - halve(rL) * (uL * uL + vL * vL + wL * wL));
-  const S hL = (EL + PL) * irL;
-  const S rR = QR[0], irR = one / rR;
-  const S uR = QR[1] * irR, vR = QR[2] * irR, wR = QR[3] * irR, ER = QR[4];
-  const S PR = gm1 * (ER - halve(rR) * (uR * uR + vR * vR + wR * wR));
-  const S hR = (ER + PR) * irR;
+  const S rL = L.r, uL = L.u, vL = L.v, wL = L.w, EL = L.E, PL = L.P, hL = L.h;
+  const S rR = R.r, uR = R.u, vR = R.v, wR = R.w, ER = R.E, PR = R.P, hR = R.h;
 
   // Roe-averaged state
   const S rho = sqrt(rL * rR);
@@ -68,10 +101,7 @@ __device__ __forceinline__ int roe_flux(const S* QL, const S* QR, const S nx, co
   const S thetaf = u * nx + v * ny + w * nz;
 
   // entropy-fixed |eigenvalues|
-  const S thetaL = uL * nx + vL * ny + wL * nz;
-  const S thetaR = uR * nx + vR * ny + wR * nz;
-  const S cL = sqrt(gamma * PL * irL);
-  const S cR = sqrt(gamma * PR * irR);
+  const S thetaL = L.th, thetaR = R.th, cL = L.c, cR = R.c;
   const S l0 = entropy_fix(thetaf, thetaL, thetaR);
   const S l3 = entropy_fix(thetaf + c, thetaL + cL, thetaR + cR);
   const S l4 = entropy_fix(thetaf - c, thetaL - cL, thetaR - cR);

@@ -127,21 +127,27 @@ __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restr
   for (int t = 0; t < NVARS; t++) { QL[t] = q[(size_t)n.x * NVARS + t]; QR[t] = q[(size_t)n.y * NVARS + t]; }
   const double h = 1.0e-8;
   const double ih = 1.0 / h;
+  const double g = k.gamma, gm1 = k.gamma - 1.0, ig = 1.0 / k.gamma;
+  // each perturbation changes one side; the other side's primitives are reused
+  const RoeSide<double> sL = roe_side(QL, a.x, a.y, a.z, g, gm1), sR = roe_side(QR, a.x, a.y, a.z, g, gm1);
   double fS[NEQN];
-  numflux(QL, QR, a, k.gamma, fS, health);
+  roe_core(sL, sR, QL, QR, a.x, a.y, a.z, a.w, g, gm1, ig, fS);
+  if (kneecap5(fS)) atomicAdd(&health[H_KNEECAP], 1ull);
   double tL[25], tR[25];
   for (int i = 0; i < NEQN; i++) {
     double QP[NEQN], fP[NEQN];
 #pragma unroll
     for (int t = 0; t < NEQN; t++) QP[t] = QL[t];
     QP[i] += h;
-    numflux(QP, QR, a, k.gamma, fP, health);
+    roe_core(roe_side(QP, a.x, a.y, a.z, g, gm1), sR, QP, QR, a.x, a.y, a.z, a.w, g, gm1, ig, fP);
+    if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
     for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = (fS[j] - fP[j]) * ih;
 #pragma unroll
     for (int t = 0; t < NEQN; t++) QP[t] = QR[t];
     QP[i] += h;
-    numflux(QL, QP, a, k.gamma, fP, health);
+    roe_core(sL, roe_side(QP, a.x, a.y, a.z, g, gm1), QL, QP, a.x, a.y, a.z, a.w, g, gm1, ig, fP);
+    if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
     for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = (fP[j] - fS[j]) * ih;
   }
@@ -194,10 +200,12 @@ __global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __re
     QR[t] = to_df(q[(size_t)n.y * NVARS + t]);
   }
   const dfl nx = to_df(a.x), ny = to_df(a.y), nz = to_df(a.z), ar = to_df(a.w);
-  const dfl g = to_df(k.gamma), gm1 = to_df(k.gamma - 1.0), ig = to_df(1.0 / k.gamma), igm1 = to_df(1.0 / (k.gamma - 1.0));
+  const dfl g = to_df(k.gamma), gm1 = to_df(k.gamma - 1.0), ig = to_df(1.0 / k.gamma);
   const dfl h = to_df(1.0e-8);
+  // each perturbation changes one side; the other side's primitives are reused
+  const RoeSide<dfl> sL = roe_side(QL, nx, ny, nz, g, gm1), sR = roe_side(QR, nx, ny, nz, g, gm1);
   dfl fS[NEQN];
-  roe_flux<dfl>(QL, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fS);
+  roe_core(sL, sR, QL, QR, nx, ny, nz, ar, g, gm1, ig, fS);
   if (kneecap5(fS)) atomicAdd(&health[H_KNEECAP], 1ull);
   VR tL[25], tR[25];
   for (int i = 0; i < NEQN; i++) {
@@ -205,14 +213,14 @@ __global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __re
 #pragma unroll
     for (int t = 0; t < NEQN; t++) QP[t] = QL[t];
     QP[i] = QP[i] + h;
-    roe_flux<dfl>(QP, QR, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
+    roe_core(roe_side(QP, nx, ny, nz, g, gm1), sR, QP, QR, nx, ny, nz, ar, g, gm1, ig, fP);
     if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
     for (int j = 0; j < NEQN; j++) tL[j * 5 + i] = df_quot(fS[j] - fP[j], VR(0));
 #pragma unroll
     for (int t = 0; t < NEQN; t++) QP[t] = QR[t];
     QP[i] = QP[i] + h;
-    roe_flux<dfl>(QL, QP, nx, ny, nz, ar, g, gm1, ig, igm1, fP);
+    roe_core(sL, roe_side(QP, nx, ny, nz, g, gm1), QL, QP, nx, ny, nz, ar, g, gm1, ig, fP);
     if (kneecap5(fP)) atomicAdd(&health[H_KNEECAP], 1ull);
 #pragma unroll
     for (int j = 0; j < NEQN; j++) tR[j * 5 + i] = df_quot(fP[j] - fS[j], VR(0));
@@ -579,7 +587,15 @@ struct RowBatch {
   static constexpr int n = sizeof(typename OffAcc<T>::type) == 8 ? 8 : 16;
 };
 
-template <class T>
+// x gathers: through L1, or (CG) from L2 for kernels in which other blocks
+// write x between reads (L1 is not coherent across SMs within a launch)
+template <bool CG, class A>
+__device__ __forceinline__ A ldx(const A* p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+
+template <class T, bool CG = false>
 __device__ __forceinline__ void row_issue(int b0, int nb, int jl, int lane, const T* __restrict__ M,
                                           const typename OffAcc<T>::type* __restrict__ xa,
                                           typename OffAcc<T>::type (&av)[RowBatch<T>::n],
@@ -593,11 +609,11 @@ __device__ __forceinline__ void row_issue(int b0, int nb, int jl, int lane, cons
     const int j = __shfl_sync(0xffffffffu, jl, u);
     const bool ok = active && u < nb;
     av[u] = ok ? off_val(M[(size_t)(b0 + u) * 25 + lane]) : A(0);
-    xv[u] = ok ? xa[(size_t)j * 5 + c] : A(0);
+    xv[u] = ok ? ldx<CG>(&xa[(size_t)j * 5 + c]) : A(0);
   }
 }
 
-template <class T>
+template <class T, bool CG = false>
 __device__ __forceinline__ typename OffAcc<T>::type row_finish(int b0, int nb, int jl, int lane,
                                                                const int* __restrict__ ja, const T* __restrict__ M,
                                                                const typename OffAcc<T>::type* __restrict__ xa,
@@ -613,7 +629,7 @@ __device__ __forceinline__ typename OffAcc<T>::type row_finish(int b0, int nb, i
   const bool active = lane < 25;
   for (int k = kRowBatch; k < nb; k++) {
     const int j = k < 32 ? __shfl_sync(0xffffffffu, jl, k & 31) : ja[b0 + k];
-    if (active) acc = fma(off_val(M[(size_t)(b0 + k) * 25 + lane]), xa[(size_t)j * 5 + c], acc);
+    if (active) acc = fma(off_val(M[(size_t)(b0 + k) * 25 + lane]), ldx<CG>(&xa[(size_t)j * 5 + c]), acc);
   }
   return sum5(acc);
 }
@@ -641,52 +657,115 @@ __global__ void k_to_f32(long long n, const double* __restrict__ x, float* __res
 // One colour of a block Gauss-Seidel sweep (CRS::SGS, ucs/crs.tcc:62):
 // warps stride over the colour's rows; for each, rhs = b_i - sum_j A_ij x_j
 // over the off-diagonal blocks, then x_i = D_i^-1 rhs as a 25-lane product
-// with the stored inverse.  While a row's coefficients are in flight the warp
-// already loads the next row's id, block range and column indices, so a row
-// costs about one memory latency instead of four.  K is the vector type
+// with the stored inverse.  desc holds each row's (id, first off-diagonal
+// block, block count) in colour order, read two rows ahead; while a row's
+// coefficients are in flight the warp already loads the next row's column
+// indices, so a row costs about one memory latency.  K is the vector type
 // (FP64, or FP32 inside the FP32 Krylov solver); xa is x in the products'
 // accumulation type (x itself, or its FP32 copy, which the sweep keeps
-// current).  Rows of one colour share no block, so no row reads an x this
-// launch writes.
-template <class T, class K>
-__global__ void __launch_bounds__(256, 3) k_sgs_color(int nrows, const int* __restrict__ rows,
-                                                      const int* __restrict__ ia, const int* __restrict__ ja,
-                                                      const T* __restrict__ M, const K* __restrict__ dinv,
-                                                      const K* __restrict__ b, K* __restrict__ x,
-                                                      typename OffAcc<T>::type* __restrict__ xa) {
+// current).  Rows of one colour share no block, so no row reads an x written
+// in the same colour.  g is the warp's first row, W the number of warps.
+template <class T, class K, bool CG>
+__device__ __forceinline__ void sgs_rows(int nrows, const int4* __restrict__ desc, const int* __restrict__ ja,
+                                         const T* __restrict__ M,
+                                         const K* __restrict__ dinv, const K* __restrict__ b, K* x,
+                                         typename OffAcc<T>::type* xa, int g, const int W) {
   typedef typename OffAcc<T>::type A;
   const int lane = threadIdx.x & 31;
-  const int W = gridDim.x * 8;
-  int g = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (g >= nrows) return;
-  int i = rows[g];
-  int b0, nb, jl;
-  row_meta(ia, ja, i, lane, b0, nb, jl);
-  int in = g + W < nrows ? rows[g + W] : -1;
+  const int4 none = make_int4(-1, 0, 0, 0);
+  int4 d = desc[g];
+  int i = d.x, b0 = d.y, nb = d.z;
+  int jl = lane < nb ? ja[b0 + lane] : 0;
+  int4 dn = g + W < nrows ? desc[g + W] : none;
   const int r = lane / 5, c = lane % 5;
   while (true) {
     A av[RowBatch<T>::n], xv[RowBatch<T>::n];
-    row_issue<T>(b0, nb, jl, lane, M, xa, av, xv);
-    const int inn = g + 2 * W < nrows ? rows[g + 2 * W] : -1;
-    int b0n = 0, nbn = 0, jln = 0;
-    if (in >= 0) row_meta(ia, ja, in, lane, b0n, nbn, jln);
-    const K s = (K)row_finish<T>(b0, nb, jl, lane, ja, M, xa, av, xv);
+    row_issue<T, CG>(b0, nb, jl, lane, M, xa, av, xv);
+    // the row's right-hand side and inverse diagonal block travel with its
+    // coefficients instead of after the sum
+    const K bi = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] : K(0);
+    const K di = lane < 25 ? dinv[(size_t)i * 25 + lane] : K(0);
+    const int4 dnn = g + 2 * W < nrows ? desc[g + 2 * W] : none;
+    const int jln = (dn.x >= 0 && lane < dn.z) ? ja[dn.y + lane] : 0;
+    const K s = (K)row_finish<T, CG>(b0, nb, jl, lane, ja, M, xa, av, xv);
     // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
-    const K rhs = (lane < 25 && c == 0) ? b[(size_t)i * 5 + r] - s : K(0);
+    const K rhs = (lane < 25 && c == 0) ? bi - s : K(0);
     const K rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
-    K v = lane < 25 ? dinv[(size_t)i * 25 + lane] * rc : K(0);
+    K v = di * rc;
     v = sum5(v);
     if (lane < 25 && c == 0) {
       x[(size_t)i * 5 + r] = v;
       if ((const void*)xa != (const void*)x) xa[(size_t)i * 5 + r] = (A)v;
     }
-    if (in < 0) break;
+    if (dn.x < 0) break;
     g += W;
-    i = in;
-    in = inn;
-    b0 = b0n;
-    nb = nbn;
+    i = dn.x;
+    b0 = dn.y;
+    nb = dn.z;
     jl = jln;
+    dn = dnn;
+  }
+}
+
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident): a
+// counter and a generation word.  The wait is bounded; on time-out the
+// block sets *err and the caller returns.
+constexpr long long kBarrierSpins = 1LL << 22;
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* __restrict__ bar, unsigned int nblocks,
+                                             int* __restrict__ err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g0 = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g0) {
+        if (++spins > kBarrierSpins) {
+          atomicExch(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// nsweeps symmetric sweeps (all colours forward, then backward) in one
+// cooperative launch: the colours are separated by grid barriers instead of
+// kernel boundaries, and x is gathered from L2.  Each row's arithmetic does
+// not depend on which warp takes it, so the result is that of per-colour
+// launches.
+template <class T, class K>
+__global__ void __launch_bounds__(256, 3) k_sgs_sweep(int ncolor, const int* __restrict__ cptr,
+                                                      const int4* __restrict__ desc, const int* __restrict__ ja,
+                                                      const T* __restrict__ M,
+                                                      const K* __restrict__ dinv, const K* __restrict__ b,
+                                                      K* x, typename OffAcc<T>::type* xa,
+                                                      int nsweeps, unsigned int* __restrict__ bar,
+                                                      int* __restrict__ err) {
+  const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
+  const int nphase = nsweeps * 2 * ncolor;
+  for (int p = 0; p < nphase; p++) {
+    const int cc = p % ncolor, dir = (p / ncolor) & 1;
+    const int c = dir == 0 ? cc : ncolor - 1 - cc;
+    const int r0 = cptr[c], nr = cptr[c + 1] - r0;
+    sgs_rows<T, K, true>(nr, desc + r0, ja, M, dinv, b, x, xa, g, W);
+    if (p + 1 < nphase && !grid_barrier(bar, gridDim.x, err)) return;
   }
 }
 
@@ -703,23 +782,265 @@ __global__ void __launch_bounds__(256, 3) k_spmv(int nnode, const int* __restric
   const int W = gridDim.x * 8;
   int i = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= nnode) return;
+  // row pointers are read two rows ahead, column indices one row ahead
   int b0, nb, jl;
   row_meta(ia, ja, i, lane, b0, nb, jl);
+  int i1 = i + W, b01 = 0, nb1 = 0;
+  if (i1 < nnode) {
+    b01 = ia[i1] + 1;
+    nb1 = ia[i1 + 1] - b01;
+  }
   while (true) {
     A av[RowBatch<T>::n], xv[RowBatch<T>::n];
     row_issue<T>(b0, nb, jl, lane, M, xa, av, xv);
     K d = lane < 25 ? diag[(size_t)i * 25 + lane] * x[(size_t)i * 5 + lane % 5] : K(0);
-    const int in = i + W;
-    int b0n = 0, nbn = 0, jln = 0;
-    if (in < nnode) row_meta(ia, ja, in, lane, b0n, nbn, jln);
+    const int i2 = i1 + W;
+    int b02 = 0, nb2 = 0;
+    if (i2 < nnode) {
+      b02 = ia[i2] + 1;
+      nb2 = ia[i2 + 1] - b02;
+    }
+    const int jl1 = (i1 < nnode && lane < nb1) ? ja[b01 + lane] : 0;
     const K s = (K)row_finish<T>(b0, nb, jl, lane, ja, M, xa, av, xv);
     d = sum5(d);
     if (lane < 25 && lane % 5 == 0) y[(size_t)i * 5 + lane / 5] = s + d;
-    if (in >= nnode) break;
-    i = in;
-    b0 = b0n;
-    nb = nbn;
-    jl = jln;
+    if (i1 >= nnode) break;
+    i = i1;
+    b0 = b01;
+    nb = nb1;
+    jl = jl1;
+    i1 = i2;
+    b01 = b02;
+    nb1 = nb2;
+  }
+}
+
+// ---- asynchronous-copy row pipeline (FP32 blocks and vectors) ------------
+// A warp streams its rows through a ring of kRowStages shared-memory stages
+// filled by 16-byte cp.async.cg copies (L2 only): the row's contiguous
+// off-diagonal blocks (one aligned window) and, per block, the aligned
+// 32-byte window holding the 5 entries of x it multiplies.  The data of the
+// next rows are in flight while the current row is summed, without holding
+// registers, so a warp keeps several rows' loads outstanding.  Every copy
+// stays inside its array: the allocations carry 16 bytes of tail padding.
+constexpr int kRowStages = 3;
+constexpr int kStageBlocks = 16;  // blocks staged per row; further blocks are read directly
+
+struct RowStage {
+  float m[kStageBlocks * 25 + 4];  // window of the row's blocks
+  float x[kStageBlocks * 8];       // per block: a 32-byte window holding its 5 x entries
+  float dinv[28];                  // window of the row's inverse diagonal block (sweeps)
+  float b[8];                      // window of the row's right-hand side (sweeps)
+};
+static_assert(sizeof(RowStage) % 16 == 0, "stage size");
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// start the copies of row (b0, nb, jl) into stage st, and with dinv the
+// windows of row i's inverse diagonal block and right-hand side; always
+// commits a group
+__device__ __forceinline__ void row_stage_issue(bool valid, int b0, int nb, int jl, int lane,
+                                                const float* __restrict__ M, const float* xa, RowStage* st,
+                                                int i = 0, const float* __restrict__ dinv = nullptr,
+                                                const float* __restrict__ b = nullptr) {
+  const int ns = min(nb, kStageBlocks);
+  const int jb = __shfl_sync(0xffffffffu, jl, lane >> 1);
+  if (valid) {
+    const uintptr_t g0 = reinterpret_cast<uintptr_t>(M + (size_t)b0 * 25);
+    const uintptr_t a0 = g0 & ~(uintptr_t)15;
+    const int n16 = (int)((g0 - a0 + (uintptr_t)ns * 100 + 15) >> 4);
+    const uint32_t sm = umma::smem_addr(st->m);
+    for (int c = lane; c < n16; c += 32) cp_async16(sm + 16 * c, reinterpret_cast<const void*>(a0 + 16 * (uintptr_t)c));
+    const int u = lane >> 1;
+    if (u < ns) {
+      const uintptr_t xw = reinterpret_cast<uintptr_t>(xa + (size_t)jb * 5) & ~(uintptr_t)15;
+      cp_async16(umma::smem_addr(st->x) + 32 * u + 16 * (lane & 1), reinterpret_cast<const void*>(xw + 16 * (lane & 1)));
+    }
+    if (dinv) {
+      // 7 chunks cover the 100-byte block from its aligned start, 2 the 20-byte b entries
+      if (lane < 7) {
+        const uintptr_t dw = reinterpret_cast<uintptr_t>(dinv + (size_t)i * 25) & ~(uintptr_t)15;
+        cp_async16(umma::smem_addr(st->dinv) + 16 * lane, reinterpret_cast<const void*>(dw + 16 * lane));
+      } else if (lane < 9) {
+        const uintptr_t bw = reinterpret_cast<uintptr_t>(b + (size_t)i * 5) & ~(uintptr_t)15;
+        cp_async16(umma::smem_addr(st->b) + 16 * (lane - 7), reinterpret_cast<const void*>(bw + 16 * (lane - 7)));
+      }
+    }
+  }
+  cp_async_commit();
+}
+
+// off-diagonal sum of a staged row; lane 5r receives row r's sum
+__device__ __forceinline__ float row_stage_sum(int b0, int nb, int jl, int lane, const RowStage* st,
+                                               const int* __restrict__ ja, const float* __restrict__ M,
+                                               const float* xa) {
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  const int ns = min(nb, kStageBlocks);
+  const int mo = (int)((reinterpret_cast<uintptr_t>(M + (size_t)b0 * 25) & 15) >> 2);
+  float acc = 0.f;
+#pragma unroll
+  for (int u = 0; u < kStageBlocks; u++) {
+    if (u >= ns) break;
+    const int j = __shfl_sync(0xffffffffu, jl, u);
+    const int xo = (int)((reinterpret_cast<uintptr_t>(xa + (size_t)j * 5) & 15) >> 2);
+    if (active) acc = fmaf(st->m[mo + u * 25 + lane], st->x[u * 8 + xo + c], acc);
+  }
+  for (int k = kStageBlocks; k < nb; k++) {
+    const int j = k < 32 ? __shfl_sync(0xffffffffu, jl, k & 31) : ja[b0 + k];
+    if (active) acc = fmaf(M[(size_t)(b0 + k) * 25 + lane], __ldcg(&xa[(size_t)j * 5 + c]), acc);
+  }
+  return sum5(acc);
+}
+
+// y = A x with FP32 blocks and vectors through the staged pipeline: warps
+// stride over rows, each row's copies issued two rows before its sum, its
+// row pointers and column indices one row before that.
+__global__ void __launch_bounds__(256, 4) k_spmv_staged(int nnode, const int* __restrict__ ia,
+                                                        const int* __restrict__ ja, const float* __restrict__ M,
+                                                        const float* __restrict__ diag, const float* __restrict__ x,
+                                                        float* __restrict__ y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  RowStage* st = reinterpret_cast<RowStage*>(smem_raw) + wid * kRowStages;
+  const int W = gridDim.x * 8;
+  int iA = blockIdx.x * 8 + wid;
+  if (iA >= nnode) return;
+  // rows A (summed this iteration), B (in flight), C (issued this
+  // iteration), N (next; its bounds and column indices are read ahead)
+  auto bounds = [&](int i, int& b0, int& nb) {
+    if (i < nnode) {
+      b0 = ia[i] + 1;
+      nb = ia[i + 1] - b0;
+    } else {
+      b0 = 0;
+      nb = 0;
+    }
+  };
+  auto cols = [&](int i, int b0, int nb) { return (i < nnode && lane < nb) ? ja[b0 + lane] : 0; };
+  int bA, nA, bB, nB, bC, nC, bN, nN;
+  bounds(iA, bA, nA);
+  int jA = cols(iA, bA, nA);
+  int iB = iA + W;
+  bounds(iB, bB, nB);
+  int jB = cols(iB, bB, nB);
+  row_stage_issue(true, bA, nA, jA, lane, M, x, &st[0]);
+  row_stage_issue(iB < nnode, bB, nB, jB, lane, M, x, &st[1]);
+  int iC = iB + W;
+  bounds(iC, bC, nC);
+  int jC = cols(iC, bC, nC);
+  int iN = iC + W;
+  bounds(iN, bN, nN);
+  int sA = 0, sB = 1, sC = 2;
+  while (true) {
+    row_stage_issue(iC < nnode, bC, nC, jC, lane, M, x, &st[sC]);
+    const int jN = cols(iN, bN, nN);
+    const int iNN = iN + W;
+    int bNN, nNN;
+    bounds(iNN, bNN, nNN);
+    const float d = lane < 25 ? diag[(size_t)iA * 25 + lane] * x[(size_t)iA * 5 + lane % 5] : 0.f;
+    cp_async_wait<2>();
+    __syncwarp();
+    const float sum = row_stage_sum(bA, nA, jA, lane, &st[sA], ja, M, x);
+    const float dd = sum5(d);
+    if (lane < 25 && lane % 5 == 0) y[(size_t)iA * 5 + lane / 5] = sum + dd;
+    __syncwarp();
+    if (iB >= nnode) break;
+    iA = iB; bA = bB; nA = nB; jA = jB;
+    iB = iC; bB = bC; nB = nC; jB = jC;
+    iC = iN; bC = bN; nC = nN; jC = jN;
+    iN = iNN; bN = bNN; nN = nNN;
+    const int t = sA;
+    sA = sB;
+    sB = sC;
+    sC = t;
+  }
+  cp_async_wait<0>();
+}
+
+// The rows of one colour of an FP32 sweep through the staged pipeline
+// (sgs_rows' arithmetic on staged data): desc gives the rows in colour order,
+// g the warp's first row, W the number of warps.  Drains its copies before
+// returning.
+__device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restrict__ desc, const int* __restrict__ ja,
+                                                const float* __restrict__ M, const float* __restrict__ dinv,
+                                                const float* __restrict__ b, float* x, int g, const int W,
+                                                RowStage* st) {
+  const int lane = threadIdx.x & 31;
+  if (g >= nrows) return;
+  const int r = lane / 5, c = lane % 5;
+  const int4 none = make_int4(-1, 0, 0, 0);
+  auto cols = [&](const int4& d) { return (d.x >= 0 && lane < d.z) ? ja[d.y + lane] : 0; };
+  int4 dA = desc[g];
+  int jA = cols(dA);
+  int4 dB = g + W < nrows ? desc[g + W] : none;
+  int jB = cols(dB);
+  row_stage_issue(true, dA.y, dA.z, jA, lane, M, x, &st[0], dA.x, dinv, b);
+  row_stage_issue(dB.x >= 0, dB.y, dB.z, jB, lane, M, x, &st[1], dB.x, dinv, b);
+  int gC = g + 2 * W;
+  int4 dC = gC < nrows ? desc[gC] : none;
+  int jC = cols(dC);
+  int4 dN = gC + W < nrows ? desc[gC + W] : none;
+  int sA = 0, sB = 1, sC = 2;
+  while (true) {
+    row_stage_issue(dC.x >= 0, dC.y, dC.z, jC, lane, M, x, &st[sC], dC.x, dinv, b);
+    const int jN = cols(dN);
+    const int gNN = gC + 2 * W;
+    const int4 dNN = gNN < nrows ? desc[gNN] : none;
+    cp_async_wait<2>();
+    __syncwarp();
+    const RowStage* sa = &st[sA];
+    const float s = row_stage_sum(dA.y, dA.z, jA, lane, sa, ja, M, x);
+    const int i = dA.x;
+    const int bo = (int)((reinterpret_cast<uintptr_t>(b + (size_t)i * 5) & 15) >> 2);
+    const int dof = (int)((reinterpret_cast<uintptr_t>(dinv + (size_t)i * 25) & 15) >> 2);
+    // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
+    const float rhs = (lane < 25 && c == 0) ? sa->b[bo + r] - s : 0.f;
+    const float rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
+    float v = lane < 25 ? sa->dinv[dof + lane] * rc : 0.f;
+    v = sum5(v);
+    if (lane < 25 && c == 0) x[(size_t)i * 5 + r] = v;
+    __syncwarp();
+    if (dB.x < 0) break;
+    dA = dB; jA = jB;
+    dB = dC; jB = jC;
+    dC = dN; jC = jN;
+    dN = dNN;
+    gC += W;
+    const int t = sA;
+    sA = sB;
+    sB = sC;
+    sC = t;
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+}
+
+// nsweeps FP32 sweeps in one cooperative launch through the staged pipeline
+// (k_sgs_sweep's phases and barriers).
+__global__ void __launch_bounds__(256, 4) k_sgs_sweep_staged(int ncolor, const int* __restrict__ cptr,
+                                                             const int4* __restrict__ desc,
+                                                             const int* __restrict__ ja, const float* __restrict__ M,
+                                                             const float* __restrict__ dinv,
+                                                             const float* __restrict__ b, float* x, int nsweeps,
+                                                             unsigned int* __restrict__ bar, int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RowStage* st = reinterpret_cast<RowStage*>(smem_raw) + (threadIdx.x >> 5) * kRowStages;
+  const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
+  const int nphase = nsweeps * 2 * ncolor;
+  for (int p = 0; p < nphase; p++) {
+    const int cc = p % ncolor, dir = (p / ncolor) & 1;
+    const int c = dir == 0 ? cc : ncolor - 1 - cc;
+    const int r0 = cptr[c], nr = cptr[c + 1] - r0;
+    sgs_rows_staged(nr, desc + r0, ja, M, dinv, b, x, g, W, st);
+    if (p + 1 < nphase && !grid_barrier(bar, gridDim.x, err)) return;
   }
 }
 
@@ -883,10 +1204,11 @@ __global__ void k_min_final(int nblocks, const double* __restrict__ part, double
 template <class K>
 __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, const K* __restrict__ V,
                                                         const K* __restrict__ w, double* __restrict__ part,
-                                                        int part_stride, unsigned int* __restrict__ done,
+                                                        unsigned int* __restrict__ done,
                                                         double* __restrict__ out, float* __restrict__ outf) {
   // eight vectors per pass over w: w is read nv/8 times, each V_k once;
-  // per-thread sums in the vector type, block sums in FP64
+  // per-thread sums in the vector type, block sums in FP64, stored dot-major
+  // ([k][block]) for the final sums
   __shared__ double red[kNormThreads / 32][8];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -911,7 +1233,7 @@ __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, cons
     if (threadIdx.x < nk) {
       double sacc = 0.0;
       for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q][threadIdx.x];
-      part[(size_t)blockIdx.x * part_stride + k0 + threadIdx.x] = sacc;
+      part[(size_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = sacc;
     }
     __syncthreads();
   }
@@ -923,7 +1245,7 @@ __global__ void __launch_bounds__(kNormThreads) k_mdot(long long n, int nv, cons
   if (last) {
     __threadfence();
     for (int k = wid; k < nv; k += kNormThreads / 32) {
-      const double sum = warp_col_sum(part, (int)gridDim.x, part_stride, k, lane);
+      const double sum = warp_col_sum(part + (size_t)k * gridDim.x, (int)gridDim.x, 1, 0, lane);
       if (lane == 0) {
         out[k] = sum;
         outf[k] = (float)sum;
@@ -941,6 +1263,100 @@ __global__ void k_orth_update(long long n, int nv, const K* __restrict__ V, cons
     K v = w[i];
     for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
     w[i] = v;
+  }
+}
+
+// w -= sum_k h[k] V_k (the first Gram-Schmidt pass), then dots[k] =
+// (w, V_k) of the result (the second pass's coefficients), nv <= 32, in one
+// pass over V: the update as in k_orth_update, the dot products with the
+// per-thread, per-block and final summation orders of k_mdot.  Partials are
+// stored dot-major ([k][block]).
+template <class K>
+__global__ void __launch_bounds__(kNormThreads) k_orth_mdot(long long n, int nv, const K* __restrict__ V,
+                                                             const K* __restrict__ h, K* __restrict__ w,
+                                                             double* __restrict__ part,
+                                                             unsigned int* __restrict__ done,
+                                                             double* __restrict__ out, float* __restrict__ outf) {
+  __shared__ double red[kNormThreads / 32][32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  K acc[32];
+#pragma unroll
+  for (int u = 0; u < 32; u++) acc[u] = K(0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    K v = w[i];
+    for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
+    w[i] = v;
+#pragma unroll
+    for (int u = 0; u < 32; u++)
+      if (u < nv) acc[u] = fma(v, V[(size_t)u * n + i], acc[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < 32; u++) {
+    if (u >= nv) break;
+    K a = acc[u];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) red[wid][u] = (double)a;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double sacc = 0.0;
+    for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q][threadIdx.x];
+    part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sacc;
+  }
+  __threadfence();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int k = wid; k < nv; k += kNormThreads / 32) {
+      const double sum = warp_col_sum(part + (size_t)k * gridDim.x, (int)gridDim.x, 1, 0, lane);
+      if (lane == 0) {
+        out[k] = sum;
+        outf[k] = (float)sum;
+      }
+    }
+    if (threadIdx.x == 0) *done = 0u;
+  }
+}
+
+// w -= sum_k h[k] V_k (the second Gram-Schmidt pass) with (w, w) of the
+// result: per-thread sums in the vector type and FP64 block sums as in
+// k_mdot, the last block writing the total to out[0]
+template <class K>
+__global__ void __launch_bounds__(kNormThreads) k_orth_norm(long long n, int nv, const K* __restrict__ V,
+                                                             const K* __restrict__ h, K* __restrict__ w,
+                                                             double* __restrict__ part,
+                                                             unsigned int* __restrict__ done,
+                                                             double* __restrict__ out) {
+  __shared__ double red[kNormThreads / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  K acc = K(0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    K v = w[i];
+    for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
+    w[i] = v;
+    acc = fma(v, v, acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[wid] = (double)acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int q = 0; q < kNormThreads / 32; q++) sacc += red[q];
+    part[blockIdx.x] = sacc;
+  }
+  __threadfence();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    if (wid == 0) {
+      const double sum = warp_col_sum(part, (int)gridDim.x, 1, 0, lane);
+      if (lane == 0) out[0] = sum;
+    }
+    if (threadIdx.x == 0) *done = 0u;
   }
 }
 

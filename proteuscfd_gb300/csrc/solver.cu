@@ -168,6 +168,7 @@ struct Solver {
   float* d_diagf = nullptr;     // [nnode][25] FP32 copies of diag and dinv (FP32 Krylov solver)
   float* d_dinvf = nullptr;
   double* d_wd = nullptr;       // [nnode][5] FP64 scratch of the Krylov solver
+  double* d_mv = nullptr;       // pcfd_matvec / pcfd_sgs_rhs scratch (two FP64 vectors, two padded FP32)
   float* d_dotsf = nullptr;     // FP32 copies of the Krylov dot results
   unsigned int* d_mdot_done = nullptr;  // blocks finished in k_mdot (re-armed by its last block)
   int* d_piv = nullptr;         // [nnode][5]
@@ -180,12 +181,17 @@ struct Solver {
   int ncolor = 0;
   std::vector<int> color_ptr;   // [ncolor+1] into d_color_rows
   int* d_color_rows = nullptr;  // [nnode]
+  int* d_cptr = nullptr;        // [ncolor+1] colour pointers on the device
+  int4* d_rowdesc = nullptr;    // [nnode] (row, first off-diagonal block, block count) in colour order
+  unsigned int* d_gbar = nullptr;  // grid barrier of the SGS sweep kernel (count, generation)
+  int* d_sgs_err = nullptr;     // set when a sweep's grid barrier timed out
+  int nsm = 0;                  // multiprocessors of the device
   // FGMRES work space (allocated on first use)
   int fg_m = 0;
   double* d_V = nullptr;        // [m+1][nnode*5]
   double* d_Z = nullptr;        // [m][nnode*5]
   double* d_w = nullptr;        // [nnode*5]
-  double* d_dots = nullptr;     // [kNormBlocks][m+2] partial dot products
+  double* d_dots = nullptr;     // [kKrylovBlocks][m+2] partial dot products
 
   // profiling
   int profile = 0;
@@ -199,6 +205,10 @@ struct Solver {
 };
 
 constexpr int kNormBlocks = 304;  // 2 x 152 SMs
+// Krylov vector kernels (dot products, orthogonalisation, scaling, the
+// solution update) stream several vectors per element: 8 blocks of 256
+// threads per SM keep enough loads in flight
+constexpr int kKrylovBlocks = 8 * 152;
 constexpr int kNormThreads = 256;
 
 template <class F>
@@ -1211,6 +1221,7 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
 // other blocks of the same launch in k_mdot).
 __device__ __forceinline__ double warp_col_sum(const double* part, int nb, int st, int k, int lane) {
   double v = 0.0;
+#pragma unroll 8
   for (int b = lane; b < nb; b += 32) v += __ldcg(&part[(size_t)b * st + k]);
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -1268,7 +1279,7 @@ void free_solver(Solver* s) {
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
-                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_mdot_done, s->d_scal, s->d_color_rows, s->d_V, s->d_Z, s->d_w, s->d_dots,
+                  s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_mdot_done, s->d_scal, s->d_color_rows, s->d_cptr, s->d_rowdesc, s->d_mv, s->d_gbar, s->d_sgs_err, s->d_V, s->d_Z, s->d_w, s->d_dots,
                   s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1586,10 +1597,11 @@ int ensure_matrix(Solver* s, int prec) {
   if (!s->d_xf) {
     int rc = dalloc(&s->d_xf, (size_t)s->nnode * NEQN);
     if (!rc) rc = dalloc(&s->d_diagf, (size_t)s->nnode * 25);
-    if (!rc) rc = dalloc(&s->d_dinvf, (size_t)s->nnode * 25);
+    if (!rc) rc = dalloc(&s->d_dinvf, (size_t)s->nnode * 25 + 4);  // tail padding for staged windows
     if (rc) return rc;
   }
-  size_t bytes = (size_t)s->nblocks * 25 * prec_bytes(prec);
+  // 16 bytes of tail padding for the aligned windows of the staged row kernels
+  size_t bytes = (size_t)s->nblocks * 25 * prec_bytes(prec) + 16;
   cudaError_t e = cudaMalloc(&s->d_M, bytes);
   if (e != cudaSuccess) return set_err(PCFD_ERR_NOMEM, std::string("matrix: ") + cudaGetErrorString(e));
   CUDA_TRY(cudaMemsetAsync(s->d_M, 0, bytes, s->stream));
@@ -1710,9 +1722,45 @@ int run_sumsq(Solver* s, const double* v, long long n, double* out_dev) {
 // order; here rows of one colour (no two adjacent) update together and the
 // colours are swept forward then backward, the GPU form of the same
 // smoother.  Returns |norm(x_last) - norm(x_previous)| as the reference does.
+// nsweeps symmetric block-SGS sweeps (CRS::SGS, ucs/crs.tcc:62) as one
+// cooperative launch of k_sgs_sweep: as many blocks as can be resident (at
+// most three per multiprocessor), none beyond what the largest colour needs.
+template <class T, class K>
+int run_sweeps(Solver* s, int nsweeps, const K* dinv, const K* b, K* x, typename OffAcc<T>::type* xa) {
+  if (nsweeps <= 0) return PCFD_OK;
+  auto kern = k_sgs_sweep<T, K>;
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+  if (per_sm < 1) return set_err(PCFD_ERR_CUDA, "sgs: sweep kernel cannot be resident");
+  int maxrows = 1;
+  for (int c = 0; c < s->ncolor; c++) maxrows = std::max(maxrows, s->color_ptr[c + 1] - s->color_ptr[c]);
+  int grid = std::max(1, std::min(std::min(per_sm, 3) * s->nsm, nblk(maxrows, 8)));
+  const T* M = (const T*)s->d_M;
+  int ncolor = s->ncolor;
+  void* args[] = {&ncolor, &s->d_cptr, &s->d_rowdesc, &s->d_ja, &M,         &dinv,         &b,
+                  &x,      &xa,        &nsweeps,       &s->d_gbar, &s->d_sgs_err};
+  cudaError_t ce = cudaSuccess;
+  int rc = launch(s, T_SGS, [&] { ce = cudaLaunchCooperativeKernel((void*)kern, grid, 256, args, 0, s->stream); });
+  if (rc) return rc;
+  if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("sgs sweep launch: ") + cudaGetErrorString(ce));
+  return PCFD_OK;
+}
+
+// a timed-out grid barrier in an earlier sweep (read at the call's
+// synchronisation point)
+int check_sweeps(Solver* s) {
+  int e = 0;
+  CUDA_TRY(cudaMemcpy(&e, s->d_sgs_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    CUDA_TRY(cudaMemset(s->d_sgs_err, 0, sizeof(int)));
+    CUDA_TRY(cudaMemset(s->d_gbar, 0, 2 * sizeof(unsigned int)));
+    return set_err(PCFD_ERR_CUDA, "sgs: a sweep's grid barrier timed out");
+  }
+  return PCFD_OK;
+}
+
 template <class T>
 int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
-  const T* M = (const T*)s->d_M;
   const double cnt = (double)s->nnode * NEQN;
   double prev = 0.0, cur = 0.0;
   typedef typename OffAcc<T>::type A;
@@ -1724,30 +1772,27 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
     if (rc) return rc;
     xa = (A*)s->d_xf;
   }
-  for (int sw = 0; sw < nsweeps; sw++) {
-    for (int dir = 0; dir < 2; dir++) {
-      for (int cc = 0; cc < s->ncolor; cc++) {
-        int c = dir == 0 ? cc : s->ncolor - 1 - cc;
-        int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
-        if (nr == 0) continue;
-        int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T, double><<<row_grid(nr), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja,
-                                                                    M, s->d_dinv, b, x, xa);
-        });
-        if (rc) return rc;
-      }
-    }
-    if (dnorm && sw >= nsweeps - 2) {
-      int rc = run_sumsq(s, x, (long long)s->nnode * NEQN, s->d_scal + 2);
-      if (rc) return rc;
-      double v;
-      CUDA_TRY(cudaMemcpyAsync(&v, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-      CUDA_TRY(cudaStreamSynchronize(s->stream));
-      prev = cur;
-      cur = std::sqrt(v) / cnt;
-    }
+  auto norm = [&](double& out) -> int {
+    int rc = run_sumsq(s, x, (long long)s->nnode * NEQN, s->d_scal + 2);
+    if (rc) return rc;
+    double v;
+    CUDA_TRY(cudaMemcpyAsync(&v, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    out = std::sqrt(v) / cnt;
+    return PCFD_OK;
+  };
+  int rc;
+  if (dnorm && nsweeps >= 2) {
+    // the reference returns the norm change of the last sweep
+    if ((rc = run_sweeps<T, double>(s, nsweeps - 1, s->d_dinv, b, x, xa))) return rc;
+    if ((rc = norm(prev))) return rc;
+    if ((rc = run_sweeps<T, double>(s, 1, s->d_dinv, b, x, xa))) return rc;
+    if ((rc = norm(cur))) return rc;
+  } else {
+    if ((rc = run_sweeps<T, double>(s, nsweeps, s->d_dinv, b, x, xa))) return rc;
+    if (dnorm && nsweeps == 1 && (rc = norm(cur))) return rc;
   }
-  if (dnorm) *dnorm = std::fabs((nsweeps >= 2 ? prev : 0.0) - cur);
+  if (dnorm) *dnorm = std::fabs(prev - cur);
   return PCFD_OK;
 }
 
@@ -1764,19 +1809,36 @@ int run_sgs(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
 // preconditioner; FP32 or BF16 matrix storage)
 template <class T>
 int run_sgs_f_t(Solver* s, int nsweeps, const float* b, float* x) {
-  const T* M = (const T*)s->d_M;
-  for (int sw = 0; sw < nsweeps; sw++)
-    for (int dir = 0; dir < 2; dir++)
-      for (int cc = 0; cc < s->ncolor; cc++) {
-        int c = dir == 0 ? cc : s->ncolor - 1 - cc;
-        int r0 = s->color_ptr[c], nr = s->color_ptr[c + 1] - r0;
-        if (nr == 0) continue;
-        int rc = launch(s, T_SGS, [&] {
-          k_sgs_color<T, float><<<row_grid(nr), 256, 0, s->stream>>>(nr, s->d_color_rows + r0, s->d_ia, s->d_ja, M,
-                                                                   s->d_dinvf, b, x, x);
-        });
-        if (rc) return rc;
-      }
+  return run_sweeps<T, float>(s, nsweeps, s->d_dinvf, b, x, x);
+}
+
+// FP32 blocks: the staged sweep kernel (cooperative, up to four blocks per
+// multiprocessor)
+template <>
+int run_sgs_f_t<float>(Solver* s, int nsweeps, const float* b, float* x) {
+  if (nsweeps <= 0) return PCFD_OK;
+  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage);
+  static bool attr = false;
+  if (!attr) {
+    CUDA_TRY(cudaFuncSetAttribute(k_sgs_sweep_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sgs_sweep_staged, 256, smem));
+  if (per_sm < 1) return set_err(PCFD_ERR_CUDA, "sgs: staged sweep kernel cannot be resident");
+  int maxrows = 1;
+  for (int c = 0; c < s->ncolor; c++) maxrows = std::max(maxrows, s->color_ptr[c + 1] - s->color_ptr[c]);
+  int grid = std::max(1, std::min(std::min(per_sm, 4) * s->nsm, nblk(maxrows, 8)));
+  const float* M = (const float*)s->d_M;
+  const float* dinv = s->d_dinvf;
+  int ncolor = s->ncolor;
+  void* args[] = {&ncolor, &s->d_cptr, &s->d_rowdesc, &s->d_ja, &M, &dinv, &b, &x, &nsweeps, &s->d_gbar, &s->d_sgs_err};
+  cudaError_t ce = cudaSuccess;
+  int rc = launch(s, T_SGS, [&] {
+    ce = cudaLaunchCooperativeKernel((void*)k_sgs_sweep_staged, grid, 256, args, smem, s->stream);
+  });
+  if (rc) return rc;
+  if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("sgs sweep launch: ") + cudaGetErrorString(ce));
   return PCFD_OK;
 }
 
@@ -1835,6 +1897,22 @@ int run_spmv_f_t(Solver* s, const float* x, float* y) {
   });
 }
 
+// FP32 blocks: the staged pipeline (k_spmv_staged), four blocks per
+// multiprocessor
+template <>
+int run_spmv_f_t<float>(Solver* s, const float* x, float* y) {
+  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage);
+  static bool attr = false;
+  if (!attr) {
+    CUDA_TRY(cudaFuncSetAttribute(k_spmv_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  const int grid = std::max(1, std::min(nblk(s->nnode, 8), 4 * s->nsm));
+  return launch(s, T_SPMV, [&] {
+    k_spmv_staged<<<grid, 256, smem, s->stream>>>(s->nnode, s->d_ia, s->d_ja, (const float*)s->d_M, s->d_diagf, x, y);
+  });
+}
+
 int run_spmv_f(Solver* s, const float* x, float* y) {
   if (s->jac_prec == 1) return run_spmv_f_t<float>(s, x, y);
   return run_spmv_f_t<__nv_bfloat16>(s, x, y);
@@ -1857,11 +1935,12 @@ int ensure_krylov(Solver* s, int m) {
   s->d_V = s->d_Z = s->d_w = s->d_dots = nullptr;
   const size_t n = (size_t)s->nnode * NEQN;
   int rc;
-  if ((rc = dalloc(&s->d_V, n * (m + 1)))) return rc;
-  if ((rc = dalloc(&s->d_Z, n * m))) return rc;
+  // (with tail padding for the staged row kernels' aligned windows)
+  if ((rc = dalloc(&s->d_V, n * (m + 1) + 4))) return rc;
+  if ((rc = dalloc(&s->d_Z, n * m + 4))) return rc;
   if ((rc = dalloc(&s->d_w, n))) return rc;
-  // partials [kNormBlocks][m+2], then four result slots of m+2 each
-  if ((rc = dalloc(&s->d_dots, (size_t)kNormBlocks * (m + 2) + 4 * (m + 2)))) return rc;
+  // partials [kKrylovBlocks][m+2], then four result slots of m+2 each
+  if ((rc = dalloc(&s->d_dots, (size_t)kKrylovBlocks * (m + 2) + 4 * (m + 2)))) return rc;
   if (s->d_dotsf) cudaFree(s->d_dotsf);
   s->d_dotsf = nullptr;
   if ((rc = dalloc(&s->d_dotsf, 4 * (size_t)(m + 2)))) return rc;
@@ -1876,7 +1955,7 @@ int ensure_krylov(Solver* s, int m) {
 
 // result slot `slot` (0..3) of the Krylov dot buffer, m+2 doubles
 double* krylov_slot(Solver* s, int slot) {
-  return s->d_dots + (size_t)kNormBlocks * (s->fg_m + 2) + (size_t)slot * (s->fg_m + 2);
+  return s->d_dots + (size_t)kKrylovBlocks * (s->fg_m + 2) + (size_t)slot * (s->fg_m + 2);
 }
 
 float* krylov_slot_f(Solver* s, int slot) { return s->d_dotsf + (size_t)slot * (s->fg_m + 2); }
@@ -1892,12 +1971,32 @@ float* krylov_coef<float>(Solver* s, int slot) { return krylov_slot_f(s, slot); 
 template <class K>
 int run_mdot_dev(Solver* s, const K* V, int nv, const K* w, int slot) {
   const long long n = (long long)s->nnode * NEQN;
-  const int stride = s->fg_m + 2;
   double* part = s->d_dots;
   double* res = krylov_slot(s, slot);
   float* resf = krylov_slot_f(s, slot);
   return launch(s, T_KRYLOV, [&] {
-    k_mdot<K><<<kNormBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, stride, s->d_mdot_done, res, resf);
+    k_mdot<K><<<kKrylovBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, w, part, s->d_mdot_done, res, resf);
+  });
+}
+
+// w -= sum_k h[k] V_k with (w, w) of the result into result slot 0
+template <class K>
+int run_orth_norm(Solver* s, const K* V, int nv, const K* h, K* w) {
+  const long long n = (long long)s->nnode * NEQN;
+  return launch(s, T_KRYLOV, [&] {
+    k_orth_norm<K><<<kKrylovBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
+                                                                  krylov_slot(s, 0));
+  });
+}
+
+// w -= sum_k h[k] V_k, then its dot products with V_0..V_{nv-1} into result
+// slot `slot` (nv <= 32)
+template <class K>
+int run_orth_mdot(Solver* s, const K* V, int nv, const K* h, K* w, int slot) {
+  const long long n = (long long)s->nnode * NEQN;
+  return launch(s, T_KRYLOV, [&] {
+    k_orth_mdot<K><<<kKrylovBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
+                                                                  krylov_slot(s, slot), krylov_slot_f(s, slot));
   });
 }
 
@@ -1983,7 +2082,7 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
     double beta = std::sqrt(bb);
     if (beta0 < 0.0) beta0 = beta;
     if (beta == 0.0 || beta0 == 0.0) { rel = 0.0; break; }
-    if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kNormBlocks, 256, 0, s->stream>>>(n, K(1.0 / beta), w, V); })))
+    if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kKrylovBlocks, 256, 0, s->stream>>>(n, K(1.0 / beta), w, V); })))
       return rc;
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -1995,14 +2094,18 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
       if ((rc = krylov_prec(s, std::max(1, o->nsgs), lp_here, V + (size_t)j * n, zj))) return rc;
       if ((rc = krylov_spmv(s, zj, w))) return rc;
       // CGS2 with the coefficients kept on the device (slots 1, 2) and the
-      // norm of the result (slot 0); one host synchronisation per iteration
-      for (int pass = 0; pass < 2; pass++) {
-        if ((rc = run_mdot_dev<K>(s, V, j + 1, w, 1 + pass))) return rc;
-        K* dv = krylov_coef<K>(s, 1 + pass);
-        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<K><<<kNormBlocks, 256, 0, s->stream>>>(n, j + 1, V, dv, w); })))
+      // norm of the result (slot 0, formed by the second update); one host
+      // synchronisation per iteration
+      if ((rc = run_mdot_dev<K>(s, V, j + 1, w, 1))) return rc;
+      if (j + 1 <= 32) {
+        if ((rc = run_orth_mdot<K>(s, V, j + 1, krylov_coef<K>(s, 1), w, 2))) return rc;
+      } else {
+        K* dv = krylov_coef<K>(s, 1);
+        if ((rc = launch(s, T_KRYLOV, [&] { k_orth_update<K><<<kKrylovBlocks, 256, 0, s->stream>>>(n, j + 1, V, dv, w); })))
           return rc;
+        if ((rc = run_mdot_dev<K>(s, V, j + 1, w, 2))) return rc;
       }
-      if ((rc = run_mdot_dev<K>(s, w, 1, w, 0))) return rc;
+      if ((rc = run_orth_norm<K>(s, V, j + 1, krylov_coef<K>(s, 2), w))) return rc;
       CUDA_TRY(cudaMemcpyAsync(dd.data(), krylov_slot(s, 0), dd.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                s->stream));
       CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -2012,7 +2115,7 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
       hcol[j + 1] = hn;
       if (hn > 0.0) {
         K* vn = V + (size_t)(j + 1) * n;
-        if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kNormBlocks, 256, 0, s->stream>>>(n, K(1.0 / hn), w, vn); })))
+        if ((rc = launch(s, T_KRYLOV, [&] { k_scale_copy<K><<<kKrylovBlocks, 256, 0, s->stream>>>(n, K(1.0 / hn), w, vn); })))
           return rc;
       }
       // apply previous rotations, then a new one
@@ -2041,7 +2144,7 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
     }
     for (int k = 0; k < j; k++) yk[k] = (K)y[k];
     CUDA_TRY(cudaMemcpyAsync(hdev, yk.data(), j * sizeof(K), cudaMemcpyHostToDevice, s->stream));
-    if ((rc = launch(s, T_KRYLOV, [&] { k_combine<K><<<kNormBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
+    if ((rc = launch(s, T_KRYLOV, [&] { k_combine<K><<<kKrylovBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
       return rc;
     if (rel < rtol) break;
     if (use_lp && rel > 0.9 * beta / beta0) {
@@ -2414,6 +2517,12 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   if (ce != cudaSuccess) { free_solver(s); return set_err(PCFD_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(ce)); }
   cudaEventCreate(&s->ev0);
   cudaEventCreate(&s->ev1);
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (s->nsm <= 0) s->nsm = 1;
+  }
 
   // --- host-side integer preprocessing of the GPU maps ---
   // node -> incident edges, ascending edge id
@@ -2647,6 +2756,19 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     TRY(dput(&s->d_pos_lr, pos_lr.data(), pos_lr.size()));
     TRY(dput(&s->d_pos_rl, pos_rl.data(), pos_rl.size()));
     TRY(dput(&s->d_color_rows, rows.data(), rows.size()));
+    TRY(dput(&s->d_cptr, s->color_ptr.data(), s->color_ptr.size()));
+    {
+      std::vector<int4> desc(nn);
+      for (long long g = 0; g < nn; g++) {
+        const int i = rows[g];
+        desc[g] = make_int4(i, ia[i] + 1, ia[i + 1] - ia[i] - 1, 0);
+      }
+      TRY(dput(&s->d_rowdesc, desc.data(), desc.size()));
+    }
+    TRY(dalloc(&s->d_gbar, 2));
+    TRY(dalloc(&s->d_sgs_err, 1));
+    CUDA_TRY(cudaMemset(s->d_gbar, 0, 2 * sizeof(unsigned int)));
+    CUDA_TRY(cudaMemset(s->d_sgs_err, 0, sizeof(int)));
     TRY(dalloc(&s->d_diag, (size_t)nn * 25));
     TRY(dalloc(&s->d_dlu, (size_t)nn * 25));
     TRY(dalloc(&s->d_dinv, (size_t)nn * 25));
@@ -2951,7 +3073,71 @@ PCFD_API int pcfd_sgs(pcfd_solver_t h, int nsweeps, double* x_out, double* dnorm
     CUDA_TRY(cudaMemcpyAsync(x_out, s->d_x, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
                              s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return check_sweeps(s);
+}
+
+PCFD_API int pcfd_matvec(pcfd_solver_t h, const double* x, double* y, int vec_precision) {
+  Solver* s = (Solver*)h;
+  if (!s || !x || !y || vec_precision < 0 || vec_precision > 1) return set_err(PCFD_ERR_ARG, "pcfd_matvec: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_matvec: no Jacobian assembled");
+  if (vec_precision == 1 && s->jac_prec == 0)
+    return set_err(PCFD_ERR_STATE, "pcfd_matvec: FP32 vectors need FP32 or BF16 matrix storage");
+  const long long n = (long long)s->nnode * NEQN;
+  // scratch: two FP64 vectors, then two FP32 vectors with tail padding
+  if (!s->d_mv) {
+    int rc = dalloc(&s->d_mv, (size_t)2 * n + (size_t)n + 4);
+    if (rc) return rc;
+  }
+  double* xd = s->d_mv;
+  double* yd = s->d_mv + n;
+  float* xf = (float*)(s->d_mv + 2 * n);
+  float* yf = xf + n + 4;
+  CUDA_TRY(cudaMemcpyAsync(xd, x, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc;
+  if (vec_precision == 0) {
+    rc = run_spmv(s, xd, yd);
+  } else {
+    rc = launch(s, T_SPMV, [&] { k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, xd, xf); });
+    if (!rc) rc = run_spmv_f(s, xf, yf);
+    if (!rc) rc = launch(s, T_SPMV, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, yf, yd); });
+  }
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(y, yd, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
   return PCFD_OK;
+}
+
+PCFD_API int pcfd_sgs_rhs(pcfd_solver_t h, int nsweeps, const double* b, double* x_out, int vec_precision) {
+  Solver* s = (Solver*)h;
+  if (!s || !b || !x_out || nsweeps < 0 || vec_precision < 0 || vec_precision > 1)
+    return set_err(PCFD_ERR_ARG, "pcfd_sgs_rhs: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_sgs_rhs: no Jacobian assembled");
+  if (vec_precision == 1 && s->jac_prec == 0)
+    return set_err(PCFD_ERR_STATE, "pcfd_sgs_rhs: FP32 vectors need FP32 or BF16 matrix storage");
+  const long long n = (long long)s->nnode * NEQN;
+  if (!s->d_mv) {
+    int rc = dalloc(&s->d_mv, (size_t)2 * n + (size_t)n + 4);
+    if (rc) return rc;
+  }
+  double* bd = s->d_mv;
+  double* xd = s->d_mv + n;
+  float* bf = (float*)(s->d_mv + 2 * n);
+  float* xf = bf + n + 4;
+  CUDA_TRY(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc;
+  if (vec_precision == 0) {
+    CUDA_TRY(cudaMemsetAsync(xd, 0, n * sizeof(double), s->stream));
+    rc = run_sgs(s, nsweeps, bd, xd, nullptr);
+  } else {
+    CUDA_TRY(cudaMemsetAsync(xf, 0, n * sizeof(float), s->stream));
+    rc = launch(s, T_SGS, [&] { k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, bd, bf); });
+    if (!rc) rc = run_sgs_f(s, nsweeps, bf, xf);
+    if (!rc) rc = launch(s, T_SGS, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, xf, xd); });
+  }
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(x_out, xd, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return check_sweeps(s);
 }
 
 PCFD_API int pcfd_apply_dq(pcfd_solver_t h, const double* x_in, double* dqnorm) {
@@ -3023,7 +3209,7 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   } else {
     CUDA_TRY(cudaStreamSynchronize(s->stream));
   }
-  return PCFD_OK;
+  return check_sweeps(s);
 }
 
 // ---- learned right preconditioner --------------------------------------

@@ -6,7 +6,7 @@ import pytest
 
 from oracle_lib import OracleImplicit
 from parity import assert_field_close
-from proteuscfd_gb300 import SolutionSpace, cases
+from proteuscfd_gb300 import Mesh, Param, SolutionSpace, cases
 from proteuscfd_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
@@ -191,3 +191,84 @@ def test_fgmres_reduces_linear_residual():
                                fgmres_rtol=1e-6, jac_precision=prec)
         assert rep["lin_res"] < 1e-6, rep
         assert np.isfinite(rep["dqnorm"]) and rep["dqnorm"] > 0
+
+
+def star_mesh(npts=40):
+    """A ball of tets around one centre node joined to npts hull vertices:
+    its Jacobian row has npts off-diagonal blocks, past the block counts the
+    row kernels stage or shuffle (16 and 32)."""
+    from scipy.spatial import ConvexHull
+    k = np.arange(npts) + 0.5
+    phi = np.arccos(1 - 2 * k / npts)
+    th = np.pi * (1 + 5 ** 0.5) * k
+    pts = np.c_[np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)]
+    xyz = np.vstack([[0.0, 0.0, 0.0], pts])
+    tris, tets = [], []
+    for a, b, c in ConvexHull(pts).simplices:
+        tris.append([a + 1, b + 1, c + 1])
+        v = np.dot(np.cross(pts[b] - pts[a], pts[c] - pts[a]), -pts[a])
+        tets.append([0, a + 1, c + 1, b + 1] if v > 0 else [0, a + 1, b + 1, c + 1])
+    return Mesh.from_elements(xyz, np.array(tris), np.ones(len(tris), int), np.array(tets))
+
+
+@pytest.mark.parametrize("which", ["star", "box"])
+def test_matvec_matches_crs_product(which):
+    """pcfd_matvec (CRSMatrix::MatVecMultiply, ucs/crs.tcc:484) against the
+    CRS product of the assembled matrix, for FP64/FP32/BF16 block storage and
+    FP64 or FP32 vectors; the star row (40 blocks) covers the rows longer than
+    the staged and shuffled block counts, the 40x32x32 box many rows per warp."""
+    if which == "star":
+        m = star_mesh(40)
+        prm = Param(gamma=1.4, mach=0.7, bc_type={1: N.BC_FARFIELD})
+    else:
+        c = cases.ns_flatplate(40, 32, 32, seed=3)
+        m = cases.build_mesh(c)
+        prm = c.param
+    S = SolutionSpace(m, prm)
+    S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 2))
+    rng = np.random.default_rng(4)
+    x = rng.normal(size=(m.nnode, 5))
+    for prec in (0, 1, 2):
+        S.set_jacobian_precision(prec)
+        S.compute_timesteps(5.0)
+        S.compute_jacobians()
+        M = S.get_jacobian().reshape(-1, 5, 5)
+        ia, ja, _ = S.crs_structure()
+        ref = np.add.reduceat(np.einsum("kij,kj->ki", M, x[ja]), ia[:-1], axis=0)
+        scale = np.add.reduceat(np.einsum("kij,kj->ki", np.abs(M), np.abs(x[ja])), ia[:-1], axis=0)
+        err = np.abs(S.matvec(x) - ref) / scale
+        assert err.max() < (1e-13 if prec == 0 else 2e-6), (prec, err.max())
+        if prec > 0:
+            err = np.abs(S.matvec(x, fp32=True) - ref) / scale
+            assert err.max() < 2e-6, (prec, err.max())
+        else:
+            with pytest.raises(N.PcfdError):
+                S.matvec(x, fp32=True)
+    S.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "fp32", "bf16"])
+def test_sgs_rhs_matches_colored_oracle(prec):
+    """pcfd_sgs_rhs against the oracle's row update in the GPU's colour order
+    on the same stored matrix: FP64 vectors to rounding, and the FP32
+    Krylov preconditioner's sweep (FP32 vectors and diagonal inverse, FP32
+    accumulation) to FP32 accuracy, on a box with many rows per warp."""
+    c = cases.ns_flatplate(40, 32, 32, seed=3)
+    m = cases.build_mesh(c)
+    S = SolutionSpace(m, c.param)
+    O = OracleImplicit(m, c.param)
+    S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 2))
+    S.set_jacobian_precision(prec)
+    S.compute_timesteps(5.0)
+    S.compute_jacobians()
+    b = np.random.default_rng(6).normal(size=(m.nnode, 5))
+    Mlu, pv = O.lu(S.get_jacobian())
+    cptr, rows = S.coloring()
+    xo = O.sgs_colored(Mlu, pv, b, 3, cptr, rows)
+    x = S.sgs_rhs(b, 3)
+    tol = 1e-10 if prec == 0 else 2e-4   # FP64 vectors over an FP32/BF16 matrix accumulate in FP32
+    assert np.abs(x - xo).max() <= tol * np.abs(xo).max(), np.abs(x - xo).max() / np.abs(xo).max()
+    if prec > 0:
+        xf = S.sgs_rhs(b, 3, fp32=True)
+        assert np.abs(xf - xo).max() <= 2e-4 * np.abs(xo).max(), np.abs(xf - xo).max() / np.abs(xo).max()
+    S.close()
