@@ -344,10 +344,17 @@ def chemistry_study(args):
         c.production_rates_dev(n, d_rho.data_ptr(), d_T.data_ptr(), d_w.data_ptr())
     ms = [c.production_rates_dev(n, d_rho.data_ptr(), d_T.data_ptr(), d_w.data_ptr()) for _ in range(args.steps)]
     ms_avg = float(np.mean(ms))
+    # host API with pinned host buffers (copies in, rates out)
+    rho_h = torch.empty(rho.shape, dtype=torch.float64, pin_memory=True).numpy()
+    T_h = torch.empty(T.shape, dtype=torch.float64, pin_memory=True).numpy()
+    w_h = torch.empty(rho.shape, dtype=torch.float64, pin_memory=True).numpy()
+    rho_h[:] = rho
+    T_h[:] = T
+    c.production_rates(rho_h, T_h, out=w_h)
     t0 = time.perf_counter()
     k = 3
     for _ in range(k):
-        c.production_rates(rho, T)
+        c.production_rates(rho_h, T_h, out=w_h)
     e2e = (time.perf_counter() - t0) / k
     ns = 20000
     t0 = time.perf_counter()
@@ -429,17 +436,20 @@ def run_gb300(args, ws, rank, local, pg):
     timers = S.timers()
     S.profile(False)
 
-    # end to end through the C ABI with host buffers: H2D of q, the step,
-    # D2H of b and the norms, every step
-    qh = np.ascontiguousarray(q0)
+    # end to end through the C ABI with host buffers in pinned memory: H2D of
+    # q, the step, D2H of b and the norms, every step
+    import torch
+    qh = torch.empty(q0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    qh[:] = q0
+    bh = torch.empty((m.nnode, 5), dtype=torch.float64, pin_memory=True).numpy()
     S.set_state(qh)
     S.residual_full()
-    S.get_residual()
+    S.get_residual(out=bh)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         S.set_state(qh)
         S.residual_full()
-        b = S.get_residual()
+        b = S.get_residual(out=bh)
     N.check(lib.pcfd_device_sync(), "sync")
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(pg, e2e_s)

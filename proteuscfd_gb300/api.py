@@ -254,8 +254,12 @@ class SolutionSpace:
         N.check(self._lib.pcfd_residual(self._h, N.dptr(b) if want_b else None, N.dptr(norms)), "pcfd_residual")
         return b, norms
 
-    def get_residual(self):
-        b = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+    def get_residual(self, out=None):
+        """The residual [nnode][5]; out, when given, is a C-contiguous FP64
+        array of that shape to fill (for instance in pinned host memory)."""
+        b = np.empty((self.mesh.nnode, NEQN), dtype=np.float64) if out is None else out
+        if b.shape != (self.mesh.nnode, NEQN) or b.dtype != np.float64 or not b.flags["C_CONTIGUOUS"]:
+            raise ValueError("get_residual: out must be a C-contiguous float64 array of shape (nnode, 5)")
         N.check(self._lib.pcfd_get_residual(self._h, N.dptr(b)), "pcfd_get_residual")
         return b
 

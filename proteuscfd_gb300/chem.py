@@ -58,13 +58,16 @@ class ChemModel:
         N.check(self._lib.pcfd_chem_create(C.byref(self._m), C.byref(h)), "pcfd_chem_create")
         self._h = h
 
-    def production_rates(self, rhoi, T):
-        """rhoi [n][nspecies] kg/m^3, T [n] K -> wdot [n][nspecies] kg/(m^3 s)."""
+    def production_rates(self, rhoi, T, out=None):
+        """rhoi [n][nspecies] kg/m^3, T [n] K -> wdot [n][nspecies] kg/(m^3 s);
+        out, when given, is the C-contiguous FP64 result array to fill."""
         rhoi = np.ascontiguousarray(rhoi, dtype=np.float64)
         T = np.ascontiguousarray(T, dtype=np.float64)
         n = T.shape[0]
         assert rhoi.shape == (n, self.nspecies)
-        w = np.empty_like(rhoi)
+        w = np.empty_like(rhoi) if out is None else out
+        if w.shape != rhoi.shape or w.dtype != np.float64 or not w.flags["C_CONTIGUOUS"]:
+            raise ValueError("production_rates: out must be a C-contiguous float64 array shaped like rhoi")
         N.check(self._lib.pcfd_chem_production_rates(self._h, n, N.dptr(rhoi), N.dptr(T), N.dptr(w)),
                 "pcfd_chem_production_rates")
         return w

@@ -2350,13 +2350,18 @@ int lp_precondition(Solver* s, int nsgs, const double* v, double* z) {
   return lp_forward(s, false, z);
 }
 
-// the same on FP32 Krylov vectors (through FP64 copies)
+// the same on FP32 Krylov vectors: the sweep in the FP32 solver's own
+// kernel (into z, which is padded like every Krylov vector), the network on
+// an FP64 copy of its result
 int lp_precondition_f(Solver* s, int nsgs, const float* v, float* z) {
   Learned* lp = s->lp;
   if (!lp) return set_err(PCFD_ERR_STATE, "learned preconditioner: pcfd_lp_init not called");
   const long long n = (long long)lp->n * NEQN;
-  int rc = launch(s, T_KRYLOV, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, v, lp->vbuf); });
-  if (rc || (rc = lp_precondition(s, nsgs, lp->vbuf, s->d_wd))) return rc;
+  CUDA_TRY(cudaMemsetAsync(z, 0, n * sizeof(float), s->stream));
+  int rc = run_sgs_f(s, nsgs, v, z);
+  if (rc) return rc;
+  rc = launch(s, T_KRYLOV, [&] { k_f32_to_f64<<<kNormBlocks, 256, 0, s->stream>>>(n, z, lp->y); });
+  if (rc || (rc = lp_features(s)) || (rc = lp_forward(s, false, s->d_wd))) return rc;
   return launch(s, T_KRYLOV, [&] { k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_wd, z); });
 }
 
