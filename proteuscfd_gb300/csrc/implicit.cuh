@@ -180,7 +180,7 @@ __device__ __forceinline__ float store_blk(float*, float v) { return v; }
 __device__ __forceinline__ double store_blk(double*, double v) { return v; }
 
 template <class T>
-__global__ void __launch_bounds__(128) k_jac_edge_df(int nedge, const int2* __restrict__ en,
+__global__ void __launch_bounds__(128, 3) k_jac_edge_df(int nedge, const int2* __restrict__ en,
                                                      const D4* __restrict__ ea, const double* __restrict__ eh,
                                                      const double* __restrict__ q, const int* __restrict__ pos_lr,
                                                      const int* __restrict__ pos_rl, JacConst k, T* __restrict__ M,
@@ -1134,45 +1134,53 @@ __global__ void k_sum_final(int nblocks, const double* __restrict__ part, double
   if (threadIdx.x == 0) *out = s;
 }
 
-// MaxEigenvalue (ucs/compressible.tcc:799) of the face-averaged state
-__device__ __forceinline__ double max_eig(const double* QL, const double* QR, const D4& a, double gamma, double half) {
-  double Q0 = half * (QL[0] + QR[0]), Q1 = half * (QL[1] + QR[1]), Q2 = half * (QL[2] + QR[2]),
-         Q3 = half * (QL[3] + QR[3]), Q4 = half * (QL[4] + QR[4]);
-  double gm1 = gamma - 1.0;
-  double ir = 1.0 / Q0;
-  double u = Q1 * ir, v = Q2 * ir, w = Q3 * ir;
-  double v2h = 0.5 * (u * u + v * v + w * w);
-  double P = gm1 * (Q4 - Q0 * v2h);
-  double c = sqrt(gamma * P * ir);
-  double theta = u * a.x + v * a.y + w * a.z;
-  double e4 = fabs(theta + c), e5 = fabs(theta - c);
+// MaxEigenvalue (ucs/compressible.tcc:799) of the face-averaged state, in
+// the residual's scalar type S (FP64, or double-float)
+template <class S, class V>
+__device__ __forceinline__ S max_eig(const S* QL, const S* QR, const V& a, S gamma) {
+  const S Q0 = halve(QL[0] + QR[0]), Q1 = halve(QL[1] + QR[1]), Q2 = halve(QL[2] + QR[2]),
+          Q3 = halve(QL[3] + QR[3]), Q4 = halve(QL[4] + QR[4]);
+  const S gm1 = gamma - Sc<S>::c(1.0);
+  const S ir = Sc<S>::c(1.0) / Q0;
+  const S u = Q1 * ir, v = Q2 * ir, w = Q3 * ir;
+  const S v2h = halve(u * u + v * v + w * w);
+  const S P = gm1 * (Q4 - Q0 * v2h);
+  const S c = sqrt(gamma * P * ir);
+  const S theta = u * a.x + v * a.y + w * a.z;
+  const S e4 = fabs(theta + c), e5 = fabs(theta - c);
   return e4 > e5 ? e4 : e5;
 }
 
 // ComputeTimesteps (ucs/timestep.tcc:7) with local time stepping:
 // dt_i = CFL vol_i / sum(max eigenvalue * area) over the node's faces.
+template <class S>
 __global__ void __launch_bounds__(128) k_timestep(int nnode, const int* __restrict__ nptr, const int* __restrict__ nedg,
-                                                  const int* __restrict__ nnbr, const D4* __restrict__ ea,
+                                                  const int* __restrict__ nnbr,
+                                                  const typename V4<S>::type* __restrict__ ea,
                                                   const int* __restrict__ bptr, const int* __restrict__ bhe,
-                                                  const int2* __restrict__ bn, const D4* __restrict__ ba,
-                                                  const double* __restrict__ q, const double* __restrict__ vol,
-                                                  double gamma, double cfl, double* __restrict__ dt) {
+                                                  const int2* __restrict__ bn,
+                                                  const typename V4<S>::type* __restrict__ ba, const S* __restrict__ q,
+                                                  const double* __restrict__ vol, double gamma_d, double cfl,
+                                                  double* __restrict__ dt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnode) return;
-  double s = 0.0;
-  const double* qi = &q[(size_t)i * NVARS];
+  const S gamma = Sc<S>::from(gamma_d);
+  S s = Sc<S>::c(0.0);
+  const S* qi = &q[(size_t)i * NVARS];
   for (int k = nptr[i]; k < nptr[i + 1]; k++) {
     int se = nedg[k];
     int e = se < 0 ? ~se : se;
-    const double* qj = &q[(size_t)nnbr[k] * NVARS];
+    const S* qj = &q[(size_t)nnbr[k] * NVARS];
+    const typename V4<S>::type a = ea[e];
     // the reference averages left and right in edge orientation
-    s += (se < 0 ? max_eig(qi, qj, ea[e], gamma, 0.5) : max_eig(qj, qi, ea[e], gamma, 0.5)) * ea[e].w;
+    s += (se < 0 ? max_eig(qi, qj, a, gamma) : max_eig(qj, qi, a, gamma)) * a.w;
   }
   for (int p = bptr[i]; p < bptr[i + 1]; p++) {
     int he = bhe[p];
-    s += max_eig(qi, &q[(size_t)bn[he].y * NVARS], ba[he], gamma, 0.5) * ba[he].w;
+    const typename V4<S>::type a = ba[he];
+    s += max_eig(qi, &q[(size_t)bn[he].y * NVARS], a, gamma) * a.w;
   }
-  dt[i] = cfl * (vol[i] / s);
+  dt[i] = cfl * (vol[i] / Sc<S>::to(s));
 }
 
 __global__ void __launch_bounds__(kNormThreads) k_min_part(int n, const double* __restrict__ v,

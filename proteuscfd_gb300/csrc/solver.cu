@@ -1616,11 +1616,22 @@ double ramp_cfl(int iter, double cfl_start, double cfl, int ramp_steps) {
   return cfl;
 }
 
+// local time steps in the residual's arithmetic (the pseudo-time step does
+// not enter the converged answer)
 int run_timestep(Solver* s, double cfl) {
-  int rc = launch(s, T_TIMESTEP, [&] {
-    k_timestep<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_ea,
-                                                          s->d_bptr, s->d_bhe, s->d_bn, s->d_ba, s->d_q, s->d_vol,
-                                                          s->prm.gamma, cfl, s->d_dt);
+  int rc = prep_state(s, s->arith);
+  if (rc) return rc;
+  rc = launch(s, T_TIMESTEP, [&] {
+    if (s->arith) {
+      RBuf<dfl> r = rbuf_f(s);
+      k_timestep<dfl><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.ea,
+                                                                 s->d_bptr, s->d_bhe, s->d_bn, r.ba, r.q, s->d_vol,
+                                                                 s->prm.gamma, cfl, s->d_dt);
+    } else {
+      k_timestep<double><<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr,
+                                                                    s->d_ea, s->d_bptr, s->d_bhe, s->d_bn, s->d_ba,
+                                                                    s->d_q, s->d_vol, s->prm.gamma, cfl, s->d_dt);
+    }
   });
   if (rc) return rc;
   rc = launch(s, T_TIMESTEP, [&] { k_min_part<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_dt, s->d_part); });
@@ -1699,7 +1710,7 @@ int run_jacobian(Solver* s) {
     int rc = ensure_matrix(s, 0);
     if (rc) return rc;
   }
-  int rc = run_bcs(s);
+  int rc = run_bcs(s, s->arith);
   if (rc) return rc;
   // the gradient no longer matches the state; the limiter field keeps its
   // values, as the reference's does between evaluations
