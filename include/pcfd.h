@@ -353,6 +353,38 @@ PCFD_API int pcfd_chem_production_rates(pcfd_chem_t c, long long n, const double
 PCFD_API int pcfd_chem_production_rates_dev(pcfd_chem_t c, long long n, const double* rhoi, const double* T,
                                             double* wdot, double* ms_out);
 
+/* Node state of the reacting equation set (CompressibleFREqnSet, ideal-gas
+ * mixture, Dalton's law).  Variables are non-dimensional as in the reference,
+ * with these scales (Param::ref_*, ucs/param.tcc:372-397). */
+typedef struct {
+  double density, pressure, temperature, specific_enthalpy, velocity;
+} pcfd_chem_ref;
+/* With dev = 0 the arrays are host arrays (copied through the handle's
+ * buffers); with dev = 1 they are device arrays, used in place on the
+ * handle's stream.  Per node, ns = the model's species count. */
+/* NewtonFindTGivenP (ucs/compressibleFR.tcc:2343): rhoi [n][ns], P [n],
+ * T_init [n] -> T [n]; *nonconverged (optional) counts nodes that used all 28
+ * iterations (the reference warns). */
+PCFD_API int pcfd_chem_find_T_given_P(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                      const double* P, const double* T_init, double* T, long long* nonconverged,
+                                      int dev);
+/* ConservativeToNative (:2133): the FP64 temperature Newton from total
+ * energy.  q [n][ns+4] = (rhoi, rho u, rho v, rho w, rho Et), P [n] the
+ * stored pressure (initial guess) -> native [n][4] = (u, v, w, T).  Returns
+ * PCFD_ERR_NUMERIC when a node needs more than 20 iterations (the reference
+ * aborts). */
+PCFD_API int pcfd_chem_conservative_to_native(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* q,
+                                              const double* P, double* native, int dev);
+/* NativeToConservative (:2117) with GetTotalEnergy (:1219): rhoi [n][ns],
+ * native [n][4] = (u, v, w, T), P [n] -> q [n][4] = (rho u, rho v, rho w,
+ * rho Et). */
+PCFD_API int pcfd_chem_native_to_conservative(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                              const double* native, const double* P, double* q, int dev);
+/* ComputeAuxiliaryVariables (:755): rhoi [n][ns], T [n] -> P [n], cvi
+ * [n][ns], concentrations [n][ns] (ChemModel::MassToMole, ucs/chem.tcc:980). */
+PCFD_API int pcfd_chem_aux(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi, const double* T,
+                           double* P, double* cvi, double* mol, int dev);
+
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1
  * double-float - the same kernels with every FP64 operation replaced by a

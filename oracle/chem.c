@@ -98,3 +98,133 @@ void oracle_chem_rates_n(const pcfd_chem_model* m, long long n, const double* rh
   for (long long p = 0; p < n; p++)
     oracle_chem_rates(m, rhoi + p * m->nspecies, T[p], wdot + p * m->nspecies);
 }
+
+/* ---- node state of the reacting equation set (ideal-gas mixture) ------- */
+
+/* Species<T>::GetCp and GetH (ucs/species.tcc:43,56; href = 0, :327), J/kg */
+static double species_cp(const pcfd_chem_model* m, int s, double T) {
+  const double* a = thermo_coeff(m, s, T);
+  double cp_R = a[0] + T * (a[1] + T * (a[2] + T * (a[3] + T * a[4])));
+  return cp_R * (UNIV_R_ / m->mw[s]);
+}
+static double species_h(const pcfd_chem_model* m, int s, double T) {
+  const double* a = thermo_coeff(m, s, T);
+  double h_R = a[5] + T * (a[0] + T * (a[1] / 2.0 + T * (a[2] / 3.0 + T * (a[3] / 4.0 + T * a[4] / 5.0))));
+  return h_R * (UNIV_R_ / m->mw[s]);
+}
+/* ChemModel::GetP (ucs/chem.tcc:989), Dalton's law over IdealGasEOS::GetP */
+static double mix_P(const pcfd_chem_model* m, const double* rhoiDim, double T) {
+  double P = 0.0;
+  for (int i = 0; i < m->nspecies; i++) P += rhoiDim[i] * (UNIV_R_ / m->mw[i]) * T;
+  return P;
+}
+/* ChemModel::GetSpecificEnthalpy (ucs/chem.tcc:586) */
+static double mix_h(const pcfd_chem_model* m, const double* X, double T) {
+  double h = 0.0;
+  for (int i = 0; i < m->nspecies; i++) h += species_h(m, i, T) * X[i];
+  return h;
+}
+
+/* CompressibleFREqnSet::NewtonFindTGivenP (ucs/compressibleFR.tcc:2343);
+ * returns the iterations used (28 = not converged) */
+int oracle_chem_find_T(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double P, double Tinit,
+                       double* T) {
+  const int maxit = 28;
+  const double tol = 1.0e-15;
+  double TDim = Tinit * ref->temperature;
+  double PgoalDim = P * ref->pressure;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < m->nspecies; i++) rhoiDim[i] = rhoi[i] * ref->density;
+  int j;
+  for (j = 0; j < maxit; j++) {
+    double TpDim = TDim + 1.0e-8;
+    double PDim = mix_P(m, rhoiDim, TDim);
+    double PpDim = mix_P(m, rhoiDim, TpDim);
+    double zpoint = PgoalDim - PDim;
+    double zpointp = PgoalDim - PpDim;
+    double dzdT = (zpointp - zpoint) / (TpDim - TDim);
+    double dT = -zpoint / dzdT;
+    if (fabs(dT / ref->temperature) < tol) break;
+    TDim += dT;
+  }
+  *T = TDim / ref->temperature;
+  return j;
+}
+
+/* ConservativeToNative (ucs/compressibleFR.tcc:2133); returns the
+ * iterations used (20 = not converged, where the reference aborts) */
+int oracle_chem_c2n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* q, double P, double* native) {
+  const int ns = m->nspecies, maxit = 20;
+  const double tol = 1.0e-12;
+  double rho = 0.0, R = 0.0;
+  double Y[PCFD_CHEM_MAX_SPECIES], rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) {
+    rho += q[i];
+    rhoiDim[i] = q[i] * ref->density;
+    R += rhoiDim[i] * (UNIV_R_ / m->mw[i]);
+  }
+  R /= ref->density * rho;
+  for (int i = 0; i < ns; i++) Y[i] = q[i] / rho;
+  double u = q[ns] / rho, v = q[ns + 1] / rho, w = q[ns + 2] / rho;
+  double v2 = u * u + v * v + w * w;
+  double res = q[ns + 3] - 0.5 * v2 * rho;
+  /* IdealGasEOS::GetT (ucs/EOS.tcc:22) from the stored pressure */
+  double T = (P * ref->pressure) / ((rho * ref->density) * R) / ref->temperature;
+  int j;
+  for (j = 0; j < maxit; j++) {
+    double Tp = T + 1.0e-8;
+    double H = rho * (mix_h(m, Y, T * ref->temperature) / ref->specific_enthalpy);
+    double Hp = rho * (mix_h(m, Y, Tp * ref->temperature) / ref->specific_enthalpy);
+    double Pn = mix_P(m, rhoiDim, T * ref->temperature) / ref->pressure;
+    double Pp = mix_P(m, rhoiDim, Tp * ref->temperature) / ref->pressure;
+    double E = H - Pn, Ep = Hp - Pp;
+    double zpoint = res - E, zpointp = res - Ep;
+    double dzdT = (zpointp - zpoint) / (Tp - T);
+    double dT = -zpoint / dzdT;
+    T += dT;
+    if (fabs(dT) < tol) break;
+  }
+  native[0] = u;
+  native[1] = v;
+  native[2] = w;
+  native[3] = T;
+  return j;
+}
+
+/* NativeToConservative (ucs/compressibleFR.tcc:2117) with GetTotalEnergy
+ * (:1219): q = (rho u, rho v, rho w, rho Et) */
+void oracle_chem_n2c(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, const double* native,
+                     double P, double* q) {
+  const int ns = m->nspecies;
+  double rho = 0.0, X[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rho += rhoi[i];
+  for (int i = 0; i < ns; i++) X[i] = rhoi[i] / rho;
+  double u = native[0], v = native[1], w = native[2], T = native[3];
+  double v2 = u * u + v * v + w * w;
+  double h = mix_h(m, X, T * ref->temperature) / ref->specific_enthalpy;
+  double E = h * rho - P;
+  q[0] = u * rho;
+  q[1] = v * rho;
+  q[2] = w * rho;
+  q[3] = E + 0.5 * rho * v2;
+}
+
+/* ComputeAuxiliaryVariables (ucs/compressibleFR.tcc:755) */
+void oracle_chem_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T, double* P,
+                     double* cvi, double* mol) {
+  const int ns = m->nspecies;
+  double rho = 0.0, rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) {
+    rho += rhoi[i];
+    rhoiDim[i] = rhoi[i] * ref->density;
+  }
+  double TDim = T * ref->temperature;
+  double pDim = mix_P(m, rhoiDim, TDim);
+  *P = pDim / ref->pressure;
+  double s_ref = ref->velocity * ref->velocity / ref->temperature;
+  for (int i = 0; i < ns; i++) {
+    /* IdealGasEOS::GetCv (ucs/EOS.tcc:79): Mayer's relation with the species R */
+    cvi[i] = (species_cp(m, i, TDim) - UNIV_R_ / m->mw[i]) / s_ref;
+    mol[i] = rhoi[i] / m->mw[i] / 1000.0;
+  }
+}

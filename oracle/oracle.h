@@ -60,6 +60,13 @@ double oracle_chem_kf(const pcfd_chem_reaction* r, double T);
 double oracle_chem_kc(const pcfd_chem_model* m, const pcfd_chem_reaction* r, double T);
 void oracle_chem_rates(const pcfd_chem_model* m, const double* rhoi, double T, double* wdot);
 void oracle_chem_rates_n(const pcfd_chem_model* m, long long n, const double* rhoi, const double* T, double* wdot);
+int oracle_chem_find_T(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double P, double Tinit,
+                       double* T);
+int oracle_chem_c2n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* q, double P, double* native);
+void oracle_chem_n2c(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, const double* native,
+                     double P, double* q);
+void oracle_chem_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T, double* P,
+                     double* cvi, double* mol);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,8 @@ LIB_PATH = Path(__file__).resolve().parent / "libpcfd.so"
 
 PCFD_OK = 0
 ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "MESH", 5: "NOMEM", 6: "UNSUPPORTED", 7: "NUMERIC"}
+(PCFD_ERR_ARG, PCFD_ERR_STATE, PCFD_ERR_CUDA, PCFD_ERR_MESH, PCFD_ERR_NOMEM, PCFD_ERR_UNSUPPORTED,
+ PCFD_ERR_NUMERIC) = range(1, 8)
 
 # boundary condition types: the reference's BCTypes values (ucs/bc_defines.h:4)
 BC_PARALLEL = 0
@@ -109,6 +111,12 @@ _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 _LLP = C.POINTER(C.c_longlong)
+class ChemRef(C.Structure):
+    """pcfd_chem_ref: the reacting equation set's reference scales."""
+    _fields_ = [("density", C.c_double), ("pressure", C.c_double), ("temperature", C.c_double),
+                ("specific_enthalpy", C.c_double), ("velocity", C.c_double)]
+
+
 _FP = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes); every symbol include/pcfd.h declares
@@ -150,6 +158,12 @@ PROTOTYPES = {
     "pcfd_set_residual_arithmetic": (C.c_int, [_P, C.c_int]),
     "pcfd_get_limiter": (C.c_int, [_P, _DP]),
     "pcfd_chem_create": (C.c_int, [C.POINTER(ChemModelC), C.POINTER(_P)]),
+    # array arguments as void*: host arrays (dev = 0) or device addresses (dev = 1)
+    "pcfd_chem_find_T_given_P": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P,
+                                           C.POINTER(C.c_longlong), C.c_int]),
+    "pcfd_chem_conservative_to_native": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, C.c_int]),
+    "pcfd_chem_native_to_conservative": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, C.c_int]),
+    "pcfd_chem_aux": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, _P, C.c_int]),
     "pcfd_chem_destroy": (C.c_int, [_P]),
     "pcfd_chem_production_rates": (C.c_int, [_P, C.c_longlong, _DP, _DP, _DP]),
     "pcfd_chem_production_rates_dev": (C.c_int, [_P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, _DP]),

@@ -79,6 +79,64 @@ class ChemModel:
                 "pcfd_chem_production_rates_dev")
         return ms.value
 
+    # ---- node state of the reacting equation set (non-dimensional variables) ----
+
+    @staticmethod
+    def ref(density, pressure, temperature, specific_enthalpy, velocity):
+        """Reference scales (Param::ref_*) of the non-dimensional variables."""
+        return N.ChemRef(density, pressure, temperature, specific_enthalpy, velocity)
+
+    def _arr(self, a, shape):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.shape != shape:
+            raise ValueError("expected shape %s, got %s" % (shape, a.shape))
+        return a
+
+    def find_T_given_P(self, ref, rhoi, P, T_init):
+        """NewtonFindTGivenP per node: returns (T, nodes not converged)."""
+        n = len(P)
+        rhoi = self._arr(rhoi, (n, self.nspecies))
+        P, T_init = self._arr(P, (n,)), self._arr(T_init, (n,))
+        T = np.empty(n)
+        bad = C.c_longlong()
+        N.check(self._lib.pcfd_chem_find_T_given_P(self._h, C.byref(ref), n, N.dptr(rhoi), N.dptr(P), N.dptr(T_init),
+                                                   N.dptr(T), C.byref(bad), 0), "pcfd_chem_find_T_given_P")
+        return T, bad.value
+
+    def conservative_to_native(self, ref, q, P):
+        """q [n][ns+4] = (rhoi, rho u, rho v, rho w, rho Et), P [n] -> [n][4] = (u, v, w, T)."""
+        n = len(P)
+        q, P = self._arr(q, (n, self.nspecies + 4)), self._arr(P, (n,))
+        out = np.empty((n, 4))
+        N.check(self._lib.pcfd_chem_conservative_to_native(self._h, C.byref(ref), n, N.dptr(q), N.dptr(P),
+                                                           N.dptr(out), 0), "pcfd_chem_conservative_to_native")
+        return out
+
+    def conservative_to_native_dev(self, ref, n, q_ptr, P_ptr, out_ptr):
+        """The same on device addresses."""
+        N.check(self._lib.pcfd_chem_conservative_to_native(self._h, C.byref(ref), int(n), q_ptr, P_ptr, out_ptr, 1),
+                "pcfd_chem_conservative_to_native")
+
+    def native_to_conservative(self, ref, rhoi, native, P):
+        """rhoi [n][ns], native [n][4] = (u, v, w, T), P [n] -> [n][4] = (rho u, rho v, rho w, rho Et)."""
+        n = len(P)
+        rhoi = self._arr(rhoi, (n, self.nspecies))
+        native, P = self._arr(native, (n, 4)), self._arr(P, (n,))
+        out = np.empty((n, 4))
+        N.check(self._lib.pcfd_chem_native_to_conservative(self._h, C.byref(ref), n, N.dptr(rhoi), N.dptr(native),
+                                                           N.dptr(P), N.dptr(out), 0),
+                "pcfd_chem_native_to_conservative")
+        return out
+
+    def aux(self, ref, rhoi, T):
+        """ComputeAuxiliaryVariables: returns (P [n], cvi [n][ns], concentrations [n][ns])."""
+        n = len(T)
+        rhoi, T = self._arr(rhoi, (n, self.nspecies)), self._arr(T, (n,))
+        P, cvi, mol = np.empty(n), np.empty((n, self.nspecies)), np.empty((n, self.nspecies))
+        N.check(self._lib.pcfd_chem_aux(self._h, C.byref(ref), n, N.dptr(rhoi), N.dptr(T), N.dptr(P), N.dptr(cvi),
+                                        N.dptr(mol), 0), "pcfd_chem_aux")
+        return P, cvi, mol
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pcfd_chem_destroy(self._h)

@@ -7,6 +7,11 @@
 //   Reaction<T>::GetBackwardReactionRate      ucs/reaction.tcc:683
 //   Reaction<T>::GetMassProductionRate        ucs/reaction.tcc:763
 //   Species<T>::GetThermoCoeff                ucs/species.tcc:96
+// and the node state of the reacting equation set (ideal-gas mixture):
+//   CompressibleFREqnSet<T>::NewtonFindTGivenP      ucs/compressibleFR.tcc:2343
+//   CompressibleFREqnSet<T>::ConservativeToNative   ucs/compressibleFR.tcc:2133
+//   CompressibleFREqnSet<T>::NativeToConservative   ucs/compressibleFR.tcc:2117
+//   CompressibleFREqnSet<T>::ComputeAuxiliaryVariables ucs/compressibleFR.tcc:755
 // The reference evaluates each reaction's rates once per species it
 // produces; here each reaction is evaluated once per node and its
 // contribution added to every species it changes, in reaction order, which
@@ -32,6 +37,9 @@ struct ChemHandle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double *d_rho = nullptr, *d_T = nullptr, *d_w = nullptr;
   long long cap = 0;
+  double* d_buf = nullptr;  // host-array calls of the node-state functions
+  size_t buf_cap = 0;
+  long long* d_count = nullptr;
 };
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -145,6 +153,150 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
   for (int k = 0; k < ns; k++) wdot[p * ns + k] = w[k];
 }
 
+// ---- node state of the reacting equation set ------------------------------
+
+// Species<T>::GetCp and GetH (ucs/species.tcc:43,56; href = 0, :327), J/kg
+__device__ __forceinline__ double species_cp(const pcfd_chem_model& m, int s, double T) {
+  const double* a = thermo_coeff(m, s, T);
+  const double cp_R = a[0] + T * (a[1] + T * (a[2] + T * (a[3] + T * a[4])));
+  return cp_R * (kUnivR / m.mw[s]);
+}
+__device__ __forceinline__ double species_h(const pcfd_chem_model& m, int s, double T) {
+  const double* a = thermo_coeff(m, s, T);
+  const double h_R = a[5] + T * (a[0] + T * (a[1] / 2.0 + T * (a[2] / 3.0 + T * (a[3] / 4.0 + T * a[4] / 5.0))));
+  return h_R * (kUnivR / m.mw[s]);
+}
+// ChemModel::GetP (ucs/chem.tcc:989): Dalton's law over IdealGasEOS::GetP
+__device__ __forceinline__ double mix_P(const pcfd_chem_model& m, const double* rhoiDim, double T) {
+  double P = 0.0;
+  for (int i = 0; i < m.nspecies; i++) P += rhoiDim[i] * (kUnivR / m.mw[i]) * T;
+  return P;
+}
+// ChemModel::GetSpecificEnthalpy (ucs/chem.tcc:586)
+__device__ __forceinline__ double mix_h(const pcfd_chem_model& m, const double* X, double T) {
+  double h = 0.0;
+  for (int i = 0; i < m.nspecies; i++) h += species_h(m, i, T) * X[i];
+  return h;
+}
+
+// NewtonFindTGivenP: the pressure is linear in T, so the finite-difference
+// Newton step lands in one or two iterations; counts nodes that used all 28
+__global__ void __launch_bounds__(128) k_chem_find_T(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                     pcfd_chem_ref ref, const double* __restrict__ rhoi,
+                                                     const double* __restrict__ P, const double* __restrict__ Tinit,
+                                                     double* __restrict__ Tout, long long* __restrict__ nonconv) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[p * ns + i] * ref.density;
+  double TDim = Tinit[p] * ref.temperature;
+  const double PgoalDim = P[p] * ref.pressure;
+  int j;
+  for (j = 0; j < 28; j++) {
+    const double TpDim = TDim + 1.0e-8;
+    const double zpoint = PgoalDim - mix_P(m, rhoiDim, TDim);
+    const double zpointp = PgoalDim - mix_P(m, rhoiDim, TpDim);
+    const double dzdT = (zpointp - zpoint) / (TpDim - TDim);
+    const double dT = -zpoint / dzdT;
+    if (fabs(dT / ref.temperature) < 1.0e-15) break;
+    TDim += dT;
+  }
+  if (j == 28) atomicAdd((unsigned long long*)nonconv, 1ull);
+  Tout[p] = TDim / ref.temperature;
+}
+
+// ConservativeToNative: the temperature Newton from total energy in FP64
+// (finite-difference slope, |dT| < 1e-12, at most 20 iterations)
+__global__ void __launch_bounds__(128) k_chem_c2n(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                  pcfd_chem_ref ref, const double* __restrict__ q,
+                                                  const double* __restrict__ Pst, double* __restrict__ native,
+                                                  long long* __restrict__ nonconv) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies;
+  const double* qp = q + p * (ns + 4);
+  double rho = 0.0, R = 0.0, Y[PCFD_CHEM_MAX_SPECIES], rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) {
+    rho += qp[i];
+    rhoiDim[i] = qp[i] * ref.density;
+    R += rhoiDim[i] * (kUnivR / m.mw[i]);
+  }
+  R /= ref.density * rho;
+  for (int i = 0; i < ns; i++) Y[i] = qp[i] / rho;
+  const double u = qp[ns] / rho, v = qp[ns + 1] / rho, w = qp[ns + 2] / rho;
+  const double v2 = u * u + v * v + w * w;
+  const double res = qp[ns + 3] - 0.5 * v2 * rho;
+  // IdealGasEOS::GetT (ucs/EOS.tcc:22) from the stored pressure
+  double T = (Pst[p] * ref.pressure) / ((rho * ref.density) * R) / ref.temperature;
+  int j;
+  for (j = 0; j < 20; j++) {
+    const double Tp = T + 1.0e-8;
+    const double H = rho * (mix_h(m, Y, T * ref.temperature) / ref.specific_enthalpy);
+    const double Hp = rho * (mix_h(m, Y, Tp * ref.temperature) / ref.specific_enthalpy);
+    const double Pn = mix_P(m, rhoiDim, T * ref.temperature) / ref.pressure;
+    const double Pp = mix_P(m, rhoiDim, Tp * ref.temperature) / ref.pressure;
+    const double zpoint = res - (H - Pn), zpointp = res - (Hp - Pp);
+    const double dzdT = (zpointp - zpoint) / (Tp - T);
+    const double dT = -zpoint / dzdT;
+    T += dT;
+    if (fabs(dT) < 1.0e-12) break;
+  }
+  if (j == 20) atomicAdd((unsigned long long*)nonconv, 1ull);
+  double* o = native + p * 4;
+  o[0] = u;
+  o[1] = v;
+  o[2] = w;
+  o[3] = T;
+}
+
+// NativeToConservative with GetTotalEnergy (ucs/compressibleFR.tcc:1219)
+__global__ void __launch_bounds__(128) k_chem_n2c(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                  pcfd_chem_ref ref, const double* __restrict__ rhoi,
+                                                  const double* __restrict__ native, const double* __restrict__ P,
+                                                  double* __restrict__ q) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies;
+  double rho = 0.0, X[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rho += rhoi[p * ns + i];
+  for (int i = 0; i < ns; i++) X[i] = rhoi[p * ns + i] / rho;
+  const double* nv = native + p * 4;
+  const double u = nv[0], v = nv[1], w = nv[2], T = nv[3];
+  const double v2 = u * u + v * v + w * w;
+  const double h = mix_h(m, X, T * ref.temperature) / ref.specific_enthalpy;
+  const double E = h * rho - P[p];
+  double* o = q + p * 4;
+  o[0] = u * rho;
+  o[1] = v * rho;
+  o[2] = w * rho;
+  o[3] = E + 0.5 * rho * v2;
+}
+
+// ComputeAuxiliaryVariables: pressure, species cv (Mayer's relation with the
+// species R, IdealGasEOS::GetCv, ucs/EOS.tcc:79) and concentrations
+__global__ void __launch_bounds__(128) k_chem_aux(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                  pcfd_chem_ref ref, const double* __restrict__ rhoi,
+                                                  const double* __restrict__ T, double* __restrict__ Pout,
+                                                  double* __restrict__ cvi, double* __restrict__ mol) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[p * ns + i] * ref.density;
+  const double TDim = T[p] * ref.temperature;
+  Pout[p] = mix_P(m, rhoiDim, TDim) / ref.pressure;
+  const double s_ref = ref.velocity * ref.velocity / ref.temperature;
+  for (int i = 0; i < ns; i++) {
+    cvi[p * ns + i] = (species_cp(m, i, TDim) - kUnivR / m.mw[i]) / s_ref;
+    mol[p * ns + i] = rhoi[p * ns + i] / m.mw[i] / 1000.0;
+  }
+}
+
 int validate(const pcfd_chem_model* m) {
   if (m->nspecies < 1 || m->nspecies > PCFD_CHEM_MAX_SPECIES || m->nreactions < 0 ||
       m->nreactions > PCFD_CHEM_MAX_REACTIONS)
@@ -161,6 +313,67 @@ int validate(const pcfd_chem_model* m) {
     }
   }
   return 1;
+}
+
+int ensure_buf(ChemHandle* c, size_t ndoubles) {
+  if (c->buf_cap >= ndoubles) return PCFD_OK;
+  cudaFree(c->d_buf);
+  c->d_buf = nullptr;
+  c->buf_cap = 0;
+  CHEM_TRY(cudaMalloc(&c->d_buf, ndoubles * sizeof(double)), "chem buffers");
+  c->buf_cap = ndoubles;
+  return PCFD_OK;
+}
+
+// Runs one node-state kernel on the handle's stream.  Inputs and outputs are
+// (pointer, doubles per node) pairs; with dev = 0 they are staged through
+// the handle's buffer (inputs copied in, outputs copied back).  Returns the
+// count the kernel left in *d_count.
+template <int NIN, int NOUT, class F>
+int node_call(ChemHandle* c, long long n, int dev, const double* const (&in)[NIN], const int (&win)[NIN],
+              double* const (&out)[NOUT], const int (&wout)[NOUT], long long* count, F&& launch_kernel) {
+  const double* din[NIN];
+  double* dout[NOUT];
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  if (dev) {
+    for (int k = 0; k < NIN; k++) din[k] = in[k];
+    for (int k = 0; k < NOUT; k++) dout[k] = out[k];
+  } else {
+    size_t total = 0;
+    for (int k = 0; k < NIN; k++) total += (size_t)n * win[k];
+    for (int k = 0; k < NOUT; k++) total += (size_t)n * wout[k];
+    int rc = ensure_buf(c, total);
+    if (rc) return rc;
+    double* b = c->d_buf;
+    for (int k = 0; k < NIN; k++) {
+      CHEM_TRY(cudaMemcpyAsync(b, in[k], (size_t)n * win[k] * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+               "chem copy in");
+      din[k] = b;
+      b += (size_t)n * win[k];
+    }
+    for (int k = 0; k < NOUT; k++) {
+      dout[k] = b;
+      b += (size_t)n * wout[k];
+    }
+  }
+  launch_kernel(din, dout);
+  CHEM_TRY(cudaGetLastError(), "chem node-state launch");
+  if (!dev)
+    for (int k = 0; k < NOUT; k++)
+      CHEM_TRY(cudaMemcpyAsync(out[k], dout[k], (size_t)n * wout[k] * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream),
+               "chem copy out");
+  long long cnt = 0;
+  CHEM_TRY(cudaMemcpyAsync(&cnt, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem node-state");
+  if (count) *count = cnt;
+  return PCFD_OK;
+}
+
+bool ref_ok(const pcfd_chem_ref* r) {
+  return r && r->density > 0.0 && r->pressure > 0.0 && r->temperature > 0.0 && r->specific_enthalpy > 0.0 &&
+         r->velocity > 0.0;
 }
 
 int ensure_io(ChemHandle* c, long long n) {
@@ -216,6 +429,8 @@ PCFD_API int pcfd_chem_destroy(pcfd_chem_t h) {
   cudaFree(c->d_rho);
   cudaFree(c->d_T);
   cudaFree(c->d_w);
+  cudaFree(c->d_buf);
+  cudaFree(c->d_count);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -267,6 +482,82 @@ PCFD_API int pcfd_chem_production_rates(pcfd_chem_t h, long long n, const double
            "chem copy");
   CHEM_TRY(cudaStreamSynchronize(c->stream), "chem sync");
   return PCFD_OK;
+}
+
+#define CHEM_GRID(n) (unsigned)(((n) + 127) / 128), 128, 0, c->stream
+
+PCFD_API int pcfd_chem_find_T_given_P(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                      const double* P, const double* T_init, double* T, long long* nonconverged,
+                                      int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!rhoi || !P || !T_init || !T))) {
+    pcfd_set_last_error("pcfd_chem_find_T_given_P: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (nonconverged) *nonconverged = 0;
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const pcfd_chem_ref r = *ref;
+  return node_call<3, 1>(c, n, dev, {rhoi, P, T_init}, {ns, 1, 1}, {T}, {1}, nonconverged,
+                         [&](const double* const* in, double* const* out) {
+                           k_chem_find_T<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], in[2], out[0], c->d_count);
+                         });
+}
+
+PCFD_API int pcfd_chem_conservative_to_native(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* q,
+                                              const double* P, double* native, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!q || !P || !native))) {
+    pcfd_set_last_error("pcfd_chem_conservative_to_native: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const pcfd_chem_ref r = *ref;
+  long long bad = 0;
+  int rc = node_call<2, 1>(c, n, dev, {q, P}, {ns + 4, 1}, {native}, {4}, &bad,
+                           [&](const double* const* in, double* const* out) {
+                             k_chem_c2n<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], out[0], c->d_count);
+                           });
+  if (rc) return rc;
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_conservative_to_native: the temperature Newton iteration did not converge on " +
+                        std::to_string(bad) + " node(s)");
+    return PCFD_ERR_NUMERIC;
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_native_to_conservative(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                              const double* native, const double* P, double* q, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!rhoi || !native || !P || !q))) {
+    pcfd_set_last_error("pcfd_chem_native_to_conservative: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const pcfd_chem_ref r = *ref;
+  return node_call<3, 1>(c, n, dev, {rhoi, native, P}, {ns, 4, 1}, {q}, {4}, nullptr,
+                         [&](const double* const* in, double* const* out) {
+                           k_chem_n2c<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], in[2], out[0]);
+                         });
+}
+
+PCFD_API int pcfd_chem_aux(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* rhoi, const double* T,
+                           double* P, double* cvi, double* mol, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!rhoi || !T || !P || !cvi || !mol))) {
+    pcfd_set_last_error("pcfd_chem_aux: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const pcfd_chem_ref r = *ref;
+  return node_call<2, 3>(c, n, dev, {rhoi, T}, {ns, 1}, {P, cvi, mol}, {1, ns, ns}, nullptr,
+                         [&](const double* const* in, double* const* out) {
+                           k_chem_aux<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], out[0], out[1], out[2]);
+                         });
 }
 
 }  // extern "C"

@@ -39,3 +39,24 @@ def conservation(spec, w):
         a = np.array([ATOMS[nm][e] for nm in names])
         elem.append(np.abs((mol * a).sum(axis=1)) / ((np.abs(mol) * a).sum(axis=1) + 1e-300))
     return mass.max(), max(x.max() for x in elem)
+
+
+def reference_scales():
+    """Reference scales in the reference's style (ucs/param.tcc:372-397):
+    air at 300 K and 101325 Pa, velocity = speed of sound, density =
+    p / velocity^2, specific enthalpy = velocity^2."""
+    from proteuscfd_gb300.chem import ChemModel
+    v = (1.4 * 287.0 * 300.0) ** 0.5
+    return ChemModel.ref(101325.0 / v ** 2, 101325.0, 300.0 / 1.4, v * v, v)
+
+
+def fr_states(n, seed=2):
+    """Non-dimensional reacting node states: species densities, velocities,
+    T from 250 to 6000 K (scaled), and the pressure aux variable."""
+    rng = np.random.default_rng(seed)
+    ref = reference_scales()
+    ns = len(mechanism()["species"])
+    rhoi = (10.0 ** rng.uniform(-4, 0, size=(n, ns))) / ref.density
+    vel = rng.normal(size=(n, 3)) * 0.5
+    T = rng.uniform(250.0, 6000.0, size=n) / ref.temperature
+    return ref, rhoi, vel, T

@@ -49,6 +49,12 @@ def lib():
             "oracle_chem_rates_n": (None, [C.POINTER(N.ChemModelC), C.c_longlong, _DP, _DP, _DP]),
             "oracle_chem_kf": (C.c_double, [C.POINTER(N.ChemReaction), C.c_double]),
             "oracle_chem_kc": (C.c_double, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemReaction), C.c_double]),
+            "oracle_chem_find_T": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double,
+                                             C.c_double, _DP]),
+            "oracle_chem_c2n": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP]),
+            "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
+            "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
+                                       _DP]),
             "oracle_lp_nparam": (C.c_int, []),
             "oracle_lp_graph": (None, [MV, _IP, _IP, _FP]),
             "oracle_lp_features": (C.c_double, [C.c_int, _DP, _DP, _DP, _DP, C.c_double, _FP]),
@@ -283,3 +289,49 @@ def chem_rates(model_struct, rhoi, T):
     w = np.zeros_like(rhoi)
     lib().oracle_chem_rates_n(C.byref(model_struct), T.shape[0], dp(rhoi), dp(T), dp(w))
     return w
+
+
+class OracleChemState:
+    """The oracle's node state of the reacting equation set, node by node."""
+
+    def __init__(self, model_struct, ref):
+        self.m, self.ref, self.L = model_struct, ref, lib()
+        self.ns = model_struct.nspecies
+
+    def find_T(self, rhoi, P, T_init):
+        T, its = np.empty(len(P)), np.empty(len(P), dtype=int)
+        for k in range(len(P)):
+            t = C.c_double()
+            its[k] = self.L.oracle_chem_find_T(C.byref(self.m), C.byref(self.ref),
+                                               dp(np.ascontiguousarray(rhoi[k], np.float64)), float(P[k]),
+                                               float(T_init[k]), C.byref(t))
+            T[k] = t.value
+        return T, its
+
+    def c2n(self, q, P):
+        out, its = np.empty((len(P), 4)), np.empty(len(P), dtype=int)
+        for k in range(len(P)):
+            o = np.empty(4)
+            its[k] = self.L.oracle_chem_c2n(C.byref(self.m), C.byref(self.ref),
+                                            dp(np.ascontiguousarray(q[k], np.float64)), float(P[k]), dp(o))
+            out[k] = o
+        return out, its
+
+    def n2c(self, rhoi, native, P):
+        out = np.empty((len(P), 4))
+        for k in range(len(P)):
+            o = np.empty(4)
+            self.L.oracle_chem_n2c(C.byref(self.m), C.byref(self.ref), dp(np.ascontiguousarray(rhoi[k], np.float64)),
+                                   dp(np.ascontiguousarray(native[k], np.float64)), float(P[k]), dp(o))
+            out[k] = o
+        return out
+
+    def aux(self, rhoi, T):
+        n = len(T)
+        P, cvi, mol = np.empty(n), np.empty((n, self.ns)), np.empty((n, self.ns))
+        for k in range(n):
+            p, c, mo = C.c_double(), np.empty(self.ns), np.empty(self.ns)
+            self.L.oracle_chem_aux(C.byref(self.m), C.byref(self.ref), dp(np.ascontiguousarray(rhoi[k], np.float64)),
+                                   float(T[k]), C.byref(p), dp(c), dp(mo))
+            P[k], cvi[k], mol[k] = p.value, c, mo
+        return P, cvi, mol

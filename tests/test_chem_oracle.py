@@ -61,3 +61,44 @@ def test_oracle_dissociation_direction():
     w = chem_rates(m, rho, np.array([6000.0, 300.0]))
     assert w[0, 0] < 0 and w[0, 1] > 0
     assert w[1, 1] < 0 and w[1, 0] > 0
+
+
+def test_find_T_given_P_reference_known_answer():
+    """The reference's own test (unitTest/compressibleFRTest.h:6-29): 21 % of
+    1.161 kg/m^3 in species 0 and 79 % in species 2 (O2 and N in the 5-species
+    mechanism's order) at 101,200 Pa gives 166.5 K +- 0.01, and 83.25 K at
+    half the pressure, from a 150 K start."""
+    from chem_cases import reference_scales
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    assert [s["name"] for s in spec["species"]][0] == "O2" and spec["species"][2]["name"] == "N"
+    ref = reference_scales()
+    O = OracleChemState(model_struct(spec), ref)
+    rho = 1.161 / ref.density
+    rhoi = np.array([[0.21 * rho, 0.0, 0.79 * rho, 0.0, 0.0]] * 2)
+    T, its = O.find_T(rhoi, np.array([101200.0, 50600.0]) / ref.pressure, np.full(2, 150.0 / ref.temperature))
+    T *= ref.temperature
+    assert abs(T[0] - 166.5) < 0.01 and abs(T[1] - 166.5 / 2.0) < 0.01, T
+    assert np.all(its < 28)
+
+
+def test_fr_native_conservative_round_trip():
+    """NativeToConservative followed by ConservativeToNative (the FP64
+    temperature Newton from total energy) returns the temperature and
+    velocities; ComputeAuxiliaryVariables' pressure is Dalton's law."""
+    from chem_cases import fr_states
+    from oracle_lib import OracleChemState
+    ref, rhoi, vel, T = fr_states(200)
+    O = OracleChemState(model_struct(mechanism()), ref)
+    P, cvi, mol = O.aux(rhoi, T)
+    mw = np.array([s["MW"] for s in mechanism()["species"]])
+    R = 8.31447215 / mw
+    assert np.allclose(P * ref.pressure, (rhoi * ref.density * R).sum(axis=1) * T * ref.temperature, rtol=1e-14)
+    assert np.all(cvi > 0)
+    assert np.allclose(mol, rhoi / mw / 1000.0, rtol=0)
+    native = np.c_[vel, T]
+    qm = O.n2c(rhoi, native, P)
+    back, its = O.c2n(np.c_[rhoi, qm], P * 1.3)   # a stale pressure as the initial guess
+    assert np.all(its < 20)
+    assert np.allclose(back[:, 3], T, rtol=1e-11, atol=0)
+    assert np.allclose(back[:, :3], vel, rtol=1e-14, atol=1e-15)

@@ -44,3 +44,78 @@ def test_bad_model_rejected():
     bad = dict(spec, reactions=[dict(spec["reactions"][0], **{"global": [0, 1, 2, 3, 99]})])
     with pytest.raises(N.PcfdError):
         ChemModel(bad)
+
+
+def test_fr_find_T_given_P_known_answer_gpu():
+    """unitTest/compressibleFRTest.h:6-29 on the GPU: 166.5 K and 83.25 K
+    (+- 0.01), and the same values as the oracle."""
+    from chem_cases import reference_scales
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    ref = reference_scales()
+    C = ChemModel(spec)
+    rho = 1.161 / ref.density
+    rhoi = np.array([[0.21 * rho, 0.0, 0.79 * rho, 0.0, 0.0]] * 2)
+    P = np.array([101200.0, 50600.0]) / ref.pressure
+    T0 = np.full(2, 150.0 / ref.temperature)
+    T, bad = C.find_T_given_P(ref, rhoi, P, T0)
+    assert bad == 0
+    Td = T * ref.temperature
+    assert abs(Td[0] - 166.5) < 0.01 and abs(Td[1] - 83.25) < 0.01, Td
+    To, _ = OracleChemState(model_struct(spec), ref).find_T(rhoi, P, T0)
+    assert np.allclose(T, To, rtol=1e-14, atol=0)
+    C.close()
+
+
+def test_fr_node_state_parity():
+    """ComputeAuxiliaryVariables, NativeToConservative and the FP64
+    temperature Newton of ConservativeToNative against the oracle on 3,000
+    seeded states (250 to 6000 K), host arrays and device arrays."""
+    import torch
+    from chem_cases import fr_states
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    ref, rhoi, vel, T = fr_states(3000, seed=5)
+    C = ChemModel(spec)
+    O = OracleChemState(model_struct(spec), ref)
+    P, cvi, mol = C.aux(ref, rhoi, T)
+    Po, cvo, mo = O.aux(rhoi, T)
+    assert np.allclose(P, Po, rtol=1e-14, atol=0)
+    assert np.allclose(cvi, cvo, rtol=1e-13, atol=0)
+    assert np.allclose(mol, mo, rtol=1e-15, atol=0)
+    native = np.c_[vel, T]
+    qm = C.native_to_conservative(ref, rhoi, native, P)
+    qo = O.n2c(rhoi, native, Po)
+    assert np.allclose(qm, qo, rtol=1e-13, atol=1e-15)
+    q = np.c_[rhoi, qm]
+    Pst = P * 1.3   # a stale stored pressure as the initial guess
+    back = C.conservative_to_native(ref, q, Pst)
+    bo, its = O.c2n(q, Pst)
+    assert np.all(its < 20)
+    assert np.allclose(back, bo, rtol=1e-12, atol=1e-15)
+    assert np.allclose(back[:, 3], T, rtol=1e-11, atol=0)
+    # device arrays, in place on the handle's stream
+    dq = torch.from_numpy(q).cuda()
+    dP = torch.from_numpy(Pst).cuda()
+    dout = torch.empty((len(T), 4), dtype=torch.float64, device="cuda")
+    C.conservative_to_native_dev(ref, len(T), dq.data_ptr(), dP.data_ptr(), dout.data_ptr())
+    assert np.array_equal(dout.cpu().numpy(), back)
+    C.close()
+
+
+def test_fr_conservative_to_native_reports_nonconvergence():
+    """A total energy below every temperature's (negative internal energy)
+    leaves the Newton iteration unconverged after 20 iterations: the call
+    returns PCFD_ERR_NUMERIC, as the reference aborts."""
+    from chem_cases import fr_states
+    from proteuscfd_gb300 import _native as N
+    spec = mechanism()
+    ref, rhoi, vel, T = fr_states(4, seed=9)
+    C = ChemModel(spec)
+    P, _, _ = C.aux(ref, rhoi, T)
+    qm = C.native_to_conservative(ref, rhoi, np.c_[vel, T], P)
+    qm[1, 3] = -1.0e3 * abs(qm[1, 3])
+    with pytest.raises(N.PcfdError) as e:
+        C.conservative_to_native(ref, np.c_[rhoi, qm], P)
+    assert e.value.code == N.PCFD_ERR_NUMERIC
+    C.close()
