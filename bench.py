@@ -360,12 +360,41 @@ def chemistry_study(args):
     t0 = time.perf_counter()
     chem_rates(model_struct(spec), rho[:ns], T[:ns])
     tcpu = time.perf_counter() - t0
+    # the FP64 temperature Newton of ConservativeToNative on the same node
+    # count: device arrays, a stale stored pressure (x1.3) as the start
+    from chem_cases import fr_states
+    from oracle_lib import OracleChemState
+    ref, frho, vel, fT = fr_states(n, seed=6)
+    P, _, _ = c.aux(ref, frho, fT)
+    qm = c.native_to_conservative(ref, frho, np.c_[vel, fT], P)
+    q = np.ascontiguousarray(np.c_[frho, qm])
+    d_q = torch.from_numpy(q).cuda()
+    d_P = torch.from_numpy(P * 1.3).cuda()
+    d_out = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        c.conservative_to_native_dev(ref, n, d_q.data_ptr(), d_P.data_ptr(), d_out.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.conservative_to_native_dev(ref, n, d_q.data_ptr(), d_P.data_ptr(), d_out.data_ptr())
+    tn_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    tn_err = float(np.abs(d_out[:, 3].cpu().numpy() - fT).max() / fT.max())
+    nsn = 20000
+    O = OracleChemState(model_struct(spec), ref)
+    t0 = time.perf_counter()
+    O.c2n_batch(q[:nsn], P[:nsn] * 1.3)
+    tn_cpu = time.perf_counter() - t0
     c.close()
     return {"workload": "5-species air, 6 reactions (chemModels/5speciesAir.rxn), %d nodes, T 300-8000 K" % n,
             "mnodes_per_s": n / (ms_avg * 1e-3) / 1e6, "ms": ms_avg,
             "e2e_mnodes_per_s": n / e2e / 1e6,
             "cpu_baseline": {"mnodes_per_s": ns / tcpu / 1e6, "cores": 1, "kind": "port",
-                             "sample": "%d nodes by the oracle, 1 thread" % ns}}
+                             "sample": "%d nodes by the oracle, 1 thread" % ns},
+            "temperature_newton": {
+                "what": "ConservativeToNative: FP64 temperature Newton from total energy, %d nodes, 250-6000 K, "
+                        "stored pressure x1.3 as the start; wall time of the device-array call" % n,
+                "ms": tn_ms, "mnodes_per_s": n / (tn_ms * 1e-3) / 1e6, "max_rel_T_error": tn_err,
+                "cpu_baseline": {"mnodes_per_s": nsn / tn_cpu / 1e6, "cores": 1, "kind": "port",
+                                 "sample": "%d nodes by the oracle, 1 thread" % nsn}}}
 
 
 def wall_force(m, case, q):

@@ -228,3 +228,13 @@ void oracle_chem_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const d
     mol[i] = rhoi[i] / m->mw[i] / 1000.0;
   }
 }
+
+/* the same over n nodes (q [n][ns+4], P [n], native [n][4]); returns the
+ * number of nodes that used all 20 iterations */
+long long oracle_chem_c2n_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,
+                            const double* P, double* native) {
+  long long bad = 0;
+  for (long long p = 0; p < n; p++)
+    if (oracle_chem_c2n(m, ref, q + p * (m->nspecies + 4), P[p], native + p * 4) == 20) bad++;
+  return bad;
+}

@@ -63,6 +63,8 @@ void oracle_chem_rates_n(const pcfd_chem_model* m, long long n, const double* rh
 int oracle_chem_find_T(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double P, double Tinit,
                        double* T);
 int oracle_chem_c2n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* q, double P, double* native);
+long long oracle_chem_c2n_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,
+                            const double* P, double* native);
 void oracle_chem_n2c(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, const double* native,
                      double P, double* q);
 void oracle_chem_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T, double* P,

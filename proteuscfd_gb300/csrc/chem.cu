@@ -30,9 +30,21 @@ namespace {
 constexpr double kUnivR = 8.31447215;  // ucs/chem_constants.h:5
 constexpr double kPref = 101325.0;     // ucs/reaction.tcc:665
 
+// Per-species constants of the thermodynamic functions, formed once per
+// handle so that no FP64 division is left in the per-node loops: the species
+// gas constant R = R_univ / MW (Species::Init, ucs/species.tcc:315), and per
+// curve the enthalpy polynomial's coefficients (a5, a0, a1/2, a2/3, a3/4,
+// a4/5) and the cp polynomial's (a0..a4).
+struct ChemDerived {
+  double R[PCFD_CHEM_MAX_SPECIES];
+  double h[2][PCFD_CHEM_MAX_SPECIES][6];
+  double cp[2][PCFD_CHEM_MAX_SPECIES][5];
+};
+
 struct ChemHandle {
   pcfd_chem_model host;
   pcfd_chem_model* dev = nullptr;
+  ChemDerived* dder = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double *d_rho = nullptr, *d_T = nullptr, *d_w = nullptr;
@@ -155,39 +167,45 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
 
 // ---- node state of the reacting equation set ------------------------------
 
+// the curve of Species::GetThermoCoeff (ucs/species.tcc:96): the high set
+// above 1000 K (and above 6000 K, at the unpinned T), the low set otherwise
+__device__ __forceinline__ int curve(double T) { return (T > 1000.0) ? 1 : 0; }
+
 // Species<T>::GetCp and GetH (ucs/species.tcc:43,56; href = 0, :327), J/kg
-__device__ __forceinline__ double species_cp(const pcfd_chem_model& m, int s, double T) {
-  const double* a = thermo_coeff(m, s, T);
+__device__ __forceinline__ double species_cp(const ChemDerived& d, int s, double T) {
+  const double* a = d.cp[curve(T)][s];
   const double cp_R = a[0] + T * (a[1] + T * (a[2] + T * (a[3] + T * a[4])));
-  return cp_R * (kUnivR / m.mw[s]);
+  return cp_R * d.R[s];
 }
-__device__ __forceinline__ double species_h(const pcfd_chem_model& m, int s, double T) {
-  const double* a = thermo_coeff(m, s, T);
-  const double h_R = a[5] + T * (a[0] + T * (a[1] / 2.0 + T * (a[2] / 3.0 + T * (a[3] / 4.0 + T * a[4] / 5.0))));
-  return h_R * (kUnivR / m.mw[s]);
+__device__ __forceinline__ double species_h(const ChemDerived& d, int s, double T) {
+  const double* c = d.h[curve(T)][s];
+  const double h_R = c[0] + T * (c[1] + T * (c[2] + T * (c[3] + T * (c[4] + T * c[5]))));
+  return h_R * d.R[s];
 }
 // ChemModel::GetP (ucs/chem.tcc:989): Dalton's law over IdealGasEOS::GetP
-__device__ __forceinline__ double mix_P(const pcfd_chem_model& m, const double* rhoiDim, double T) {
+__device__ __forceinline__ double mix_P(const ChemDerived& d, int ns, const double* rhoiDim, double T) {
   double P = 0.0;
-  for (int i = 0; i < m.nspecies; i++) P += rhoiDim[i] * (kUnivR / m.mw[i]) * T;
+  for (int i = 0; i < ns; i++) P += rhoiDim[i] * d.R[i] * T;
   return P;
 }
 // ChemModel::GetSpecificEnthalpy (ucs/chem.tcc:586)
-__device__ __forceinline__ double mix_h(const pcfd_chem_model& m, const double* X, double T) {
+__device__ __forceinline__ double mix_h(const ChemDerived& d, int ns, const double* X, double T) {
   double h = 0.0;
-  for (int i = 0; i < m.nspecies; i++) h += species_h(m, i, T) * X[i];
+  for (int i = 0; i < ns; i++) h += species_h(d, i, T) * X[i];
   return h;
 }
 
 // NewtonFindTGivenP: the pressure is linear in T, so the finite-difference
 // Newton step lands in one or two iterations; counts nodes that used all 28
 __global__ void __launch_bounds__(128) k_chem_find_T(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                     const ChemDerived* __restrict__ gd,
                                                      pcfd_chem_ref ref, const double* __restrict__ rhoi,
                                                      const double* __restrict__ P, const double* __restrict__ Tinit,
                                                      double* __restrict__ Tout, long long* __restrict__ nonconv) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= n) return;
   const pcfd_chem_model& m = *gm;
+  const ChemDerived& d = *gd;
   const int ns = m.nspecies;
   double rhoiDim[PCFD_CHEM_MAX_SPECIES];
   for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[p * ns + i] * ref.density;
@@ -196,8 +214,8 @@ __global__ void __launch_bounds__(128) k_chem_find_T(long long n, const pcfd_che
   int j;
   for (j = 0; j < 28; j++) {
     const double TpDim = TDim + 1.0e-8;
-    const double zpoint = PgoalDim - mix_P(m, rhoiDim, TDim);
-    const double zpointp = PgoalDim - mix_P(m, rhoiDim, TpDim);
+    const double zpoint = PgoalDim - mix_P(d, ns, rhoiDim, TDim);
+    const double zpointp = PgoalDim - mix_P(d, ns, rhoiDim, TpDim);
     const double dzdT = (zpointp - zpoint) / (TpDim - TDim);
     const double dT = -zpoint / dzdT;
     if (fabs(dT / ref.temperature) < 1.0e-15) break;
@@ -210,19 +228,21 @@ __global__ void __launch_bounds__(128) k_chem_find_T(long long n, const pcfd_che
 // ConservativeToNative: the temperature Newton from total energy in FP64
 // (finite-difference slope, |dT| < 1e-12, at most 20 iterations)
 __global__ void __launch_bounds__(128) k_chem_c2n(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                     const ChemDerived* __restrict__ gd,
                                                   pcfd_chem_ref ref, const double* __restrict__ q,
                                                   const double* __restrict__ Pst, double* __restrict__ native,
                                                   long long* __restrict__ nonconv) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= n) return;
   const pcfd_chem_model& m = *gm;
+  const ChemDerived& d = *gd;
   const int ns = m.nspecies;
   const double* qp = q + p * (ns + 4);
   double rho = 0.0, R = 0.0, Y[PCFD_CHEM_MAX_SPECIES], rhoiDim[PCFD_CHEM_MAX_SPECIES];
   for (int i = 0; i < ns; i++) {
     rho += qp[i];
     rhoiDim[i] = qp[i] * ref.density;
-    R += rhoiDim[i] * (kUnivR / m.mw[i]);
+    R += rhoiDim[i] * d.R[i];
   }
   R /= ref.density * rho;
   for (int i = 0; i < ns; i++) Y[i] = qp[i] / rho;
@@ -234,10 +254,10 @@ __global__ void __launch_bounds__(128) k_chem_c2n(long long n, const pcfd_chem_m
   int j;
   for (j = 0; j < 20; j++) {
     const double Tp = T + 1.0e-8;
-    const double H = rho * (mix_h(m, Y, T * ref.temperature) / ref.specific_enthalpy);
-    const double Hp = rho * (mix_h(m, Y, Tp * ref.temperature) / ref.specific_enthalpy);
-    const double Pn = mix_P(m, rhoiDim, T * ref.temperature) / ref.pressure;
-    const double Pp = mix_P(m, rhoiDim, Tp * ref.temperature) / ref.pressure;
+    const double H = rho * (mix_h(d, ns, Y, T * ref.temperature) / ref.specific_enthalpy);
+    const double Hp = rho * (mix_h(d, ns, Y, Tp * ref.temperature) / ref.specific_enthalpy);
+    const double Pn = mix_P(d, ns, rhoiDim, T * ref.temperature) / ref.pressure;
+    const double Pp = mix_P(d, ns, rhoiDim, Tp * ref.temperature) / ref.pressure;
     const double zpoint = res - (H - Pn), zpointp = res - (Hp - Pp);
     const double dzdT = (zpointp - zpoint) / (Tp - T);
     const double dT = -zpoint / dzdT;
@@ -254,12 +274,14 @@ __global__ void __launch_bounds__(128) k_chem_c2n(long long n, const pcfd_chem_m
 
 // NativeToConservative with GetTotalEnergy (ucs/compressibleFR.tcc:1219)
 __global__ void __launch_bounds__(128) k_chem_n2c(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                     const ChemDerived* __restrict__ gd,
                                                   pcfd_chem_ref ref, const double* __restrict__ rhoi,
                                                   const double* __restrict__ native, const double* __restrict__ P,
                                                   double* __restrict__ q) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= n) return;
   const pcfd_chem_model& m = *gm;
+  const ChemDerived& d = *gd;
   const int ns = m.nspecies;
   double rho = 0.0, X[PCFD_CHEM_MAX_SPECIES];
   for (int i = 0; i < ns; i++) rho += rhoi[p * ns + i];
@@ -267,7 +289,7 @@ __global__ void __launch_bounds__(128) k_chem_n2c(long long n, const pcfd_chem_m
   const double* nv = native + p * 4;
   const double u = nv[0], v = nv[1], w = nv[2], T = nv[3];
   const double v2 = u * u + v * v + w * w;
-  const double h = mix_h(m, X, T * ref.temperature) / ref.specific_enthalpy;
+  const double h = mix_h(d, ns, X, T * ref.temperature) / ref.specific_enthalpy;
   const double E = h * rho - P[p];
   double* o = q + p * 4;
   o[0] = u * rho;
@@ -279,20 +301,22 @@ __global__ void __launch_bounds__(128) k_chem_n2c(long long n, const pcfd_chem_m
 // ComputeAuxiliaryVariables: pressure, species cv (Mayer's relation with the
 // species R, IdealGasEOS::GetCv, ucs/EOS.tcc:79) and concentrations
 __global__ void __launch_bounds__(128) k_chem_aux(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                     const ChemDerived* __restrict__ gd,
                                                   pcfd_chem_ref ref, const double* __restrict__ rhoi,
                                                   const double* __restrict__ T, double* __restrict__ Pout,
                                                   double* __restrict__ cvi, double* __restrict__ mol) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= n) return;
   const pcfd_chem_model& m = *gm;
+  const ChemDerived& d = *gd;
   const int ns = m.nspecies;
   double rhoiDim[PCFD_CHEM_MAX_SPECIES];
   for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[p * ns + i] * ref.density;
   const double TDim = T[p] * ref.temperature;
-  Pout[p] = mix_P(m, rhoiDim, TDim) / ref.pressure;
+  Pout[p] = mix_P(d, ns, rhoiDim, TDim) / ref.pressure;
   const double s_ref = ref.velocity * ref.velocity / ref.temperature;
   for (int i = 0; i < ns; i++) {
-    cvi[p * ns + i] = (species_cp(m, i, TDim) - kUnivR / m.mw[i]) / s_ref;
+    cvi[p * ns + i] = (species_cp(d, i, TDim) - d.R[i]) / s_ref;
     mol[p * ns + i] = rhoi[p * ns + i] / m.mw[i] / 1000.0;
   }
 }
@@ -412,6 +436,21 @@ PCFD_API int pcfd_chem_create(const pcfd_chem_model* model, pcfd_chem_t* out) {
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e == cudaSuccess) e = cudaMalloc(&c->dev, sizeof(pcfd_chem_model));
   if (e == cudaSuccess) e = cudaMemcpy(c->dev, model, sizeof(pcfd_chem_model), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    ChemDerived d;
+    std::memset(&d, 0, sizeof(d));
+    for (int s = 0; s < model->nspecies; s++) {
+      d.R[s] = kUnivR / model->mw[s];
+      for (int k = 0; k < 2; k++) {
+        const double* a = k ? model->nasa_hi[s] : model->nasa_lo[s];
+        const double hc[6] = {a[5], a[0], a[1] / 2.0, a[2] / 3.0, a[3] / 4.0, a[4] / 5.0};
+        for (int t = 0; t < 6; t++) d.h[k][s][t] = hc[t];
+        for (int t = 0; t < 5; t++) d.cp[k][s][t] = a[t];
+      }
+    }
+    e = cudaMalloc(&c->dder, sizeof(ChemDerived));
+    if (e == cudaSuccess) e = cudaMemcpy(c->dder, &d, sizeof(ChemDerived), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     int rc = cuda_fail(e, "pcfd_chem_create");
     pcfd_chem_destroy((pcfd_chem_t)c);
@@ -426,6 +465,7 @@ PCFD_API int pcfd_chem_destroy(pcfd_chem_t h) {
   if (!c) return PCFD_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   cudaFree(c->dev);
+  cudaFree(c->dder);
   cudaFree(c->d_rho);
   cudaFree(c->d_T);
   cudaFree(c->d_w);
@@ -500,7 +540,7 @@ PCFD_API int pcfd_chem_find_T_given_P(pcfd_chem_t h, const pcfd_chem_ref* ref, l
   const pcfd_chem_ref r = *ref;
   return node_call<3, 1>(c, n, dev, {rhoi, P, T_init}, {ns, 1, 1}, {T}, {1}, nonconverged,
                          [&](const double* const* in, double* const* out) {
-                           k_chem_find_T<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], in[2], out[0], c->d_count);
+                           k_chem_find_T<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], in[2], out[0], c->d_count);
                          });
 }
 
@@ -517,7 +557,7 @@ PCFD_API int pcfd_chem_conservative_to_native(pcfd_chem_t h, const pcfd_chem_ref
   long long bad = 0;
   int rc = node_call<2, 1>(c, n, dev, {q, P}, {ns + 4, 1}, {native}, {4}, &bad,
                            [&](const double* const* in, double* const* out) {
-                             k_chem_c2n<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], out[0], c->d_count);
+                             k_chem_c2n<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], out[0], c->d_count);
                            });
   if (rc) return rc;
   if (bad) {
@@ -540,7 +580,7 @@ PCFD_API int pcfd_chem_native_to_conservative(pcfd_chem_t h, const pcfd_chem_ref
   const pcfd_chem_ref r = *ref;
   return node_call<3, 1>(c, n, dev, {rhoi, native, P}, {ns, 4, 1}, {q}, {4}, nullptr,
                          [&](const double* const* in, double* const* out) {
-                           k_chem_n2c<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], in[2], out[0]);
+                           k_chem_n2c<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], in[2], out[0]);
                          });
 }
 
@@ -556,7 +596,7 @@ PCFD_API int pcfd_chem_aux(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n,
   const pcfd_chem_ref r = *ref;
   return node_call<2, 3>(c, n, dev, {rhoi, T}, {ns, 1}, {P, cvi, mol}, {1, ns, ns}, nullptr,
                          [&](const double* const* in, double* const* out) {
-                           k_chem_aux<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], out[0], out[1], out[2]);
+                           k_chem_aux<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], out[0], out[1], out[2]);
                          });
 }
 

@@ -52,6 +52,8 @@ def lib():
             "oracle_chem_find_T": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double,
                                              C.c_double, _DP]),
             "oracle_chem_c2n": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP]),
+            "oracle_chem_c2n_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_longlong, _DP,
+                                                 _DP, _DP]),
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
@@ -316,6 +318,14 @@ class OracleChemState:
                                             dp(np.ascontiguousarray(q[k], np.float64)), float(P[k]), dp(o))
             out[k] = o
         return out, its
+
+    def c2n_batch(self, q, P):
+        """c2n over all nodes in one oracle call; returns (native, nodes not converged)."""
+        q = np.ascontiguousarray(q, np.float64)
+        P = np.ascontiguousarray(P, np.float64)
+        out = np.empty((len(P), 4))
+        bad = self.L.oracle_chem_c2n_n(C.byref(self.m), C.byref(self.ref), len(P), dp(q), dp(P), dp(out))
+        return out, bad
 
     def n2c(self, rhoi, native, P):
         out = np.empty((len(P), 4))
