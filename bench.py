@@ -383,12 +383,42 @@ def chemistry_study(args):
     t0 = time.perf_counter()
     O.c2n_batch(q[:nsn], P[:nsn] * 1.3)
     tn_cpu = time.perf_counter() - t0
+    # the reacting inviscid edge flux (HLLC) over the edges of the
+    # 160x112x112 box (2,007,040 nodes), device arrays
+    from proteuscfd_gb300 import Mesh
+    from chem_cases import fr_records
+    mesh = Mesh.box(160, 112, 112, jitter=0.2, seed=2)
+    ne = mesh.nedge
+    ea = np.asarray(mesh.edge_area)
+    avec = np.ascontiguousarray(ea)
+    recs = c.node_records(ref, frho, vel, fT)
+    d_rec = torch.from_numpy(recs).cuda()
+    d_e = torch.from_numpy(np.ascontiguousarray(np.asarray(mesh.edges, dtype=np.int32))).cuda()
+    d_a = torch.from_numpy(avec).cuda()
+    d_f = torch.empty((ne, len(spec["species"]) + 4), dtype=torch.float64, device="cuda")
+    fopts = c.flux_opts(1.0, 0.0, 0)
+    for _ in range(3):
+        c.hllc_flux_dev(ref, fopts, n, d_rec.data_ptr(), ne, d_e.data_ptr(), d_a.data_ptr(), d_f.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.hllc_flux_dev(ref, fopts, n, d_rec.data_ptr(), ne, d_e.data_ptr(), d_a.data_ptr(), d_f.data_ptr())
+    hl_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    nse = 20000
+    t0 = time.perf_counter()
+    O.hllc_batch(fopts, recs, np.asarray(mesh.edges[:nse], dtype=np.int32), avec[:nse])
+    hl_cpu = time.perf_counter() - t0
     c.close()
     return {"workload": "5-species air, 6 reactions (chemModels/5speciesAir.rxn), %d nodes, T 300-8000 K" % n,
             "mnodes_per_s": n / (ms_avg * 1e-3) / 1e6, "ms": ms_avg,
             "e2e_mnodes_per_s": n / e2e / 1e6,
             "cpu_baseline": {"mnodes_per_s": ns / tcpu / 1e6, "cores": 1, "kind": "port",
                              "sample": "%d nodes by the oracle, 1 thread" % ns},
+            "hllc_flux": {
+                "what": "CompressibleFREqnSet::HLLCFlux over the %d edges of the 160x112x112 box (%d node records, "
+                        "random states as above), FP64; wall time of the device-array call" % (ne, n),
+                "ms": hl_ms, "medges_per_s": ne / (hl_ms * 1e-3) / 1e6,
+                "cpu_baseline": {"medges_per_s": nse / hl_cpu / 1e6, "cores": 1, "kind": "port",
+                                 "sample": "%d edges by the oracle, 1 thread" % nse}},
             "temperature_newton": {
                 "what": "ConservativeToNative: FP64 temperature Newton from total energy, %d nodes, 250-6000 K, "
                         "stored pressure x1.3 as the start; wall time of the device-array call" % n,

@@ -384,6 +384,24 @@ PCFD_API int pcfd_chem_native_to_conservative(pcfd_chem_t c, const pcfd_chem_ref
  * [n][ns], concentrations [n][ns] (ChemModel::MassToMole, ucs/chem.tcc:980). */
 PCFD_API int pcfd_chem_aux(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi, const double* T,
                            double* P, double* cvi, double* mol, int dev);
+/* Options of the reacting inviscid flux: beta of the eigenvalue
+ * modification (1 = none; Gupta's low-Mach form otherwise), the reference
+ * gauge pressure Pref (GetPressure(Qinf), ucs/compressibleFR.tcc:1517) and
+ * Param::symmetry2D (0 off, 1..3 zero the x, y or z momentum flux). */
+typedef struct {
+  double beta, pref;
+  int symmetry2D;
+} pcfd_chem_flux_opts;
+/* CompressibleFREqnSet::HLLCFlux (ucs/compressibleFR.tcc:301; RoeFlux
+ * forwards to it, :293) on a static grid: q [nnode][6 + 3 ns] node records
+ * (rhoi, u, v, w, T | P, rho, cvi, concentrations, as ComputeAuxiliaryVariables
+ * leaves them), edges [nedge][2] (left, right), avec [nedge][4] (unit normal,
+ * area) -> flux [nedge][ns + 4] out of the left node.  *nfail (optional)
+ * counts edges whose wave speeds left no HLLC branch (the reference's soft
+ * abort); their flux is zero and the call returns PCFD_ERR_NUMERIC. */
+PCFD_API int pcfd_chem_hllc_flux(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, long long nnode,
+                                 const double* q, long long nedge, const int* edges, const double* avec, double* flux,
+                                 long long* nfail, int dev);
 
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1

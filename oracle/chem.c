@@ -238,3 +238,128 @@ long long oracle_chem_c2n_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, 
     if (oracle_chem_c2n(m, ref, q + p * (m->nspecies + 4), P[p], native + p * 4) == 20) bad++;
   return bad;
 }
+
+/* ChemModel::GetFluidProperties (ucs/chem.tcc:545) through
+ * CompressibleFREqnSet::GetFluidProperties (ucs/compressibleFR.tcc:1523):
+ * the non-dimensional speed of sound squared of a node record */
+static double fr_c2(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T) {
+  const int ns = m->nspecies;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES], X[PCFD_CHEM_MAX_SPECIES];
+  double Tdim = T * ref->temperature;
+  double rho = 0.0, R = 0.0;
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[i] * ref->density;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  for (int i = 0; i < ns; i++) R += rhoiDim[i] * (UNIV_R_ / m->mw[i]);
+  R /= rho;
+  for (int i = 0; i < ns; i++) X[i] = rhoiDim[i] / rho;
+  double cp = 0.0, cv = 0.0;
+  for (int i = 0; i < ns; i++) cp += species_cp(m, i, Tdim) * X[i];
+  for (int i = 0; i < ns; i++) cv += X[i] * (species_cp(m, i, Tdim) - UNIV_R_ / m->mw[i]);
+  double gamma = cp / cv;
+  double c2Dim = gamma * R * Tdim;
+  return c2Dim / (ref->velocity * ref->velocity);
+}
+
+/* GetTotalEnthalpy (ucs/compressibleFR.tcc:1249) */
+static double fr_Ht(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q) {
+  const int ns = m->nspecies;
+  double X[PCFD_CHEM_MAX_SPECIES];
+  double T = Q[ns + 3], rho = Q[ns + 5], u = Q[ns], v = Q[ns + 1], w = Q[ns + 2];
+  double v2 = u * u + v * v + w * w;
+  for (int i = 0; i < ns; i++) X[i] = Q[i] / rho;
+  double h = mix_h(m, X, T * ref->temperature) / ref->specific_enthalpy;
+  return h * rho + 0.5 * rho * v2;
+}
+
+/* CompressibleFREqnSet::HLLCFlux (ucs/compressibleFR.tcc:301), vdotn = 0;
+ * returns 1 when no branch applies (the reference's soft abort; flux = 0) */
+int oracle_chem_hllc(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                     const double* QL, const double* QR, const double* avec, double* flux) {
+  const int ns = m->nspecies;
+  const double beta = o->beta, Pref = o->pref;
+  const double *rhoiL = QL, *rhoiR = QR;
+  double uL = QL[ns], vL = QL[ns + 1], wL = QL[ns + 2], TL = QL[ns + 3], pL = QL[ns + 4], rhoL = QL[ns + 5];
+  double uR = QR[ns], vR = QR[ns + 1], wR = QR[ns + 2], TR = QR[ns + 3], pR = QR[ns + 4], rhoR = QR[ns + 5];
+  double pgL = pL - Pref, pgR = pR - Pref;
+  double c2L = fr_c2(m, ref, rhoiL, TL), c2R = fr_c2(m, ref, rhoiR, TR);
+  double ETL = fr_Ht(m, ref, QL) - pL, ETR = fr_Ht(m, ref, QR) - pR;
+  double thetaL = uL * avec[0] + vL * avec[1] + wL * avec[2];
+  double thetaR = uR * avec[0] + vR * avec[1] + wR * avec[2];
+  /* Roe-averaged record (ComputeAuxiliaryVariables on it, :755) */
+  double rho = sqrt(rhoL * rhoR);
+  double sigma = rho / (rhoL + rho);
+  double roe[6 + 3 * PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) roe[i] = rhoiL[i] + sigma * (rhoiR[i] - rhoiL[i]);
+  double u = uL + sigma * (uR - uL), v = vL + sigma * (vR - vL), w = wL + sigma * (wR - wL);
+  double T = TL + sigma * (TR - TL);
+  double theta = u * avec[0] + v * avec[1] + w * avec[2];
+  double c2 = fr_c2(m, ref, roe, T);
+  double oneMBeta = 1.0 - beta;
+  double thetaPrime = theta * (1.0 + beta) * 0.5;
+  double cPrime = 0.5 * sqrt(theta * theta * (oneMBeta * oneMBeta) + 4.0 * beta * c2);
+  double thetaLPrime = thetaL * (1.0 + beta) * 0.5, thetaRPrime = thetaR * (1.0 + beta) * 0.5;
+  double cLPrime = 0.5 * sqrt(thetaL * thetaL * (oneMBeta * oneMBeta) + 4.0 * beta * c2L);
+  double cRPrime = 0.5 * sqrt(thetaR * thetaR * (oneMBeta * oneMBeta) + 4.0 * beta * c2R);
+  double eig5L = thetaLPrime - cLPrime, eig4R = thetaRPrime + cRPrime;
+  double eig4 = thetaPrime + cPrime, eig5 = thetaPrime - cPrime;
+  double SL = (eig5L < eig5) ? eig5L : eig5;
+  double SR = (eig4R > eig4) ? eig4R : eig4;
+  double SM = (pgR - pgL + rhoL * thetaL * (SL - thetaL) - rhoR * thetaR * (SR - thetaR)) /
+              (rhoL * (SL - thetaL) - rhoR * (SR - thetaR));
+  double Qf[PCFD_CHEM_MAX_SPECIES + 4], pStar = 0.0;
+  int fail = 0;
+  if (SL >= 0.0) {
+    for (int i = 0; i < ns; i++) Qf[i] = rhoiL[i];
+    Qf[ns] = rhoL * uL; Qf[ns + 1] = rhoL * vL; Qf[ns + 2] = rhoL * wL; Qf[ns + 3] = ETL;
+    pStar = pgL;
+    SM = thetaL;
+  } else if (SR <= 0.0) {
+    for (int i = 0; i < ns; i++) Qf[i] = rhoiR[i];
+    Qf[ns] = rhoR * uR; Qf[ns + 1] = rhoR * vR; Qf[ns + 2] = rhoR * wR; Qf[ns + 3] = ETR;
+    pStar = pgR;
+    SM = thetaR;
+  } else if (SL <= 0.0 && SM >= 0.0) {
+    pStar = pgL + rhoL * (thetaL - SL) * (thetaL - SM);
+    double omega = 1.0 / (SL - SM), const1 = SL - thetaL, const2 = pStar - pgL;
+    for (int i = 0; i < ns; i++) Qf[i] = omega * const1 * rhoiL[i];
+    Qf[ns] = omega * (const1 * rhoL * uL + const2 * avec[0]);
+    Qf[ns + 1] = omega * (const1 * rhoL * vL + const2 * avec[1]);
+    Qf[ns + 2] = omega * (const1 * rhoL * wL + const2 * avec[2]);
+    Qf[ns + 3] = omega * (const1 * ETL - pgL * thetaL + (pStar * SM)) + Pref * (SM - thetaL) * omega;
+  } else if (SM <= 0.0 && SR >= 0.0) {
+    pStar = pgR + rhoR * (thetaR - SR) * (thetaR - SM);
+    double omega = 1.0 / (SR - SM), const1 = SR - thetaR, const2 = pStar - pgR;
+    for (int i = 0; i < ns; i++) Qf[i] = omega * const1 * rhoiR[i];
+    Qf[ns] = omega * (const1 * rhoR * uR + const2 * avec[0]);
+    Qf[ns + 1] = omega * (const1 * rhoR * vR + const2 * avec[1]);
+    Qf[ns + 2] = omega * (const1 * rhoR * wR + const2 * avec[2]);
+    Qf[ns + 3] = omega * (const1 * ETR - pgR * thetaR + (pStar * SM)) + Pref * (SM - thetaR) * omega;
+  } else {
+    fail = 1;
+  }
+  if (fail) {
+    for (int i = 0; i < ns + 4; i++) flux[i] = 0.0;
+    return 1;
+  }
+  double area = avec[3];
+  double thetabar = SM;  /* theta - vdotn on a static grid */
+  for (int i = 0; i < ns; i++) flux[i] = area * Qf[i] * SM;
+  flux[ns] = area * (Qf[ns] * SM + pStar * avec[0]);
+  flux[ns + 1] = area * (Qf[ns + 1] * SM + pStar * avec[1]);
+  flux[ns + 2] = area * (Qf[ns + 2] * SM + pStar * avec[2]);
+  flux[ns + 3] = area * (Qf[ns + 3] * SM + pStar * thetabar) + Pref * thetabar * area;
+  if (o->symmetry2D >= 1 && o->symmetry2D <= 3) flux[ns + o->symmetry2D - 1] = 0.0;
+  return 0;
+}
+
+/* the same over an edge list (q [nnode][6 + 3 ns], edges [E][2], avec
+ * [E][4], flux [E][ns + 4]); returns the number of failed edges */
+long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                             const double* q, long long nedge, const int* edges, const double* avec, double* flux) {
+  const int nv = 6 + 3 * m->nspecies;
+  long long bad = 0;
+  for (long long e = 0; e < nedge; e++)
+    bad += oracle_chem_hllc(m, ref, o, q + (size_t)edges[2 * e] * nv, q + (size_t)edges[2 * e + 1] * nv,
+                            avec + 4 * e, flux + e * (m->nspecies + 4));
+  return bad;
+}

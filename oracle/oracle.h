@@ -69,6 +69,10 @@ void oracle_chem_n2c(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const d
                      double P, double* q);
 void oracle_chem_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T, double* P,
                      double* cvi, double* mol);
+int oracle_chem_hllc(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                     const double* QL, const double* QR, const double* avec, double* flux);
+long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                             const double* q, long long nedge, const int* edges, const double* avec, double* flux);
 
 #ifdef __cplusplus
 }

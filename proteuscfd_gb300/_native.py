@@ -117,6 +117,11 @@ class ChemRef(C.Structure):
                 ("specific_enthalpy", C.c_double), ("velocity", C.c_double)]
 
 
+class ChemFluxOpts(C.Structure):
+    """pcfd_chem_flux_opts: beta, the gauge reference pressure, symmetry2D."""
+    _fields_ = [("beta", C.c_double), ("pref", C.c_double), ("symmetry2D", C.c_int)]
+
+
 _FP = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes); every symbol include/pcfd.h declares
@@ -164,6 +169,8 @@ PROTOTYPES = {
     "pcfd_chem_conservative_to_native": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, C.c_int]),
     "pcfd_chem_native_to_conservative": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, C.c_int]),
     "pcfd_chem_aux": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, _P, C.c_int]),
+    "pcfd_chem_hllc_flux": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_longlong, _P,
+                                      C.c_longlong, _P, _P, _P, C.POINTER(C.c_longlong), C.c_int]),
     "pcfd_chem_destroy": (C.c_int, [_P]),
     "pcfd_chem_production_rates": (C.c_int, [_P, C.c_longlong, _DP, _DP, _DP]),
     "pcfd_chem_production_rates_dev": (C.c_int, [_P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, _DP]),

@@ -137,6 +137,41 @@ class ChemModel:
                                         N.dptr(mol), 0), "pcfd_chem_aux")
         return P, cvi, mol
 
+    def node_records(self, ref, rhoi, vel, T):
+        """The reacting node record [n][6 + 3 ns] (rhoi, u, v, w, T, P, rho,
+        cvi, concentrations) that ComputeAuxiliaryVariables completes."""
+        n = len(T)
+        P, cvi, mol = self.aux(ref, rhoi, T)
+        rhoi = self._arr(rhoi, (n, self.nspecies))
+        return np.ascontiguousarray(np.c_[rhoi, np.asarray(vel, np.float64), T, P, rhoi.sum(axis=1), cvi, mol])
+
+    @staticmethod
+    def flux_opts(beta=1.0, pref=0.0, symmetry2D=0):
+        return N.ChemFluxOpts(beta, pref, symmetry2D)
+
+    def hllc_flux(self, ref, opts, q, edges, avec):
+        """HLLCFlux over an edge list: q [n][6 + 3 ns] node records, edges
+        [E][2] (left, right), avec [E][4] (unit normal, area) -> flux [E][ns + 4]."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        edges = np.ascontiguousarray(edges, dtype=np.int32)
+        avec = np.ascontiguousarray(avec, dtype=np.float64)
+        ne = len(edges)
+        if q.shape[1] != 6 + 3 * self.nspecies or edges.shape != (ne, 2) or avec.shape != (ne, 4):
+            raise ValueError("hllc_flux: bad shapes")
+        flux = np.empty((ne, self.nspecies + 4))
+        bad = C.c_longlong()
+        N.check(self._lib.pcfd_chem_hllc_flux(self._h, C.byref(ref), C.byref(opts), len(q), N.dptr(q), ne,
+                                              edges.ctypes.data_as(C.c_void_p), N.dptr(avec), N.dptr(flux),
+                                              C.byref(bad), 0), "pcfd_chem_hllc_flux")
+        return flux
+
+    def hllc_flux_dev(self, ref, opts, nnode, q_ptr, nedge, edges_ptr, avec_ptr, flux_ptr):
+        """The same on device addresses; returns the failure count."""
+        bad = C.c_longlong()
+        N.check(self._lib.pcfd_chem_hllc_flux(self._h, C.byref(ref), C.byref(opts), int(nnode), q_ptr, int(nedge),
+                                              edges_ptr, avec_ptr, flux_ptr, C.byref(bad), 1), "pcfd_chem_hllc_flux")
+        return bad.value
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pcfd_chem_destroy(self._h)

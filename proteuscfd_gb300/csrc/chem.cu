@@ -12,6 +12,8 @@
 //   CompressibleFREqnSet<T>::ConservativeToNative   ucs/compressibleFR.tcc:2133
 //   CompressibleFREqnSet<T>::NativeToConservative   ucs/compressibleFR.tcc:2117
 //   CompressibleFREqnSet<T>::ComputeAuxiliaryVariables ucs/compressibleFR.tcc:755
+// and its inviscid edge flux:
+//   CompressibleFREqnSet<T>::HLLCFlux               ucs/compressibleFR.tcc:301
 // The reference evaluates each reaction's rates once per species it
 // produces; here each reaction is evaluated once per node and its
 // contribution added to every species it changes, in reaction order, which
@@ -321,6 +323,145 @@ __global__ void __launch_bounds__(128) k_chem_aux(long long n, const pcfd_chem_m
   }
 }
 
+// ChemModel::GetFluidProperties (ucs/chem.tcc:545) through the equation
+// set's wrapper (ucs/compressibleFR.tcc:1523): the non-dimensional speed of
+// sound squared, gamma R T with the mixture's cp / cv
+__device__ __forceinline__ double fr_c2(const ChemDerived& d, int ns, const pcfd_chem_ref& ref, const double* rhoi,
+                                        double T) {
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  const double Tdim = T * ref.temperature;
+  double rho = 0.0, R = 0.0, cp = 0.0, cv = 0.0;
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[i] * ref.density;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  for (int i = 0; i < ns; i++) R += rhoiDim[i] * d.R[i];
+  R /= rho;
+  for (int i = 0; i < ns; i++) {
+    const double X = rhoiDim[i] / rho;
+    const double cpi = species_cp(d, i, Tdim);
+    cp += cpi * X;
+    cv += X * (cpi - d.R[i]);
+  }
+  const double gamma = cp / cv;
+  return gamma * R * Tdim / (ref.velocity * ref.velocity);
+}
+
+// GetTotalEnthalpy (ucs/compressibleFR.tcc:1249) of a node record
+__device__ __forceinline__ double fr_Ht(const ChemDerived& d, int ns, const pcfd_chem_ref& ref, const double* Q) {
+  double X[PCFD_CHEM_MAX_SPECIES];
+  const double T = Q[ns + 3], rho = Q[ns + 5], u = Q[ns], v = Q[ns + 1], w = Q[ns + 2];
+  const double v2 = u * u + v * v + w * w;
+  for (int i = 0; i < ns; i++) X[i] = Q[i] / rho;
+  const double h = mix_h(d, ns, X, T * ref.temperature) / ref.specific_enthalpy;
+  return h * rho + 0.5 * rho * v2;
+}
+
+// HLLC flux of one edge on a static grid (vdotn = 0), in FP64; the wave
+// speeds are the Roe-averaged and one-sided eigenvalues with Gupta's beta
+// modification.  Writes zeros and returns 1 when no branch applies.
+__device__ int fr_hllc(const ChemDerived& d, int ns, const pcfd_chem_ref& ref, const pcfd_chem_flux_opts& o,
+                       const double* QL, const double* QR, const double4 a, double* flux) {
+  const double beta = o.beta, Pref = o.pref;
+  const double uL = QL[ns], vL = QL[ns + 1], wL = QL[ns + 2], TL = QL[ns + 3], pL = QL[ns + 4], rhoL = QL[ns + 5];
+  const double uR = QR[ns], vR = QR[ns + 1], wR = QR[ns + 2], TR = QR[ns + 3], pR = QR[ns + 4], rhoR = QR[ns + 5];
+  const double pgL = pL - Pref, pgR = pR - Pref;
+  const double c2L = fr_c2(d, ns, ref, QL, TL), c2R = fr_c2(d, ns, ref, QR, TR);
+  const double ETL = fr_Ht(d, ns, ref, QL) - pL, ETR = fr_Ht(d, ns, ref, QR) - pR;
+  const double thetaL = uL * a.x + vL * a.y + wL * a.z;
+  const double thetaR = uR * a.x + vR * a.y + wR * a.z;
+  const double rho = sqrt(rhoL * rhoR);
+  const double sigma = rho / (rhoL + rho);
+  double roe[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) roe[i] = QL[i] + sigma * (QR[i] - QL[i]);
+  const double u = uL + sigma * (uR - uL), v = vL + sigma * (vR - vL), w = wL + sigma * (wR - wL);
+  const double T = TL + sigma * (TR - TL);
+  const double theta = u * a.x + v * a.y + w * a.z;
+  const double c2 = fr_c2(d, ns, ref, roe, T);
+  const double oneMBeta = 1.0 - beta;
+  const double thetaPrime = theta * (1.0 + beta) * 0.5;
+  const double cPrime = 0.5 * sqrt(theta * theta * (oneMBeta * oneMBeta) + 4.0 * beta * c2);
+  const double thetaLPrime = thetaL * (1.0 + beta) * 0.5, thetaRPrime = thetaR * (1.0 + beta) * 0.5;
+  const double cLPrime = 0.5 * sqrt(thetaL * thetaL * (oneMBeta * oneMBeta) + 4.0 * beta * c2L);
+  const double cRPrime = 0.5 * sqrt(thetaR * thetaR * (oneMBeta * oneMBeta) + 4.0 * beta * c2R);
+  const double eig5L = thetaLPrime - cLPrime, eig4R = thetaRPrime + cRPrime;
+  const double eig4 = thetaPrime + cPrime, eig5 = thetaPrime - cPrime;
+  const double SL = (eig5L < eig5) ? eig5L : eig5;
+  const double SR = (eig4R > eig4) ? eig4R : eig4;
+  double SM = (pgR - pgL + rhoL * thetaL * (SL - thetaL) - rhoR * thetaR * (SR - thetaR)) /
+              (rhoL * (SL - thetaL) - rhoR * (SR - thetaR));
+  // the state of the chosen HLLC region: species densities scaled by sf of
+  // side s, momentum and energy as below
+  const double* Qs;
+  double sf, m0, m1, m2, Et, pStar;
+  if (SL >= 0.0) {
+    Qs = QL; sf = 1.0;
+    m0 = rhoL * uL; m1 = rhoL * vL; m2 = rhoL * wL; Et = ETL;
+    pStar = pgL;
+    SM = thetaL;
+  } else if (SR <= 0.0) {
+    Qs = QR; sf = 1.0;
+    m0 = rhoR * uR; m1 = rhoR * vR; m2 = rhoR * wR; Et = ETR;
+    pStar = pgR;
+    SM = thetaR;
+  } else if (SL <= 0.0 && SM >= 0.0) {
+    pStar = pgL + rhoL * (thetaL - SL) * (thetaL - SM);
+    const double omega = 1.0 / (SL - SM), const1 = SL - thetaL, const2 = pStar - pgL;
+    Qs = QL; sf = omega * const1;
+    m0 = omega * (const1 * rhoL * uL + const2 * a.x);
+    m1 = omega * (const1 * rhoL * vL + const2 * a.y);
+    m2 = omega * (const1 * rhoL * wL + const2 * a.z);
+    Et = omega * (const1 * ETL - pgL * thetaL + (pStar * SM)) + Pref * (SM - thetaL) * omega;
+  } else if (SM <= 0.0 && SR >= 0.0) {
+    pStar = pgR + rhoR * (thetaR - SR) * (thetaR - SM);
+    const double omega = 1.0 / (SR - SM), const1 = SR - thetaR, const2 = pStar - pgR;
+    Qs = QR; sf = omega * const1;
+    m0 = omega * (const1 * rhoR * uR + const2 * a.x);
+    m1 = omega * (const1 * rhoR * vR + const2 * a.y);
+    m2 = omega * (const1 * rhoR * wR + const2 * a.z);
+    Et = omega * (const1 * ETR - pgR * thetaR + (pStar * SM)) + Pref * (SM - thetaR) * omega;
+  } else {
+    for (int i = 0; i < ns + 4; i++) flux[i] = 0.0;
+    return 1;
+  }
+  const double area = a.w;
+  for (int i = 0; i < ns; i++) flux[i] = area * (sf * Qs[i]) * SM;
+  flux[ns] = area * (m0 * SM + pStar * a.x);
+  flux[ns + 1] = area * (m1 * SM + pStar * a.y);
+  flux[ns + 2] = area * (m2 * SM + pStar * a.z);
+  flux[ns + 3] = area * (Et * SM + pStar * SM) + Pref * SM * area;
+  if (o.symmetry2D >= 1 && o.symmetry2D <= 3) flux[ns + o.symmetry2D - 1] = 0.0;
+  return 0;
+}
+
+// one thread per edge; the two node records are read as consecutive
+// doubles (6 + 3 ns per node)
+__global__ void __launch_bounds__(128) k_chem_hllc(long long nedge, long long nnode,
+                                                   const pcfd_chem_model* __restrict__ gm,
+                                                   const ChemDerived* __restrict__ gd, pcfd_chem_ref ref,
+                                                   pcfd_chem_flux_opts o, const double* __restrict__ q,
+                                                   const int2* __restrict__ edges, const double4* __restrict__ avec,
+                                                   double* __restrict__ flux, long long* __restrict__ nfail) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int ns = gm->nspecies;
+  const int nv = 6 + 3 * ns;
+  const int2 n = edges[e];
+  if (n.x < 0 || n.y < 0 || n.x >= nnode || n.y >= nnode) {
+    // an edge naming a node outside the record array: no access, counted
+    for (int i = 0; i < ns + 4; i++) flux[e * (ns + 4) + i] = 0.0;
+    atomicAdd((unsigned long long*)nfail, 1ull);
+    return;
+  }
+  double QL[6 + 2 * PCFD_CHEM_MAX_SPECIES], QR[6 + 2 * PCFD_CHEM_MAX_SPECIES];
+  // the flux reads the record up to rho (ns + 6 values)
+  for (int i = 0; i < ns + 6; i++) {
+    QL[i] = q[(size_t)n.x * nv + i];
+    QR[i] = q[(size_t)n.y * nv + i];
+  }
+  double f[PCFD_CHEM_MAX_SPECIES + 4];
+  if (fr_hllc(*gd, ns, ref, o, QL, QR, avec[e], f)) atomicAdd((unsigned long long*)nfail, 1ull);
+  for (int i = 0; i < ns + 4; i++) flux[e * (ns + 4) + i] = f[i];
+}
+
 int validate(const pcfd_chem_model* m) {
   if (m->nspecies < 1 || m->nspecies > PCFD_CHEM_MAX_SPECIES || m->nreactions < 0 ||
       m->nreactions > PCFD_CHEM_MAX_REACTIONS)
@@ -598,6 +739,73 @@ PCFD_API int pcfd_chem_aux(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n,
                          [&](const double* const* in, double* const* out) {
                            k_chem_aux<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], out[0], out[1], out[2]);
                          });
+}
+
+PCFD_API int pcfd_chem_hllc_flux(pcfd_chem_t h, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, long long nnode,
+                                 const double* q, long long nedge, const int* edges, const double* avec, double* flux,
+                                 long long* nfail, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || !o || nnode < 0 || nedge < 0 ||
+      (nedge > 0 && (nnode <= 0 || !q || !edges || !avec || !flux))) {
+    pcfd_set_last_error("pcfd_chem_hllc_flux: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (nfail) *nfail = 0;
+  if (nedge == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  if (!dev) {
+    // the node ids are checked here; device callers own their edge list
+    for (long long e = 0; e < 2 * nedge; e++)
+      if (edges[e] < 0 || edges[e] >= nnode) {
+        pcfd_set_last_error("pcfd_chem_hllc_flux: edge node id out of range");
+        return PCFD_ERR_ARG;
+      }
+  }
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  const double* dq = q;
+  const int2* de = (const int2*)edges;
+  const double4* da = (const double4*)avec;
+  double* df = flux;
+  if (!dev) {
+    // staging: avec first (the double4 loads want 32-byte alignment; the
+    // buffer is 256-byte aligned), then q, flux and the edge ids
+    const size_t need = (size_t)nedge * 4 + (size_t)nnode * nv + (size_t)nedge * (ns + 4) + (size_t)nedge;
+    int rc = ensure_buf(c, need);
+    if (rc) return rc;
+    double* b = c->d_buf;
+    CHEM_TRY(cudaMemcpyAsync(b, avec, (size_t)nedge * 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream), "chem copy");
+    da = (const double4*)b;
+    b += (size_t)nedge * 4;
+    CHEM_TRY(cudaMemcpyAsync(b, q, (size_t)nnode * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream), "chem copy");
+    dq = b;
+    b += (size_t)nnode * nv;
+    df = b;
+    b += (size_t)nedge * (ns + 4);
+    CHEM_TRY(cudaMemcpyAsync(b, edges, (size_t)nedge * 2 * sizeof(int), cudaMemcpyHostToDevice, c->stream), "chem copy");
+    de = (const int2*)b;
+  } else if ((reinterpret_cast<uintptr_t>(avec) & 31) != 0 || (reinterpret_cast<uintptr_t>(edges) & 7) != 0) {
+    pcfd_set_last_error("pcfd_chem_hllc_flux: device avec must be 32-byte and edges 8-byte aligned");
+    return PCFD_ERR_ARG;
+  }
+  const pcfd_chem_ref r = *ref;
+  const pcfd_chem_flux_opts oo = *o;
+  k_chem_hllc<<<CHEM_GRID(nedge)>>>(nedge, nnode, c->dev, c->dder, r, oo, dq, de, da, df, c->d_count);
+  CHEM_TRY(cudaGetLastError(), "k_chem_hllc launch");
+  if (!dev)
+    CHEM_TRY(cudaMemcpyAsync(flux, df, (size_t)nedge * (ns + 4) * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  long long bad = 0;
+  CHEM_TRY(cudaMemcpyAsync(&bad, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "k_chem_hllc");
+  if (nfail) *nfail = bad;
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_hllc_flux: " + std::to_string(bad) +
+                        " edge(s) with no HLLC branch or a node id out of range");
+    return PCFD_ERR_NUMERIC;
+  }
+  return PCFD_OK;
 }
 
 }  // extern "C"

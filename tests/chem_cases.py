@@ -60,3 +60,20 @@ def fr_states(n, seed=2):
     vel = rng.normal(size=(n, 3)) * 0.5
     T = rng.uniform(250.0, 6000.0, size=n) / ref.temperature
     return ref, rhoi, vel, T
+
+
+def fr_edges(nnode, nedge, seed=3):
+    """Random node pairs with unit normals and areas."""
+    rng = np.random.default_rng(seed)
+    e = rng.integers(0, nnode, size=(nedge, 2)).astype(np.int32)
+    nrm = rng.normal(size=(nedge, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    return e, np.c_[nrm, rng.uniform(0.1, 2.0, size=nedge)]
+
+
+def fr_records(ref, rhoi, vel, T):
+    """Node records through the oracle's ComputeAuxiliaryVariables."""
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300.chem import model_struct
+    P, cvi, mol = OracleChemState(model_struct(mechanism()), ref).aux(rhoi, T)
+    return np.ascontiguousarray(np.c_[rhoi, vel, T, P, rhoi.sum(axis=1), cvi, mol])

@@ -54,6 +54,10 @@ def lib():
             "oracle_chem_c2n": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP]),
             "oracle_chem_c2n_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_longlong, _DP,
                                                  _DP, _DP]),
+            "oracle_chem_hllc": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.ChemFluxOpts),
+                                           _DP, _DP, _DP, _DP]),
+            "oracle_chem_hllc_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
+                                                  C.POINTER(N.ChemFluxOpts), _DP, C.c_longlong, _IP, _DP, _DP]),
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
@@ -345,3 +349,27 @@ class OracleChemState:
                                    float(T[k]), C.byref(p), dp(c), dp(mo))
             P[k], cvi[k], mol[k] = p.value, c, mo
         return P, cvi, mol
+
+    def hllc(self, opts, q, edges, avec):
+        """HLLCFlux edge by edge; returns (flux [E][ns + 4], failures)."""
+        ne = len(edges)
+        flux = np.empty((ne, self.ns + 4))
+        bad = 0
+        for e in range(ne):
+            f = np.empty(self.ns + 4)
+            bad += self.L.oracle_chem_hllc(C.byref(self.m), C.byref(self.ref), C.byref(opts),
+                                           dp(np.ascontiguousarray(q[edges[e][0]], np.float64)),
+                                           dp(np.ascontiguousarray(q[edges[e][1]], np.float64)),
+                                           dp(np.ascontiguousarray(avec[e], np.float64)), dp(f))
+            flux[e] = f
+        return flux, bad
+
+    def hllc_batch(self, opts, q, edges, avec):
+        """HLLCFlux over the edge list in one oracle call."""
+        q = np.ascontiguousarray(q, np.float64)
+        edges = np.ascontiguousarray(edges, np.int32)
+        avec = np.ascontiguousarray(avec, np.float64)
+        flux = np.empty((len(edges), self.ns + 4))
+        bad = self.L.oracle_chem_hllc_n(C.byref(self.m), C.byref(self.ref), C.byref(opts), dp(q), len(edges),
+                                        ip(edges), dp(avec), dp(flux))
+        return flux, bad

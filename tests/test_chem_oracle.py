@@ -102,3 +102,36 @@ def test_fr_native_conservative_round_trip():
     assert np.all(its < 20)
     assert np.allclose(back[:, 3], T, rtol=1e-11, atol=0)
     assert np.allclose(back[:, :3], vel, rtol=1e-14, atol=1e-15)
+
+
+def test_fr_hllc_consistency():
+    """HLLCFlux(Q, Q) is the physical flux: rho_i theta, rho u theta +
+    (p - Pref) n (the reference carries the gauge pressure in the momentum
+    flux), theta (rho Et + p), times the area; symmetry2D zeroes one momentum
+    component."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import _native as N
+    ref, rhoi, vel, T = fr_states(20, seed=11)
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(mechanism()), ref)
+    ns = O.ns
+    rng = np.random.default_rng(1)
+    nrm = rng.normal(size=(20, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    avec = np.c_[nrm, rng.uniform(0.5, 2.0, 20)]
+    pref = 0.7
+    for beta in (1.0, 0.3):
+        f, bad = O.hllc(N.ChemFluxOpts(beta, pref, 0), q, np.c_[np.arange(20), np.arange(20)], avec)
+        assert bad == 0
+        th = (vel * nrm).sum(axis=1)
+        rho = rhoi.sum(axis=1)
+        P = q[:, ns + 4]
+        X = rhoi / rho[:, None]
+        Et = O.n2c(rhoi, np.c_[vel, T], P)[:, 3]
+        ref_f = np.c_[rhoi * th[:, None], rho[:, None] * vel * th[:, None] + (P - pref)[:, None] * nrm,
+                      th * (Et + P)] * avec[:, 3:4]
+        scale = np.abs(ref_f).max(axis=1, keepdims=True)
+        assert np.abs(f - ref_f).max() <= 1e-12 * scale.max(), np.abs(f - ref_f).max()
+    f2, _ = O.hllc(N.ChemFluxOpts(1.0, pref, 2), q, np.c_[np.arange(20), np.arange(20)], avec)
+    assert np.all(f2[:, ns + 1] == 0.0)
