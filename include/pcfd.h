@@ -402,6 +402,20 @@ typedef struct {
 PCFD_API int pcfd_chem_hllc_flux(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, long long nnode,
                                  const double* q, long long nedge, const int* edges, const double* avec, double* flux,
                                  long long* nfail, int dev);
+/* Attaches a mesh (pcfd_mesh_view as for pcfd_create) to the chemistry
+ * handle for pcfd_chem_residual: edges, areas, boundary half-edges, dual
+ * volumes and the node -> edge lists are copied to HBM once. */
+PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t c, const pcfd_mesh_view* m);
+/* SpatialResidual (ucs/residual.tcc:66) of the reacting equation set, first
+ * order and inviscid, on the attached mesh: q [nnode + nbedge][6 + 3 ns]
+ * records, the phantom records after the nodes as the boundary conditions
+ * leave them -> b [nnode][ns + 4] (optional) = -sum of the HLLC fluxes out of
+ * each node (edges in ascending id, then boundary half-edges) + vol * wdot
+ * (SourceTerm, ucs/compressibleFR.tcc:1276, when reactions != 0; wdot made
+ * non-dimensional by ref_density / ref_time), and norms [1 + ns + 4]
+ * (optional; ParallelL2Norm and StridedParallelL2Norm).  dev as above (q, b). */
+PCFD_API int pcfd_chem_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                double ref_time, int reactions, const double* q, double* b, double* norms, int dev);
 
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1

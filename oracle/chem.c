@@ -363,3 +363,52 @@ long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref,
                             avec + 4 * e, flux + e * (m->nspecies + 4));
   return bad;
 }
+
+/* SpatialResidual (ucs/residual.tcc:66) of the reacting equation set,
+ * first order and inviscid: edge fluxes scattered as the Driver does (left
+ * node -flux, right node +flux), boundary half-edges against their phantom
+ * records (the Bdriver), then SourceTerm (ucs/compressibleFR.tcc:1276) with
+ * the production rates made non-dimensional by ref_density / ref_time; the
+ * norms of ComputeResiduals (ucs/residual.tcc:13, ParallelL2Norm). */
+void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                          const pcfd_mesh_view* mv, const double* q, double ref_time, int reactions, double* b,
+                          double* norms) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  const int nn = mv->nnode;
+  double flux[PCFD_CHEM_MAX_SPECIES + 4];
+  for (size_t i = 0; i < (size_t)nn * neqn; i++) b[i] = 0.0;
+  for (int e = 0; e < mv->nedge; e++) {
+    int a = mv->edges[2 * e], c = mv->edges[2 * e + 1];
+    oracle_chem_hllc(m, ref, o, q + (size_t)a * nv, q + (size_t)c * nv, mv->edge_area + 4 * (size_t)e, flux);
+    for (int i = 0; i < neqn; i++) b[(size_t)c * neqn + i] += flux[i];
+    for (int i = 0; i < neqn; i++) b[(size_t)a * neqn + i] += -flux[i];
+  }
+  for (int k = 0; k < mv->nbedge; k++) {
+    int a = mv->bedges[2 * k], c = mv->bedges[2 * k + 1];
+    oracle_chem_hllc(m, ref, o, q + (size_t)a * nv, q + (size_t)c * nv, mv->bedge_area + 4 * (size_t)k, flux);
+    for (int i = 0; i < neqn; i++) b[(size_t)a * neqn + i] += -flux[i];
+  }
+  if (reactions) {
+    double rhoi[PCFD_CHEM_MAX_SPECIES], wdot[PCFD_CHEM_MAX_SPECIES];
+    for (int n = 0; n < nn; n++) {
+      const double* Q = q + (size_t)n * nv;
+      double T = Q[ns + 3] * ref->temperature;
+      for (int i = 0; i < ns; i++) rhoi[i] = Q[i] * ref->density;
+      oracle_chem_rates(m, rhoi, T, wdot);
+      for (int i = 0; i < ns; i++) {
+        wdot[i] /= (ref->density / ref_time);
+        b[(size_t)n * neqn + i] += mv->vol[n] * wdot[i];
+      }
+    }
+  }
+  if (norms) {
+    double s = 0.0;
+    for (size_t i = 0; i < (size_t)nn * neqn; i++) s += b[i] * b[i];
+    norms[0] = sqrt(s) / (double)((size_t)nn * neqn);
+    for (int j = 0; j < neqn; j++) {
+      double t = 0.0;
+      for (int i = 0; i < nn; i++) t += b[(size_t)i * neqn + j] * b[(size_t)i * neqn + j];
+      norms[1 + j] = sqrt(t) / (double)nn;
+    }
+  }
+}

@@ -73,6 +73,9 @@ int oracle_chem_hllc(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const p
                      const double* QL, const double* QR, const double* avec, double* flux);
 long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
                              const double* q, long long nedge, const int* edges, const double* avec, double* flux);
+void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                          const pcfd_mesh_view* mv, const double* q, double ref_time, int reactions, double* b,
+                          double* norms);
 
 #ifdef __cplusplus
 }

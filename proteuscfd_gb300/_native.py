@@ -171,6 +171,9 @@ PROTOTYPES = {
     "pcfd_chem_aux": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, _P, C.c_int]),
     "pcfd_chem_hllc_flux": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_longlong, _P,
                                       C.c_longlong, _P, _P, _P, C.POINTER(C.c_longlong), C.c_int]),
+    "pcfd_chem_attach_mesh": (C.c_int, [_P, C.POINTER(MeshView)]),
+    "pcfd_chem_residual": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_double, C.c_int, _P, _P,
+                                     _P, C.c_int]),
     "pcfd_chem_destroy": (C.c_int, [_P]),
     "pcfd_chem_production_rates": (C.c_int, [_P, C.c_longlong, _DP, _DP, _DP]),
     "pcfd_chem_production_rates_dev": (C.c_int, [_P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, _DP]),

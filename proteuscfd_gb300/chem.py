@@ -172,6 +172,30 @@ class ChemModel:
                                               edges_ptr, avec_ptr, flux_ptr, C.byref(bad), 1), "pcfd_chem_hllc_flux")
         return bad.value
 
+    def attach_mesh(self, mesh):
+        """Copies the mesh's edges, areas, boundary half-edges and dual
+        volumes to the device for residual()."""
+        N.check(self._lib.pcfd_chem_attach_mesh(self._h, C.byref(mesh.view)), "pcfd_chem_attach_mesh")
+        self._mesh = mesh
+
+    def residual(self, ref, opts, ref_time, reactions, q):
+        """First-order inviscid residual of the reacting set on the attached
+        mesh: q [nnode + nbedge][6 + 3 ns] records -> (b [nnode][ns + 4], norms [1 + ns + 4])."""
+        m = self._mesh
+        q = self._arr(q, (m.nnode + m.nbedge, 6 + 3 * self.nspecies))
+        b = np.empty((m.nnode, self.nspecies + 4))
+        norms = np.empty(1 + self.nspecies + 4)
+        N.check(self._lib.pcfd_chem_residual(self._h, C.byref(ref), C.byref(opts), float(ref_time), int(reactions),
+                                             N.dptr(q), N.dptr(b), N.dptr(norms), 0), "pcfd_chem_residual")
+        return b, norms
+
+    def residual_dev(self, ref, opts, ref_time, reactions, q_ptr, b_ptr=None):
+        """The same with q (and b, optional) as device addresses; returns the norms."""
+        norms = np.empty(1 + self.nspecies + 4)
+        N.check(self._lib.pcfd_chem_residual(self._h, C.byref(ref), C.byref(opts), float(ref_time), int(reactions),
+                                             q_ptr, b_ptr, N.dptr(norms), 1), "pcfd_chem_residual")
+        return norms
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pcfd_chem_destroy(self._h)

@@ -14,6 +14,7 @@
 //   CompressibleFREqnSet<T>::ComputeAuxiliaryVariables ucs/compressibleFR.tcc:755
 // and its inviscid edge flux:
 //   CompressibleFREqnSet<T>::HLLCFlux               ucs/compressibleFR.tcc:301
+// and its first-order inviscid residual (SpatialResidual, ucs/residual.tcc:66).
 // The reference evaluates each reaction's rates once per species it
 // produces; here each reaction is evaluated once per node and its
 // contribution added to every species it changes, in reaction order, which
@@ -24,12 +25,18 @@
 
 #include <cstring>
 #include <string>
+#include <vector>
 
 void pcfd_set_last_error(const std::string& msg);
 
 namespace {
 
 constexpr double kUnivR = 8.31447215;  // ucs/chem_constants.h:5
+
+// an edge's unit normal and area, one 32-byte load
+struct __align__(32) EdgeArea {
+  double x, y, z, w;
+};
 constexpr double kPref = 101325.0;     // ucs/reaction.tcc:665
 
 // Per-species constants of the thermodynamic functions, formed once per
@@ -54,7 +61,16 @@ struct ChemHandle {
   double* d_buf = nullptr;  // host-array calls of the node-state functions
   size_t buf_cap = 0;
   long long* d_count = nullptr;
+  // attached mesh (pcfd_chem_attach_mesh)
+  long long nnode = 0, nedge = 0, nbedge = 0;
+  int2 *d_en = nullptr, *d_bn = nullptr;
+  EdgeArea *d_ea = nullptr, *d_ba = nullptr;
+  double* d_vol = nullptr;
+  int *d_nptr = nullptr, *d_nedg = nullptr, *d_bptr = nullptr, *d_bhe = nullptr;
+  double *d_q = nullptr, *d_ef = nullptr, *d_bf = nullptr, *d_b = nullptr, *d_part = nullptr, *d_norms = nullptr;
 };
+
+constexpr int kChemNormBlocks = 304;  // fixed grid of the residual gather: a fixed summation order
 
 int cuda_fail(cudaError_t e, const char* what) {
   pcfd_set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -115,26 +131,14 @@ __device__ double equilibrium_const(const pcfd_chem_model& m, const pcfd_chem_re
   return Kc;
 }
 
-__global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem_model* __restrict__ gm,
-                                                    const double* __restrict__ rhoi, const double* __restrict__ Tn,
-                                                    double* __restrict__ wdot) {
-  __shared__ pcfd_chem_model m;
-  {
-    // stage the mechanism (about 17 KB) with 8-byte copies
-    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gm);
-    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&m);
-    for (int k = threadIdx.x; k < (int)(sizeof(pcfd_chem_model) / 8); k += blockDim.x) dst[k] = src[k];
-  }
-  __syncthreads();
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= n) return;
+// mass production rates of one node (rhoi [ns] kg/m^3, T K -> wdot [ns])
+__device__ void node_rates(const pcfd_chem_model& m, const double* rhoi, const double T, double* wdot) {
   const int ns = m.nspecies;
   double X[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES];
   for (int k = 0; k < ns; k++) {
-    X[k] = rhoi[p * ns + k] / m.mw[k];
+    X[k] = rhoi[k] / m.mw[k];
     w[k] = 0.0;
   }
-  const double T = Tn[p];
   const double logT = log(T);
   double Xsum = 0.0;
   for (int k = 0; k < ns; k++) Xsum += X[k];
@@ -164,7 +168,23 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
       w[g] += t;
     }
   }
-  for (int k = 0; k < ns; k++) wdot[p * ns + k] = w[k];
+  for (int k = 0; k < ns; k++) wdot[k] = w[k];
+}
+
+__global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                    const double* __restrict__ rhoi, const double* __restrict__ Tn,
+                                                    double* __restrict__ wdot) {
+  __shared__ pcfd_chem_model m;
+  {
+    // stage the mechanism (about 17 KB) with 8-byte copies
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gm);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&m);
+    for (int k = threadIdx.x; k < (int)(sizeof(pcfd_chem_model) / 8); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  node_rates(m, rhoi + p * m.nspecies, Tn[p], wdot + p * m.nspecies);
 }
 
 // ---- node state of the reacting equation set ------------------------------
@@ -359,7 +379,7 @@ __device__ __forceinline__ double fr_Ht(const ChemDerived& d, int ns, const pcfd
 // speeds are the Roe-averaged and one-sided eigenvalues with Gupta's beta
 // modification.  Writes zeros and returns 1 when no branch applies.
 __device__ int fr_hllc(const ChemDerived& d, int ns, const pcfd_chem_ref& ref, const pcfd_chem_flux_opts& o,
-                       const double* QL, const double* QR, const double4 a, double* flux) {
+                       const double* QL, const double* QR, const EdgeArea a, double* flux) {
   const double beta = o.beta, Pref = o.pref;
   const double uL = QL[ns], vL = QL[ns + 1], wL = QL[ns + 2], TL = QL[ns + 3], pL = QL[ns + 4], rhoL = QL[ns + 5];
   const double uR = QR[ns], vR = QR[ns + 1], wR = QR[ns + 2], TR = QR[ns + 3], pR = QR[ns + 4], rhoR = QR[ns + 5];
@@ -438,7 +458,7 @@ __global__ void __launch_bounds__(128) k_chem_hllc(long long nedge, long long nn
                                                    const pcfd_chem_model* __restrict__ gm,
                                                    const ChemDerived* __restrict__ gd, pcfd_chem_ref ref,
                                                    pcfd_chem_flux_opts o, const double* __restrict__ q,
-                                                   const int2* __restrict__ edges, const double4* __restrict__ avec,
+                                                   const int2* __restrict__ edges, const EdgeArea* __restrict__ avec,
                                                    double* __restrict__ flux, long long* __restrict__ nfail) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= nedge) return;
@@ -460,6 +480,112 @@ __global__ void __launch_bounds__(128) k_chem_hllc(long long nedge, long long nn
   double f[PCFD_CHEM_MAX_SPECIES + 4];
   if (fr_hllc(*gd, ns, ref, o, QL, QR, avec[e], f)) atomicAdd((unsigned long long*)nfail, 1ull);
   for (int i = 0; i < ns + 4; i++) flux[e * (ns + 4) + i] = f[i];
+}
+
+// boundary half-edges: the node's record against its phantom record
+__global__ void __launch_bounds__(128) k_chem_bflux(long long nbedge, const pcfd_chem_model* __restrict__ gm,
+                                                    const ChemDerived* __restrict__ gd, pcfd_chem_ref ref,
+                                                    pcfd_chem_flux_opts o, const double* __restrict__ q,
+                                                    const int2* __restrict__ bn, const EdgeArea* __restrict__ ba,
+                                                    double* __restrict__ bf, long long* __restrict__ nfail) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= nbedge) return;
+  const int ns = gm->nspecies;
+  const int nv = 6 + 3 * ns;
+  const int2 n = bn[k];
+  double QL[6 + 2 * PCFD_CHEM_MAX_SPECIES], QR[6 + 2 * PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns + 6; i++) {
+    QL[i] = q[(size_t)n.x * nv + i];
+    QR[i] = q[(size_t)n.y * nv + i];
+  }
+  double f[PCFD_CHEM_MAX_SPECIES + 4];
+  if (fr_hllc(*gd, ns, ref, o, QL, QR, ba[k], f)) atomicAdd((unsigned long long*)nfail, 1ull);
+  for (int i = 0; i < ns + 4; i++) bf[k * (ns + 4) + i] = f[i];
+}
+
+// per node: -sum of the fluxes out of it (incident edges in ascending id,
+// signed: ~e where the node is the edge's left end), then its boundary
+// half-edges, then vol * wdot; per-block partial sums of squares
+__global__ void __launch_bounds__(256) k_chem_gather(long long nnode, const pcfd_chem_model* __restrict__ gm,
+                                                     pcfd_chem_ref ref, double ref_time, int reactions,
+                                                     const double* __restrict__ q, const int* __restrict__ nptr,
+                                                     const int* __restrict__ nedg, const double* __restrict__ ef,
+                                                     const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                     const double* __restrict__ bf, const double* __restrict__ vol,
+                                                     double* __restrict__ b, double* __restrict__ part) {
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  double acc[PCFD_CHEM_MAX_SPECIES + 4];
+  for (int j = 0; j < neqn; j++) acc[j] = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnode;
+       i += (long long)gridDim.x * blockDim.x) {
+    double r[PCFD_CHEM_MAX_SPECIES + 4];
+    for (int j = 0; j < neqn; j++) r[j] = 0.0;
+    for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+      const int se = nedg[k];
+      if (se < 0) {
+        const double* f = &ef[(size_t)(~se) * neqn];
+        for (int j = 0; j < neqn; j++) r[j] += -f[j];
+      } else {
+        const double* f = &ef[(size_t)se * neqn];
+        for (int j = 0; j < neqn; j++) r[j] += f[j];
+      }
+    }
+    for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+      const double* f = &bf[(size_t)bhe[p] * neqn];
+      for (int j = 0; j < neqn; j++) r[j] += -f[j];
+    }
+    if (reactions) {
+      const double* Q = &q[(size_t)i * nv];
+      double rhoi[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES];
+      for (int s = 0; s < ns; s++) rhoi[s] = Q[s] * ref.density;
+      node_rates(m, rhoi, Q[ns + 3] * ref.temperature, w);
+      for (int s = 0; s < ns; s++) {
+        const double wn = w[s] / (ref.density / ref_time);
+        r[s] += vol[i] * wn;
+      }
+    }
+    for (int j = 0; j < neqn; j++) {
+      b[(size_t)i * neqn + j] = r[j];
+      acc[j] += r[j] * r[j];
+    }
+  }
+  // deterministic block sums: warp shuffles, then a fixed-order sum
+  __shared__ double red[8][PCFD_CHEM_MAX_SPECIES + 4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = 0; j < neqn; j++) {
+    double v = acc[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < neqn) {
+    double v = 0.0;
+    for (int w = 0; w < 8; w++) v += red[w][threadIdx.x];
+    part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+// the norms from the per-block partials, a warp per component, fixed order
+__global__ void k_chem_norms(int nblocks, long long nnode, int neqn, const double* __restrict__ part,
+                             double* __restrict__ norms) {
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  if (c >= neqn) return;
+  double v = 0.0;
+  for (int bl = lane; bl < nblocks; bl += 32) v += part[(size_t)c * nblocks + bl];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) norms[1 + c] = sqrt(v) / (double)nnode;
+  // resGlobal from the component sums (all squares), one more pass by warp 0
+  if (c == 0) {
+    double t = 0.0;
+    for (int j = 0; j < neqn; j++) {
+      double s = 0.0;
+      for (int bl = lane; bl < nblocks; bl += 32) s += part[(size_t)j * nblocks + bl];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      t += s;
+    }
+    if (lane == 0) norms[0] = sqrt(t) / ((double)nnode * neqn);
+  }
 }
 
 int validate(const pcfd_chem_model* m) {
@@ -612,6 +738,9 @@ PCFD_API int pcfd_chem_destroy(pcfd_chem_t h) {
   cudaFree(c->d_w);
   cudaFree(c->d_buf);
   cudaFree(c->d_count);
+  void* mesh_ptrs[] = {c->d_en, c->d_bn, c->d_ea, c->d_ba, c->d_vol, c->d_nptr, c->d_nedg, c->d_bptr,
+                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms};
+  for (void* p : mesh_ptrs) cudaFree(p);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -766,17 +895,17 @@ PCFD_API int pcfd_chem_hllc_flux(pcfd_chem_t h, const pcfd_chem_ref* ref, const 
   CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
   const double* dq = q;
   const int2* de = (const int2*)edges;
-  const double4* da = (const double4*)avec;
+  const EdgeArea* da = (const EdgeArea*)avec;
   double* df = flux;
   if (!dev) {
-    // staging: avec first (the double4 loads want 32-byte alignment; the
+    // staging: avec first (the EdgeArea loads want 32-byte alignment; the
     // buffer is 256-byte aligned), then q, flux and the edge ids
     const size_t need = (size_t)nedge * 4 + (size_t)nnode * nv + (size_t)nedge * (ns + 4) + (size_t)nedge;
     int rc = ensure_buf(c, need);
     if (rc) return rc;
     double* b = c->d_buf;
     CHEM_TRY(cudaMemcpyAsync(b, avec, (size_t)nedge * 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream), "chem copy");
-    da = (const double4*)b;
+    da = (const EdgeArea*)b;
     b += (size_t)nedge * 4;
     CHEM_TRY(cudaMemcpyAsync(b, q, (size_t)nnode * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream), "chem copy");
     dq = b;
@@ -803,6 +932,136 @@ PCFD_API int pcfd_chem_hllc_flux(pcfd_chem_t h, const pcfd_chem_ref* ref, const 
   if (bad) {
     pcfd_set_last_error("pcfd_chem_hllc_flux: " + std::to_string(bad) +
                         " edge(s) with no HLLC branch or a node id out of range");
+    return PCFD_ERR_NUMERIC;
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !m || m->nnode <= 0 || m->nedge < 0 || m->nbedge < 0 || (m->nedge > 0 && (!m->edges || !m->edge_area)) ||
+      (m->nbedge > 0 && (!m->bedges || !m->bedge_area)) || !m->vol) {
+    pcfd_set_last_error("pcfd_chem_attach_mesh: bad mesh");
+    return PCFD_ERR_ARG;
+  }
+  const long long nn = m->nnode, ne = m->nedge, nb = m->nbedge, ntot = nn + nb;
+  for (long long e = 0; e < 2 * ne; e++)
+    if (m->edges[e] < 0 || m->edges[e] >= nn) {
+      pcfd_set_last_error("pcfd_chem_attach_mesh: edge node id out of range");
+      return PCFD_ERR_ARG;
+    }
+  for (long long k = 0; k < nb; k++)
+    if (m->bedges[2 * k] < 0 || m->bedges[2 * k] >= nn || m->bedges[2 * k + 1] < nn || m->bedges[2 * k + 1] >= ntot) {
+      pcfd_set_last_error("pcfd_chem_attach_mesh: boundary half-edge ids out of range");
+      return PCFD_ERR_ARG;
+    }
+  // node -> incident edges (ascending id, ~e at the left end), node -> half-edges
+  std::vector<int> nptr(nn + 1, 0), bptr(nn + 1, 0);
+  for (long long e = 0; e < ne; e++) {
+    nptr[m->edges[2 * e] + 1]++;
+    nptr[m->edges[2 * e + 1] + 1]++;
+  }
+  for (long long k = 0; k < nb; k++) bptr[m->bedges[2 * k] + 1]++;
+  for (long long i = 0; i < nn; i++) {
+    nptr[i + 1] += nptr[i];
+    bptr[i + 1] += bptr[i];
+  }
+  std::vector<int> nedg(2 * ne > 0 ? 2 * ne : 1), bhe(nb > 0 ? nb : 1), fill(nptr.begin(), nptr.end() - 1),
+      bfill(bptr.begin(), bptr.end() - 1);
+  for (long long e = 0; e < ne; e++) {
+    nedg[fill[m->edges[2 * e]]++] = ~(int)e;
+    nedg[fill[m->edges[2 * e + 1]]++] = (int)e;
+  }
+  for (long long k = 0; k < nb; k++) bhe[bfill[m->bedges[2 * k]]++] = (int)k;
+  void* mesh_ptrs[] = {c->d_en, c->d_bn, c->d_ea, c->d_ba, c->d_vol, c->d_nptr, c->d_nedg, c->d_bptr,
+                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms};
+  for (void* p : mesh_ptrs) cudaFree(p);
+  c->d_en = c->d_bn = nullptr;
+  c->d_ea = c->d_ba = nullptr;
+  c->d_vol = c->d_q = c->d_ef = c->d_bf = c->d_b = c->d_part = c->d_norms = nullptr;
+  c->d_nptr = c->d_nedg = c->d_bptr = c->d_bhe = nullptr;
+  c->nnode = c->nedge = c->nbedge = 0;
+  const int ns = c->host.nspecies, neqn = ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, bytes > 0 ? bytes : 16);
+    if (e == cudaSuccess && bytes > 0) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = up((void**)&c->d_en, m->edges, (size_t)ne * 2 * sizeof(int));
+  if (e == cudaSuccess) e = up((void**)&c->d_ea, m->edge_area, (size_t)ne * 4 * sizeof(double));
+  if (e == cudaSuccess) e = up((void**)&c->d_bn, m->bedges, (size_t)nb * 2 * sizeof(int));
+  if (e == cudaSuccess) e = up((void**)&c->d_ba, m->bedge_area, (size_t)nb * 4 * sizeof(double));
+  if (e == cudaSuccess) e = up((void**)&c->d_vol, m->vol, (size_t)nn * sizeof(double));
+  if (e == cudaSuccess) e = up((void**)&c->d_nptr, nptr.data(), nptr.size() * sizeof(int));
+  if (e == cudaSuccess) e = up((void**)&c->d_nedg, nedg.data(), nedg.size() * sizeof(int));
+  if (e == cudaSuccess) e = up((void**)&c->d_bptr, bptr.data(), bptr.size() * sizeof(int));
+  if (e == cudaSuccess) e = up((void**)&c->d_bhe, bhe.data(), bhe.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_q, (size_t)ntot * nv * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_ef, ((size_t)ne > 0 ? ne : 1) * neqn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bf, ((size_t)nb > 0 ? nb : 1) * neqn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_b, (size_t)nn * neqn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_part, (size_t)kChemNormBlocks * neqn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_norms, (size_t)(1 + neqn) * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(e, "pcfd_chem_attach_mesh");
+  c->nnode = nn;
+  c->nedge = ne;
+  c->nbedge = nb;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_residual(pcfd_chem_t h, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                double ref_time, int reactions, const double* q, double* b, double* norms, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || !o || !q || !(ref_time > 0.0)) {
+    pcfd_set_last_error("pcfd_chem_residual: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0) {
+    pcfd_set_last_error("pcfd_chem_residual: no mesh attached (pcfd_chem_attach_mesh)");
+    return PCFD_ERR_STATE;
+  }
+  const int ns = c->host.nspecies, neqn = ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, ne = c->nedge, nb = c->nbedge;
+  const double* dq = q;
+  if (!dev) {
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    dq = c->d_q;
+  }
+  double* db = (dev && b) ? b : c->d_b;
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  const pcfd_chem_ref r = *ref;
+  const pcfd_chem_flux_opts oo = *o;
+  if (ne > 0) {
+    k_chem_hllc<<<CHEM_GRID(ne)>>>(ne, nn + nb, c->dev, c->dder, r, oo, dq, c->d_en, c->d_ea, c->d_ef, c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_hllc launch");
+  }
+  if (nb > 0) {
+    k_chem_bflux<<<CHEM_GRID(nb)>>>(nb, c->dev, c->dder, r, oo, dq, c->d_bn, c->d_ba, c->d_bf, c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_bflux launch");
+  }
+  k_chem_gather<<<kChemNormBlocks, 256, 0, c->stream>>>(nn, c->dev, r, ref_time, reactions, dq, c->d_nptr, c->d_nedg,
+                                                        c->d_ef, c->d_bptr, c->d_bhe, c->d_bf, c->d_vol, db,
+                                                        c->d_part);
+  CHEM_TRY(cudaGetLastError(), "k_chem_gather launch");
+  k_chem_norms<<<1, 32 * neqn, 0, c->stream>>>(kChemNormBlocks, nn, neqn, c->d_part, c->d_norms);
+  CHEM_TRY(cudaGetLastError(), "k_chem_norms launch");
+  if (b && !dev)
+    CHEM_TRY(cudaMemcpyAsync(b, db, (size_t)nn * neqn * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  if (norms)
+    CHEM_TRY(cudaMemcpyAsync(norms, c->d_norms, (size_t)(1 + neqn) * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream),
+             "chem copy out");
+  long long bad = 0;
+  CHEM_TRY(cudaMemcpyAsync(&bad, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem residual");
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_residual: " + std::to_string(bad) + " face(s) with no HLLC branch");
     return PCFD_ERR_NUMERIC;
   }
   return PCFD_OK;

@@ -58,6 +58,8 @@ def lib():
                                            _DP, _DP, _DP, _DP]),
             "oracle_chem_hllc_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
                                                   C.POINTER(N.ChemFluxOpts), _DP, C.c_longlong, _IP, _DP, _DP]),
+            "oracle_chem_residual": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.ChemFluxOpts),
+                                            C.POINTER(N.MeshView), _DP, C.c_double, C.c_int, _DP, _DP]),
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
@@ -373,3 +375,12 @@ class OracleChemState:
         bad = self.L.oracle_chem_hllc_n(C.byref(self.m), C.byref(self.ref), C.byref(opts), dp(q), len(edges),
                                         ip(edges), dp(avec), dp(flux))
         return flux, bad
+
+    def residual(self, opts, mesh, q, ref_time, reactions):
+        """SpatialResidual of the reacting set (first order, inviscid)."""
+        q = np.ascontiguousarray(q, np.float64)
+        b = np.empty((mesh.nnode, self.ns + 4))
+        norms = np.empty(1 + self.ns + 4)
+        self.L.oracle_chem_residual(C.byref(self.m), C.byref(self.ref), C.byref(opts), C.byref(mesh.view), dp(q),
+                                    float(ref_time), int(reactions), dp(b), dp(norms))
+        return b, norms

@@ -135,3 +135,21 @@ def test_fr_hllc_consistency():
         assert np.abs(f - ref_f).max() <= 1e-12 * scale.max(), np.abs(f - ref_f).max()
     f2, _ = O.hllc(N.ChemFluxOpts(1.0, pref, 2), q, np.c_[np.arange(20), np.arange(20)], avec)
     assert np.all(f2[:, ns + 1] == 0.0)
+
+
+def test_fr_residual_freestream_preserved():
+    """A uniform reacting state on every node and phantom of a closed
+    jittered box leaves a zero residual with reactions off (the dual faces
+    close and HLLC(Q, Q) is the physical flux)."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    from proteuscfd_gb300 import _native as N
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=3)
+    ref, rhoi, vel, T = fr_states(1, seed=4)
+    q = np.tile(fr_records(ref, rhoi, vel, T), (m.nnode + m.nbedge, 1))
+    O = OracleChemState(model_struct(mechanism()), ref)
+    b, norms = O.residual(N.ChemFluxOpts(1.0, 0.3, 0), m, q, 1e-3, 0)
+    ns = O.ns
+    scale = np.abs(q[0, :ns]).max() * np.abs(vel).max() * np.asarray(m.edge_area)[:, 3].max()
+    assert np.abs(b).max() < 1e-13 * max(scale, 1.0), np.abs(b).max()
