@@ -826,13 +826,25 @@ __global__ void __launch_bounds__(256, 3) k_spmv(int nnode, const int* __restric
 constexpr int kRowStages = 3;
 constexpr int kStageBlocks = 16;  // blocks staged per row; further blocks are read directly
 
-struct RowStage {
-  float m[kStageBlocks * 25 + 4];  // window of the row's blocks
-  float x[kStageBlocks * 8];       // per block: a 32-byte window holding its 5 x entries
-  float dinv[28];                  // window of the row's inverse diagonal block (sweeps)
-  float b[8];                      // window of the row's right-hand side (sweeps)
+// Window sizes of one stage in elements of E (float or double): a 16-byte
+// chunk holds C elements, so an aligned window of a k-element run starting
+// anywhere in a chunk holds k + C - 1 elements, rounded up to whole chunks.
+template <class E>
+struct StageGeom {
+  static constexpr int C = 16 / (int)sizeof(E);
+  static constexpr int XCH = (5 + C - 1 + C - 1) / C;    // chunks of one block's x window
+  static constexpr int DCH = (25 + C - 1 + C - 1) / C;   // chunks of the inverse diagonal block
+  static constexpr int BCH = (5 + C - 1 + C - 1) / C;    // chunks of the right-hand side
 };
-static_assert(sizeof(RowStage) % 16 == 0, "stage size");
+
+template <class E>
+struct RowStage {
+  E m[kStageBlocks * 25 + StageGeom<E>::C];       // window of the row's blocks
+  E x[kStageBlocks * StageGeom<E>::XCH * StageGeom<E>::C];  // per block: a window holding its 5 x entries
+  E dinv[StageGeom<E>::DCH * StageGeom<E>::C];    // window of the row's inverse diagonal block (sweeps)
+  E b[StageGeom<E>::BCH * StageGeom<E>::C];       // window of the row's right-hand side (sweeps)
+};
+static_assert(sizeof(RowStage<float>) % 16 == 0 && sizeof(RowStage<double>) % 16 == 0, "stage size");
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
@@ -843,59 +855,68 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// element offset of p inside its 16-byte chunk
+template <class E>
+__device__ __forceinline__ int chunk_off(const E* p) {
+  return (int)((reinterpret_cast<uintptr_t>(p) & 15) / sizeof(E));
+}
+__device__ __forceinline__ const void* chunk_of(const void* p, int k) {
+  return reinterpret_cast<const void*>((reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)15) + 16 * (uintptr_t)k);
+}
+
 // start the copies of row (b0, nb, jl) into stage st, and with dinv the
 // windows of row i's inverse diagonal block and right-hand side; always
 // commits a group
+template <class E>
 __device__ __forceinline__ void row_stage_issue(bool valid, int b0, int nb, int jl, int lane,
-                                                const float* __restrict__ M, const float* xa, RowStage* st,
-                                                int i = 0, const float* __restrict__ dinv = nullptr,
-                                                const float* __restrict__ b = nullptr) {
+                                                const E* __restrict__ M, const E* xa, RowStage<E>* st, int i = 0,
+                                                const E* __restrict__ dinv = nullptr, const E* __restrict__ b = nullptr) {
+  typedef StageGeom<E> G;
   const int ns = min(nb, kStageBlocks);
-  const int jb = __shfl_sync(0xffffffffu, jl, lane >> 1);
+  // column ids of the blocks whose x chunks this lane copies (two passes)
+  const int j0 = __shfl_sync(0xffffffffu, jl, min(lane / G::XCH, 31));
+  const int j1 = __shfl_sync(0xffffffffu, jl, min((lane + 32) / G::XCH, 31));
   if (valid) {
-    const uintptr_t g0 = reinterpret_cast<uintptr_t>(M + (size_t)b0 * 25);
-    const uintptr_t a0 = g0 & ~(uintptr_t)15;
-    const int n16 = (int)((g0 - a0 + (uintptr_t)ns * 100 + 15) >> 4);
+    const E* g = M + (size_t)b0 * 25;
+    const int n16 = (int)(((reinterpret_cast<uintptr_t>(g) & 15) + (uintptr_t)ns * 25 * sizeof(E) + 15) >> 4);
     const uint32_t sm = umma::smem_addr(st->m);
-    for (int c = lane; c < n16; c += 32) cp_async16(sm + 16 * c, reinterpret_cast<const void*>(a0 + 16 * (uintptr_t)c));
-    const int u = lane >> 1;
-    if (u < ns) {
-      const uintptr_t xw = reinterpret_cast<uintptr_t>(xa + (size_t)jb * 5) & ~(uintptr_t)15;
-      cp_async16(umma::smem_addr(st->x) + 32 * u + 16 * (lane & 1), reinterpret_cast<const void*>(xw + 16 * (lane & 1)));
+    for (int c = lane; c < n16; c += 32) cp_async16(sm + 16 * c, chunk_of(g, c));
+    const uint32_t sx = umma::smem_addr(st->x);
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+      const int c = lane + 32 * pass;
+      const int u = c / G::XCH;
+      if (u < ns) cp_async16(sx + 16 * c, chunk_of(xa + (size_t)(pass ? j1 : j0) * 5, c % G::XCH));
     }
     if (dinv) {
-      // 7 chunks cover the 100-byte block from its aligned start, 2 the 20-byte b entries
-      if (lane < 7) {
-        const uintptr_t dw = reinterpret_cast<uintptr_t>(dinv + (size_t)i * 25) & ~(uintptr_t)15;
-        cp_async16(umma::smem_addr(st->dinv) + 16 * lane, reinterpret_cast<const void*>(dw + 16 * lane));
-      } else if (lane < 9) {
-        const uintptr_t bw = reinterpret_cast<uintptr_t>(b + (size_t)i * 5) & ~(uintptr_t)15;
-        cp_async16(umma::smem_addr(st->b) + 16 * (lane - 7), reinterpret_cast<const void*>(bw + 16 * (lane - 7)));
-      }
+      if (lane < G::DCH) cp_async16(umma::smem_addr(st->dinv) + 16 * lane, chunk_of(dinv + (size_t)i * 25, lane));
+      else if (lane < G::DCH + G::BCH)
+        cp_async16(umma::smem_addr(st->b) + 16 * (lane - G::DCH), chunk_of(b + (size_t)i * 5, lane - G::DCH));
     }
   }
   cp_async_commit();
 }
 
 // off-diagonal sum of a staged row; lane 5r receives row r's sum
-__device__ __forceinline__ float row_stage_sum(int b0, int nb, int jl, int lane, const RowStage* st,
-                                               const int* __restrict__ ja, const float* __restrict__ M,
-                                               const float* xa) {
+template <class E>
+__device__ __forceinline__ E row_stage_sum(int b0, int nb, int jl, int lane, const RowStage<E>* st,
+                                           const int* __restrict__ ja, const E* __restrict__ M, const E* xa) {
+  typedef StageGeom<E> G;
   const int c = lane % 5;
   const bool active = lane < 25;
   const int ns = min(nb, kStageBlocks);
-  const int mo = (int)((reinterpret_cast<uintptr_t>(M + (size_t)b0 * 25) & 15) >> 2);
-  float acc = 0.f;
+  const int mo = chunk_off(M + (size_t)b0 * 25);
+  E acc = E(0);
 #pragma unroll
   for (int u = 0; u < kStageBlocks; u++) {
     if (u >= ns) break;
     const int j = __shfl_sync(0xffffffffu, jl, u);
-    const int xo = (int)((reinterpret_cast<uintptr_t>(xa + (size_t)j * 5) & 15) >> 2);
-    if (active) acc = fmaf(st->m[mo + u * 25 + lane], st->x[u * 8 + xo + c], acc);
+    const int xo = chunk_off(xa + (size_t)j * 5);
+    if (active) acc = fma(st->m[mo + u * 25 + lane], st->x[u * G::XCH * G::C + xo + c], acc);
   }
   for (int k = kStageBlocks; k < nb; k++) {
     const int j = k < 32 ? __shfl_sync(0xffffffffu, jl, k & 31) : ja[b0 + k];
-    if (active) acc = fmaf(M[(size_t)(b0 + k) * 25 + lane], __ldcg(&xa[(size_t)j * 5 + c]), acc);
+    if (active) acc = fma(M[(size_t)(b0 + k) * 25 + lane], __ldcg(&xa[(size_t)j * 5 + c]), acc);
   }
   return sum5(acc);
 }
@@ -909,7 +930,7 @@ __global__ void __launch_bounds__(256, 4) k_spmv_staged(int nnode, const int* __
                                                         float* __restrict__ y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  RowStage* st = reinterpret_cast<RowStage*>(smem_raw) + wid * kRowStages;
+  RowStage<float>* st = reinterpret_cast<RowStage<float>*>(smem_raw) + wid * kRowStages;
   const int W = gridDim.x * 8;
   int iA = blockIdx.x * 8 + wid;
   if (iA >= nnode) return;
@@ -965,14 +986,14 @@ __global__ void __launch_bounds__(256, 4) k_spmv_staged(int nnode, const int* __
   cp_async_wait<0>();
 }
 
-// The rows of one colour of an FP32 sweep through the staged pipeline
-// (sgs_rows' arithmetic on staged data): desc gives the rows in colour order,
-// g the warp's first row, W the number of warps.  Drains its copies before
-// returning.
+// The rows of one colour of a sweep through the staged pipeline (sgs_rows'
+// arithmetic on staged data), E the element type of blocks and vectors:
+// desc gives the rows in colour order, g the warp's first row, W the number
+// of warps.  Drains its copies before returning.
+template <class E>
 __device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restrict__ desc, const int* __restrict__ ja,
-                                                const float* __restrict__ M, const float* __restrict__ dinv,
-                                                const float* __restrict__ b, float* x, int g, const int W,
-                                                RowStage* st) {
+                                                const E* __restrict__ M, const E* __restrict__ dinv,
+                                                const E* __restrict__ b, E* x, int g, const int W, RowStage<E>* st) {
   const int lane = threadIdx.x & 31;
   if (g >= nrows) return;
   const int r = lane / 5, c = lane % 5;
@@ -982,29 +1003,29 @@ __device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restric
   int jA = cols(dA);
   int4 dB = g + W < nrows ? desc[g + W] : none;
   int jB = cols(dB);
-  row_stage_issue(true, dA.y, dA.z, jA, lane, M, x, &st[0], dA.x, dinv, b);
-  row_stage_issue(dB.x >= 0, dB.y, dB.z, jB, lane, M, x, &st[1], dB.x, dinv, b);
+  row_stage_issue<E>(true, dA.y, dA.z, jA, lane, M, x, &st[0], dA.x, dinv, b);
+  row_stage_issue<E>(dB.x >= 0, dB.y, dB.z, jB, lane, M, x, &st[1], dB.x, dinv, b);
   int gC = g + 2 * W;
   int4 dC = gC < nrows ? desc[gC] : none;
   int jC = cols(dC);
   int4 dN = gC + W < nrows ? desc[gC + W] : none;
   int sA = 0, sB = 1, sC = 2;
   while (true) {
-    row_stage_issue(dC.x >= 0, dC.y, dC.z, jC, lane, M, x, &st[sC], dC.x, dinv, b);
+    row_stage_issue<E>(dC.x >= 0, dC.y, dC.z, jC, lane, M, x, &st[sC], dC.x, dinv, b);
     const int jN = cols(dN);
     const int gNN = gC + 2 * W;
     const int4 dNN = gNN < nrows ? desc[gNN] : none;
     cp_async_wait<2>();
     __syncwarp();
-    const RowStage* sa = &st[sA];
-    const float s = row_stage_sum(dA.y, dA.z, jA, lane, sa, ja, M, x);
+    const RowStage<E>* sa = &st[sA];
+    const E s = row_stage_sum<E>(dA.y, dA.z, jA, lane, sa, ja, M, x);
     const int i = dA.x;
-    const int bo = (int)((reinterpret_cast<uintptr_t>(b + (size_t)i * 5) & 15) >> 2);
-    const int dof = (int)((reinterpret_cast<uintptr_t>(dinv + (size_t)i * 25) & 15) >> 2);
+    const int bo = chunk_off(b + (size_t)i * 5);
+    const int dof = chunk_off(dinv + (size_t)i * 25);
     // rhs_r = b_r - s_r on lane 5r; lane l = 5r + c then forms D^-1[r][c] rhs_c
-    const float rhs = (lane < 25 && c == 0) ? sa->b[bo + r] - s : 0.f;
-    const float rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
-    float v = lane < 25 ? sa->dinv[dof + lane] * rc : 0.f;
+    const E rhs = (lane < 25 && c == 0) ? sa->b[bo + r] - s : E(0);
+    const E rc = __shfl_sync(0xffffffffu, rhs, (5 * c) & 31);
+    E v = lane < 25 ? sa->dinv[dof + lane] * rc : E(0);
     v = sum5(v);
     if (lane < 25 && c == 0) x[(size_t)i * 5 + r] = v;
     __syncwarp();
@@ -1023,23 +1044,23 @@ __device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restric
   __syncwarp();
 }
 
-// nsweeps FP32 sweeps in one cooperative launch through the staged pipeline
-// (k_sgs_sweep's phases and barriers).
-__global__ void __launch_bounds__(256, 4) k_sgs_sweep_staged(int ncolor, const int* __restrict__ cptr,
-                                                             const int4* __restrict__ desc,
-                                                             const int* __restrict__ ja, const float* __restrict__ M,
-                                                             const float* __restrict__ dinv,
-                                                             const float* __restrict__ b, float* x, int nsweeps,
-                                                             unsigned int* __restrict__ bar, int* __restrict__ err) {
+// nsweeps sweeps in one cooperative launch through the staged pipeline
+// (k_sgs_sweep's phases and barriers); FP32 or FP64 blocks and vectors.
+template <class E>
+__global__ void __launch_bounds__(256) k_sgs_sweep_staged(int ncolor, const int* __restrict__ cptr,
+                                                          const int4* __restrict__ desc, const int* __restrict__ ja,
+                                                          const E* __restrict__ M, const E* __restrict__ dinv,
+                                                          const E* __restrict__ b, E* x, int nsweeps,
+                                                          unsigned int* __restrict__ bar, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  RowStage* st = reinterpret_cast<RowStage*>(smem_raw) + (threadIdx.x >> 5) * kRowStages;
+  RowStage<E>* st = reinterpret_cast<RowStage<E>*>(smem_raw) + (threadIdx.x >> 5) * kRowStages;
   const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
   const int nphase = nsweeps * 2 * ncolor;
   for (int p = 0; p < nphase; p++) {
     const int cc = p % ncolor, dir = (p / ncolor) & 1;
     const int c = dir == 0 ? cc : ncolor - 1 - cc;
     const int r0 = cptr[c], nr = cptr[c + 1] - r0;
-    sgs_rows_staged(nr, desc + r0, ja, M, dinv, b, x, g, W, st);
+    sgs_rows_staged<E>(nr, desc + r0, ja, M, dinv, b, x, g, W, st);
     if (p + 1 < nphase && !grid_barrier(bar, gridDim.x, err)) return;
   }
 }

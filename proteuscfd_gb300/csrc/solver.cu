@@ -1770,6 +1770,9 @@ int check_sweeps(Solver* s) {
   return PCFD_OK;
 }
 
+template <class E>
+int run_sweeps_staged(Solver* s, int nsweeps, const E* dinv, const E* b, E* x);
+
 template <class T>
 int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm) {
   const double cnt = (double)s->nnode * NEQN;
@@ -1792,15 +1795,21 @@ int run_sgs_t(Solver* s, int nsweeps, const double* b, double* x, double* dnorm)
     out = std::sqrt(v) / cnt;
     return PCFD_OK;
   };
+  // FP64 blocks and vectors run the staged kernel, mixed types the
+  // register-staged one
+  auto sweeps = [&](int k) -> int {
+    if (std::is_same<T, double>::value) return run_sweeps_staged<double>(s, k, s->d_dinv, b, x);
+    return run_sweeps<T, double>(s, k, s->d_dinv, b, x, xa);
+  };
   int rc;
   if (dnorm && nsweeps >= 2) {
     // the reference returns the norm change of the last sweep
-    if ((rc = run_sweeps<T, double>(s, nsweeps - 1, s->d_dinv, b, x, xa))) return rc;
+    if ((rc = sweeps(nsweeps - 1))) return rc;
     if ((rc = norm(prev))) return rc;
-    if ((rc = run_sweeps<T, double>(s, 1, s->d_dinv, b, x, xa))) return rc;
+    if ((rc = sweeps(1))) return rc;
     if ((rc = norm(cur))) return rc;
   } else {
-    if ((rc = run_sweeps<T, double>(s, nsweeps, s->d_dinv, b, x, xa))) return rc;
+    if ((rc = sweeps(nsweeps))) return rc;
     if (dnorm && nsweeps == 1 && (rc = norm(cur))) return rc;
   }
   if (dnorm) *dnorm = std::fabs(prev - cur);
@@ -1823,34 +1832,38 @@ int run_sgs_f_t(Solver* s, int nsweeps, const float* b, float* x) {
   return run_sweeps<T, float>(s, nsweeps, s->d_dinvf, b, x, x);
 }
 
-// FP32 blocks: the staged sweep kernel (cooperative, up to four blocks per
-// multiprocessor)
-template <>
-int run_sgs_f_t<float>(Solver* s, int nsweeps, const float* b, float* x) {
+// nsweeps sweeps through the staged kernel (cooperative; as many blocks as
+// fit, at most four per multiprocessor), blocks and vectors of type E
+template <class E>
+int run_sweeps_staged(Solver* s, int nsweeps, const E* dinv, const E* b, E* x) {
   if (nsweeps <= 0) return PCFD_OK;
-  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage);
+  auto kern = k_sgs_sweep_staged<E>;
+  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage<E>);
   static bool attr = false;
   if (!attr) {
-    CUDA_TRY(cudaFuncSetAttribute(k_sgs_sweep_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr = true;
   }
   int per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sgs_sweep_staged, 256, smem));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
   if (per_sm < 1) return set_err(PCFD_ERR_CUDA, "sgs: staged sweep kernel cannot be resident");
   int maxrows = 1;
   for (int c = 0; c < s->ncolor; c++) maxrows = std::max(maxrows, s->color_ptr[c + 1] - s->color_ptr[c]);
   int grid = std::max(1, std::min(std::min(per_sm, 4) * s->nsm, nblk(maxrows, 8)));
-  const float* M = (const float*)s->d_M;
-  const float* dinv = s->d_dinvf;
+  const E* M = (const E*)s->d_M;
   int ncolor = s->ncolor;
   void* args[] = {&ncolor, &s->d_cptr, &s->d_rowdesc, &s->d_ja, &M, &dinv, &b, &x, &nsweeps, &s->d_gbar, &s->d_sgs_err};
   cudaError_t ce = cudaSuccess;
-  int rc = launch(s, T_SGS, [&] {
-    ce = cudaLaunchCooperativeKernel((void*)k_sgs_sweep_staged, grid, 256, args, smem, s->stream);
-  });
+  int rc = launch(s, T_SGS, [&] { ce = cudaLaunchCooperativeKernel((void*)kern, grid, 256, args, smem, s->stream); });
   if (rc) return rc;
   if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("sgs sweep launch: ") + cudaGetErrorString(ce));
   return PCFD_OK;
+}
+
+// FP32 blocks and vectors: the staged kernel
+template <>
+int run_sgs_f_t<float>(Solver* s, int nsweeps, const float* b, float* x) {
+  return run_sweeps_staged<float>(s, nsweeps, s->d_dinvf, b, x);
 }
 
 int run_sgs_f(Solver* s, int nsweeps, const float* b, float* x) {
@@ -1912,7 +1925,7 @@ int run_spmv_f_t(Solver* s, const float* x, float* y) {
 // multiprocessor
 template <>
 int run_spmv_f_t<float>(Solver* s, const float* x, float* y) {
-  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage);
+  constexpr int smem = 8 * kRowStages * (int)sizeof(RowStage<float>);
   static bool attr = false;
   if (!attr) {
     CUDA_TRY(cudaFuncSetAttribute(k_spmv_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -2420,8 +2433,8 @@ int lp_alloc(Solver* s) {
   if ((rc = dalloc(&lp->dm, nh))) return rc;
   if ((rc = dalloc(&lp->dz, nh))) return rc;
   if ((rc = dalloc(&lp->part, lp->part_len))) return rc;
-  if ((rc = dalloc(&lp->y, (size_t)n * NEQN))) return rc;
-  if ((rc = dalloc(&lp->vbuf, (size_t)n * NEQN))) return rc;
+  if ((rc = dalloc(&lp->y, (size_t)n * NEQN + 4))) return rc;  // tail padding: staged sweep windows
+  if ((rc = dalloc(&lp->vbuf, (size_t)n * NEQN + 4))) return rc;
   if ((rc = dalloc(&lp->sigma, 1))) return rc;
   if ((rc = dalloc(&lp->err, 1))) return rc;
   CUDA_TRY(cudaMemsetAsync(lp->err, 0, sizeof(int), s->stream));
@@ -2675,7 +2688,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dalloc(&s->d_q, (size_t)s->ntot * NVARS));
   TRY(dalloc(&s->d_grad, (size_t)nn * NTERMS * 3));
   TRY(dalloc(&s->d_lim, (size_t)nn * NEQN));
-  TRY(dalloc(&s->d_b, (size_t)nn * NEQN));
+  TRY(dalloc(&s->d_b, (size_t)nn * NEQN + 4));  // tail padding: staged sweep windows
   TRY(dalloc(&s->d_ef, (size_t)ne * NEQN));
   TRY(dalloc(&s->d_bf, (size_t)nb * NEQN));
   TRY(dalloc(&s->d_part, (size_t)kNormBlocks * 6));
@@ -2787,11 +2800,11 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
     CUDA_TRY(cudaMemset(s->d_sgs_err, 0, sizeof(int)));
     TRY(dalloc(&s->d_diag, (size_t)nn * 25));
     TRY(dalloc(&s->d_dlu, (size_t)nn * 25));
-    TRY(dalloc(&s->d_dinv, (size_t)nn * 25));
+    TRY(dalloc(&s->d_dinv, (size_t)nn * 25 + 4));
     TRY(dalloc(&s->d_piv, (size_t)nn * 5));
     TRY(dalloc(&s->d_bblk, (size_t)std::max<long long>(nb, 1) * 25));
     TRY(dalloc(&s->d_dt, (size_t)nn));
-    TRY(dalloc(&s->d_x, (size_t)nn * NEQN));
+    TRY(dalloc(&s->d_x, (size_t)nn * NEQN + 4));
     TRY(dalloc(&s->d_scal, 16));
   }
 #undef TRY
