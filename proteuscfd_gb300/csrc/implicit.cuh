@@ -866,29 +866,37 @@ __device__ __forceinline__ const void* chunk_of(const void* p, int k) {
 
 // start the copies of row (b0, nb, jl) into stage st, and with dinv the
 // windows of row i's inverse diagonal block and right-hand side; always
-// commits a group
-template <class E>
+// commits a group.  PARTS selects the copies: 1 the matrix, inverse
+// diagonal and right-hand side (constant during a sweep), 2 the x windows.
+template <class E, int PARTS = 3>
 __device__ __forceinline__ void row_stage_issue(bool valid, int b0, int nb, int jl, int lane,
                                                 const E* __restrict__ M, const E* xa, RowStage<E>* st, int i = 0,
                                                 const E* __restrict__ dinv = nullptr, const E* __restrict__ b = nullptr) {
   typedef StageGeom<E> G;
   const int ns = min(nb, kStageBlocks);
   // column ids of the blocks whose x chunks this lane copies (two passes)
-  const int j0 = __shfl_sync(0xffffffffu, jl, min(lane / G::XCH, 31));
-  const int j1 = __shfl_sync(0xffffffffu, jl, min((lane + 32) / G::XCH, 31));
+  int j0 = 0, j1 = 0;
+  if (PARTS & 2) {
+    j0 = __shfl_sync(0xffffffffu, jl, min(lane / G::XCH, 31));
+    j1 = __shfl_sync(0xffffffffu, jl, min((lane + 32) / G::XCH, 31));
+  }
   if (valid) {
-    const E* g = M + (size_t)b0 * 25;
-    const int n16 = (int)(((reinterpret_cast<uintptr_t>(g) & 15) + (uintptr_t)ns * 25 * sizeof(E) + 15) >> 4);
-    const uint32_t sm = umma::smem_addr(st->m);
-    for (int c = lane; c < n16; c += 32) cp_async16(sm + 16 * c, chunk_of(g, c));
-    const uint32_t sx = umma::smem_addr(st->x);
-#pragma unroll
-    for (int pass = 0; pass < 2; pass++) {
-      const int c = lane + 32 * pass;
-      const int u = c / G::XCH;
-      if (u < ns) cp_async16(sx + 16 * c, chunk_of(xa + (size_t)(pass ? j1 : j0) * 5, c % G::XCH));
+    if (PARTS & 1) {
+      const E* g = M + (size_t)b0 * 25;
+      const int n16 = (int)(((reinterpret_cast<uintptr_t>(g) & 15) + (uintptr_t)ns * 25 * sizeof(E) + 15) >> 4);
+      const uint32_t sm = umma::smem_addr(st->m);
+      for (int c = lane; c < n16; c += 32) cp_async16(sm + 16 * c, chunk_of(g, c));
     }
-    if (dinv) {
+    if (PARTS & 2) {
+      const uint32_t sx = umma::smem_addr(st->x);
+#pragma unroll
+      for (int pass = 0; pass < 2; pass++) {
+        const int c = lane + 32 * pass;
+        const int u = c / G::XCH;
+        if (u < ns) cp_async16(sx + 16 * c, chunk_of(xa + (size_t)(pass ? j1 : j0) * 5, c % G::XCH));
+      }
+    }
+    if ((PARTS & 1) && dinv) {
       if (lane < G::DCH) cp_async16(umma::smem_addr(st->dinv) + 16 * lane, chunk_of(dinv + (size_t)i * 25, lane));
       else if (lane < G::DCH + G::BCH)
         cp_async16(umma::smem_addr(st->b) + 16 * (lane - G::DCH), chunk_of(b + (size_t)i * 5, lane - G::DCH));
@@ -986,25 +994,45 @@ __global__ void __launch_bounds__(256, 4) k_spmv_staged(int nnode, const int* __
   cp_async_wait<0>();
 }
 
+// The first two rows of a warp in one colour of a sweep: their descriptors
+// and column indices, and the copies that do not depend on x (matrix,
+// inverse diagonal, right-hand side; two groups when the warp has rows).
+// Issued before the barrier that ends the previous colour.
+template <class E>
+__device__ __forceinline__ void sgs_head(int nrows, const int4* __restrict__ desc, const int* __restrict__ ja,
+                                         const E* __restrict__ M, const E* __restrict__ dinv,
+                                         const E* __restrict__ b, int g, const int W, RowStage<E>* st, int4& dA,
+                                         int& jA, int4& dB, int& jB) {
+  const int lane = threadIdx.x & 31;
+  const int4 none = make_int4(-1, 0, 0, 0);
+  dA = g < nrows ? desc[g] : none;
+  dB = g + W < nrows ? desc[g + W] : none;
+  jA = (dA.x >= 0 && lane < dA.z) ? ja[dA.y + lane] : 0;
+  jB = (dB.x >= 0 && lane < dB.z) ? ja[dB.y + lane] : 0;
+  if (g >= nrows) return;
+  row_stage_issue<E, 1>(true, dA.y, dA.z, jA, lane, M, nullptr, &st[0], dA.x, dinv, b);
+  row_stage_issue<E, 1>(dB.x >= 0, dB.y, dB.z, jB, lane, M, nullptr, &st[1], dB.x, dinv, b);
+}
+
 // The rows of one colour of a sweep through the staged pipeline (sgs_rows'
 // arithmetic on staged data), E the element type of blocks and vectors:
 // desc gives the rows in colour order, g the warp's first row, W the number
-// of warps.  Drains its copies before returning.
+// of warps, and (dA, jA, dB, jB) the head sgs_head read and started.
+// Drains its copies before returning.
 template <class E>
 __device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restrict__ desc, const int* __restrict__ ja,
                                                 const E* __restrict__ M, const E* __restrict__ dinv,
-                                                const E* __restrict__ b, E* x, int g, const int W, RowStage<E>* st) {
+                                                const E* __restrict__ b, E* x, int g, const int W, RowStage<E>* st,
+                                                int4 dA, int jA, int4 dB, int jB) {
   const int lane = threadIdx.x & 31;
   if (g >= nrows) return;
   const int r = lane / 5, c = lane % 5;
   const int4 none = make_int4(-1, 0, 0, 0);
   auto cols = [&](const int4& d) { return (d.x >= 0 && lane < d.z) ? ja[d.y + lane] : 0; };
-  int4 dA = desc[g];
-  int jA = cols(dA);
-  int4 dB = g + W < nrows ? desc[g + W] : none;
-  int jB = cols(dB);
-  row_stage_issue<E>(true, dA.y, dA.z, jA, lane, M, x, &st[0], dA.x, dinv, b);
-  row_stage_issue<E>(dB.x >= 0, dB.y, dB.z, jB, lane, M, x, &st[1], dB.x, dinv, b);
+  // groups: head A, head B, x of A, x of B, then one per further row, so
+  // the wait for all but the two newest completes row A's copies
+  row_stage_issue<E, 2>(true, dA.y, dA.z, jA, lane, M, x, &st[0]);
+  row_stage_issue<E, 2>(dB.x >= 0, dB.y, dB.z, jB, lane, M, x, &st[1]);
   int gC = g + 2 * W;
   int4 dC = gC < nrows ? desc[gC] : none;
   int jC = cols(dC);
@@ -1046,8 +1074,10 @@ __device__ __forceinline__ void sgs_rows_staged(int nrows, const int4* __restric
 
 // nsweeps sweeps in one cooperative launch through the staged pipeline
 // (k_sgs_sweep's phases and barriers); FP32 or FP64 blocks and vectors.
+// Each warp starts the x-independent copies of its first two rows of the
+// next colour before the barrier, so they overlap the wait.
 template <class E>
-__global__ void __launch_bounds__(256) k_sgs_sweep_staged(int ncolor, const int* __restrict__ cptr,
+__global__ void __launch_bounds__(256, sizeof(E) == 8 ? 2 : 4) k_sgs_sweep_staged(int ncolor, const int* __restrict__ cptr,
                                                           const int4* __restrict__ desc, const int* __restrict__ ja,
                                                           const E* __restrict__ M, const E* __restrict__ dinv,
                                                           const E* __restrict__ b, E* x, int nsweeps,
@@ -1056,12 +1086,27 @@ __global__ void __launch_bounds__(256) k_sgs_sweep_staged(int ncolor, const int*
   RowStage<E>* st = reinterpret_cast<RowStage<E>*>(smem_raw) + (threadIdx.x >> 5) * kRowStages;
   const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
   const int nphase = nsweeps * 2 * ncolor;
-  for (int p = 0; p < nphase; p++) {
+  auto colour = [&](int p) {
     const int cc = p % ncolor, dir = (p / ncolor) & 1;
-    const int c = dir == 0 ? cc : ncolor - 1 - cc;
-    const int r0 = cptr[c], nr = cptr[c + 1] - r0;
-    sgs_rows_staged<E>(nr, desc + r0, ja, M, dinv, b, x, g, W, st);
-    if (p + 1 < nphase && !grid_barrier(bar, gridDim.x, err)) return;
+    return dir == 0 ? cc : ncolor - 1 - cc;
+  };
+  int c = colour(0);
+  int r0 = cptr[c], nr = cptr[c + 1] - r0;
+  int4 dA, dB;
+  int jA, jB;
+  sgs_head<E>(nr, desc + r0, ja, M, dinv, b, g, W, st, dA, jA, dB, jB);
+  for (int p = 0; p < nphase; p++) {
+    sgs_rows_staged<E>(nr, desc + r0, ja, M, dinv, b, x, g, W, st, dA, jA, dB, jB);
+    if (p + 1 < nphase) {
+      c = colour(p + 1);
+      r0 = cptr[c];
+      nr = cptr[c + 1] - r0;
+      sgs_head<E>(nr, desc + r0, ja, M, dinv, b, g, W, st, dA, jA, dB, jB);
+      if (!grid_barrier(bar, gridDim.x, err)) {
+        cp_async_wait<0>();
+        return;
+      }
+    }
   }
 }
 
