@@ -421,6 +421,21 @@ def chemistry_study(args):
     for _ in range(args.steps):
         c.residual_dev(ref, fopts, ref_time, 1, d_qall.data_ptr(), d_b.data_ptr())
     rs_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    # the source-term Jacobian (one-sided differences of the chemistry source,
+    # one 9x9 block per node) on the same node records, device arrays
+    nq = len(spec["species"]) + 4
+    d_vol = torch.ones(n, dtype=torch.float64, device="cuda")
+    d_A = torch.empty((n, nq, nq), dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        c.source_jacobian_dev(ref, ref_time, n, d_rec.data_ptr(), d_vol.data_ptr(), d_A.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.source_jacobian_dev(ref, ref_time, n, d_rec.data_ptr(), d_vol.data_ptr(), d_A.data_ptr())
+    sj_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    nsj = 5000
+    t0 = time.perf_counter()
+    O.source_jacobian(recs[:nsj], np.ones(nsj), ref_time)
+    sj_cpu = time.perf_counter() - t0
     c.close()
     return {"workload": "5-species air, 6 reactions (chemModels/5speciesAir.rxn), %d nodes, T 300-8000 K" % n,
             "mnodes_per_s": n / (ms_avg * 1e-3) / 1e6, "ms": ms_avg,
@@ -438,6 +453,12 @@ def chemistry_study(args):
                         "box: %d edges, %d boundary half-edges, %d nodes; wall time of the device-array call" % (
                             ne, nb, n),
                 "ms": rs_ms, "medges_per_s": ne / (rs_ms * 1e-3) / 1e6},
+            "source_jacobian": {
+                "what": "SourceTermJacobian: one-sided differences of the chemistry source, a %dx%d block per node, "
+                        "%d nodes (records as above); wall time of the device-array call" % (nq, nq, n),
+                "ms": sj_ms, "mnodes_per_s": n / (sj_ms * 1e-3) / 1e6,
+                "cpu_baseline": {"mnodes_per_s": nsj / sj_cpu / 1e6, "cores": 1, "kind": "port",
+                                 "sample": "%d nodes by the oracle, 1 thread" % nsj}},
             "temperature_newton": {
                 "what": "ConservativeToNative: FP64 temperature Newton from total energy, %d nodes, 250-6000 K, "
                         "stored pressure x1.3 as the start; wall time of the device-array call" % n,

@@ -392,6 +392,16 @@ typedef struct {
   double beta, pref;
   int symmetry2D;
 } pcfd_chem_flux_opts;
+/* EqnSet::SourceTermJacobian (ucs/eqnset.tcc:163) of the reacting set as
+ * the Jacobian assembly takes it (ucs/jacobian.tcc:201, which subtracts it
+ * from the diagonal block): q [n][6 + 3 ns] node records (rhoi and T read),
+ * vol [n] dual volumes -> A [n][(ns + 4)^2] row-major, A[j (ns + 4) + i] =
+ * (S_j(Q + h e_i) - S_j(Q)) / h with h = 1e-8 on the non-dimensional native
+ * value i, S = SourceTerm (ucs/compressibleFR.tcc:1276, reactions on) =
+ * vol * wdot / (ref_density / ref_time) in the species rows, zero in the
+ * momentum and energy rows.  dev as above (q, vol, A). */
+PCFD_API int pcfd_chem_source_jacobian(pcfd_chem_t c, const pcfd_chem_ref* ref, double ref_time, long long n,
+                                       const double* q, const double* vol, double* A, int dev);
 /* CompressibleFREqnSet::HLLCFlux (ucs/compressibleFR.tcc:301; RoeFlux
  * forwards to it, :293) on a static grid: q [nnode][6 + 3 ns] node records
  * (rhoi, u, v, w, T | P, rho, cvi, concentrations, as ComputeAuxiliaryVariables

@@ -412,3 +412,49 @@ void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, co
     }
   }
 }
+
+/* CompressibleFREqnSet::SourceTerm (ucs/compressibleFR.tcc:1276), reactions
+ * on, no gravity: vol * wdot made non-dimensional by ref_density / ref_time
+ * in the species rows, zero in the momentum and energy rows.  Reads rhoi and
+ * T of the native record only. */
+static void fr_source(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q, double vol,
+                      double ref_time, double* source) {
+  const int ns = m->nspecies;
+  double rhoi[PCFD_CHEM_MAX_SPECIES], wdot[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns + 4; i++) source[i] = 0.0;
+  const double T = Q[ns + 3] * ref->temperature;
+  for (int i = 0; i < ns; i++) rhoi[i] = Q[i] * ref->density;
+  oracle_chem_rates(m, rhoi, T, wdot);
+  for (int i = 0; i < ns; i++) {
+    wdot[i] /= (ref->density / ref_time);
+    source[i] = vol * wdot[i];
+  }
+}
+
+/* EqnSet::SourceTermJacobian (ucs/eqnset.tcc:163) on one node record Q:
+ * A[j*neqn + i] = (S_j(Q + h e_i) - S_j(Q)) / h, h = 1e-8, one column per
+ * native value.  The reference recomputes the auxiliary values of the
+ * perturbed record before each SourceTerm call; SourceTerm reads none of
+ * them, so they are not formed here. */
+void oracle_chem_source_jacobian(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double ref_time,
+                                 const double* Q, double vol, double* A) {
+  const int ns = m->nspecies, neqn = ns + 4;
+  const double h = 1.0e-8;
+  double source[PCFD_CHEM_MAX_SPECIES + 4], sourceP[PCFD_CHEM_MAX_SPECIES + 4];
+  double QP[PCFD_CHEM_MAX_SPECIES + 4];
+  for (int k = 0; k < neqn * neqn; k++) A[k] = 0.0;
+  fr_source(m, ref, Q, vol, ref_time, source);
+  for (int i = 0; i < neqn; i++) {
+    for (int k = 0; k < neqn; k++) QP[k] = Q[k];
+    QP[i] += h;
+    fr_source(m, ref, QP, vol, ref_time, sourceP);
+    for (int j = 0; j < neqn; j++) A[j * neqn + i] = (sourceP[j] - source[j]) / h;
+  }
+}
+
+void oracle_chem_source_jacobian_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double ref_time, long long n,
+                                   const double* q, const double* vol, double* A) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  for (long long p = 0; p < n; p++)
+    oracle_chem_source_jacobian(m, ref, ref_time, q + p * nv, vol[p], A + p * neqn * neqn);
+}

@@ -76,6 +76,10 @@ long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref,
 void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
                           const pcfd_mesh_view* mv, const double* q, double ref_time, int reactions, double* b,
                           double* norms);
+void oracle_chem_source_jacobian(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double ref_time,
+                                 const double* Q, double vol, double* A);
+void oracle_chem_source_jacobian_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double ref_time, long long n,
+                                   const double* q, const double* vol, double* A);
 
 #ifdef __cplusplus
 }

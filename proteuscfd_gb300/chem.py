@@ -172,6 +172,23 @@ class ChemModel:
                                               edges_ptr, avec_ptr, flux_ptr, C.byref(bad), 1), "pcfd_chem_hllc_flux")
         return bad.value
 
+    def source_jacobian(self, ref, ref_time, q, vol):
+        """SourceTermJacobian per node: q [n][6 + 3 ns] records, vol [n] ->
+        A [n][ns + 4][ns + 4], A[p, j, i] = dS_j / dQ_i by one-sided
+        differences (h = 1e-8)."""
+        n = len(vol)
+        q, vol = self._arr(q, (n, 6 + 3 * self.nspecies)), self._arr(vol, (n,))
+        neqn = self.nspecies + 4
+        A = np.empty((n, neqn, neqn))
+        N.check(self._lib.pcfd_chem_source_jacobian(self._h, C.byref(ref), float(ref_time), n, N.dptr(q), N.dptr(vol),
+                                                    N.dptr(A), 0), "pcfd_chem_source_jacobian")
+        return A
+
+    def source_jacobian_dev(self, ref, ref_time, n, q_ptr, vol_ptr, A_ptr):
+        """The same on device addresses."""
+        N.check(self._lib.pcfd_chem_source_jacobian(self._h, C.byref(ref), float(ref_time), int(n), q_ptr, vol_ptr,
+                                                    A_ptr, 1), "pcfd_chem_source_jacobian")
+
     def attach_mesh(self, mesh):
         """Copies the mesh's edges, areas, boundary half-edges and dual
         volumes to the device for residual()."""

@@ -131,21 +131,23 @@ __device__ double equilibrium_const(const pcfd_chem_model& m, const pcfd_chem_re
   return Kc;
 }
 
-// mass production rates of one node (rhoi [ns] kg/m^3, T K -> wdot [ns])
-__device__ void node_rates(const pcfd_chem_model& m, const double* rhoi, const double T, double* wdot) {
+// mass production rates of one node (rhoi [ns] kg/m^3 -> wdot [ns]) with
+// the rate constants of reaction j given by consts(j, Kf, Kb)
+template <class Consts>
+__device__ __forceinline__ void rates_with(const pcfd_chem_model& m, const double* rhoi, Consts&& consts,
+                                          double* wdot) {
   const int ns = m.nspecies;
   double X[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES];
   for (int k = 0; k < ns; k++) {
     X[k] = rhoi[k] / m.mw[k];
     w[k] = 0.0;
   }
-  const double logT = log(T);
   double Xsum = 0.0;
   for (int k = 0; k < ns; k++) Xsum += X[k];
   for (int j = 0; j < m.nreactions; j++) {
     const pcfd_chem_reaction& r = m.rx[j];
-    const double Kf = forward_rate(r, T);
-    const double Kb = Kf / equilibrium_const(m, r, T, logT);
+    double Kf, Kb;
+    consts(j, Kf, Kb);
     double form = 1.0, dest = 1.0;
     for (int l = 0; l < r.nlocal; l++) {
       const double x = X[r.global[l]];
@@ -171,6 +173,21 @@ __device__ void node_rates(const pcfd_chem_model& m, const double* rhoi, const d
   for (int k = 0; k < ns; k++) wdot[k] = w[k];
 }
 
+// forward (Arrhenius) and backward (forward / equilibrium constant) rate
+// constants of reaction j at T
+__device__ __forceinline__ void rate_consts(const pcfd_chem_model& m, int j, double T, double logT, double& Kf,
+                                            double& Kb) {
+  const pcfd_chem_reaction& r = m.rx[j];
+  Kf = forward_rate(r, T);
+  Kb = Kf / equilibrium_const(m, r, T, logT);
+}
+
+// mass production rates of one node (rhoi [ns] kg/m^3, T K -> wdot [ns])
+__device__ void node_rates(const pcfd_chem_model& m, const double* rhoi, const double T, double* wdot) {
+  const double logT = log(T);
+  rates_with(m, rhoi, [&](int j, double& Kf, double& Kb) { rate_consts(m, j, T, logT, Kf, Kb); }, wdot);
+}
+
 __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem_model* __restrict__ gm,
                                                     const double* __restrict__ rhoi, const double* __restrict__ Tn,
                                                     double* __restrict__ wdot) {
@@ -185,6 +202,73 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= n) return;
   node_rates(m, rhoi + p * m.nspecies, Tn[p], wdot + p * m.nspecies);
+}
+
+// EqnSet::SourceTermJacobian (ucs/eqnset.tcc:163) of the reacting set, one
+// thread per node: A[j*neqn + i] = (S_j(Q + h e_i) - S_j(Q)) / h, h = 1e-8,
+// S = SourceTerm (ucs/compressibleFR.tcc:1276) = vol * wdot / (ref_density /
+// ref_time) in the species rows.  SourceTerm reads rhoi and T only, and the
+// rate constants depend on T only: the ns species columns reuse the base
+// point's constants (the same values the reference recomputes), and only
+// the T column forms them again.  Every entry is formed as the reference
+// forms it, so the velocity columns and the momentum and energy rows are
+// (S - S) / h.
+__global__ void __launch_bounds__(128) k_chem_source_jac(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                         pcfd_chem_ref ref, double ref_time,
+                                                         const double* __restrict__ q, const double* __restrict__ vol,
+                                                         double* __restrict__ A) {
+  __shared__ pcfd_chem_model m;
+  {
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gm);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&m);
+    for (int k = threadIdx.x; k < (int)(sizeof(pcfd_chem_model) / 8); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int ns = m.nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  const double h = 1.0e-8;
+  const double* Q = q + p * nv;
+  const double V = vol[p];
+  const double scale = ref.density / ref_time;
+  double* Ap = A + p * (long long)neqn * neqn;
+  double rhoi[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES], S0[PCFD_CHEM_MAX_SPECIES + 4];
+  double Kf[PCFD_CHEM_MAX_REACTIONS], Kb[PCFD_CHEM_MAX_REACTIONS];
+  for (int k = 0; k < ns; k++) rhoi[k] = Q[k] * ref.density;
+  const double T0 = Q[ns + 3] * ref.temperature;
+  {
+    const double logT = log(T0);
+    for (int j = 0; j < m.nreactions; j++) rate_consts(m, j, T0, logT, Kf[j], Kb[j]);
+  }
+  auto stored = [&](int j, double& kf, double& kb) {
+    kf = Kf[j];
+    kb = Kb[j];
+  };
+  rates_with(m, rhoi, stored, w);
+  for (int k = 0; k < ns; k++) S0[k] = V * (w[k] / scale);
+  for (int k = ns; k < neqn; k++) S0[k] = 0.0;
+  // a column of the difference quotients from the perturbed source in w
+  auto column = [&](int i) {
+    for (int j = 0; j < ns; j++) Ap[j * neqn + i] = (V * (w[j] / scale) - S0[j]) / h;
+    for (int j = ns; j < neqn; j++) Ap[j * neqn + i] = (0.0 - S0[j]) / h;
+  };
+  for (int i = 0; i < ns; i++) {
+    const double keep = rhoi[i];
+    rhoi[i] = (Q[i] + h) * ref.density;
+    rates_with(m, rhoi, stored, w);
+    rhoi[i] = keep;
+    column(i);
+  }
+  for (int i = ns; i < ns + 3; i++) {
+    for (int j = 0; j < ns; j++) Ap[j * neqn + i] = (S0[j] - S0[j]) / h;
+    for (int j = ns; j < neqn; j++) Ap[j * neqn + i] = (0.0 - S0[j]) / h;
+  }
+  {
+    const double T = (Q[ns + 3] + h) * ref.temperature;
+    const double logT = log(T);
+    rates_with(m, rhoi, [&](int j, double& kf, double& kb) { rate_consts(m, j, T, logT, kf, kb); }, w);
+    column(ns + 3);
+  }
 }
 
 // ---- node state of the reacting equation set ------------------------------
@@ -867,6 +951,22 @@ PCFD_API int pcfd_chem_aux(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n,
   return node_call<2, 3>(c, n, dev, {rhoi, T}, {ns, 1}, {P, cvi, mol}, {1, ns, ns}, nullptr,
                          [&](const double* const* in, double* const* out) {
                            k_chem_aux<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], out[0], out[1], out[2]);
+                         });
+}
+
+PCFD_API int pcfd_chem_source_jacobian(pcfd_chem_t h, const pcfd_chem_ref* ref, double ref_time, long long n,
+                                       const double* q, const double* vol, double* A, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || !(ref_time > 0.0) || n < 0 || (n > 0 && (!q || !vol || !A))) {
+    pcfd_set_last_error("pcfd_chem_source_jacobian: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  const pcfd_chem_ref r = *ref;
+  return node_call<2, 1>(c, n, dev, {q, vol}, {nv, 1}, {A}, {neqn * neqn}, nullptr,
+                         [&](const double* const* in, double* const* out) {
+                           k_chem_source_jac<<<CHEM_GRID(n)>>>(n, c->dev, r, ref_time, in[0], in[1], out[0]);
                          });
 }
 

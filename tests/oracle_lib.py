@@ -60,6 +60,8 @@ def lib():
                                                   C.POINTER(N.ChemFluxOpts), _DP, C.c_longlong, _IP, _DP, _DP]),
             "oracle_chem_residual": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.ChemFluxOpts),
                                             C.POINTER(N.MeshView), _DP, C.c_double, C.c_int, _DP, _DP]),
+            "oracle_chem_source_jacobian_n": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_double,
+                                                     C.c_longlong, _DP, _DP, _DP]),
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
@@ -375,6 +377,15 @@ class OracleChemState:
         bad = self.L.oracle_chem_hllc_n(C.byref(self.m), C.byref(self.ref), C.byref(opts), dp(q), len(edges),
                                         ip(edges), dp(avec), dp(flux))
         return flux, bad
+
+    def source_jacobian(self, q, vol, ref_time):
+        """SourceTermJacobian per node -> [n][ns + 4][ns + 4]."""
+        q = np.ascontiguousarray(q, np.float64)
+        vol = np.ascontiguousarray(vol, np.float64)
+        A = np.empty((len(vol), self.ns + 4, self.ns + 4))
+        self.L.oracle_chem_source_jacobian_n(C.byref(self.m), C.byref(self.ref), float(ref_time), len(vol), dp(q),
+                                             dp(vol), dp(A))
+        return A
 
     def residual(self, opts, mesh, q, ref_time, reactions):
         """SpatialResidual of the reacting set (first order, inviscid)."""

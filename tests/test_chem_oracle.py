@@ -153,3 +153,43 @@ def test_fr_residual_freestream_preserved():
     ns = O.ns
     scale = np.abs(q[0, :ns]).max() * np.abs(vel).max() * np.asarray(m.edge_area)[:, 3].max()
     assert np.abs(b).max() < 1e-13 * max(scale, 1.0), np.abs(b).max()
+
+
+def test_fr_source_jacobian_against_central_differences():
+    """The oracle's SourceTermJacobian (one-sided, h = 1e-8) against central
+    differences of the oracle's own source term with a larger step: equal to
+    the one-sided truncation and rounding error.  Velocity columns and the
+    momentum and energy rows are zero, and the species rows of every column
+    sum to zero (mass is conserved by every reaction)."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    ref, rhoi, vel, T = fr_states(40, seed=21)
+    T = np.clip(T, 1500.0 / ref.temperature, None)
+    q = fr_records(ref, rhoi, vel, T)
+    vol = np.random.default_rng(5).uniform(0.5, 2.0, size=len(T))
+    ref_time = 2.5e-4
+    O = OracleChemState(model_struct(mechanism()), ref)
+    A = O.source_jacobian(q, vol, ref_time)
+    ns = O.ns
+    neqn = ns + 4
+    assert A.shape == (len(T), neqn, neqn)
+    assert np.all(A[:, ns:, :] == 0.0) and np.all(A[:, :, ns:ns + 3] == 0.0)
+
+    def source(Q):
+        w = chem_rates(model_struct(mechanism()), (Q[:, :ns] * ref.density).copy(), Q[:, ns + 3] * ref.temperature)
+        return vol[:, None] * (w / (ref.density / ref_time))
+
+    S0 = source(q)
+    smax = np.abs(S0).max(axis=1)
+    cols = list(range(ns)) + [ns + 3]
+    for i in cols:
+        hc = 1e-5 * np.abs(q[:, i]).max()
+        qp, qm = q.copy(), q.copy()
+        qp[:, i] += hc
+        qm[:, i] -= hc
+        Ac = (source(qp) - source(qm)) / (2 * hc)
+        scale = np.abs(Ac).max(axis=1) + smax
+        err = np.abs(A[:, :ns, i] - Ac).max(axis=1) / scale
+        assert err.max() < 1e-5, (i, err.max())
+        colsum = np.abs(A[:, :ns, i].sum(axis=1)) / scale
+        assert colsum.max() < 5e-5, (i, colsum.max())

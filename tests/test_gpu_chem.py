@@ -212,3 +212,61 @@ def test_fr_residual_parity(reactions):
     nd = C.residual_dev(ref, opts, ref_time, reactions, dq.data_ptr(), db.data_ptr())
     assert np.array_equal(db.cpu().numpy(), b) and np.array_equal(nd, norms)
     C.close()
+
+
+def test_source_jacobian_parity():
+    """SourceTermJacobian on the GPU against the oracle's, node by node, on
+    seeded reacting states (host arrays, then device arrays).  The one-sided
+    difference divides the rates' last-ulp differences between CUDA's and
+    the host's libm by h = 1e-8, so entries are compared to 1e-5 of the
+    node's scale (largest entry of the column plus the largest source
+    value); the zero rows and columns are exact."""
+    import torch
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    ref, rhoi, vel, T = fr_states(3000, seed=23)
+    q = fr_records(ref, rhoi, vel, T)
+    vol = np.random.default_rng(6).uniform(0.5, 2.0, size=len(T))
+    ref_time = 2.5e-4
+    C = ChemModel(spec)
+    A = C.source_jacobian(ref, ref_time, q, vol)
+    Ao = OracleChemState(model_struct(spec), ref).source_jacobian(q, vol, ref_time)
+    ns = C.nspecies
+    assert np.all(A[:, ns:, :] == 0.0) and np.all(A[:, :, ns:ns + 3] == 0.0)
+    w = chem_rates(model_struct(spec), (q[:, :ns] * ref.density).copy(), q[:, ns + 3] * ref.temperature)
+    smax = np.abs(vol[:, None] * w / (ref.density / ref_time)).max(axis=1)
+    scale = np.abs(Ao).max(axis=1) + smax[:, None]
+    err = (np.abs(A - Ao) / scale[:, None, :]).max()
+    assert err < 1e-5, err
+    dq = torch.from_numpy(q).cuda()
+    dv = torch.from_numpy(vol).cuda()
+    dA = torch.empty(A.shape, dtype=torch.float64, device="cuda")
+    C.source_jacobian_dev(ref, ref_time, len(vol), dq.data_ptr(), dv.data_ptr(), dA.data_ptr())
+    assert np.array_equal(dA.cpu().numpy(), A)
+    C.close()
+
+
+def test_source_jacobian_full_size_mass_conservation():
+    """At the reacting box's size (2,007,040 nodes) the species rows of every
+    column of the source Jacobian sum to zero up to the difference quotient's
+    rounding, as every reaction conserves mass."""
+    from chem_cases import fr_states
+    spec = mechanism()
+    C = ChemModel(spec)
+    ref, rhoi, vel, T = fr_states(2007040, seed=24)
+    P, cvi, mol = C.aux(ref, rhoi, T)
+    q = np.ascontiguousarray(np.c_[rhoi, vel, T, P, rhoi.sum(axis=1), cvi, mol])
+    vol = np.full(len(T), 1.0)
+    ref_time = 2.5e-4
+    A = C.source_jacobian(ref, ref_time, q, vol)
+    ns = C.nspecies
+    assert np.all(np.isfinite(A))
+    # the quotient's rounding scales with the source itself where the
+    # reactions are frozen (low T), so the bound includes it
+    w = C.production_rates(rhoi * ref.density, T * ref.temperature)
+    smax = np.abs(w / (ref.density / ref_time)).max(axis=1)
+    colsum = np.abs(A[:, :ns, :].sum(axis=1))
+    scale = np.abs(A[:, :ns, :]).max(axis=1) + smax[:, None]
+    assert (colsum / scale).max() < 1e-4, (colsum / scale).max()
+    C.close()
