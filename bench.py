@@ -436,6 +436,18 @@ def chemistry_study(args):
     t0 = time.perf_counter()
     O.source_jacobian(recs[:nsj], np.ones(nsj), ref_time)
     sj_cpu = time.perf_counter() - t0
+    # the native-variable temporal terms added in place into those blocks
+    rng = np.random.default_rng(9)
+    d_dtau = torch.from_numpy(rng.uniform(1e-3, 1e-1, size=n)).cuda()
+    d_beta = torch.from_numpy(rng.uniform(0.2, 1.0, size=n)).cuda()
+    for _ in range(3):
+        c.temporal_terms_dev(ref, n, d_rec.data_ptr(), d_vol.data_ptr(), d_dtau.data_ptr(), d_beta.data_ptr(), 1.0,
+                             0.0, 0, d_A.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.temporal_terms_dev(ref, n, d_rec.data_ptr(), d_vol.data_ptr(), d_dtau.data_ptr(), d_beta.data_ptr(), 1.0,
+                             0.0, 0, d_A.data_ptr())
+    tt_ms = (time.perf_counter() - t0) / args.steps * 1e3
     c.close()
     return {"workload": "5-species air, 6 reactions (chemModels/5speciesAir.rxn), %d nodes, T 300-8000 K" % n,
             "mnodes_per_s": n / (ms_avg * 1e-3) / 1e6, "ms": ms_avg,
@@ -453,6 +465,10 @@ def chemistry_study(args):
                         "box: %d edges, %d boundary half-edges, %d nodes; wall time of the device-array call" % (
                             ne, nb, n),
                 "ms": rs_ms, "medges_per_s": ne / (rs_ms * 1e-3) / 1e6},
+            "temporal_terms": {
+                "what": "ContributeTemporalTerms: native-variable temporal terms with beta preconditioning added in "
+                        "place into %d %dx%d blocks; wall time of the device-array call" % (n, nq, nq),
+                "ms": tt_ms, "mnodes_per_s": n / (tt_ms * 1e-3) / 1e6},
             "source_jacobian": {
                 "what": "SourceTermJacobian: one-sided differences of the chemistry source, a %dx%d block per node, "
                         "%d nodes (records as above); wall time of the device-array call" % (nq, nq, n),

@@ -402,6 +402,17 @@ typedef struct {
  * momentum and energy rows.  dev as above (q, vol, A). */
 PCFD_API int pcfd_chem_source_jacobian(pcfd_chem_t c, const pcfd_chem_ref* ref, double ref_time, long long n,
                                        const double* q, const double* vol, double* A, int dev);
+/* CompressibleFREqnSet::ContributeTemporalTerms (ucs/compressibleFR.tcc:1319)
+ * as ComputeJacobians' temporal loop calls it per node (ucs/jacobian.tcc:214):
+ * q [n][6 + 3 ns] node records, vol [n], dtau [n] (pseudo-time steps), beta
+ * [n] (Gupta's preconditioning parameter), cnp1 (1, or 1.5 for second order
+ * in time), dt (the real time step, read when local_ts != 0) -> A [n][(ns +
+ * 4)^2] row-major diagonal blocks, IN AND OUT: the temporal terms (vol/dt
+ * times dq/dQ, conservative over native, with the beta terms in the
+ * temperature column) are added to what A holds.  dev as above. */
+PCFD_API int pcfd_chem_temporal_terms(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* q,
+                                      const double* vol, const double* dtau, const double* beta, double cnp1,
+                                      double dt, int local_ts, double* A, int dev);
 /* CompressibleFREqnSet::HLLCFlux (ucs/compressibleFR.tcc:301; RoeFlux
  * forwards to it, :293) on a static grid: q [nnode][6 + 3 ns] node records
  * (rhoi, u, v, w, T | P, rho, cvi, concentrations, as ComputeAuxiliaryVariables

@@ -458,3 +458,123 @@ void oracle_chem_source_jacobian_n(const pcfd_chem_model* m, const pcfd_chem_ref
   for (long long p = 0; p < n; p++)
     oracle_chem_source_jacobian(m, ref, ref_time, q + p * nv, vol[p], A + p * neqn * neqn);
 }
+
+/* CompressibleFREqnSet::GetFluidProperties (ucs/compressibleFR.tcc:1523)
+ * over ChemModel::GetFluidProperties (ucs/chem.tcc:545): the mixture R and
+ * the frozen speed of sound squared, non-dimensional */
+static void fr_fluid_R_c2(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T,
+                          double* R, double* c2) {
+  const int ns = m->nspecies;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES], X[PCFD_CHEM_MAX_SPECIES];
+  const double s_ref = ref->velocity * ref->velocity / ref->temperature;
+  const double Tdim = T * ref->temperature;
+  double rho = 0.0, RDim = 0.0, cp = 0.0, cv = 0.0;
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[i] * ref->density;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  for (int i = 0; i < ns; i++) RDim += rhoiDim[i] * (UNIV_R_ / m->mw[i]);
+  RDim /= rho;
+  for (int i = 0; i < ns; i++) X[i] = rhoiDim[i] / rho;
+  for (int i = 0; i < ns; i++) cp += species_cp(m, i, Tdim) * X[i];
+  for (int i = 0; i < ns; i++) cv += X[i] * (species_cp(m, i, Tdim) - UNIV_R_ / m->mw[i]);
+  const double gamma = cp / cv;
+  *R = RDim / s_ref;
+  *c2 = (gamma * RDim * Tdim) / (ref->velocity * ref->velocity);
+}
+
+/* ChemModel::dEtdP_dEtdRhoi (ucs/chem.tcc:829) with dRmixdRhoi (:862), at
+ * constant T (dimensional arguments); returns dEt/dP */
+static double fr_dEt(const pcfd_chem_model* m, const double* rhoi, double T, double v2, double* dEtdRhoi) {
+  const int ns = m->nspecies;
+  const double hv2 = 0.5 * v2;
+  double rhomix = 0.0, Rmix = 0.0;
+  for (int i = 0; i < ns; i++) {
+    rhomix += rhoi[i];
+    Rmix += rhoi[i] * (UNIV_R_ / m->mw[i]);
+  }
+  Rmix /= rhomix;
+  const double dPdrhomix = Rmix * T; /* IdealGasEOS::GetdP_dRho (ucs/EOS.tcc:60) */
+  const double dPdRmix = rhomix * T; /* GetdP_dR (:54) */
+  for (int i = 0; i < ns; i++) {
+    double dR = (UNIV_R_ / m->mw[i]) * (rhomix - rhoi[i]) / (rhomix * rhomix);
+    for (int j = 0; j < ns; j++) {
+      if (j == i) continue;
+      dR -= (UNIV_R_ / m->mw[j]) * rhoi[j] / (rhomix * rhomix);
+    }
+    dEtdRhoi[i] = hv2 + species_h(m, i, T) - (dPdrhomix + dPdRmix * dR);
+  }
+  double dEtdP = 0.0;
+  const double dTdP = 1.0 / (rhomix * Rmix); /* GetdT_dP (:42) */
+  for (int i = 0; i < ns; i++) dEtdP += rhoi[i] * species_cp(m, i, T) * dTdP;
+  dEtdP -= 1.0;
+  return dEtdP;
+}
+
+/* CompressibleFREqnSet::ContributeTemporalTerms (ucs/compressibleFR.tcc:1319)
+ * on one node record Q (rhoi, u, v, w, T, P, rho, ...): adds vol/dt terms
+ * times dq/dQ (conservative over native) with Gupta's beta preconditioning
+ * on the temperature column into the block A [(ns+4)^2]. */
+void oracle_chem_temporal(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q, double vol,
+                          double cnp1, double dt, double dtau, double beta, int local_ts, double* A) {
+  const int ns = m->nspecies, neqn = ns + 4;
+  const int uloc = ns, vloc = ns + 1, wloc = ns + 2, tloc = ns + 3;
+  double dEtdRhoi[PCFD_CHEM_MAX_SPECIES], rhoiDim[PCFD_CHEM_MAX_SPECIES], Yi[PCFD_CHEM_MAX_SPECIES];
+  double thetaOBetai[PCFD_CHEM_MAX_SPECIES];
+  const double vOverDt = local_ts ? cnp1 * vol / dt + vol / dtau : cnp1 * vol / dtau;
+  const double rho = Q[ns + 5], T = Q[tloc], P = Q[ns + 4];
+  const double u = Q[uloc], v = Q[vloc], w = Q[wloc];
+  const double rvOverDt = rho * vOverDt;
+  double v2 = u * u + v * v + w * w;
+  double R, c2;
+  fr_fluid_R_c2(m, ref, Q, T, &R, &c2);
+  const double s_ref = ref->velocity * ref->velocity / ref->temperature;
+  const double rhoDim = rho * ref->density;
+  const double TDim = T * ref->temperature;
+  v2 *= ref->velocity * ref->velocity;
+  (void)P;
+  for (int i = 0; i < ns; i++) {
+    rhoiDim[i] = Q[i] * ref->density;
+    Yi[i] = Q[i] / rho;
+  }
+  double dEtdP = fr_dEt(m, rhoiDim, TDim, v2, dEtdRhoi);
+  const double ref_detdrho = ref->specific_enthalpy * ref->density / ref->density;
+  for (int i = 0; i < ns; i++) dEtdRhoi[i] /= ref_detdrho;
+  const double ref_detdP = ref->specific_enthalpy * ref->density / ref->pressure;
+  dEtdP /= ref_detdP;
+  double dPdT = rhoDim * (R * s_ref); /* IdealGasEOS::GetdP_dT (ucs/EOS.tcc:66) */
+  dPdT /= (ref->pressure / ref->temperature);
+  const double oneOBeta = 1.0 / beta, oneMbeta = 1.0 - beta;
+  for (int i = 0; i < ns; i++) thetaOBetai[i] = (Yi[i] * oneMbeta / c2) * oneOBeta;
+  for (int i = 0; i < ns; i++) {
+    A[neqn * i + i] += vOverDt;
+    A[neqn * i + tloc] += thetaOBetai[i] * vOverDt * dPdT;
+  }
+  const int mloc[3] = {uloc, vloc, wloc};
+  const double vel[3] = {u, v, w};
+  for (int d = 0; d < 3; d++) {
+    double precond = 0.0;
+    for (int j = 0; j < ns; j++) {
+      A[neqn * mloc[d] + j] += vel[d] * vOverDt;
+      precond += thetaOBetai[j] * vel[d];
+    }
+    A[neqn * mloc[d] + mloc[d]] += rvOverDt;
+    A[neqn * mloc[d] + tloc] += precond * vOverDt * dPdT;
+  }
+  double precond = 0.0;
+  for (int j = 0; j < ns; j++) {
+    A[neqn * tloc + j] += dEtdRhoi[j] * vOverDt;
+    precond += dEtdRhoi[j] * thetaOBetai[j];
+  }
+  A[neqn * tloc + uloc] += u * rvOverDt;
+  A[neqn * tloc + vloc] += v * rvOverDt;
+  A[neqn * tloc + wloc] += w * rvOverDt;
+  precond += dEtdP * oneOBeta;
+  A[neqn * tloc + tloc] += precond * vOverDt * dPdT;
+}
+
+void oracle_chem_temporal_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,
+                            const double* vol, const double* dtau, const double* beta, double cnp1, double dt,
+                            int local_ts, double* A) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  for (long long p = 0; p < n; p++)
+    oracle_chem_temporal(m, ref, q + p * nv, vol[p], cnp1, dt, dtau[p], beta[p], local_ts, A + p * neqn * neqn);
+}

@@ -80,6 +80,11 @@ void oracle_chem_source_jacobian(const pcfd_chem_model* m, const pcfd_chem_ref* 
                                  const double* Q, double vol, double* A);
 void oracle_chem_source_jacobian_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double ref_time, long long n,
                                    const double* q, const double* vol, double* A);
+void oracle_chem_temporal(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q, double vol,
+                          double cnp1, double dt, double dtau, double beta, int local_ts, double* A);
+void oracle_chem_temporal_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,
+                            const double* vol, const double* dtau, const double* beta, double cnp1, double dt,
+                            int local_ts, double* A);
 
 #ifdef __cplusplus
 }

@@ -169,6 +169,8 @@ PROTOTYPES = {
     "pcfd_chem_conservative_to_native": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, C.c_int]),
     "pcfd_chem_native_to_conservative": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, C.c_int]),
     "pcfd_chem_aux": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, _P, C.c_int]),
+    "pcfd_chem_temporal_terms": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, C.c_double,
+                                           C.c_double, C.c_int, _P, C.c_int]),
     "pcfd_chem_source_jacobian": (C.c_int, [_P, C.POINTER(ChemRef), C.c_double, C.c_longlong, _P, _P, _P,
                                             C.c_int]),
     "pcfd_chem_hllc_flux": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_longlong, _P,

@@ -189,6 +189,28 @@ class ChemModel:
         N.check(self._lib.pcfd_chem_source_jacobian(self._h, C.byref(ref), float(ref_time), int(n), q_ptr, vol_ptr,
                                                     A_ptr, 1), "pcfd_chem_source_jacobian")
 
+    def temporal_terms(self, ref, q, vol, dtau, beta, cnp1=1.0, dt=0.0, local_ts=0, A=None):
+        """ContributeTemporalTerms per node: q [n][6 + 3 ns] records, vol,
+        dtau, beta [n] -> A [n][ns + 4][ns + 4] + the temporal terms (A zero
+        when not given)."""
+        n = len(vol)
+        neqn = self.nspecies + 4
+        q = self._arr(q, (n, 6 + 3 * self.nspecies))
+        vol, dtau, beta = self._arr(vol, (n,)), self._arr(dtau, (n,)), self._arr(beta, (n,))
+        A = np.zeros((n, neqn, neqn)) if A is None else np.array(A, dtype=np.float64, order="C", copy=True)
+        if A.shape != (n, neqn, neqn):
+            raise ValueError("temporal_terms: A must be [n][ns + 4][ns + 4]")
+        N.check(self._lib.pcfd_chem_temporal_terms(self._h, C.byref(ref), n, N.dptr(q), N.dptr(vol), N.dptr(dtau),
+                                                   N.dptr(beta), float(cnp1), float(dt), int(local_ts), N.dptr(A), 0),
+                "pcfd_chem_temporal_terms")
+        return A
+
+    def temporal_terms_dev(self, ref, n, q_ptr, vol_ptr, dtau_ptr, beta_ptr, cnp1, dt, local_ts, A_ptr):
+        """The same on device addresses; adds into the blocks at A_ptr."""
+        N.check(self._lib.pcfd_chem_temporal_terms(self._h, C.byref(ref), int(n), q_ptr, vol_ptr, dtau_ptr, beta_ptr,
+                                                   float(cnp1), float(dt), int(local_ts), A_ptr, 1),
+                "pcfd_chem_temporal_terms")
+
     def attach_mesh(self, mesh):
         """Copies the mesh's edges, areas, boundary half-edges and dual
         volumes to the device for residual()."""

@@ -131,17 +131,15 @@ __device__ double equilibrium_const(const pcfd_chem_model& m, const pcfd_chem_re
   return Kc;
 }
 
-// mass production rates of one node (rhoi [ns] kg/m^3 -> wdot [ns]) with
-// the rate constants of reaction j given by consts(j, Kf, Kb)
+// mass production rates of one node from its molar concentrations X [ns]
+// (rhoi / MW) -> wdot [ns], with the rate constants of reaction j given by
+// consts(j, Kf, Kb)
 template <class Consts>
-__device__ __forceinline__ void rates_with(const pcfd_chem_model& m, const double* rhoi, Consts&& consts,
+__device__ __forceinline__ void rates_with(const pcfd_chem_model& m, const double* X, Consts&& consts,
                                           double* wdot) {
   const int ns = m.nspecies;
-  double X[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES];
-  for (int k = 0; k < ns; k++) {
-    X[k] = rhoi[k] / m.mw[k];
-    w[k] = 0.0;
-  }
+  double w[PCFD_CHEM_MAX_SPECIES];
+  for (int k = 0; k < ns; k++) w[k] = 0.0;
   double Xsum = 0.0;
   for (int k = 0; k < ns; k++) Xsum += X[k];
   for (int j = 0; j < m.nreactions; j++) {
@@ -184,8 +182,10 @@ __device__ __forceinline__ void rate_consts(const pcfd_chem_model& m, int j, dou
 
 // mass production rates of one node (rhoi [ns] kg/m^3, T K -> wdot [ns])
 __device__ void node_rates(const pcfd_chem_model& m, const double* rhoi, const double T, double* wdot) {
+  double X[PCFD_CHEM_MAX_SPECIES];
+  for (int k = 0; k < m.nspecies; k++) X[k] = rhoi[k] / m.mw[k];
   const double logT = log(T);
-  rates_with(m, rhoi, [&](int j, double& Kf, double& Kb) { rate_consts(m, j, T, logT, Kf, Kb); }, wdot);
+  rates_with(m, X, [&](int j, double& Kf, double& Kb) { rate_consts(m, j, T, logT, Kf, Kb); }, wdot);
 }
 
 __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem_model* __restrict__ gm,
@@ -210,9 +210,10 @@ __global__ void __launch_bounds__(128) k_chem_rates(long long n, const pcfd_chem
 // ref_time) in the species rows.  SourceTerm reads rhoi and T only, and the
 // rate constants depend on T only: the ns species columns reuse the base
 // point's constants (the same values the reference recomputes), and only
-// the T column forms them again.  Every entry is formed as the reference
-// forms it, so the velocity columns and the momentum and energy rows are
-// (S - S) / h.
+// the T column forms them again; likewise the concentrations rhoi / MW of
+// the species a column does not perturb.  The velocity columns are
+// (S - S) / h and the momentum and energy rows (0 - 0) / h in the
+// reference: S - S and +0 here, the same values without the division.
 __global__ void __launch_bounds__(128) k_chem_source_jac(long long n, const pcfd_chem_model* __restrict__ gm,
                                                          pcfd_chem_ref ref, double ref_time,
                                                          const double* __restrict__ q, const double* __restrict__ vol,
@@ -232,9 +233,9 @@ __global__ void __launch_bounds__(128) k_chem_source_jac(long long n, const pcfd
   const double V = vol[p];
   const double scale = ref.density / ref_time;
   double* Ap = A + p * (long long)neqn * neqn;
-  double rhoi[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES], S0[PCFD_CHEM_MAX_SPECIES + 4];
+  double X[PCFD_CHEM_MAX_SPECIES], w[PCFD_CHEM_MAX_SPECIES], S0[PCFD_CHEM_MAX_SPECIES];
   double Kf[PCFD_CHEM_MAX_REACTIONS], Kb[PCFD_CHEM_MAX_REACTIONS];
-  for (int k = 0; k < ns; k++) rhoi[k] = Q[k] * ref.density;
+  for (int k = 0; k < ns; k++) X[k] = (Q[k] * ref.density) / m.mw[k];
   const double T0 = Q[ns + 3] * ref.temperature;
   {
     const double logT = log(T0);
@@ -244,31 +245,29 @@ __global__ void __launch_bounds__(128) k_chem_source_jac(long long n, const pcfd
     kf = Kf[j];
     kb = Kb[j];
   };
-  rates_with(m, rhoi, stored, w);
+  rates_with(m, X, stored, w);
   for (int k = 0; k < ns; k++) S0[k] = V * (w[k] / scale);
-  for (int k = ns; k < neqn; k++) S0[k] = 0.0;
   // a column of the difference quotients from the perturbed source in w
   auto column = [&](int i) {
     for (int j = 0; j < ns; j++) Ap[j * neqn + i] = (V * (w[j] / scale) - S0[j]) / h;
-    for (int j = ns; j < neqn; j++) Ap[j * neqn + i] = (0.0 - S0[j]) / h;
   };
   for (int i = 0; i < ns; i++) {
-    const double keep = rhoi[i];
-    rhoi[i] = (Q[i] + h) * ref.density;
-    rates_with(m, rhoi, stored, w);
-    rhoi[i] = keep;
+    const double keep = X[i];
+    X[i] = ((Q[i] + h) * ref.density) / m.mw[i];
+    rates_with(m, X, stored, w);
+    X[i] = keep;
     column(i);
   }
-  for (int i = ns; i < ns + 3; i++) {
-    for (int j = 0; j < ns; j++) Ap[j * neqn + i] = (S0[j] - S0[j]) / h;
-    for (int j = ns; j < neqn; j++) Ap[j * neqn + i] = (0.0 - S0[j]) / h;
-  }
+  for (int i = ns; i < ns + 3; i++)
+    for (int j = 0; j < ns; j++) Ap[j * neqn + i] = S0[j] - S0[j];
   {
     const double T = (Q[ns + 3] + h) * ref.temperature;
     const double logT = log(T);
-    rates_with(m, rhoi, [&](int j, double& kf, double& kb) { rate_consts(m, j, T, logT, kf, kb); }, w);
+    rates_with(m, X, [&](int j, double& kf, double& kb) { rate_consts(m, j, T, logT, kf, kb); }, w);
     column(ns + 3);
   }
+  for (int j = ns; j < neqn; j++)
+    for (int i = 0; i < neqn; i++) Ap[j * neqn + i] = 0.0;
 }
 
 // ---- node state of the reacting equation set ------------------------------
@@ -447,6 +446,125 @@ __device__ __forceinline__ double fr_c2(const ChemDerived& d, int ns, const pcfd
   }
   const double gamma = cp / cv;
   return gamma * R * Tdim / (ref.velocity * ref.velocity);
+}
+
+// CompressibleFREqnSet::GetFluidProperties (ucs/compressibleFR.tcc:1523)
+// over ChemModel::GetFluidProperties (ucs/chem.tcc:545): the mixture R and
+// the frozen speed of sound squared, non-dimensional
+__device__ __forceinline__ void fr_fluid_R_c2(const ChemDerived& d, int ns, const pcfd_chem_ref& ref,
+                                              const double* rhoi, double T, double& R, double& c2) {
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  const double s_ref = ref.velocity * ref.velocity / ref.temperature;
+  const double Tdim = T * ref.temperature;
+  double rho = 0.0, RDim = 0.0, cp = 0.0, cv = 0.0;
+  for (int i = 0; i < ns; i++) rhoiDim[i] = rhoi[i] * ref.density;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  for (int i = 0; i < ns; i++) RDim += rhoiDim[i] * d.R[i];
+  RDim /= rho;
+  for (int i = 0; i < ns; i++) {
+    const double X = rhoiDim[i] / rho;
+    const double cpi = species_cp(d, i, Tdim);
+    cp += cpi * X;
+    cv += X * (cpi - d.R[i]);
+  }
+  const double gamma = cp / cv;
+  R = RDim / s_ref;
+  c2 = gamma * RDim * Tdim / (ref.velocity * ref.velocity);
+}
+
+// CompressibleFREqnSet::ContributeTemporalTerms (ucs/compressibleFR.tcc:1319),
+// one thread per node: Aout = Ain + vol/dt terms times dq/dQ (conservative
+// over native), with ChemModel::dEtdP_dEtdRhoi (ucs/chem.tcc:829, at
+// constant T) and Gupta's beta preconditioning on the temperature column.
+// The species speeds of sound are the mixture's, as the reference sets them.
+__global__ void __launch_bounds__(128) k_chem_temporal(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                       const ChemDerived* __restrict__ gd, pcfd_chem_ref ref,
+                                                       const double* __restrict__ q, const double* __restrict__ vol,
+                                                       const double* __restrict__ dtau,
+                                                       const double* __restrict__ betav, double cnp1, double dt,
+                                                       int local_ts, const double* Ain, double* Aout) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const ChemDerived& d = *gd;
+  const int ns = gm->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  const int uloc = ns, vloc = ns + 1, wloc = ns + 2, tloc = ns + 3;
+  const double* Q = q + p * nv;
+  const double* Ai = Ain + p * (long long)neqn * neqn;
+  double* Ao = Aout + p * (long long)neqn * neqn;
+  if (Ao != Ai)
+    for (int k = 0; k < neqn * neqn; k++) Ao[k] = Ai[k];
+  const double V = vol[p], beta = betav[p];
+  const double vOverDt = local_ts ? cnp1 * V / dt + V / dtau[p] : cnp1 * V / dtau[p];
+  const double rho = Q[ns + 5], T = Q[tloc];
+  const double u = Q[uloc], v = Q[vloc], w = Q[wloc];
+  const double rvOverDt = rho * vOverDt;
+  double v2 = u * u + v * v + w * w;
+  double R, c2;
+  fr_fluid_R_c2(d, ns, ref, Q, T, R, c2);
+  const double s_ref = ref.velocity * ref.velocity / ref.temperature;
+  const double rhoDim = rho * ref.density;
+  const double TDim = T * ref.temperature;
+  v2 *= ref.velocity * ref.velocity;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES], dEtdRhoi[PCFD_CHEM_MAX_SPECIES], theta[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rhoiDim[i] = Q[i] * ref.density;
+  // dEtdP_dEtdRhoi with dRmixdRhoi (ucs/chem.tcc:862), dimensional
+  double dEtdP;
+  {
+    const double hv2 = 0.5 * v2;
+    double rhomix = 0.0, Rmix = 0.0;
+    for (int i = 0; i < ns; i++) {
+      rhomix += rhoiDim[i];
+      Rmix += rhoiDim[i] * d.R[i];
+    }
+    Rmix /= rhomix;
+    const double dPdrhomix = Rmix * TDim, dPdRmix = rhomix * TDim;
+    for (int i = 0; i < ns; i++) {
+      double dR = d.R[i] * (rhomix - rhoiDim[i]) / (rhomix * rhomix);
+      for (int j = 0; j < ns; j++) {
+        if (j == i) continue;
+        dR -= d.R[j] * rhoiDim[j] / (rhomix * rhomix);
+      }
+      dEtdRhoi[i] = hv2 + species_h(d, i, TDim) - (dPdrhomix + dPdRmix * dR);
+    }
+    const double dTdP = 1.0 / (rhomix * Rmix);
+    dEtdP = 0.0;
+    for (int i = 0; i < ns; i++) dEtdP += rhoiDim[i] * species_cp(d, i, TDim) * dTdP;
+    dEtdP -= 1.0;
+  }
+  const double ref_detdrho = ref.specific_enthalpy * ref.density / ref.density;
+  for (int i = 0; i < ns; i++) dEtdRhoi[i] /= ref_detdrho;
+  const double ref_detdP = ref.specific_enthalpy * ref.density / ref.pressure;
+  dEtdP /= ref_detdP;
+  double dPdT = rhoDim * (R * s_ref);
+  dPdT /= (ref.pressure / ref.temperature);
+  const double oneOBeta = 1.0 / beta, oneMbeta = 1.0 - beta;
+  for (int i = 0; i < ns; i++) theta[i] = (Q[i] / rho * oneMbeta / c2) * oneOBeta;
+  for (int i = 0; i < ns; i++) {
+    Ao[neqn * i + i] += vOverDt;
+    Ao[neqn * i + tloc] += theta[i] * vOverDt * dPdT;
+  }
+  const double vel[3] = {u, v, w};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int r = uloc + k;
+    double precond = 0.0;
+    for (int j = 0; j < ns; j++) {
+      Ao[neqn * r + j] += vel[k] * vOverDt;
+      precond += theta[j] * vel[k];
+    }
+    Ao[neqn * r + r] += rvOverDt;
+    Ao[neqn * r + tloc] += precond * vOverDt * dPdT;
+  }
+  double precond = 0.0;
+  for (int j = 0; j < ns; j++) {
+    Ao[neqn * tloc + j] += dEtdRhoi[j] * vOverDt;
+    precond += dEtdRhoi[j] * theta[j];
+  }
+  Ao[neqn * tloc + uloc] += u * rvOverDt;
+  Ao[neqn * tloc + vloc] += v * rvOverDt;
+  Ao[neqn * tloc + wloc] += w * rvOverDt;
+  precond += dEtdP * oneOBeta;
+  Ao[neqn * tloc + tloc] += precond * vOverDt * dPdT;
 }
 
 // GetTotalEnthalpy (ucs/compressibleFR.tcc:1249) of a node record
@@ -967,6 +1085,24 @@ PCFD_API int pcfd_chem_source_jacobian(pcfd_chem_t h, const pcfd_chem_ref* ref, 
   return node_call<2, 1>(c, n, dev, {q, vol}, {nv, 1}, {A}, {neqn * neqn}, nullptr,
                          [&](const double* const* in, double* const* out) {
                            k_chem_source_jac<<<CHEM_GRID(n)>>>(n, c->dev, r, ref_time, in[0], in[1], out[0]);
+                         });
+}
+
+PCFD_API int pcfd_chem_temporal_terms(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* q,
+                                      const double* vol, const double* dtau, const double* beta, double cnp1,
+                                      double dt, int local_ts, double* A, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!q || !vol || !dtau || !beta || !A))) {
+    pcfd_set_last_error("pcfd_chem_temporal_terms: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  const pcfd_chem_ref r = *ref;
+  return node_call<5, 1>(c, n, dev, {q, vol, dtau, beta, A}, {nv, 1, 1, 1, neqn * neqn}, {A}, {neqn * neqn}, nullptr,
+                         [&](const double* const* in, double* const* out) {
+                           k_chem_temporal<<<CHEM_GRID(n)>>>(n, c->dev, c->dder, r, in[0], in[1], in[2], in[3], cnp1,
+                                                             dt, local_ts, in[4], out[0]);
                          });
 }
 

@@ -62,6 +62,8 @@ def lib():
                                             C.POINTER(N.MeshView), _DP, C.c_double, C.c_int, _DP, _DP]),
             "oracle_chem_source_jacobian_n": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_double,
                                                      C.c_longlong, _DP, _DP, _DP]),
+            "oracle_chem_temporal_n": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_longlong, _DP, _DP,
+                                              _DP, _DP, C.c_double, C.c_double, C.c_int, _DP]),
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
@@ -385,6 +387,16 @@ class OracleChemState:
         A = np.empty((len(vol), self.ns + 4, self.ns + 4))
         self.L.oracle_chem_source_jacobian_n(C.byref(self.m), C.byref(self.ref), float(ref_time), len(vol), dp(q),
                                              dp(vol), dp(A))
+        return A
+
+    def temporal(self, q, vol, dtau, beta, cnp1, dt, local_ts, A=None):
+        """ContributeTemporalTerms per node, added into A [n][ns + 4][ns + 4]
+        (zeros when not given); returns A."""
+        n = len(vol)
+        A = np.zeros((n, self.ns + 4, self.ns + 4)) if A is None else np.ascontiguousarray(A, np.float64).copy()
+        arr = lambda x: np.ascontiguousarray(x, np.float64)
+        self.L.oracle_chem_temporal_n(C.byref(self.m), C.byref(self.ref), n, dp(arr(q)), dp(arr(vol)), dp(arr(dtau)),
+                                      dp(arr(beta)), float(cnp1), float(dt), int(local_ts), dp(A))
         return A
 
     def residual(self, opts, mesh, q, ref_time, reactions):

@@ -193,3 +193,47 @@ def test_fr_source_jacobian_against_central_differences():
         assert err.max() < 1e-5, (i, err.max())
         colsum = np.abs(A[:, :ns, i].sum(axis=1)) / scale
         assert colsum.max() < 5e-5, (i, colsum.max())
+
+
+def test_fr_temporal_terms_are_conservative_over_native():
+    """ContributeTemporalTerms with beta = 1 (no preconditioning) adds
+    vol/dtau times the Jacobian of the conservative variables (rhoi, rho u,
+    rho v, rho w, rho Et) over the native ones (rhoi, u, v, w, T); checked
+    against central differences of the oracle's NativeToConservative, with
+    the pressure of each perturbed state from ComputeAuxiliaryVariables.
+    With beta < 1 only the temperature column changes, and adding into a
+    block adds."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    ref, rhoi, vel, T = fr_states(12, seed=31)
+    q = fr_records(ref, rhoi, vel, T)
+    n = len(T)
+    vol = np.linspace(0.5, 2.0, n)
+    dtau = np.linspace(0.01, 0.2, n)
+    O = OracleChemState(model_struct(mechanism()), ref)
+    ns = O.ns
+    A1 = O.temporal(q, vol, dtau, np.ones(n), 1.0, 0.0, 0)
+
+    def cons(nat):
+        r, vv, t = nat[:, :ns], nat[:, ns:ns + 3], nat[:, ns + 3]
+        P, _, _ = O.aux(r, t)
+        return np.c_[r, O.n2c(r, np.c_[vv, t], P)]
+
+    nat = np.c_[rhoi, vel, T]
+    J = np.empty((n, ns + 4, ns + 4))
+    for i in range(ns + 4):
+        hc = 1e-6 * max(np.abs(nat[:, i]).max(), 1e-3)
+        p, m = nat.copy(), nat.copy()
+        p[:, i] += hc
+        m[:, i] -= hc
+        J[:, :, i] = (cons(p) - cons(m)) / (2 * hc)
+    want = (vol / dtau)[:, None, None] * J
+    scale = np.abs(want).max(axis=2, keepdims=True)
+    err = (np.abs(A1 - want) / scale).max()
+    assert err < 1e-6, err
+    base = np.random.default_rng(2).normal(size=A1.shape)
+    Ab = O.temporal(q, vol, dtau, np.full(n, 0.3), 1.0, 0.0, 0, A=base)
+    A3 = O.temporal(q, vol, dtau, np.full(n, 0.3), 1.0, 0.0, 0)
+    assert np.allclose(Ab - base, A3, rtol=1e-12, atol=1e-12 * np.abs(A3).max())
+    assert np.array_equal(A3[:, :, :ns + 3], A1[:, :, :ns + 3])
+    assert not np.allclose(A3[:, :, ns + 3], A1[:, :, ns + 3])

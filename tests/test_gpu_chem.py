@@ -270,3 +270,37 @@ def test_source_jacobian_full_size_mass_conservation():
     scale = np.abs(A[:, :ns, :]).max(axis=1) + smax[:, None]
     assert (colsum / scale).max() < 1e-4, (colsum / scale).max()
     C.close()
+
+
+@pytest.mark.parametrize("local_ts", [0, 1])
+def test_temporal_terms_parity(local_ts):
+    """ContributeTemporalTerms on the GPU against the oracle on seeded
+    reacting records with per-node volumes, pseudo-time steps and beta in
+    (0.2, 1], added into a random block (host arrays), then in place on
+    device arrays."""
+    import torch
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    ref, rhoi, vel, T = fr_states(4000, seed=33)
+    q = fr_records(ref, rhoi, vel, T)
+    n = len(T)
+    rng = np.random.default_rng(8)
+    vol = rng.uniform(0.5, 2.0, size=n)
+    dtau = rng.uniform(1e-3, 1e-1, size=n)
+    beta = rng.uniform(0.2, 1.0, size=n)
+    C = ChemModel(spec)
+    ns = C.nspecies
+    base = rng.normal(size=(n, ns + 4, ns + 4))
+    A = C.temporal_terms(ref, q, vol, dtau, beta, 1.5, 0.05, local_ts, A=base)
+    Ao = OracleChemState(model_struct(spec), ref).temporal(q, vol, dtau, beta, 1.5, 0.05, local_ts, A=base)
+    scale = np.abs(Ao).max(axis=2, keepdims=True)
+    err = (np.abs(A - Ao) / scale).max()
+    assert err < 1e-13, err
+    dq = torch.from_numpy(q).cuda()
+    dv, dt_, db = (torch.from_numpy(x).cuda() for x in (vol, dtau, beta))
+    dA = torch.from_numpy(base.copy()).cuda()
+    C.temporal_terms_dev(ref, n, dq.data_ptr(), dv.data_ptr(), dt_.data_ptr(), db.data_ptr(), 1.5, 0.05, local_ts,
+                         dA.data_ptr())
+    assert np.array_equal(dA.cpu().numpy(), A)
+    C.close()
