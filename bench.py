@@ -621,6 +621,20 @@ def run_gb300(args, ws, rank, local, pg):
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_sample(12.0, 1)
         line["cpu_baseline"] = base
+    # the FP32 block SpMV of the mixed solver on this machine's matrix: one mixed
+    # Newton step assembles it (FP32 storage), then K device-timed products
+    # on resident vectors (the matrix is larger than L2)
+    S.set_state(q0)
+    S.set_residual_arithmetic(1)
+    S.newton_iterate(1, **dict(CONV_ARMS["mixed"]["opts"], fgmres_m=2))
+    S.bench_spmv(3)
+    spmv_ms = S.bench_spmv(args.steps) / args.steps
+    nb = S.nblocks()
+    spmv_bytes = (nb - m.nnode) * (25 * 4 + 4) + m.nnode * (4 + 5 * 4 + 5 * 4 + 25 * 4)
+    line["spmv"] = {"what": "FP32 block SpMV y = A x (k_spmv_staged) of the mixed solver's %d-block matrix, "
+                            "vectors resident" % nb,
+                    "ms": spmv_ms, "bytes": spmv_bytes, "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
+                    "peak_gbs": peak, "frac": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peak if peak else None}
     S.close()
     if rank == 0 and ws == 1 and not args.no_chemistry:
         line["chemistry"] = chemistry_study(args)

@@ -453,6 +453,11 @@ PCFD_API int pcfd_set_residual_arithmetic(pcfd_solver_t s, int mode);
  * returns their device time from CUDA events recorded on that stream (the
  * reference's ResidualTimer, ucs/solutionSpace.tcc:692-701). */
 PCFD_API int pcfd_bench_residual_full(pcfd_solver_t s, int nsteps, double* ms_out, double* norms_out);
+/* Device time (CUDA events on the library's stream) of nrep back-to-back
+ * products y = A x of the assembled matrix (MatVecMultiply, ucs/crs.tcc:484)
+ * on device-resident vectors: FP64 vectors with vec_precision 0, the FP32
+ * Krylov solver's product with 1 (FP32 or BF16 storage). */
+PCFD_API int pcfd_bench_spmv(pcfd_solver_t s, int nrep, int vec_precision, double* ms_out);
 /* Selects the CUDA device for handles created afterwards on this thread. */
 PCFD_API int pcfd_set_device(int device);
 /* Waits for all work on the current device. */

@@ -276,6 +276,13 @@ class SolutionSpace:
                 "pcfd_bench_residual_full")
         return ms.value, norms
 
+    def bench_spmv(self, nrep, fp32=True):
+        """Device time (ms) of nrep back-to-back products with the assembled
+        matrix (FP32 vectors through the FP32 Krylov product, or FP64)."""
+        ms = C.c_double()
+        N.check(self._lib.pcfd_bench_spmv(self._h, int(nrep), 1 if fp32 else 0, C.byref(ms)), "pcfd_bench_spmv")
+        return ms.value
+
     def set_residual_arithmetic(self, mode):
         """0 FP64, 1 double-float on the FP32 pipes (composite calls only)."""
         N.check(self._lib.pcfd_set_residual_arithmetic(self._h, int(mode)), "pcfd_set_residual_arithmetic")

@@ -914,13 +914,15 @@ __device__ __forceinline__ E row_stage_sum(int b0, int nb, int jl, int lane, con
   const bool active = lane < 25;
   const int ns = min(nb, kStageBlocks);
   const int mo = chunk_off(M + (size_t)b0 * 25);
+  // lane u's block: where its x entries start in the stage (formed once per
+  // row, one shuffle per block below)
+  const int xoff = lane * G::XCH * G::C + chunk_off(xa + (size_t)jl * 5);
   E acc = E(0);
 #pragma unroll
   for (int u = 0; u < kStageBlocks; u++) {
     if (u >= ns) break;
-    const int j = __shfl_sync(0xffffffffu, jl, u);
-    const int xo = chunk_off(xa + (size_t)j * 5);
-    if (active) acc = fma(st->m[mo + u * 25 + lane], st->x[u * G::XCH * G::C + xo + c], acc);
+    const int xo = __shfl_sync(0xffffffffu, xoff, u);
+    if (active) acc = fma(st->m[mo + u * 25 + lane], st->x[xo + c], acc);
   }
   for (int k = kStageBlocks; k < nb; k++) {
     const int j = k < 32 ? __shfl_sync(0xffffffffu, jl, k & 31) : ja[b0 + k];

@@ -3136,6 +3136,45 @@ PCFD_API int pcfd_matvec(pcfd_solver_t h, const double* x, double* y, int vec_pr
   return PCFD_OK;
 }
 
+PCFD_API int pcfd_bench_spmv(pcfd_solver_t h, int nrep, int vec_precision, double* ms_out) {
+  Solver* s = (Solver*)h;
+  if (!s || nrep <= 0 || !ms_out || vec_precision < 0 || vec_precision > 1)
+    return set_err(PCFD_ERR_ARG, "pcfd_bench_spmv: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_bench_spmv: no Jacobian assembled");
+  if (vec_precision == 1 && s->jac_prec == 0)
+    return set_err(PCFD_ERR_STATE, "pcfd_bench_spmv: FP32 vectors need FP32 or BF16 matrix storage");
+  const long long n = (long long)s->nnode * NEQN;
+  if (!s->d_mv) {
+    int rc = dalloc(&s->d_mv, (size_t)2 * n + (size_t)n + 4);
+    if (rc) return rc;
+  }
+  double* xd = s->d_mv;
+  double* yd = s->d_mv + n;
+  float* xf = (float*)(s->d_mv + 2 * n);
+  float* yf = xf + n + 4;
+  // x = 0 (the products' cost does not depend on the values)
+  CUDA_TRY(cudaMemsetAsync(s->d_mv, 0, ((size_t)2 * n + (size_t)n + 4) * sizeof(double), s->stream));
+  int saved = s->profile;
+  s->profile = 0;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaEventRecord(e0, s->stream));
+  int rc = PCFD_OK;
+  for (int it = 0; it < nrep && rc == PCFD_OK; it++) rc = vec_precision ? run_spmv_f(s, xf, yf) : run_spmv(s, xd, yd);
+  cudaEventRecord(e1, s->stream);
+  cudaError_t ce = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->profile = saved;
+  if (rc) return rc;
+  if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("bench spmv: ") + cudaGetErrorString(ce));
+  *ms_out = ms;
+  return PCFD_OK;
+}
+
 PCFD_API int pcfd_sgs_rhs(pcfd_solver_t h, int nsweeps, const double* b, double* x_out, int vec_precision) {
   Solver* s = (Solver*)h;
   if (!s || !b || !x_out || nsweeps < 0 || vec_precision < 0 || vec_precision > 1)
