@@ -1356,16 +1356,26 @@ __global__ void __launch_bounds__(kNormThreads) k_orth_mdot(long long n, int nv,
   __shared__ double red[kNormThreads / 32][32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  K acc[32];
+  K acc[32], hh[32];
 #pragma unroll
-  for (int u = 0; u < 32; u++) acc[u] = K(0);
+  for (int u = 0; u < 32; u++) {
+    acc[u] = K(0);
+    hh[u] = u < nv ? h[u] : K(0);
+  }
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    // the element's V entries loaded ahead (independent loads in flight),
+    // then the update in the sequential order and the dot products
+    K vv[32];
+#pragma unroll
+    for (int u = 0; u < 32; u++) vv[u] = u < nv ? V[(size_t)u * n + i] : K(0);
     K v = w[i];
-    for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
+#pragma unroll
+    for (int u = 0; u < 32; u++)
+      if (u < nv) v -= hh[u] * vv[u];
     w[i] = v;
 #pragma unroll
     for (int u = 0; u < 32; u++)
-      if (u < nv) acc[u] = fma(v, V[(size_t)u * n + i], acc[u]);
+      if (u < nv) acc[u] = fma(v, vv[u], acc[u]);
   }
 #pragma unroll
   for (int u = 0; u < 32; u++) {
@@ -1409,11 +1419,31 @@ __global__ void __launch_bounds__(kNormThreads) k_orth_norm(long long n, int nv,
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   K acc = K(0);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    K v = w[i];
-    for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
-    w[i] = v;
-    acc = fma(v, v, acc);
+  if (nv <= 32) {
+    // up to 32 vectors: V entries and coefficients in registers, loaded ahead
+    K hh[32];
+#pragma unroll
+    for (int u = 0; u < 32; u++) hh[u] = u < nv ? h[u] : K(0);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      K vv[32];
+#pragma unroll
+      for (int u = 0; u < 32; u++) vv[u] = u < nv ? V[(size_t)u * n + i] : K(0);
+      K v = w[i];
+#pragma unroll
+      for (int u = 0; u < 32; u++)
+        if (u < nv) v -= hh[u] * vv[u];
+      w[i] = v;
+      acc = fma(v, v, acc);
+    }
+  } else {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      K v = w[i];
+      for (int k = 0; k < nv; k++) v -= h[k] * V[(size_t)k * n + i];
+      w[i] = v;
+      acc = fma(v, v, acc);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if (lane == 0) red[wid] = (double)acc;

@@ -186,6 +186,7 @@ struct Solver {
   unsigned int* d_gbar = nullptr;  // grid barrier of the SGS sweep kernel (count, generation)
   int* d_sgs_err = nullptr;     // set when a sweep's grid barrier timed out
   int nsm = 0;                  // multiprocessors of the device
+  int orth_grid[4] = {0, 0, 0, 0};  // one-wave grids of k_orth_norm / k_orth_mdot (float, double)
   // FGMRES work space (allocated on first use)
   int fg_m = 0;
   double* d_V = nullptr;        // [m+1][nnode*5]
@@ -2003,13 +2004,28 @@ int run_mdot_dev(Solver* s, const K* V, int nv, const K* w, int slot) {
   });
 }
 
+// One wave of a Gram-Schmidt kernel: its resident blocks per multiprocessor
+// times the multiprocessors (they hold the element's vectors in registers,
+// so fewer blocks fit than the fixed Krylov grid); each kernel reduces its
+// own partials, so the grid only has to be fixed per device.
+template <class F>
+int orth_grid(Solver* s, int slot, F kernel) {
+  if (!s->orth_grid[slot]) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kNormThreads, 0);
+    s->orth_grid[slot] = std::max(1, std::min(kKrylovBlocks, std::max(1, per_sm) * s->nsm));
+  }
+  return s->orth_grid[slot];
+}
+
 // w -= sum_k h[k] V_k with (w, w) of the result into result slot 0
 template <class K>
 int run_orth_norm(Solver* s, const K* V, int nv, const K* h, K* w) {
   const long long n = (long long)s->nnode * NEQN;
+  const int grid = orth_grid(s, std::is_same<K, double>::value ? 1 : 0, k_orth_norm<K>);
   return launch(s, T_KRYLOV, [&] {
-    k_orth_norm<K><<<kKrylovBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
-                                                                  krylov_slot(s, 0));
+    k_orth_norm<K><<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
+                                                         krylov_slot(s, 0));
   });
 }
 
@@ -2018,9 +2034,10 @@ int run_orth_norm(Solver* s, const K* V, int nv, const K* h, K* w) {
 template <class K>
 int run_orth_mdot(Solver* s, const K* V, int nv, const K* h, K* w, int slot) {
   const long long n = (long long)s->nnode * NEQN;
+  const int grid = orth_grid(s, std::is_same<K, double>::value ? 3 : 2, k_orth_mdot<K>);
   return launch(s, T_KRYLOV, [&] {
-    k_orth_mdot<K><<<kKrylovBlocks, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
-                                                                  krylov_slot(s, slot), krylov_slot_f(s, slot));
+    k_orth_mdot<K><<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
+                                                         krylov_slot(s, slot), krylov_slot_f(s, slot));
   });
 }
 
