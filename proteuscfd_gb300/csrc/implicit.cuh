@@ -745,6 +745,22 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* __restrict__ bar, uns
   return s_ok != 0;
 }
 
+// Colour of phase p of symmetric sweeps (colours forward, then backward).
+__device__ __forceinline__ int sgs_colour(int p, int ncolor) {
+  const int cc = p % ncolor, dir = (p / ncolor) & 1;
+  return dir == 0 ? cc : ncolor - 1 - cc;
+}
+// The phase after p, skipping a phase of the colour just swept (the last
+// colour of a forward sweep opens the backward one, the first colour of a
+// backward sweep opens the next forward one): a colour's rows read only
+// other colours' x, unchanged in between, so the repeat would write the
+// same values.
+__device__ __forceinline__ int sgs_next_phase(int p, int nphase, int ncolor) {
+  int q = p + 1;
+  while (q < nphase && sgs_colour(q, ncolor) == sgs_colour(p, ncolor)) q++;
+  return q;
+}
+
 // nsweeps symmetric sweeps (all colours forward, then backward) in one
 // cooperative launch: the colours are separated by grid barriers instead of
 // kernel boundaries, and x is gathered from L2.  Each row's arithmetic does
@@ -760,12 +776,11 @@ __global__ void __launch_bounds__(256, 3) k_sgs_sweep(int ncolor, const int* __r
                                                       int* __restrict__ err) {
   const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
   const int nphase = nsweeps * 2 * ncolor;
-  for (int p = 0; p < nphase; p++) {
-    const int cc = p % ncolor, dir = (p / ncolor) & 1;
-    const int c = dir == 0 ? cc : ncolor - 1 - cc;
+  for (int p = 0; p < nphase; p = sgs_next_phase(p, nphase, ncolor)) {
+    const int c = sgs_colour(p, ncolor);
     const int r0 = cptr[c], nr = cptr[c + 1] - r0;
     sgs_rows<T, K, true>(nr, desc + r0, ja, M, dinv, b, x, xa, g, W);
-    if (p + 1 < nphase && !grid_barrier(bar, gridDim.x, err)) return;
+    if (sgs_next_phase(p, nphase, ncolor) < nphase && !grid_barrier(bar, gridDim.x, err)) return;
   }
 }
 
@@ -1088,19 +1103,17 @@ __global__ void __launch_bounds__(256, sizeof(E) == 8 ? 2 : 4) k_sgs_sweep_stage
   RowStage<E>* st = reinterpret_cast<RowStage<E>*>(smem_raw) + (threadIdx.x >> 5) * kRowStages;
   const int g = blockIdx.x * 8 + (threadIdx.x >> 5), W = gridDim.x * 8;
   const int nphase = nsweeps * 2 * ncolor;
-  auto colour = [&](int p) {
-    const int cc = p % ncolor, dir = (p / ncolor) & 1;
-    return dir == 0 ? cc : ncolor - 1 - cc;
-  };
-  int c = colour(0);
+  if (nphase <= 0) return;
+  int c = sgs_colour(0, ncolor);
   int r0 = cptr[c], nr = cptr[c + 1] - r0;
   int4 dA, dB;
   int jA, jB;
   sgs_head<E>(nr, desc + r0, ja, M, dinv, b, g, W, st, dA, jA, dB, jB);
-  for (int p = 0; p < nphase; p++) {
+  for (int p = 0; p < nphase;) {
     sgs_rows_staged<E>(nr, desc + r0, ja, M, dinv, b, x, g, W, st, dA, jA, dB, jB);
-    if (p + 1 < nphase) {
-      c = colour(p + 1);
+    p = sgs_next_phase(p, nphase, ncolor);
+    if (p < nphase) {
+      c = sgs_colour(p, ncolor);
       r0 = cptr[c];
       nr = cptr[c + 1] - r0;
       sgs_head<E>(nr, desc + r0, ja, M, dinv, b, g, W, st, dA, jA, dB, jB);
