@@ -185,8 +185,8 @@ def run_reference(args, rank, pg):
 # a tighter solve spends Krylov iterations without saving steps); "mixed_bf16" the same
 # with BF16 Jacobian storage (FP32 accumulation).  "mixed_learned": the
 # same with the learned correction on top of the SGS sweep for the first
-# three Krylov directions of each cycle (the directions closest to the
-# right-hand sides the network is trained on).
+# Krylov direction of each cycle (the residual itself, the right-hand side
+# the network is trained on).
 CONV_COMMON = dict(cfl_start=1.0, limiter_freeze=60, first_order_steps=20)
 CONV_ARMS = {
     "fp64": dict(arith=0, opts=dict(CONV_COMMON, cfl=50.0, cfl_ramp_steps=40, nsgs=10, linear_solver=0,
@@ -197,7 +197,7 @@ CONV_ARMS = {
                                           fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=2)),
     "mixed_learned": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=2,
                                              fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1,
-                                             lp_directions=3)),
+                                             lp_directions=1)),
 }
 
 
