@@ -1360,7 +1360,7 @@ __global__ void k_orth_update(long long n, int nv, const K* __restrict__ V, cons
 // pass over V: the update as in k_orth_update, the dot products with the
 // per-thread, per-block and final summation orders of k_mdot.  Partials are
 // stored dot-major ([k][block]).
-template <class K>
+template <class K, int NV>
 __global__ void __launch_bounds__(kNormThreads) k_orth_mdot(long long n, int nv, const K* __restrict__ V,
                                                              const K* __restrict__ h, K* __restrict__ w,
                                                              double* __restrict__ part,
@@ -1369,29 +1369,30 @@ __global__ void __launch_bounds__(kNormThreads) k_orth_mdot(long long n, int nv,
   __shared__ double red[kNormThreads / 32][32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  K acc[32], hh[32];
+  K acc[NV], hh[NV];
 #pragma unroll
-  for (int u = 0; u < 32; u++) {
+  for (int u = 0; u < NV; u++) {
     acc[u] = K(0);
     hh[u] = u < nv ? h[u] : K(0);
   }
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     // the element's V entries loaded ahead (independent loads in flight),
     // then the update in the sequential order and the dot products
-    K vv[32];
+    K vv[NV];
+    const K* vp = V + i;
 #pragma unroll
-    for (int u = 0; u < 32; u++) vv[u] = u < nv ? V[(size_t)u * n + i] : K(0);
+    for (int u = 0; u < NV; u++) vv[u] = u < nv ? vp[(size_t)u * n] : K(0);
     K v = w[i];
 #pragma unroll
-    for (int u = 0; u < 32; u++)
+    for (int u = 0; u < NV; u++)
       if (u < nv) v -= hh[u] * vv[u];
     w[i] = v;
 #pragma unroll
-    for (int u = 0; u < 32; u++)
+    for (int u = 0; u < NV; u++)
       if (u < nv) acc[u] = fma(v, vv[u], acc[u]);
   }
 #pragma unroll
-  for (int u = 0; u < 32; u++) {
+  for (int u = 0; u < NV; u++) {
     if (u >= nv) break;
     K a = acc[u];
     for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
@@ -1422,7 +1423,7 @@ __global__ void __launch_bounds__(kNormThreads) k_orth_mdot(long long n, int nv,
 // w -= sum_k h[k] V_k (the second Gram-Schmidt pass) with (w, w) of the
 // result: per-thread sums in the vector type and FP64 block sums as in
 // k_mdot, the last block writing the total to out[0]
-template <class K>
+template <class K, int NV>
 __global__ void __launch_bounds__(kNormThreads) k_orth_norm(long long n, int nv, const K* __restrict__ V,
                                                              const K* __restrict__ h, K* __restrict__ w,
                                                              double* __restrict__ part,
@@ -1432,19 +1433,20 @@ __global__ void __launch_bounds__(kNormThreads) k_orth_norm(long long n, int nv,
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   K acc = K(0);
-  if (nv <= 32) {
-    // up to 32 vectors: V entries and coefficients in registers, loaded ahead
-    K hh[32];
+  if (nv <= NV) {
+    // up to NV vectors: V entries and coefficients in registers, loaded ahead
+    K hh[NV];
 #pragma unroll
-    for (int u = 0; u < 32; u++) hh[u] = u < nv ? h[u] : K(0);
+    for (int u = 0; u < NV; u++) hh[u] = u < nv ? h[u] : K(0);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-      K vv[32];
+      K vv[NV];
+      const K* vp = V + i;
 #pragma unroll
-      for (int u = 0; u < 32; u++) vv[u] = u < nv ? V[(size_t)u * n + i] : K(0);
+      for (int u = 0; u < NV; u++) vv[u] = u < nv ? vp[(size_t)u * n] : K(0);
       K v = w[i];
 #pragma unroll
-      for (int u = 0; u < 32; u++)
+      for (int u = 0; u < NV; u++)
         if (u < nv) v -= hh[u] * vv[u];
       w[i] = v;
       acc = fma(v, v, acc);

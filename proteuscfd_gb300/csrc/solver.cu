@@ -186,7 +186,7 @@ struct Solver {
   unsigned int* d_gbar = nullptr;  // grid barrier of the SGS sweep kernel (count, generation)
   int* d_sgs_err = nullptr;     // set when a sweep's grid barrier timed out
   int nsm = 0;                  // multiprocessors of the device
-  int orth_grid[4] = {0, 0, 0, 0};  // one-wave grids of k_orth_norm / k_orth_mdot (float, double)
+  int orth_grid[16] = {};  // one-wave grids of k_orth_norm / k_orth_mdot per type and register width
   // FGMRES work space (allocated on first use)
   int fg_m = 0;
   double* d_V = nullptr;        // [m+1][nnode*5]
@@ -2018,15 +2018,38 @@ int orth_grid(Solver* s, int slot, F kernel) {
   return s->orth_grid[slot];
 }
 
+// The Gram-Schmidt kernels hold up to NV vectors in registers; each call
+// takes the smallest of 4, 8, 16, 32 that holds nv (larger nv: 32, where
+// k_orth_norm falls back to its sequential loop).
+template <class K, template <class, int> class KER, class F4, class F8, class F16, class F32>
+int orth_launch(Solver* s, int base, int nv, F4 f4, F8 f8, F16 f16, F32 f32) {
+  const int t = std::is_same<K, double>::value ? 4 : 0;
+  if (nv <= 4) return f4(orth_grid(s, base + t + 0, KER<K, 4>::fn()));
+  if (nv <= 8) return f8(orth_grid(s, base + t + 1, KER<K, 8>::fn()));
+  if (nv <= 16) return f16(orth_grid(s, base + t + 2, KER<K, 16>::fn()));
+  return f32(orth_grid(s, base + t + 3, KER<K, 32>::fn()));
+}
+template <class K, int NV>
+struct OrthNormK {
+  static auto fn() { return k_orth_norm<K, NV>; }
+};
+template <class K, int NV>
+struct OrthMdotK {
+  static auto fn() { return k_orth_mdot<K, NV>; }
+};
+
 // w -= sum_k h[k] V_k with (w, w) of the result into result slot 0
 template <class K>
 int run_orth_norm(Solver* s, const K* V, int nv, const K* h, K* w) {
   const long long n = (long long)s->nnode * NEQN;
-  const int grid = orth_grid(s, std::is_same<K, double>::value ? 1 : 0, k_orth_norm<K>);
-  return launch(s, T_KRYLOV, [&] {
-    k_orth_norm<K><<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
-                                                         krylov_slot(s, 0));
-  });
+  auto go = [&](auto kernel, int grid) {
+    return launch(s, T_KRYLOV, [&] {
+      kernel<<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done, krylov_slot(s, 0));
+    });
+  };
+  return orth_launch<K, OrthNormK>(
+      s, 0, nv, [&](int g) { return go(k_orth_norm<K, 4>, g); }, [&](int g) { return go(k_orth_norm<K, 8>, g); },
+      [&](int g) { return go(k_orth_norm<K, 16>, g); }, [&](int g) { return go(k_orth_norm<K, 32>, g); });
 }
 
 // w -= sum_k h[k] V_k, then its dot products with V_0..V_{nv-1} into result
@@ -2034,11 +2057,15 @@ int run_orth_norm(Solver* s, const K* V, int nv, const K* h, K* w) {
 template <class K>
 int run_orth_mdot(Solver* s, const K* V, int nv, const K* h, K* w, int slot) {
   const long long n = (long long)s->nnode * NEQN;
-  const int grid = orth_grid(s, std::is_same<K, double>::value ? 3 : 2, k_orth_mdot<K>);
-  return launch(s, T_KRYLOV, [&] {
-    k_orth_mdot<K><<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done,
-                                                         krylov_slot(s, slot), krylov_slot_f(s, slot));
-  });
+  auto go = [&](auto kernel, int grid) {
+    return launch(s, T_KRYLOV, [&] {
+      kernel<<<grid, kNormThreads, 0, s->stream>>>(n, nv, V, h, w, s->d_dots, s->d_mdot_done, krylov_slot(s, slot),
+                                                    krylov_slot_f(s, slot));
+    });
+  };
+  return orth_launch<K, OrthMdotK>(
+      s, 8, nv, [&](int g) { return go(k_orth_mdot<K, 4>, g); }, [&](int g) { return go(k_orth_mdot<K, 8>, g); },
+      [&](int g) { return go(k_orth_mdot<K, 16>, g); }, [&](int g) { return go(k_orth_mdot<K, 32>, g); });
 }
 
 
