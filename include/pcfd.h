@@ -104,9 +104,20 @@ PCFD_API int pcfd_mesh_build(pcfd_mesh_t m);
 PCFD_API int pcfd_mesh_view_get(pcfd_mesh_t m, pcfd_mesh_view* v);
 PCFD_API int pcfd_mesh_stats(pcfd_mesh_t m, int* nelem_tri, int* nelem_tet, int* rewound, int* unclosed,
                              double* max_open, double* total_vol);
-/* Mesh::ReorderMeshCuthillMcKee(1) order (ucs/mesh.tcc:2412): order[new] = old. */
+/* The array Mesh::ReorderMeshCuthillMcKee(1) leaves in Mesh::ordering
+ * (ucs/mesh.tcc:2412-2490), bit for bit: Cuthill-McKee from node 0 with
+ * degree-sorted neighbour lists, reversed.  The reference then uses it as an
+ * old-to-new map (ReorderC2nMap, :224): node n becomes ordering[n].  Computed
+ * on the current numbering; builds the point-surrounding-point map if needed. */
 PCFD_API int pcfd_mesh_rcm_order(pcfd_mesh_t m, int* order_out);
-/* Mesh::ReorderC2nMap (ucs/mesh.tcc:224): renumber nodes; rebuild afterwards. */
+/* The reference's set-up reorder (SolutionSpace constructor,
+ * ucs/solutionSpace.tcc:61-66: BuildMapsDecomp, ReorderMeshCuthillMcKee(1),
+ * ReorderC2nMap) applied to the element list and coordinates; call
+ * pcfd_mesh_build afterwards.  order_out (optional, [nnode]) receives the
+ * ordering array. */
+PCFD_API int pcfd_mesh_reorder_rcm(pcfd_mesh_t m, int* order_out);
+/* Renumber nodes by an explicit permutation, order[new] = old (a
+ * ReorderC2nMap with a caller's map); rebuild afterwards. */
 PCFD_API int pcfd_mesh_renumber(pcfd_mesh_t m, const int* order);
 PCFD_API void pcfd_mesh_destroy(pcfd_mesh_t m);
 PCFD_API const char* pcfd_mesh_last_error(void);
@@ -135,6 +146,16 @@ typedef struct pcfd_params {
   int ntags;              /* entries in bc_type/bc_twall, indexed by factag */
   const int* bc_type;     /* pcfd_bc_type per factag */
   const double* bc_twall; /* BCObj::twall per factag [K]; < 0 = adiabatic */
+  int torder;             /* Param::torder: 1 adds the temporal residual (TemporalResidual,
+                           * ucs/residual.tcc:125) as the reference always does (its default
+                           * and minimum); 0 leaves it out */
+  double time_step;       /* Param::dt ("timeStep"): must be <= 0, a steady run; the reference's
+                           * default -1.0 makes the temporal residual b += vol (q - q_old), with
+                           * q_old the state at the start of the step (0 reads as -1.0) */
+  double tinf, pinf;      /* non-dimensional freestream temperature and pressure,
+                           * initialTemperature/ref_temperature and initialPressure/ref_pressure
+                           * (CompressibleEqnSet::UpdateQinf, ucs/compressible.tcc:835-836); the
+                           * reference's scaling makes both 1 up to rounding; 0 reads as 1 */
 } pcfd_params;
 
 typedef void* pcfd_solver_t;

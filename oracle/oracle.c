@@ -6,17 +6,14 @@
  * the checker for the CUDA implementation.  It is never linked into, called
  * by or shipped with the product library.
  *
- * Pinning: the whole reference (ucs.x) needs HDF5, MPI and METIS, so it is
- * not built here.  The block LU, LuSolve and MatVecMult restated below are
- * pinned bit-for-bit against the reference's own ucs/matrix.h, and the dual
- * metric primitives against ucs/geometry.h, by compiling those two
- * self-contained headers (oracle/ref_pin.cpp, built into oracle/_ref/).
- * The mesh metrics are pinned to the reference unit tests' known answers
- * (unit-cube volume, unitTest/meshTest.h:97-109) and the gradient to the
- * exactness checks of unitTest/gradientTest.h.  The flux, boundary,
- * limiter and viscous routines follow the cited reference lines operation
- * for operation but have no reference-generated vectors: their parity is
- * unpinned beyond those restatements.
+ * Pinning: the reference solver itself is built from its own sources by
+ * oracle/refbuild (with stand-ins for MPI, HDF5 and METIS) and run on small
+ * cases; tests/golden/ref_*.npz hold what it computed stage by stage (state
+ * after the boundary update, gradient, limiter, residual and norms, Jacobian,
+ * SGS update, Newton iterates).  tests/test_ref_oracle.py requires this file
+ * to reproduce them.  The block LU, LuSolve and MatVecMult are also pinned
+ * bit-for-bit against the reference's own ucs/matrix.h, and the dual metric
+ * primitives against ucs/geometry.h (oracle/ref_pin.cpp).
  *
  * Layouts are the reference's: q [nnode+nbnode][10], qgrad [nnode][9][3],
  * limiter [nnode][5], b [nnode][5].
@@ -73,7 +70,8 @@ static double compute_pressure(const double* Q, double gamma) {
 /* UpdateQinf, ucs/compressible.tcc:827: rho = p gamma / T with p = T = 1. */
 void oracle_qinf(const pcfd_params* prm, double* Qinf) {
   double gamma = prm->gamma, gm1 = gamma - 1.0;
-  double T = 1.0, p = 1.0;
+  double T = prm->tinf == 0.0 ? 1.0 : prm->tinf;  /* ucs/compressible.tcc:835-837 */
+  double p = prm->pinf == 0.0 ? 1.0 : prm->pinf;
   double rho = p * gamma / T;
   double V = prm->mach;
   double u = prm->flowdir[0] * V, v = prm->flowdir[1] * V, w = prm->flowdir[2] * V;
@@ -704,6 +702,23 @@ int oracle_residual(const pcfd_mesh_view* m, const pcfd_params* prm, const doubl
  * which the rounding of b is judged. */
 int oracle_residual_scaled(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
                            const double* lim, double* b, double* babs, double* norms, long long* nkneecap) {
+  return oracle_residual_full(m, prm, q, NULL, grad, lim, b, babs, norms, nkneecap);
+}
+
+/* Param::dt as the temporal residual reads it: <= 0 is steady (0 stands for
+ * the reference's default, -1.0). */
+static double param_time_step(const pcfd_params* prm) {
+  return prm->time_step == 0.0 ? -1.0 : prm->time_step;
+}
+
+/* ComputeResiduals (ucs/residual.tcc:13): SpatialResidual, then, when qold
+ * ([nnode][5], the conservative state at the start of the step) is given and
+ * Param::torder is set, TemporalResidual (:125) with Param::dt - for a steady
+ * run (dt = -1) b += vol (q - qold), non-zero where the boundary update
+ * overwrote a node's state - then the boundary hook and the norms. */
+int oracle_residual_full(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* qold,
+                         const double* grad, const double* lim, double* b, double* babs, double* norms,
+                         long long* nkneecap) {
   const int nn = m->nnode;
   const double gamma = prm->gamma, chi = prm->chi;
   const int ho = prm->sorder > 1;
@@ -805,6 +820,17 @@ int oracle_residual_scaled(const pcfd_mesh_view* m, const pcfd_params* prm, cons
       oracle_viscous_flux(prm, Qavg, &grad[(size_t)a * NTERMS * 3], avec, 0.0, flux);
       for (int i = 0; i < NEQN; i++) b[(size_t)a * NEQN + i] += -flux[i];
       ACCUM_ABS(a, flux);
+    }
+  }
+  /* TemporalResidual, ucs/residual.tcc:125-179 (first order: cnp1 = 1, cnm1 = 0) */
+  if (qold && prm->torder) {
+    const double timestep = param_time_step(prm);
+    for (int i = 0; i < nn; i++) {
+      double dt = 1.0 * m->vol[i] / timestep; /* the cnm1 = 0 term adds nothing */
+      for (int j = 0; j < NEQN; j++) {
+        double dq = q[(size_t)i * NVARS + j] - qold[(size_t)i * NEQN + j];
+        b[(size_t)i * NEQN + j] -= dt * dq;
+      }
     }
   }
   /* Bkernel_BC_Res_Modify, ucs/bc.tcc:903 -> ModifyViscousWallResidual (:1612) */

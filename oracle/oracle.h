@@ -26,6 +26,9 @@ int oracle_limiter(const pcfd_mesh_view* m, const pcfd_params* prm, const double
                    double* l, long long* nclip);
 int oracle_residual(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
                     const double* lim, double* b, double* norms, long long* nkneecap);
+int oracle_residual_full(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* qold,
+                         const double* grad, const double* lim, double* b, double* babs, double* norms,
+                         long long* nkneecap);
 int oracle_residual_scaled(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
                            const double* lim, double* b, double* babs, double* norms, long long* nkneecap);
 int oracle_lu(double* a, int* p, int n);

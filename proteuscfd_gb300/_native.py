@@ -66,6 +66,7 @@ class Params(C.Structure):
         ("sorder", C.c_int), ("chi", C.c_double), ("viscous", C.c_int), ("limiter", C.c_int),
         ("venkat_K", C.c_double), ("no_cvbc", C.c_int), ("jac_boundary_eval", C.c_int), ("ntags", C.c_int),
         ("bc_type", C.POINTER(C.c_int)), ("bc_twall", C.POINTER(C.c_double)),
+        ("torder", C.c_int), ("time_step", C.c_double), ("tinf", C.c_double), ("pinf", C.c_double),
     ]
 
 
@@ -132,6 +133,7 @@ PROTOTYPES = {
     "pcfd_mesh_view_get": (C.c_int, [_P, C.POINTER(MeshView)]),
     "pcfd_mesh_stats": (C.c_int, [_P, _IP, _IP, _IP, _IP, _DP, _DP]),
     "pcfd_mesh_rcm_order": (C.c_int, [_P, _IP]),
+    "pcfd_mesh_reorder_rcm": (C.c_int, [_P, _IP]),
     "pcfd_mesh_renumber": (C.c_int, [_P, _IP]),
     "pcfd_mesh_destroy": (None, [_P]),
     "pcfd_mesh_last_error": (C.c_char_p, []),

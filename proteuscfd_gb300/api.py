@@ -42,12 +42,27 @@ NTERMS = 9
 class Mesh:
     """Host mesh with the reference's maps and dual metrics."""
 
-    def __init__(self, handle):
+    def __init__(self, handle, reorder=False, nnode=0):
+        """Takes ownership of a mesh handle and builds its maps and metrics.
+        ``reorder`` first applies the reference's set-up reorder (reverse
+        Cuthill-McKee from node 0, ``Param::reorder``, on by default in the
+        reference; ucs/solutionSpace.tcc:61-66); ``ordering`` then holds the
+        reference's ``Mesh::ordering`` (old node n is now ordering[n])."""
         self._lib = N.load()
         self._h = None
+        self.ordering = None
         if not handle:
             raise N.PcfdError(4, "mesh create", self._lib.pcfd_mesh_last_error().decode())
         self._h = handle
+        if reorder:
+            order = np.zeros(nnode, dtype=np.int32) if nnode > 0 else None
+            rc = self._lib.pcfd_mesh_reorder_rcm(self._h, N.iptr(order) if order is not None else None)
+            if rc != 0:
+                msg = self._lib.pcfd_mesh_last_error().decode()
+                self._lib.pcfd_mesh_destroy(self._h)
+                self._h = None
+                raise N.PcfdError(rc, "pcfd_mesh_reorder_rcm", msg)
+            self.ordering = order
         rc = self._lib.pcfd_mesh_build(self._h)
         if rc != 0:
             msg = self._lib.pcfd_mesh_last_error().decode()
@@ -59,19 +74,19 @@ class Mesh:
 
     @classmethod
     def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5,
-            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6)):
+            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6), reorder=False):
         p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags))
-        return cls(N.load().pcfd_mesh_box_create(C.byref(p)))
+        return cls(N.load().pcfd_mesh_box_create(C.byref(p)), reorder, nx * ny * nz)
 
     @classmethod
-    def from_elements(cls, xyz, tris, tri_tags, tets):
+    def from_elements(cls, xyz, tris, tri_tags, tets, reorder=False):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         tris = np.ascontiguousarray(tris, dtype=np.int32)
         tri_tags = np.ascontiguousarray(tri_tags, dtype=np.int32)
         tets = np.ascontiguousarray(tets, dtype=np.int32)
         h = N.load().pcfd_mesh_from_elements(len(xyz), N.dptr(xyz), len(tris), N.iptr(tris), N.iptr(tri_tags),
                                              len(tets), N.iptr(tets))
-        return cls(h)
+        return cls(h, reorder, len(xyz))
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -170,6 +185,10 @@ class Param:
     venkat_K: float = 1.0
     no_cvbc: int = 0
     jac_boundary_eval: int = 0
+    torder: int = 1            # Param::torder: the temporal residual is always on in the reference
+    time_step: float = -1.0    # Param::dt: steady (the reference's default)
+    tinf: float = 1.0          # freestream T / ref_temperature (UpdateQinf)
+    pinf: float = 1.0          # freestream p / ref_pressure
     bc_type: dict = field(default_factory=dict)   # factag -> BC type
     bc_twall: dict = field(default_factory=dict)  # factag -> wall temperature [K] (<0 adiabatic)
 
@@ -188,6 +207,8 @@ class Param:
         p.sorder, p.chi, p.viscous, p.limiter = self.sorder, self.chi, self.viscous, self.limiter
         p.venkat_K, p.no_cvbc, p.ntags = self.venkat_K, self.no_cvbc, ntags
         p.jac_boundary_eval = self.jac_boundary_eval
+        p.torder, p.time_step = self.torder, self.time_step
+        p.tinf, p.pinf = self.tinf, self.pinf
         p.bc_type = N.iptr(bct)
         p.bc_twall = N.dptr(btw)
         p._keep = (bct, btw)

@@ -14,6 +14,7 @@
 //   boundary winding check ................. ucs/mesh.tcc:2336  (Mesh::FixBoundaryWindings)
 //   weighted LSQ normal matrices ........... ucs/gradient.tcc:115,461 (ComputeNodeLSQCoefficients)
 //   reverse Cuthill-McKee renumbering ...... ucs/mesh.tcc:2412  (Mesh::ReorderMeshCuthillMcKee)
+//   ... applied to the elements ............ ucs/mesh.tcc:224   (Mesh::ReorderC2nMap)
 //
 // It also holds the synthetic workload generator: an Nx x Ny x Nz node box
 // split into 6 Kuhn tetrahedra per hex (all sharing the hex's (0,0,0)-(1,1,1)
@@ -138,21 +139,21 @@ const int kTetFl[12] = {0, 1, 2, 0, 3, 1, 0, 2, 3, 1, 3, 2};
 
 int elem_nnodes(int t) { return t == ETRI ? 3 : 4; }
 
-// Mesh::EliminateRepeats (ucs/mesh.tcc:1341): keeps first occurrences in order.
-int eliminate_repeats(int* a, int n) {
-  if (n <= 0) return 0;
-  std::vector<char> flag(n, 1);
-  for (int i = 0; i < n; i++)
-    if (flag[i])
-      for (int j = i + 1; j < n; j++)
-        if (a[i] == a[j]) flag[j] = 0;
-  int unique = 1;
-  for (int i = 1; i < n; i++)
-    if (flag[i]) a[unique++] = a[i];
+// Mesh::EliminateRepeats (ucs/mesh.tcc:1341): keeps the first occurrence of
+// each value, in order.  The reference compares every pair (O(k^2) per node);
+// a per-node stamp gives the same list in O(k).
+int eliminate_repeats(int* a, int n, std::vector<int>& stamp, int tag) {
+  int unique = 0;
+  for (int i = 0; i < n; i++) {
+    const int v = a[i];
+    if (stamp[v] == tag) continue;
+    stamp[v] = tag;
+    a[unique++] = v;
+  }
   return unique;
 }
 
-int build_maps(HostMesh& m) {
+int build_psp_only(HostMesh& m) {
   const int nn = m.nnode;
   const int ne = (int)m.etype.size();
   // BuildElsp
@@ -178,6 +179,7 @@ int build_maps(HostMesh& m) {
   m.psp.clear();
   m.psp.reserve((size_t)nn * 16);
   std::vector<int> tmp;
+  std::vector<int> stamp(nn, -1);
   for (int i = 0; i < nn; i++) {
     tmp.clear();
     for (int k = m.ielsp[i]; k < m.ielsp[i + 1]; k++) {
@@ -193,10 +195,17 @@ int build_maps(HostMesh& m) {
         for (int q = 0; q < 3; q++) tmp.push_back(nodes[kClTet[3 * lnode + q]]);
       }
     }
-    int u = eliminate_repeats(tmp.data(), (int)tmp.size());
+    int u = eliminate_repeats(tmp.data(), (int)tmp.size(), stamp, i);
     m.psp.insert(m.psp.end(), tmp.begin(), tmp.begin() + u);
     m.ipsp[i + 1] = (int)m.psp.size();
   }
+  return 0;
+}
+
+int build_maps(HostMesh& m) {
+  if (build_psp_only(m) != 0) return -1;
+  const int nn = m.nnode;
+  const int ne = (int)m.etype.size();
   // FixBoundaryWindings: every boundary triangle must face away from its tet.
   // The generator winds them outward already; this counts any that are not
   // and rewinds them the way the reference does (nodes 2,1,0).
@@ -394,42 +403,92 @@ int calc_metrics(HostMesh& m) {
   return 0;
 }
 
-// Reverse Cuthill-McKee renumbering of the nodes following
-// Mesh::ReorderMeshCuthillMcKee (ucs/mesh.tcc:2412-2490): breadth-first from
-// the lowest-degree unvisited node, neighbours queued by ascending degree,
-// then the order reversed.  Ties between equal degrees keep psp order
-// (std::stable_sort); the reference's std::sort is unstable, so equal-degree
-// ties are the one place this ordering is not pinned to the reference.
-int rcm_order(const HostMesh& m, std::vector<int>& order) {
+// Cuthill-McKee ordering exactly as Mesh::ReorderMeshCuthillMcKee computes it
+// (ucs/mesh.tcc:2412-2490): node 0 is the first vertex; the unused
+// neighbours of the current vertex, in psp order, are queued as (node,
+// degree) pairs, sorted by ascending degree with std::sort and the
+// reference's comparison (DegreeCompare, ucs/oddsNends.cpp:4-7) - the same
+// libstdc++ sort on the same sequence, so equal-degree ties fall the same
+// way - appended to the ordering and to the breadth-first queue; when that
+// queue runs dry the next vertex is the first unused node.  The list is then
+// reversed.  The reference scans every node each pass to test for unused
+// ones (NegativeQueue, :9-17, O(N^2)); a running count gives the same test.
+struct IntInt {
+  int a, b;
+};
+bool degree_compare(IntInt i, IntInt j) { return i.b < j.b; }
+
+int ref_cuthill_mckee(const HostMesh& m, std::vector<int>& ordering, std::string& err) {
   const int nn = m.nnode;
-  std::vector<int> deg(nn);
-  for (int i = 0; i < nn; i++) deg[i] = m.ipsp[i + 1] - m.ipsp[i];
-  std::vector<char> seen(nn, 0);
-  order.clear();
-  order.reserve(nn);
-  std::vector<int> nb;
-  int start_scan = 0;
-  while ((int)order.size() < nn) {
-    int root = -1, best = 1 << 30;
-    for (int i = start_scan; i < nn; i++)
-      if (!seen[i] && deg[i] < best) { best = deg[i]; root = i; }
-    seen[root] = 1;
-    size_t head = order.size();
-    order.push_back(root);
-    while (head < order.size()) {
-      int v = order[head++];
-      nb.clear();
-      for (int j = m.ipsp[v]; j < m.ipsp[v + 1]; j++)
-        if (!seen[m.psp[j]]) nb.push_back(m.psp[j]);
-      std::stable_sort(nb.begin(), nb.end(), [&](int a, int b) { return deg[a] < deg[b]; });
-      for (int w : nb)
-        if (!seen[w]) { seen[w] = 1; order.push_back(w); }
-    }
-    while (start_scan < nn && seen[start_scan]) start_scan++;
+  ordering.assign(nn, 0);
+  if (nn == 0) return 0;
+  std::vector<IntInt> Q(nn);
+  for (int j = 0; j < nn; j++) {
+    Q[j].a = j;
+    Q[j].b = m.ipsp[j + 1] - m.ipsp[j];
   }
-  std::reverse(order.begin(), order.end());
+  std::deque<int> S;
+  std::deque<IntInt> R;
+  int i = 0;
+  const int startnode = 0;
+  ordering[i] = startnode;
+  int z = ordering[i];
+  Q[startnode].a = -1;
+  long long unused = nn - 1;
+  long long stalls = 0;
+  while (unused > 0) {
+    const long long before = unused;
+    for (int k = m.ipsp[z]; k < m.ipsp[z + 1]; k++) {
+      const int nb = m.psp[k];
+      if (nb < nn && Q[nb].a >= 0) {
+        R.push_back(Q[nb]);
+        Q[nb].a = -1;
+        unused--;
+      }
+    }
+    std::sort(R.begin(), R.end(), degree_compare);
+    while (!R.empty()) {
+      i++;
+      ordering[i] = R.front().a;
+      R.pop_front();
+      S.push_back(ordering[i]);
+    }
+    if (!S.empty()) {
+      z = S.front();
+      S.pop_front();
+    } else {
+      for (int j = 0; j < nn; j++)
+        if (Q[j].a >= 0) { z = j; break; }
+    }
+    // The reference never marks a re-seeded vertex used, so a component whose
+    // re-seed has no unused neighbour would loop forever there; stop instead.
+    stalls = (unused == before && S.empty()) ? stalls + 1 : 0;
+    if (stalls > 1) {
+      err = "Cuthill-McKee: disconnected mesh (an isolated node) cannot be ordered";
+      return -1;
+    }
+  }
+  // reverse (ReorderMeshCuthillMcKee(1))
+  std::reverse(ordering.begin(), ordering.end());
   return 0;
 }
+
+// Mesh::ReorderC2nMap (ucs/mesh.tcc:224-262): the reference applies the
+// ordering as an old-to-new map, node n of every element becomes ordering[n]
+// and the coordinates of node i move to ordering[i].
+void apply_c2n_map(HostMesh& m, const std::vector<int>& ordering) {
+  for (size_t e = 0; e < m.etype.size(); e++)
+    for (int q = 0; q < elem_nnodes(m.etype[e]); q++) m.enodes[4 * e + q] = ordering[m.enodes[4 * e + q]];
+  std::vector<double> x2((size_t)3 * m.nnode);
+  for (int i = 0; i < m.nnode; i++)
+    for (int c = 0; c < 3; c++) x2[3 * (size_t)ordering[i] + c] = m.xyz[3 * (size_t)i + c];
+  m.xyz.swap(x2);
+  m.maps_built = m.metrics_built = 0;
+}
+
+// Element-surrounding-point and point-surrounding-point maps only
+// (Mesh::BuildMapsDecomp, ucs/mesh.tcc:316), as the reorder needs them.
+int build_psp_only(HostMesh& m);
 
 thread_local std::string g_last_mesh_error;
 
@@ -646,10 +705,21 @@ PCFD_API int pcfd_mesh_stats(pcfd_mesh_t h, int* nelem_tri, int* nelem_tet, int*
 PCFD_API int pcfd_mesh_rcm_order(pcfd_mesh_t h, int* order_out) {
   if (!h || !order_out) return PCFD_ERR_ARG;
   HostMesh* m = (HostMesh*)h;
-  if (!m->maps_built) return PCFD_ERR_STATE;
-  std::vector<int> order;
-  rcm_order(*m, order);
-  std::memcpy(order_out, order.data(), sizeof(int) * order.size());
+  if (!m->maps_built && build_psp_only(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  std::vector<int> ordering;
+  if (ref_cuthill_mckee(*m, ordering, m->err) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  std::memcpy(order_out, ordering.data(), sizeof(int) * ordering.size());
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_mesh_reorder_rcm(pcfd_mesh_t h, int* order_out) {
+  if (!h) return PCFD_ERR_ARG;
+  HostMesh* m = (HostMesh*)h;
+  if (build_psp_only(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  std::vector<int> ordering;
+  if (ref_cuthill_mckee(*m, ordering, m->err) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  apply_c2n_map(*m, ordering);
+  if (order_out) std::memcpy(order_out, ordering.data(), sizeof(int) * ordering.size());
   return PCFD_OK;
 }
 

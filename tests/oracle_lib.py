@@ -33,6 +33,7 @@ def lib():
             "oracle_limiter": (C.c_int, [MV, PP, _DP, _DP, _DP, _LLP]),
             "oracle_residual": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _LLP]),
             "oracle_residual_scaled": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _DP, _LLP]),
+            "oracle_residual_full": (C.c_int, [MV, PP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _LLP]),
             "oracle_lu": (C.c_int, [_DP, _IP, C.c_int]),
             "oracle_timestep": (C.c_double, [MV, PP, _DP, C.c_double, _DP]),
             "oracle_crs_init": (None, [MV, _IP, _IP]),
@@ -183,17 +184,21 @@ class OracleSpace:
                                      C.byref(nclip)) == 0
         return l, nclip.value
 
-    def residual(self, q, g=None, l=None):
+    def residual(self, q, g=None, l=None, qold=None):
+        """ComputeResiduals; qold ([nnode][5], the state at the start of the
+        step) adds the reference's temporal residual."""
         n = self.mesh.nnode
         q = np.ascontiguousarray(q, dtype=np.float64)
         g = np.zeros((n, 27)) if g is None else np.ascontiguousarray(g)
         l = np.ones((n, 5)) if l is None else np.ascontiguousarray(l)
+        qo = None if qold is None else np.ascontiguousarray(np.asarray(qold, dtype=np.float64)[:n, :5])
         b = np.zeros((n, 5))
         babs = np.zeros((n, 5))
         norms = np.zeros(6)
         kc = C.c_longlong()
-        assert self.L.oracle_residual_scaled(C.byref(self.mesh.view), C.byref(self.cp), dp(q), dp(g), dp(l), dp(b),
-                                             dp(babs), dp(norms), C.byref(kc)) == 0
+        assert self.L.oracle_residual_full(C.byref(self.mesh.view), C.byref(self.cp), dp(q),
+                                           dp(qo) if qo is not None else None, dp(g), dp(l), dp(b),
+                                           dp(babs), dp(norms), C.byref(kc)) == 0
         self.last_babs = babs
         return b, norms, kc.value
 
@@ -262,36 +267,56 @@ class OracleImplicit(OracleSpace):
         dn = self.L.oracle_apply_dq(C.byref(self.mesh.view), C.byref(self.cp), dp(x), dp(q))
         return q, dn
 
-    def newton(self, q, nsteps, cfl=5.0, nsgs=10, cfl_start=0.0, cfl_ramp_steps=0, coloring=None):
-        """Solve's loop with PreIterate, PreTimeAdvance and NewtonIterate in
-        the reference's order; returns the final q and the resGlobal history."""
+    def newton(self, q, nsteps, cfl=5.0, nsgs=10, cfl_start=0.0, cfl_ramp_steps=0, coloring=None,
+               first_order_steps=0, limiter_refresh=1, limiter_freeze=999999):
+        """Solve's loop (ucs/solve.tcc:24-60): PreIterate, then per step
+        PreTimeAdvance (q_old, Jacobian, time steps) and NewtonIterate
+        (boundary update, gradient, limiter, residual with the temporal term,
+        SGS, ApplyDQ) in the reference's order and with its iteration
+        counter, which starts at 0 (so the first step is first order).
+        Returns the final q and the resGlobal history."""
         def ramp(it):
             cs = cfl_start if cfl_start > 0 else cfl
             if cfl_ramp_steps > 0 and it < cfl_ramp_steps:
                 return (cfl - cs) / cfl_ramp_steps * it + cs
             return cfl
         q = np.ascontiguousarray(q, dtype=np.float64).copy()
-        dt, _ = self.timestep(q, ramp(1))
+        dt, _ = self.timestep(q, ramp(0))
         hist = []
-        for it in range(1, nsteps + 1):
+        p = self.param
+        for it in range(nsteps):
+            qold = q[:self.mesh.nnode, :5].copy()
             M, q = self.jacobian(q, dt)
             dt, _ = self.timestep(q, ramp(it))
             q = self.update_bcs(q)
-            p = self.param
+            ho = p.sorder > 1 and it > first_order_steps
             g = l = None
-            if p.sorder > 1 or p.viscous:
+            if ho or p.viscous:
                 g = self.gradient(q)
-            if p.sorder > 1:
+            if ho and p.limiter and it % limiter_refresh == 0 and it < limiter_freeze:
                 l, _ = self.limiter(q, g)
-            b, norms, _ = self.residual(q, g, l)
+                self._lim = l
+            elif ho and p.limiter:
+                l = self._lim
+            if ho:
+                b, norms, _ = self.residual(q, g, l, qold=qold)
+            else:
+                b, norms, _ = OracleImplicit._first_order(self).residual(q, g, None, qold=qold)
             hist.append(norms[0])
             Mlu, pv = self.lu(M)
             if coloring is None:
                 x, _ = self.sgs(Mlu, pv, b, nsgs)
             else:
                 x = self.sgs_colored(Mlu, pv, b, nsgs, *coloring)
+            x[~np.isfinite(x).all(axis=1)] = 0.0
             q, _ = self.apply_dq(x, q)
         return q, hist
+
+    def _first_order(self):
+        if getattr(self, "_fo", None) is None:
+            import dataclasses
+            self._fo = OracleSpace(self.mesh, dataclasses.replace(self.param, sorder=1))
+        return self._fo
 
 
 def chem_rates(model_struct, rhoi, T):

@@ -90,13 +90,21 @@ def test_box_volume_equals_geometry():
     assert abs(m.vol.sum() - 1.0) < 1e-13
 
 
-def test_rcm_is_a_permutation_and_reduces_bandwidth():
+def test_rcm_order_is_the_reference_sequence_applied_as_old_to_new():
+    """pcfd_mesh_rcm_order returns Mesh::ordering as ReorderMeshCuthillMcKee(1)
+    leaves it: the reversed Cuthill-McKee sequence (position -> node), whose
+    neighbours in the sequence are neighbours in the mesh, so read that way it
+    has a small bandwidth.  The reference's ReorderC2nMap then applies it as an
+    old-to-new map (node n becomes ordering[n]); the reordered mesh built with
+    reorder=True follows that."""
     m = Mesh.box(10, 9, 8, jitter=0.2)
     order = m.rcm_order()
     assert sorted(order.tolist()) == list(range(m.nnode))
-    inv = np.empty_like(order)
-    inv[order] = np.arange(m.nnode)
+    assert order[-1] == 0  # the sequence starts at node 0 and is reversed
+    pos = np.empty_like(order)
+    pos[order] = np.arange(m.nnode)
     e = m.edges
-    bw_new = np.abs(inv[e[:, 0]] - inv[e[:, 1]]).max()
-    bw_old = np.abs(e[:, 0] - e[:, 1]).max()
-    assert bw_new <= bw_old
+    assert np.abs(pos[e[:, 0]] - pos[e[:, 1]]).max() < 0.3 * m.nnode
+    r = Mesh.box(10, 9, 8, jitter=0.2, reorder=True)
+    np.testing.assert_array_equal(r.ordering, order)
+    np.testing.assert_array_equal(r.xyz[order], m.xyz)
