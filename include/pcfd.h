@@ -167,8 +167,14 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* mesh, const pcfd_params* params, 
 PCFD_API int pcfd_destroy(pcfd_solver_t s);
 
 /* q in the reference layout: [nnode+nbnode][nvars], nvars = 10
- * (rho, rho u, rho v, rho w, rho E | T, P, u, v, w), ucs/compressible.tcc:11-22. */
+ * (rho, rho u, rho v, rho w, rho E | T, P, u, v, w), ucs/compressible.tcc:11-22.
+ * The state set also becomes q_old, the start-of-step state of the temporal
+ * residual (SolutionSpace::Init copies q into qold, ucs/solutionSpace.tcc:279). */
 PCFD_API int pcfd_set_state(pcfd_solver_t s, const double* q, int nvars, int nrows);
+/* q_old alone (SolutionField STATE_N of the state, ucs/solutionField.tcc:203):
+ * the first 5 values of the first nnode rows of q, rows of nvars = 10 or 5
+ * values.  pcfd_newton_step sets it itself at the start of each step. */
+PCFD_API int pcfd_set_qold(pcfd_solver_t s, const double* q, int nvars, int nrows);
 PCFD_API int pcfd_get_state(pcfd_solver_t s, double* q, int nvars, int nrows);
 /* freestream state Qinf (10 values), CompressibleEqnSet::UpdateQinf (ucs/compressible.tcc:827) */
 PCFD_API int pcfd_get_qinf(pcfd_solver_t s, double* qinf10);
@@ -242,7 +248,8 @@ PCFD_API int pcfd_sgs_rhs(pcfd_solver_t s, int nsweeps, const double* b, double*
 PCFD_API int pcfd_apply_dq(pcfd_solver_t s, const double* x_in, double* dqnorm);
 
 typedef struct pcfd_newton_opts {
-  int iter;             /* outer iteration number, from 1 (SolutionSpace::iter) */
+  int iter;             /* SolutionSpace::iter: the reference's counter, 0 on the first step
+                         * (which is therefore first order, ucs/solutionSpace.tcc:663,671) */
   double cfl;           /* Param::cfl */
   double cfl_start;     /* Param::cflStart (ramp start; <= 0: no ramp) */
   int cfl_ramp_steps;   /* Param::cflRampingSteps */

@@ -140,6 +140,7 @@ PROTOTYPES = {
     "pcfd_create": (C.c_int, [C.POINTER(MeshView), C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "pcfd_destroy": (C.c_int, [_P]),
     "pcfd_set_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
+    "pcfd_set_qold": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
     "pcfd_get_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
     "pcfd_get_qinf": (C.c_int, [_P, _DP]),
     "pcfd_update_bcs": (C.c_int, [_P]),

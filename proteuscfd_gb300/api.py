@@ -245,6 +245,13 @@ class SolutionSpace:
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.nrows, NVARS)
         N.check(self._lib.pcfd_set_state(self._h, N.dptr(q), NVARS, self.nrows), "pcfd_set_state")
 
+    def set_qold(self, q):
+        """The start-of-step state of the temporal residual ([nnode][5] or
+        [nrows][10]); set_state and newton_iterate set it themselves."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        q2 = q.reshape(q.shape[0], -1)
+        N.check(self._lib.pcfd_set_qold(self._h, N.dptr(q2), q2.shape[1], q2.shape[0]), "pcfd_set_qold")
+
     def get_state(self):
         q = np.empty((self.nrows, NVARS), dtype=np.float64)
         N.check(self._lib.pcfd_get_state(self._h, N.dptr(q), NVARS, self.nrows), "pcfd_get_state")
@@ -481,13 +488,14 @@ class SolutionSpace:
 
 
 def solve(space: SolutionSpace, nsteps: int, drop: float = 0.0, **opts):
-    """Outer iterations (``Solve``, ucs/solve.tcc:24).  Runs ``nsteps``
-    iterations, or stops early once resGlobal has dropped by ``drop``
-    relative to the first iteration (the reference itself never stops
-    early).  Returns the per-iteration reports."""
+    """Outer iterations (``Solve``, ucs/solve.tcc:24) with the reference's
+    counter (0 on the first step).  Runs ``nsteps`` iterations, or stops
+    early once resGlobal has dropped by ``drop`` relative to the first
+    iteration (the reference itself never stops early).  Returns the
+    per-iteration reports."""
     hist = []
     r0 = None
-    for it in range(1, nsteps + 1):
+    for it in range(nsteps):
         rep = space.newton_iterate(it, **opts)
         hist.append(rep)
         if r0 is None:

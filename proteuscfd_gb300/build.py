@@ -28,10 +28,13 @@ REF_DIR = ORACLE_DIR / "_ref"
 REF_LIB = REF_DIR / "libref_pin.so"
 REFERENCE_SRC = Path(os.environ.get("PCFD_REFERENCE_SRC", "/root/reference"))
 
+# Host code rounds each operation on its own (no fused multiply-add, which
+# aarch64 compilers form by default), as the reference's x86 build does, so
+# host preprocessing gives the same bits on both machines.
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",
-    "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
 ]
 
 
@@ -73,7 +76,8 @@ def build_library(verbose: bool = False) -> Path:
         objs.append(obj)
     for src in cpp:
         obj = BUILD / (src.stem + ".cpp.o")
-        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall", "-c", str(src), "-o", str(obj)])
+        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall", "-c",
+                     str(src), "-o", str(obj)])
         objs.append(obj)
     _run_all(cmds)
     tmp = LIB.with_suffix(".so.tmp")
@@ -90,7 +94,11 @@ def build_oracle(verbose: bool = False) -> Path:
     srcs = csrcs + [ORACLE_DIR / "oracle.h", ROOT / "include" / "pcfd.h"]
     if _stale(ORACLE_LIB, srcs + [Path(__file__)]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run_all([["gcc", "-O2", "-std=c11", "-fPIC", "-shared"] + [str(c) for c in csrcs] + ["-o", str(tmp), "-lm"]])
+        # -ffp-contract=off: every operation rounded on its own, as in the
+        # reference's x86 build, on the Arm machine too (whose compiler would
+        # otherwise fuse multiply-adds and move the oracle off the reference's bits)
+        _run_all([["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off"] + [str(c) for c in csrcs] +
+                  ["-o", str(tmp), "-lm"]])
         os.replace(tmp, ORACLE_LIB)
         if verbose:
             print("built", ORACLE_LIB)

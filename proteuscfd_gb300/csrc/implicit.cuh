@@ -113,9 +113,14 @@ struct JacConst {
 // Kernel_NumJac (ucs/jacobian.tcc:254): one-sided finite differences of the
 // Roe flux (h = 1e-8, 11 flux evaluations per edge) into A(R,L) and A(L,R),
 // plus Kernel_Viscous_Jac (:734) when viscous.
+// q is the state the inviscid differences see (the state before the boundary
+// conditions: ComputeSpatialJacobian runs Kernel_NumJac before Bkernel_NumJac
+// applies them, ucs/jacobian.tcc:186-188); qv the state after them, which
+// the viscous blocks see (Kernel_Viscous_Jac runs after, :190-194).
 template <class T>
 __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restrict__ en, const D4* __restrict__ ea,
                                                   const double* __restrict__ eh, const double* __restrict__ q,
+                                                  const double* __restrict__ qv,
                                                   const int* __restrict__ pos_lr, const int* __restrict__ pos_rl,
                                                   JacConst k, T* __restrict__ M, unsigned long long* health) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,6 +160,11 @@ __global__ void __launch_bounds__(128) k_jac_edge(int nedge, const int2* __restr
     double dx[3] = {2.0 * eh[3 * (size_t)e], 2.0 * eh[3 * (size_t)e + 1], 2.0 * eh[3 * (size_t)e + 2]};
     double s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
     double vL[25], vR[25];
+#pragma unroll
+    for (int t = 0; t < NVARS; t++) {
+      QL[t] = qv[(size_t)n.x * NVARS + t];
+      QR[t] = qv[(size_t)n.y * NVARS + t];
+    }
     viscous_jacobian<double>(QL, QR, dx, s2, a.x, a.y, a.z, a.w, k.gamma, k.Pr, k.inv_retilde, k.S, vL, vR);
 #pragma unroll
     for (int t = 0; t < 25; t++) { tL[t] += vL[t]; tR[t] += vR[t]; }
@@ -182,7 +192,8 @@ __device__ __forceinline__ double store_blk(double*, double v) { return v; }
 template <class T>
 __global__ void __launch_bounds__(128, 3) k_jac_edge_df(int nedge, const int2* __restrict__ en,
                                                      const D4* __restrict__ ea, const double* __restrict__ eh,
-                                                     const double* __restrict__ q, const int* __restrict__ pos_lr,
+                                                     const double* __restrict__ q, const double* __restrict__ qv,
+                                                     const int* __restrict__ pos_lr,
                                                      const int* __restrict__ pos_rl, JacConst k, T* __restrict__ M,
                                                      unsigned long long* health) {
   // FP64 blocks keep FP64 quotients and viscous blocks; FP32 and BF16
@@ -229,8 +240,8 @@ __global__ void __launch_bounds__(128, 3) k_jac_edge_df(int nedge, const int2* _
     VR QLv[NVARS], QRv[NVARS];
 #pragma unroll
     for (int t = 0; t < NVARS; t++) {
-      QLv[t] = (VR)q[(size_t)n.x * NVARS + t];
-      QRv[t] = (VR)q[(size_t)n.y * NVARS + t];
+      QLv[t] = (VR)qv[(size_t)n.x * NVARS + t];
+      QRv[t] = (VR)qv[(size_t)n.y * NVARS + t];
     }
     VR dx[3] = {(VR)(2.0 * eh[3 * (size_t)e]), (VR)(2.0 * eh[3 * (size_t)e + 1]), (VR)(2.0 * eh[3 * (size_t)e + 2])};
     VR s2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
@@ -246,26 +257,11 @@ __global__ void __launch_bounds__(128, 3) k_jac_edge_df(int nedge, const int2* _
   for (int t = 0; t < 25; t++) { bl[t] = store_blk(bl, tL[t]); br[t] = store_blk(br, tR[t]); }
 }
 
-// Bkernel_NumJac (ucs/jacobian.tcc:459) with jacobianBoundaryEval = 0: the
-// phantom state is re-derived from each perturbed interior state through
-// the boundary condition, and the difference quotient goes to the diagonal.
-// The state itself went through UpdateBCs just before (the reference applies
-// the boundary conditions to the stored state inside this kernel).
-__global__ void __launch_bounds__(128) k_jac_bedge(int nbedge, const int2* __restrict__ bn, const D4* __restrict__ ba,
-                                                   const int* __restrict__ bbc, const double* __restrict__ btw,
-                                                   const int* __restrict__ bnrm, BcConst bk, int beval,
-                                                   const double* __restrict__ q, double* __restrict__ bblk,
-                                                   unsigned long long* health) {
-  int he = blockIdx.x * blockDim.x + threadIdx.x;
-  if (he >= nbedge) return;
-  const int2 n = bn[he];
-  const D4 a = ba[he];
-  double QL[NVARS], QR[NVARS], nQ[NVARS];
-  for (int t = 0; t < NVARS; t++) { QL[t] = q[(size_t)n.x * NVARS + t]; QR[t] = q[(size_t)n.y * NVARS + t]; }
-  const int bct = bbc[he];
-  for (int t = 0; t < NVARS; t++) nQ[t] = 0.0;
-  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
-    for (int t = 0; t < NVARS; t++) nQ[t] = q[(size_t)bnrm[he] * NVARS + t];
+// The differences of one boundary half-edge from its post-condition states
+// QL, QR (Bkernel_NumJac's loop, ucs/jacobian.tcc:470-520).
+__device__ void jac_bedge_fd(int he, int bct, const D4 a, double Tw, const double* nQ, const BcConst& bk, int beval,
+                             const double* QL, const double* QR, double* __restrict__ bblk,
+                             unsigned long long* health) {
   const double h = 1.0e-8;
   const double ih = 1.0 / h;
   double fS[NEQN];
@@ -273,7 +269,7 @@ __global__ void __launch_bounds__(128) k_jac_bedge(int nbedge, const int2* __res
     // base state through the same boundary-condition map as the perturbed ones
     double QBL[NVARS], QBR[NVARS];
     for (int t = 0; t < NVARS; t++) { QBL[t] = QL[t]; QBR[t] = QR[t]; }
-    apply_bc(bk, bct, QBL, QBR, a, btw[he], nQ);
+    apply_bc(bk, bct, QBL, QBR, a, Tw, nQ);
     numflux(QBL, QBR, a, bk.gamma, fS, health);
   } else {
     numflux(QL, QR, a, bk.gamma, fS, health);
@@ -285,9 +281,88 @@ __global__ void __launch_bounds__(128) k_jac_bedge(int nbedge, const int2* __res
     QPL[i] += h;
     aux_vars(bk.gamma, QPL);
     aux_vars(bk.gamma, QPR);
-    if (beval != 1) apply_bc(bk, bct, QPL, QPR, a, btw[he], nQ);
+    if (beval != 1) apply_bc(bk, bct, QPL, QPR, a, Tw, nQ);
     numflux(QPL, QPR, a, bk.gamma, fL, health);
     for (int j = 0; j < NEQN; j++) out[j * 5 + i] = (fL[j] - fS[j]) * ih;
+  }
+}
+
+// The node and phantom states one boundary half-edge of Bkernel_NumJac
+// (ucs/jacobian.tcc:459) works on.  Thread t < nind takes an independent
+// half-edge (its node has no hard-setting condition); the rest take slot
+// p = t - nind of a hard-set node's ordered list, whose earlier slots'
+// hard sets are replayed on the node state first - the reference applies the
+// conditions in place, half-edge after half-edge, before each difference.
+// The states are read from q as it was before this pass.
+struct BedgeSlots {
+  int nind;
+  const int* ind;     // [nind] independent half-edges
+  const int* slot_group, *gnode, *gptr, *ghe;
+};
+
+__device__ __forceinline__ int bedge_states(const BedgeSlots& sl, int t, const BcConst& k, const int2* __restrict__ bn,
+                                            const int* __restrict__ bbc, const double* __restrict__ btw,
+                                            const int* __restrict__ bnrm, const double* __restrict__ q, double* QL,
+                                            double* QR) {
+  int he;
+  if (t < sl.nind) {
+    he = sl.ind[t];
+    for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)bn[he].x * NVARS + j];
+  } else {
+    const int p = t - sl.nind;
+    he = sl.ghe[p];
+    const int g = sl.slot_group[p];
+    for (int j = 0; j < NVARS; j++) QL[j] = q[(size_t)sl.gnode[g] * NVARS + j];
+    replay_group(k, sl.gptr[g], p, sl.ghe, bn, bbc, btw, bnrm, q, QL);
+  }
+  for (int j = 0; j < NVARS; j++) QR[j] = q[(size_t)bn[he].y * NVARS + j];
+  return he;
+}
+
+// Bkernel_NumJac (ucs/jacobian.tcc:459) with jacobianBoundaryEval = 0: the
+// condition is applied to the half-edge's states (CalculateBoundaryVariables,
+// which the reference runs inside this kernel), the phantom state is
+// re-derived from each perturbed interior state through the condition, and
+// the difference quotient goes to the diagonal.
+__global__ void __launch_bounds__(128) k_jac_bedge(int nthreads, BedgeSlots sl, const int2* __restrict__ bn,
+                                                   const D4* __restrict__ ba, const int* __restrict__ bbc,
+                                                   const double* __restrict__ btw, const int* __restrict__ bnrm,
+                                                   BcConst bk, int beval, const double* __restrict__ q,
+                                                   double* __restrict__ bblk, unsigned long long* health) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nthreads) return;
+  double QL[NVARS], QR[NVARS], nQ[NVARS];
+  const int he = bedge_states(sl, t, bk, bn, bbc, btw, bnrm, q, QL, QR);
+  const D4 a = ba[he];
+  const int bct = bbc[he];
+  for (int j = 0; j < NVARS; j++) nQ[j] = 0.0;
+  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+    for (int j = 0; j < NVARS; j++) nQ[j] = q[(size_t)bnrm[he] * NVARS + j];
+  if (!apply_bc(bk, bct, QL, QR, a, btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
+  jac_bedge_fd(he, bct, a, btw[he], nQ, bk, beval, QL, QR, bblk, health);
+}
+
+// One thread walking the half-edges in order on a private copy of the state
+// (the exact reference order when a no-slip normal node is itself hard-set
+// by a condition, so a condition reads a state an earlier one wrote).
+__global__ void k_jac_bedge_sequential(int nbedge, const int2* __restrict__ bn, const D4* __restrict__ ba,
+                                       const int* __restrict__ bbc, const double* __restrict__ btw,
+                                       const int* __restrict__ bnrm, BcConst bk, int beval, double* __restrict__ qw,
+                                       double* __restrict__ bblk, unsigned long long* health) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int he = 0; he < nbedge; he++) {
+    const int2 n = bn[he];
+    double* QL = &qw[(size_t)n.x * NVARS];
+    double* QR = &qw[(size_t)n.y * NVARS];
+    double nQ[NVARS];
+    const int bct = bbc[he];
+    for (int j = 0; j < NVARS; j++) nQ[j] = 0.0;
+    if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+      for (int j = 0; j < NVARS; j++) nQ[j] = qw[(size_t)bnrm[he] * NVARS + j];
+    if (!apply_bc(bk, bct, QL, QR, ba[he], btw[he], nQ)) atomicAdd(&health[H_BADBC], 1ull);
+    double L[NVARS], R[NVARS];
+    for (int j = 0; j < NVARS; j++) { L[j] = QL[j]; R[j] = QR[j]; }
+    jac_bedge_fd(he, bct, ba[he], btw[he], nQ, bk, beval, L, R, bblk, health);
   }
 }
 
@@ -352,25 +427,29 @@ __device__ int apply_bc_df(int bct, dfl gamma, int no_cvbc, const dfl* qinf, dfl
 // ten far-field or wall sub-iterations and the six Roe fluxes of a
 // half-edge on the FP32 pipes; the difference quotients (FP64 diagonal
 // contributions) carry ~1e-6 relative error, as in k_jac_edge_df.
-__global__ void __launch_bounds__(128) k_jac_bedge_df(int nbedge, const int2* __restrict__ bn,
+__global__ void __launch_bounds__(128) k_jac_bedge_df(int nthreads, BedgeSlots sl, const int2* __restrict__ bn,
                                                       const D4* __restrict__ ba, const int* __restrict__ bbc,
                                                       const double* __restrict__ btw, const int* __restrict__ bnrm,
                                                       BcConst bk, int beval, const double* __restrict__ q,
                                                       double* __restrict__ bblk, unsigned long long* health) {
-  int he = blockIdx.x * blockDim.x + threadIdx.x;
-  if (he >= nbedge) return;
-  const int2 n = bn[he];
+  const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tt >= nthreads) return;
+  double QL0[NVARS], QR0[NVARS], nQ0[NVARS];
+  const int he = bedge_states(sl, tt, bk, bn, bbc, btw, bnrm, q, QL0, QR0);
+  const int bct = bbc[he];
+  for (int t = 0; t < NVARS; t++) nQ0[t] = 0.0;
+  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
+    for (int t = 0; t < NVARS; t++) nQ0[t] = q[(size_t)bnrm[he] * NVARS + t];
+  // the condition on the stored state, in FP64 as the boundary update does
+  if (!apply_bc(bk, bct, QL0, QR0, ba[he], btw[he], nQ0)) atomicAdd(&health[H_BADBC], 1ull);
   const D4 a = ba[he];
   dfl QL[NVARS], QR[NVARS], nQ[NVARS], qinf[NVARS];
   for (int t = 0; t < NVARS; t++) {
-    QL[t] = to_df(q[(size_t)n.x * NVARS + t]);
-    QR[t] = to_df(q[(size_t)n.y * NVARS + t]);
+    QL[t] = to_df(QL0[t]);
+    QR[t] = to_df(QR0[t]);
     qinf[t] = to_df(bk.qinf[t]);
-    nQ[t] = Sc<dfl>::c(0.0);
+    nQ[t] = to_df(nQ0[t]);
   }
-  const int bct = bbc[he];
-  if (bct == PCFD_BC_NOSLIP && bnrm[he] >= 0)
-    for (int t = 0; t < NVARS; t++) nQ[t] = to_df(q[(size_t)bnrm[he] * NVARS + t]);
   const dfl gamma = to_df(bk.gamma), gm1 = to_df(bk.gamma - 1.0), ig = to_df(1.0 / bk.gamma),
             igm1 = to_df(1.0 / (bk.gamma - 1.0));
   const dfl ax = to_df(a.x), ay = to_df(a.y), az = to_df(a.z), aw = to_df(a.w), Tw = to_df(btw[he]);

@@ -131,6 +131,8 @@ struct Solver {
   double* d_grad = nullptr;     // [nnode][27]
   double* d_lim = nullptr;      // [nnode][5]
   double* d_b = nullptr;        // [nnode][5]
+  double* d_qold = nullptr;     // [nnode][5] conservative state at the start of the step (STATE_N)
+  double* d_qpre = nullptr;     // [ntot][10] state before the Jacobian's boundary pass
   double* d_ef = nullptr;       // [nedge][5] edge flux scratch
   double* d_bf = nullptr;       // [nbedge][5] half-edge flux scratch
   double* d_part = nullptr;     // [kNormBlocks][6] norm partial sums (scratch)
@@ -299,6 +301,42 @@ struct BcConst {
   double qinf[NVARS];
 };
 
+// Arithmetic at the reference's decision points (a limiter's "does the
+// extrapolation raise the value", the far field's "is there flow through
+// the face") in the reference's rounding: each product and sum rounded on its
+// own, in its order, no fused multiply-add.  A state whose answer sits on
+// the tie (a zero velocity component, a flat field) then takes the
+// reference's branch; the double-float arithmetic keeps its own forms.
+template <class S>
+__device__ __forceinline__ S dot3_ref(S a0, S b0, S a1, S b1, S a2, S b2) {
+  return a0 * b0 + a1 * b1 + a2 * b2;
+}
+template <>
+__device__ __forceinline__ double dot3_ref<double>(double a0, double b0, double a1, double b1, double a2, double b2) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
+}
+// q + ExtrapolateCorrection(dq, grad, dx) (ucs/eqnset.h:231) with a limiter of one
+template <class S>
+__device__ __forceinline__ S extrap_ref(S qi, S dq, S gdx, S hchi, S omc, bool chi0) {
+  return chi0 ? qi + gdx : qi + (hchi * dq + omc * gdx);
+}
+template <>
+__device__ __forceinline__ double extrap_ref<double>(double qi, double dq, double gdx, double hchi, double omc,
+                                                     bool chi0) {
+  return chi0 ? __dadd_rn(qi, gdx) : __dadd_rn(qi, __dadd_rn(__dmul_rn(hchi, dq), __dmul_rn(omc, gdx)));
+}
+// GetTheta (ucs/compressible.tcc:996): u nx + v ny + w nz of the averaged state
+template <class S>
+__device__ __forceinline__ S theta_ref(S t0, S t1, S t2, S t3, S ax, S ay, S az) {
+  const S it0 = Sc<S>::c(1.0) / t0;
+  return t1 * it0 * ax + t2 * it0 * ay + t3 * it0 * az;
+}
+template <>
+__device__ __forceinline__ double theta_ref<double>(double t0, double t1, double t2, double t3, double ax, double ay,
+                                                    double az) {
+  return dot3_ref<double>(__ddiv_rn(t1, t0), ax, __ddiv_rn(t2, t0), ay, __ddiv_rn(t3, t0), az);
+}
+
 // GetFarfieldBoundaryVariables (ucs/compressible.tcc:1246), static grid;
 // S = double, or dfl for the double-float residual arithmetic.  qinf and
 // the stored pressure pi come in as S.
@@ -310,7 +348,7 @@ __device__ void bc_farfield(S gamma, const S* Qinf, const S* QL, S pi, S* QR, co
     S t0 = (QL[0] + QR[0]) * half, t1 = (QL[1] + QR[1]) * half, t2 = (QL[2] + QR[2]) * half,
       t3 = (QL[3] + QR[3]) * half, t4 = (QL[4] + QR[4]) * half;
     S it0 = one / t0;
-    S theta = t1 * it0 * ax + t2 * it0 * ay + t3 * it0 * az;
+    S theta = theta_ref<S>(t0, t1, t2, t3, ax, ay, az);
     S rhoi = QL[0];
     S iri = one / QL[0];
     S ui = QL[1] * iri, vi = QL[2] * iri, wi = QL[3] * iri;
@@ -715,8 +753,8 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
       if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
 #pragma unroll
       for (int t = 0; t < NEQN; t++) {
-        S gdx = gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2;
-        S Q = CHI0 ? qi[t] + gdx : qi[t] + (hchi * (qj[t] - qi[t]) + omc * gdx);
+        S gdx = dot3_ref<S>(gi[3 * t], dx0, gi[3 * t + 1], dx1, gi[3 * t + 2], dx2);
+        S Q = extrap_ref<S>(qi[t], qj[t] - qi[t], gdx, hchi, omc, CHI0);
         S r = one;
         if (Q > qi[t]) r = (qmax[t] - qi[t]) / (Q - qi[t]);
         else if (Q < qi[t]) r = (qmin[t] - qi[t]) / (Q - qi[t]);
@@ -767,11 +805,11 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
     if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
-      S gdx = gi[3 * t] * dx0 + gi[3 * t + 1] * dx1 + gi[3 * t + 2] * dx2;
+      S gdx = dot3_ref<S>(gi[3 * t], dx0, gi[3 * t + 1], dx1, gi[3 * t + 2], dx2);
       S corr = CHI0 ? gdx : hchi * (qj[t] - qi[t]) + omc * gdx;
       S num, den;
       if (F64) {
-        S Q = qi[t] + corr;
+        S Q = extrap_ref<S>(qi[t], qj[t] - qi[t], gdx, hchi, omc, CHI0);
         S DM = Q - qi[t];
         bool pos = Q > qi[t];
         S DP = pos ? dpp[t] : dpm[t];
@@ -1159,7 +1197,10 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
                                                          const S* __restrict__ bf, const int* __restrict__ bbc,
                                                          const double* __restrict__ btw, double* __restrict__ b,
                                                          double* __restrict__ part, int* __restrict__ clipflag,
-                                                         const int* __restrict__ clipany) {
+                                                         const int* __restrict__ clipany,
+                                                         const double* __restrict__ q,
+                                                         const double* __restrict__ qold,
+                                                         const double* __restrict__ vol, double timestep) {
   __shared__ double red[kNormThreads / 32][6];
   double acc[6] = {0, 0, 0, 0, 0, 0};
   const int any = *(volatile const int*)clipany;
@@ -1189,6 +1230,14 @@ __global__ void __launch_bounds__(kNormThreads) k_gather(int nnode, const int* _
     double rd[NEQN];
 #pragma unroll
     for (int t = 0; t < NEQN; t++) rd[t] = Sc<S>::to(r[t]);
+    if (qold) {
+      // TemporalResidual (ucs/residual.tcc:150-175), first order: b -= (vol/dt) (q - q_old),
+      // in the reference's rounding (no contraction)
+      const double c = vol[i] / timestep;
+#pragma unroll
+      for (int t = 0; t < NEQN; t++)
+        rd[t] = __dsub_rn(rd[t], __dmul_rn(c, __dsub_rn(q[(size_t)i * NVARS + t], qold[(size_t)i * NEQN + t])));
+    }
     for (int p = bptr[i]; p < bptr[i + 1]; p++) {
       int he = bhe[p];
       if (bbc[he] != PCFD_BC_NOSLIP) continue;
@@ -1277,7 +1326,7 @@ void free_solver(Solver* s) {
   free_learned(s->lp);
   void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
-                  s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_ef, s->d_bf, s->d_part,
+                  s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_qold, s->d_qpre, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
                   s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_mdot_done, s->d_scal, s->d_color_rows, s->d_cptr, s->d_rowdesc, s->d_mv, s->d_gbar, s->d_sgs_err, s->d_V, s->d_Z, s->d_w, s->d_dots,
@@ -1341,12 +1390,34 @@ FluxConst make_flux_const(const Solver* s) {
   return k;
 }
 
+// Param::dt as the temporal residual reads it: <= 0 is steady, 0 stands for
+// the reference's default -1.0
+double param_time_step(const pcfd_params& p) { return p.time_step == 0.0 ? -1.0 : p.time_step; }
+
+// SolutionField::EvolveInTime for the state (ucs/solutionField.tcc:203): the
+// conservative state of the interior nodes becomes the step's q_old
+__global__ void k_save_qold(int nnode, const double* __restrict__ q, double* __restrict__ qold) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x)
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) qold[(size_t)i * NEQN + t] = q[(size_t)i * NVARS + t];
+}
+
+int save_qold(Solver* s) {
+  return launch(s, T_SETUP, [&] {
+    k_save_qold<<<nblk(s->nnode, 256), 256, 0, s->stream>>>(s->nnode, s->d_q, s->d_qold);
+  });
+}
+
 void host_qinf(const pcfd_params& p, double* Q) {
-  // UpdateQinf (ucs/compressible.tcc:827): p = T = 1, rho = gamma p / T
+  // UpdateQinf (ucs/compressible.tcc:827-864): rho = gamma p / T with the
+  // non-dimensional freestream T and p (1 up to the rounding of the
+  // reference's scaling)
   double gamma = p.gamma, gm1 = gamma - 1.0;
-  double rho = 1.0 * gamma / 1.0;
+  const double T = p.tinf == 0.0 ? 1.0 : p.tinf;
+  const double pr = p.pinf == 0.0 ? 1.0 : p.pinf;
+  double rho = pr * gamma / T;
   double u = p.flowdir[0] * p.mach, v = p.flowdir[1] * p.mach, w = p.flowdir[2] * p.mach;
-  double E = 1.0 / gm1 + 0.5 * rho * (u * u + v * v + w * w);
+  double E = pr / gm1 + 0.5 * rho * (u * u + v * v + w * w);
   Q[0] = rho; Q[1] = rho * u; Q[2] = rho * v; Q[3] = rho * w; Q[4] = E;
   double ir = 1.0 / Q[0];
   double uu = Q[1] * ir, vv = Q[2] * ir, ww = Q[3] * ir;
@@ -1563,7 +1634,8 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
   rc = launch(s, T_GATHER, [&] {
     k_gather<S><<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, r.ef, s->d_bptr, s->d_bhe,
                                                             r.bf, s->d_bbc, s->d_btw, s->d_b, s->d_part, s->d_clipflag,
-                                                            s->d_clipany);
+                                                            s->d_clipany, s->d_q, s->prm.torder ? s->d_qold : nullptr,
+                                                            s->d_vol, param_time_step(s->prm));
   });
   if (rc) return rc;
   return launch(s, T_NORM, [&] {
@@ -1657,25 +1729,33 @@ int run_jacobian_t(Solver* s) {
   T* M = (T*)s->d_M;
   JacConst jk = make_jac_const(s);
   BcConst bk = make_bc_const(s);
+  // inviscid differences on the state before the conditions, viscous blocks
+  // on the state after them (ComputeSpatialJacobian's order)
   int rc = launch(s, T_JAC_EDGE, [&] {
     if (s->arith)
-      k_jac_edge_df<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
-                                                                  s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
+      k_jac_edge_df<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_qpre,
+                                                                  s->d_q, s->d_pos_lr, s->d_pos_rl, jk, M,
+                                                                  s->d_health);
     else
-      k_jac_edge<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_q,
-                                                               s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
+      k_jac_edge<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_qpre,
+                                                               s->d_q, s->d_pos_lr, s->d_pos_rl, jk, M, s->d_health);
   });
   if (rc) return rc;
   if (s->nbedge > 0) {
+    const BedgeSlots sl{s->nbind, s->d_bind, s->d_bgslot, s->d_bgnode, s->d_bgptr, s->d_bghe};
+    const int nth = s->nbind + s->nbgslot;
     rc = launch(s, T_JAC_BEDGE, [&] {
-      if (s->arith)
-        k_jac_bedge_df<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc,
-                                                                   s->d_btw, s->d_bnrm, bk, s->prm.jac_boundary_eval,
-                                                                   s->d_q, s->d_bblk, s->d_health);
+      if (s->bc_sequential)
+        k_jac_bedge_sequential<<<1, 1, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, bk,
+                                                       s->prm.jac_boundary_eval, s->d_qpre, s->d_bblk, s->d_health);
+      else if (s->arith)
+        k_jac_bedge_df<<<nblk(nth, 128), 128, 0, s->stream>>>(nth, sl, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
+                                                             s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_qpre,
+                                                             s->d_bblk, s->d_health);
       else
-        k_jac_bedge<<<nblk(s->nbedge, 128), 128, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
-                                                                s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_q,
-                                                                s->d_bblk, s->d_health);
+        k_jac_bedge<<<nblk(nth, 128), 128, 0, s->stream>>>(nth, sl, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm,
+                                                          bk, s->prm.jac_boundary_eval, s->d_qpre, s->d_bblk,
+                                                          s->d_health);
     });
     if (rc) return rc;
   }
@@ -1711,6 +1791,16 @@ int run_jacobian(Solver* s) {
     int rc = ensure_matrix(s, 0);
     if (rc) return rc;
   }
+  // ComputeSpatialJacobian (ucs/jacobian.tcc:130) reads the state before the
+  // boundary conditions for its inviscid differences, and its boundary pass
+  // applies the conditions to the stored state (what UpdateBCs does) before
+  // the viscous blocks: keep a copy of the state before, then update it
+  if (!s->d_qpre) {
+    int rc = dalloc(&s->d_qpre, (size_t)s->ntot * NVARS);
+    if (rc) return rc;
+  }
+  CUDA_TRY(cudaMemcpyAsync(s->d_qpre, s->d_q, (size_t)s->ntot * NVARS * sizeof(double), cudaMemcpyDeviceToDevice,
+                           s->stream));
   int rc = run_bcs(s, s->arith);
   if (rc) return rc;
   // the gradient no longer matches the state; the limiter field keeps its
@@ -2543,6 +2633,10 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   if (prm->limiter < 0 || prm->limiter > 3)
     return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: limiter must be 0 (off), 1 (Barth), 2 (Venkatakrishnan) or 3 "
                                          "(modified Venkatakrishnan)");
+  if (prm->torder < 0 || prm->torder > 1 || prm->time_step > 0.0)
+    return set_err(PCFD_ERR_UNSUPPORTED, "pcfd_create: steady runs only (torder 0 or 1, time_step <= 0); the "
+                                         "second-order time-accurate residual is not built");
+  if (prm->tinf < 0.0 || prm->pinf < 0.0) return set_err(PCFD_ERR_ARG, "pcfd_create: tinf and pinf must be >= 0");
   if (prm->viscous && (prm->Re <= 0.0 || prm->Pr <= 0.0 || prm->ref_temperature <= 0.0))
     return set_err(PCFD_ERR_ARG, "pcfd_create: viscous run needs Re, Pr and ref_temperature > 0");
   const long long nn = m->nnode, ne = m->nedge, nb = m->nbedge;
@@ -2733,6 +2827,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dalloc(&s->d_grad, (size_t)nn * NTERMS * 3));
   TRY(dalloc(&s->d_lim, (size_t)nn * NEQN));
   TRY(dalloc(&s->d_b, (size_t)nn * NEQN + 4));  // tail padding: staged sweep windows
+  TRY(dalloc(&s->d_qold, (size_t)nn * NEQN));
   TRY(dalloc(&s->d_ef, (size_t)ne * NEQN));
   TRY(dalloc(&s->d_bf, (size_t)nb * NEQN));
   TRY(dalloc(&s->d_part, (size_t)kNormBlocks * 6));
@@ -2755,6 +2850,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(launch(s, T_SETUP, [&] {
     k_fill_state<<<nblk(s->ntot, 256), 256, 0, s->stream>>>(s->ntot, d_qinf, s->d_q);
   }));
+  TRY(save_qold(s));
   ce = cudaStreamSynchronize(s->stream);
   cudaFree(d_sw);
   cudaFree(d_qinf);
@@ -2868,9 +2964,21 @@ PCFD_API int pcfd_set_state(pcfd_solver_t h, const double* q, int nvars, int nro
   Solver* s = (Solver*)h;
   if (!s || !q || nvars != NVARS || nrows != s->ntot) return set_err(PCFD_ERR_ARG, "pcfd_set_state: bad arguments");
   CUDA_TRY(cudaMemcpyAsync(s->d_q, q, (size_t)nrows * NVARS * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc = save_qold(s);
+  if (rc) return rc;
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   s->have_grad = s->have_lim = 0;
   s->f_q_valid = 0;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_set_qold(pcfd_solver_t h, const double* q, int nvars, int nrows) {
+  Solver* s = (Solver*)h;
+  if (!s || !q || (nvars != NVARS && nvars != NEQN) || nrows < s->nnode)
+    return set_err(PCFD_ERR_ARG, "pcfd_set_qold: bad arguments");
+  CUDA_TRY(cudaMemcpy2DAsync(s->d_qold, NEQN * sizeof(double), q, (size_t)nvars * sizeof(double),
+                             NEQN * sizeof(double), (size_t)s->nnode, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
   return PCFD_OK;
 }
 
@@ -3266,7 +3374,7 @@ PCFD_API int pcfd_apply_dq(pcfd_solver_t h, const double* x_in, double* dqnorm) 
 
 PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_newton_report* rep) {
   Solver* s = (Solver*)h;
-  if (!s || !o || o->iter < 1 || o->nsgs < 0 || !(o->cfl > 0.0))
+  if (!s || !o || o->iter < 0 || o->nsgs < 0 || !(o->cfl > 0.0))
     return set_err(PCFD_ERR_ARG, "pcfd_newton_step: bad arguments");
   if (o->linear_solver < 0 || o->linear_solver > 2)
     return set_err(PCFD_ERR_ARG, "pcfd_newton_step: linear_solver must be 0 (SGS), 1 (FGMRES) or 2 (learned)");
@@ -3278,8 +3386,10 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   // SolutionSpace::PreIterate (ucs/solutionSpace.tcc:510): a time step exists
   // before the first Jacobian
   if (!s->have_dt && (rc = run_timestep(s, cfl))) return rc;
-  // PreTimeAdvance (:573): Jacobian with the time step of the previous
-  // iteration, then this iteration's CFL and time steps
+  // PreTimeAdvance (:573): the state becomes the step's q_old (EvolveInTime),
+  // the Jacobian uses the time step of the previous iteration, then this
+  // iteration's CFL and time steps
+  if (s->prm.torder && (rc = save_qold(s))) return rc;
   const int jf = o->jac_update_freq > 0 ? o->jac_update_freq : 1;
   if (o->nsgs > 0 && (o->iter % jf == 0 || o->iter == 1 || !s->have_jac) && (rc = run_jacobian(s))) return rc;
   if ((rc = run_timestep(s, cfl))) return rc;

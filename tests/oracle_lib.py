@@ -203,7 +203,9 @@ class OracleSpace:
         return b, norms, kc.value
 
     def full(self, q):
-        """UpdateBCs, gradient, limiter, residual - the NewtonIterate order."""
+        """UpdateBCs, gradient, limiter, residual - the NewtonIterate order;
+        the state given is the step's q_old of the temporal residual."""
+        q_in = np.asarray(q, dtype=np.float64)
         q = self.update_bcs(q)
         p = self.param
         g = l = None
@@ -211,7 +213,7 @@ class OracleSpace:
             g = self.gradient(q)
         if p.sorder > 1:
             l, _ = self.limiter(q, g)
-        b, norms, _ = self.residual(q, g, l)
+        b, norms, _ = self.residual(q, g, l, qold=q_in)
         return q, g, l, b, norms
 
 

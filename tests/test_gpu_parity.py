@@ -53,7 +53,7 @@ def test_stagewise_parity(case, state):
         assert nclip == 0
         assert np.abs(lg - l).max() <= 1e-12
     bg, ng = S.compute_residuals()
-    bo, no, kc = O.residual(qo, g, l)
+    bo, no, kc = O.residual(qo, g, l, qold=q0)  # set_state makes q0 the step's q_old
     assert kc == 0
     assert_residual_close(bg, bo, O.last_babs)
     assert np.allclose(ng, no, rtol=1e-12, atol=0)
@@ -143,7 +143,7 @@ def test_pressure_clip_matches_oracle(seed):
     S.gradient()
     lg = S.limiter()
     assert np.abs(lg - l).max() <= 1e-12
-    bo, no, _ = O.residual(qo, g, l)
+    bo, no, _ = O.residual(qo, g, l, qold=q0)
     bg, ng = S.compute_residuals()
     assert_residual_close(bg, bo, O.last_babs)
     # fused path: the clip detected inside the edge-flux pass
