@@ -130,14 +130,33 @@ def max_over_ranks(pg, x):
     return float(t.item())
 
 
-def cpu_sample(steps_budget_s=15.0, threads=1, nx=40, ny=30, nz=30):
-    """The oracle (a scalar C port of the reference path) timed on the host
-    cores on a bounded sample of the same workload family."""
+# The CPU baseline's bounded sample of the workload family: a box of the
+# same generator, clustering and boundary conditions, small enough that
+# every host thread evaluates its own residual within a second or so.
+CPU_SAMPLE_DIMS = (64, 44, 44)
+
+
+def product_loaded():
+    """Whether this process has mapped the product library (it must not, in
+    the reference arm)."""
+    try:
+        return "libpcfd.so" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return None
+
+
+def cpu_sample(budget_s=15.0, threads=1, dims=CPU_SAMPLE_DIMS):
+    """The oracle - a C restatement of the reference path, bit-identical to
+    it on the reference's own outputs - timed on the host cores: each thread
+    runs whole residual evaluations (boundary update, LSQ gradient, limiter,
+    fluxes, norms) of the sample box, built by the oracle's own mesh
+    generator (nothing of the product is loaded).  Returns (baseline dict,
+    seconds, evaluations)."""
     sys.path.insert(0, str(ROOT / "tests"))
-    from oracle_lib import OracleSpace
+    from oracle_lib import OracleMesh, OracleSpace
     from proteuscfd_gb300 import cases
-    case = cases.ns_flatplate(nx, ny, nz)
-    m = cases.build_mesh(case)
+    case = cases.ns_flatplate(*dims)
+    m = OracleMesh.box(dims[0], dims[1], dims[2], **case.mesh_kw)
     O = OracleSpace(m, case.param)
     nrows = m.nnode + m.nbedge
     q0 = cases.perturbed_state(O.qinf(), nrows, seed=1)
@@ -145,33 +164,39 @@ def cpu_sample(steps_budget_s=15.0, threads=1, nx=40, ny=30, nz=30):
     done = 0
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        while time.perf_counter() - t0 < steps_budget_s or done == 0:
+        while time.perf_counter() - t0 < budget_s or done == 0:
             list(ex.map(lambda _: O.full(q0), range(threads)))
             done += threads
     dt = time.perf_counter() - t0
     return {"value": done * m.nedge / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d full residual evaluations of the %dx%dx%d second-order NS box (%d edges) by the "
-                      "oracle, %d thread(s), %.1f s" % (done, nx, ny, nz, m.nedge, threads, dt)}, dt, done
+            "sample": "%d second-order NS residual evaluations (UpdateBCs, LSQ gradient, limiter, Roe + viscous "
+                      "fluxes, norms) of the %dx%dx%d box of the same family (%d edges) by the oracle, %d "
+                      "thread(s) each evaluating its own, %.1f s" % (done, dims[0], dims[1], dims[2], m.nedge,
+                                                                      threads, dt)}, dt, done
 
 
 def run_reference(args, rank, pg):
-    """--impl reference: the reference's CPU path (the oracle port; the
-    reference itself does not build without HDF5/MPI/METIS) on all host
-    threads, rank 0 only."""
+    """--impl reference: the reference's CPU path - the oracle port, which is
+    bit-identical to the reference's own residual on its outputs (the
+    reference itself needs HDF5/MPI/METIS and its source tree, absent on the
+    GPU machine) - on all host threads, rank 0 only, over a bounded sample of the
+    workload; the process loads nothing of the product."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     w = WORKLOADS[args.workload]
-    # warm-up then timed steps; each step = one parallel round over all threads
-    cpu_sample(0.0, threads)
-    base, dt, done = cpu_sample(max(5.0, 2.0 * args.steps), threads)
+    cpu_sample(0.0, threads)  # warm-up: page in, one round per thread
+    base, dt, done = cpu_sample(max(5.0, 1.0 * args.steps), threads)
+    rounds = max(done // threads, 1)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done / threads, 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / rounds,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "ns_flatplate %dx%dx%d (CPU sample 40x30x30)" % (w["nx"], w["ny"], w["nz"]),
-                       "sample_edges": None},
+            "config": {"workload": "ns_flatplate %dx%dx%d (second-order laminar NS residual, Mach 0.8, Re 1e5); "
+                                   "CPU sample: the %dx%dx%d box of the same family" % (
+                                       w["nx"], w["ny"], w["nz"], *CPU_SAMPLE_DIMS)},
             "cpu_baseline": base,
+            "product_library_loaded": product_loaded(),
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -527,32 +552,35 @@ def run_gb300(args, ws, rank, local, pg):
         barrier(pg)
         return max_over_ranks(pg, ms), norms, launches, clk
 
-    # reference precision first, then the double-float kernels; the headline
-    # uses double-float only when its norms agree with FP64 to 1e-10
-    arith_names = {0: "f64", 1: "df64 (FP32 pair, ~48-bit significand)"}
-    results = {}
-    if args.arith != "dfonly":
-        results[0] = timed(0)
-    if args.arith in ("df", "best", "dfonly"):
+    # the headline is the reference's arithmetic, FP64; the double-float
+    # kernels (FP32 pairs on the FP32 pipes, ~48-bit significand) are
+    # reported beside it
+    results = {0: timed(0)}
+    if args.arith != "f64":
         results[1] = timed(1)
-    if 0 not in results:
-        results[0] = results[1]
-    ms64, norms64, launches64, clk64 = results[0]
-    df_ok = 1 in results and abs(results[1][1][0] - norms64[0]) <= 1e-10 * abs(norms64[0])
-    use = 1 if (args.arith in ("df", "dfonly") or (args.arith == "best" and df_ok)) else 0
-    ms, norms, launches, clk = results[use]
-    S.set_residual_arithmetic(use)
+    ms, norms, launches, clk = results[0]
+    S.set_residual_arithmetic(0)
     ms_per_step = ms / args.steps
     value = ws * m.nedge / (ms_per_step * 1e-3) / 1e6
 
-    # per-kernel breakdown (events around each launch on the library's stream)
-    S.profile(True)
-    S.profile_reset()
-    nprof = 3
-    for _ in range(nprof):
-        S.residual_full()
-    timers = S.timers()
-    S.profile(False)
+    def kernel_times(arith, nprof=3):
+        """per-kernel device times (events around each launch on the
+        library's stream) over nprof evaluations in the given arithmetic"""
+        S.set_residual_arithmetic(arith)
+        S.set_state(q0)
+        S.profile(True)
+        S.profile_reset()
+        for _ in range(nprof):
+            S.residual_full()
+        t = S.timers()
+        S.profile(False)
+        tot = sum(v[0] for v in t.values() if v[1]) or 1.0
+        return {k: {"ms_per_step": v[0] / nprof, "launches_per_step": v[1] / nprof, "share": v[0] / tot}
+                for k, v in t.items() if v[1]}
+
+    kernels = kernel_times(0)
+    kernels_df = kernel_times(1) if 1 in results else None
+    S.set_residual_arithmetic(0)
 
     # end to end through the C ABI with host buffers in pinned memory: H2D of
     # q, the step, D2H of b and the norms, every step
@@ -574,55 +602,65 @@ def run_gb300(args, ws, rank, local, pg):
     h2d = qh.nbytes
     d2h = b.nbytes + 6 * 8
 
-    # roofline of the dominant kernel, the inviscid edge-flux kernel
-    # (MUSCL + Roe + clip test): algorithmic bytes per launch = 104 B/edge
-    # (2 int32 ids 8, area vector 32, edge half-vector 24, flux written 40)
-    # + 200 B/node (conservative q 40, the 15 gradient terms of the
-    # conservative variables 120, limiter 40), each array once per launch
-    ef_ms, ef_n = timers.get("edge_flux", (0.0, 0))
-    ef_avg = ef_ms / max(ef_n, 1)
-    alg_bytes = 104.0 * m.nedge + 200.0 * m.nnode
-    achieved = alg_bytes / (ef_avg * 1e-3) / 1e9 if ef_avg > 0 else None
-    # DRAM traffic per launch: one ncu capture of this kernel on the 64x48x48
-    # box (dram__bytes_read.sum + dram__bytes_write.sum = 133.26 MB against
-    # 133.36 MB algorithmic), scaled by the algorithmic bytes of this box -
-    # the traffic grows with the edges and nodes it streams
-    traffic = alg_bytes * (133.26 / 133.36)
+    # roofline of the dominant FP64 kernel.  Algorithmic bytes per launch,
+    # each array once (B/edge, B/node):
+    #   edge_flux   (MUSCL + Roe + clip test): 104 = ids 8, area 32, edge
+    #               half-vector 24, flux written 40; 200 = q 40, the 15
+    #               gradient terms of the conservative variables 120, limiter 40
+    #   edge_viscous: 144 = ids 8, area 32, half-vector 24, flux read and
+    #               written 80; 256 = q 40, gradient 216
+    #   lsq_gradient: 56 = ids 8, LSQ weights of both ends 48; 288 = the 9
+    #               gradient variables 72, gradient written 216
+    #   venkat_limiter: 32 = ids 8, half-vector 24; 208 = q 40, gradient 120,
+    #               volume 8, limiter written 40
+    #   residual_gather: 88 = the edge's flux read at both ends 80, its id in
+    #               the node list 8; 80 = q_old 40, b written 40
+    alg_per = {"edge_flux": (104.0, 200.0), "edge_viscous": (144.0, 256.0), "lsq_gradient": (56.0, 288.0),
+               "venkat_limiter": (32.0, 208.0), "residual_gather": (88.0, 80.0)}
+    top = max((k for k in kernels if k in alg_per), key=lambda k: kernels[k]["ms_per_step"])
+    top_ms = kernels[top]["ms_per_step"] / max(kernels[top]["launches_per_step"], 1.0)
+    alg_bytes = alg_per[top][0] * m.nedge + alg_per[top][1] * m.nnode
+    achieved = alg_bytes / (top_ms * 1e-3) / 1e9 if top_ms > 0 else None
+    # DRAM traffic per launch from one ncu capture of the kernel on a small
+    # box of the family (profiles/), scaled by the algorithmic bytes: the
+    # traffic grows with the edges and nodes streamed
+    traffic_ratio = {"edge_flux": 133.26 / 133.36}
+    traffic = alg_bytes * traffic_ratio[top] if top in traffic_ratio else None
     peak, peak_kind = peaks()
-    tot_prof = sum(v[0] for v in timers.values() if v[1]) or 1.0
-    kernels = {k: {"ms_per_step": v[0] / nprof, "share": v[0] / tot_prof} for k, v in timers.items() if v[1]}
+    # the whole residual against its algorithmic bytes: 40 B/edge + 360 B/node
+    # + 84 B/half-edge (gradients and limiter given)
+    res_bytes = 40.0 * m.nedge + 360.0 * m.nnode + 84.0 * m.nbedge
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": arith_names[use], "data": "synthetic",
+        "dtype": "f64", "data": "synthetic",
         "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+Venkat "
                                "limiter K=5+Roe+viscous), Mach 0.8, Re 1e5" % (w["nx"], w["ny"], w["nz"]),
                    "nodes": m.nnode, "edges": m.nedge, "half_edges": m.nbedge,
                    "l2": "inputs larger than L2 (edge arrays alone %.0f MB)" % (m.nedge * 104 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU", "mesh_build_s": round(t_mesh, 2)},
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "mesh_build_s": round(t_mesh, 2),
+                   "limiter_K": case.param.venkat_K},
         "resGlobal": float(norms[0]),
-        "arithmetic": {"used": arith_names[use],
-                       "f64": ({"value": ws * m.nedge / (ms64 / args.steps * 1e-3) / 1e6,
-                                "ms_per_step": ms64 / args.steps, "resGlobal": float(norms64[0])}
-                               if args.arith != "dfonly" else None),
-                       "df64": ({"value": ws * m.nedge / (results[1][0] / args.steps * 1e-3) / 1e6,
-                                 "ms_per_step": results[1][0] / args.steps, "resGlobal": float(results[1][1][0]),
-                                 "resGlobal_rel_diff_vs_f64": abs(results[1][1][0] - norms64[0]) / abs(norms64[0])}
-                                if 1 in results else None)},
+        "residual_hbm_frac": res_bytes / (ms_per_step * 1e-3) / 1e9 / peak,
+        "df64": ({"what": "the same residual in double-float arithmetic (FP32 pairs, ~48-bit significand)",
+                  "value": ws * m.nedge / (results[1][0] / args.steps * 1e-3) / 1e6,
+                  "ms_per_step": results[1][0] / args.steps, "resGlobal": float(results[1][1][0]),
+                  "resGlobal_rel_diff_vs_f64": abs(results[1][1][0] - norms[0]) / abs(norms[0]),
+                  "kernels": kernels_df} if 1 in results else None),
         "gpu_launches": int(launches),
         "kernels": kernels,
-        "roofline": {"bound": "hbm", "kernel": "edge_flux", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "note": "FP32-issue bound (double-float Roe flux; FP64-pipe bound in FP64 arithmetic); "
-                             "HBM fraction of the measured copy peak"},
+                     "note": "HBM fraction of the measured copy peak; the FP64 kernels are bound by the FP64 pipe "
+                             "(2 FP64 fused multiply-adds per clock per SM on GB300), not by HBM"},
         "clocks": clk.summary(),
         "e2e": {"value": ws * m.nedge / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        base, _, _ = cpu_sample(12.0, 1)
+        base, _, _ = cpu_sample(12.0, os.cpu_count() or 1)
         line["cpu_baseline"] = base
     # the FP32 block SpMV of the mixed solver on this machine's matrix: one mixed
     # Newton step assembles it (FP32 storage), then K device-timed products
@@ -653,10 +691,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ns128", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ns256", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--arith", default="best", choices=["f64", "df", "best", "dfonly"],
-                    help="residual arithmetic: FP64, double-float, or double-float when it agrees with FP64")
+    ap.add_argument("--arith", default="both", choices=["f64", "both"],
+                    help="time the FP64 residual only, or the double-float one beside it")
     ap.add_argument("--converge", default="fp64,mixed,mixed_learned",
                     help="comma-separated arms of the time-to-1e-10 study on one GPU ('' to skip)")
     ap.add_argument("--converge-workload", default="ns64", choices=sorted(WORKLOADS))

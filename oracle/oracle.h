@@ -47,6 +47,15 @@ void oracle_sgs_colored(int nnode, const int* ia, const int* ja, const double* M
                         double* x, int nsweeps, int ncolor, const int* cptr, const int* rows);
 double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* x, double* q);
 
+/* mesh generator and preprocessing (mesh.c) */
+typedef struct oracle_mesh_s oracle_mesh;
+oracle_mesh* oracle_mesh_box(const pcfd_box_params* p);
+oracle_mesh* oracle_mesh_elements(int nnode, const double* xyz, int ntri, const int* tri, const int* tri_tag, int ntet,
+                                  const int* tet);
+int oracle_mesh_build(oracle_mesh* m);
+int oracle_mesh_view(const oracle_mesh* m, pcfd_mesh_view* v);
+void oracle_mesh_free(oracle_mesh* m);
+
 /* learned preconditioner network (learned.c) */
 double oracle_bf16(double v);
 int oracle_lp_nparam(void);

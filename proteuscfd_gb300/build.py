@@ -90,7 +90,7 @@ def build_library(verbose: bool = False) -> Path:
 
 def build_oracle(verbose: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure)."""
-    csrcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "learned.c", ORACLE_DIR / "chem.c"]
+    csrcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "learned.c", ORACLE_DIR / "chem.c", ORACLE_DIR / "mesh.c"]
     srcs = csrcs + [ORACLE_DIR / "oracle.h", ROOT / "include" / "pcfd.h"]
     if _stale(ORACLE_LIB, srcs + [Path(__file__)]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")

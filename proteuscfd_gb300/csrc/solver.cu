@@ -730,6 +730,34 @@ __global__ void __launch_bounds__(128) k_gradient(int nnode, const int* __restri
 // the edge's right end).  Writes the raw value, the clamped value (lim may
 // be null) and the clip flag.  CHI0: chi = 0, so the extrapolation is
 // q + grad.dx exactly and the 0.5 chi dQ term is skipped (bit-identical).
+// a fused multiply-add for the FP64 path of the limiter (the double-float
+// path never reaches it)
+template <class S>
+__device__ __forceinline__ S fma_s(S a, S b, S c) { return a * b + c; }
+template <>
+__device__ __forceinline__ double fma_s<double>(double a, double b, double c) { return fma(a, b, c); }
+
+// Neighbour bounds (Kernel_FindMinMax: qmax = v unless qmax > v, qmin = v
+// unless qmin < v).  In FP64 the comparisons run on the integer pipes, on
+// keys that order doubles as their values (sign bit flips the magnitude),
+// so the FP64 pipe the limiter is bound by does not spend two comparisons
+// per neighbour and equation on them; the double-float path compares values.
+__device__ __forceinline__ long long dkey(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+template <class S>
+__device__ __forceinline__ void bound_upd(S v, S& mn, S& mx, long long&, long long&) {
+  mx = (mx > v) ? mx : v;
+  mn = (mn < v) ? mn : v;
+}
+template <>
+__device__ __forceinline__ void bound_upd<double>(double v, double& mn, double& mx, long long& kmn, long long& kmx) {
+  const long long kv = dkey(v);
+  if (!(kmx > kv)) { kmx = kv; mx = v; }
+  if (!(kmn < kv)) { kmn = kv; mn = v; }
+}
+
 template <class S, int LIM, bool CHI0>
 __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __restrict__ nedg,
                                            const int* __restrict__ nnbr, const S* __restrict__ q,
@@ -784,16 +812,20 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
   // division per equation remains instead of one per edge and equation.
   // DP takes one of two values per equation (qmax - q or qmin - q, by the
   // sign of DM); both and their squares are formed once, outside the
-  // neighbour loop.  FP64 keeps the reference's expression order
-  // (ucs/limiters.tcc:617); double-float forms DM as the extrapolation's
-  // correction itself and adds eps^2 to DP^2 first.
+  // neighbour loop together with DP^2 + eps^2.  FP64 forms DM as the
+  // reference does (extrapolated value minus node value, in its rounding,
+  // since the sign of DM picks DP) and then num = DP^2 + eps^2 + 2 DM DP and
+  // den = DP^2 + eps^2 + DM (DP + 2 DM) with fused multiply-adds: three FP64
+  // instructions where the reference's expression order takes eight (the
+  // FP64 pipe bounds this kernel); double-float forms DM as the
+  // extrapolation's correction itself.
   constexpr bool F64 = std::is_same<S, double>::value;
   S dpp[NEQN], dpm[NEQN], bp[NEQN], bm[NEQN], bn[NEQN], bd[NEQN];
   for (int t = 0; t < NEQN; t++) {
     dpp[t] = qmax[t] - qi[t];
     dpm[t] = qmin[t] - qi[t];
-    bp[t] = F64 ? dpp[t] * dpp[t] : dpp[t] * dpp[t] + ep2;
-    bm[t] = F64 ? dpm[t] * dpm[t] : dpm[t] * dpm[t] + ep2;
+    bp[t] = dpp[t] * dpp[t] + ep2;
+    bm[t] = dpm[t] * dpm[t] + ep2;
     bn[t] = one;
     bd[t] = one;
   }
@@ -813,10 +845,9 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
         S DM = Q - qi[t];
         bool pos = Q > qi[t];
         S DP = pos ? dpp[t] : dpm[t];
-        S P2 = pos ? bp[t] : bm[t];
-        S mp = DM * DP;
-        num = P2 + ep2 + twice(mp);
-        den = P2 + twice(DM * DM) + mp + ep2;
+        S C1 = pos ? bp[t] : bm[t];
+        num = fma_s(DM, DP + DP, C1);
+        den = fma_s(DM, fma_s(Sc<S>::c(2.0), DM, DP), C1);
       } else {
         S DM = corr;
         bool pos = DM > zero;
@@ -861,13 +892,11 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
   }
   for (int t = 0; t < NEQN * 3; t++) gi[t] = grad[(size_t)i * NTERMS * 3 + t];
   const int k0 = nptr[i], k1 = nptr[i + 1];
+  long long kmn[NEQN], kmx[NEQN];
+  for (int t = 0; t < NEQN; t++) kmn[t] = kmx[t] = 0;  // the key of +0.0, the bounds' start
   for (int k = k0; k < k1; k++) {
     const S* qj = &q[(size_t)nnbr[k] * NVARS];
-    for (int t = 0; t < NEQN; t++) {
-      S v = qj[t];
-      qmax[t] = (qmax[t] > v) ? qmax[t] : v;
-      qmin[t] = (qmin[t] < v) ? qmin[t] : v;
-    }
+    for (int t = 0; t < NEQN; t++) bound_upd<S>(qj[t], qmin[t], qmax[t], kmn[t], kmx[t]);
   }
   limit_node<S, LIM, CHI0>(i, k0, k1, nedg, nnbr, q, eh, vol, chi_d, K3, qi, gi, qmin, qmax, limraw, lim, clipflag);
 }

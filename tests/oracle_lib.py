@@ -68,6 +68,11 @@ def lib():
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
+            "oracle_mesh_box": (C.c_void_p, [C.POINTER(N.BoxParams)]),
+            "oracle_mesh_elements": (C.c_void_p, [C.c_int, _DP, C.c_int, _IP, _IP, C.c_int, _IP]),
+            "oracle_mesh_build": (C.c_int, [C.c_void_p]),
+            "oracle_mesh_view": (C.c_int, [C.c_void_p, MV]),
+            "oracle_mesh_free": (None, [C.c_void_p]),
             "oracle_lp_nparam": (C.c_int, []),
             "oracle_lp_graph": (None, [MV, _IP, _IP, _FP]),
             "oracle_lp_features": (C.c_double, [C.c_int, _DP, _DP, _DP, _DP, C.c_double, _FP]),
@@ -95,6 +100,64 @@ def ip(a):
 def fp(a):
     assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(_FP)
+
+
+class OracleMesh:
+    """A mesh generated and preprocessed by the oracle alone (oracle/mesh.c),
+    with the attributes the oracle's solution spaces read from a mesh."""
+
+    def __init__(self, handle):
+        self.L = lib()
+        if not handle:
+            raise RuntimeError("oracle mesh: bad input")
+        self._h = handle
+        rc = self.L.oracle_mesh_build(self._h)
+        if rc != 0:
+            self.L.oracle_mesh_free(self._h)
+            self._h = None
+            raise RuntimeError("oracle_mesh_build failed (%d)" % rc)
+        from proteuscfd_gb300 import _native as N
+        self.view = N.MeshView()
+        assert self.L.oracle_mesh_view(self._h, C.byref(self.view)) == 0
+
+    @classmethod
+    def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5, y_ratio=1.0,
+            tags=(1, 2, 3, 4, 5, 6)):
+        from proteuscfd_gb300 import _native as N
+        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags))
+        return cls(lib().oracle_mesh_box(C.byref(p)))
+
+    @classmethod
+    def from_elements(cls, xyz, tris, tri_tags, tets):
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        tris = np.ascontiguousarray(tris, np.int32)
+        tri_tags = np.ascontiguousarray(tri_tags, np.int32)
+        tets = np.ascontiguousarray(tets, np.int32)
+        return cls(lib().oracle_mesh_elements(len(xyz), dp(xyz), len(tris), ip(tris), ip(tri_tags), len(tets),
+                                              ip(tets)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self.L.oracle_mesh_free(self._h)
+            self._h = None
+
+    def _a(self, ptr, n, dtype, cols=1):
+        a = np.ctypeslib.as_array(ptr, shape=(n * cols,)).view(dtype)
+        return a.reshape(-1, cols) if cols > 1 else a
+
+    nnode = property(lambda self: self.view.nnode)
+    nedge = property(lambda self: self.view.nedge)
+    nbedge = property(lambda self: self.view.nbedge)
+    edges = property(lambda self: self._a(self.view.edges, self.nedge, np.int32, 2))
+    edge_area = property(lambda self: self._a(self.view.edge_area, self.nedge, np.float64, 4))
+    bedges = property(lambda self: self._a(self.view.bedges, self.nbedge, np.int32, 2))
+    bedge_area = property(lambda self: self._a(self.view.bedge_area, self.nbedge, np.float64, 4))
+    bfactag = property(lambda self: self._a(self.view.bfactag, self.nbedge, np.int32))
+    xyz = property(lambda self: self._a(self.view.xyz, self.nnode, np.float64, 3))
+    vol = property(lambda self: self._a(self.view.vol, self.nnode, np.float64))
+    sw = property(lambda self: self._a(self.view.sw, self.nnode, np.float64, 6))
+    ipsp = property(lambda self: self._a(self.view.ipsp, self.nnode + 1, np.int32))
+    psp = property(lambda self: self._a(self.view.psp, int(self.ipsp[-1]), np.int32))
 
 
 class OracleNet:
