@@ -67,6 +67,8 @@ typedef struct pcfd_box_params {
   double ramp_x0;
   double y_ratio;     /* geometric clustering ratio toward y=0 (<= 1: uniform) */
   int tags[6];
+  int jitter_mode;    /* 0: each axis by its own local spacing; 1: every axis by the node's
+                       * smallest local spacing (keeps stretched near-wall cells valid) */
 } pcfd_box_params;
 
 typedef void* pcfd_mesh_t;
@@ -195,6 +197,14 @@ PCFD_API int pcfd_set_limiter(pcfd_solver_t s, const double* l);
 /* ComputeResiduals (ucs/residual.tcc:13): b (= -R) into b_out [nnode][5]
  * (optional) and norms_out[0..5] = {resGlobal, per-equation norms}. */
 PCFD_API int pcfd_residual(pcfd_solver_t s, double* b_out, double* norms_out);
+/* Forces::ComputeYpCf -> FORCE_Kernel (ucs/forces.tcc:124-197,376-408) on the
+ * body made of the given boundary tags (a composite body of the .bc file):
+ * out6[0..2] pressure force sum p |a| n, out6[3..5] viscous force on its
+ * no-slip half-edges (the stress of ComputeStressVector, ucs/compressible.tcc:
+ * 1113, which reads the gradients of the momentum components).  Uses the
+ * current state and the last FP64 gradient (computed here first when there is
+ * none).  Summed in a fixed order; moments are not formed. */
+PCFD_API int pcfd_forces(pcfd_solver_t s, const int* tags, int ntags, double* out6);
 /* b (= -R) of the last residual evaluation, [nnode][5], without recomputing. */
 PCFD_API int pcfd_get_residual(pcfd_solver_t s, double* b_out);
 /* UpdateBCs + gradient + limiter + residual in one call, the sequence

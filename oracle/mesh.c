@@ -166,9 +166,11 @@ oracle_mesh* oracle_mesh_box(const pcfd_box_params* p) {
         double x = cx[i], y = cy[j], z = cz[k];
         int interior = i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1;
         if (interior && p->jitter > 0.0) {
-          x += p->jitter * LH(cx, nx, i) * sm_sym(&rng);
-          y += p->jitter * LH(cy, ny, j) * sm_sym(&rng);
-          z += p->jitter * LH(cz, nz, k) * sm_sym(&rng);
+          double hx = LH(cx, nx, i), hy = LH(cy, ny, j), hz = LH(cz, nz, k);
+          if (p->jitter_mode == 1) hx = hy = hz = fmin(hx, fmin(hy, hz));
+          x += p->jitter * hx * sm_sym(&rng);
+          y += p->jitter * hy * sm_sym(&rng);
+          z += p->jitter * hz * sm_sym(&rng);
         }
         if (p->ramp_deg != 0.0 && x > p->ramp_x0) y = y + tanr * (x - p->ramp_x0) * (p->ly - y) / p->ly;
         size_t n = (size_t)i + (size_t)nx * (j + (size_t)ny * k);

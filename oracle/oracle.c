@@ -1315,3 +1315,44 @@ double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* 
   for (size_t k = 0; k < (size_t)nn * NEQN; k++) t += x[k] * x[k];
   return sqrt(t) / (double)((size_t)nn * NEQN);
 }
+
+/* Forces::ComputeYpCf -> FORCE_Kernel (ucs/forces.tcc:124-197, :376-408):
+ * over the boundary half-edges in order, those whose tag belongs to the body
+ * (in_body[factag] != 0) add p |a| n to the pressure force and, on no-slip
+ * walls of a viscous run, the wall stress |a| to the viscous force.
+ * ComputeStressVector (ucs/compressible.tcc:1113) reads the stress from
+ * gradient entries 3..11, the gradients of the momentum components (the
+ * velocity gradients sit at 18..26); this restates it as written.
+ * out[0..2] pressure force, out[3..5] viscous force. */
+void oracle_forces(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
+                   const int* in_body, double* out) {
+  for (int j = 0; j < 6; j++) out[j] = 0.0;
+  const double Sconst = 110.4 / prm->ref_temperature;
+  const double retilde = prm->Re / prm->mach;
+  for (int eid = 0; eid < m->nbedge; eid++) {
+    const int tag = m->bfactag[eid];
+    if (tag < 0 || tag >= prm->ntags || !in_body[tag]) continue;
+    const int a = m->bedges[2 * eid];
+    const double* avec = &m->bedge_area[4 * eid];
+    const double* Q = &q[(size_t)a * NVARS];
+    const double p = Q[6];
+    for (int j = 0; j < 3; j++) out[j] += p * avec[j] * avec[3];
+    if (prm->bc_type[tag] == PCFD_BC_NOSLIP && prm->viscous) {
+      const double T = Q[5];
+      const double mu = (1.0 + Sconst) * pow(T, 1.5) / (T + Sconst);
+      const double* g = &grad[(size_t)a * NTERMS * 3];
+      const double ux = g[3], uy = g[4], uz = g[5], vx = g[6], vy = g[7], vz = g[8], wx = g[9], wy = g[10],
+                   wz = g[11];
+      const double div = -2.0 / 3.0 * (ux + vy + wz);
+      const double txx = 2.0 * ux + div, tyy = 2.0 * vy + div, tzz = 2.0 * wz + div;
+      const double txy = uy + vx, txz = uz + wx, tyz = vz + wy;
+      const double txn = txx * avec[0] + txy * avec[1] + txz * avec[2];
+      const double tyn = txy * avec[0] + tyy * avec[1] + tyz * avec[2];
+      const double tzn = txz * avec[0] + tyz * avec[1] + tzz * avec[2];
+      const double s0 = -(mu / retilde) * txn, s1 = -(mu / retilde) * tyn, s2 = -(mu / retilde) * tzn;
+      out[3] += s0 * avec[3];
+      out[4] += s1 * avec[3];
+      out[5] += s2 * avec[3];
+    }
+  }
+}

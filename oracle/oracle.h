@@ -47,6 +47,9 @@ void oracle_sgs_colored(int nnode, const int* ia, const int* ja, const double* M
                         double* x, int nsweeps, int ncolor, const int* cptr, const int* rows);
 double oracle_apply_dq(const pcfd_mesh_view* m, const pcfd_params* prm, double* x, double* q);
 
+void oracle_forces(const pcfd_mesh_view* m, const pcfd_params* prm, const double* q, const double* grad,
+                   const int* in_body, double* out);
+
 /* mesh generator and preprocessing (mesh.c) */
 typedef struct oracle_mesh_s oracle_mesh;
 oracle_mesh* oracle_mesh_box(const pcfd_box_params* p);

@@ -164,6 +164,20 @@ std::vector<Real> newton_stages(SolutionSpace<Real>* space, const std::string& p
   return norms;
 }
 
+// The pressure and viscous force on composite body 1 as PostTimeAdvance's
+// Forces::Compute left them (FORCE_Kernel, ucs/forces.tcc:124), when the
+// case defines a body.
+void dump_forces(SolutionSpace<Real>* space, const std::string& pre) {
+  Forces<Real>* f = space->forces;
+  if (!f || f->num_bodies < 1) return;
+  double v[6];
+  for (int j = 0; j < 3; ++j) {
+    v[j] = real(f->bodies[1].forces[j]);
+    v[3 + j] = real(f->bodies[1].vforces[j]);
+  }
+  dump(pre + "forces", v, 1, 6);
+}
+
 }  // namespace
 
 int main(int argc, char* argv[]) {
@@ -312,6 +326,7 @@ int main(int argc, char* argv[]) {
 
   std::vector<Real> norms = newton_stages(space, "s1_");
   space->PostTimeAdvance();
+  dump_forces(space, "s1_");
   // the second step is the first with second-order fluxes and a limiter
   // (NewtonIterate tests iter > nFirstOrderSteps; iter starts at 0)
   if (nsteps >= 2) {
@@ -320,6 +335,7 @@ int main(int argc, char* argv[]) {
     if (A) dump("s2_jacobian", A->M, A->nblocks, (long long)neqn * neqn);
     std::vector<Real> n2 = newton_stages(space, "s2_");
     space->PostTimeAdvance();
+    dump_forces(space, "s2_");
   }
 
   // 4. whole steps

@@ -44,7 +44,7 @@ class BoxParams(C.Structure):
         ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
         ("jitter", C.c_double), ("seed", C.c_uint64),
         ("ramp_deg", C.c_double), ("ramp_x0", C.c_double), ("y_ratio", C.c_double),
-        ("tags", C.c_int * 6),
+        ("tags", C.c_int * 6), ("jitter_mode", C.c_int),
     ]
 
 
@@ -141,6 +141,7 @@ PROTOTYPES = {
     "pcfd_destroy": (C.c_int, [_P]),
     "pcfd_set_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
     "pcfd_set_qold": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
+    "pcfd_forces": (C.c_int, [_P, _IP, C.c_int, _DP]),
     "pcfd_get_state": (C.c_int, [_P, _DP, C.c_int, C.c_int]),
     "pcfd_get_qinf": (C.c_int, [_P, _DP]),
     "pcfd_update_bcs": (C.c_int, [_P]),

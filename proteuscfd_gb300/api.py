@@ -74,8 +74,9 @@ class Mesh:
 
     @classmethod
     def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5,
-            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6), reorder=False):
-        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags))
+            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6), reorder=False, jitter_mode=0):
+        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags),
+                        jitter_mode)
         return cls(N.load().pcfd_mesh_box_create(C.byref(p)), reorder, nx * ny * nz)
 
     @classmethod
@@ -251,6 +252,14 @@ class SolutionSpace:
         q = np.ascontiguousarray(q, dtype=np.float64)
         q2 = q.reshape(q.shape[0], -1)
         N.check(self._lib.pcfd_set_qold(self._h, N.dptr(q2), q2.shape[1], q2.shape[0]), "pcfd_set_qold")
+
+    def forces(self, tags):
+        """(pressure force, viscous force) on the body made of the given
+        boundary tags (Forces::Compute's FORCE_Kernel)."""
+        t = np.ascontiguousarray(list(tags), dtype=np.int32)
+        out = np.empty(6, dtype=np.float64)
+        N.check(self._lib.pcfd_forces(self._h, N.iptr(t), len(t), N.dptr(out)), "pcfd_forces")
+        return out[:3], out[3:]
 
     def get_state(self):
         q = np.empty((self.nrows, NVARS), dtype=np.float64)

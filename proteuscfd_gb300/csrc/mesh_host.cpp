@@ -542,9 +542,11 @@ PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p) {
         double x = cx[i], y = cy[j], z = cz[k];
         bool interior = i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1;
         if (interior && p->jitter > 0.0) {
-          x += p->jitter * local_h(cx, i) * rng.sym();
-          y += p->jitter * local_h(cy, j) * rng.sym();
-          z += p->jitter * local_h(cz, k) * rng.sym();
+          double hx = local_h(cx, i), hy = local_h(cy, j), hz = local_h(cz, k);
+          if (p->jitter_mode == 1) hx = hy = hz = std::min(hx, std::min(hy, hz));
+          x += p->jitter * hx * rng.sym();
+          y += p->jitter * hy * rng.sym();
+          z += p->jitter * hz * rng.sym();
         }
         if (p->ramp_deg != 0.0 && x > p->ramp_x0) {
           // shear y so the bottom wall ramps up by ramp_deg and the top stays flat

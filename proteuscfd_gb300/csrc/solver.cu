@@ -111,6 +111,7 @@ struct Solver {
   D4* d_ba = nullptr;      // [nbedge]
   int* d_bbc = nullptr;         // [nbedge] bc type
   double* d_btw = nullptr;      // [nbedge] non-dimensional wall temperature
+  int* d_bfactag = nullptr;     // [nbedge] boundary tag
   int* d_bnrm = nullptr;        // [nbedge] no-slip normal node (or -1)
   double* d_xyz = nullptr;      // [nnode][3]
   double* d_vol = nullptr;      // [nnode]
@@ -1353,7 +1354,7 @@ void free_learned(Learned* lp);
 void free_solver(Solver* s) {
   if (!s) return;
   free_learned(s->lp);
-  void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, s->d_xyz,
+  void* ptrs[] = {s->d_en, s->d_ea, s->d_eh, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bfactag, s->d_bnrm, s->d_xyz,
                   s->d_vol, s->d_nptr, s->d_nedg, s->d_nnbr, s->d_lsq, s->d_bptr, s->d_bhe, s->d_bgnode,
                   s->d_bgptr, s->d_bghe, s->d_bgslot, s->d_bgqr, s->d_q, s->d_grad, s->d_lim, s->d_b, s->d_qold, s->d_qpre, s->d_ef, s->d_bf, s->d_part,
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
@@ -2808,6 +2809,7 @@ PCFD_API int pcfd_create(const pcfd_mesh_view* m, const pcfd_params* prm, pcfd_s
   TRY(dput(&s->d_ba, ba.data(), nb));
   TRY(dput(&s->d_bbc, bbc.data(), nb));
   TRY(dput(&s->d_btw, btw.data(), nb));
+  TRY(dput(&s->d_bfactag, m->bfactag, nb));
   TRY(dput(&s->d_bnrm, bnrm.data(), nb));
   TRY(dput(&s->d_xyz, m->xyz, 3 * nn));
   TRY(dput(&s->d_vol, m->vol, nn));
@@ -3046,6 +3048,95 @@ PCFD_API int pcfd_gradient(pcfd_solver_t h, double* qgrad_out) {
                              cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   return PCFD_OK;
+}
+
+// FORCE_Kernel (ucs/forces.tcc:124-197) over the boundary half-edges: a
+// half-edge whose tag belongs to the body adds p |a| n to the pressure force
+// and, on a no-slip wall of a viscous run, the wall stress times |a| to the
+// viscous force.  The stress is ComputeStressVector's
+// (ucs/compressible.tcc:1113), which reads gradient entries 3..11 (those of
+// the momentum components); Sutherland's law as in the viscous flux.
+// Per-block sums in a fixed order, then one warp per component.
+__global__ void __launch_bounds__(kNormThreads) k_forces(int nbedge, const int2* __restrict__ bn,
+                                                         const D4* __restrict__ ba, const int* __restrict__ bfactag,
+                                                         const int* __restrict__ bbc, const int* __restrict__ in_body,
+                                                         const double* __restrict__ q, const double* __restrict__ grad,
+                                                         int viscous, double Sconst, double inv_retilde,
+                                                         double* __restrict__ part) {
+  __shared__ double red[kNormThreads / 32][6];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int he = blockIdx.x * blockDim.x + threadIdx.x; he < nbedge; he += gridDim.x * blockDim.x) {
+    if (!in_body[bfactag[he]]) continue;
+    const int a = bn[he].x;
+    const D4 av = ba[he];
+    const double* Q = &q[(size_t)a * NVARS];
+    const double p = Q[6];
+    acc[0] += p * av.x * av.w;
+    acc[1] += p * av.y * av.w;
+    acc[2] += p * av.z * av.w;
+    if (viscous && bbc[he] == PCFD_BC_NOSLIP) {
+      const double T = Q[5];
+      const double mu = sutherland(T, Sconst);
+      const double* g = &grad[(size_t)a * NTERMS * 3];
+      const double ux = g[3], uy = g[4], uz = g[5], vx = g[6], vy = g[7], vz = g[8], wx = g[9], wy = g[10],
+                   wz = g[11];
+      const double div = -2.0 / 3.0 * (ux + vy + wz);
+      const double txx = 2.0 * ux + div, tyy = 2.0 * vy + div, tzz = 2.0 * wz + div;
+      const double txy = uy + vx, txz = uz + wx, tyz = vz + wy;
+      const double c = -(mu * inv_retilde) * av.w;
+      acc[3] += c * (txx * av.x + txy * av.y + txz * av.z);
+      acc[4] += c * (txy * av.x + tyy * av.y + tyz * av.z);
+      acc[5] += c * (txz * av.x + tyz * av.y + tzz * av.z);
+    }
+  }
+  for (int c = 0; c < 6; c++) {
+    double v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int w = 0; w < kNormThreads / 32; w++) v += red[w][threadIdx.x];
+    part[(size_t)blockIdx.x * 6 + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_forces_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  if (c >= 6) return;
+  const double v = warp_col_sum(part, nblocks, 6, c, lane);
+  if (lane == 0) out[c] = v;
+}
+
+PCFD_API int pcfd_forces(pcfd_solver_t h, const int* tags, int ntags, double* out6) {
+  Solver* s = (Solver*)h;
+  if (!s || !tags || ntags <= 0 || !out6) return set_err(PCFD_ERR_ARG, "pcfd_forces: bad arguments");
+  std::vector<int> mask(s->prm.ntags, 0);
+  for (int i = 0; i < ntags; i++) {
+    if (tags[i] < 0 || tags[i] >= s->prm.ntags) return set_err(PCFD_ERR_ARG, "pcfd_forces: tag without a BC");
+    mask[tags[i]] = 1;
+  }
+  int rc;
+  if (s->prm.viscous && (!s->have_grad || s->grad_arith != 0) && (rc = run_gradient(s, 0))) return rc;
+  int* d_mask = nullptr;
+  double* d_out = nullptr;
+  if ((rc = dput(&d_mask, mask.data(), mask.size()))) return rc;
+  if ((rc = dalloc(&d_out, 6))) { cudaFree(d_mask); return rc; }
+  const double Sconst = 110.4 / s->prm.ref_temperature;
+  const double inv_retilde = s->prm.Re != 0.0 ? s->prm.mach / s->prm.Re : 0.0;
+  rc = launch(s, T_SETUP, [&] {
+    k_forces<<<kNormBlocks, kNormThreads, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bfactag, s->d_bbc, d_mask,
+                                                          s->d_q, s->d_grad, s->prm.viscous, Sconst, inv_retilde,
+                                                          s->d_part);
+  });
+  if (!rc) rc = launch(s, T_SETUP, [&] { k_forces_final<<<1, 192, 0, s->stream>>>(kNormBlocks, s->d_part, d_out); });
+  if (!rc && cudaMemcpyAsync(out6, d_out, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+    rc = set_err(PCFD_ERR_CUDA, "pcfd_forces: copy");
+  if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = set_err(PCFD_ERR_CUDA, "pcfd_forces: sync");
+  cudaFree(d_mask);
+  cudaFree(d_out);
+  return rc;
 }
 
 PCFD_API int pcfd_limiter(pcfd_solver_t h, double* l_out) {

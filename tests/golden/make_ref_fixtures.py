@@ -191,6 +191,10 @@ def write_bc(path, c):
         if tag in c.get("twall", {}):
             extra = " twall = [%r]" % c["twall"][tag]
         lines.append('surface #%d = %s "face%d"%s' % (tag, kind, tag, extra))
+    # the no-slip walls as composite body 1, whose forces the reference reports
+    walls = [t for t, k in sorted(c["bc"].items()) if k == "noSlip"]
+    if walls:
+        lines.append("body #1 = [%s]" % ", ".join(str(t) for t in walls))
     Path(path).write_text("\n".join(lines) + "\n")
 
 

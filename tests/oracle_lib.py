@@ -68,6 +68,7 @@ def lib():
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
+            "oracle_forces": (None, [MV, PP, _DP, _DP, _IP, _DP]),
             "oracle_mesh_box": (C.c_void_p, [C.POINTER(N.BoxParams)]),
             "oracle_mesh_elements": (C.c_void_p, [C.c_int, _DP, C.c_int, _IP, _IP, C.c_int, _IP]),
             "oracle_mesh_build": (C.c_int, [C.c_void_p]),
@@ -122,9 +123,10 @@ class OracleMesh:
 
     @classmethod
     def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5, y_ratio=1.0,
-            tags=(1, 2, 3, 4, 5, 6)):
+            tags=(1, 2, 3, 4, 5, 6), jitter_mode=0):
         from proteuscfd_gb300 import _native as N
-        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags))
+        p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags),
+                        jitter_mode)
         return cls(lib().oracle_mesh_box(C.byref(p)))
 
     @classmethod
@@ -264,6 +266,17 @@ class OracleSpace:
                                            dp(babs), dp(norms), C.byref(kc)) == 0
         self.last_babs = babs
         return b, norms, kc.value
+
+    def forces(self, q, g, tags):
+        """FORCE_Kernel over the half-edges with the given tags: (pressure
+        force, viscous force)."""
+        mask = np.zeros(self.cp.ntags, np.int32)
+        mask[list(tags)] = 1
+        out = np.zeros(6)
+        g = np.zeros((self.mesh.nnode, 27)) if g is None else np.ascontiguousarray(g, np.float64)
+        self.L.oracle_forces(C.byref(self.mesh.view), C.byref(self.cp), dp(np.ascontiguousarray(q, np.float64)),
+                             dp(g), ip(mask), dp(out))
+        return out[:3], out[3:]
 
     def full(self, q):
         """UpdateBCs, gradient, limiter, residual - the NewtonIterate order;

@@ -134,3 +134,18 @@ def test_apply_dq_matches_reference(case):
     S.set_state(f["s1_q_bc"])
     S.apply_dq(f["s1_x_sgs"])
     close(S.get_state()[:n], f["s1_q"], 1e-13, "state after ApplyDQ")
+
+
+@pytest.mark.parametrize("case", [c for c in R.CASES if "s1_forces" in R.load(c)])
+def test_forces_match_oracle(case):
+    """pcfd_forces against the oracle's FORCE_Kernel (itself bit-identical to
+    the reference's reported forces) on the reference's state and gradient."""
+    f, m, p, S = space(case)
+    walls = [int(t) for t, k in f["case_bc_types"] if k == 4]
+    S.set_state(f["s1_q_bc"])
+    g = S.gradient()
+    fp, fv = S.forces(walls)
+    O = OracleImplicit(m, p)
+    op, ov = O.forces(f["s1_q_bc"], g, walls)
+    np.testing.assert_allclose(fp, op, rtol=1e-13, atol=1e-16 * np.abs(op).max())
+    np.testing.assert_allclose(fv, ov, rtol=1e-12, atol=1e-12 * np.abs(ov).max())

@@ -31,6 +31,7 @@ def test_oracle_preprocessing_matches_reference(case):
 
 
 @pytest.mark.parametrize("kw", [dict(nx=9, ny=7, nz=6, lx=1.3, jitter=0.2, seed=4, y_ratio=1.1),
+                                dict(nx=9, ny=8, nz=5, lx=1.1, jitter=0.2, seed=5, y_ratio=1.2, jitter_mode=1),
                                 dict(nx=10, ny=6, nz=5, lx=2.0, jitter=0.2, seed=9, ramp_deg=15.0, ramp_x0=0.5)])
 def test_oracle_box_matches_product_box(kw):
     o = OracleMesh.box(**kw)

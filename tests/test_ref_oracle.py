@@ -86,3 +86,18 @@ def test_oracle_newton_iterates_match_reference(case):
     np.testing.assert_array_equal(q[:n], ref_final)
     ref_hist = [R.scalar(f, "s1_norms"), f["s2_norms"].ravel()[0]] + list(f.get("resglobal_steps3on", []))
     assert hist == ref_hist[:len(hist)]
+
+
+@pytest.mark.parametrize("case", [c for c in R.CASES if "s1_forces" in R.load(c)])
+def test_oracle_forces_match_reference(case):
+    """The body forces Forces::Compute reports after each step (FORCE_Kernel
+    on the no-slip wall: pressure and viscous parts), bit for bit."""
+    f = R.load(case)
+    m = R.mesh(f)
+    O = OracleImplicit(m, R.param(f))
+    n = m.nnode
+    walls = [int(t) for t, k in f["case_bc_types"] if k == 4]
+    for st in ("s1_", "s2_"):
+        q = np.concatenate([f[st + "q"], f[st + "q_bc"][n:]])
+        fp, fv = O.forces(q, f[st + "qgrad"], walls)
+        np.testing.assert_array_equal(np.r_[fp, fv], f[st + "forces"].ravel())
