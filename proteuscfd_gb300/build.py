@@ -26,7 +26,8 @@ ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_DIR = ORACLE_DIR / "_ref"
 REF_LIB = REF_DIR / "libref_pin.so"
-REFERENCE_SRC = Path(os.environ.get("PCFD_REFERENCE_SRC", "/root/reference"))
+# The reference checkout, for the optional reference-side build below; unset: skipped.
+REFERENCE_SRC = Path(os.environ["PCFD_REFERENCE_SRC"]) if os.environ.get("PCFD_REFERENCE_SRC") else None
 
 # Host code rounds each operation on its own (no fused multiply-add, which
 # aarch64 compilers form by default), as the reference's x86 build does, so
@@ -106,10 +107,15 @@ def build_oracle(verbose: bool = False) -> Path:
 
 
 def build_ref_pin(verbose: bool = False):
-    """Compile the reference's self-contained matrix/geometry headers, if present."""
+    """Compile the reference's self-contained matrix/geometry headers when
+    PCFD_REFERENCE_SRC names a checkout of the reference; skipped otherwise."""
+    if REFERENCE_SRC is None:
+        if verbose:
+            print("PCFD_REFERENCE_SRC unset: reference-side build skipped")
+        return None
     ucs = REFERENCE_SRC / "ucs"
     if not (ucs / "matrix.h").exists():
-        return None
+        raise RuntimeError("PCFD_REFERENCE_SRC=%s holds no ucs/matrix.h" % REFERENCE_SRC)
     src = ORACLE_DIR / "ref_pin.cpp"
     deps = [src, ucs / "matrix.h", ucs / "geometry.h"]
     if _stale(REF_LIB, deps):

@@ -23,7 +23,10 @@ import tempfile
 import types
 from pathlib import Path
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+_REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PCFD_REFERENCE_SRC")
+if not _REF:
+    sys.exit("usage: make_chem_fixture.py <reference checkout> (or set PCFD_REFERENCE_SRC)")
+REF = Path(_REF)
 OUT = Path(__file__).resolve().parent / "chem_5species_air.json"
 
 

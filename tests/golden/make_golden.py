@@ -13,6 +13,7 @@ Usage: python tests/golden/make_golden.py [/path/to/reference]
 """
 import ctypes as C
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -43,14 +44,16 @@ def read_gmsh2(path):
 
 
 def main():
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PCFD_REFERENCE_SRC")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set PCFD_REFERENCE_SRC)")
+    ref = Path(ref)
     xyz, tris, tags, tets = read_gmsh2(ref / "unitTest" / "meshResources" / "cube.msh")
     (HERE / "cube_msh.json").write_text(json.dumps(
         {"source": "unitTest/meshResources/cube.msh", "expect": {"nnode": 14, "nelem": 48, "volume": 1.0},
          "xyz": xyz, "tris": tris, "tri_tags": tags, "tets": tets}))
 
     sys.path.insert(0, str(ROOT))
-    import os
     os.environ["PCFD_REFERENCE_SRC"] = str(ref)
     from proteuscfd_gb300 import build as B
     lib_path = B.build_ref_pin()

@@ -16,7 +16,7 @@ For each case this script
   3. packs every array it wrote into ``ref_<case>.npz``.
 
 Usage: python tests/golden/make_ref_fixtures.py <reference checkout>
-       (or set PCFD_REFERENCE)
+       (or set PCFD_REFERENCE_SRC)
 """
 from __future__ import annotations
 
@@ -253,9 +253,9 @@ def run_case(exe, name, c, workdir):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PCFD_REFERENCE")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PCFD_REFERENCE_SRC")
     if not ref:
-        sys.exit("usage: make_ref_fixtures.py <reference checkout> (or set PCFD_REFERENCE)")
+        sys.exit("usage: make_ref_fixtures.py <reference checkout> (or set PCFD_REFERENCE_SRC)")
     subprocess.run(["make", "-C", str(ROOT / "oracle" / "refbuild"), "REF=%s" % ref, "-j8"], check=True,
                    stdout=subprocess.DEVNULL)
     exe = ROOT / "oracle" / "_ref" / "ref_dump"

@@ -2,6 +2,7 @@
 fixture against the reference's own files, and conservation properties of
 the production rates (test infrastructure checks; no GPU)."""
 import json
+import os
 import subprocess
 import sys
 from pathlib import Path
@@ -13,7 +14,8 @@ from chem_cases import FIXTURE, conservation, mechanism, states
 from oracle_lib import chem_rates
 from proteuscfd_gb300.chem import model_struct
 
-REF = Path("/root/reference")
+# the reference checkout, when PCFD_REFERENCE_SRC names one
+REF = Path(os.environ.get("PCFD_REFERENCE_SRC") or "/nonexistent")
 
 
 def test_fixture_shape():
