@@ -125,6 +125,22 @@ PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, doubl
     scratch = g_scratch_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
+  // the stream must belong to the current device, whose scratch address was
+  // looked up above, and must not be capturing: the call synchronizes it
+  if (st) {
+    int sdev = -1;
+    e = cudaStreamGetDevice(st, &sdev);
+    if (e != cudaSuccess) return fail(PCFD_ERR_ARG, std::string("cudaStreamGetDevice: ") + cudaGetErrorString(e));
+    if (sdev != dev)
+      return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: stream belongs to device " + std::to_string(sdev) +
+                                    ", the current device is " + std::to_string(dev));
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return fail(PCFD_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: the stream is capturing; the call synchronizes "
+                              "the stream and cannot be captured");
   const int nblocks = (int)((nnode + kRowsPerBlock - 1) / kRowsPerBlock);
   k_norm_partials<<<nblocks, kThreads, 0, st>>>(nnode, b, scratch);
   k_norm_finish<<<1, 32, 0, st>>>(nblocks, nnode, scratch, norms);
