@@ -69,6 +69,13 @@ typedef struct pcfd_box_params {
   int tags[6];
   int jitter_mode;    /* 0: each axis by its own local spacing; 1: every axis by the node's
                        * smallest local spacing (keeps stretched near-wall cells valid) */
+  int wall_start_i;   /* y=0 face cells with i < wall_start_i carry upstream_tag instead of
+                       * tags[2] (a run-in ahead of a wall's leading edge; 0 = none) */
+  int upstream_tag;
+  double wall_ar_max; /* y clustering with a floor on the first wall cell: at least the x
+                       * spacing / wall_ar_max high; the spacing grows by y_ratio from there
+                       * and stops growing at the spacing that fills ly (0: one geometric
+                       * series over the whole height, however thin its first cell) */
 } pcfd_box_params;
 
 typedef void* pcfd_mesh_t;
@@ -524,13 +531,14 @@ PCFD_API int pcfd_get_health(pcfd_solver_t s, long long* counters8);
  * This entry point has no counterpart in the reference.
  * b: device pointer to [nnode][5] doubles; norms: device pointer to 6
  * doubles, written as pcfd_residual's norms_out (resGlobal, then the five
- * per-equation norms); stream: a cudaStream_t, or null for the default
- * stream; synchronous at return.  The only scratch is one fixed array inside
- * the library (768 KiB per GPU, held until the process exits), which limits
- * nnode to 33,554,432; larger inputs return PCFD_ERR_ARG.  The first call on
- * each device looks up that array's device address, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race on it and must be serialised by the caller. */
+ * per-equation norms); stream: a cudaStream_t of the current device, or null
+ * for the default stream (another device's stream returns PCFD_ERR_ARG).  The
+ * call synchronizes the stream before it returns, so it cannot be part of a
+ * CUDA graph: on a capturing stream it returns PCFD_ERR_ARG and enqueues
+ * nothing.  The only scratch is one fixed array inside the library (768 KiB
+ * per GPU, held until the process exits), which limits nnode to 33,554,432;
+ * larger inputs return PCFD_ERR_ARG.  All calls share the array: calls that
+ * overlap on the GPU race on it and must be serialised by the caller. */
 PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, double* norms, void* stream);
 
 PCFD_API const char* pcfd_last_error(void);

@@ -147,10 +147,30 @@ oracle_mesh* oracle_mesh_box(const pcfd_box_params* p) {
   for (int i = 0; i < nx; i++) cx[i] = p->lx * (double)i / (double)(nx - 1);
   for (int k = 0; k < nz; k++) cz[k] = p->lz * (double)k / (double)(nz - 1);
   if (p->y_ratio > 1.0) {
-    double h = (p->y_ratio - 1.0) / (pow(p->y_ratio, (double)(ny - 1)) - 1.0), y = 0.0;
+    /* spacings in units of ly: h0 r^k, capped at hc (the first cell floored at
+     * the x spacing / wall_ar_max, the cap then fills the height) */
+    double h0 = (p->y_ratio - 1.0) / (pow(p->y_ratio, (double)(ny - 1)) - 1.0), y = 0.0;
+    double hc = 1e300;
+    const double h0_min = p->wall_ar_max > 0.0 ? p->lx / (double)(nx - 1) / p->ly / p->wall_ar_max : 0.0;
+    if (h0 < h0_min) {
+      h0 = h0_min;
+      double lo = h0, hi = 1.0;
+      for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        double s = 0.0, hk = h0;
+        for (int j = 0; j < ny - 1; j++) {
+          s += fmin(hk, mid);
+          hk *= p->y_ratio;
+        }
+        if (s < 1.0) lo = mid; else hi = mid;
+      }
+      hc = hi;
+    }
+    double h = h0;
     for (int j = 0; j < ny; j++) {
       cy[j] = p->ly * y;
-      y += h;
+      y += fmin(h, hc);
       h *= p->y_ratio;
     }
     cy[ny - 1] = p->ly;
@@ -229,7 +249,7 @@ oracle_mesh* oracle_mesh_box(const pcfd_box_params* p) {
           m->en[4 * e + 1] = v1;
           m->en[4 * e + 2] = v2;
           m->en[4 * e + 3] = -1;
-          m->etag[e] = p->tags[f];
+          m->etag[e] = (f == 2 && ci < p->wall_start_i) ? p->upstream_tag : p->tags[f];
           e++;
         }
       }

@@ -45,6 +45,7 @@ class BoxParams(C.Structure):
         ("jitter", C.c_double), ("seed", C.c_uint64),
         ("ramp_deg", C.c_double), ("ramp_x0", C.c_double), ("y_ratio", C.c_double),
         ("tags", C.c_int * 6), ("jitter_mode", C.c_int),
+        ("wall_start_i", C.c_int), ("upstream_tag", C.c_int), ("wall_ar_max", C.c_double),
     ]
 
 

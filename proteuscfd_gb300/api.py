@@ -74,9 +74,10 @@ class Mesh:
 
     @classmethod
     def box(cls, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, ramp_deg=0.0, ramp_x0=0.5,
-            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6), reorder=False, jitter_mode=0):
+            y_ratio=1.0, tags=(1, 2, 3, 4, 5, 6), reorder=False, jitter_mode=0, wall_start_i=0, upstream_tag=7,
+            wall_ar_max=0.0):
         p = N.BoxParams(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio, (C.c_int * 6)(*tags),
-                        jitter_mode)
+                        jitter_mode, wall_start_i, upstream_tag, wall_ar_max)
         return cls(N.load().pcfd_mesh_box_create(C.byref(p)), reorder, nx * ny * nz)
 
     @classmethod

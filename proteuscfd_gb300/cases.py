@@ -41,11 +41,16 @@ def ns_flatplate(nx=128, ny=96, nz=96, seed=2, venkat_K=5.0):
     Sutherland viscosity; second order with LSQ gradients and the modified
     Venkatakrishnan limiter; adiabatic no-slip wall at y=0 with geometric
     y-clustering (ratio 1.1), far field at x=0, x=max and y=max, symmetry
-    at z=0/1.  Box [0,(nx-1)/(ny-1)]x[0,1]x[0,1]."""
+    at z=0/1.  Box [0,(nx-1)/(ny-1)]x[0,1]x[0,1].
+
+    The wall starts at x = (nx-ny)/(ny-1), so the plate is one unit long (the
+    Reynolds number's length), behind a symmetry run-in (tag 7) that keeps its
+    leading edge off the far-field inflow boundary.  With the wall's leading
+    edge on the inflow corner the reference solver diverges there."""
     p = Param(gamma=1.4, mach=0.8, Re=1.0e5, Pr=0.72, PrT=0.85, ref_temperature=300.0,
               sorder=2, chi=0.0, viscous=1, limiter=3, venkat_K=venkat_K,
               bc_type={1: N.BC_FARFIELD, 2: N.BC_FARFIELD, 3: N.BC_NOSLIP, 4: N.BC_FARFIELD,
-                       5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY},
+                       5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY, 7: N.BC_SYMMETRY},
               bc_twall={3: -1.0})
     # jitter of +/-0.2 h with h the node's smallest local spacing, on every
     # axis: the clustered wall cells (aspect ratio ~900 at 128x96x96) stay
@@ -53,7 +58,7 @@ def ns_flatplate(nx=128, ny=96, nz=96, seed=2, venkat_K=5.0):
     # layer by ~50 wall-normal spacings, on which the reference solver itself
     # diverges.
     kw = dict(lx=(nx - 1) / (ny - 1), ly=1.0, lz=1.0, jitter=0.2, seed=seed, ramp_deg=0.0, y_ratio=1.1,
-              jitter_mode=1)
+              jitter_mode=1, wall_start_i=nx - ny if nx > ny else (nx - 1) // 4, upstream_tag=7)
     return Case("ns_flatplate_%dx%dx%d" % (nx, ny, nz), nx, ny, nz, kw, p)
 
 

@@ -516,11 +516,33 @@ PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p) {
   for (int i = 0; i < nx; i++) cx[i] = p->lx * (double)i / (double)(nx - 1);
   for (int k = 0; k < nz; k++) cz[k] = p->lz * (double)k / (double)(nz - 1);
   if (p->y_ratio > 1.0) {
+    // spacings in units of ly: h0 r^k, capped at hc
     double h0 = (p->y_ratio - 1.0) / (std::pow(p->y_ratio, (double)(ny - 1)) - 1.0);
+    double hc = 1e300;
+    const double h0_min = p->wall_ar_max > 0.0 ? p->lx / (double)(nx - 1) / p->ly / p->wall_ar_max : 0.0;
+    if (h0 < h0_min) {
+      // the cap hc that makes the ny-1 spacings sum to 1, by bisection
+      h0 = h0_min;
+      auto total = [&](double cap) {
+        double s = 0.0, h = h0;
+        for (int j = 0; j < ny - 1; j++) {
+          s += std::min(h, cap);
+          h *= p->y_ratio;
+        }
+        return s;
+      };
+      double lo = h0, hi = 1.0;
+      for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (total(mid) < 1.0) lo = mid; else hi = mid;
+      }
+      hc = hi;
+    }
     double y = 0.0, h = h0;
     for (int j = 0; j < ny; j++) {
       cy[j] = p->ly * y;
-      y += h;
+      y += std::min(h, hc);
       h *= p->y_ratio;
     }
     cy[ny - 1] = p->ly;
@@ -573,7 +595,7 @@ PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p) {
     int axis = f / 2, side = f % 2;
     double out[3] = {0, 0, 0};
     out[axis] = side ? 1.0 : -1.0;
-    int tag = p->tags[f];
+    const int tag_f = p->tags[f];
     int na = axis == 0 ? ny : nx;  // first in-face axis extent
     int nb = axis == 2 ? ny : nz;  // second in-face axis extent
     for (int b = 0; b < nb - 1; b++)
@@ -583,6 +605,7 @@ PCFD_API pcfd_mesh_t pcfd_mesh_box_create(const pcfd_box_params* p) {
         if (axis == 0) { ci = side ? nx - 2 : 0; cj = a; ck = b; }
         else if (axis == 1) { ci = a; cj = side ? ny - 2 : 0; ck = b; }
         else { ci = a; cj = b; ck = side ? nz - 2 : 0; }
+        const int tag = (f == 2 && ci < p->wall_start_i) ? p->upstream_tag : tag_f;
         for (int u = 0; u < 2; u++)
           for (int v = 0; v < 2; v++)
             for (int w = 0; w < 2; w++) c[u][v][w] = id(ci + u, cj + v, ck + w);
