@@ -201,153 +201,204 @@ def run_reference(args, rank, pg):
     print(json.dumps(line), flush=True)
 
 
-# Newton settings of the convergence study.  "fp64" is the reference's plain
-# method: FP64 residual and Jacobian, 10 block-SGS sweeps per step.  "mixed":
-# double-float residual and Jacobian fluxes, FP32 Jacobian storage,
-# FGMRES(30) right-preconditioned by one SGS sweep, stopped at a 0.1
-# reduction of the linear residual (an inexact-Newton forcing term: the
-# pseudo-time step, not the linear accuracy, sets the Newton step count, so
-# a tighter solve spends Krylov iterations without saving steps); "mixed_bf16" the same
-# with BF16 Jacobian storage (FP32 accumulation).  "mixed_learned": the
-# same with the learned correction on top of the SGS sweep for the first
-# Krylov direction of each cycle (the residual itself, the right-hand side
-# the network is trained on).
-CONV_COMMON = dict(cfl_start=1.0, limiter_freeze=60, first_order_steps=20)
+# The convergence study.  Every arm starts from the same state: a shared
+# start-up of CONV_PREFIX["steps"] plain FP64 steps (first order, then second
+# order with the limiter live, CFL ramped from 1) that ends with the limiter
+# frozen (limiterFreeze, ucs/solutionSpace.tcc:681).  From there all arms solve
+# the same discrete equations with the same frozen limiter, and differ only
+# in the linear solve and its arithmetic; the Newton residual, gradients,
+# limiter and norms stay FP64 in every arm.
+#   fp64:  the reference's method, block-SGS sweeps on the FP64 Jacobian; 30
+#          sweeps at CFL 1000 were the fastest of the settings tried on the
+#          128x96x96 box (10 sweeps at CFL 200, 20 at CFL 1000, 30 at CFL 3000
+#          were slower or stalled)
+#   mixed: FP32 Jacobian (differences in double-float), FGMRES(30)
+#          right-preconditioned by two FP32 SGS sweeps, stopped at a 0.1
+#          reduction of the linear residual (an inexact-Newton forcing term),
+#          CFL 1000
+#   mixed_bf16: the same with BF16 off-diagonal storage (FP32 accumulation)
+#   mixed_learned: mixed with the learned correction on the first Krylov
+#          direction of each cycle (the residual itself, the right-hand side
+#          the network is trained on)
+CONV_PREFIX = dict(steps=60, cfl=50.0, cfl_start=1.0, cfl_ramp_steps=40, nsgs=10, first_order_steps=20,
+                   linear_solver=0, jac_precision=0)
+_MIXED = dict(nsgs=2, linear_solver=1, fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1,
+              first_order_steps=20)
 CONV_ARMS = {
-    "fp64": dict(arith=0, opts=dict(CONV_COMMON, cfl=50.0, cfl_ramp_steps=40, nsgs=10, linear_solver=0,
-                                    jac_precision=0)),
-    "mixed": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=1,
-                                     fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1)),
-    "mixed_bf16": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=1,
-                                          fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=2)),
-    "mixed_learned": dict(arith=1, opts=dict(CONV_COMMON, cfl=100.0, cfl_ramp_steps=40, nsgs=1, linear_solver=2,
-                                             fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1,
-                                             lp_directions=1)),
+    "fp64": dict(cfl=1000.0, nsgs=30, linear_solver=0, jac_precision=0, first_order_steps=20),
+    "fp64_s20": dict(cfl=1000.0, nsgs=20, linear_solver=0, jac_precision=0, first_order_steps=20),
+    "mixed": dict(_MIXED, cfl=1000.0),
+    "mixed_s1": dict(_MIXED, cfl=300.0, nsgs=1),
+    "mixed_bf16": dict(_MIXED, cfl=1000.0, jac_precision=2),
+    "mixed_learned": dict(_MIXED, cfl=1000.0, linear_solver=2, lp_directions=1),
 }
 
 
-def train_learned(dims, seed, iters, epochs, lr, krylov_pairs=0):
-    """Training pairs from the mixed solver's own systems on a mesh with
-    another seed; returns the parameters and the training record."""
-    from proteuscfd_gb300 import SolutionSpace, cases
+def flatplate(dims, seed=2, mach=None, aoa_deg=0.0, Re=None):
+    """The convergence family's case (cases.ns_flatplate) at other flow
+    conditions: Mach, angle of attack in the x-y plane, Reynolds number."""
+    from proteuscfd_gb300 import cases
     case = cases.ns_flatplate(*dims, seed=seed)
-    case.param.jac_boundary_eval = 3
-    m = cases.build_mesh(case)
-    S = SolutionSpace(m, case.param)
-    S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, seed))
-    S.set_residual_arithmetic(1)
-    S.lp_init(1)
-    t0 = time.perf_counter()
-    npairs = 0
-    for it in range(1, iters + 1):
-        S.newton_iterate(it, **CONV_ARMS["mixed"]["opts"])
-        if it >= 3 and it % 3 == 0:
-            npairs = S.lp_collect(nsgs=1, rtol=1e-6, krylov_pairs=krylov_pairs)
-    t_collect = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    l0, l1 = S.lp_train(epochs=epochs, lr=lr)
-    t_train = time.perf_counter() - t0
-    w = S.lp_get_params()
-    S.close()
-    return w, {"mesh": "%dx%dx%d" % dims, "seed": seed, "pairs": npairs, "epochs": epochs, "lr": lr,
-               "loss_first_epoch": l0, "loss_last_epoch": l1, "collect_s": round(t_collect, 2),
-               "train_s": round(t_train, 2)}
+    if mach is not None:
+        case.param.mach = mach
+    if Re is not None:
+        case.param.Re = Re
+    a = np.radians(aoa_deg)
+    case.param.flowdir = (float(np.cos(a)), float(np.sin(a)), 0.0)
+    return case
+
+
+def train_learned(dims, nruns, steps, every, epochs, lr, seed=1000):
+    """Training of the learned preconditioner on pairs the plain mixed solver
+    generates.  Each run draws a flow (Mach ~ U[0.5, 2], angle of attack ~
+    U[-5, 5] degrees, Re ~ log-U[1e4, 1e6]) on a box of the family with its
+    own mesh and state seeds (none is the study's), runs the mixed method
+    from the perturbed freestream, and every `every` steps stores the pair
+    (residual, Newton update solved to 1e-6) with its first Krylov pairs.
+    The network trains on each run's pairs in turn (Adam), carrying its
+    parameters from run to run.  A run whose state stops being finite
+    contributes the pairs it stored before."""
+    from proteuscfd_gb300 import SolutionSpace, cases
+    rng = np.random.default_rng(seed)
+    w, runs, t0 = None, [], time.perf_counter()
+    for r in range(nruns):
+        mach = float(rng.uniform(0.5, 2.0))
+        aoa = float(rng.uniform(-5.0, 5.0))
+        Re = float(10.0 ** rng.uniform(4.0, 6.0))
+        case = flatplate(dims, seed=seed + 2 * r + 1, mach=mach, aoa_deg=aoa, Re=Re)
+        m = cases.build_mesh(case)
+        S = SolutionSpace(m, case.param)
+        S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, seed + 2 * r + 2))
+        S.lp_init(1)
+        if w is not None:
+            S.lp_set_params(w)
+        npairs, ok = 0, True
+        for it in range(steps):
+            rep = S.newton_iterate(it, **dict(_MIXED, cfl=100.0, cfl_start=1.0, cfl_ramp_steps=40,
+                                              limiter_freeze=CONV_PREFIX["steps"]))
+            if not np.isfinite(rep["res"][0]):
+                ok = False
+                break
+            if it >= 10 and it % every == 0:
+                try:
+                    npairs = S.lp_collect(nsgs=_MIXED["nsgs"], rtol=1e-6, krylov_pairs=2)
+                except Exception as exc:  # a linear system the solve cannot reach 1e-6 on
+                    ok = "collect: %s" % exc
+                    break
+        rec = {"mach": round(mach, 3), "aoa_deg": round(aoa, 2), "Re": round(Re), "pairs": npairs, "finite": ok}
+        if npairs:
+            l0, l1 = S.lp_train(epochs=epochs, lr=lr)
+            w = S.lp_get_params()
+            rec.update(loss_first_epoch=l0, loss_last_epoch=l1)
+        runs.append(rec)
+        S.close()
+    return w, {"mesh": "%dx%dx%d" % dims, "runs": runs, "pairs": sum(x["pairs"] for x in runs),
+               "epochs_per_run": epochs, "lr": lr, "train_s": round(time.perf_counter() - t0, 2)}
 
 
 def converge_study(args):
-    """Wall time to a 1e-10 drop of resGlobal on one GPU, per arm, with the
-    final-field and wall-force differences against the FP64 arm."""
+    """Wall time to a 1e-10 drop of resGlobal on one GPU, per arm, from the
+    shared start-up; each arm's final field and body force (pressure plus
+    viscous, FORCE_Kernel) against the FP64 arm's."""
     from proteuscfd_gb300 import SolutionSpace, cases
     from proteuscfd_gb300 import _native as N
     w = WORKLOADS[args.converge_workload]
     dims = (w["nx"], w["ny"], w["nz"])
-    out = {"workload": "ns_flatplate %dx%dx%d (mesh seed 2, state seed 1), second order, Mach 0.8, Re 1e5" % dims,
-           "target_drop": 1e-10, "time_cap_s": args.converge_cap,
-           "limiter_freeze": args.converge_limiter_freeze}
+    case = flatplate(dims)
+    walls = [t for t, b in case.param.bc_type.items() if b == N.BC_NOSLIP]
+    t0 = time.perf_counter()
+    m = cases.build_mesh(case)
+    out = {"workload": "ns_flatplate %dx%dx%d (mesh seed 2, state seed 1), second order, Mach 0.8, Re 1e5, "
+                       "modified Venkatakrishnan K=%g" % (dims + (case.param.venkat_K,)),
+           "nodes": m.nnode, "edges": m.nedge, "mesh_build_s": round(time.perf_counter() - t0, 2),
+           "target_drop": 1e-10, "time_cap_s": args.converge_cap, "arms": {}}
     lp_w = None
     if "mixed_learned" in args.converge_arms:
-        # same resolution, unseen mesh and state seed
-        lp_w, out["learned_training"] = train_learned(dims, 7, 60, 150, 2e-3)
-    finals, frozen_lim = {}, None
+        tdims = WORKLOADS[args.learned_train_workload]
+        lp_w, out["learned_training"] = train_learned((tdims["nx"], tdims["ny"], tdims["nz"]), args.learned_runs,
+                                                      90, 10, 30, 2e-3)
+    # the shared start-up
+    P = CONV_PREFIX["steps"]
+    S = SolutionSpace(m, case.param)
+    S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 1))
+    N.check(N.load().pcfd_device_sync(), "sync")
+    t0 = time.perf_counter()
+    hist = []
+    for it in range(P):
+        opts = {k: v for k, v in CONV_PREFIX.items() if k != "steps"}
+        hist.append(S.newton_iterate(it, limiter_freeze=P, **opts)["res"][0])
+    t_pre = time.perf_counter() - t0
+    r0 = hist[0]
+    q_pre, lim_pre = S.get_state(), S.get_limiter()
+    S.close()
+    out["startup"] = {"steps": P, "wall_s": round(t_pre, 3), "drop": hist[-1] / r0, "opts": CONV_PREFIX}
+    finals = {}
     for name in args.converge_arms:
         arm = CONV_ARMS[name]
-        case = cases.ns_flatplate(*dims)
-        case.param.jac_boundary_eval = 3
-        m = cases.build_mesh(case)
         S = SolutionSpace(m, case.param)
-        S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 1))
-        S.set_residual_arithmetic(arm["arith"])
-        if arm["opts"]["linear_solver"] == 2:
+        S.set_state(q_pre)
+        S.set_limiter(lim_pre)
+        if arm["linear_solver"] == 2:
             S.lp_init(1)
-            S.lp_set_params(lp_w)
-        opts = dict(arm["opts"], limiter_freeze=args.converge_limiter_freeze)
+            if lp_w is not None:
+                S.lp_set_params(lp_w)
         N.check(N.load().pcfd_device_sync(), "sync")
-        hist, t_at, lin, fb = [], {}, 0, 0
+        h, t_at, lin, fb = [], {}, 0, 0
         t0 = time.perf_counter()
-        for it in range(1, args.converge_iters + 1):
-            rep = S.newton_iterate(it, **opts)
-            r = rep["res"][0]
-            hist.append(r)
+        it = P
+        while True:
+            rep = S.newton_iterate(it, limiter_freeze=P, **arm)
+            it += 1
+            r = rep["res"][0] / r0
+            h.append(r)
             lin += rep["lin_iters"]
             fb += rep["lp_fallbacks"]
             el = time.perf_counter() - t0
-            for d in (1e-2, 1e-4, 1e-6, 1e-8, 1e-10):
-                if d not in t_at and r <= d * hist[0]:
-                    t_at[d] = [it, round(el, 3)]
-            if not np.isfinite(r) or r <= 1e-10 * hist[0] or el > args.converge_cap:
+            for d in (1e-4, 1e-6, 1e-8, 1e-10):
+                if d not in t_at and r <= d:
+                    t_at[d] = [P + len(h), round(t_pre + el, 3)]
+            if not np.isfinite(r) or r <= 1e-10 or el > args.converge_cap or len(h) >= args.converge_iters:
                 break
         wall = time.perf_counter() - t0
-        q = S.get_state()
-        finals[name] = (q[:m.nnode, :5].copy(), wall_force(m, case, q))
-        if name == "fp64" and len(hist) > opts["first_order_steps"]:
-            frozen_lim = S.get_limiter()
-        rec = {"iters": len(hist), "wall_s": round(wall, 3), "drop": hist[-1] / hist[0],
-               "reached_1e-10": 1e-10 in t_at, "s_to_drop": {str(k): v for k, v in t_at.items()},
-               "linear_iters_per_step": lin / len(hist), "health": S.health()}
+        fp, fv = S.forces(walls)
+        finals[name] = (S.get_state()[:m.nnode, :5].copy(), np.r_[fp, fv])
+        # where a late step's time goes: three more steps with a CUDA event
+        # pair around every launch (after the timed run and its final field)
+        S.profile(True)
+        S.profile_reset()
+        for k in range(3):
+            S.newton_iterate(it + k, limiter_freeze=P, **arm)
+        tm = S.timers()
+        S.profile(False)
+        rec = {"steps_after_startup": len(h), "wall_s_after_startup": round(wall, 3),
+               "wall_s_total": round(t_pre + wall, 3), "drop": h[-1], "reached_1e-10": 1e-10 in t_at,
+               "steps_s_to_drop": {str(k): v for k, v in t_at.items()},
+               "linear_iters_per_step": lin / len(h), "ms_per_step": 1e3 * wall / len(h),
+               "opts": arm, "health": S.health(),
+               "late_step_ms_by_kernel_group": {k: round(v[0] / 3, 3) for k, v in tm.items() if v[1]}}
         if fb:
             rec["sgs_fallbacks"] = fb
-        if not np.isfinite(hist[-1]):
+        if not np.isfinite(h[-1]):
             rec["stopped"] = "non-finite residual"
-            rec["res_history"] = [float(v) for v in hist[-10:]]
-        out[name] = rec
+        out["arms"][name] = rec
         S.close()
-    if "fp64" in finals and "mixed" in finals and frozen_lim is not None:
-        # The frozen limiter makes the converged field depend on the state at
-        # the freeze, which differs between arms.  This check solves the
-        # mixed arm's equations with the FP64 arm's frozen limiter from the
-        # start, so that both solve the same discrete equations and only the
-        # arithmetic differs.
-        case = cases.ns_flatplate(*dims)
-        case.param.jac_boundary_eval = 3
-        m = cases.build_mesh(case)
-        S = SolutionSpace(m, case.param)
-        S.set_state(cases.perturbed_state(S.qinf(), m.nnode + m.nbedge, 1))
-        S.set_residual_arithmetic(1)
-        S.set_limiter(frozen_lim)
-        opts = dict(CONV_ARMS["mixed"]["opts"], limiter_freeze=1)
-        r0, t0, its = None, time.perf_counter(), 0
-        for it in range(1, args.converge_iters + 1):
-            r = S.newton_iterate(it, **opts)["res"][0]
-            r0 = r if r0 is None else r0
-            its = it
-            if not np.isfinite(r) or r <= 1e-10 * r0 or time.perf_counter() - t0 > args.converge_cap:
-                break
-        q = S.get_state()
-        qref, fref = finals["fp64"]
-        out["mixed"]["same_limiter_check"] = {
-            "iters": its, "drop": r / r0,
-            "field_rel_l2_vs_fp64": float(np.linalg.norm(q[:m.nnode, :5] - qref) / np.linalg.norm(qref)),
-            "wall_force_rel_err_vs_fp64": float(np.linalg.norm(wall_force(m, case, q) - fref) / np.linalg.norm(fref))}
-        S.close()
-    if "fp64" in finals:
-        qref, fref = finals["fp64"]
+    ref = "fp64" if "fp64" in finals else None
+    if ref:
+        qref, fref = finals[ref]
+        drag_ref = fref[0] + fref[3]
         for name, (qa, fa) in finals.items():
-            if name == "fp64":
+            rec = out["arms"][name]
+            rec["force_pressure"] = [float(v) for v in fa[:3]]
+            rec["force_viscous"] = [float(v) for v in fa[3:]]
+            if name == ref:
                 continue
-            out[name]["field_rel_l2_vs_fp64"] = float(np.linalg.norm(qa - qref) / np.linalg.norm(qref))
-            out[name]["wall_force_rel_err_vs_fp64"] = float(np.linalg.norm(fa - fref) / np.linalg.norm(fref))
-            if out[name]["reached_1e-10"] and out["fp64"]["reached_1e-10"]:
-                out[name]["speedup_vs_fp64"] = out["fp64"]["s_to_drop"]["1e-10"][1] / out[name]["s_to_drop"]["1e-10"][1]
+            rec["field_rel_l2_vs_fp64"] = float(np.linalg.norm(qa - qref) / np.linalg.norm(qref))
+            rec["force_rel_err_vs_fp64"] = float(np.linalg.norm(fa - fref) / np.linalg.norm(fref))
+            rec["drag_rel_err_vs_fp64"] = float(abs(fa[0] + fa[3] - drag_ref) / abs(drag_ref))
+            if rec["reached_1e-10"] and out["arms"][ref]["reached_1e-10"]:
+                rec["speedup_vs_fp64"] = out["arms"][ref]["wall_s_total"] / rec["wall_s_total"]
+                rec["speedup_vs_fp64_after_startup"] = (out["arms"][ref]["wall_s_after_startup"] /
+                                                        rec["wall_s_after_startup"])
     return out
 
 
@@ -511,19 +562,6 @@ def chemistry_study(args):
                                  "sample": "%d nodes by the oracle, 1 thread" % nsn}}}
 
 
-def wall_force(m, case, q):
-    """Pressure force on the no-slip wall: sum over its boundary half-edges of
-    p(node) times the outward dual-face area vector."""
-    from proteuscfd_gb300 import _native as N
-    be = np.asarray(m.bedges).reshape(-1, 2)
-    ba = np.asarray(m.bedge_area).reshape(-1, 4)
-    tags = np.asarray(m.bfactag)
-    wall = [t for t, b in case.param.bc_type.items() if b == N.BC_NOSLIP]
-    sel = np.isin(tags, wall)
-    p = q[be[sel, 0], 6]
-    return (p[:, None] * ba[sel, :3] * ba[sel, 3:4]).sum(axis=0)
-
-
 def run_gb300(args, ws, rank, local, pg):
     from proteuscfd_gb300 import SolutionSpace, cases
     from proteuscfd_gb300 import _native as N
@@ -604,29 +642,44 @@ def run_gb300(args, ws, rank, local, pg):
 
     # roofline of the dominant FP64 kernel.  Algorithmic bytes per launch,
     # each array once (B/edge, B/node):
-    #   edge_flux   (MUSCL + Roe + clip test): 104 = ids 8, area 32, edge
-    #               half-vector 24, flux written 40; 200 = q 40, the 15
-    #               gradient terms of the conservative variables 120, limiter 40
+    #   edge_flux   (MUSCL + Roe + clip test, both ends' corrections stored
+    #               by the limiter pass): 160 = ids 8, area 32, corrections
+    #               80, flux written 40; 80 = q 40, limiter 40
     #   edge_viscous: 144 = ids 8, area 32, half-vector 24, flux read and
     #               written 80; 256 = q 40, gradient 216
     #   lsq_gradient: 56 = ids 8, LSQ weights of both ends 48; 288 = the 9
     #               gradient variables 72, gradient written 216
-    #   venkat_limiter: 32 = ids 8, half-vector 24; 208 = q 40, gradient 120,
-    #               volume 8, limiter written 40
+    #   venkat_limiter: 112 = ids 8, half-vector 24, both ends' corrections
+    #               written 80; 208 = q 40, gradient 120, volume 8, limiter
+    #               written 40
     #   residual_gather: 88 = the edge's flux read at both ends 80, its id in
     #               the node list 8; 80 = q_old 40, b written 40
-    alg_per = {"edge_flux": (104.0, 200.0), "edge_viscous": (144.0, 256.0), "lsq_gradient": (56.0, 288.0),
-               "venkat_limiter": (32.0, 208.0), "residual_gather": (88.0, 80.0)}
+    alg_per = {"edge_flux": (160.0, 80.0), "edge_viscous": (144.0, 256.0), "lsq_gradient": (56.0, 288.0),
+               "venkat_limiter": (112.0, 208.0), "residual_gather": (88.0, 80.0)}
     top = max((k for k in kernels if k in alg_per), key=lambda k: kernels[k]["ms_per_step"])
     top_ms = kernels[top]["ms_per_step"] / max(kernels[top]["launches_per_step"], 1.0)
     alg_bytes = alg_per[top][0] * m.nedge + alg_per[top][1] * m.nnode
     achieved = alg_bytes / (top_ms * 1e-3) / 1e9 if top_ms > 0 else None
-    # DRAM traffic per launch from one ncu capture of the kernel on a small
-    # box of the family (profiles/), scaled by the algorithmic bytes: the
-    # traffic grows with the edges and nodes streamed
-    traffic_ratio = {"edge_flux": 133.26 / 133.36}
+    # DRAM traffic per launch from one ncu capture of the kernels on the
+    # 128x96x96 box (profiles/residual_fp64_ns128.md), as a ratio to their
+    # algorithmic bytes there, scaled to this box: the traffic grows with the
+    # edges and nodes streamed
+    traffic_ratio = {"edge_flux": 1462.9 / 1393.9, "venkat_limiter": 1700.8 / 1155.1, "edge_viscous": 1498.7 / 1471.6,
+                     "lsq_gradient": 790.8 / 794.6, "residual_gather": 640.3 / 809.2}
     traffic = alg_bytes * traffic_ratio[top] if top in traffic_ratio else None
     peak, peak_kind = peaks()
+    # The FP64 kernels are bound by the FP64 pipe (2 FP64 instructions per
+    # clock per SM on GB300).  FP64 thread instructions per edge and per node
+    # of each kernel, from one ncu capture on the 128x96x96 box
+    # (sm__inst_executed_pipe_fp64 x 32, profiles/residual_fp64_ns128.md);
+    # achieved = those instructions over the kernel's event-timed launch,
+    # peak = 2 x SMs x the median SM clock sampled during the timed region.
+    fp64_inst = {"edge_flux": (257.0, 0.0), "venkat_limiter": (0.0, 1145.0), "edge_viscous": (152.0, 0.0),
+                 "lsq_gradient": (0.0, 506.0), "residual_gather": (0.0, 184.0)}
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clk.summary().get("sm_mhz") or 0.0
+    fp64_peak = 2.0 * nsm * sm_mhz * 1e6 / 1e9  # G instructions / s
+    fp64_ach = (fp64_inst[top][0] * m.nedge + fp64_inst[top][1] * m.nnode) / (top_ms * 1e-3) / 1e9
     # the whole residual against its algorithmic bytes: 40 B/edge + 360 B/node
     # + 84 B/half-edge (gradients and limiter given)
     res_bytes = 40.0 * m.nedge + 360.0 * m.nnode + 84.0 * m.nbedge
@@ -655,6 +708,11 @@ def run_gb300(args, ws, rank, local, pg):
                      "peak_source": peak_kind,
                      "note": "HBM fraction of the measured copy peak; the FP64 kernels are bound by the FP64 pipe "
                              "(2 FP64 fused multiply-adds per clock per SM on GB300), not by HBM"},
+        "roofline_fp64": {"bound": "fp64 pipe", "kernel": top, "achieved": fp64_ach, "peak": fp64_peak,
+                          "unit": "G FP64 instructions/s", "frac": fp64_ach / fp64_peak if fp64_peak else None,
+                          "instructions_per_edge_node": fp64_inst[top],
+                          "source": "instruction counts from ncu (profiles/residual_fp64_ns128.md); peak 2/clock/SM "
+                                    "x %d SMs x median SM clock" % nsm},
         "clocks": clk.summary(),
         "e2e": {"value": ws * m.nedge / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -667,7 +725,7 @@ def run_gb300(args, ws, rank, local, pg):
     # on resident vectors (the matrix is larger than L2)
     S.set_state(q0)
     S.set_residual_arithmetic(1)
-    S.newton_iterate(1, **dict(CONV_ARMS["mixed"]["opts"], fgmres_m=2))
+    S.newton_iterate(1, **dict(CONV_ARMS["mixed"], fgmres_m=2))
     S.bench_spmv(3)
     spmv_ms = S.bench_spmv(args.steps) / args.steps
     nb = S.nblocks()
@@ -676,6 +734,33 @@ def run_gb300(args, ws, rank, local, pg):
                             "vectors resident" % nb,
                     "ms": spmv_ms, "bytes": spmv_bytes, "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
                     "peak_gbs": peak, "frac": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peak if peak else None}
+
+    # the block-SGS sweep (k_sgs_sweep_staged, one cooperative launch per
+    # call): the mixed solver's FP32 preconditioner sweep on the FP32 matrix,
+    # then the FP64 arm's 10 FP64 sweeps on the FP64 matrix.  Algorithmic
+    # bytes per sweep: the matrix twice (forward and backward pass) as in the
+    # SpMV, plus the LU'd diagonal and pivots and the vectors,
+    # 2 x SpMV + N (25 s + 20) with s the matrix scalar size.
+    def sgs_bytes(sz):
+        spmv = (nb - m.nnode) * (25 * sz + 4) + m.nnode * (4 + 5 * sz + 5 * sz + 25 * sz)
+        return 2 * spmv + m.nnode * (25 * sz + 20)
+
+    S.bench_sgs(3, 1, fp32=True)
+    sgs32_ms = S.bench_sgs(args.steps, 1, fp32=True) / args.steps
+    S.set_residual_arithmetic(0)
+    S.newton_iterate(1, **dict(CONV_ARMS["fp64"], nsgs=1))
+    S.bench_sgs(1, 10, fp32=False)
+    nrep64 = max(2, args.steps // 5)
+    sgs64_ms = S.bench_sgs(nrep64, 10, fp32=False) / (10 * nrep64)
+    line["sgs"] = {"what": "block-SGS sweep (forward + backward, k_sgs_sweep_staged) on this box's %d-block "
+                           "matrix, vectors resident; ms per sweep" % nb,
+                   "fp32": {"ms": sgs32_ms, "bytes": sgs_bytes(4),
+                            "achieved_gbs": sgs_bytes(4) / (sgs32_ms * 1e-3) / 1e9,
+                            "frac": sgs_bytes(4) / (sgs32_ms * 1e-3) / 1e9 / peak if peak else None},
+                   "fp64": {"ms": sgs64_ms, "bytes": sgs_bytes(8),
+                            "achieved_gbs": sgs_bytes(8) / (sgs64_ms * 1e-3) / 1e9,
+                            "frac": sgs_bytes(8) / (sgs64_ms * 1e-3) / 1e9 / peak if peak else None},
+                   "colors": S.crs_structure()[2]}
     S.close()
     if rank == 0 and ws == 1 and not args.no_chemistry:
         line["chemistry"] = chemistry_study(args)
@@ -699,11 +784,12 @@ def main():
                     help="comma-separated arms of the time-to-1e-10 study on one GPU ('' to skip)")
     ap.add_argument("--converge-workload", default="ns64", choices=sorted(WORKLOADS))
     ap.add_argument("--converge-cap", type=float, default=60.0, help="wall-time cap per arm, seconds")
-    ap.add_argument("--converge-iters", type=int, default=3000, help="Newton iteration cap per arm")
+    ap.add_argument("--converge-iters", type=int, default=5000, help="Newton iteration cap per arm")
+    ap.add_argument("--learned-train-workload", default="ns64", choices=sorted(WORKLOADS),
+                    help="box of the learned preconditioner's training runs")
+    ap.add_argument("--learned-runs", type=int, default=4, help="training runs (sampled flows)")
     ap.add_argument("--converge-only", action="store_true", help="run only the convergence study")
     ap.add_argument("--no-chemistry", action="store_true", help="skip the finite-rate chemistry measurement")
-    ap.add_argument("--converge-limiter-freeze", type=int, default=60,
-                    help="Newton iteration from which the limiter is frozen (0: recomputed every iteration)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.converge_arms = [a for a in args.converge.split(",") if a]

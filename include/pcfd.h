@@ -503,6 +503,12 @@ PCFD_API int pcfd_bench_residual_full(pcfd_solver_t s, int nsteps, double* ms_ou
  * on device-resident vectors: FP64 vectors with vec_precision 0, the FP32
  * Krylov solver's product with 1 (FP32 or BF16 storage). */
 PCFD_API int pcfd_bench_spmv(pcfd_solver_t s, int nrep, int vec_precision, double* ms_out);
+/* Device time (CUDA events on the library's stream) of nrep calls of nsweeps
+ * block-SGS sweeps (CRS<T>::SGS, ucs/crs.tcc:62) on the assembled matrix,
+ * right-hand side the last residual, device-resident vectors: FP64 vectors
+ * with vec_precision 0 (the matrix in its stored precision), the FP32 Krylov
+ * preconditioner's sweep with 1 (FP32 or BF16 storage). */
+PCFD_API int pcfd_bench_sgs(pcfd_solver_t s, int nrep, int nsweeps, int vec_precision, double* ms_out);
 /* Selects the CUDA device for handles created afterwards on this thread. */
 PCFD_API int pcfd_set_device(int device);
 /* Waits for all work on the current device. */

@@ -153,6 +153,7 @@ PROTOTYPES = {
     "pcfd_get_residual": (C.c_int, [_P, _DP]),
     "pcfd_bench_residual_full": (C.c_int, [_P, C.c_int, _DP, _DP]),
     "pcfd_bench_spmv": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    "pcfd_bench_sgs": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
     "pcfd_timestep": (C.c_int, [_P, C.c_double, _DP, _DP]),
     "pcfd_set_jacobian_precision": (C.c_int, [_P, C.c_int]),
     "pcfd_jacobian": (C.c_int, [_P]),

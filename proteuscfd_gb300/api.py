@@ -321,6 +321,15 @@ class SolutionSpace:
         N.check(self._lib.pcfd_bench_spmv(self._h, int(nrep), 1 if fp32 else 0, C.byref(ms)), "pcfd_bench_spmv")
         return ms.value
 
+    def bench_sgs(self, nrep, nsweeps=1, fp32=True):
+        """Device time (ms) of nrep calls of nsweeps block-SGS sweeps on the
+        assembled matrix (FP32 vectors, the Krylov preconditioner's sweep, or
+        FP64 vectors)."""
+        ms = C.c_double()
+        N.check(self._lib.pcfd_bench_sgs(self._h, int(nrep), int(nsweeps), 1 if fp32 else 0, C.byref(ms)),
+                "pcfd_bench_sgs")
+        return ms.value
+
     def set_residual_arithmetic(self, mode):
         """0 FP64, 1 double-float on the FP32 pipes (composite calls only)."""
         N.check(self._lib.pcfd_set_residual_arithmetic(self._h, int(mode)), "pcfd_set_residual_arithmetic")

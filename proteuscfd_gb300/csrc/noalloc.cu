@@ -106,8 +106,17 @@ PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, doubl
   if (nnode > kMaxNodes)
     return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: nnode " + std::to_string(nnode) +
                                   " exceeds the fixed scratch limit of " + std::to_string(kMaxNodes) + " nodes");
+  // a capturing stream is refused before any other runtime call: the call
+  // synchronizes the stream, which a capture cannot contain
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return fail(PCFD_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: the stream is capturing; the call synchronizes "
+                              "the stream and cannot be captured");
   int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(PCFD_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: device id out of range");
   double* scratch;
@@ -124,9 +133,8 @@ PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, doubl
     }
     scratch = g_scratch_addr[dev];
   }
-  cudaStream_t st = (cudaStream_t)stream;
   // the stream must belong to the current device, whose scratch address was
-  // looked up above, and must not be capturing: the call synchronizes it
+  // looked up above
   if (st) {
     int sdev = -1;
     e = cudaStreamGetDevice(st, &sdev);
@@ -135,12 +143,6 @@ PCFD_API int pcfd_residual_norms_noalloc(const double* b, long long nnode, doubl
       return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: stream belongs to device " + std::to_string(sdev) +
                                     ", the current device is " + std::to_string(dev));
   }
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  e = cudaStreamIsCapturing(st, &cap);
-  if (e != cudaSuccess) return fail(PCFD_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
-  if (cap != cudaStreamCaptureStatusNone)
-    return fail(PCFD_ERR_ARG, "pcfd_residual_norms_noalloc: the stream is capturing; the call synchronizes "
-                              "the stream and cannot be captured");
   const int nblocks = (int)((nnode + kRowsPerBlock - 1) / kRowsPerBlock);
   k_norm_partials<<<nblocks, kThreads, 0, st>>>(nnode, b, scratch);
   k_norm_finish<<<1, 32, 0, st>>>(nblocks, nnode, scratch, norms);

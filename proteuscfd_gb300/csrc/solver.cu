@@ -148,6 +148,12 @@ struct Solver {
   int lim_clipped = 0;  // 1: d_lim already went through the explicit pressure clip
   int grad_arith = 0, lim_arith = 0;
   int lim_fresh = 0;    // the limiter was computed since the last residual (its clip is pending)
+  // each edge end's MUSCL correction grad.dx ([nedge][2][5], left end
+  // first), written by the limiter pass that forms it anyway; valid for the
+  // gradient it was formed from until the next residual (chi = 0 only)
+  double* d_ext = nullptr;
+  dfl* f_ext = nullptr;
+  int ext_ready = 0, ext_arith = 0;
 
   // residual arithmetic of the composite calls: 0 FP64, 1 double-float on the
   // FP32 pipes; the double-float copies of the residual-path arrays
@@ -764,7 +770,8 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
                                            const int* __restrict__ nnbr, const S* __restrict__ q,
                                            const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
                                            double K3, const S* qi, const S* gi, const S* qmin, const S* qmax,
-                                           S* __restrict__ limraw, S* __restrict__ lim, int* __restrict__ clipflag) {
+                                           S* __restrict__ limraw, S* __restrict__ lim, int* __restrict__ clipflag,
+                                           S* __restrict__ ext) {
   const S zero = Sc<S>::c(0.0);
   const S chi = Sc<S>::from(chi_d), hchi = Sc<S>::c(0.5) * chi, omc = Sc<S>::c(1.0) - chi;
   const S one = Sc<S>::c(1.0), two = Sc<S>::c(2.0);
@@ -780,9 +787,11 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
       const S* hv = &eh[3 * (size_t)(se < 0 ? ~se : se)];
       S dx0 = hv[0], dx1 = hv[1], dx2 = hv[2];
       if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
+      S* xo = (CHI0 && ext) ? &ext[(size_t)(se < 0 ? ~se : se) * (2 * NEQN) + (se < 0 ? 0 : NEQN)] : nullptr;
 #pragma unroll
       for (int t = 0; t < NEQN; t++) {
         S gdx = dot3_ref<S>(gi[3 * t], dx0, gi[3 * t + 1], dx1, gi[3 * t + 2], dx2);
+        if (xo) xo[t] = gdx;
         S Q = extrap_ref<S>(qi[t], qj[t] - qi[t], gdx, hchi, omc, CHI0);
         S r = one;
         if (Q > qi[t]) r = (qmax[t] - qi[t]) / (Q - qi[t]);
@@ -836,9 +845,11 @@ __device__ __forceinline__ void limit_node(int i, int k0, int k1, const int* __r
     const S* hv = &eh[3 * (size_t)(se < 0 ? ~se : se)];
     S dx0 = hv[0], dx1 = hv[1], dx2 = hv[2];
     if (se >= 0) { dx0 = -dx0; dx1 = -dx1; dx2 = -dx2; }
+    S* xo = (CHI0 && ext) ? &ext[(size_t)(se < 0 ? ~se : se) * (2 * NEQN) + (se < 0 ? 0 : NEQN)] : nullptr;
 #pragma unroll
     for (int t = 0; t < NEQN; t++) {
       S gdx = dot3_ref<S>(gi[3 * t], dx0, gi[3 * t + 1], dx1, gi[3 * t + 2], dx2);
+      if (xo) xo[t] = gdx;
       S corr = CHI0 ? gdx : hchi * (qj[t] - qi[t]) + omc * gdx;
       S num, den;
       if (F64) {
@@ -881,7 +892,7 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
                                                 const S* __restrict__ q, const S* __restrict__ grad,
                                                 const S* __restrict__ eh, const double* __restrict__ vol, double chi_d,
                                                 double K3, S* __restrict__ limraw, S* __restrict__ lim,
-                                                int* __restrict__ clipflag) {
+                                                int* __restrict__ clipflag, S* __restrict__ ext) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnode) return;
   const S zero = Sc<S>::c(0.0);
@@ -899,7 +910,8 @@ __global__ void __launch_bounds__(128) k_venkat(int nnode, const int* __restrict
     const S* qj = &q[(size_t)nnbr[k] * NVARS];
     for (int t = 0; t < NEQN; t++) bound_upd<S>(qj[t], qmin[t], qmax[t], kmn[t], kmx[t]);
   }
-  limit_node<S, LIM, CHI0>(i, k0, k1, nedg, nnbr, q, eh, vol, chi_d, K3, qi, gi, qmin, qmax, limraw, lim, clipflag);
+  limit_node<S, LIM, CHI0>(i, k0, k1, nedg, nnbr, q, eh, vol, chi_d, K3, qi, gi, qmin, qmax, limraw, lim, clipflag,
+                           ext);
 }
 
 // BadExtrapolation (ucs/compressible.tcc:1056)
@@ -943,6 +955,101 @@ __device__ int clip_check(const S* qL, const S* qR, const S* gL, const S* gR, co
   S Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
   if (bad_extrap(gamma, Qr)) m |= 4;
   return m;
+}
+
+// The three BadExtrapolation tests of clip_check for the states built from
+// stored MUSCL corrections c (the limiter pass's grad.dx of each end):
+// Q = q + c * l with the raw limiter l, then the Roe average.
+template <class S>
+__device__ int clip_check_ext(const S* qL, const S* qR, const S* c, const S* lL, const S* lR, S gamma) {
+  S Qi[NEQN], Qj[NEQN];
+  for (int t = 0; t < NEQN; t++) {
+    Qi[t] = qL[t] + c[t] * lL[t];
+    Qj[t] = qR[t] + c[NEQN + t] * lR[t];
+  }
+  int m = 0;
+  if (bad_extrap(gamma, Qi)) m |= 1;
+  if (bad_extrap(gamma, Qj)) m |= 2;
+  const S gm1 = gamma - Sc<S>::c(1.0), half = Sc<S>::c(0.5);
+  S rL = Qi[0], rR = Qj[0];
+  S uL = Qi[1] / rL, vL = Qi[2] / rL, wL = Qi[3] / rL;
+  S uR = Qj[1] / rR, vR = Qj[2] / rR, wR = Qj[3] / rR;
+  S PL = gm1 * (Qi[4] - half * rL * (uL * uL + vL * vL + wL * wL));
+  S PR = gm1 * (Qj[4] - half * rR * (uR * uR + vR * vR + wR * wR));
+  S hL = (Qi[4] + PL) / rL, hR = (Qj[4] + PR) / rR;
+  S rho = sqrt(rL * rR);
+  S sg = rho / (rL + rho);
+  S u = uL + sg * (uR - uL), v = vL + sg * (vR - vL), w = wL + sg * (wR - wL), h = hL + sg * (hR - hL);
+  S v2h = half * (u * u + v * v + w * w);
+  S Qr[NEQN] = {rho, rho * u, rho * v, rho * w, rho / gamma * (h + gm1 * v2h)};
+  if (bad_extrap(gamma, Qr)) m |= 4;
+  return m;
+}
+
+// An FP32 value of x on the integer pipes: sign, exponent and the top 23
+// significand bits of the double, truncated (relative error below 2^-23),
+// 0 below FP32's normal range, infinity above it, NaN for a non-finite x.
+// An FP64 to FP32 conversion instruction would issue on the FP64 pipe, which
+// the edge pass is bound by.
+__device__ __forceinline__ float f32_of(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int e = (hi >> 20) & 0x7ff;
+  const int fe = e - 1023 + 127;
+  unsigned bits;
+  if (e == 0x7ff) bits = 0x7fc00000u;
+  else if (fe <= 0) bits = 0u;
+  else if (fe >= 255) bits = 0x7f800000u;
+  else bits = ((unsigned)fe << 23) | ((unsigned)(hi & 0xfffff) << 3) | (lo >> 29);
+  return __uint_as_float(bits | ((unsigned)hi & 0x80000000u));
+}
+__device__ __forceinline__ float f32_of(dfl x) { return x.hi; }
+
+// True when the three tests of clip_check_ext certainly pass (no clip),
+// decided in FP32: each tested quantity (density, total energy, pressure of
+// both extrapolated states and of their Roe average) must exceed the test's
+// threshold by 1e-3 of the magnitudes it is formed from, two orders above
+// the FP32 evaluation's own error (below 1e-5 of those magnitudes once each
+// density keeps at least a tenth of its parts, which the pass also asks).
+// False sends the edge to the exact test.
+template <class S>
+__device__ bool clip_clear_f32(const S* qL, const S* qR, const S* c, const S* lL, const S* lR, float gamma) {
+  const float tiny = 1.0e-10f, mrg = 1.0e-3f, gm1 = gamma - 1.0f;
+  float Q[2][NEQN], M[2][NEQN];
+  for (int t = 0; t < NEQN; t++) {
+    float a = f32_of(qL[t]), d = f32_of(c[t]) * f32_of(lL[t]);
+    Q[0][t] = a + d;
+    M[0][t] = fabsf(a) + fabsf(d);
+    a = f32_of(qR[t]);
+    d = f32_of(c[NEQN + t]) * f32_of(lR[t]);
+    Q[1][t] = a + d;
+    M[1][t] = fabsf(a) + fabsf(d);
+  }
+  float u[2], v[2], w[2], h[2], hm[2];
+  for (int k = 0; k < 2; k++) {
+    const float r = Q[k][0];
+    if (!(r > 0.1f * M[k][0])) return false;
+    const float ir = 1.0f / r;
+    u[k] = Q[k][1] * ir;
+    v[k] = Q[k][2] * ir;
+    w[k] = Q[k][3] * ir;
+    const float ke = 0.5f * r * (u[k] * u[k] + v[k] * v[k] + w[k] * w[k]);
+    const float sc = M[k][4] + ke;
+    const float p = gm1 * (Q[k][4] - ke);
+    if (!(Q[k][4] > tiny + mrg * M[k][4]) || !(p > tiny + mrg * gm1 * sc)) return false;
+    h[k] = (Q[k][4] + p) * ir;
+    hm[k] = (M[k][4] + gm1 * sc) * ir;
+  }
+  const float rho = sqrtf(Q[0][0] * Q[1][0]);
+  const float sg = rho / (Q[0][0] + rho);
+  const float ur = u[0] + sg * (u[1] - u[0]), vr = v[0] + sg * (v[1] - v[0]), wr = w[0] + sg * (w[1] - w[0]);
+  const float hr = h[0] + sg * (h[1] - h[0]);
+  const float v2h = 0.5f * (ur * ur + vr * vr + wr * wr);
+  const float e4 = rho / gamma * (hr + gm1 * v2h);
+  const float ke = rho * v2h;
+  const float sc = rho / gamma * (hm[0] + hm[1] + gm1 * v2h) + ke;
+  const float p = gm1 * (e4 - ke);
+  return rho > 0.0f && e4 > tiny + mrg * sc && p > tiny + mrg * gm1 * sc;
 }
 
 __device__ __forceinline__ int bad_extrap_d(double gamma, const double* Q) {
@@ -1052,14 +1159,16 @@ __device__ __forceinline__ int kneecap5(S* f) {
 // re-evaluates only edges touching a flagged node, after their limiters were
 // zeroed; it returns at once when nothing was flagged.  CHI0: chi = 0, so
 // the MUSCL correction is grad.dx alone (bit-identical to the general form).
-template <class S, int MODE, bool CHI0>
+// EXT (chi = 0): both ends' corrections come from ext, as the limiter pass
+// formed them from the same gradient, instead of the gradient gathers.
+template <class S, int MODE, bool CHI0, bool EXT>
 __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __restrict__ en,
                                                    const typename V4<S>::type* __restrict__ ea,
                                                    const S* __restrict__ eh, const S* __restrict__ q,
                                                    const S* __restrict__ grad, const S* __restrict__ lim, FluxConst kd,
                                                    S* __restrict__ ef, unsigned long long* health,
                                                    int* __restrict__ clipflag, int* __restrict__ clipany,
-                                                   const S* __restrict__ limraw) {
+                                                   const S* __restrict__ limraw, const S* __restrict__ ext) {
   if (MODE == 2 && *(volatile int*)clipany == 0) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nedge) return;
@@ -1073,8 +1182,17 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
 #pragma unroll
   for (int t = 0; t < NEQN; t++) { QL[t] = qL[t]; QR[t] = qR[t]; }
   S h0 = Sc<S>::c(0.0), h1 = h0, h2 = h0;
-  if (kd.ho || kd.viscous) { h0 = eh[3 * (size_t)e]; h1 = eh[3 * (size_t)e + 1]; h2 = eh[3 * (size_t)e + 2]; }
-  if (kd.ho) {
+  if (!EXT && (kd.ho || kd.viscous)) { h0 = eh[3 * (size_t)e]; h1 = eh[3 * (size_t)e + 1]; h2 = eh[3 * (size_t)e + 2]; }
+  if (EXT) {
+    const S* xe = &ext[(size_t)e * (2 * NEQN)];
+    const S* lL = &lim[(size_t)n.x * NEQN];
+    const S* lR = &lim[(size_t)n.y * NEQN];
+#pragma unroll
+    for (int t = 0; t < NEQN; t++) {
+      QL[t] = qL[t] + xe[t] * lL[t];
+      QR[t] = qR[t] + xe[NEQN + t] * lR[t];
+    }
+  } else if (kd.ho) {
     const S* gL = &grad[(size_t)n.x * NTERMS * 3];
     const S* gR = &grad[(size_t)n.y * NTERMS * 3];
     const S* lL = &lim[(size_t)n.x * NEQN];
@@ -1101,8 +1219,17 @@ __global__ void __launch_bounds__(128) k_edge_flux(int nedge, const int2* __rest
   if (MODE == 1 && kd.clip && ((clipflag[n.x] | clipflag[n.y]) & 2)) {
     // an endpoint had negative raw limiter values, which the clip sees
     // before they are clamped: test the states it would build
-    bad = clip_check(qL, qR, &grad[(size_t)n.x * NTERMS * 3], &grad[(size_t)n.y * NTERMS * 3],
-                     &limraw[(size_t)n.x * NEQN], &limraw[(size_t)n.y * NEQN], h0, h1, h2, k.chi, k.gamma);
+    if (EXT) {
+      // from the stored corrections; an FP32 pass clears the edge when its
+      // states are far from every threshold, the exact test decides the rest
+      const S* xe = &ext[(size_t)e * (2 * NEQN)];
+      const S* rl = &limraw[(size_t)n.x * NEQN];
+      const S* rr = &limraw[(size_t)n.y * NEQN];
+      bad = clip_clear_f32(qL, qR, xe, rl, rr, (float)kd.gamma) ? 0 : clip_check_ext(qL, qR, xe, rl, rr, k.gamma);
+    } else {
+      bad = clip_check(qL, qR, &grad[(size_t)n.x * NTERMS * 3], &grad[(size_t)n.y * NTERMS * 3],
+                       &limraw[(size_t)n.x * NEQN], &limraw[(size_t)n.y * NEQN], h0, h1, h2, k.chi, k.gamma);
+    }
   }
   if (MODE == 1 && kd.clip && bad) {
     if (bad & 5) atomicOr(&clipflag[n.x], 1);
@@ -1360,7 +1487,8 @@ void free_solver(Solver* s) {
                   s->d_norms, s->d_health, s->d_clipflag, s->d_clipany, s->d_bind, s->d_limraw,
                   s->d_ia, s->d_ja, s->d_pos_lr, s->d_pos_rl, s->d_M, s->d_diag, s->d_dlu, s->d_dinv, s->d_piv,
                   s->d_bblk, s->d_dt, s->d_x, s->d_xf, s->d_diagf, s->d_dinvf, s->d_wd, s->d_dotsf, s->d_mdot_done, s->d_scal, s->d_color_rows, s->d_cptr, s->d_rowdesc, s->d_mv, s->d_gbar, s->d_sgs_err, s->d_V, s->d_Z, s->d_w, s->d_dots,
-                  s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba};
+                  s->f_q, s->f_grad, s->f_lim, s->f_limraw, s->f_eh, s->f_lsq, s->f_ef, s->f_bf, s->f_ea, s->f_ba,
+                  s->d_ext, s->f_ext};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -1561,6 +1689,7 @@ int run_gradient_t(Solver* s, RBuf<S> r) {
 int run_gradient(Solver* s, int arith = 0) {
   int rc = prep_state(s, arith);
   if (rc) return rc;
+  s->ext_ready = 0;  // formed from the previous gradient
   rc = arith ? run_gradient_t(s, rbuf_f(s)) : run_gradient_t(s, rbuf_d(s));
   if (rc == PCFD_OK) {
     s->have_grad = 1;
@@ -1570,16 +1699,34 @@ int run_gradient(Solver* s, int arith = 0) {
 }
 
 template <class S>
+S*& ext_buf(Solver* s);
+template <>
+double*& ext_buf<double>(Solver* s) { return s->d_ext; }
+template <>
+dfl*& ext_buf<dfl>(Solver* s) { return s->f_ext; }
+
+template <class S>
 int run_venkat_t(Solver* s, RBuf<S> r, bool clip) {
   double K = s->prm.venkat_K;
   const bool c0 = s->prm.chi == 0.0;
   auto kern = s->prm.limiter == 1 ? (c0 ? k_venkat<S, 1, true> : k_venkat<S, 1, false>)
               : s->prm.limiter == 2 ? (c0 ? k_venkat<S, 2, true> : k_venkat<S, 2, false>)
                                     : (c0 ? k_venkat<S, 3, true> : k_venkat<S, 3, false>);
+  // the MUSCL corrections of every edge end, for the residual's edge pass
+  // (chi = 0, and not for the explicit-clip form)
+  S* ext = nullptr;
+  if (c0 && !clip) {
+    S*& buf = ext_buf<S>(s);
+    if (!buf) {
+      int rc = dalloc(&buf, (size_t)s->nedge * 2 * NEQN);
+      if (rc) return rc;
+    }
+    ext = buf;
+  }
   return launch(s, T_LIMITER, [&] {
     kern<<<nblk(s->nnode, 128), 128, 0, s->stream>>>(s->nnode, s->d_nptr, s->d_nedg, s->d_nnbr, r.q, r.grad, r.eh,
                                                      s->d_vol, s->prm.chi, K * K * K, r.limraw,
-                                                     clip ? nullptr : r.lim, s->d_clipflag);
+                                                     clip ? nullptr : r.lim, s->d_clipflag, ext);
   });
 }
 
@@ -1604,6 +1751,7 @@ int run_limiter(Solver* s, bool clip, int arith = 0) {
     return PCFD_OK;
   }
   if (!s->have_grad || s->grad_arith != arith) return set_err(PCFD_ERR_STATE, "limiter: gradient not computed");
+  s->ext_ready = 0;
   int rc = arith ? run_venkat_t(s, rbuf_f(s), clip) : run_venkat_t(s, rbuf_d(s), clip);
   if (rc) return rc;
   if (!clip) {
@@ -1612,6 +1760,8 @@ int run_limiter(Solver* s, bool clip, int arith = 0) {
     s->lim_arith = arith;
     s->lim_clipped = 0;
     s->lim_fresh = 1;
+    s->ext_ready = s->prm.chi == 0.0;
+    s->ext_arith = arith;
     return PCFD_OK;
   }
   rc = launch(s, T_LIMITER, [&] {
@@ -1628,13 +1778,19 @@ int run_limiter(Solver* s, bool clip, int arith = 0) {
 }
 
 template <class S>
-int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
+int run_residual_t(Solver* s, RBuf<S> r, FluxConst k, const S* ext) {
   const bool c0 = s->prm.chi == 0.0;
-  auto flux1 = c0 ? k_edge_flux<S, 1, true> : k_edge_flux<S, 1, false>;
-  auto flux2 = c0 ? k_edge_flux<S, 2, true> : k_edge_flux<S, 2, false>;
+  // with the limiter pass's stored corrections (ext) the edge pass reads
+  // them instead of gathering both ends' gradients
+  auto flux1 = ext  ? k_edge_flux<S, 1, true, true>
+               : c0 ? k_edge_flux<S, 1, true, false>
+                    : k_edge_flux<S, 1, false, false>;
+  auto flux2 = ext  ? k_edge_flux<S, 2, true, true>
+               : c0 ? k_edge_flux<S, 2, true, false>
+                    : k_edge_flux<S, 2, false, false>;
   int rc = launch(s, T_EDGEFLUX, [&] {
     flux1<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k, r.ef,
-                                                      s->d_health, s->d_clipflag, s->d_clipany, r.limraw);
+                                                      s->d_health, s->d_clipflag, s->d_clipany, r.limraw, ext);
   });
   if (rc) return rc;
   if (k.clip) {
@@ -1644,7 +1800,7 @@ int run_residual_t(Solver* s, RBuf<S> r, FluxConst k) {
     if (rc) return rc;
     rc = launch(s, T_CLIP, [&] {
       flux2<<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, r.ea, r.eh, r.q, r.grad, r.lim, k, r.ef,
-                                                        s->d_health, s->d_clipflag, s->d_clipany, r.limraw);
+                                                        s->d_health, s->d_clipflag, s->d_clipany, r.limraw, ext);
     });
     if (rc) return rc;
   }
@@ -1683,8 +1839,11 @@ int run_residual(Solver* s, int arith = 0, bool first_order = false) {
   if (s->lim_clipped) k.clip = 0;  // the explicit clip already ran
   int rc = prep_state(s, arith);
   if (rc) return rc;
-  rc = arith ? run_residual_t(s, rbuf_f(s), k) : run_residual_t(s, rbuf_d(s), k);
+  const bool ext = k.ho && s->ext_ready && s->ext_arith == arith;
+  rc = arith ? run_residual_t(s, rbuf_f(s), k, ext ? s->f_ext : nullptr)
+             : run_residual_t(s, rbuf_d(s), k, ext ? s->d_ext : nullptr);
   s->lim_fresh = 0;  // the pressure clip belongs to the limiter evaluation it follows
+  s->ext_ready = 0;
   return rc;
 }
 
@@ -1760,9 +1919,14 @@ int run_jacobian_t(Solver* s) {
   JacConst jk = make_jac_const(s);
   BcConst bk = make_bc_const(s);
   // inviscid differences on the state before the conditions, viscous blocks
-  // on the state after them (ComputeSpatialJacobian's order)
+  // on the state after them (ComputeSpatialJacobian's order).  The flux
+  // differences run in double-float when the residual does, and whenever
+  // the matrix is stored in FP32 or BF16: their ~48-bit significand carries
+  // the difference quotient (step 1e-8) to about 3e-7, the order of FP32
+  // storage's own rounding, at the FP32 pipes' rate.
+  const bool dfj = s->arith || !std::is_same<T, double>::value;
   int rc = launch(s, T_JAC_EDGE, [&] {
-    if (s->arith)
+    if (dfj)
       k_jac_edge_df<T><<<nblk(s->nedge, 128), 128, 0, s->stream>>>(s->nedge, s->d_en, s->d_ea, s->d_eh, s->d_qpre,
                                                                   s->d_q, s->d_pos_lr, s->d_pos_rl, jk, M,
                                                                   s->d_health);
@@ -1778,7 +1942,7 @@ int run_jacobian_t(Solver* s) {
       if (s->bc_sequential)
         k_jac_bedge_sequential<<<1, 1, 0, s->stream>>>(s->nbedge, s->d_bn, s->d_ba, s->d_bbc, s->d_btw, s->d_bnrm, bk,
                                                        s->prm.jac_boundary_eval, s->d_qpre, s->d_bblk, s->d_health);
-      else if (s->arith)
+      else if (dfj)
         k_jac_bedge_df<<<nblk(nth, 128), 128, 0, s->stream>>>(nth, sl, s->d_bn, s->d_ba, s->d_bbc, s->d_btw,
                                                              s->d_bnrm, bk, s->prm.jac_boundary_eval, s->d_qpre,
                                                              s->d_bblk, s->d_health);
@@ -3445,6 +3609,49 @@ PCFD_API int pcfd_bench_spmv(pcfd_solver_t h, int nrep, int vec_precision, doubl
   if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("bench spmv: ") + cudaGetErrorString(ce));
   *ms_out = ms;
   return PCFD_OK;
+}
+
+PCFD_API int pcfd_bench_sgs(pcfd_solver_t h, int nrep, int nsweeps, int vec_precision, double* ms_out) {
+  Solver* s = (Solver*)h;
+  if (!s || nrep <= 0 || nsweeps <= 0 || !ms_out || vec_precision < 0 || vec_precision > 1)
+    return set_err(PCFD_ERR_ARG, "pcfd_bench_sgs: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_bench_sgs: no Jacobian assembled");
+  if (vec_precision == 1 && s->jac_prec == 0)
+    return set_err(PCFD_ERR_STATE, "pcfd_bench_sgs: FP32 vectors need FP32 or BF16 matrix storage");
+  const long long n = (long long)s->nnode * NEQN;
+  if (!s->d_mv) {
+    int rc = dalloc(&s->d_mv, (size_t)2 * n + (size_t)n + 4);
+    if (rc) return rc;
+  }
+  double* xd = s->d_mv + n;
+  float* bf = (float*)(s->d_mv + 2 * n);
+  float* xf = bf + n + 4;
+  // the right-hand side is the last residual (its values do not change the
+  // sweeps' work)
+  int rc = PCFD_OK;
+  if (vec_precision == 1) rc = launch(s, T_SGS, [&] { k_to_f32<<<kNormBlocks, 256, 0, s->stream>>>(n, s->d_b, bf); });
+  if (rc) return rc;
+  CUDA_TRY(cudaMemsetAsync(xd, 0, n * sizeof(double), s->stream));
+  CUDA_TRY(cudaMemsetAsync(xf, 0, n * sizeof(float), s->stream));
+  int saved = s->profile;
+  s->profile = 0;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaEventRecord(e0, s->stream));
+  for (int it = 0; it < nrep && rc == PCFD_OK; it++)
+    rc = vec_precision ? run_sgs_f(s, nsweeps, bf, xf) : run_sgs(s, nsweeps, s->d_b, xd, nullptr);
+  cudaEventRecord(e1, s->stream);
+  cudaError_t ce = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->profile = saved;
+  if (rc) return rc;
+  if (ce != cudaSuccess) return set_err(PCFD_ERR_CUDA, std::string("bench sgs: ") + cudaGetErrorString(ce));
+  *ms_out = ms;
+  return check_sweeps(s);
 }
 
 PCFD_API int pcfd_sgs_rhs(pcfd_solver_t h, int nsweeps, const double* b, double* x_out, int vec_precision) {

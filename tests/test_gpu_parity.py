@@ -93,7 +93,7 @@ def test_full_size_freestream_and_determinism():
     case = cases.ns_flatplate(128, 96, 96)
     p = case.param
     p.bc_type = {1: N.BC_FARFIELD, 2: N.BC_FARFIELD, 3: N.BC_FARFIELD, 4: N.BC_FARFIELD,
-                 5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY}
+                 5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY, 7: N.BC_FARFIELD}
     m = cases.build_mesh(case)
     S = SolutionSpace(m, p)
     nrows = m.nnode + m.nbedge
@@ -191,7 +191,7 @@ def test_double_float_full_size_freestream():
     case = cases.ns_flatplate(128, 96, 96)
     p = case.param
     p.bc_type = {1: N.BC_FARFIELD, 2: N.BC_FARFIELD, 3: N.BC_FARFIELD, 4: N.BC_FARFIELD,
-                 5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY}
+                 5: N.BC_SYMMETRY, 6: N.BC_SYMMETRY, 7: N.BC_FARFIELD}
     m = cases.build_mesh(case)
     S = SolutionSpace(m, p)
     S.set_residual_arithmetic(1)
