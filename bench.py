@@ -203,11 +203,14 @@ def run_reference(args, rank, pg):
 
 # The convergence study.  Every arm starts from the same state: a shared
 # start-up of CONV_PREFIX["steps"] plain FP64 steps (first order, then second
-# order with the limiter live, CFL ramped from 1) that ends with the limiter
-# frozen (limiterFreeze, ucs/solutionSpace.tcc:681).  From there all arms solve
-# the same discrete equations with the same frozen limiter, and differ only
-# in the linear solve and its arithmetic; the Newton residual, gradients,
-# limiter and norms stay FP64 in every arm.
+# order with the limiter live, CFL ramped from 1 to 20) that ends with the
+# limiter frozen (limiterFreeze, ucs/solutionSpace.tcc:681).  From there all
+# arms solve the same discrete equations with the same frozen limiter, and
+# differ only in the linear solve and its arithmetic; the Newton residual,
+# gradients, limiter and norms stay FP64 in every arm.  Each arm ramps its
+# CFL linearly from the start-up's 20 to its own over CONV_RAMP steps.  (On
+# the 256x176x176 box a start-up ramping to 50 diverged within a few steps of
+# the switch to second order; ramping to 20 does not.)
 #   fp64:  the reference's method, block-SGS sweeps on the FP64 Jacobian; 30
 #          sweeps at CFL 1000 were the fastest of the settings tried on the
 #          128x96x96 box (10 sweeps at CFL 200, 20 at CFL 1000, 30 at CFL 3000
@@ -220,8 +223,11 @@ def run_reference(args, rank, pg):
 #   mixed_learned: mixed with the learned correction on the first Krylov
 #          direction of each cycle (the residual itself, the right-hand side
 #          the network is trained on)
-CONV_PREFIX = dict(steps=60, cfl=50.0, cfl_start=1.0, cfl_ramp_steps=40, nsgs=10, first_order_steps=20,
+#   mixed_learned_aug: mixed with the learned vector of each cycle's residual
+#          direction as the cycle's second direction, after plain SGS of it
+CONV_PREFIX = dict(steps=100, cfl=20.0, cfl_start=1.0, cfl_ramp_steps=60, nsgs=10, first_order_steps=20,
                    linear_solver=0, jac_precision=0)
+CONV_RAMP = 50
 _MIXED = dict(nsgs=2, linear_solver=1, fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1,
               first_order_steps=20)
 CONV_ARMS = {
@@ -231,6 +237,7 @@ CONV_ARMS = {
     "mixed_s1": dict(_MIXED, cfl=300.0, nsgs=1),
     "mixed_bf16": dict(_MIXED, cfl=1000.0, jac_precision=2),
     "mixed_learned": dict(_MIXED, cfl=1000.0, linear_solver=2, lp_directions=1),
+    "mixed_learned_aug": dict(_MIXED, cfl=1000.0, linear_solver=3),
 }
 
 
@@ -253,7 +260,9 @@ def train_learned(dims, nruns, steps, every, epochs, lr, seed=1000):
     generates.  Each run draws a flow (Mach ~ U[0.5, 2], angle of attack ~
     U[-5, 5] degrees, Re ~ log-U[1e4, 1e6]) on a box of the family with its
     own mesh and state seeds (none is the study's), runs the mixed method
-    from the perturbed freestream, and every `every` steps stores the pair
+    from the perturbed freestream through the study's schedule (CFL ramped
+    to 20 over the start-up, limiter frozen at its end, then ramped to the
+    arms' CFL), and every `every` steps after the start-up stores the pair
     (residual, Newton update solved to 1e-6) with its first Krylov pairs.
     The network trains on each run's pairs in turn (Adam), carrying its
     parameters from run to run.  A run whose state stops being finite
@@ -273,13 +282,19 @@ def train_learned(dims, nruns, steps, every, epochs, lr, seed=1000):
         if w is not None:
             S.lp_set_params(w)
         npairs, ok = 0, True
+        P = CONV_PREFIX["steps"]
         for it in range(steps):
-            rep = S.newton_iterate(it, **dict(_MIXED, cfl=100.0, cfl_start=1.0, cfl_ramp_steps=40,
-                                              limiter_freeze=CONV_PREFIX["steps"]))
+            if it < P:
+                opts = dict(_MIXED, cfl=CONV_PREFIX["cfl"], cfl_start=CONV_PREFIX["cfl_start"],
+                            cfl_ramp_steps=CONV_PREFIX["cfl_ramp_steps"])
+            else:
+                c0, c1 = CONV_PREFIX["cfl"], CONV_ARMS["mixed"]["cfl"]
+                opts = dict(_MIXED, cfl=c0 + (c1 - c0) * min(1.0, (it - P + 1) / CONV_RAMP))
+            rep = S.newton_iterate(it, limiter_freeze=P, **opts)
             if not np.isfinite(rep["res"][0]):
                 ok = False
                 break
-            if it >= 10 and it % every == 0:
+            if it >= P and (it - P) % every == 0:
                 try:
                     npairs = S.lp_collect(nsgs=_MIXED["nsgs"], rtol=1e-6, krylov_pairs=2)
                 except Exception as exc:  # a linear system the solve cannot reach 1e-6 on
@@ -316,7 +331,7 @@ def converge_study(args):
     if "mixed_learned" in args.converge_arms:
         tdims = WORKLOADS[args.learned_train_workload]
         lp_w, out["learned_training"] = train_learned((tdims["nx"], tdims["ny"], tdims["nz"]), args.learned_runs,
-                                                      90, 10, 30, 2e-3)
+                                                      CONV_PREFIX["steps"] + 60, 10, 30, 2e-3)
     # the shared start-up
     P = CONV_PREFIX["steps"]
     S = SolutionSpace(m, case.param)
@@ -338,7 +353,7 @@ def converge_study(args):
         S = SolutionSpace(m, case.param)
         S.set_state(q_pre)
         S.set_limiter(lim_pre)
-        if arm["linear_solver"] == 2:
+        if arm["linear_solver"] >= 2:
             S.lp_init(1)
             if lp_w is not None:
                 S.lp_set_params(lp_w)
@@ -347,7 +362,9 @@ def converge_study(args):
         t0 = time.perf_counter()
         it = P
         while True:
-            rep = S.newton_iterate(it, limiter_freeze=P, **arm)
+            c0, c1 = CONV_PREFIX["cfl"], arm["cfl"]
+            cfl = c0 + (c1 - c0) * min(1.0, (it - P + 1) / CONV_RAMP)
+            rep = S.newton_iterate(it, limiter_freeze=P, **dict(arm, cfl=cfl))
             it += 1
             r = rep["res"][0] / r0
             h.append(r)
@@ -367,7 +384,7 @@ def converge_study(args):
         S.profile(True)
         S.profile_reset()
         for k in range(3):
-            S.newton_iterate(it + k, limiter_freeze=P, **arm)
+            S.newton_iterate(it + k, limiter_freeze=P, **dict(arm, cfl=cfl))
         tm = S.timers()
         S.profile(False)
         rec = {"steps_after_startup": len(h), "wall_s_after_startup": round(wall, 3),
@@ -563,7 +580,7 @@ def chemistry_study(args):
 
 
 def run_gb300(args, ws, rank, local, pg):
-    from proteuscfd_gb300 import SolutionSpace, cases
+    from proteuscfd_gb300 import Mesh, SolutionSpace, cases
     from proteuscfd_gb300 import _native as N
     lib = N.load()
     N.check(lib.pcfd_set_device(local), "pcfd_set_device")
@@ -720,6 +737,35 @@ def run_gb300(args, ws, rank, local, pg):
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_sample(12.0, os.cpu_count() or 1)
         line["cpu_baseline"] = base
+
+    # node numbering: the FP64 residual on the same box numbered by the
+    # reference's set-up reorder (its reverse Cuthill-McKee list used as an
+    # old-to-new map, ucs/mesh.tcc:224) and by that sequence itself
+    def order_entry(S_, ms_):
+        S_.profile(True)
+        S_.profile_reset()
+        S_.residual_full()
+        t = S_.timers()
+        S_.profile(False)
+        return {"ms_per_step": ms_, "edge_flux_ms": t["edge_flux"][0], "lsq_gradient_ms": t["lsq_gradient"][0],
+                "venkat_limiter_ms": t["venkat_limiter"][0], "edge_viscous_ms": t["edge_viscous"][0]}
+
+    S.set_state(q0)
+    S.set_residual_arithmetic(0)
+    line["node_order"] = {"what": "FP64 residual, ms per evaluation and its largest kernels, by node numbering",
+                          "natural": order_entry(S, ms_per_step)}
+    if not args.no_node_order:
+        for name, ro in (("reference_reorder", True), ("rcm", "rcm")):
+            t0 = time.perf_counter()
+            m2 = Mesh.box(w["nx"], w["ny"], w["nz"], reorder=ro, **case.mesh_kw)
+            tb = time.perf_counter() - t0
+            S2 = SolutionSpace(m2, case.param)
+            S2.set_state(cases.perturbed_state(S2.qinf(), m2.nnode + m2.nbedge, seed=1))
+            S2.bench_residual_full(3)
+            ms2, _ = S2.bench_residual_full(args.steps)
+            line["node_order"][name] = dict(order_entry(S2, ms2 / args.steps), mesh_build_s=round(tb, 2))
+            S2.close()
+            del m2
     # the FP32 block SpMV of the mixed solver on this machine's matrix: one mixed
     # Newton step assembles it (FP32 storage), then K device-timed products
     # on resident vectors (the matrix is larger than L2)
@@ -790,6 +836,7 @@ def main():
     ap.add_argument("--learned-runs", type=int, default=4, help="training runs (sampled flows)")
     ap.add_argument("--converge-only", action="store_true", help="run only the convergence study")
     ap.add_argument("--no-chemistry", action="store_true", help="skip the finite-rate chemistry measurement")
+    ap.add_argument("--no-node-order", action="store_true", help="skip the residual on the renumbered meshes")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.converge_arms = [a for a in args.converge.split(",") if a]

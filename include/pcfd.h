@@ -275,7 +275,10 @@ typedef struct pcfd_newton_opts {
   int jac_precision;    /* 0 FP64, 1 FP32, 2 BF16 off-diagonal storage */
   int linear_solver;    /* 0 block SGS (the reference's), 1 FGMRES preconditioned by SGS,
                            2 FGMRES preconditioned by SGS plus the learned correction
-                           (pcfd_lp_*), with plain SGS-preconditioned FGMRES as the fallback */
+                           (pcfd_lp_*), with plain SGS-preconditioned FGMRES as the fallback,
+                           3 FGMRES preconditioned by SGS whose second direction in each cycle
+                           is the learned vector of the cycle's residual direction (the space
+                           holds plain SGS's first direction too, so no fallback) */
   int fgmres_m;         /* Krylov dimension per restart (FGMRES) */
   int fgmres_restarts;  /* restarts (FGMRES) */
   double fgmres_rtol;   /* relative tolerance (FGMRES) */
@@ -366,6 +369,7 @@ PCFD_API int pcfd_lp_apply(pcfd_solver_t s, int nsgs, const double* v, double* z
 #define PCFD_CHEM_MAX_SPECIES 16
 #define PCFD_CHEM_MAX_REACTIONS 32
 #define PCFD_CHEM_MAX_LOCAL 16
+#define PCFD_CHEM_MAX_TRANSPORT_FITS 4
 
 typedef struct pcfd_chem_reaction {
   int type;          /* Reaction::rxnType: 0 Arrhenius, 1 ModArrhenius, 2 GuptaModArrhenius, 3 Power */
@@ -385,6 +389,17 @@ typedef struct pcfd_chem_model {
   double nasa_hi[PCFD_CHEM_MAX_SPECIES][7];  /* above 1000 K (and above 6000 K) */
   int nreactions;
   pcfd_chem_reaction rx[PCFD_CHEM_MAX_REACTIONS];
+  /* transport (Species::GetViscosity / GetThermalConductivity,
+   * ucs/species.tcc:393,430): NASA RP-1311 fits ln(y) = A ln T + B/T + C/T^2 + D,
+   * rows {T_lo, T_hi, A, B, C, D}, viscosity in micropoise, conductivity in
+   * microwatt/(cm K); the last row whose range holds T is used.  At or below
+   * 1000 K every species takes White's Sutherland forms instead, as the
+   * reference does.  nmu/nk = 0: no transport data (the viscous flux is then
+   * refused). */
+  int nmu[PCFD_CHEM_MAX_SPECIES];
+  double mu_fit[PCFD_CHEM_MAX_SPECIES][PCFD_CHEM_MAX_TRANSPORT_FITS][6];
+  int nk[PCFD_CHEM_MAX_SPECIES];
+  double k_fit[PCFD_CHEM_MAX_SPECIES][PCFD_CHEM_MAX_TRANSPORT_FITS][6];
 } pcfd_chem_model;
 
 typedef struct pcfd_chem_s* pcfd_chem_t;
@@ -403,6 +418,9 @@ PCFD_API int pcfd_chem_production_rates_dev(pcfd_chem_t c, long long n, const do
  * with these scales (Param::ref_*, ucs/param.tcc:372-397). */
 typedef struct {
   double density, pressure, temperature, specific_enthalpy, velocity;
+  /* Param::ref_viscosity and ref_k (inputs refViscosity, refThermalConductivity,
+   * ucs/param.tcc:210-211; default 1, and 0 here reads as 1) */
+  double viscosity, conductivity;
 } pcfd_chem_ref;
 /* With dev = 0 the arrays are host arrays (copied through the handle's
  * buffers); with dev = 1 they are device arrays, used in place on the
@@ -413,6 +431,14 @@ typedef struct {
 PCFD_API int pcfd_chem_find_T_given_P(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi,
                                       const double* P, const double* T_init, double* T, long long* nonconverged,
                                       int dev);
+/* GetMolecularViscosity / GetThermalConductivity (ucs/compressibleFR.tcc:
+ * 1580,1590): the mixture's viscosity and conductivity by Wilke's rule
+ * (ChemModel::WilkesMixtureRule, ucs/chem.tcc:876) from non-dimensional
+ * rhoi [n][ns] and T [n], returned non-dimensional (over ref->viscosity and
+ * ref->conductivity).  A temperature above every fit's range returns
+ * PCFD_ERR_ARG (the reference aborts). */
+PCFD_API int pcfd_chem_transport(pcfd_chem_t c, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                 const double* T, double* mu, double* k, int dev);
 /* ConservativeToNative (:2133): the FP64 temperature Newton from total
  * energy.  q [n][ns+4] = (rhoi, rho u, rho v, rho w, rho Et), P [n] the
  * stored pressure (initial guess) -> native [n][4] = (u, v, w, T).  Returns
@@ -482,6 +508,22 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t c, const pcfd_mesh_view* m);
  * (optional; ParallelL2Norm and StridedParallelL2Norm).  dev as above (q, b). */
 PCFD_API int pcfd_chem_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
                                 double ref_time, int reactions, const double* q, double* b, double* norms, int dev);
+/* The viscous part of the reacting residual on the attached mesh:
+ * Kernel_Viscous_Flux and Bkernel_Viscous_Flux (ucs/residual.tcc:390,473)
+ * with CompressibleFREqnSet::ViscousFlux (ucs/compressibleFR.tcc:551), laminar,
+ * no species diffusion, mixture viscosity and conductivity as
+ * pcfd_chem_transport forms them.  q as for pcfd_chem_residual; grad
+ * [nnode][2 ns + 4][3] the node gradients of the reacting gradient list
+ * (rhoi, u, v, w, T, concentrations; GetGradientsLocation, :693); Re
+ * Param::Re; directional: 1 for the directional correction of the face
+ * gradient along each edge (second order past the first-order steps), which
+ * needs the attached mesh's coordinates.  b [nnode][ns + 4] receives the
+ * viscous contributions alone, summed per node in ascending edge order then
+ * half-edges; the caller adds them to pcfd_chem_residual's.  A face above
+ * every transport fit's range returns PCFD_ERR_ARG.  dev as above (q, grad, b). */
+PCFD_API int pcfd_chem_viscous_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                        double Re, int directional, const double* q, const double* grad, double* b,
+                                        int dev);
 
 /* Arithmetic of the composite residual calls (pcfd_residual_full,
  * pcfd_bench_residual_full, pcfd_newton_step): 0 FP64 (default), 1

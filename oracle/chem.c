@@ -578,3 +578,194 @@ void oracle_chem_temporal_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, 
   for (long long p = 0; p < n; p++)
     oracle_chem_temporal(m, ref, q + p * nv, vol[p], cnp1, dt, dtau[p], beta[p], local_ts, A + p * neqn * neqn);
 }
+
+/* ---- transport ------------------------------------------------------------
+ * Species<T>::GetViscosity / GetThermalConductivity (ucs/species.tcc:393,430):
+ * at or below 1000 K White's Sutherland forms with air's constants for every
+ * species (ucs/species.tcc:13-22), above it the last NASA RP-1311 fit whose
+ * range holds T, ln(y) = A ln T + B/T + C/T^2 + D, converted from micropoise
+ * and microwatt/(cm K).  *err is set when no fit holds T (the reference
+ * aborts). */
+static double transport_fit(const double (*fit)[6], int nfit, double T, double conv, int* err) {
+  int range = -1;
+  for (int i = 0; i < nfit; i++)
+    if (T >= fit[i][0] && T <= fit[i][1]) range = i;
+  if (range < 0) {
+    *err = 1;
+    return 0.0;
+  }
+  const double* c = fit[range];
+  const double ly = c[2] * log(T) + c[3] / T + c[4] / (T * T) + c[5];
+  return exp(ly) * conv;
+}
+
+static double species_mu(const pcfd_chem_model* m, int s, double T, int* err) {
+  if (T <= 1000.0) {
+    const double mu0 = 1.716e-5, T0 = 273.0, S = 111.0;
+    return mu0 * pow(T / T0, 1.5) * ((T0 + S) / (T + S));
+  }
+  return transport_fit((const double(*)[6])m->mu_fit[s], m->nmu[s], T, 1.0e-7, err);
+}
+
+static double species_k(const pcfd_chem_model* m, int s, double T, int* err) {
+  if (T <= 1000.0) {
+    const double k0 = 0.0241, T0 = 273.0, S = 194.0;
+    return k0 * pow(T / T0, 1.5) * ((T0 + S) / (T + S));
+  }
+  return transport_fit((const double(*)[6])m->k_fit[s], m->nk[s], T, 1.0e-4, err);
+}
+
+/* ChemModel<T>::WilkesMixtureRule (ucs/chem.tcc:876) with
+ * MassFractionToMoleFraction (:941): mole fractions from mass fractions, the
+ * last one 1 - the sum of the others; the weights always use the species'
+ * viscosities, whatever property is mixed. */
+static double wilke(const pcfd_chem_model* m, const double* rhoi, const double* prop, double T, int* err) {
+  const int ns = m->nspecies;
+  double rho = 0.0, X[PCFD_CHEM_MAX_SPECIES], visc[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rho += rhoi[i];
+  double summ = 0.0;
+  for (int i = 0; i < ns; i++) {
+    X[i] = (rhoi[i] / rho) / m->mw[i];
+    summ += X[i];
+  }
+  for (int i = 0; i < ns; i++) X[i] /= summ;
+  summ = 0.0;
+  for (int i = 0; i < ns - 1; i++) summ += X[i];
+  X[ns - 1] = 1.0 - summ;
+  for (int i = 0; i < ns; i++) visc[i] = species_mu(m, i, T, err);
+  const double sqrt8 = sqrt(8.0);
+  double mix = 0.0;
+  for (int i = 0; i < ns; i++) {
+    double wi = 0.0;
+    for (int j = 0; j < ns; j++) {
+      const double temp = 1.0 + sqrt(visc[i] / visc[j]) * pow(m->mw[j] / m->mw[i], 0.25);
+      const double phi = pow(1.0 + m->mw[i] / m->mw[j], -0.5) * temp * temp / sqrt8;
+      wi += X[j] * phi;
+    }
+    mix += (X[i] / wi) * prop[i];
+  }
+  return mix;
+}
+
+/* CompressibleFREqnSet<T>::GetMolecularViscosity / GetThermalConductivity
+ * (ucs/compressibleFR.tcc:1580,1590): non-dimensional rhoi and T in, the
+ * mixture values over ref_viscosity and ref_k out.  Returns 1 when T is
+ * above every fit's range. */
+int oracle_chem_transport(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T,
+                          double* mu, double* k) {
+  const int ns = m->nspecies;
+  double rd[PCFD_CHEM_MAX_SPECIES], pm[PCFD_CHEM_MAX_SPECIES], pk[PCFD_CHEM_MAX_SPECIES];
+  int err = 0;
+  for (int i = 0; i < ns; i++) rd[i] = rhoi[i] * ref->density;
+  const double Td = T * ref->temperature;
+  for (int i = 0; i < ns; i++) {
+    pm[i] = species_mu(m, i, Td, &err);
+    pk[i] = species_k(m, i, Td, &err);
+  }
+  const double rv = ref->viscosity != 0.0 ? ref->viscosity : 1.0;
+  const double rk = ref->conductivity != 0.0 ? ref->conductivity : 1.0;
+  *mu = wilke(m, rd, pm, Td, &err) / rv;
+  *k = wilke(m, rd, pk, Td, &err) / rk;
+  return err;
+}
+
+long long oracle_chem_transport_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                  const double* T, double* mu, double* k) {
+  long long bad = 0;
+  for (long long i = 0; i < n; i++)
+    bad += oracle_chem_transport(m, ref, rhoi + (size_t)i * m->nspecies, T[i], mu + i, k + i);
+  return bad;
+}
+
+/* ---- viscous flux ---------------------------------------------------------
+ * CompressibleFREqnSet<T>::ViscousFlux (ucs/compressibleFR.tcc:551) on the
+ * face state Q (native record: rhoi, u, v, w, T) with the face gradient g of
+ * the reacting set's gradient list (rhoi, u, v, w, T, concentrations; three
+ * entries each), laminar (no turbulent viscosity, so the turbulent
+ * conductivity term vanishes), no species diffusion. */
+static void fr_viscous_flux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                            double Re, const double* Q, const double* g, const double* avec, double* flux, int* err) {
+  const int ns = m->nspecies, off = 3 * ns;
+  const double ux = g[off + 0], uy = g[off + 1], uz = g[off + 2];
+  const double vx = g[off + 3], vy = g[off + 4], vz = g[off + 5];
+  const double wx = g[off + 6], wy = g[off + 7], wz = g[off + 8];
+  const double Tx = g[off + 9], Ty = g[off + 10], Tz = g[off + 11];
+  const double u = Q[ns], v = Q[ns + 1], w = Q[ns + 2];
+  double mu, kc;
+  *err |= oracle_chem_transport(m, ref, Q, Q[ns + 3], &mu, &kc);
+  const double fact = 2.0 / 3.0;
+  const double tauxx = 2.0 * fact * ux - fact * vy - fact * wz;
+  const double tauyy = 2.0 * fact * vy - fact * ux - fact * wz;
+  const double tauzz = 2.0 * fact * wz - fact * ux - fact * vy;
+  const double tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
+  const double RK = avec[3] / Re, RKT = RK * mu;
+  const double k = -kc;
+  const double Tn = Tx * avec[0] + Ty * avec[1] + Tz * avec[2];
+  const double tauxn = -tauxx * avec[0] - tauxy * avec[1] - tauxz * avec[2];
+  const double tauyn = -tauxy * avec[0] - tauyy * avec[1] - tauyz * avec[2];
+  const double tauzn = -tauxz * avec[0] - tauyz * avec[1] - tauzz * avec[2];
+  for (int i = 0; i < ns; i++) flux[i] = 0.0;
+  flux[ns + 0] = RKT * tauxn;
+  flux[ns + 1] = RKT * tauyn;
+  flux[ns + 2] = RKT * tauzn;
+  flux[ns + 3] = RKT * (tauxn * u + tauyn * v + tauzn * w) + RK * k * Tn;
+  if (o->symmetry2D >= 1 && o->symmetry2D <= 3) flux[ns + o->symmetry2D - 1] = 0.0;
+}
+
+/* Kernel_Viscous_Flux / Bkernel_Viscous_Flux (ucs/residual.tcc:390,473) of
+ * the reacting set on one partition: the face state is the average of the
+ * two native records; an interior face takes the average of the two nodes'
+ * gradients, with the directional correction along the edge when
+ * `directional` (second order past the first-order steps); a boundary face
+ * takes its node's gradient.  b [nnode][ns + 4] receives the viscous part of
+ * the residual alone (-F on the left node, +F on the right).  Returns the
+ * number of faces whose temperature was above every transport fit. */
+int oracle_chem_viscous_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                 const pcfd_mesh_view* mv, double Re, int directional, const double* q,
+                                 const double* grad, double* b) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int nn = mv->nnode;
+  double Qa[PCFD_CHEM_MAX_SPECIES + 4], flux[PCFD_CHEM_MAX_SPECIES + 4], g[3 * (2 * PCFD_CHEM_MAX_SPECIES + 4)];
+  int bad = 0;
+  for (size_t i = 0; i < (size_t)nn * neqn; i++) b[i] = 0.0;
+  for (int e = 0; e < mv->nedge; e++) {
+    const int a = mv->edges[2 * e], c = mv->edges[2 * e + 1];
+    const double* qL = q + (size_t)a * nv;
+    const double* qR = q + (size_t)c * nv;
+    for (int i = 0; i < neqn; i++) Qa[i] = (qL[i] + qR[i]) / 2.0;
+    const double* gL = grad + (size_t)a * nt * 3;
+    const double* gR = grad + (size_t)c * nt * 3;
+    for (int i = 0; i < nt * 3; i++) g[i] = 0.5 * (gL[i] + gR[i]);
+    if (directional) {
+      const double* xL = mv->xyz + 3 * (size_t)a;
+      const double* xR = mv->xyz + 3 * (size_t)c;
+      double dx[3], s2 = 0.0;
+      for (int i = 0; i < 3; i++) {
+        dx[i] = xR[i] - xL[i];
+        s2 += dx[i] * dx[i];
+      }
+      for (int j = 0; j < nt; j++) {
+        const int loc = j < ns + 4 ? j : 2 * ns + 6 + (j - ns - 4);
+        const double qdots = dx[0] * g[3 * j] + dx[1] * g[3 * j + 1] + dx[2] * g[3 * j + 2];
+        const double dq = (qR[loc] - qL[loc] - qdots) / s2;
+        for (int i = 0; i < 3; i++) g[3 * j + i] += dq * dx[i];
+      }
+    }
+    int err = 0;
+    fr_viscous_flux(m, ref, o, Re, Qa, g, mv->edge_area + 4 * (size_t)e, flux, &err);
+    bad += err;
+    for (int i = 0; i < neqn; i++) b[(size_t)c * neqn + i] += flux[i];
+    for (int i = 0; i < neqn; i++) b[(size_t)a * neqn + i] += -flux[i];
+  }
+  for (int k = 0; k < mv->nbedge; k++) {
+    const int a = mv->bedges[2 * k], c = mv->bedges[2 * k + 1];
+    const double* qL = q + (size_t)a * nv;
+    const double* qR = q + (size_t)c * nv;
+    for (int i = 0; i < neqn; i++) Qa[i] = 0.5 * (qL[i] + qR[i]);
+    int err = 0;
+    fr_viscous_flux(m, ref, o, Re, Qa, grad + (size_t)a * nt * 3, mv->bedge_area + 4 * (size_t)k, flux, &err);
+    bad += err;
+    for (int i = 0; i < neqn; i++) b[(size_t)a * neqn + i] += -flux[i];
+  }
+  return bad;
+}

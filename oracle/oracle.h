@@ -97,6 +97,13 @@ void oracle_chem_source_jacobian_n(const pcfd_chem_model* m, const pcfd_chem_ref
                                    const double* q, const double* vol, double* A);
 void oracle_chem_temporal(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q, double vol,
                           double cnp1, double dt, double dtau, double beta, int local_ts, double* A);
+int oracle_chem_transport(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* rhoi, double T,
+                          double* mu, double* k);
+long long oracle_chem_transport_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                  const double* T, double* mu, double* k);
+int oracle_chem_viscous_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                 const pcfd_mesh_view* mv, double Re, int directional, const double* q,
+                                 const double* grad, double* b);
 void oracle_chem_temporal_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,
                             const double* vol, const double* dtau, const double* beta, double cnp1, double dt,
                             int local_ts, double* A);

@@ -91,6 +91,7 @@ class NewtonReport(C.Structure):
 CHEM_MAX_SPECIES = 16
 CHEM_MAX_REACTIONS = 32
 CHEM_MAX_LOCAL = 16
+CHEM_MAX_TRANSPORT_FITS = 4
 
 
 class ChemReaction(C.Structure):
@@ -106,6 +107,10 @@ class ChemModelC(C.Structure):
         ("nspecies", C.c_int), ("mw", C.c_double * CHEM_MAX_SPECIES),
         ("nasa_lo", (C.c_double * 7) * CHEM_MAX_SPECIES), ("nasa_hi", (C.c_double * 7) * CHEM_MAX_SPECIES),
         ("nreactions", C.c_int), ("rx", ChemReaction * CHEM_MAX_REACTIONS),
+        ("nmu", C.c_int * CHEM_MAX_SPECIES),
+        ("mu_fit", ((C.c_double * 6) * CHEM_MAX_TRANSPORT_FITS) * CHEM_MAX_SPECIES),
+        ("nk", C.c_int * CHEM_MAX_SPECIES),
+        ("k_fit", ((C.c_double * 6) * CHEM_MAX_TRANSPORT_FITS) * CHEM_MAX_SPECIES),
     ]
 
 
@@ -116,7 +121,8 @@ _LLP = C.POINTER(C.c_longlong)
 class ChemRef(C.Structure):
     """pcfd_chem_ref: the reacting equation set's reference scales."""
     _fields_ = [("density", C.c_double), ("pressure", C.c_double), ("temperature", C.c_double),
-                ("specific_enthalpy", C.c_double), ("velocity", C.c_double)]
+                ("specific_enthalpy", C.c_double), ("velocity", C.c_double), ("viscosity", C.c_double),
+                ("conductivity", C.c_double)]
 
 
 class ChemFluxOpts(C.Structure):
@@ -178,6 +184,9 @@ PROTOTYPES = {
     "pcfd_chem_aux": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, _P, C.c_int]),
     "pcfd_chem_temporal_terms": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _P, _P, _P, _P, C.c_double,
                                            C.c_double, C.c_int, _P, C.c_int]),
+    "pcfd_chem_transport": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _DP, _DP, _DP, _DP, C.c_int]),
+    "pcfd_chem_viscous_residual": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_double, C.c_int,
+                                             _P, _P, _P, C.c_int]),
     "pcfd_chem_source_jacobian": (C.c_int, [_P, C.POINTER(ChemRef), C.c_double, C.c_longlong, _P, _P, _P,
                                             C.c_int]),
     "pcfd_chem_hllc_flux": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_longlong, _P,

@@ -44,17 +44,31 @@ class Mesh:
 
     def __init__(self, handle, reorder=False, nnode=0):
         """Takes ownership of a mesh handle and builds its maps and metrics.
-        ``reorder`` first applies the reference's set-up reorder (reverse
-        Cuthill-McKee from node 0, ``Param::reorder``, on by default in the
-        reference; ucs/solutionSpace.tcc:61-66); ``ordering`` then holds the
-        reference's ``Mesh::ordering`` (old node n is now ordering[n])."""
+        ``reorder`` True first applies the reference's set-up reorder
+        (reverse Cuthill-McKee from node 0, ``Param::reorder``, on by default
+        in the reference; ucs/solutionSpace.tcc:61-66); ``ordering`` then
+        holds the reference's ``Mesh::ordering`` (old node n is now
+        ordering[n]).  ``reorder="rcm"`` numbers the nodes in that reverse
+        Cuthill-McKee sequence instead (new node k is old node ordering[k]),
+        the bandwidth-reducing use of the same list."""
         self._lib = N.load()
         self._h = None
         self.ordering = None
         if not handle:
             raise N.PcfdError(4, "mesh create", self._lib.pcfd_mesh_last_error().decode())
         self._h = handle
-        if reorder:
+        if reorder == "rcm":
+            order = np.zeros(nnode, dtype=np.int32)
+            rc = self._lib.pcfd_mesh_rcm_order(self._h, N.iptr(order))
+            if rc == 0:
+                rc = self._lib.pcfd_mesh_renumber(self._h, N.iptr(order))
+            if rc != 0:
+                msg = self._lib.pcfd_mesh_last_error().decode()
+                self._lib.pcfd_mesh_destroy(self._h)
+                self._h = None
+                raise N.PcfdError(rc, "pcfd_mesh_renumber", msg)
+            self.ordering = order
+        elif reorder:
             order = np.zeros(nnode, dtype=np.int32) if nnode > 0 else None
             rc = self._lib.pcfd_mesh_reorder_rcm(self._h, N.iptr(order) if order is not None else None)
             if rc != 0:

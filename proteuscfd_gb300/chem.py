@@ -27,6 +27,15 @@ def model_struct(spec: dict) -> "N.ChemModelC":
         for i in range(7):
             m.nasa_lo[k][i] = s["lo"][i]
             m.nasa_hi[k][i] = s["hi"][i]
+    for k, s in enumerate(sp):
+        for key, cnt, fit in (("mu", m.nmu, m.mu_fit), ("k", m.nk, m.k_fit)):
+            rows = s.get(key, [])
+            if len(rows) > N.CHEM_MAX_TRANSPORT_FITS:
+                raise ValueError("too many transport fits")
+            cnt[k] = len(rows)
+            for r, row in enumerate(rows):
+                for i in range(6):
+                    fit[k][r][i] = row[i]
     m.nreactions = len(rx)
     for j, r in enumerate(rx):
         c = m.rx[j]
@@ -137,6 +146,17 @@ class ChemModel:
                                         N.dptr(mol), 0), "pcfd_chem_aux")
         return P, cvi, mol
 
+    def transport(self, ref, rhoi, T):
+        """GetMolecularViscosity / GetThermalConductivity of the reacting set
+        (Wilke's rule): non-dimensional rhoi [n][ns] and T [n] -> (mu [n], k [n]),
+        over ref.viscosity and ref.conductivity."""
+        n = len(T)
+        rhoi, T = self._arr(rhoi, (n, self.nspecies)), self._arr(T, (n,))
+        mu, k = np.empty(n), np.empty(n)
+        N.check(self._lib.pcfd_chem_transport(self._h, C.byref(ref), n, N.dptr(rhoi), N.dptr(T), N.dptr(mu),
+                                              N.dptr(k), 0), "pcfd_chem_transport")
+        return mu, k
+
     def node_records(self, ref, rhoi, vel, T):
         """The reacting node record [n][6 + 3 ns] (rhoi, u, v, w, T, P, rho,
         cvi, concentrations) that ComputeAuxiliaryVariables completes."""
@@ -227,6 +247,19 @@ class ChemModel:
         N.check(self._lib.pcfd_chem_residual(self._h, C.byref(ref), C.byref(opts), float(ref_time), int(reactions),
                                              N.dptr(q), N.dptr(b), N.dptr(norms), 0), "pcfd_chem_residual")
         return b, norms
+
+    def viscous_residual(self, ref, opts, Re, directional, q, grad):
+        """The viscous part of the reacting residual on the attached mesh:
+        q [nnode + nbedge][6 + 3 ns] records, grad [nnode][2 ns + 4][3] ->
+        b [nnode][ns + 4]."""
+        m = self._mesh
+        q = self._arr(q, (m.nnode + m.nbedge, 6 + 3 * self.nspecies))
+        grad = self._arr(grad, (m.nnode, 2 * self.nspecies + 4, 3))
+        b = np.empty((m.nnode, self.nspecies + 4))
+        N.check(self._lib.pcfd_chem_viscous_residual(self._h, C.byref(ref), C.byref(opts), float(Re), int(directional),
+                                                     q.ctypes.data, grad.ctypes.data, b.ctypes.data, 0),
+                "pcfd_chem_viscous_residual")
+        return b
 
     def residual_dev(self, ref, opts, ref_time, reactions, q_ptr, b_ptr=None):
         """The same with q (and b, optional) as device addresses; returns the norms."""

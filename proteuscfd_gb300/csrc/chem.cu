@@ -68,6 +68,8 @@ struct ChemHandle {
   double* d_vol = nullptr;
   int *d_nptr = nullptr, *d_nedg = nullptr, *d_bptr = nullptr, *d_bhe = nullptr;
   double *d_q = nullptr, *d_ef = nullptr, *d_bf = nullptr, *d_b = nullptr, *d_part = nullptr, *d_norms = nullptr;
+  double* d_xyz = nullptr;   // node coordinates (the viscous flux's directional correction)
+  double* d_grad = nullptr;  // host-array gradient of the viscous residual [nnode][2 ns + 4][3]
 };
 
 constexpr int kChemNormBlocks = 304;  // fixed grid of the residual gather: a fixed summation order
@@ -472,6 +474,98 @@ __device__ __forceinline__ void fr_fluid_R_c2(const ChemDerived& d, int ns, cons
   c2 = gamma * RDim * Tdim / (ref.velocity * ref.velocity);
 }
 
+// ---- transport ----------------------------------------------------------
+// Species::GetViscosity / GetThermalConductivity (ucs/species.tcc:393,430):
+// at or below 1000 K White's Sutherland forms with air's constants for every
+// species, above it the last NASA RP-1311 fit whose range holds T,
+// ln(y) = A ln T + B/T + C/T^2 + D, from micropoise and microwatt/(cm K).
+// *bad is set when no fit holds T (the reference aborts).
+__device__ double transport_fit(const double (*fit)[6], int nfit, double T, double conv, int& bad) {
+  int range = -1;
+  for (int i = 0; i < nfit; i++)
+    if (T >= fit[i][0] && T <= fit[i][1]) range = i;
+  if (range < 0) {
+    bad = 1;
+    return 0.0;
+  }
+  const double* c = fit[range];
+  return exp(c[2] * log(T) + c[3] / T + c[4] / (T * T) + c[5]) * conv;
+}
+
+__device__ __forceinline__ double species_mu(const pcfd_chem_model& m, int s, double T, int& bad) {
+  if (T <= 1000.0) return 1.716e-5 * pow(T / 273.0, 1.5) * ((273.0 + 111.0) / (T + 111.0));
+  return transport_fit(m.mu_fit[s], m.nmu[s], T, 1.0e-7, bad);
+}
+
+__device__ __forceinline__ double species_k(const pcfd_chem_model& m, int s, double T, int& bad) {
+  if (T <= 1000.0) return 0.0241 * pow(T / 273.0, 1.5) * ((273.0 + 194.0) / (T + 194.0));
+  return transport_fit(m.k_fit[s], m.nk[s], T, 1.0e-4, bad);
+}
+
+// ChemModel::WilkesMixtureRule (ucs/chem.tcc:876) for the viscosity and the
+// conductivity together: mole fractions from mass fractions (the last one
+// 1 - the sum of the others, MassFractionToMoleFraction, :941), weights from
+// the species' viscosities for both properties, as the reference forms them.
+__device__ void wilke_mu_k(const pcfd_chem_model& m, const double* rhoiDim, double TDim, double& mu, double& k,
+                           int& bad) {
+  const int ns = m.nspecies;
+  double X[PCFD_CHEM_MAX_SPECIES], vi[PCFD_CHEM_MAX_SPECIES], ki[PCFD_CHEM_MAX_SPECIES];
+  double rho = 0.0;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  double summ = 0.0;
+  for (int i = 0; i < ns; i++) {
+    X[i] = (rhoiDim[i] / rho) / m.mw[i];
+    summ += X[i];
+  }
+  for (int i = 0; i < ns; i++) X[i] /= summ;
+  summ = 0.0;
+  for (int i = 0; i < ns - 1; i++) summ += X[i];
+  X[ns - 1] = 1.0 - summ;
+  for (int i = 0; i < ns; i++) {
+    vi[i] = species_mu(m, i, TDim, bad);
+    ki[i] = species_k(m, i, TDim, bad);
+  }
+  const double sqrt8 = sqrt(8.0);
+  mu = 0.0;
+  k = 0.0;
+  for (int i = 0; i < ns; i++) {
+    double wi = 0.0;
+    for (int j = 0; j < ns; j++) {
+      const double temp = 1.0 + sqrt(vi[i] / vi[j]) * pow(m.mw[j] / m.mw[i], 0.25);
+      const double phi = pow(1.0 + m.mw[i] / m.mw[j], -0.5) * temp * temp / sqrt8;
+      wi += X[j] * phi;
+    }
+    mu += (X[i] / wi) * vi[i];
+    k += (X[i] / wi) * ki[i];
+  }
+}
+
+// GetMolecularViscosity / GetThermalConductivity of the reacting set
+// (ucs/compressibleFR.tcc:1580,1590), non-dimensional in and out
+__device__ __forceinline__ void fr_transport(const pcfd_chem_model& m, const pcfd_chem_ref& ref, const double* rhoi,
+                                             double T, double& mu, double& k, int& bad) {
+  double rd[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < m.nspecies; i++) rd[i] = rhoi[i] * ref.density;
+  wilke_mu_k(m, rd, T * ref.temperature, mu, k, bad);
+  mu /= (ref.viscosity != 0.0 ? ref.viscosity : 1.0);
+  k /= (ref.conductivity != 0.0 ? ref.conductivity : 1.0);
+}
+
+__global__ void __launch_bounds__(128) k_chem_transport(long long n, const pcfd_chem_model* __restrict__ gm,
+                                                        pcfd_chem_ref ref, const double* __restrict__ rhoi,
+                                                        const double* __restrict__ T, double* __restrict__ mu,
+                                                        double* __restrict__ k, long long* bad_count) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const pcfd_chem_model& m = *gm;
+  int bad = 0;
+  double a, b;
+  fr_transport(m, ref, &rhoi[p * m.nspecies], T[p], a, b, bad);
+  mu[p] = bad ? 0.0 : a;
+  k[p] = bad ? 0.0 : b;
+  if (bad) atomicAdd((unsigned long long*)bad_count, 1ull);
+}
+
 // CompressibleFREqnSet::ContributeTemporalTerms (ucs/compressibleFR.tcc:1319),
 // one thread per node: Aout = Ain + vol/dt terms times dq/dQ (conservative
 // over native), with ChemModel::dEtdP_dEtdRhoi (ucs/chem.tcc:829, at
@@ -708,6 +802,104 @@ __global__ void __launch_bounds__(128) k_chem_bflux(long long nbedge, const pcfd
 // per node: -sum of the fluxes out of it (incident edges in ascending id,
 // signed: ~e where the node is the edge's left end), then its boundary
 // half-edges, then vol * wdot; per-block partial sums of squares
+// CompressibleFREqnSet::ViscousFlux (ucs/compressibleFR.tcc:551) on the face
+// state Q (native record) and face gradient g of the reacting gradient list
+// (rhoi, u, v, w, T, concentrations): laminar, no species diffusion
+__device__ void fr_viscous_flux(const pcfd_chem_model& m, const pcfd_chem_ref& ref, int sym2d, double Re,
+                                const double* Q, const double* g, const EdgeArea& a, double* flux, int& bad) {
+  const int ns = m.nspecies, off = 3 * ns;
+  const double ux = g[off + 0], uy = g[off + 1], uz = g[off + 2];
+  const double vx = g[off + 3], vy = g[off + 4], vz = g[off + 5];
+  const double wx = g[off + 6], wy = g[off + 7], wz = g[off + 8];
+  const double Tx = g[off + 9], Ty = g[off + 10], Tz = g[off + 11];
+  const double u = Q[ns], v = Q[ns + 1], w = Q[ns + 2];
+  double mu, kc;
+  fr_transport(m, ref, Q, Q[ns + 3], mu, kc, bad);
+  const double fact = 2.0 / 3.0;
+  const double tauxx = 2.0 * fact * ux - fact * vy - fact * wz;
+  const double tauyy = 2.0 * fact * vy - fact * ux - fact * wz;
+  const double tauzz = 2.0 * fact * wz - fact * ux - fact * vy;
+  const double tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
+  const double RK = a.w / Re, RKT = RK * mu;
+  const double Tn = Tx * a.x + Ty * a.y + Tz * a.z;
+  const double tauxn = -tauxx * a.x - tauxy * a.y - tauxz * a.z;
+  const double tauyn = -tauxy * a.x - tauyy * a.y - tauyz * a.z;
+  const double tauzn = -tauxz * a.x - tauyz * a.y - tauzz * a.z;
+  for (int i = 0; i < ns; i++) flux[i] = 0.0;
+  flux[ns + 0] = RKT * tauxn;
+  flux[ns + 1] = RKT * tauyn;
+  flux[ns + 2] = RKT * tauzn;
+  flux[ns + 3] = RKT * (tauxn * u + tauyn * v + tauzn * w) + RK * (-kc) * Tn;
+  if (sym2d >= 1 && sym2d <= 3) flux[ns + sym2d - 1] = 0.0;
+}
+
+// Kernel_Viscous_Flux (ucs/residual.tcc:390) of the reacting set, one edge
+// per thread: averaged face state and gradients, the directional correction
+// along the edge when `directional`, the flux leaving the left node into ef.
+// Only the velocity and temperature terms of the gradient reach the flux, so
+// only they are corrected.
+__global__ void __launch_bounds__(128) k_chem_visc_edge(long long nedge, const pcfd_chem_model* __restrict__ gm,
+                                                        pcfd_chem_ref ref, int sym2d, double Re, int directional,
+                                                        const double* __restrict__ q, const double* __restrict__ grad,
+                                                        const double* __restrict__ xyz, const int2* __restrict__ en,
+                                                        const EdgeArea* __restrict__ ea, double* __restrict__ ef,
+                                                        long long* bad_count) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int2 n = en[e];
+  const double* qL = &q[(size_t)n.x * nv];
+  const double* qR = &q[(size_t)n.y * nv];
+  double Q[PCFD_CHEM_MAX_SPECIES + 4], g[3 * (2 * PCFD_CHEM_MAX_SPECIES + 4)];
+  for (int i = 0; i < neqn; i++) Q[i] = (qL[i] + qR[i]) / 2.0;
+  const double* gL = &grad[(size_t)n.x * nt * 3];
+  const double* gR = &grad[(size_t)n.y * nt * 3];
+  for (int j = ns; j < ns + 4; j++)
+    for (int i = 0; i < 3; i++) g[3 * j + i] = 0.5 * (gL[3 * j + i] + gR[3 * j + i]);
+  if (directional) {
+    double dx[3], s2 = 0.0;
+    for (int i = 0; i < 3; i++) {
+      dx[i] = xyz[3 * (size_t)n.y + i] - xyz[3 * (size_t)n.x + i];
+      s2 += dx[i] * dx[i];
+    }
+    for (int j = ns; j < ns + 4; j++) {
+      const double qdots = dx[0] * g[3 * j] + dx[1] * g[3 * j + 1] + dx[2] * g[3 * j + 2];
+      const double dq = (qR[j] - qL[j] - qdots) / s2;
+      for (int i = 0; i < 3; i++) g[3 * j + i] += dq * dx[i];
+    }
+  }
+  int bad = 0;
+  double f[PCFD_CHEM_MAX_SPECIES + 4];
+  fr_viscous_flux(m, ref, sym2d, Re, Q, g, ea[e], f, bad);
+  for (int i = 0; i < neqn; i++) ef[(size_t)e * neqn + i] = f[i];
+  if (bad) atomicAdd((unsigned long long*)bad_count, 1ull);
+}
+
+// Bkernel_Viscous_Flux (ucs/residual.tcc:473) on one partition: the face
+// state averages the node and its phantom record, the gradient is the node's
+__global__ void __launch_bounds__(128) k_chem_visc_bedge(long long nbedge, const pcfd_chem_model* __restrict__ gm,
+                                                         pcfd_chem_ref ref, int sym2d, double Re,
+                                                         const double* __restrict__ q,
+                                                         const double* __restrict__ grad, const int2* __restrict__ bn,
+                                                         const EdgeArea* __restrict__ ba, double* __restrict__ bf,
+                                                         long long* bad_count) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= nbedge) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int2 n = bn[k];
+  const double* qL = &q[(size_t)n.x * nv];
+  const double* qR = &q[(size_t)n.y * nv];
+  double Q[PCFD_CHEM_MAX_SPECIES + 4];
+  for (int i = 0; i < neqn; i++) Q[i] = 0.5 * (qL[i] + qR[i]);
+  int bad = 0;
+  double f[PCFD_CHEM_MAX_SPECIES + 4];
+  fr_viscous_flux(m, ref, sym2d, Re, Q, &grad[(size_t)n.x * nt * 3], ba[k], f, bad);
+  for (int i = 0; i < neqn; i++) bf[(size_t)k * neqn + i] = f[i];
+  if (bad) atomicAdd((unsigned long long*)bad_count, 1ull);
+}
+
 __global__ void __launch_bounds__(256) k_chem_gather(long long nnode, const pcfd_chem_model* __restrict__ gm,
                                                      pcfd_chem_ref ref, double ref_time, int reactions,
                                                      const double* __restrict__ q, const int* __restrict__ nptr,
@@ -795,7 +987,9 @@ int validate(const pcfd_chem_model* m) {
       m->nreactions > PCFD_CHEM_MAX_REACTIONS)
     return 0;
   for (int k = 0; k < m->nspecies; k++)
-    if (!(m->mw[k] > 0.0)) return 0;
+    if (!(m->mw[k] > 0.0) || m->nmu[k] < 0 || m->nmu[k] > PCFD_CHEM_MAX_TRANSPORT_FITS || m->nk[k] < 0 ||
+        m->nk[k] > PCFD_CHEM_MAX_TRANSPORT_FITS)
+      return 0;
   for (int j = 0; j < m->nreactions; j++) {
     const pcfd_chem_reaction& r = m->rx[j];
     if (r.type < 0 || r.type > 3 || r.nlocal < 0 || r.nlocal > PCFD_CHEM_MAX_LOCAL) return 0;
@@ -1072,6 +1266,31 @@ PCFD_API int pcfd_chem_aux(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n,
                          });
 }
 
+PCFD_API int pcfd_chem_transport(pcfd_chem_t h, const pcfd_chem_ref* ref, long long n, const double* rhoi,
+                                 const double* T, double* mu, double* k, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || n < 0 || (n > 0 && (!rhoi || !T || !mu || !k))) {
+    pcfd_set_last_error("pcfd_chem_transport: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (n == 0) return PCFD_OK;
+  const int ns = c->host.nspecies;
+  const pcfd_chem_ref r = *ref;
+  long long bad = 0;
+  int rc = node_call<2, 2>(c, n, dev, {rhoi, T}, {ns, 1}, {mu, k}, {1, 1}, &bad,
+                           [&](const double* const* in, double* const* out) {
+                             k_chem_transport<<<CHEM_GRID(n)>>>(n, c->dev, r, in[0], in[1], out[0], out[1],
+                                                                c->d_count);
+                           });
+  if (rc) return rc;
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_transport: " + std::to_string(bad) +
+                        " node(s) above every transport fit's temperature range");
+    return PCFD_ERR_ARG;
+  }
+  return PCFD_OK;
+}
+
 PCFD_API int pcfd_chem_source_jacobian(pcfd_chem_t h, const pcfd_chem_ref* ref, double ref_time, long long n,
                                        const double* q, const double* vol, double* A, int dev) {
   ChemHandle* c = (ChemHandle*)h;
@@ -1210,11 +1429,11 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   }
   for (long long k = 0; k < nb; k++) bhe[bfill[m->bedges[2 * k]]++] = (int)k;
   void* mesh_ptrs[] = {c->d_en, c->d_bn, c->d_ea, c->d_ba, c->d_vol, c->d_nptr, c->d_nedg, c->d_bptr,
-                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms};
+                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms, c->d_xyz, c->d_grad};
   for (void* p : mesh_ptrs) cudaFree(p);
   c->d_en = c->d_bn = nullptr;
   c->d_ea = c->d_ba = nullptr;
-  c->d_vol = c->d_q = c->d_ef = c->d_bf = c->d_b = c->d_part = c->d_norms = nullptr;
+  c->d_vol = c->d_q = c->d_ef = c->d_bf = c->d_b = c->d_part = c->d_norms = c->d_xyz = c->d_grad = nullptr;
   c->d_nptr = c->d_nedg = c->d_bptr = c->d_bhe = nullptr;
   c->nnode = c->nedge = c->nbedge = 0;
   const int ns = c->host.nspecies, neqn = ns + 4;
@@ -1230,6 +1449,7 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   if (e == cudaSuccess) e = up((void**)&c->d_bn, m->bedges, (size_t)nb * 2 * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_ba, m->bedge_area, (size_t)nb * 4 * sizeof(double));
   if (e == cudaSuccess) e = up((void**)&c->d_vol, m->vol, (size_t)nn * sizeof(double));
+  if (e == cudaSuccess && m->xyz) e = up((void**)&c->d_xyz, m->xyz, (size_t)nn * 3 * sizeof(double));
   if (e == cudaSuccess) e = up((void**)&c->d_nptr, nptr.data(), nptr.size() * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_nedg, nedg.data(), nedg.size() * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_bptr, bptr.data(), bptr.size() * sizeof(int));
@@ -1244,6 +1464,75 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   c->nnode = nn;
   c->nedge = ne;
   c->nbedge = nb;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_viscous_residual(pcfd_chem_t h, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                                        double Re, int directional, const double* q, const double* grad, double* b,
+                                        int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || !o || !q || !grad || !b || !(Re > 0.0)) {
+    pcfd_set_last_error("pcfd_chem_viscous_residual: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0) {
+    pcfd_set_last_error("pcfd_chem_viscous_residual: no mesh attached (pcfd_chem_attach_mesh)");
+    return PCFD_ERR_STATE;
+  }
+  if (directional && !c->d_xyz) {
+    pcfd_set_last_error("pcfd_chem_viscous_residual: the attached mesh has no coordinates");
+    return PCFD_ERR_STATE;
+  }
+  for (int s = 0; s < c->host.nspecies; s++)
+    if (c->host.nmu[s] == 0 || c->host.nk[s] == 0) {
+      pcfd_set_last_error("pcfd_chem_viscous_residual: the model has no transport fits");
+      return PCFD_ERR_STATE;
+    }
+  const int ns = c->host.nspecies, neqn = ns + 4, nt = 2 * ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, ne = c->nedge, nb = c->nbedge;
+  const double* dq = q;
+  const double* dg = grad;
+  if (!dev) {
+    if (!c->d_grad) CHEM_TRY(cudaMalloc(&c->d_grad, (size_t)nn * nt * 3 * sizeof(double)), "chem buffers");
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    CHEM_TRY(cudaMemcpyAsync(c->d_grad, grad, (size_t)nn * nt * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream),
+             "chem copy");
+    dq = c->d_q;
+    dg = c->d_grad;
+  }
+  double* db = dev ? b : c->d_b;
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  const pcfd_chem_ref r = *ref;
+  if (ne > 0) {
+    k_chem_visc_edge<<<CHEM_GRID(ne)>>>(ne, c->dev, r, o->symmetry2D, Re, directional, dq, dg, c->d_xyz, c->d_en,
+                                        c->d_ea, c->d_ef, c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_visc_edge launch");
+  }
+  if (nb > 0) {
+    k_chem_visc_bedge<<<CHEM_GRID(nb)>>>(nb, c->dev, r, o->symmetry2D, Re, dq, dg, c->d_bn, c->d_ba, c->d_bf,
+                                         c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_visc_bedge launch");
+  }
+  // the same deterministic per-node sum as the inviscid residual, without
+  // the chemistry source
+  k_chem_gather<<<kChemNormBlocks, 256, 0, c->stream>>>(nn, c->dev, r, 1.0, 0, dq, c->d_nptr, c->d_nedg, c->d_ef,
+                                                        c->d_bptr, c->d_bhe, c->d_bf, c->d_vol, db, c->d_part);
+  CHEM_TRY(cudaGetLastError(), "k_chem_gather launch");
+  if (!dev)
+    CHEM_TRY(cudaMemcpyAsync(b, db, (size_t)nn * neqn * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  long long bad = 0;
+  CHEM_TRY(cudaMemcpyAsync(&bad, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem viscous residual");
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_viscous_residual: " + std::to_string(bad) +
+                        " face(s) above every transport fit's temperature range");
+    return PCFD_ERR_ARG;
+  }
   return PCFD_OK;
 }
 

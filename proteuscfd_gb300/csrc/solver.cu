@@ -2405,8 +2405,13 @@ int krylov_residual(Solver* s, bool first, float* w) {
 // them; a cycle in which the learned preconditioner reduces the residual by
 // less than 10 % switches the rest of the solve to plain SGS and adds one
 // cycle (counted in *fallbacks).
+// aug: instead, every cycle's second direction is the learned vector of the
+// cycle's first Krylov vector (the residual direction), after plain SGS of
+// it as the first: the space then holds both, so the correction cannot make
+// a cycle worse per direction, and no fallback is needed.
 template <class K>
-int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp, int* fallbacks) {
+int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp, int* fallbacks,
+                 bool aug) {
   const int m = std::max(1, std::min(o->fgmres_m > 0 ? o->fgmres_m : 30, 60));
   int restarts = std::max(1, o->fgmres_restarts);
   if (fallbacks) *fallbacks = 0;
@@ -2442,8 +2447,9 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
     for (; j < m; j++) {
       K* zj = Z + (size_t)j * n;
       CUDA_TRY(cudaMemsetAsync(zj, 0, n * sizeof(K), s->stream));
-      const bool lp_here = use_lp && (o->lp_directions <= 0 || j < o->lp_directions);
-      if ((rc = krylov_prec(s, std::max(1, o->nsgs), lp_here, V + (size_t)j * n, zj))) return rc;
+      const bool lp_here = use_lp && (aug ? j == 1 : (o->lp_directions <= 0 || j < o->lp_directions));
+      const K* vin = (aug && j == 1) ? V : V + (size_t)j * n;
+      if ((rc = krylov_prec(s, std::max(1, o->nsgs), lp_here, vin, zj))) return rc;
       if ((rc = krylov_spmv(s, zj, w))) return rc;
       // CGS2 with the coefficients kept on the device (slots 1, 2) and the
       // norm of the result (slot 0, formed by the second update); one host
@@ -2499,7 +2505,7 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
     if ((rc = launch(s, T_KRYLOV, [&] { k_combine<K><<<kKrylovBlocks, 256, 0, s->stream>>>(n, j, Z, hdev, s->d_x); })))
       return rc;
     if (rel < rtol) break;
-    if (use_lp && rel > 0.9 * beta / beta0) {
+    if (use_lp && !aug && rel > 0.9 * beta / beta0) {
       use_lp = false;
       restarts++;
       if (fallbacks) (*fallbacks)++;
@@ -2513,9 +2519,9 @@ int run_fgmres_t(Solver* s, const pcfd_newton_opts* o, double* relres, int* iter
 }
 
 int run_fgmres(Solver* s, const pcfd_newton_opts* o, double* relres, int* iters, bool use_lp = false,
-               int* fallbacks = nullptr) {
-  if (s->jac_prec == 0) return run_fgmres_t<double>(s, o, relres, iters, use_lp, fallbacks);
-  return run_fgmres_t<float>(s, o, relres, iters, use_lp, fallbacks);
+               int* fallbacks = nullptr, bool aug = false) {
+  if (s->jac_prec == 0) return run_fgmres_t<double>(s, o, relres, iters, use_lp, fallbacks, aug);
+  return run_fgmres_t<float>(s, o, relres, iters, use_lp, fallbacks, aug);
 }
 
 // -------------------------------------------------------------------------
@@ -3703,10 +3709,11 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
   Solver* s = (Solver*)h;
   if (!s || !o || o->iter < 0 || o->nsgs < 0 || !(o->cfl > 0.0))
     return set_err(PCFD_ERR_ARG, "pcfd_newton_step: bad arguments");
-  if (o->linear_solver < 0 || o->linear_solver > 2)
-    return set_err(PCFD_ERR_ARG, "pcfd_newton_step: linear_solver must be 0 (SGS), 1 (FGMRES) or 2 (learned)");
-  if (o->linear_solver == 2 && !s->lp)
-    return set_err(PCFD_ERR_STATE, "pcfd_newton_step: linear_solver 2 needs pcfd_lp_init");
+  if (o->linear_solver < 0 || o->linear_solver > 3)
+    return set_err(PCFD_ERR_ARG,
+                   "pcfd_newton_step: linear_solver must be 0 (SGS), 1 (FGMRES), 2 or 3 (learned)");
+  if (o->linear_solver >= 2 && !s->lp)
+    return set_err(PCFD_ERR_STATE, "pcfd_newton_step: linear_solver 2 and 3 need pcfd_lp_init");
   int rc;
   if (o->jac_precision != s->jac_prec && (rc = ensure_matrix(s, o->jac_precision))) return rc;
   const double cfl = ramp_cfl(o->iter, o->cfl_start > 0.0 ? o->cfl_start : o->cfl, o->cfl, o->cfl_ramp_steps);
@@ -3739,8 +3746,9 @@ PCFD_API int pcfd_newton_step(pcfd_solver_t h, const pcfd_newton_opts* o, pcfd_n
       if ((rc = run_sgs(s, o->nsgs, s->d_b, s->d_x, &lin))) return rc;
       lin_it = o->nsgs;
     } else {
-      if ((rc = run_fgmres(s, o, &lin, &lin_it, o->linear_solver == 2, &fallbacks))) return rc;
-      if (o->linear_solver == 2 && (rc = lp_check_err(s))) return rc;
+      if ((rc = run_fgmres(s, o, &lin, &lin_it, o->linear_solver >= 2, &fallbacks, o->linear_solver == 3)))
+        return rc;
+      if (o->linear_solver >= 2 && (rc = lp_check_err(s))) return rc;
     }
   }
   double dqn = 0.0;

@@ -2,7 +2,8 @@
 the reference's 6-reaction mechanism file chemModels/5speciesAir.rxn, with
 each species' molecular weight and NASA-7 polynomials as the reference's own
 database builder (chemdata/chemDB.py, process_burcat) extracts them from
-chemdata/BURCAT_FIXED.THR.
+chemdata/BURCAT_FIXED.THR, and its viscosity and conductivity curve fits as
+the builder's process_mcbride extracts them from chemdata/trans.inp.
 
 The builder is imported from the reference tree with an in-memory stand-in
 for the HDF5 file (h5py is not installed); the reaction file is parsed by the
@@ -39,6 +40,10 @@ class _Group(dict):
 
 
 def burcat_species():
+    """The species groups the database builder writes from the Burcat thermo
+    file and then from the McBride-Gordon transport file (its own order:
+    Burcat, CEA, McBride-Gordon; only the last writes transport fits, and
+    the first fit written for a species stays)."""
     sys.modules.setdefault("h5py", types.ModuleType("h5py"))
     spec = importlib.util.spec_from_file_location("chemDB", REF / "chemdata" / "chemDB.py")
     mod = importlib.util.module_from_spec(spec)
@@ -51,6 +56,7 @@ def burcat_species():
             import contextlib, io
             with contextlib.redirect_stdout(io.StringIO()):
                 mod.process_burcat(h5, str(REF / "chemdata" / "BURCAT_FIXED.THR"))
+                mod.process_mcbride(h5, str(REF / "chemdata" / "trans.inp"))
         finally:
             os.chdir(cwd)
     return h5["/species"]
@@ -143,13 +149,19 @@ def main():
     species = []
     for s in order:
         d = db[s]
+        # a species without transport fits takes N2's (Species::Init,
+        # ucs/species.tcc:241-246,281-286)
+        tr = d if "mu" in d and "k" in d else db["N2"]
         species.append({"name": s, "MW": float(d["MW"]) / 1000.0,
                         "lo": [float(v) for v in d["NASA7_burcat1"]],
                         "hi": [float(v) for v in d["NASA7_burcat2"]],
-                        "hf298": float(d["NASA7_burcat_coeff15"])})
+                        "hf298": float(d["NASA7_burcat_coeff15"]),
+                        "mu": [[float(v) for v in row] for row in tr["mu"]],
+                        "k": [[float(v) for v in row] for row in tr["k"]]})
     for rx in reactions:
         rx["global"] = [order.index(s) for s in rx["species"]]
-    fixture = {"source": "chemModels/5speciesAir.rxn + chemdata/BURCAT_FIXED.THR via chemdata/chemDB.py",
+    fixture = {"source": "chemModels/5speciesAir.rxn + chemdata/BURCAT_FIXED.THR and chemdata/trans.inp via "
+                         "chemdata/chemDB.py",
                "univ_r": 8.31447215, "pref": 101325.0, "species": species, "reactions": reactions}
     OUT.write_text(json.dumps(fixture, indent=1) + "\n")
     print("wrote", OUT)

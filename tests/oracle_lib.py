@@ -68,6 +68,11 @@ def lib():
             "oracle_chem_n2c": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, _DP, C.c_double, _DP]),
             "oracle_chem_aux": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), _DP, C.c_double, _DP, _DP,
                                        _DP]),
+            "oracle_chem_transport_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_longlong,
+                                                       _DP, _DP, _DP, _DP]),
+            "oracle_chem_viscous_residual": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
+                                                       C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), C.c_double,
+                                                       C.c_int, _DP, _DP, _DP]),
             "oracle_forces": (None, [MV, PP, _DP, _DP, _IP, _DP]),
             "oracle_mesh_box": (C.c_void_p, [C.POINTER(N.BoxParams)]),
             "oracle_mesh_elements": (C.c_void_p, [C.c_int, _DP, C.c_int, _IP, _IP, C.c_int, _IP]),
@@ -459,6 +464,15 @@ class OracleChemState:
             P[k], cvi[k], mol[k] = p.value, c, mo
         return P, cvi, mol
 
+    def transport(self, rhoi, T):
+        """(mu [n], k [n], nodes above every fit's range)."""
+        rhoi = np.ascontiguousarray(rhoi, np.float64)
+        T = np.ascontiguousarray(T, np.float64)
+        mu, k = np.empty(len(T)), np.empty(len(T))
+        bad = self.L.oracle_chem_transport_n(C.byref(self.m), C.byref(self.ref), len(T), dp(rhoi), dp(T), dp(mu),
+                                             dp(k))
+        return mu, k, bad
+
     def hllc(self, opts, q, edges, avec):
         """HLLCFlux edge by edge; returns (flux [E][ns + 4], failures)."""
         ne = len(edges)
@@ -501,6 +515,16 @@ class OracleChemState:
         self.L.oracle_chem_temporal_n(C.byref(self.m), C.byref(self.ref), n, dp(arr(q)), dp(arr(vol)), dp(arr(dtau)),
                                       dp(arr(beta)), float(cnp1), float(dt), int(local_ts), dp(A))
         return A
+
+    def viscous_residual(self, opts, mesh, Re, directional, q, grad):
+        """The viscous part of the reacting residual; returns (b, faces above
+        every transport fit)."""
+        q = np.ascontiguousarray(q, np.float64)
+        grad = np.ascontiguousarray(grad, np.float64)
+        b = np.empty((mesh.nnode, self.ns + 4))
+        bad = self.L.oracle_chem_viscous_residual(C.byref(self.m), C.byref(self.ref), C.byref(opts), C.byref(mesh.view),
+                                                  float(Re), int(directional), dp(q), dp(grad), dp(b))
+        return b, bad
 
     def residual(self, opts, mesh, q, ref_time, reactions):
         """SpatialResidual of the reacting set (first order, inviscid)."""

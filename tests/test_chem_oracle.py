@@ -239,3 +239,108 @@ def test_fr_temporal_terms_are_conservative_over_native():
     assert np.allclose(Ab - base, A3, rtol=1e-12, atol=1e-12 * np.abs(A3).max())
     assert np.array_equal(A3[:, :, :ns + 3], A1[:, :, :ns + 3])
     assert not np.allclose(A3[:, :, ns + 3], A1[:, :, ns + 3])
+
+
+def _numpy_transport(spec, rhoi_dim, Td):
+    """Species and mixture viscosity and conductivity restated with NumPy
+    (White's forms at or below 1000 K, the last matching RP-1311 fit above,
+    Wilke's rule with mole fractions whose last is 1 - the sum of the
+    others), dimensional."""
+    sp = spec["species"]
+    mw = np.array([s["MW"] for s in sp])
+
+    def fit(rows, T, conv):
+        r = [row for row in rows if row[0] <= T <= row[1]][-1]
+        return np.exp(r[2] * np.log(T) + r[3] / T + r[4] / T ** 2 + r[5]) * conv
+
+    def props(T):
+        if T <= 1000.0:
+            mu = 1.716e-5 * (T / 273.0) ** 1.5 * (384.0 / (T + 111.0))
+            k = 0.0241 * (T / 273.0) ** 1.5 * (467.0 / (T + 194.0))
+            return np.full(len(sp), mu), np.full(len(sp), k)
+        return (np.array([fit(s["mu"], T, 1e-7) for s in sp]), np.array([fit(s["k"], T, 1e-4) for s in sp]))
+
+    mu_out, k_out = [], []
+    for r, T in zip(rhoi_dim, Td):
+        X = (r / r.sum()) / mw
+        X = X / X.sum()
+        X[-1] = 1.0 - X[:-1].sum()
+        vi, ki = props(T)
+        temp = 1.0 + np.sqrt(vi[:, None] / vi[None, :]) * (mw[None, :] / mw[:, None]) ** 0.25
+        phi = (1.0 + mw[:, None] / mw[None, :]) ** -0.5 * temp ** 2 / np.sqrt(8.0)
+        w = (phi * X[None, :]).sum(axis=1)
+        mu_out.append((X / w * vi).sum())
+        k_out.append((X / w * ki).sum())
+    return np.array(mu_out), np.array(k_out)
+
+
+def test_transport_properties():
+    """Mixture viscosity and conductivity (GetMolecularViscosity /
+    GetThermalConductivity with Wilke's rule) against a NumPy restatement,
+    White's air values at 300 K for a pure species, and the fits' own
+    range limit."""
+    from oracle_lib import OracleChemState
+    from chem_cases import reference_scales
+    spec = mechanism()
+    ref = reference_scales()
+    ref.viscosity, ref.conductivity = 1.0e-5, 0.02
+    ns = len(spec["species"])
+    rng = np.random.default_rng(4)
+    rhoi = 10.0 ** rng.uniform(-4, 0, size=(200, ns))
+    Td = np.concatenate([[300.0, 1000.0, 1000.5, 5000.0, 5000.5, 14999.0], rng.uniform(250.0, 14000.0, 194)])
+    O = OracleChemState(model_struct(spec), ref)
+    mu, k, bad = O.transport(rhoi / ref.density, Td / ref.temperature)
+    assert bad == 0
+    mu_np, k_np = _numpy_transport(spec, rhoi, Td)
+    np.testing.assert_allclose(mu * ref.viscosity, mu_np, rtol=1e-12)
+    np.testing.assert_allclose(k * ref.conductivity, k_np, rtol=1e-12)
+    # a pure species takes its own values: White's air viscosity at 300 K
+    pure = np.zeros((1, ns))
+    pure[0, 3] = 1.0
+    mu1, k1, _ = O.transport(pure / ref.density, np.array([300.0]) / ref.temperature)
+    assert abs(mu1[0] * ref.viscosity - 1.716e-5 * (300 / 273.0) ** 1.5 * 384.0 / 411.0) < 1e-20
+    assert abs(k1[0] * ref.conductivity - 0.0241 * (300 / 273.0) ** 1.5 * 467.0 / 494.0) < 1e-17
+    # N2 at 2000 K from its RP-1311 fit: about 6.3e-5 Pa s
+    mu2, _, _ = O.transport(pure / ref.density, np.array([2000.0]) / ref.temperature)
+    assert 6.0e-5 < mu2[0] * ref.viscosity < 6.7e-5
+    # above every fit's range the reference aborts; the oracle counts it
+    assert O.transport(pure / ref.density, np.array([16000.0]) / ref.temperature)[2] == 1
+
+
+def test_viscous_residual_properties():
+    """The oracle's reacting viscous residual: zero for a uniform state with
+    zero gradients; for a linear velocity u = a y with its exact gradient
+    the momentum flux through a face of unit normal y is -(area / Re) mu a,
+    and the interior faces' contributions cancel in the sum over nodes."""
+    from chem_cases import fr_records, fr_states, reference_scales
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    from proteuscfd_gb300.chem import ChemModel
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(6, 5, 4, jitter=0.2, seed=3)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=3)
+    rhoi[:] = rhoi[0]
+    vel[:] = vel[0]
+    T[:] = T[0]
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(spec), ref)
+    opts = ChemModel.flux_opts(1.0, 0.4, 0)
+    grad = np.zeros((m.nnode, 2 * ns + 4, 3))
+    b, bad = O.viscous_residual(opts, m, 1.0e4, 1, q, grad)
+    assert bad == 0 and np.abs(b).max() == 0.0
+    # u = a y at every node and phantom, exact gradient
+    a = 0.3
+    y = np.r_[m.xyz[:, 1], m.xyz[m.bedges[:, 0], 1]]
+    q2 = q.copy()
+    q2[:, ns] = a * y
+    grad[:, ns, 1] = a
+    b2, _ = O.viscous_residual(opts, m, 1.0e4, 1, q2, grad)
+    # only the x-momentum and energy rows see the shear, and the interior
+    # faces cancel in the total: what remains is the boundary faces' sum
+    assert np.abs(b2[:, :ns]).max() == 0.0
+    mu, _, _ = O.transport(rhoi[:1], T[:1])
+    ba = m.bedge_area
+    expect = -(-(mu[0] / 1.0e4) * a * (ba[:, 1] * ba[:, 3])).sum()
+    assert abs(b2[:, ns].sum() - expect) < 1e-12 * abs(expect) + 1e-18

@@ -304,3 +304,64 @@ def test_temporal_terms_parity(local_ts):
                          dA.data_ptr())
     assert np.array_equal(dA.cpu().numpy(), A)
     C.close()
+
+
+def test_transport_parity():
+    """Mixture viscosity and conductivity (Wilke's rule over White's forms
+    and the RP-1311 fits) on the GPU against the oracle; above every fit's
+    range the call is refused, as the reference aborts."""
+    from chem_cases import reference_scales
+    from oracle_lib import OracleChemState
+    spec = mechanism()
+    c = ChemModel(spec)
+    ref = reference_scales()
+    ref.viscosity, ref.conductivity = 1.0e-5, 0.02
+    rng = np.random.default_rng(9)
+    ns = len(spec["species"])
+    n = 20000
+    rhoi = 10.0 ** rng.uniform(-4, 0, size=(n, ns)) / ref.density
+    Td = rng.uniform(250.0, 14900.0, size=n)
+    Td[:6] = [300.0, 1000.0, 1000.5, 5000.0, 5000.5, 14999.0]
+    T = Td / ref.temperature
+    mu, k = c.transport(ref, rhoi, T)
+    O = OracleChemState(model_struct(spec), ref)
+    mo, ko, bad = O.transport(rhoi, T)
+    assert bad == 0
+    # the same operations; exp, log, pow and sqrt differ between CUDA's and
+    # the host's libm by an ulp or so
+    np.testing.assert_allclose(mu, mo, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(k, ko, rtol=1e-13, atol=0)
+    with pytest.raises(N.PcfdError):
+        c.transport(ref, rhoi[:1], np.array([16000.0 / ref.temperature]))
+    c.close()
+
+
+@pytest.mark.parametrize("directional", [0, 1])
+def test_fr_viscous_residual_parity(directional):
+    """The viscous part of the reacting residual (face-averaged states and
+    gradients, the directional correction, mixture transport, boundary
+    faces) on the GPU against the oracle, on a jittered box with seeded
+    records and gradients."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(12, 9, 8, jitter=0.2, seed=5)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=21)
+    q = fr_records(ref, rhoi, vel, T)
+    grad = np.random.default_rng(22).normal(size=(m.nnode, 2 * ns + 4, 3))
+    C = ChemModel(spec)
+    C.attach_mesh(m)
+    opts = C.flux_opts(1.0, 0.4, 0)
+    b = C.viscous_residual(ref, opts, 2.0e4, directional, q, grad)
+    bo, bad = OracleChemState(model_struct(spec), ref).viscous_residual(opts, m, 2.0e4, directional, q, grad)
+    assert bad == 0
+    # the same operations in the same order; the transport's exp, log and
+    # pow differ from the host's libm by an ulp or so
+    scale = np.abs(bo).max(axis=0, keepdims=True)
+    scale[scale == 0] = 1.0
+    assert (np.abs(b - bo) / scale).max() < 1e-12, (np.abs(b - bo) / scale).max()
+    assert np.abs(b[:, :ns]).max() == 0.0
+    C.close()

@@ -143,3 +143,43 @@ def test_training_and_learned_fgmres():
     print("FGMRES(10) residual: sgs %.3e, learned %.3e (%.2fx lower); fallbacks with every direction: %d"
           % (np.exp(np.mean(np.log(r_sgs))), np.exp(np.mean(np.log(r_lp))), gain, fb_all))
     assert gain > 1.0, (r_sgs, r_lp)
+
+
+def test_learned_at_study_settings_seed_spread():
+    """The convergence study's mixed settings (FP32 Jacobian, FGMRES(30)
+    stopped at a 0.1 reduction, two SGS sweeps, CFL 1000 after a ramp): from
+    the same states, Krylov iterations per Newton step with the learned
+    vector as each cycle's second direction (linear_solver 3) against plain
+    SGS, for networks trained from three initial seeds.  Bar: at most 1.25x
+    the plain iterations plus one (the learned direction is one more
+    direction; the space holds plain SGS's first direction too).  The
+    iterations per seed and the replacing form's (linear_solver 2) are
+    printed."""
+    base = dict(nsgs=2, linear_solver=1, fgmres_m=30, fgmres_restarts=1, fgmres_rtol=0.1, jac_precision=1,
+                first_order_steps=10, limiter_freeze=30, cfl_start=1.0, cfl_ramp_steps=20)
+    out = []
+    for seed in (1, 2, 3):
+        c, m, S, _ = make((24, 18, 14), seed=3)
+        S.lp_init(seed)
+        for it in range(30):
+            S.newton_iterate(it, **dict(base, cfl=100.0))
+            if it >= 10 and it % 4 == 0:
+                S.lp_collect(nsgs=2, rtol=1e-6, krylov_pairs=2)
+        S.lp_train(epochs=60, lr=2e-3)
+        it_plain, it_aug, it_rep = [], [], []
+        for it in range(30, 36):
+            st = S.get_state()
+            it_plain.append(S.newton_iterate(it, **dict(base, cfl=1000.0))["lin_iters"])
+            S.set_state(st)
+            it_aug.append(S.newton_iterate(it, **dict(base, cfl=1000.0, linear_solver=3))["lin_iters"])
+            S.set_state(st)
+            it_rep.append(S.newton_iterate(it, **dict(base, cfl=1000.0, linear_solver=2, lp_directions=1))["lin_iters"])
+            S.set_state(st)
+            S.newton_iterate(it, **dict(base, cfl=1000.0))
+        out.append((seed, np.mean(it_plain), np.mean(it_aug), np.mean(it_rep)))
+        S.close()
+    for seed, p, a, r in out:
+        print("seed %d: Krylov iterations per step plain %.2f, learned second direction %.2f, "
+              "learned first direction %.2f" % (seed, p, a, r))
+    for seed, p, a, r in out:
+        assert a <= 1.25 * p + 1.0, out

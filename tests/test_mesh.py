@@ -108,3 +108,27 @@ def test_rcm_order_is_the_reference_sequence_applied_as_old_to_new():
     r = Mesh.box(10, 9, 8, jitter=0.2, reorder=True)
     np.testing.assert_array_equal(r.ordering, order)
     np.testing.assert_array_equal(r.xyz[order], m.xyz)
+
+
+def test_rcm_numbering_reduces_bandwidth():
+    """reorder="rcm" numbers nodes in the reverse Cuthill-McKee sequence
+    (new node k is old node ordering[k]); the reference's set-up reorder
+    uses the same list as an old-to-new map, which scatters neighbours.  On
+    a structured box the natural numbering is already near the minimum
+    bandwidth (one x-y plane); the sequence from corner node 0 sweeps
+    diagonal planes, a little wider."""
+    from proteuscfd_gb300 import Mesh
+
+    def bandwidth(m):
+        e = np.asarray(m.edges).reshape(-1, 2)
+        return int(np.abs(e[:, 0] - e[:, 1]).max())
+
+    kw = dict(nx=14, ny=11, nz=9, jitter=0.2, seed=3)
+    plain = Mesh.box(**kw)
+    rcm = Mesh.box(reorder="rcm", **kw)
+    ref = Mesh.box(reorder=True, **kw)
+    assert sorted(rcm.ordering.tolist()) == list(range(plain.nnode))
+    np.testing.assert_array_equal(rcm.xyz, plain.xyz[rcm.ordering])
+    assert np.array_equal(rcm.ordering, ref.ordering)
+    assert bandwidth(rcm) < 1.5 * bandwidth(plain)
+    assert bandwidth(ref) > 4 * bandwidth(rcm)
