@@ -508,6 +508,28 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t c, const pcfd_mesh_view* m);
  * (optional; ParallelL2Norm and StridedParallelL2Norm).  dev as above (q, b). */
 PCFD_API int pcfd_chem_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
                                 double ref_time, int reactions, const double* q, double* b, double* norms, int dev);
+/* UpdateBCs (ucs/bc.tcc:1400) of the reacting set on the attached mesh (which
+ * must carry face tags), in place on q (as for pcfd_chem_residual): each
+ * half-edge in order through CalculateBoundaryVariables (:1059), then
+ * ComputeAuxiliaryVariables of its phantom and node.  Built types, per face
+ * tag (bc_type, twall and qref have ntags entries): sonic inflow / Dirichlet
+ * (node and phantom take qref[tag], a full record), sonic outflow / Neumann,
+ * the isothermal no-slip wall at rest (twall[tag] > 0 K;
+ * GetViscousWallBoundaryVariables, ucs/compressibleFR.tcc:2049) and, with
+ * no_cvbc = 1, the impermeable wall and symmetry plane
+ * (GetInviscidWallBoundaryVariables' mirror, :1042).  Any other type (far
+ * field, the characteristic wall, the adiabatic no-slip wall) returns
+ * PCFD_ERR_ARG and leaves its half-edges as they were.  dev as above (q). */
+PCFD_API int pcfd_chem_update_bcs(pcfd_chem_t c, const pcfd_chem_ref* ref, int ntags, const int* bc_type,
+                                  const double* twall, const double* qref, int no_cvbc, double* q, int dev);
+/* Gradient<T>::Compute of the reacting set on the attached mesh (which must
+ * carry coordinates and LSQ matrices): the weighted least-squares gradient
+ * (Kernel_LSQ_Gradient, ucs/gradient.tcc:251) of the gradient list rhoi, u,
+ * v, w, T, concentrations (GetGradientsLocation, ucs/compressibleFR.tcc:693)
+ * over the interior edges, then Bkernel_Symmetry_Fix (:545) on the
+ * half-edges whose tag is one of sym_tags (at most 8).  q as for
+ * pcfd_chem_residual -> grad [nnode][2 ns + 4][3].  dev as above (q, grad). */
+PCFD_API int pcfd_chem_gradient(pcfd_chem_t c, const double* q, const int* sym_tags, int nsym, double* grad, int dev);
 /* The viscous part of the reacting residual on the attached mesh:
  * Kernel_Viscous_Flux and Bkernel_Viscous_Flux (ucs/residual.tcc:390,473)
  * with CompressibleFREqnSet::ViscousFlux (ucs/compressibleFR.tcc:551), laminar,

@@ -769,3 +769,116 @@ int oracle_chem_viscous_residual(const pcfd_chem_model* m, const pcfd_chem_ref* 
   }
   return bad;
 }
+
+/* Gradient<T>::Compute for the reacting set: Kernel_LSQ_Gradient (weighted
+ * least squares, ucs/gradient.tcc:251) over the interior edges of the
+ * gradient list of CompressibleFREqnSet::GetGradientsLocation
+ * (ucs/compressibleFR.tcc:693: rhoi, u, v, w, T, concentrations), then
+ * Bkernel_Symmetry_Fix (:545) on the half-edges whose tag is one of
+ * sym_tags.  grad [nnode][2 ns + 4][3]. */
+int oracle_chem_gradient(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const int* sym_tags,
+                         int nsym, double* grad) {
+  const int ns = m->nspecies, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int nn = mv->nnode;
+  memset(grad, 0, sizeof(double) * (size_t)nn * nt * 3);
+  for (int e = 0; e < mv->nedge; e++) {
+    const int l = mv->edges[2 * e], r = mv->edges[2 * e + 1];
+    const double* xL = &mv->xyz[3 * (size_t)l];
+    const double* xR = &mv->xyz[3 * (size_t)r];
+    double dx[3] = {xL[0] - xR[0], xL[1] - xR[1], xL[2] - xR[2]};
+    const double* qL = &q[(size_t)l * nv];
+    const double* qR = &q[(size_t)r * nv];
+    const double dx2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    const double weight = 1.0 / sqrt(dx2);
+    dx[0] *= weight;
+    dx[1] *= weight;
+    dx[2] *= weight;
+    double weL[3], weR[3];
+    oracle_lsq_coeff(&mv->sw[6 * (size_t)l], dx, weL);
+    dx[0] = -dx[0];
+    dx[1] = -dx[1];
+    dx[2] = -dx[2];
+    oracle_lsq_coeff(&mv->sw[6 * (size_t)r], dx, weR);
+    for (int i = 0; i < nt; i++) {
+      const int k = i < ns + 4 ? i : 2 * ns + 6 + (i - ns - 4);
+      const double dq = weight * (qR[k] - qL[k]);
+      for (int j = 0; j < 3; j++) {
+        grad[(size_t)r * nt * 3 + 3 * i + j] += +weR[j] * dq;
+        grad[(size_t)l * nt * 3 + 3 * i + j] += -weL[j] * dq;
+      }
+    }
+  }
+  for (int k = 0; k < mv->nbedge; k++) {
+    int sym = 0;
+    for (int t = 0; t < nsym; t++) sym |= mv->bfactag[k] == sym_tags[t];
+    if (!sym) continue;
+    const int l = mv->bedges[2 * k];
+    const double* a = &mv->bedge_area[4 * (size_t)k];
+    double* g = &grad[(size_t)l * nt * 3];
+    for (int i = 0; i < nt; i++) {
+      const double dot = g[3 * i] * a[0] + g[3 * i + 1] * a[1] + g[3 * i + 2] * a[2];
+      for (int j = 0; j < 3; j++) g[3 * i + j] -= dot * a[j];
+    }
+  }
+  return 0;
+}
+
+/* ---- boundary conditions ----------------------------------------------------
+ * UpdateBCs (ucs/bc.tcc:1400) of the reacting set on one partition, half-edge
+ * by half-edge in order, each through CalculateBoundaryVariables (:1059) and
+ * then ComputeAuxiliaryVariables of the phantom and the node:
+ *   sonic inflow, Dirichlet: node and phantom take the tag's reference record;
+ *   sonic outflow, Neumann: the phantom copies the node's rhoi, u, v, w, T;
+ *   no-slip, isothermal (twall > 0, K): GetViscousWallBoundaryVariables
+ *     (ucs/compressibleFR.tcc:2049) with a resting wall: node and phantom
+ *     take u = v = w = 0 and T = twall / ref_temperature, the phantom the
+ *     node's rhoi;
+ *   impermeable wall, symmetry with no characteristic condition (no_cvbc):
+ *     GetInviscidWallBoundaryVariables (:1042), a static grid: the phantom is
+ *     the node's record with the velocity mirrored in the face.
+ * Other types (far field, the characteristic wall, the adiabatic no-slip
+ * wall) are not restated: returns the first such half-edge + 1, else 0. */
+static void fr_aux(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double* Q) {
+  const int ns = m->nspecies;
+  double rho = 0.0;
+  for (int i = 0; i < ns; i++) rho += Q[i];
+  oracle_chem_aux(m, ref, Q, Q[ns + 3], &Q[ns + 4], &Q[ns + 6], &Q[2 * ns + 6]);
+  Q[ns + 5] = rho;
+}
+
+int oracle_chem_update_bcs(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_mesh_view* mv, int ntags,
+                           const int* bc_type, const double* twall, const double* qref, int no_cvbc, double* q) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  for (int k = 0; k < mv->nbedge; k++) {
+    const int tag = mv->bfactag[k];
+    const int bt = (tag >= 0 && tag < ntags) ? bc_type[tag] : -1;
+    double* QL = q + (size_t)mv->bedges[2 * k] * nv;
+    double* QR = q + (size_t)mv->bedges[2 * k + 1] * nv;
+    const double* a = &mv->bedge_area[4 * (size_t)k];
+    if (bt == PCFD_BC_SONIC_INFLOW || bt == PCFD_BC_DIRICHLET) {
+      for (int i = 0; i < nv; i++) QR[i] = QL[i] = qref[(size_t)tag * nv + i];
+    } else if (bt == PCFD_BC_SONIC_OUTFLOW || bt == PCFD_BC_NEUMANN) {
+      for (int i = 0; i < neqn; i++) QR[i] = QL[i];
+    } else if (bt == PCFD_BC_NOSLIP && twall[tag] > 0.0) {
+      for (int i = 0; i < ns; i++) QR[i] = QL[i];
+      QR[ns + 3] = QL[ns + 3] = twall[tag] / ref->temperature;
+      QR[ns] = QL[ns] = 0.0;
+      QR[ns + 1] = QL[ns + 1] = 0.0;
+      QR[ns + 2] = QL[ns + 2] = 0.0;
+    } else if ((bt == PCFD_BC_IMPERMEABLE_WALL || bt == PCFD_BC_SYMMETRY) && no_cvbc) {
+      double Qm[6 + 3 * PCFD_CHEM_MAX_SPECIES];
+      for (int i = 0; i < nv; i++) Qm[i] = QL[i];
+      fr_aux(m, ref, Qm);
+      for (int i = 0; i < neqn; i++) QR[i] = Qm[i];
+      const double dot = 2.0 * (Qm[ns] * a[0] + Qm[ns + 1] * a[1] + Qm[ns + 2] * a[2]);
+      QR[ns] = Qm[ns] - dot * a[0];
+      QR[ns + 1] = Qm[ns + 1] - dot * a[1];
+      QR[ns + 2] = Qm[ns + 2] - dot * a[2];
+    } else {
+      return k + 1;
+    }
+    fr_aux(m, ref, QR);
+    fr_aux(m, ref, QL);
+  }
+  return 0;
+}

@@ -486,6 +486,8 @@ static void lsq_coeff(const double* s, const double* dxbar, double* we) {
   we[0] = (r11 == 0.0) ? 0.0 : (dxbar[0] - r12 * we[1] - r13 * we[2]) / r11;
 }
 
+void oracle_lsq_coeff(const double* s, const double* dxbar, double* we) { lsq_coeff(s, dxbar, we); }
+
 static const int kGradList[NTERMS] = {0, 1, 2, 3, 4, 5, 7, 8, 9}; /* GetGradientsLocation, :1014 */
 
 /* Gradient::Compute with Kernel_LSQ_Gradient (weighted), then

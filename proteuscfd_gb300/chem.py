@@ -248,6 +248,43 @@ class ChemModel:
                                              N.dptr(q), N.dptr(b), N.dptr(norms), 0), "pcfd_chem_residual")
         return b, norms
 
+    @staticmethod
+    def bc_tables(nrec, bc_type, twall=None, qref=None):
+        """Per-tag tables of update_bcs from dicts tag -> type / K / record."""
+        ntags = max(bc_type) + 1
+        bt = np.full(ntags, -1, dtype=np.int32)
+        tw = np.zeros(ntags)
+        qr = np.zeros((ntags, nrec))
+        for t, v in bc_type.items():
+            bt[t] = v
+        for t, v in (twall or {}).items():
+            tw[t] = v
+        for t, v in (qref or {}).items():
+            qr[t] = v
+        return bt, tw, qr
+
+    def update_bcs(self, ref, q, bc_type, twall=None, qref=None, no_cvbc=1):
+        """UpdateBCs of the reacting set on the attached mesh: returns the
+        updated records (q [nnode + nbedge][6 + 3 ns] is not changed)."""
+        m = self._mesh
+        nrec = 6 + 3 * self.nspecies
+        q = np.array(self._arr(q, (m.nnode + m.nbedge, nrec)), copy=True)
+        bt, tw, qr = self.bc_tables(nrec, bc_type, twall, qref)
+        N.check(self._lib.pcfd_chem_update_bcs(self._h, C.byref(ref), len(bt), N.iptr(bt), N.dptr(tw), N.dptr(qr),
+                                               int(no_cvbc), q.ctypes.data, 0), "pcfd_chem_update_bcs")
+        return q
+
+    def gradient(self, q, sym_tags=()):
+        """The reacting set's LSQ gradient on the attached mesh: q [nnode + nbedge][6 + 3 ns]
+        -> grad [nnode][2 ns + 4][3], with the symmetry fix on the given tags."""
+        m = self._mesh
+        q = self._arr(q, (m.nnode + m.nbedge, 6 + 3 * self.nspecies))
+        tags = np.ascontiguousarray(list(sym_tags) or [0], dtype=np.int32)
+        grad = np.empty((m.nnode, 2 * self.nspecies + 4, 3))
+        N.check(self._lib.pcfd_chem_gradient(self._h, q.ctypes.data, N.iptr(tags), len(sym_tags), grad.ctypes.data, 0),
+                "pcfd_chem_gradient")
+        return grad
+
     def viscous_residual(self, ref, opts, Re, directional, q, grad):
         """The viscous part of the reacting residual on the attached mesh:
         q [nnode + nbedge][6 + 3 ns] records, grad [nnode][2 ns + 4][3] ->

@@ -69,6 +69,10 @@ struct ChemHandle {
   int *d_nptr = nullptr, *d_nedg = nullptr, *d_bptr = nullptr, *d_bhe = nullptr;
   double *d_q = nullptr, *d_ef = nullptr, *d_bf = nullptr, *d_b = nullptr, *d_part = nullptr, *d_norms = nullptr;
   double* d_xyz = nullptr;   // node coordinates (the viscous flux's directional correction)
+  double* d_sw = nullptr;    // LSQ normal matrices [nnode][6] (the gradient)
+  int* d_btag = nullptr;     // half-edge face tags (the gradient's symmetry fix, the conditions)
+  void* d_bctab = nullptr;   // per-tag condition tables of pcfd_chem_update_bcs
+  size_t bc_cap = 0;
   double* d_grad = nullptr;  // host-array gradient of the viscous residual [nnode][2 ns + 4][3]
 };
 
@@ -802,6 +806,175 @@ __global__ void __launch_bounds__(128) k_chem_bflux(long long nbedge, const pcfd
 // per node: -sum of the fluxes out of it (incident edges in ascending id,
 // signed: ~e where the node is the edge's left end), then its boundary
 // half-edges, then vol * wdot; per-block partial sums of squares
+// Gradient<T>::Compute of the reacting set, one node per thread: the
+// weighted least-squares gradient (Kernel_LSQ_Gradient, ucs/gradient.tcc:251,
+// with ComputeLSQCoefficients, :141) of the gradient list of
+// GetGradientsLocation (ucs/compressibleFR.tcc:693: rhoi, u, v, w, T,
+// concentrations) over the node's edges in ascending edge order, each edge's
+// term formed as the edge-ordered sum forms it; then Bkernel_Symmetry_Fix
+// (:545) on the node's half-edges whose tag is in sym (nsym entries).
+constexpr int kChemMaxSym = 8;
+struct ChemSym {
+  int n;
+  int tag[kChemMaxSym];
+};
+
+__global__ void __launch_bounds__(128) k_chem_gradient(long long nnode, const pcfd_chem_model* __restrict__ gm,
+                                                       const double* __restrict__ q, const int2* __restrict__ en,
+                                                       const int* __restrict__ nptr, const int* __restrict__ nedg,
+                                                       const double* __restrict__ xyz, const double* __restrict__ sw,
+                                                       const int* __restrict__ bptr, const int* __restrict__ bhe,
+                                                       const int* __restrict__ btag, const EdgeArea* __restrict__ ba,
+                                                       ChemSym sym, double* __restrict__ grad) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  const pcfd_chem_model& m = *gm;
+  const int ns = m.nspecies, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  double g[3 * (2 * PCFD_CHEM_MAX_SPECIES + 4)];
+  for (int t = 0; t < 3 * nt; t++) g[t] = 0.0;
+  const double* s = &sw[6 * i];
+  const double s11 = s[0], s12 = s[1], s13 = s[2], s22 = s[3], s23 = s[4], s33 = s[5];
+  const double r11 = s11, r12 = s12, r13 = s13;
+  const double r12_r11 = (r11 == 0.0) ? 0.0 : r12 / r11;
+  const double r22 = s22 - r12 * r12_r11;
+  const double r23 = s23 - r12_r11 * r13;
+  const double r13_r11 = (r11 == 0.0) ? 0.0 : r13 / r11;
+  const double r23_r22 = (r22 == 0.0) ? 0.0 : r23 / r22;
+  const double r33 = s33 - r13 * r13_r11 - r23 * r23_r22;
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    const int se = nedg[k];
+    const bool left = se < 0;
+    const int2 n = en[left ? ~se : se];
+    const double* xL = &xyz[3 * (size_t)n.x];
+    const double* xR = &xyz[3 * (size_t)n.y];
+    double d0 = xL[0] - xR[0], d1 = xL[1] - xR[1], d2 = xL[2] - xR[2];
+    const double weight = 1.0 / sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    d0 *= weight;
+    d1 *= weight;
+    d2 *= weight;
+    if (!left) {
+      d0 = -d0;
+      d1 = -d1;
+      d2 = -d2;
+    }
+    const double dykdx = (d1 - r12_r11 * d0);
+    const double we2 = (r33 == 0.0) ? 0.0 : (d2 - r13_r11 * d0 - r23_r22 * dykdx) / r33;
+    const double we1 = (r22 == 0.0) ? 0.0 : (dykdx - r23 * we2) / r22;
+    const double we0 = (r11 == 0.0) ? 0.0 : (d0 - r12 * we1 - r13 * we2) / r11;
+    const double* qL = &q[(size_t)n.x * nv];
+    const double* qR = &q[(size_t)n.y * nv];
+    for (int t = 0; t < nt; t++) {
+      const int loc = t < ns + 4 ? t : 2 * ns + 6 + (t - ns - 4);
+      const double dq = weight * (qR[loc] - qL[loc]);
+      if (left) {
+        g[3 * t + 0] += -we0 * dq;
+        g[3 * t + 1] += -we1 * dq;
+        g[3 * t + 2] += -we2 * dq;
+      } else {
+        g[3 * t + 0] += +we0 * dq;
+        g[3 * t + 1] += +we1 * dq;
+        g[3 * t + 2] += +we2 * dq;
+      }
+    }
+  }
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    const int he = bhe[p];
+    bool on = false;
+    for (int u = 0; u < sym.n; u++) on |= btag[he] == sym.tag[u];
+    if (!on) continue;
+    const EdgeArea a = ba[he];
+    for (int t = 0; t < nt; t++) {
+      const double dot = g[3 * t] * a.x + g[3 * t + 1] * a.y + g[3 * t + 2] * a.z;
+      g[3 * t + 0] -= dot * a.x;
+      g[3 * t + 1] -= dot * a.y;
+      g[3 * t + 2] -= dot * a.z;
+    }
+  }
+  for (int t = 0; t < 3 * nt; t++) grad[(size_t)i * nt * 3 + t] = g[t];
+}
+
+// ComputeAuxiliaryVariables (ucs/compressibleFR.tcc:755) of one record in
+// place: P, rho, cvi, concentrations from rhoi and T (as k_chem_aux forms them)
+__device__ void record_aux(const pcfd_chem_model& m, const ChemDerived& d, const pcfd_chem_ref& ref, double* Q) {
+  const int ns = m.nspecies;
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES], rho = 0.0;
+  for (int i = 0; i < ns; i++) {
+    rho += Q[i];
+    rhoiDim[i] = Q[i] * ref.density;
+  }
+  const double TDim = Q[ns + 3] * ref.temperature;
+  Q[ns + 4] = mix_P(d, ns, rhoiDim, TDim) / ref.pressure;
+  Q[ns + 5] = rho;
+  const double s_ref = ref.velocity * ref.velocity / ref.temperature;
+  for (int i = 0; i < ns; i++) {
+    Q[ns + 6 + i] = (species_cp(d, i, TDim) - d.R[i]) / s_ref;
+    Q[2 * ns + 6 + i] = Q[i] / m.mw[i] / 1000.0;
+  }
+}
+
+// UpdateBCs (ucs/bc.tcc:1400) of the reacting set, one boundary node per
+// thread: the node's half-edges in ascending order, each through
+// CalculateBoundaryVariables (:1059) and then ComputeAuxiliaryVariables of
+// its phantom and of the node.  A half-edge changes only its node and its
+// own phantom, so per node this is the reference's sequential order.
+// Types: sonic inflow / Dirichlet (the tag's reference record), sonic
+// outflow / Neumann (copy), isothermal no-slip with a resting wall
+// (GetViscousWallBoundaryVariables, ucs/compressibleFR.tcc:2049), and with
+// no_cvbc the impermeable wall / symmetry (mirror, :1042); any other type
+// is counted in *bad and leaves the records as they are.
+struct ChemBc {
+  int ntags, no_cvbc;
+  const int* type;
+  const double* twall;
+  const double* qref;
+};
+
+__global__ void __launch_bounds__(128) k_chem_bcs(long long nnode, const pcfd_chem_model* __restrict__ gm,
+                                                  const ChemDerived* __restrict__ gd, pcfd_chem_ref ref, ChemBc bc,
+                                                  const int2* __restrict__ bn, const EdgeArea* __restrict__ ba,
+                                                  const int* __restrict__ btag, const int* __restrict__ bptr,
+                                                  const int* __restrict__ bhe, double* __restrict__ q,
+                                                  long long* bad_count) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nnode || bptr[i] == bptr[i + 1]) return;
+  const pcfd_chem_model& m = *gm;
+  const ChemDerived& d = *gd;
+  const int ns = m.nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  double* QL = &q[(size_t)i * nv];
+  for (int p = bptr[i]; p < bptr[i + 1]; p++) {
+    const int k = bhe[p];
+    const int tag = btag[k];
+    const int bt = (tag >= 0 && tag < bc.ntags) ? bc.type[tag] : -1;
+    double* QR = &q[(size_t)bn[k].y * nv];
+    if (bt == PCFD_BC_SONIC_INFLOW || bt == PCFD_BC_DIRICHLET) {
+      for (int j = 0; j < nv; j++) QR[j] = QL[j] = bc.qref[(size_t)tag * nv + j];
+    } else if (bt == PCFD_BC_SONIC_OUTFLOW || bt == PCFD_BC_NEUMANN) {
+      for (int j = 0; j < neqn; j++) QR[j] = QL[j];
+    } else if (bt == PCFD_BC_NOSLIP && bc.twall[tag] > 0.0) {
+      for (int j = 0; j < ns; j++) QR[j] = QL[j];
+      QR[ns + 3] = QL[ns + 3] = bc.twall[tag] / ref.temperature;
+      QR[ns] = QL[ns] = 0.0;
+      QR[ns + 1] = QL[ns + 1] = 0.0;
+      QR[ns + 2] = QL[ns + 2] = 0.0;
+    } else if ((bt == PCFD_BC_IMPERMEABLE_WALL || bt == PCFD_BC_SYMMETRY) && bc.no_cvbc) {
+      double Qm[6 + 3 * PCFD_CHEM_MAX_SPECIES];
+      for (int j = 0; j < nv; j++) Qm[j] = QL[j];
+      record_aux(m, d, ref, Qm);
+      for (int j = 0; j < neqn; j++) QR[j] = Qm[j];
+      const EdgeArea a = ba[k];
+      const double dot = 2.0 * (Qm[ns] * a.x + Qm[ns + 1] * a.y + Qm[ns + 2] * a.z);
+      QR[ns] = Qm[ns] - dot * a.x;
+      QR[ns + 1] = Qm[ns + 1] - dot * a.y;
+      QR[ns + 2] = Qm[ns + 2] - dot * a.z;
+    } else {
+      atomicAdd((unsigned long long*)bad_count, 1ull);
+      continue;
+    }
+    record_aux(m, d, ref, QR);
+    record_aux(m, d, ref, QL);
+  }
+}
+
 // CompressibleFREqnSet::ViscousFlux (ucs/compressibleFR.tcc:551) on the face
 // state Q (native record) and face gradient g of the reacting gradient list
 // (rhoi, u, v, w, T, concentrations): laminar, no species diffusion
@@ -1429,11 +1602,15 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   }
   for (long long k = 0; k < nb; k++) bhe[bfill[m->bedges[2 * k]]++] = (int)k;
   void* mesh_ptrs[] = {c->d_en, c->d_bn, c->d_ea, c->d_ba, c->d_vol, c->d_nptr, c->d_nedg, c->d_bptr,
-                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms, c->d_xyz, c->d_grad};
+                       c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms, c->d_xyz, c->d_grad,
+                       c->d_sw, c->d_btag, c->d_bctab};
   for (void* p : mesh_ptrs) cudaFree(p);
   c->d_en = c->d_bn = nullptr;
   c->d_ea = c->d_ba = nullptr;
-  c->d_vol = c->d_q = c->d_ef = c->d_bf = c->d_b = c->d_part = c->d_norms = c->d_xyz = c->d_grad = nullptr;
+  c->d_vol = c->d_q = c->d_ef = c->d_bf = c->d_b = c->d_part = c->d_norms = c->d_xyz = c->d_grad = c->d_sw = nullptr;
+  c->d_btag = nullptr;
+  c->d_bctab = nullptr;
+  c->bc_cap = 0;
   c->d_nptr = c->d_nedg = c->d_bptr = c->d_bhe = nullptr;
   c->nnode = c->nedge = c->nbedge = 0;
   const int ns = c->host.nspecies, neqn = ns + 4;
@@ -1450,6 +1627,8 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   if (e == cudaSuccess) e = up((void**)&c->d_ba, m->bedge_area, (size_t)nb * 4 * sizeof(double));
   if (e == cudaSuccess) e = up((void**)&c->d_vol, m->vol, (size_t)nn * sizeof(double));
   if (e == cudaSuccess && m->xyz) e = up((void**)&c->d_xyz, m->xyz, (size_t)nn * 3 * sizeof(double));
+  if (e == cudaSuccess && m->sw) e = up((void**)&c->d_sw, m->sw, (size_t)nn * 6 * sizeof(double));
+  if (e == cudaSuccess && m->bfactag) e = up((void**)&c->d_btag, m->bfactag, (size_t)nb * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_nptr, nptr.data(), nptr.size() * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_nedg, nedg.data(), nedg.size() * sizeof(int));
   if (e == cudaSuccess) e = up((void**)&c->d_bptr, bptr.data(), bptr.size() * sizeof(int));
@@ -1464,6 +1643,100 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   c->nnode = nn;
   c->nedge = ne;
   c->nbedge = nb;
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_update_bcs(pcfd_chem_t h, const pcfd_chem_ref* ref, int ntags, const int* bc_type,
+                                  const double* twall, const double* qref, int no_cvbc, double* q, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || ntags <= 0 || !bc_type || !twall || !qref || !q) {
+    pcfd_set_last_error("pcfd_chem_update_bcs: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0 || (c->nbedge > 0 && !c->d_btag)) {
+    pcfd_set_last_error("pcfd_chem_update_bcs: no mesh with face tags attached");
+    return PCFD_ERR_STATE;
+  }
+  const int ns = c->host.nspecies;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, nb = c->nbedge;
+  // the per-tag tables on the device
+  const size_t tb = (size_t)ntags * (sizeof(int) + sizeof(double) + nv * sizeof(double));
+  if (c->bc_cap < tb) {
+    cudaFree(c->d_bctab);
+    c->d_bctab = nullptr;
+    c->bc_cap = 0;
+    CHEM_TRY(cudaMalloc(&c->d_bctab, tb), "chem buffers");
+    c->bc_cap = tb;
+  }
+  double* d_twall = (double*)c->d_bctab;
+  double* d_qref = d_twall + ntags;
+  int* d_type = (int*)(d_qref + (size_t)ntags * nv);
+  CHEM_TRY(cudaMemcpyAsync(d_twall, twall, (size_t)ntags * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+           "chem copy");
+  CHEM_TRY(cudaMemcpyAsync(d_qref, qref, (size_t)ntags * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+           "chem copy");
+  CHEM_TRY(cudaMemcpyAsync(d_type, bc_type, (size_t)ntags * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "chem copy");
+  double* dq = q;
+  if (!dev) {
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    dq = c->d_q;
+  }
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  const ChemBc bc{ntags, no_cvbc, d_type, d_twall, d_qref};
+  k_chem_bcs<<<CHEM_GRID(nn)>>>(nn, c->dev, c->dder, *ref, bc, c->d_bn, c->d_ba, c->d_btag, c->d_bptr, c->d_bhe, dq,
+                                c->d_count);
+  CHEM_TRY(cudaGetLastError(), "k_chem_bcs launch");
+  if (!dev)
+    CHEM_TRY(cudaMemcpyAsync(q, dq, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  long long bad = 0;
+  CHEM_TRY(cudaMemcpyAsync(&bad, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem boundary conditions");
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_update_bcs: " + std::to_string(bad) +
+                        " half-edge(s) with a condition the reacting path does not build (far field, "
+                        "characteristic wall, adiabatic no-slip)");
+    return PCFD_ERR_ARG;
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_gradient(pcfd_chem_t h, const double* q, const int* sym_tags, int nsym, double* grad,
+                                int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !q || !grad || nsym < 0 || nsym > kChemMaxSym || (nsym > 0 && !sym_tags)) {
+    pcfd_set_last_error("pcfd_chem_gradient: bad arguments (at most 8 symmetry tags)");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0 || !c->d_xyz || !c->d_sw || (c->nbedge > 0 && !c->d_btag)) {
+    pcfd_set_last_error("pcfd_chem_gradient: no mesh with coordinates and LSQ matrices attached");
+    return PCFD_ERR_STATE;
+  }
+  const int ns = c->host.nspecies, nt = 2 * ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, nb = c->nbedge;
+  ChemSym sym{nsym, {0}};
+  for (int u = 0; u < nsym; u++) sym.tag[u] = sym_tags[u];
+  const double* dq = q;
+  double* dg = grad;
+  if (!dev) {
+    if (!c->d_grad) CHEM_TRY(cudaMalloc(&c->d_grad, (size_t)nn * nt * 3 * sizeof(double)), "chem buffers");
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    dq = c->d_q;
+    dg = c->d_grad;
+  }
+  k_chem_gradient<<<CHEM_GRID(nn)>>>(nn, c->dev, dq, c->d_en, c->d_nptr, c->d_nedg, c->d_xyz, c->d_sw, c->d_bptr,
+                                     c->d_bhe, c->d_btag, c->d_ba, sym, dg);
+  CHEM_TRY(cudaGetLastError(), "k_chem_gradient launch");
+  if (!dev)
+    CHEM_TRY(cudaMemcpyAsync(grad, dg, (size_t)nn * nt * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem gradient");
   return PCFD_OK;
 }
 

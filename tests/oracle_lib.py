@@ -70,6 +70,10 @@ def lib():
                                        _DP]),
             "oracle_chem_transport_n": (C.c_longlong, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.c_longlong,
                                                        _DP, _DP, _DP, _DP]),
+            "oracle_chem_gradient": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.MeshView), _DP, _IP, C.c_int,
+                                               _DP]),
+            "oracle_chem_update_bcs": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.MeshView),
+                                                 C.c_int, _IP, _DP, _DP, C.c_int, _DP]),
             "oracle_chem_viscous_residual": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
                                                        C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), C.c_double,
                                                        C.c_int, _DP, _DP, _DP]),
@@ -515,6 +519,22 @@ class OracleChemState:
         self.L.oracle_chem_temporal_n(C.byref(self.m), C.byref(self.ref), n, dp(arr(q)), dp(arr(vol)), dp(arr(dtau)),
                                       dp(arr(beta)), float(cnp1), float(dt), int(local_ts), dp(A))
         return A
+
+    def update_bcs(self, mesh, q, bc_type, twall=None, qref=None, no_cvbc=1):
+        """(updated records, first half-edge of an unbuilt type + 1 or 0)."""
+        from proteuscfd_gb300.chem import ChemModel
+        q = np.array(q, dtype=np.float64, copy=True)
+        bt, tw, qr = ChemModel.bc_tables(q.shape[1], bc_type, twall, qref)
+        rc = self.L.oracle_chem_update_bcs(C.byref(self.m), C.byref(self.ref), C.byref(mesh.view), len(bt), ip(bt),
+                                           dp(tw), dp(np.ascontiguousarray(qr)), int(no_cvbc), dp(q))
+        return q, rc
+
+    def gradient(self, mesh, q, sym_tags=()):
+        q = np.ascontiguousarray(q, np.float64)
+        tags = np.ascontiguousarray(list(sym_tags) or [0], dtype=np.int32)
+        grad = np.empty((mesh.nnode, 2 * self.ns + 4, 3))
+        self.L.oracle_chem_gradient(C.byref(self.m), C.byref(mesh.view), dp(q), ip(tags), len(sym_tags), dp(grad))
+        return grad
 
     def viscous_residual(self, opts, mesh, Re, directional, q, grad):
         """The viscous part of the reacting residual; returns (b, faces above

@@ -344,3 +344,73 @@ def test_viscous_residual_properties():
     ba = m.bedge_area
     expect = -(-(mu[0] / 1.0e4) * a * (ba[:, 1] * ba[:, 3])).sum()
     assert abs(b2[:, ns].sum() - expect) < 1e-12 * abs(expect) + 1e-18
+
+
+def test_gradient_linear_exactness():
+    """The oracle's reacting LSQ gradient reproduces fields linear in x, y, z
+    exactly at every node (the weighted least squares is exact for them),
+    and the symmetry fix removes the normal part on the listed tags."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=4)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=5)
+    x = np.r_[m.xyz, m.xyz[m.bedges[:, 0]]]
+    a = np.array([0.3, -0.2, 0.1])
+    lin = x @ a
+    rhoi[:] = rhoi[0] * (1.0 + 0.1 * lin[:, None])
+    vel[:, 0] = 0.2 + 0.5 * lin
+    T[:] = T[0] * (1.0 + 0.05 * lin)
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(spec), ref)
+    g = O.gradient(m, q)
+    assert np.allclose(g[:, ns, :], 0.5 * a, rtol=0, atol=1e-12)         # u
+    assert np.allclose(g[:, ns + 3, :], 0.05 * T[0] * a, rtol=0, atol=1e-12)  # T
+    assert np.allclose(g[:, 0, :], 0.1 * rhoi[0, 0] * a, rtol=0, atol=1e-9 * rhoi[0, 0])
+    gs = O.gradient(m, q, sym_tags=[5, 6])
+    zmin = m.bfactag == 5
+    nodes = np.unique(m.bedges[zmin, 0])
+    assert np.allclose(gs[nodes, ns, 2], 0.0, atol=1e-12)
+
+
+def test_boundary_conditions():
+    """The oracle's reacting UpdateBCs: inflow nodes and phantoms take the
+    reference record, outflow phantoms copy their node, the isothermal wall
+    rests at its temperature, and the mirror flips the normal velocity and
+    keeps the tangential one; an unbuilt type (far field) is reported."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    from proteuscfd_gb300 import _native as N
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=4)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=6)
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(spec), ref)
+    types = {1: N.BC_SONIC_INFLOW, 2: N.BC_SONIC_OUTFLOW, 3: N.BC_NOSLIP, 4: N.BC_SYMMETRY, 5: N.BC_SYMMETRY,
+             6: N.BC_IMPERMEABLE_WALL}
+    qin = q[0].copy()
+    q2, rc = O.update_bcs(m, q, types, twall={3: 2000.0}, qref={1: qin})
+    assert rc == 0
+    be, tag, ba = m.bedges, m.bfactag, m.bedge_area
+    order = np.arange(m.nbedge)
+    last = {}
+    for k in order:          # the last half-edge of each node decides its state
+        last[be[k, 0]] = k
+    for k in order:
+        node, ph = be[k]
+        if tag[k] == 1:
+            assert np.allclose(q2[ph, :ns + 4], qin[:ns + 4], rtol=0, atol=0)
+        if tag[k] == 3 and last[node] == k:
+            assert np.all(q2[node, ns:ns + 3] == 0.0) and q2[node, ns + 3] == 2000.0 / ref.temperature
+        if tag[k] in (4, 6) and last[node] == k:
+            vn = q2[node, ns:ns + 3] @ ba[k, :3]
+            assert np.allclose(q2[ph, ns:ns + 3] @ ba[k, :3], -vn, atol=1e-13)
+    # far field is not restated: reported, records left as they were
+    _, rc = O.update_bcs(m, q, {**types, 2: N.BC_FARFIELD}, twall={3: 2000.0}, qref={1: qin})
+    assert rc > 0 and tag[rc - 1] == 2

@@ -365,3 +365,61 @@ def test_fr_viscous_residual_parity(directional):
     assert (np.abs(b - bo) / scale).max() < 1e-12, (np.abs(b - bo) / scale).max()
     assert np.abs(b[:, :ns]).max() == 0.0
     C.close()
+
+
+def test_fr_gradient_parity_and_viscous_chain():
+    """The reacting LSQ gradient on the GPU against the oracle (the same
+    operations in the same order per node), with the symmetry fix on two
+    tags; then the viscous residual fed the GPU's own gradient."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    m = Mesh.box(12, 9, 8, jitter=0.2, seed=6)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=23)
+    q = fr_records(ref, rhoi, vel, T)
+    C = ChemModel(spec)
+    C.attach_mesh(m)
+    O = OracleChemState(model_struct(spec), ref)
+    g = C.gradient(q, sym_tags=[5, 6])
+    go = O.gradient(m, q, sym_tags=[5, 6])
+    scale = np.abs(go).reshape(m.nnode, -1).max(axis=0)
+    scale[scale == 0] = 1.0
+    assert (np.abs(g - go).reshape(m.nnode, -1) / scale).max() < 1e-13
+    opts = C.flux_opts(1.0, 0.4, 0)
+    b = C.viscous_residual(ref, opts, 2.0e4, 1, q, g)
+    bo, _ = O.viscous_residual(opts, m, 2.0e4, 1, q, go)
+    sc = np.abs(bo).max(axis=0, keepdims=True)
+    sc[sc == 0] = 1.0
+    assert (np.abs(b - bo) / sc).max() < 1e-11
+    C.close()
+
+
+def test_fr_boundary_conditions_parity():
+    """The reacting UpdateBCs on the GPU against the oracle (inflow, outflow,
+    isothermal wall, mirror), node by node in half-edge order; an unbuilt
+    type is refused."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    m = Mesh.box(12, 9, 8, jitter=0.2, seed=7)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=24)
+    q = fr_records(ref, rhoi, vel, T)
+    C = ChemModel(spec)
+    C.attach_mesh(m)
+    O = OracleChemState(model_struct(spec), ref)
+    types = {1: N.BC_SONIC_INFLOW, 2: N.BC_SONIC_OUTFLOW, 3: N.BC_NOSLIP, 4: N.BC_SYMMETRY, 5: N.BC_SYMMETRY,
+             6: N.BC_IMPERMEABLE_WALL}
+    kw = dict(twall={3: 2000.0}, qref={1: q[0]})
+    q2 = C.update_bcs(ref, q, types, **kw)
+    qo, rc = O.update_bcs(m, q, types, **kw)
+    assert rc == 0
+    scale = np.abs(qo).max(axis=0, keepdims=True)
+    scale[scale == 0] = 1.0
+    assert (np.abs(q2 - qo) / scale).max() < 1e-13
+    with pytest.raises(N.PcfdError):
+        C.update_bcs(ref, q, {**types, 2: N.BC_FARFIELD}, **kw)
+    C.close()
