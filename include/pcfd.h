@@ -508,6 +508,17 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t c, const pcfd_mesh_view* m);
  * (optional; ParallelL2Norm and StridedParallelL2Norm).  dev as above (q, b). */
 PCFD_API int pcfd_chem_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
                                 double ref_time, int reactions, const double* q, double* b, double* norms, int dev);
+/* The same residual at second order (Kernel_Inviscid_Flux past the
+ * first-order steps, ucs/residual.tcc:192): each edge's records extrapolated
+ * to the midpoint by ExtrapolateVariables (ucs/compressibleFR.tcc:734),
+ * q + lim (chi/2 dQ + (1 - chi) grad.dx) on rhoi, u, v, w, T, their pressure
+ * and density recomputed, then HLLC; boundary half-edges stay first order
+ * (one partition).  grad [nnode][2 ns + 4][3] as pcfd_chem_gradient forms
+ * it, lim [nnode][ns + 4] the limiter (ones: unlimited).  Needs the attached
+ * mesh's coordinates.  dev as above (q, grad, lim, b). */
+PCFD_API int pcfd_chem_residual_ho(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, double chi,
+                                   double ref_time, int reactions, const double* q, const double* grad,
+                                   const double* lim, double* b, double* norms, int dev);
 /* UpdateBCs (ucs/bc.tcc:1400) of the reacting set on the attached mesh (which
  * must carry face tags), in place on q (as for pcfd_chem_residual): each
  * half-edge in order through CalculateBoundaryVariables (:1059), then

@@ -370,16 +370,49 @@ long long oracle_chem_hllc_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref,
  * records (the Bdriver), then SourceTerm (ucs/compressibleFR.tcc:1276) with
  * the production rates made non-dimensional by ref_density / ref_time; the
  * norms of ComputeResiduals (ucs/residual.tcc:13, ParallelL2Norm). */
-void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
-                          const pcfd_mesh_view* mv, const double* q, double ref_time, int reactions, double* b,
-                          double* norms) {
-  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+static void fr_aux_rec(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double* Q);
+
+/* With grad and lim (the second-order form, Kernel_Inviscid_Flux,
+ * ucs/residual.tcc:192): each edge's two records are extrapolated to the
+ * edge midpoint by CompressibleFREqnSet::ExtrapolateVariables
+ * (ucs/compressibleFR.tcc:734), q + lim (chi/2 dQ + (1 - chi) grad.dx) on
+ * rhoi, u, v, w, T with dx = (x_R - x_L)/2, and their auxiliary variables
+ * recomputed; boundary half-edges keep their records (one partition). */
+static void chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                          const pcfd_mesh_view* mv, const double* q, const double* grad, const double* lim,
+                          double chi, double ref_time, int reactions, double* b, double* norms) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
   const int nn = mv->nnode;
   double flux[PCFD_CHEM_MAX_SPECIES + 4];
+  double QL[6 + 3 * PCFD_CHEM_MAX_SPECIES], QR[6 + 3 * PCFD_CHEM_MAX_SPECIES];
   for (size_t i = 0; i < (size_t)nn * neqn; i++) b[i] = 0.0;
   for (int e = 0; e < mv->nedge; e++) {
     int a = mv->edges[2 * e], c = mv->edges[2 * e + 1];
-    oracle_chem_hllc(m, ref, o, q + (size_t)a * nv, q + (size_t)c * nv, mv->edge_area + 4 * (size_t)e, flux);
+    const double* qa = q + (size_t)a * nv;
+    const double* qc = q + (size_t)c * nv;
+    if (grad) {
+      double dx[3];
+      for (int i = 0; i < 3; i++) dx[i] = 0.5 * (mv->xyz[3 * (size_t)c + i] - mv->xyz[3 * (size_t)a + i]);
+      for (int i = 0; i < nv; i++) {
+        QL[i] = qa[i];
+        QR[i] = qc[i];
+      }
+      const double* gL = grad + (size_t)a * nt * 3;
+      const double* gR = grad + (size_t)c * nt * 3;
+      for (int j = 0; j < neqn; j++) {
+        const double dQ = qc[j] - qa[j];
+        const double cl = 0.5 * chi * dQ + (1.0 - chi) * (gL[3 * j] * dx[0] + gL[3 * j + 1] * dx[1] + gL[3 * j + 2] * dx[2]);
+        const double cr = 0.5 * chi * (-dQ) +
+                          (1.0 - chi) * (gR[3 * j] * (-dx[0]) + gR[3 * j + 1] * (-dx[1]) + gR[3 * j + 2] * (-dx[2]));
+        QL[j] = qa[j] + cl * lim[(size_t)a * neqn + j];
+        QR[j] = qc[j] + cr * lim[(size_t)c * neqn + j];
+      }
+      fr_aux_rec(m, ref, QL);
+      fr_aux_rec(m, ref, QR);
+      oracle_chem_hllc(m, ref, o, QL, QR, mv->edge_area + 4 * (size_t)e, flux);
+    } else {
+      oracle_chem_hllc(m, ref, o, qa, qc, mv->edge_area + 4 * (size_t)e, flux);
+    }
     for (int i = 0; i < neqn; i++) b[(size_t)c * neqn + i] += flux[i];
     for (int i = 0; i < neqn; i++) b[(size_t)a * neqn + i] += -flux[i];
   }
@@ -411,6 +444,18 @@ void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, co
       norms[1 + j] = sqrt(t) / (double)nn;
     }
   }
+}
+
+void oracle_chem_residual(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                          const pcfd_mesh_view* mv, const double* q, double ref_time, int reactions, double* b,
+                          double* norms) {
+  chem_residual(m, ref, o, mv, q, NULL, NULL, 0.0, ref_time, reactions, b, norms);
+}
+
+void oracle_chem_residual_ho(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o,
+                             const pcfd_mesh_view* mv, const double* q, const double* grad, const double* lim,
+                             double chi, double ref_time, int reactions, double* b, double* norms) {
+  chem_residual(m, ref, o, mv, q, grad, lim, chi, ref_time, reactions, b, norms);
 }
 
 /* CompressibleFREqnSet::SourceTerm (ucs/compressibleFR.tcc:1276), reactions
@@ -882,3 +927,6 @@ int oracle_chem_update_bcs(const pcfd_chem_model* m, const pcfd_chem_ref* ref, c
   }
   return 0;
 }
+
+/* ComputeAuxiliaryVariables of one record in place */
+static void fr_aux_rec(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double* Q) { fr_aux(m, ref, Q); }

@@ -298,6 +298,20 @@ class ChemModel:
                 "pcfd_chem_viscous_residual")
         return b
 
+    def residual_ho(self, ref, opts, chi, ref_time, reactions, q, grad, lim):
+        """The reacting residual at second order: q records, grad [nnode][2 ns + 4][3],
+        lim [nnode][ns + 4] -> (b [nnode][ns + 4], norms [1 + ns + 4])."""
+        m = self._mesh
+        q = self._arr(q, (m.nnode + m.nbedge, 6 + 3 * self.nspecies))
+        grad = self._arr(grad, (m.nnode, 2 * self.nspecies + 4, 3))
+        lim = self._arr(lim, (m.nnode, self.nspecies + 4))
+        b = np.empty((m.nnode, self.nspecies + 4))
+        norms = np.empty(1 + self.nspecies + 4)
+        N.check(self._lib.pcfd_chem_residual_ho(self._h, C.byref(ref), C.byref(opts), float(chi), float(ref_time),
+                                                int(reactions), q.ctypes.data, grad.ctypes.data, lim.ctypes.data,
+                                                b.ctypes.data, N.dptr(norms), 0), "pcfd_chem_residual_ho")
+        return b, norms
+
     def residual_dev(self, ref, opts, ref_time, reactions, q_ptr, b_ptr=None):
         """The same with q (and b, optional) as device addresses; returns the norms."""
         norms = np.empty(1 + self.nspecies + 4)

@@ -72,6 +72,7 @@ struct ChemHandle {
   double* d_sw = nullptr;    // LSQ normal matrices [nnode][6] (the gradient)
   int* d_btag = nullptr;     // half-edge face tags (the gradient's symmetry fix, the conditions)
   void* d_bctab = nullptr;   // per-tag condition tables of pcfd_chem_update_bcs
+  double* d_lim = nullptr;   // host-array limiter of the second-order residual [nnode][ns + 4]
   size_t bc_cap = 0;
   double* d_grad = nullptr;  // host-array gradient of the viscous residual [nnode][2 ns + 4][3]
 };
@@ -780,6 +781,53 @@ __global__ void __launch_bounds__(128) k_chem_hllc(long long nedge, long long nn
   double f[PCFD_CHEM_MAX_SPECIES + 4];
   if (fr_hllc(*gd, ns, ref, o, QL, QR, avec[e], f)) atomicAdd((unsigned long long*)nfail, 1ull);
   for (int i = 0; i < ns + 4; i++) flux[e * (ns + 4) + i] = f[i];
+}
+
+// Kernel_Inviscid_Flux (ucs/residual.tcc:192) at second order: both records
+// extrapolated to the edge midpoint (ExtrapolateVariables,
+// ucs/compressibleFR.tcc:734: q + lim (chi/2 dQ + (1 - chi) grad.dx) on
+// rhoi, u, v, w, T, dx = (x_R - x_L)/2), their pressure and density
+// recomputed (the part of ComputeAuxiliaryVariables the flux reads), then
+// the HLLC flux
+__global__ void __launch_bounds__(128) k_chem_hllc2(long long nedge, const pcfd_chem_model* __restrict__ gm,
+                                                    const ChemDerived* __restrict__ gd, pcfd_chem_ref ref,
+                                                    pcfd_chem_flux_opts o, double chi, const double* __restrict__ q,
+                                                    const double* __restrict__ grad, const double* __restrict__ lim,
+                                                    const double* __restrict__ xyz, const int2* __restrict__ edges,
+                                                    const EdgeArea* __restrict__ avec, double* __restrict__ flux,
+                                                    long long* __restrict__ nfail) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= nedge) return;
+  const int ns = gm->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int2 n = edges[e];
+  const double* qa = &q[(size_t)n.x * nv];
+  const double* qc = &q[(size_t)n.y * nv];
+  double dx[3];
+  for (int i = 0; i < 3; i++) dx[i] = 0.5 * (xyz[3 * (size_t)n.y + i] - xyz[3 * (size_t)n.x + i]);
+  const double* gL = &grad[(size_t)n.x * nt * 3];
+  const double* gR = &grad[(size_t)n.y * nt * 3];
+  double QL[6 + 2 * PCFD_CHEM_MAX_SPECIES], QR[6 + 2 * PCFD_CHEM_MAX_SPECIES];
+  for (int j = 0; j < neqn; j++) {
+    const double dQ = qc[j] - qa[j];
+    const double cl = 0.5 * chi * dQ + (1.0 - chi) * (gL[3 * j] * dx[0] + gL[3 * j + 1] * dx[1] + gL[3 * j + 2] * dx[2]);
+    const double cr = 0.5 * chi * (-dQ) +
+                      (1.0 - chi) * (gR[3 * j] * (-dx[0]) + gR[3 * j + 1] * (-dx[1]) + gR[3 * j + 2] * (-dx[2]));
+    QL[j] = qa[j] + cl * lim[(size_t)n.x * neqn + j];
+    QR[j] = qc[j] + cr * lim[(size_t)n.y * neqn + j];
+  }
+  for (int k = 0; k < 2; k++) {
+    double* Q = k ? QR : QL;
+    double rhoiDim[PCFD_CHEM_MAX_SPECIES], rho = 0.0;
+    for (int i = 0; i < ns; i++) {
+      rho += Q[i];
+      rhoiDim[i] = Q[i] * ref.density;
+    }
+    Q[ns + 4] = mix_P(*gd, ns, rhoiDim, Q[ns + 3] * ref.temperature) / ref.pressure;
+    Q[ns + 5] = rho;
+  }
+  double f[PCFD_CHEM_MAX_SPECIES + 4];
+  if (fr_hllc(*gd, ns, ref, o, QL, QR, avec[e], f)) atomicAdd((unsigned long long*)nfail, 1ull);
+  for (int i = 0; i < neqn; i++) flux[e * neqn + i] = f[i];
 }
 
 // boundary half-edges: the node's record against its phantom record
@@ -1603,7 +1651,7 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   for (long long k = 0; k < nb; k++) bhe[bfill[m->bedges[2 * k]]++] = (int)k;
   void* mesh_ptrs[] = {c->d_en, c->d_bn, c->d_ea, c->d_ba, c->d_vol, c->d_nptr, c->d_nedg, c->d_bptr,
                        c->d_bhe, c->d_q, c->d_ef, c->d_bf, c->d_b, c->d_part, c->d_norms, c->d_xyz, c->d_grad,
-                       c->d_sw, c->d_btag, c->d_bctab};
+                       c->d_sw, c->d_btag, c->d_bctab, c->d_lim};
   for (void* p : mesh_ptrs) cudaFree(p);
   c->d_en = c->d_bn = nullptr;
   c->d_ea = c->d_ba = nullptr;
@@ -1611,6 +1659,7 @@ PCFD_API int pcfd_chem_attach_mesh(pcfd_chem_t h, const pcfd_mesh_view* m) {
   c->d_btag = nullptr;
   c->d_bctab = nullptr;
   c->bc_cap = 0;
+  c->d_lim = nullptr;
   c->d_nptr = c->d_nedg = c->d_bptr = c->d_bhe = nullptr;
   c->nnode = c->nedge = c->nbedge = 0;
   const int ns = c->host.nspecies, neqn = ns + 4;
@@ -1860,6 +1909,82 @@ PCFD_API int pcfd_chem_residual(pcfd_chem_t h, const pcfd_chem_ref* ref, const p
   CHEM_TRY(cudaStreamSynchronize(c->stream), "chem residual");
   if (bad) {
     pcfd_set_last_error("pcfd_chem_residual: " + std::to_string(bad) + " face(s) with no HLLC branch");
+    return PCFD_ERR_NUMERIC;
+  }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_residual_ho(pcfd_chem_t h, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, double chi,
+                                   double ref_time, int reactions, const double* q, const double* grad,
+                                   const double* lim, double* b, double* norms, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !ref_ok(ref) || !o || !q || !grad || !lim || !(ref_time > 0.0)) {
+    pcfd_set_last_error("pcfd_chem_residual_ho: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0) {
+    pcfd_set_last_error("pcfd_chem_residual_ho: no mesh attached (pcfd_chem_attach_mesh)");
+    return PCFD_ERR_STATE;
+  }
+  if (!c->d_xyz) {
+    pcfd_set_last_error("pcfd_chem_residual_ho: the attached mesh has no coordinates");
+    return PCFD_ERR_STATE;
+  }
+  const int ns = c->host.nspecies, neqn = ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, ne = c->nedge, nb = c->nbedge;
+  const double* dq = q;
+  if (!dev) {
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    dq = c->d_q;
+  }
+  const int nt = 2 * ns + 4;
+  const double* dg = grad;
+  const double* dl = lim;
+  if (!dev) {
+    if (!c->d_grad) CHEM_TRY(cudaMalloc(&c->d_grad, (size_t)nn * nt * 3 * sizeof(double)), "chem buffers");
+    if (!c->d_lim) CHEM_TRY(cudaMalloc(&c->d_lim, (size_t)nn * neqn * sizeof(double)), "chem buffers");
+    CHEM_TRY(cudaMemcpyAsync(c->d_grad, grad, (size_t)nn * nt * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream),
+             "chem copy");
+    CHEM_TRY(cudaMemcpyAsync(c->d_lim, lim, (size_t)nn * neqn * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    dg = c->d_grad;
+    dl = c->d_lim;
+  }
+  double* db = (dev && b) ? b : c->d_b;
+  if (!c->d_count) CHEM_TRY(cudaMalloc(&c->d_count, sizeof(long long)), "chem buffers");
+  CHEM_TRY(cudaMemsetAsync(c->d_count, 0, sizeof(long long), c->stream), "chem count");
+  const pcfd_chem_ref r = *ref;
+  const pcfd_chem_flux_opts oo = *o;
+  if (ne > 0) {
+    k_chem_hllc2<<<CHEM_GRID(ne)>>>(ne, c->dev, c->dder, r, oo, chi, dq, dg, dl, c->d_xyz, c->d_en, c->d_ea, c->d_ef,
+                                    c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_hllc2 launch");
+  }
+  if (nb > 0) {
+    k_chem_bflux<<<CHEM_GRID(nb)>>>(nb, c->dev, c->dder, r, oo, dq, c->d_bn, c->d_ba, c->d_bf, c->d_count);
+    CHEM_TRY(cudaGetLastError(), "k_chem_bflux launch");
+  }
+  k_chem_gather<<<kChemNormBlocks, 256, 0, c->stream>>>(nn, c->dev, r, ref_time, reactions, dq, c->d_nptr, c->d_nedg,
+                                                        c->d_ef, c->d_bptr, c->d_bhe, c->d_bf, c->d_vol, db,
+                                                        c->d_part);
+  CHEM_TRY(cudaGetLastError(), "k_chem_gather launch");
+  k_chem_norms<<<1, 32 * neqn, 0, c->stream>>>(kChemNormBlocks, nn, neqn, c->d_part, c->d_norms);
+  CHEM_TRY(cudaGetLastError(), "k_chem_norms launch");
+  if (b && !dev)
+    CHEM_TRY(cudaMemcpyAsync(b, db, (size_t)nn * neqn * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  if (norms)
+    CHEM_TRY(cudaMemcpyAsync(norms, c->d_norms, (size_t)(1 + neqn) * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream),
+             "chem copy out");
+  long long bad = 0;
+  CHEM_TRY(cudaMemcpyAsync(&bad, c->d_count, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "chem count");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem residual");
+  if (bad) {
+    pcfd_set_last_error("pcfd_chem_residual_ho: " + std::to_string(bad) + " face(s) with no HLLC branch");
     return PCFD_ERR_NUMERIC;
   }
   return PCFD_OK;

@@ -72,6 +72,9 @@ def lib():
                                                        _DP, _DP, _DP, _DP]),
             "oracle_chem_gradient": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.MeshView), _DP, _IP, C.c_int,
                                                _DP]),
+            "oracle_chem_residual_ho": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
+                                               C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), _DP, _DP, _DP,
+                                               C.c_double, C.c_double, C.c_int, _DP, _DP]),
             "oracle_chem_update_bcs": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.MeshView),
                                                  C.c_int, _IP, _DP, _DP, C.c_int, _DP]),
             "oracle_chem_viscous_residual": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
@@ -545,6 +548,18 @@ class OracleChemState:
         bad = self.L.oracle_chem_viscous_residual(C.byref(self.m), C.byref(self.ref), C.byref(opts), C.byref(mesh.view),
                                                   float(Re), int(directional), dp(q), dp(grad), dp(b))
         return b, bad
+
+    def residual_ho(self, opts, mesh, q, grad, lim, chi, ref_time, reactions):
+        """SpatialResidual of the reacting set at second order (inviscid)."""
+        q = np.ascontiguousarray(q, np.float64)
+        grad = np.ascontiguousarray(grad, np.float64)
+        lim = np.ascontiguousarray(lim, np.float64)
+        b = np.empty((mesh.nnode, self.ns + 4))
+        norms = np.empty(1 + self.ns + 4)
+        self.L.oracle_chem_residual_ho(C.byref(self.m), C.byref(self.ref), C.byref(opts), C.byref(mesh.view), dp(q),
+                                       dp(grad), dp(lim), float(chi), float(ref_time), int(reactions), dp(b),
+                                       dp(norms))
+        return b, norms
 
     def residual(self, opts, mesh, q, ref_time, reactions):
         """SpatialResidual of the reacting set (first order, inviscid)."""

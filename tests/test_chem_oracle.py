@@ -414,3 +414,31 @@ def test_boundary_conditions():
     # far field is not restated: reported, records left as they were
     _, rc = O.update_bcs(m, q, {**types, 2: N.BC_FARFIELD}, twall={3: 2000.0}, qref={1: qin})
     assert rc > 0 and tag[rc - 1] == 2
+
+
+def test_second_order_residual_reduces_to_first_order():
+    """The oracle's second-order reacting residual equals the first-order one
+    when the corrections vanish (zero gradient and chi = 0, or a zero
+    limiter), and differs when they do not."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    from proteuscfd_gb300.chem import ChemModel
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(6, 5, 4, jitter=0.2, seed=8)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=8)
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(spec), ref)
+    opts = ChemModel.flux_opts(1.0, 0.4, 0)
+    b1, n1 = O.residual(opts, m, q, 2.5e-4, 1)
+    zero_g = np.zeros((m.nnode, 2 * ns + 4, 3))
+    ones = np.ones((m.nnode, ns + 4))
+    b2, _ = O.residual_ho(opts, m, q, zero_g, ones, 0.0, 2.5e-4, 1)
+    assert np.array_equal(b1, b2)
+    g = np.random.default_rng(1).normal(size=zero_g.shape) * 1e-3
+    b3, _ = O.residual_ho(opts, m, q, g, np.zeros_like(ones), 0.0, 2.5e-4, 1)
+    assert np.array_equal(b1, b3)
+    b4, _ = O.residual_ho(opts, m, q, g, ones, 0.0, 2.5e-4, 1)
+    assert not np.array_equal(b1, b4)
