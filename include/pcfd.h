@@ -519,6 +519,14 @@ PCFD_API int pcfd_chem_residual(pcfd_chem_t c, const pcfd_chem_ref* ref, const p
 PCFD_API int pcfd_chem_residual_ho(pcfd_chem_t c, const pcfd_chem_ref* ref, const pcfd_chem_flux_opts* o, double chi,
                                    double ref_time, int reactions, const double* q, const double* grad,
                                    const double* lim, double* b, double* norms, int dev);
+/* Limiter<T>::Compute with the modified Venkatakrishnan kernel (limiter 3,
+ * ucs/limiters.tcc:53,534; K = 1 as the reference hard-codes it) on the
+ * reacting set's native variables rhoi, u, v, w, T over the attached mesh
+ * (with coordinates): neighbour bounds from 0, each incident edge's
+ * unlimited extrapolation, the minimum, negatives clamped to 0.  The
+ * pressure clip (Kernel_PressureClip, :737) is not applied.  q, grad as for
+ * pcfd_chem_residual_ho -> lim [nnode][ns + 4].  dev as above. */
+PCFD_API int pcfd_chem_limiter(pcfd_chem_t c, double chi, const double* q, const double* grad, double* lim, int dev);
 /* UpdateBCs (ucs/bc.tcc:1400) of the reacting set on the attached mesh (which
  * must carry face tags), in place on q (as for pcfd_chem_residual): each
  * half-edge in order through CalculateBoundaryVariables (:1059), then

@@ -13,6 +13,7 @@
  * (ucs/reaction.tcc:665).
  */
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "oracle.h"
@@ -930,3 +931,66 @@ int oracle_chem_update_bcs(const pcfd_chem_model* m, const pcfd_chem_ref* ref, c
 
 /* ComputeAuxiliaryVariables of one record in place */
 static void fr_aux_rec(const pcfd_chem_model* m, const pcfd_chem_ref* ref, double* Q) { fr_aux(m, ref, Q); }
+
+/* Limiter<T>::Compute (ucs/limiters.tcc:53) with the modified
+ * Venkatakrishnan kernel (limiter = 3, Kernel_VenkatMod, :534, K = 1 as
+ * hard-coded there) on the reacting set's native variables (rhoi, u, v, w,
+ * T): neighbour bounds from 0 (Kernel_FindMinMax, :135), each edge end's
+ * unlimited extrapolation (ExtrapolateVariables, ucs/compressibleFR.tcc:734),
+ * the running minimum, negatives clamped to 0 (:118-124).  The pressure clip
+ * (Kernel_PressureClip, :737) is not restated.  lim [nnode][ns + 4]. */
+void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const double* grad,
+                         double chi, double* lim) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const int nn = mv->nnode;
+  double* qmin = (double*)calloc((size_t)nn * neqn, sizeof(double));
+  double* qmax = (double*)calloc((size_t)nn * neqn, sizeof(double));
+  for (size_t i = 0; i < (size_t)nn * neqn; i++) lim[i] = 1.0;
+  for (int e = 0; e < mv->nedge; e++) {
+    const int l = mv->edges[2 * e], r = mv->edges[2 * e + 1];
+    for (int j = 0; j < neqn; j++) {
+      const double vl = q[(size_t)l * nv + j], vr = q[(size_t)r * nv + j];
+      double* xl = &qmax[(size_t)l * neqn + j];
+      double* nl = &qmin[(size_t)l * neqn + j];
+      double* xr = &qmax[(size_t)r * neqn + j];
+      double* nr = &qmin[(size_t)r * neqn + j];
+      *xl = *xl > vr ? *xl : vr;
+      *nl = *nl < vr ? *nl : vr;
+      *xr = *xr > vl ? *xr : vl;
+      *nr = *nr < vl ? *nr : vl;
+    }
+  }
+  const double Pi = 3.141592653589793, K3 = 1.0;
+  for (int e = 0; e < mv->nedge; e++) {
+    const int l = mv->edges[2 * e], r = mv->edges[2 * e + 1];
+    const double* qL = &q[(size_t)l * nv];
+    const double* qR = &q[(size_t)r * nv];
+    double dx[3];
+    for (int i = 0; i < 3; i++) dx[i] = 0.5 * (mv->xyz[3 * (size_t)r + i] - mv->xyz[3 * (size_t)l + i]);
+    for (int side = 0; side < 2; side++) {
+      const int a = side ? r : l;
+      const double* qa = side ? qR : qL;
+      const double* qb = side ? qL : qR;
+      const double s = side ? -1.0 : 1.0;
+      const double* g = &grad[(size_t)a * nt * 3];
+      const double ep2 = (6.0 * Pi * mv->vol[a]) * K3;
+      double DP = 0.0;
+      for (int j = 0; j < neqn; j++) {
+        const double dQ = qb[j] - qa[j];
+        const double corr = 0.5 * chi * dQ + (1.0 - chi) * (g[3 * j] * (s * dx[0]) + g[3 * j + 1] * (s * dx[1]) +
+                                                             g[3 * j + 2] * (s * dx[2]));
+        const double Q = qa[j] + corr * 1.0;
+        const double DM = Q - qa[j];
+        if (Q > qa[j]) DP = qmax[(size_t)a * neqn + j] - qa[j];
+        else if (Q < qa[j]) DP = qmin[(size_t)a * neqn + j] - qa[j];
+        const double temp = (DP * DP + ep2 + 2.0 * DM * DP) / (DP * DP + 2.0 * DM * DM + DM * DP + ep2);
+        double* lj = &lim[(size_t)a * neqn + j];
+        if (temp < *lj) *lj = temp;
+      }
+    }
+  }
+  for (size_t i = 0; i < (size_t)nn * neqn; i++)
+    if (lim[i] < 0.0) lim[i] = 0.0;
+  free(qmin);
+  free(qmax);
+}

@@ -187,6 +187,7 @@ PROTOTYPES = {
     "pcfd_chem_transport": (C.c_int, [_P, C.POINTER(ChemRef), C.c_longlong, _DP, _DP, _DP, _DP, C.c_int]),
     "pcfd_chem_residual_ho": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_double, C.c_double,
                                         C.c_int, _P, _P, _P, _P, _DP, C.c_int]),
+    "pcfd_chem_limiter": (C.c_int, [_P, C.c_double, _P, _P, _P, C.c_int]),
     "pcfd_chem_update_bcs": (C.c_int, [_P, C.POINTER(ChemRef), C.c_int, _IP, _DP, _DP, C.c_int, _P, C.c_int]),
     "pcfd_chem_gradient": (C.c_int, [_P, _P, _IP, C.c_int, _P, C.c_int]),
     "pcfd_chem_viscous_residual": (C.c_int, [_P, C.POINTER(ChemRef), C.POINTER(ChemFluxOpts), C.c_double, C.c_int,

@@ -298,6 +298,17 @@ class ChemModel:
                 "pcfd_chem_viscous_residual")
         return b
 
+    def limiter(self, chi, q, grad):
+        """The modified Venkatakrishnan limiter of the native variables (no
+        pressure clip): -> lim [nnode][ns + 4]."""
+        m = self._mesh
+        q = self._arr(q, (m.nnode + m.nbedge, 6 + 3 * self.nspecies))
+        grad = self._arr(grad, (m.nnode, 2 * self.nspecies + 4, 3))
+        lim = np.empty((m.nnode, self.nspecies + 4))
+        N.check(self._lib.pcfd_chem_limiter(self._h, float(chi), q.ctypes.data, grad.ctypes.data, lim.ctypes.data, 0),
+                "pcfd_chem_limiter")
+        return lim
+
     def residual_ho(self, ref, opts, chi, ref_time, reactions, q, grad, lim):
         """The reacting residual at second order: q records, grad [nnode][2 ns + 4][3],
         lim [nnode][ns + 4] -> (b [nnode][ns + 4], norms [1 + ns + 4])."""

@@ -1023,6 +1023,61 @@ __global__ void __launch_bounds__(128) k_chem_bcs(long long nnode, const pcfd_ch
   }
 }
 
+// Limiter<T>::Compute with Kernel_VenkatMod (ucs/limiters.tcc:53,534; K = 1
+// as hard-coded there) on the reacting set's native variables, one node per
+// thread: neighbour bounds from 0 (Kernel_FindMinMax, :135), each incident
+// edge's unlimited extrapolation (ExtrapolateVariables,
+// ucs/compressibleFR.tcc:734, dx = (x_j - x_i)/2), the running minimum,
+// negatives clamped to 0.  The pressure clip is not applied.
+__global__ void __launch_bounds__(128) k_chem_limiter(long long nnode, const pcfd_chem_model* __restrict__ gm,
+                                                      double chi, const double* __restrict__ q,
+                                                      const double* __restrict__ grad, const double* __restrict__ xyz,
+                                                      const double* __restrict__ vol, const int2* __restrict__ en,
+                                                      const int* __restrict__ nptr, const int* __restrict__ nedg,
+                                                      double* __restrict__ lim) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nnode) return;
+  const int ns = gm->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  const double* qi = &q[(size_t)i * nv];
+  double mn[PCFD_CHEM_MAX_SPECIES + 4], mx[PCFD_CHEM_MAX_SPECIES + 4], l[PCFD_CHEM_MAX_SPECIES + 4];
+  for (int j = 0; j < neqn; j++) {
+    mn[j] = mx[j] = 0.0;
+    l[j] = 1.0;
+  }
+  auto nbr = [&](int k) {
+    const int se = nedg[k];
+    const int2 n = en[se < 0 ? ~se : se];
+    return se < 0 ? n.y : n.x;
+  };
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    const double* qj = &q[(size_t)nbr(k) * nv];
+    for (int j = 0; j < neqn; j++) {
+      mx[j] = mx[j] > qj[j] ? mx[j] : qj[j];
+      mn[j] = mn[j] < qj[j] ? mn[j] : qj[j];
+    }
+  }
+  const double ep2 = (6.0 * 3.141592653589793 * vol[i]) * 1.0;
+  const double* g = &grad[(size_t)i * nt * 3];
+  for (int k = nptr[i]; k < nptr[i + 1]; k++) {
+    const int j0 = nbr(k);
+    const double* qj = &q[(size_t)j0 * nv];
+    double dx[3];
+    for (int c = 0; c < 3; c++) dx[c] = 0.5 * (xyz[3 * (size_t)j0 + c] - xyz[3 * (size_t)i + c]);
+    double DP = 0.0;
+    for (int j = 0; j < neqn; j++) {
+      const double dQ = qj[j] - qi[j];
+      const double corr = 0.5 * chi * dQ + (1.0 - chi) * (g[3 * j] * dx[0] + g[3 * j + 1] * dx[1] + g[3 * j + 2] * dx[2]);
+      const double Q = qi[j] + corr * 1.0;
+      const double DM = Q - qi[j];
+      if (Q > qi[j]) DP = mx[j] - qi[j];
+      else if (Q < qi[j]) DP = mn[j] - qi[j];
+      const double t = (DP * DP + ep2 + 2.0 * DM * DP) / (DP * DP + 2.0 * DM * DM + DM * DP + ep2);
+      if (t < l[j]) l[j] = t;
+    }
+  }
+  for (int j = 0; j < neqn; j++) lim[(size_t)i * neqn + j] = l[j] < 0.0 ? 0.0 : l[j];
+}
+
 // CompressibleFREqnSet::ViscousFlux (ucs/compressibleFR.tcc:551) on the face
 // state Q (native record) and face gradient g of the reacting gradient list
 // (rhoi, u, v, w, T, concentrations): laminar, no species diffusion
@@ -1751,6 +1806,43 @@ PCFD_API int pcfd_chem_update_bcs(pcfd_chem_t h, const pcfd_chem_ref* ref, int n
                         "characteristic wall, adiabatic no-slip)");
     return PCFD_ERR_ARG;
   }
+  return PCFD_OK;
+}
+
+PCFD_API int pcfd_chem_limiter(pcfd_chem_t h, double chi, const double* q, const double* grad, double* lim, int dev) {
+  ChemHandle* c = (ChemHandle*)h;
+  if (!c || !q || !grad || !lim) {
+    pcfd_set_last_error("pcfd_chem_limiter: bad arguments");
+    return PCFD_ERR_ARG;
+  }
+  if (c->nnode <= 0 || !c->d_xyz) {
+    pcfd_set_last_error("pcfd_chem_limiter: no mesh with coordinates attached");
+    return PCFD_ERR_STATE;
+  }
+  const int ns = c->host.nspecies, neqn = ns + 4, nt = 2 * ns + 4;
+  const size_t nv = 6 + 3 * (size_t)ns;
+  const long long nn = c->nnode, nb = c->nbedge;
+  const double* dq = q;
+  const double* dg = grad;
+  double* dl = lim;
+  if (!dev) {
+    if (!c->d_grad) CHEM_TRY(cudaMalloc(&c->d_grad, (size_t)nn * nt * 3 * sizeof(double)), "chem buffers");
+    if (!c->d_lim) CHEM_TRY(cudaMalloc(&c->d_lim, (size_t)nn * neqn * sizeof(double)), "chem buffers");
+    CHEM_TRY(cudaMemcpyAsync(c->d_q, q, (size_t)(nn + nb) * nv * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+             "chem copy");
+    CHEM_TRY(cudaMemcpyAsync(c->d_grad, grad, (size_t)nn * nt * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream),
+             "chem copy");
+    dq = c->d_q;
+    dg = c->d_grad;
+    dl = c->d_lim;
+  }
+  k_chem_limiter<<<CHEM_GRID(nn)>>>(nn, c->dev, chi, dq, dg, c->d_xyz, c->d_vol, c->d_en, c->d_nptr, c->d_nedg, dl);
+  CHEM_TRY(cudaGetLastError(), "k_chem_limiter launch");
+  if (!dev)
+    CHEM_TRY(cudaMemcpyAsync(lim, dl, (size_t)nn * neqn * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+             "chem copy out");
+  CHEM_TRY(cudaStreamSynchronize(c->stream), "chem limiter");
   return PCFD_OK;
 }
 

@@ -72,6 +72,8 @@ def lib():
                                                        _DP, _DP, _DP, _DP]),
             "oracle_chem_gradient": (C.c_int, [C.POINTER(N.ChemModelC), C.POINTER(N.MeshView), _DP, _IP, C.c_int,
                                                _DP]),
+            "oracle_chem_limiter": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.MeshView), _DP, _DP, C.c_double,
+                                           _DP]),
             "oracle_chem_residual_ho": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
                                                C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), _DP, _DP, _DP,
                                                C.c_double, C.c_double, C.c_int, _DP, _DP]),
@@ -548,6 +550,13 @@ class OracleChemState:
         bad = self.L.oracle_chem_viscous_residual(C.byref(self.m), C.byref(self.ref), C.byref(opts), C.byref(mesh.view),
                                                   float(Re), int(directional), dp(q), dp(grad), dp(b))
         return b, bad
+
+    def limiter(self, mesh, q, grad, chi):
+        q = np.ascontiguousarray(q, np.float64)
+        grad = np.ascontiguousarray(grad, np.float64)
+        lim = np.empty((mesh.nnode, self.ns + 4))
+        self.L.oracle_chem_limiter(C.byref(self.m), C.byref(mesh.view), dp(q), dp(grad), float(chi), dp(lim))
+        return lim
 
     def residual_ho(self, opts, mesh, q, grad, lim, chi, ref_time, reactions):
         """SpatialResidual of the reacting set at second order (inviscid)."""

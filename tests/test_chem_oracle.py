@@ -442,3 +442,26 @@ def test_second_order_residual_reduces_to_first_order():
     assert np.array_equal(b1, b3)
     b4, _ = O.residual_ho(opts, m, q, g, ones, 0.0, 2.5e-4, 1)
     assert not np.array_equal(b1, b4)
+
+
+def test_limiter_properties():
+    """The oracle's reacting limiter: values in [0, 1], exactly 1 for a
+    uniform field (no extrapolated change), and below 1 where the
+    extrapolation overshoots the neighbour bounds."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    ns = len(spec["species"])
+    m = Mesh.box(7, 6, 5, jitter=0.2, seed=9)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=9)
+    q = fr_records(ref, rhoi, vel, T)
+    O = OracleChemState(model_struct(spec), ref)
+    g = O.gradient(m, q)
+    lim = O.limiter(m, q, g, 0.0)
+    assert lim.min() >= 0.0 and lim.max() <= 1.0 and lim.min() < 1.0
+    qu = q.copy()
+    qu[:] = q[0]
+    lu = O.limiter(m, qu, np.zeros_like(g), 0.0)
+    assert np.all(lu == 1.0)

@@ -457,3 +457,25 @@ def test_fr_second_order_residual_parity():
         assert (np.abs(b - bo) / scale).max() < 1e-11, (np.abs(b - bo) / scale).max()
         assert np.allclose(norms, no, rtol=1e-11, atol=0)
     C.close()
+
+
+def test_fr_limiter_parity():
+    """The reacting modified Venkatakrishnan limiter on the GPU against the
+    oracle's edge-by-edge minimum, on seeded records with their gradient."""
+    from chem_cases import fr_records, fr_states
+    from oracle_lib import OracleChemState
+    from proteuscfd_gb300 import Mesh
+    spec = mechanism()
+    m = Mesh.box(12, 9, 8, jitter=0.2, seed=10)
+    nrows = m.nnode + m.nbedge
+    ref, rhoi, vel, T = fr_states(nrows, seed=27)
+    q = fr_records(ref, rhoi, vel, T)
+    C = ChemModel(spec)
+    C.attach_mesh(m)
+    O = OracleChemState(model_struct(spec), ref)
+    g = C.gradient(q)
+    for chi in (0.0, 0.5):
+        lim = C.limiter(chi, q, g)
+        lo = O.limiter(m, q, g, chi)
+        assert np.abs(lim - lo).max() < 1e-12, np.abs(lim - lo).max()
+    C.close()
