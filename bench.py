@@ -347,6 +347,7 @@ def converge_study(args):
     q_pre, lim_pre = S.get_state(), S.get_limiter()
     S.close()
     out["startup"] = {"steps": P, "wall_s": round(t_pre, 3), "drop": hist[-1] / r0, "opts": CONV_PREFIX}
+    print(json.dumps({"startup": out["startup"], "nodes": m.nnode}), file=sys.stderr, flush=True)
     finals = {}
     for name in args.converge_arms:
         arm = CONV_ARMS[name]
@@ -374,6 +375,10 @@ def converge_study(args):
             for d in (1e-4, 1e-6, 1e-8, 1e-10):
                 if d not in t_at and r <= d:
                     t_at[d] = [P + len(h), round(t_pre + el, 3)]
+            if len(h) % 25 == 0:
+                # progress on stderr, so a run cut short still leaves its history
+                print(json.dumps({"arm": name, "step": P + len(h), "drop": r, "wall_s": round(el, 2),
+                                  "lin": rep["lin_iters"]}), file=sys.stderr, flush=True)
             if not np.isfinite(r) or r <= 1e-10 or el > args.converge_cap or len(h) >= args.converge_iters:
                 break
         wall = time.perf_counter() - t0
@@ -398,6 +403,7 @@ def converge_study(args):
         if not np.isfinite(h[-1]):
             rec["stopped"] = "non-finite residual"
         out["arms"][name] = rec
+        print(json.dumps({"arm_done": name, "rec": rec}), file=sys.stderr, flush=True)
         S.close()
     ref = "fp64" if "fp64" in finals else None
     if ref:
@@ -705,8 +711,9 @@ def run_gb300(args, ws, rank, local, pg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+Venkat "
-                               "limiter K=5+Roe+viscous), Mach 0.8, Re 1e5" % (w["nx"], w["ny"], w["nz"]),
+        "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+modified "
+                               "Venkatakrishnan limiter K=%g+Roe+viscous), Mach 0.8, Re 1e5"
+                               % (w["nx"], w["ny"], w["nz"], case.param.venkat_K),
                    "nodes": m.nnode, "edges": m.nedge, "half_edges": m.nbedge,
                    "l2": "inputs larger than L2 (edge arrays alone %.0f MB)" % (m.nedge * 104 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "mesh_build_s": round(t_mesh, 2),
