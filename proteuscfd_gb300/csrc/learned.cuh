@@ -204,13 +204,71 @@ __global__ void k_lp_encode(int n, const float* __restrict__ x, const float* __r
       __floats2bfloat162_rn(fmaxf(a0, 0.f), fmaxf(a1, 0.f));
 }
 
+// Packed FP32 fused multiply-add of two lanes (PTX fma.rn.f32x2): each half
+// is rounded as fmaf rounds it.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)),
+        "l"(*reinterpret_cast<const uint64_t*>(&c)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+
+// m for one block of up to 32 neighbours of a row: lane k holds the k-th
+// neighbour's index jl and edge features el; cnt of them are valid.  The row
+// loads of 16 neighbours are issued together, then summed in neighbour order
+// (the order of the sequential sum).  The channel pair's gate and sum use
+// packed FMAs: the same operations and roundings as gate_eval(g, e, 1) and
+// two fmaf, in half the instructions.  The per-neighbour branch stays: the
+// branch-free form (zero rows in the padded slots) measured twice as slow,
+// with the row loads no longer in flight together.
+__device__ __forceinline__ void lp_gather_block(const Gate2& g, const __nv_bfloat16* __restrict__ h_in, int c,
+                                                int jl, float4 el, int cnt, float& a0, float& a1) {
+  const float2 w0 = make_float2(g.w0[0], g.w1[0]), w1 = make_float2(g.w0[1], g.w1[1]);
+  const float2 w2 = make_float2(g.w0[2], g.w1[2]), w3 = make_float2(g.w0[3], g.w1[3]);
+  const float2 c0 = make_float2(g.c0, g.c1);
+  float2 acc = make_float2(a0, a1);
+  for (int t = 0; t < cnt; t += 16) {
+    uint32_t raw[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      const int j = __shfl_sync(0xffffffffu, jl, t + u);
+      raw[u] = 0u;
+      if (t + u < cnt) raw[u] = *reinterpret_cast<const uint32_t*>(&h_in[(size_t)j * LP_H + c]);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      float4 e;
+      e.x = __shfl_sync(0xffffffffu, el.x, t + u);
+      e.y = __shfl_sync(0xffffffffu, el.y, t + u);
+      e.z = __shfl_sync(0xffffffffu, el.z, t + u);
+      e.w = __shfl_sync(0xffffffffu, el.w, t + u);
+      if (t + u < cnt) {
+        const float2 hh = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw[u]));
+        float2 gv = fma2(w0, make_float2(e.x, e.x), c0);
+        gv = fma2(w1, make_float2(e.y, e.y), gv);
+        gv = fma2(w2, make_float2(e.z, e.z), gv);
+        gv = fma2(w3, make_float2(e.w, e.w), gv);
+        acc = fma2(gv, hh, acc);
+      }
+    }
+  }
+  a0 = acc.x;
+  a1 = acc.y;
+}
+
 // One message-passing layer for 128 nodes.  Gather phase: warp w builds rows
-// 16w..16w+15 of A = [h | m]; lane l owns channels 2l, 2l+1.  Then one
-// 128x64x128 MMA, and the epilogue (warps 0-3, one row per thread) adds the
-// bias, applies ReLU and stores h' in BF16; the last layer also applies the
-// decoder and writes either out (FP32) or z = y + sigma * out (FP64).
+// 16w..16w+15 of A = [h | m]; lane l owns channels 2l, 2l+1.  The warp's row
+// pointers arrive in one load; a row's neighbour indices and edge features
+// arrive in one coalesced load, issued while the previous row's neighbour rows
+// are gathered; 16 neighbour rows are in flight at once.  Then one 128x64x128
+// MMA, and the epilogue (warps 0-3, one row per thread, TMEM read 16 columns at
+// a time) adds the bias, applies ReLU and stores h' in BF16; the last layer
+// also applies the decoder and writes either out (FP32) or z = y + sigma * out
+// (FP64).  80 registers: three CTAs per multiprocessor.
 template <bool LAST>
-__global__ void __launch_bounds__(LP_THREADS) k_lp_layer(
+__global__ void __launch_bounds__(LP_THREADS, 3) k_lp_layer(
     int n, const int* __restrict__ nptr, const int* __restrict__ nnbr, const float4* __restrict__ ef,
     const float* __restrict__ invdeg, const __nv_bfloat16* __restrict__ h_in, const float* __restrict__ wl,
     const __nv_bfloat16* __restrict__ img, __nv_bfloat16* __restrict__ h_out, __nv_bfloat16* __restrict__ m_out,
@@ -219,42 +277,51 @@ __global__ void __launch_bounds__(LP_THREADS) k_lp_layer(
   extern __shared__ unsigned char lp_raw[];
   const LpSmem sm = lp_smem(lp_raw);
   constexpr int K = 2 * LP_H;
+  constexpr int RPW = LP_TILE / 8;  // rows per warp
   lp_begin(sm, img, LP_H);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = 2 * lane;
   const int base = blockIdx.x * LP_TILE;
+  const int r0 = warp * RPW;
   {
     const Gate2 g = load_gate(wl, c);
-    for (int rr = 0; rr < LP_TILE / 8; rr++) {
-      const int r = warp * (LP_TILE / 8) + rr;
+    // lane k <= RPW holds nptr of row r0 + k (nptr has n + 1 entries)
+    int pl = 0;
+    if (lane <= RPW && base + r0 + lane <= n) pl = nptr[base + r0 + lane];
+    // the first 32 neighbours of row rr: index and edge features
+    auto fetch = [&](int rr, int& jl, float4& el) {
+      const int p0 = __shfl_sync(0xffffffffu, pl, rr), p1 = __shfl_sync(0xffffffffu, pl, rr + 1);
+      jl = 0;
+      el = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (base + r0 + rr < n && lane < p1 - p0) {
+        jl = nnbr[p0 + lane];
+        el = ef[p0 + lane];
+      }
+    };
+    int jl;
+    float4 el;
+    fetch(0, jl, el);
+    for (int rr = 0; rr < RPW; rr++) {
+      int jn = 0;
+      float4 en = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (rr + 1 < RPW) fetch(rr + 1, jn, en);
+      const int r = r0 + rr;
       const int i = base + r;
       __nv_bfloat162 hv = __floats2bfloat162_rn(0.f, 0.f), mv = hv;
       if (i < n) {
+        const int p0 = __shfl_sync(0xffffffffu, pl, rr), p1 = __shfl_sync(0xffffffffu, pl, rr + 1);
         hv = *reinterpret_cast<const __nv_bfloat162*>(&h_in[(size_t)i * LP_H + c]);
         float a0 = 0.f, a1 = 0.f;
-        const int p0 = nptr[i], p1 = nptr[i + 1];
-        int p = p0;
-        for (; p + 1 < p1; p += 2) {
-          const int j0 = nnbr[p], j1 = nnbr[p + 1];
-          const float4 e0 = ef[p], e1 = ef[p + 1];
-          const float2 h0 =
-              __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&h_in[(size_t)j0 * LP_H + c]));
-          const float2 h1 =
-              __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&h_in[(size_t)j1 * LP_H + c]));
-          const float2 g0 = gate_eval(g, e0, 1.f), g1 = gate_eval(g, e1, 1.f);
-          a0 = fmaf(g0.x, h0.x, a0);
-          a1 = fmaf(g0.y, h0.y, a1);
-          a0 = fmaf(g1.x, h1.x, a0);
-          a1 = fmaf(g1.y, h1.y, a1);
-        }
-        if (p < p1) {
-          const int j0 = nnbr[p];
-          const float4 e0 = ef[p];
-          const float2 h0 =
-              __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&h_in[(size_t)j0 * LP_H + c]));
-          const float2 g0 = gate_eval(g, e0, 1.f);
-          a0 = fmaf(g0.x, h0.x, a0);
-          a1 = fmaf(g0.y, h0.y, a1);
+        lp_gather_block(g, h_in, c, jl, el, min(p1 - p0, 32), a0, a1);
+        // rows with more than 32 neighbours
+        for (int pb = p0 + 32; pb < p1; pb += 32) {
+          int jx = 0;
+          float4 ex = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (lane < p1 - pb) {
+            jx = nnbr[pb + lane];
+            ex = ef[pb + lane];
+          }
+          lp_gather_block(g, h_in, c, jx, ex, min(p1 - pb, 32), a0, a1);
         }
         const float id = invdeg[i];
         mv = __floats2bfloat162_rn(a0 * id, a1 * id);
@@ -262,6 +329,8 @@ __global__ void __launch_bounds__(LP_THREADS) k_lp_layer(
       }
       st_a2(sm.a, r, c, K, hv);
       st_a2(sm.a, r, LP_H + c, K, mv);
+      jl = jn;
+      el = en;
     }
   }
   bool ok;
@@ -271,46 +340,49 @@ __global__ void __launch_bounds__(LP_THREADS) k_lp_layer(
   } else if (warp < 4) {
     const int r = warp * 32 + lane;
     const int i = base + r;
-    float v[LP_H];
+    float o[LP_NOUT];
 #pragma unroll
-    for (int cc = 0; cc < LP_H; cc += 16) umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cc, v + cc);
-    if (i < n) {
+    for (int oo = 0; oo < LP_NOUT; oo++) o[oo] = LAST ? w[LP_OFF_BOUT + oo] : 0.f;
 #pragma unroll
-      for (int k = 0; k < LP_H; k++) v[k] = bfr(fmaxf(v[k] + wl[LP_L_B + k], 0.f));
-      if (!LAST || h_out) {
-        uint4* dst = reinterpret_cast<uint4*>(&h_out[(size_t)i * LP_H]);
+    for (int cc = 0; cc < LP_H; cc += 16) {
+      float v[16];
+      umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cc, v);
+      if (i < n) {
 #pragma unroll
-        for (int q8 = 0; q8 < LP_H / 8; q8++) {
-          __nv_bfloat162 b0 = __floats2bfloat162_rn(v[8 * q8], v[8 * q8 + 1]);
-          __nv_bfloat162 b1 = __floats2bfloat162_rn(v[8 * q8 + 2], v[8 * q8 + 3]);
-          __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * q8 + 4], v[8 * q8 + 5]);
-          __nv_bfloat162 b3 = __floats2bfloat162_rn(v[8 * q8 + 6], v[8 * q8 + 7]);
-          uint4 u;
-          u.x = *reinterpret_cast<uint32_t*>(&b0);
-          u.y = *reinterpret_cast<uint32_t*>(&b1);
-          u.z = *reinterpret_cast<uint32_t*>(&b2);
-          u.w = *reinterpret_cast<uint32_t*>(&b3);
-          dst[q8] = u;
+        for (int k = 0; k < 16; k++) v[k] = bfr(fmaxf(v[k] + wl[LP_L_B + cc + k], 0.f));
+        if (!LAST || h_out) {
+          uint4* dst = reinterpret_cast<uint4*>(&h_out[(size_t)i * LP_H + cc]);
+#pragma unroll
+          for (int q8 = 0; q8 < 2; q8++) {
+            __nv_bfloat162 b0 = __floats2bfloat162_rn(v[8 * q8], v[8 * q8 + 1]);
+            __nv_bfloat162 b1 = __floats2bfloat162_rn(v[8 * q8 + 2], v[8 * q8 + 3]);
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * q8 + 4], v[8 * q8 + 5]);
+            __nv_bfloat162 b3 = __floats2bfloat162_rn(v[8 * q8 + 6], v[8 * q8 + 7]);
+            uint4 u;
+            u.x = *reinterpret_cast<uint32_t*>(&b0);
+            u.y = *reinterpret_cast<uint32_t*>(&b1);
+            u.z = *reinterpret_cast<uint32_t*>(&b2);
+            u.w = *reinterpret_cast<uint32_t*>(&b3);
+            dst[q8] = u;
+          }
+        }
+        if (LAST) {
+#pragma unroll
+          for (int oo = 0; oo < LP_NOUT; oo++)
+#pragma unroll
+            for (int k = 0; k < 16; k++) o[oo] = fmaf(bfr(w[LP_OFF_WOUT + oo * LP_H + cc + k]), v[k], o[oo]);
         }
       }
-      if (LAST) {
-        float o[LP_NOUT];
+    }
+    if (LAST && i < n) {
+      if (out) {
 #pragma unroll
-        for (int oo = 0; oo < LP_NOUT; oo++) {
-          float a = w[LP_OFF_BOUT + oo];
+        for (int oo = 0; oo < LP_NOUT; oo++) out[(size_t)i * LP_NOUT + oo] = o[oo];
+      }
+      if (z) {
+        const double sg = *sigma_dev;
 #pragma unroll
-          for (int k = 0; k < LP_H; k++) a = fmaf(bfr(w[LP_OFF_WOUT + oo * LP_H + k]), v[k], a);
-          o[oo] = a;
-        }
-        if (out) {
-#pragma unroll
-          for (int oo = 0; oo < LP_NOUT; oo++) out[(size_t)i * LP_NOUT + oo] = o[oo];
-        }
-        if (z) {
-          const double sg = *sigma_dev;
-#pragma unroll
-          for (int oo = 0; oo < LP_NOUT; oo++) z[(size_t)i * 5 + oo] = y[(size_t)i * 5 + oo] + sg * (double)o[oo];
-        }
+        for (int oo = 0; oo < LP_NOUT; oo++) z[(size_t)i * 5 + oo] = y[(size_t)i * 5 + oo] + sg * (double)o[oo];
       }
     }
   }

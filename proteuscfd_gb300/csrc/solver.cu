@@ -2775,6 +2775,11 @@ int lp_alloc(Solver* s) {
   CUDA_TRY(cudaMemsetAsync(lp->h, 0, (LP_NL + 1) * nh * sizeof(__nv_bfloat16), s->stream));
   CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
   CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
+  // three layer CTAs (3 x 51 KB) share a multiprocessor
+  CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared));
+  CUDA_TRY(cudaFuncSetAttribute(k_lp_layer<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared));
   CUDA_TRY(cudaFuncSetAttribute(k_lp_layer_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_SMEM));
   return launch(s, T_SETUP, [&] {
     k_lp_graph<<<nblk(n, 256), 256, 0, s->stream>>>(n, s->d_nptr, s->d_nedg, s->d_en, s->d_ea, s->d_xyz,
