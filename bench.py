@@ -130,6 +130,12 @@ def max_over_ranks(pg, x):
     return float(t.item())
 
 
+def replica_value(ws, units_per_rank, slowest_ms_per_step):
+    """Whole-job throughput in M units/s: every replica's units over the
+    slowest rank's step time."""
+    return ws * units_per_rank / (slowest_ms_per_step * 1e-3) / 1e6
+
+
 # The CPU baseline's bounded sample of the workload family: a box of the
 # same generator, clustering and boundary conditions, small enough that
 # every host thread evaluates its own residual within a second or so.
@@ -622,7 +628,7 @@ def run_gb300(args, ws, rank, local, pg):
     ms, norms, launches, clk = results[0]
     S.set_residual_arithmetic(0)
     ms_per_step = ms / args.steps
-    value = ws * m.nedge / (ms_per_step * 1e-3) / 1e6
+    value = replica_value(ws, m.nedge, ms_per_step)
 
     def kernel_times(arith, nprof=3):
         """per-kernel device times (events around each launch on the
