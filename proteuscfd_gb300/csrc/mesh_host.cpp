@@ -29,13 +29,16 @@
 #include "../../include/pcfd.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -140,17 +143,64 @@ const int kTetFl[12] = {0, 1, 2, 0, 3, 1, 0, 2, 3, 1, 3, 2};
 int elem_nnodes(int t) { return t == ETRI ? 3 : 4; }
 
 // Mesh::EliminateRepeats (ucs/mesh.tcc:1341): keeps the first occurrence of
-// each value, in order.  The reference compares every pair (O(k^2) per node);
-// a per-node stamp gives the same list in O(k).
-int eliminate_repeats(int* a, int n, std::vector<int>& stamp, int tag) {
+// each value, in order.  The lists are a node's element neighbours (a few
+// dozen values), so a search of the kept prefix is enough.
+int eliminate_repeats(int* a, int n) {
   int unique = 0;
   for (int i = 0; i < n; i++) {
     const int v = a[i];
-    if (stamp[v] == tag) continue;
-    stamp[v] = tag;
-    a[unique++] = v;
+    bool seen = false;
+    for (int j = 0; j < unique; j++)
+      if (a[j] == v) { seen = true; break; }
+    if (!seen) a[unique++] = v;
   }
   return unique;
+}
+
+// Splits [0, n) into contiguous chunks, one per host thread (one chunk below
+// a size where threads do not pay), and runs body(begin, end, chunk) on
+// each.  Each chunk writes only its own outputs, so results do not depend on
+// the thread count.  A chunk whose thread cannot be started runs on the
+// calling thread; an exception in any chunk is raised again here after all
+// chunks finished.  Returns the number of chunks.
+template <class F>
+int parallel_chunks(long long n, F body) {
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  if (nt > 64) nt = 64;
+  if (n < 65536 || nt == 1) {
+    body(0LL, n, 0);
+    return 1;
+  }
+  const long long chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> pool;
+  std::vector<std::exception_ptr> fail(nt);
+  auto run = [&](long long b, long long e, int c) {
+    try {
+      body(b, e, c);
+    } catch (...) {
+      fail[c] = std::current_exception();
+    }
+  };
+  int nc = 0;
+  for (unsigned t = 0; t < nt; t++) {
+    const long long b = (long long)t * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    const int c = nc++;
+    try {
+      pool.emplace_back(run, b, e, c);
+    } catch (...) {
+      run(b, e, c);
+    }
+  }
+  for (auto& th : pool) th.join();
+  for (auto& f : fail)
+    if (f) std::rethrow_exception(f);
+  return nc;
+}
+template <class F>
+void parallel_ranges(long long n, F body) {
+  parallel_chunks(n, [&](long long b, long long e, int) { body(b, e); });
 }
 
 int build_psp_only(HostMesh& m) {
@@ -174,30 +224,44 @@ int build_psp_only(HostMesh& m) {
         m.elsp[fill[node]++] = e;
       }
   }
-  // BuildPsp
+  // BuildPsp: per node, the other nodes of its elements in elsp order
+  // (kClTri / kClTet), first occurrences kept.  Nodes are independent: each
+  // chunk of nodes builds its own lists, concatenated in node order.
   m.ipsp.assign(nn + 1, 0);
-  m.psp.clear();
-  m.psp.reserve((size_t)nn * 16);
-  std::vector<int> tmp;
-  std::vector<int> stamp(nn, -1);
-  for (int i = 0; i < nn; i++) {
-    tmp.clear();
-    for (int k = m.ielsp[i]; k < m.ielsp[i + 1]; k++) {
-      int e = m.elsp[k];
-      const int* nodes = &m.enodes[4 * e];
-      int nl = elem_nnodes(m.etype[e]);
-      int lnode = -1;
-      for (int q = 0; q < nl; q++)
-        if (nodes[q] == i) { lnode = q; break; }
-      if (m.etype[e] == ETRI) {
-        for (int q = 0; q < 2; q++) tmp.push_back(nodes[kClTri[2 * lnode + q]]);
-      } else {
-        for (int q = 0; q < 3; q++) tmp.push_back(nodes[kClTet[3 * lnode + q]]);
+  std::vector<std::vector<int>> part(64);
+  parallel_chunks(nn, [&](long long b, long long e, int c) {
+    std::vector<int>& out = part[c];
+    out.reserve((size_t)(e - b) * 16);
+    std::vector<int> tmp;
+    for (long long i = b; i < e; i++) {
+      tmp.clear();
+      for (int k = m.ielsp[i]; k < m.ielsp[i + 1]; k++) {
+        const int el = m.elsp[k];
+        const int* nodes = &m.enodes[4 * (size_t)el];
+        const int nl = elem_nnodes(m.etype[el]);
+        int lnode = -1;
+        for (int q = 0; q < nl; q++)
+          if (nodes[q] == i) { lnode = q; break; }
+        if (m.etype[el] == ETRI) {
+          for (int q = 0; q < 2; q++) tmp.push_back(nodes[kClTri[2 * lnode + q]]);
+        } else {
+          for (int q = 0; q < 3; q++) tmp.push_back(nodes[kClTet[3 * lnode + q]]);
+        }
       }
+      const int u = eliminate_repeats(tmp.data(), (int)tmp.size());
+      out.insert(out.end(), tmp.begin(), tmp.begin() + u);
+      m.ipsp[i + 1] = u;
     }
-    int u = eliminate_repeats(tmp.data(), (int)tmp.size(), stamp, i);
-    m.psp.insert(m.psp.end(), tmp.begin(), tmp.begin() + u);
-    m.ipsp[i + 1] = (int)m.psp.size();
+  });
+  for (int i = 0; i < nn; i++) m.ipsp[i + 1] += m.ipsp[i];
+  m.psp.resize((size_t)m.ipsp[nn]);
+  {
+    size_t off = 0;
+    for (auto& pv : part) {
+      std::copy(pv.begin(), pv.end(), m.psp.begin() + off);
+      off += pv.size();
+      std::vector<int>().swap(pv);
+    }
   }
   return 0;
 }
@@ -264,18 +328,84 @@ int build_maps(HostMesh& m) {
   return 0;
 }
 
+// The median-dual pieces of edge (n1, n2) inside element e, as
+// CalcAreasVolumes forms them (ucs/mesh.tcc:1822-1985): the edge midpoint,
+// the centroids of the two faces that share the edge, the element centroid,
+// and the orientation of the edge in the element's edge table.  False when e
+// is not a tet holding both nodes.
+struct EdgeTetGeom {
+  double o, edgept[3], f1[3], f2[3], ept[3];
+};
+inline bool edge_tet_geom(const HostMesh& m, int n1, int n2, int e, EdgeTetGeom& g) {
+  if (m.etype[e] != ETET) return false;
+  const int* nodes = &m.enodes[4 * (size_t)e];
+  int l1 = -1, l2 = -1;
+  for (int q = 0; q < 4; q++) {
+    if (nodes[q] == n1) l1 = q;
+    else if (nodes[q] == n2) l2 = q;
+  }
+  if (l1 < 0 || l2 < 0) return false;  // edge not in this element
+  int orientation = 0, eid = -1;
+  for (int j = 0; j < 6; j++) {
+    if (kTetEorder[2 * j] == l1 && kTetEorder[2 * j + 1] == l2) { eid = j; orientation = 1; break; }
+    if (kTetEorder[2 * j + 1] == l1 && kTetEorder[2 * j] == l2) { eid = j; orientation = -1; break; }
+  }
+  const double* X = m.xyz.data();
+  const int face1 = kTetE2f[2 * eid], face2 = kTetE2f[2 * eid + 1];
+  mid2(&X[3 * (size_t)n1], &X[3 * (size_t)n2], g.edgept);
+  const int* fa = &kTetFl[3 * face1];
+  cen3(&X[3 * (size_t)nodes[fa[0]]], &X[3 * (size_t)nodes[fa[1]]], &X[3 * (size_t)nodes[fa[2]]], g.f1);
+  const int* fb = &kTetFl[3 * face2];
+  cen3(&X[3 * (size_t)nodes[fb[0]]], &X[3 * (size_t)nodes[fb[1]]], &X[3 * (size_t)nodes[fb[2]]], g.f2);
+  cen4(&X[3 * (size_t)nodes[0]], &X[3 * (size_t)nodes[1]], &X[3 * (size_t)nodes[2]], &X[3 * (size_t)nodes[3]],
+       g.ept);
+  g.o = (double)orientation;
+  return true;
+}
+
+// Calls fn(g) for each tet holding edge (n1, n2), in the order the
+// reference visits them: the second node's elements in elsp order.  Every
+// node's elsp list is in ascending element order (BuildElsp fills them
+// element by element), so the tets holding both nodes are the merge
+// intersection of the two lists, in that same order; only those tets' node
+// lists are read.
+template <class F>
+inline void for_edge_tets(const HostMesh& m, int n1, int n2, EdgeTetGeom& g, F fn) {
+  int a = m.ielsp[n1], ae = m.ielsp[n1 + 1];
+  int b = m.ielsp[n2], be = m.ielsp[n2 + 1];
+  while (a < ae && b < be) {
+    const int ea = m.elsp[a], eb = m.elsp[b];
+    if (ea < eb) {
+      a++;
+    } else if (eb < ea) {
+      b++;
+    } else {
+      if (edge_tet_geom(m, n1, n2, eb, g)) fn(g);
+      a++;
+      b++;
+    }
+  }
+}
+
 int calc_metrics(HostMesh& m) {
   const int nn = m.nnode;
   m.vol.assign(nn, 0.0);
   // every tet must be right-handed (positive volume in the reference's
   // CalcTetVol convention) for the dual areas to point from n[0] to n[1]
-  m.inverted = 0;
-  for (size_t e = 0; e < m.etype.size(); e++) {
-    if (m.etype[e] != ETET) continue;
-    const int* q = &m.enodes[4 * e];
-    if (!(tet_vol(&m.xyz[3 * (size_t)q[0]], &m.xyz[3 * (size_t)q[1]], &m.xyz[3 * (size_t)q[2]],
-                  &m.xyz[3 * (size_t)q[3]]) > 0.0))
-      m.inverted++;
+  {
+    std::atomic<int> inverted(0);
+    parallel_ranges((long long)m.etype.size(), [&](long long b, long long e) {
+      int bad = 0;
+      for (long long t = b; t < e; t++) {
+        if (m.etype[t] != ETET) continue;
+        const int* q = &m.enodes[4 * t];
+        if (!(tet_vol(&m.xyz[3 * (size_t)q[0]], &m.xyz[3 * (size_t)q[1]], &m.xyz[3 * (size_t)q[2]],
+                      &m.xyz[3 * (size_t)q[3]]) > 0.0))
+          bad++;
+      }
+      inverted += bad;
+    });
+    m.inverted = inverted.load();
   }
   if (m.inverted) {
     m.err = "mesh has " + std::to_string(m.inverted) + " inverted or degenerate tetrahedra";
@@ -285,120 +415,152 @@ int calc_metrics(HostMesh& m) {
   m.ba.assign((size_t)4 * m.nbedge, 0.0);
   const double* X = m.xyz.data();
   // interior edges: two dual-face triangles and four sub-volumes per
-  // surrounding element (CalcAreasVolumes, ucs/mesh.tcc:1822-1985)
-  for (int i = 0; i < m.nedge; i++) {
-    int n1 = m.edges[2 * i], n2 = m.edges[2 * i + 1];
-    for (int k = m.ielsp[n2]; k < m.ielsp[n2 + 1]; k++) {
-      int e = m.elsp[k];
-      if (m.etype[e] != ETET) continue;
-      const int* nodes = &m.enodes[4 * e];
-      int l1 = -1, l2 = -1;
-      for (int q = 0; q < 4; q++) {
-        if (nodes[q] == n1) l1 = q;
-        else if (nodes[q] == n2) l2 = q;
-      }
-      if (l1 < 0 || l2 < 0) continue;  // edge not in this element
-      int orientation = 0, eid = -1;
-      for (int j = 0; j < 6; j++) {
-        if (kTetEorder[2 * j] == l1 && kTetEorder[2 * j + 1] == l2) { eid = j; orientation = 1; break; }
-        if (kTetEorder[2 * j + 1] == l1 && kTetEorder[2 * j] == l2) { eid = j; orientation = -1; break; }
-      }
-      int face1 = kTetE2f[2 * eid], face2 = kTetE2f[2 * eid + 1];
-      double edgept[3], f1[3], f2[3], ept[3], area[3];
-      mid2(&X[3 * n1], &X[3 * n2], edgept);
-      const int* fa = &kTetFl[3 * face1];
-      cen3(&X[3 * nodes[fa[0]]], &X[3 * nodes[fa[1]]], &X[3 * nodes[fa[2]]], f1);
-      const int* fb = &kTetFl[3 * face2];
-      cen3(&X[3 * nodes[fb[0]]], &X[3 * nodes[fb[1]]], &X[3 * nodes[fb[2]]], f2);
-      cen4(&X[3 * nodes[0]], &X[3 * nodes[1]], &X[3 * nodes[2]], &X[3 * nodes[3]], ept);
-      double o = (double)orientation;
+  // surrounding element (CalcAreasVolumes, ucs/mesh.tcc:1822-1985).  The
+  // reference visits the edges in order and, per edge, the elements of its
+  // second node in elsp order, adding the face triangles to the edge's area
+  // and two sub-volumes to each end's volume.  Here the areas are formed per
+  // edge (in parallel: each edge owns its area), and each node's volume by
+  // one thread that visits the node's edges in ascending edge order - the
+  // reference's sequence of additions to that node, so the sums are
+  // bit-identical whatever the thread count.
+  parallel_ranges(m.nedge, [&](long long b, long long e) {
+    EdgeTetGeom g;
+    for (long long i = b; i < e; i++) {
+      const int n1 = m.edges[2 * i], n2 = m.edges[2 * i + 1];
       double* a = &m.ea[4 * i];
-      tri_area(ept, f2, edgept, area);
-      area[0] = o * area[0]; area[1] = o * area[1]; area[2] = o * area[2];
-      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
-      tri_area(edgept, f1, ept, area);
-      area[0] = o * area[0]; area[1] = o * area[1]; area[2] = o * area[2];
-      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
-      double tv0 = o * tet_vol(&X[3 * n1], ept, f2, edgept);
-      double tv1 = o * tet_vol(&X[3 * n1], f1, ept, edgept);
-      double tv2 = o * tet_vol(&X[3 * n2], ept, f1, edgept);
-      double tv3 = o * tet_vol(&X[3 * n2], f2, ept, edgept);
-      m.vol[n1] += tv0; m.vol[n1] += tv1;
-      m.vol[n2] += tv2; m.vol[n2] += tv3;
+      for_edge_tets(m, n1, n2, g, [&](const EdgeTetGeom& t) {
+        double area[3];
+        tri_area(t.ept, t.f2, t.edgept, area);
+        area[0] = t.o * area[0]; area[1] = t.o * area[1]; area[2] = t.o * area[2];
+        a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+        tri_area(t.edgept, t.f1, t.ept, area);
+        area[0] = t.o * area[0]; area[1] = t.o * area[1]; area[2] = t.o * area[2];
+        a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+      });
     }
-  }
+  });
   // boundary half-edges: two triangles of the boundary face's median dual
-  // (ucs/mesh.tcc:2148-2190)
-  for (int i = 0; i < m.nbedge; i++) {
-    int n1 = m.bedges[2 * i];
-    int e = m.belem[i];
-    const int* nodes = &m.enodes[4 * e];
-    int nid = -1;
-    for (int q = 0; q < 3; q++)
-      if (nodes[q] == n1) nid = q;
-    double ept[3], edgept[3], area[3];
-    cen3(&X[3 * nodes[0]], &X[3 * nodes[1]], &X[3 * nodes[2]], ept);
-    int alt = nodes[kClTri[2 * nid]];
-    mid2(&X[3 * n1], &X[3 * alt], edgept);
-    tri_area(ept, &X[3 * n1], edgept, area);
-    double* a = &m.ba[4 * i];
-    a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
-    alt = nodes[kClTri[2 * nid + 1]];
-    mid2(&X[3 * n1], &X[3 * alt], edgept);
-    tri_area(edgept, &X[3 * n1], ept, area);
-    a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
-  }
-  // CheckForClosure (ucs/mesh.tcc:2274): sum of signed face areas per node
+  // (ucs/mesh.tcc:2148-2190); each half-edge owns its area
+  parallel_ranges(m.nbedge, [&](long long b, long long e) {
+    for (long long i = b; i < e; i++) {
+      const int n1 = m.bedges[2 * i];
+      const int* nodes = &m.enodes[4 * (size_t)m.belem[i]];
+      int nid = -1;
+      for (int q = 0; q < 3; q++)
+        if (nodes[q] == n1) nid = q;
+      double ept[3], edgept[3], area[3];
+      cen3(&X[3 * (size_t)nodes[0]], &X[3 * (size_t)nodes[1]], &X[3 * (size_t)nodes[2]], ept);
+      int alt = nodes[kClTri[2 * nid]];
+      mid2(&X[3 * (size_t)n1], &X[3 * (size_t)alt], edgept);
+      tri_area(ept, &X[3 * (size_t)n1], edgept, area);
+      double* a = &m.ba[4 * i];
+      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+      alt = nodes[kClTri[2 * nid + 1]];
+      mid2(&X[3 * (size_t)n1], &X[3 * (size_t)alt], edgept);
+      tri_area(edgept, &X[3 * (size_t)n1], ept, area);
+      a[0] = a[0] + area[0]; a[1] = a[1] + area[1]; a[2] = a[2] + area[2];
+    }
+  });
+  // Per node: the dual volume, the closure sum of CheckForClosure
+  // (ucs/mesh.tcc:2274; the signed face areas, before they are normalised)
+  // and the weighted LSQ normal matrix (Kernel_LSQ_CoefficientsWeighted,
+  // ucs/gradient.tcc:461; the boundary variant only adds for ghost nodes,
+  // which a single partition does not have).  The reference accumulates all
+  // three edge by edge into both ends; here one thread forms a node's sums
+  // over its edges in ascending edge order (then, for the closure sum, its
+  // half-edges in ascending order): the same additions in the same order.
+  m.sw.assign((size_t)6 * nn, 0.0);
   {
-    std::vector<double> s((size_t)3 * nn, 0.0);
+    // a node's interior edges, ascending, with the node's end (bit 0: 0 the
+    // edge's first node, 1 its second); its boundary half-edges, ascending
+    std::vector<int> iptr(nn + 1, 0), bptr(nn + 1, 0);
     for (int i = 0; i < m.nedge; i++) {
-      int n1 = m.edges[2 * i], n2 = m.edges[2 * i + 1];
-      for (int c = 0; c < 3; c++) {
-        s[3 * n1 + c] = s[3 * n1 + c] - m.ea[4 * i + c];
-        s[3 * n2 + c] = s[3 * n2 + c] + m.ea[4 * i + c];
+      iptr[m.edges[2 * i] + 1]++;
+      iptr[m.edges[2 * i + 1] + 1]++;
+    }
+    for (int i = 0; i < m.nbedge; i++) bptr[m.bedges[2 * i] + 1]++;
+    for (int i = 0; i < nn; i++) {
+      iptr[i + 1] += iptr[i];
+      bptr[i + 1] += bptr[i];
+    }
+    std::vector<uint32_t> inc((size_t)iptr[nn]);
+    std::vector<int> binc((size_t)bptr[nn]);
+    {
+      std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+      for (int i = 0; i < m.nedge; i++) {
+        inc[fill[m.edges[2 * i]]++] = (uint32_t)i << 1;
+        inc[fill[m.edges[2 * i + 1]]++] = ((uint32_t)i << 1) | 1u;
       }
+      std::vector<int> bfill(bptr.begin(), bptr.end() - 1);
+      for (int i = 0; i < m.nbedge; i++) binc[bfill[m.bedges[2 * i]]++] = i;
     }
-    for (int i = 0; i < m.nbedge; i++) {
-      int n1 = m.bedges[2 * i];
-      for (int c = 0; c < 3; c++) s[3 * n1 + c] = s[3 * n1 + c] - m.ba[4 * i + c];
-    }
+    std::vector<double> open(nn);
+    parallel_ranges(nn, [&](long long b, long long e) {
+      EdgeTetGeom g;
+      for (long long n = b; n < e; n++) {
+        double v = 0.0, sc[3] = {0.0, 0.0, 0.0}, w[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int t = iptr[n]; t < iptr[n + 1]; t++) {
+          const uint32_t i = inc[t] >> 1;
+          const bool second = (inc[t] & 1u) != 0;
+          const int n1 = m.edges[2 * (size_t)i], n2 = m.edges[2 * (size_t)i + 1];
+          for_edge_tets(m, n1, n2, g, [&](const EdgeTetGeom& t) {
+            if (!second) {
+              const double* p1 = &X[3 * (size_t)n1];
+              v += t.o * tet_vol(p1, t.ept, t.f2, t.edgept);
+              v += t.o * tet_vol(p1, t.f1, t.ept, t.edgept);
+            } else {
+              const double* p2 = &X[3 * (size_t)n2];
+              v += t.o * tet_vol(p2, t.ept, t.f1, t.edgept);
+              v += t.o * tet_vol(p2, t.f2, t.ept, t.edgept);
+            }
+          });
+          const double* a = &m.ea[4 * (size_t)i];
+          for (int c = 0; c < 3; c++) sc[c] = second ? sc[c] + a[c] : sc[c] - a[c];
+          double dx[3];
+          sub3(&X[3 * (size_t)n1], &X[3 * (size_t)n2], dx);
+          const double ds2 = 1.0 / (dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+          double tt[6];
+          if (!second) {
+            tt[0] = dx[0] * dx[0] * ds2;
+            tt[1] = dx[0] * dx[1] * ds2;
+            tt[2] = dx[0] * dx[2] * ds2;
+            tt[3] = dx[1] * dx[1] * ds2;
+            tt[4] = dx[1] * dx[2] * ds2;
+            tt[5] = dx[2] * dx[2] * ds2;
+          } else {
+            // the second node's terms are formed from the negated difference
+            tt[0] = dx[0] * dx[0] * ds2;
+            tt[3] = dx[1] * dx[1] * ds2;
+            tt[5] = dx[2] * dx[2] * ds2;
+            dx[0] = -dx[0]; dx[1] = -dx[1]; dx[2] = -dx[2];
+            tt[1] = (dx[0] * dx[1]) * ds2;
+            tt[2] = (dx[0] * dx[2]) * ds2;
+            tt[4] = (dx[1] * dx[2]) * ds2;
+          }
+          for (int c = 0; c < 6; c++) w[c] += tt[c];
+        }
+        for (int t = bptr[n]; t < bptr[n + 1]; t++) {
+          const double* a = &m.ba[4 * (size_t)binc[t]];
+          for (int c = 0; c < 3; c++) sc[c] = sc[c] - a[c];
+        }
+        m.vol[n] = v;
+        for (int c = 0; c < 6; c++) m.sw[6 * n + c] = w[c];
+        open[n] = mag3(sc);
+      }
+    });
     m.unclosed = 0;
     m.max_open = 0.0;
     for (int i = 0; i < nn; i++) {
-      double mg = mag3(&s[3 * i]);
-      if (mg > m.max_open) m.max_open = mg;
-      if (mg > 1.0e-10) m.unclosed++;
+      if (open[i] > m.max_open) m.max_open = open[i];
+      if (open[i] > 1.0e-10) m.unclosed++;
     }
   }
-  for (int i = 0; i < m.nedge; i++) m.ea[4 * i + 3] = normalize3(&m.ea[4 * i], &m.ea[4 * i]);
-  for (int i = 0; i < m.nbedge; i++) m.ba[4 * i + 3] = normalize3(&m.ba[4 * i], &m.ba[4 * i]);
-  // Weighted LSQ normal matrices (Kernel_LSQ_CoefficientsWeighted,
-  // ucs/gradient.tcc:461); the boundary variant only adds for ghost nodes,
-  // which a single partition does not have.
-  m.sw.assign((size_t)6 * nn, 0.0);
-  for (int i = 0; i < m.nedge; i++) {
-    int l = m.edges[2 * i], r = m.edges[2 * i + 1];
-    double dx[3];
-    sub3(&X[3 * l], &X[3 * r], dx);
-    double ds2 = 1.0 / (dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
-    double tl[6], tr[6];
-    tl[0] = dx[0] * dx[0] * ds2;
-    tl[1] = dx[0] * dx[1] * ds2;
-    tl[2] = dx[0] * dx[2] * ds2;
-    tl[3] = dx[1] * dx[1] * ds2;
-    tl[4] = dx[1] * dx[2] * ds2;
-    tl[5] = dx[2] * dx[2] * ds2;
-    dx[0] = -dx[0]; dx[1] = -dx[1]; dx[2] = -dx[2];
-    tr[0] = tl[0];
-    tr[1] = (dx[0] * dx[1]) * ds2;
-    tr[2] = (dx[0] * dx[2]) * ds2;
-    tr[3] = tl[3];
-    tr[4] = (dx[1] * dx[2]) * ds2;
-    tr[5] = tl[5];
-    // DriverScatter adds the right side first, then the left
-    for (int c = 0; c < 6; c++) m.sw[6 * r + c] += tr[c];
-    for (int c = 0; c < 6; c++) m.sw[6 * l + c] += tl[c];
-  }
+  parallel_ranges(m.nedge, [&](long long b, long long e) {
+    for (long long i = b; i < e; i++) m.ea[4 * i + 3] = normalize3(&m.ea[4 * i], &m.ea[4 * i]);
+  });
+  parallel_ranges(m.nbedge, [&](long long b, long long e) {
+    for (long long i = b; i < e; i++) m.ba[4 * i + 3] = normalize3(&m.ba[4 * i], &m.ba[4 * i]);
+  });
   m.metrics_built = 1;
   return 0;
 }
@@ -681,8 +843,16 @@ PCFD_API pcfd_mesh_t pcfd_mesh_from_elements(int nnode, const double* xyz, int n
 PCFD_API int pcfd_mesh_build(pcfd_mesh_t h) {
   if (!h) return PCFD_ERR_ARG;
   HostMesh* m = (HostMesh*)h;
-  if (build_maps(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
-  if (calc_metrics(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  try {
+    if (build_maps(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+    if (calc_metrics(*m) != 0) { g_last_mesh_error = m->err; return PCFD_ERR_MESH; }
+  } catch (const std::bad_alloc&) {
+    g_last_mesh_error = "pcfd_mesh_build: out of host memory";
+    return PCFD_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    g_last_mesh_error = std::string("pcfd_mesh_build: ") + e.what();
+    return PCFD_ERR_MESH;
+  }
   return PCFD_OK;
 }
 

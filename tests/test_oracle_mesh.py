@@ -34,7 +34,11 @@ def test_oracle_preprocessing_matches_reference(case):
                                 dict(nx=9, ny=8, nz=5, lx=1.1, jitter=0.2, seed=5, y_ratio=1.2, jitter_mode=1),
                                 dict(nx=10, ny=6, nz=5, lx=2.0, jitter=0.2, seed=9, ramp_deg=15.0, ramp_x0=0.5),
                                 dict(nx=14, ny=12, nz=4, lx=13 / 11, jitter=0.2, seed=6, y_ratio=1.1, wall_ar_max=3.0,
-                                     wall_start_i=2, upstream_tag=7)])
+                                     wall_start_i=2, upstream_tag=7),
+                                # large enough (98,560 nodes, 74k half-edges) for the product's
+                                # preprocessing to run its loops on several host threads
+                                dict(nx=56, ny=44, nz=40, lx=55 / 43, jitter=0.2, seed=3, y_ratio=1.1, jitter_mode=1,
+                                     wall_ar_max=50.0, wall_start_i=12, upstream_tag=7)])
 def test_oracle_box_matches_product_box(kw):
     o = OracleMesh.box(**kw)
     p = Mesh.box(**kw)
