@@ -18,9 +18,11 @@
 //   4. further whole steps (PostTimeAdvance, PreTimeAdvance, NewtonIterate),
 //      recording their residual norms and the final state.
 //
-// An optional <case>.qinit ([nnode][5] conservative doubles in the file's
-// node order) replaces the freestream initial state before step 1, so the
-// gradients, limiters and viscous terms are all active.
+// An optional <case>.qinit ([nnode][neqn] doubles of the equation set's stored
+// variables, in the file's node order) replaces the freestream initial state
+// before step 1, so the gradients, limiters and viscous terms are all active.
+// An optional <case>/chemdb.txt is written into <case>/chemdb.h5 first, the
+// species database a reacting case names (write_chem_db below).
 //
 // Usage: ref_dump <case directory> <case name> <output directory> <steps>
 // Output: one raw little-endian file per array plus index.txt
@@ -64,6 +66,7 @@
 #include "limiters.h"
 #include "crs.h"
 #include "crsmatrix.h"
+#include "h5layer.h"
 
 #include <cmath>
 #include <cstdio>
@@ -178,6 +181,44 @@ void dump_forces(SolutionSpace<Real>* space, const std::string& pre) {
   dump(pre + "forces", v, 1, 6);
 }
 
+// The species database of a reacting case.  The reference reads it from an
+// HDF5 file (Species::GetDBInfo, ucs/species.tcc:140) that its Python
+// builder writes; here <case>/chemdb.txt carries the same datasets as text
+// (one per line: "species <name>", "<dataset> <value>" for scalars,
+// "<dataset> <rows> <cols> <values...>" for arrays) and is written through
+// the reference's own h5layer writers into <case>/chemdb.h5 (the stand-in
+// file store), which the case's chemicalDatabase names.
+int write_chem_db(const std::string& dir) {
+  std::ifstream in((dir + "chemdb.txt").c_str());
+  if (!in.is_open()) return 0;
+  hid_t f = HDF_CreateFile(dir + "chemdb.h5", 1);
+  if (f < 0) return -1;
+  std::string line, group;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::string key;
+    if (!(ls >> key)) continue;
+    if (key == "species") {
+      std::string name;
+      ls >> name;
+      group = "/species/" + name;
+      continue;
+    }
+    std::vector<double> v;
+    double x;
+    while (ls >> x) v.push_back(x);
+    if (v.size() == 1) {
+      HDF_WriteScalar(f, group, key, &v[0]);
+    } else if (v.size() >= 2) {
+      const int rows = (int)v[0], cols = (int)v[1];
+      if ((size_t)rows * cols + 2 != v.size()) return -2;
+      HDF_WriteArray(f, group, key, &v[2], rows, cols);
+    }
+  }
+  HDF_CloseFile(f);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char* argv[]) {
@@ -211,6 +252,7 @@ int main(int argc, char* argv[]) {
   std::vector<Param<Real>*> paramList;
   TemporalControl<Real> temporalControl;
   HDF_TurnOffErrorHandling();
+  if (write_chem_db(dir) != 0) { std::fprintf(stderr, "chemistry database write failed\n"); return 4; }
   Abort.rootDirectory = dir;
   if (ReadParamFile(paramList, casename, dir)) { std::fprintf(stderr, "param read failed\n"); return 4; }
   if (temporalControl.Read(casename, dir)) { std::fprintf(stderr, "temporal control read failed\n"); return 4; }
@@ -257,6 +299,14 @@ int main(int argc, char* argv[]) {
   // (ucs/compressible.tcc:835-836)
   dump_scalar("qinf_T", real(param->initialTemperature / param->ref_temperature));
   dump_scalar("qinf_p", real(param->initialPressure / param->ref_pressure));
+  // the reference scales (Param::PostCompute, ucs/param.tcc:355) the reacting
+  // set's non-dimensional arithmetic uses
+  {
+    double refs[9] = {real(param->ref_density), real(param->ref_pressure), real(param->ref_temperature),
+                      real(param->ref_specific_enthalpy), real(param->ref_velocity), real(param->ref_viscosity),
+                      real(param->ref_k), real(param->ref_time), real(param->ref_length)};
+    dump("refs", refs, 1, 9);
+  }
 
   // mesh maps and metrics (after the reorder, which ucs.x does at set-up)
   dump_elements("elements", m->elementList);

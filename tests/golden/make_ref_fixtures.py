@@ -7,8 +7,10 @@ For each case this script
   1. writes a jittered Kuhn-split tetrahedral box as UGRID (the reference's
      ASCII reader, ucs/mesh.tcc:6740) with boundary tags 1..6 on the faces
      x=0, x=max, y=0, y=max, z=0, z=max, a ``.param`` and a ``.bc`` file, and a
-     seeded ``.qinit`` state (freestream x (1 + U[-amp, amp]) per conserved
-     component);
+     seeded ``.qinit`` state (freestream x (1 + U[-amp, amp]) per stored
+     variable); a reacting case also gets its mechanism file and the species
+     datasets as ``chemdb.txt``, which the harness stores as the case's
+     chemical database;
   2. runs ``oracle/_ref/ref_dump``, which decomposes the mesh into one
      partition (udecomp.x), sets the solver up as ucs.x does (reverse
      Cuthill-McKee reorder, maps, metrics, CRS) and runs Newton steps stage by
@@ -51,7 +53,37 @@ CASES = {
         eqn="compressibleNS", mach=0.8, sorder=2, limiter=1, nsgs=6, cfl=3.0, steps=2, amp=0.02,
         bc={1: "farField", 2: "farField", 3: "noSlip", 4: "farField", 5: "symmetry", 6: "symmetry"},
         twall={3: -1.0}, reorder=0),
+    # the reacting set: 5-species air (the reference's chemModels/5speciesAir.rxn), laminar NS,
+    # second order, an isothermal no-slip wall, finite-rate chemistry on
+    "fr_plate": dict(
+        n=(7, 6, 5), lx=1.2, ly=1.0, lz=1.0, jitter=0.2, seed=14, ramp_deg=0.0, ramp_x0=0.5, y_ratio=1.1,
+        eqn="compressibleNSFR", mach=2.0, sorder=2, limiter=3, nsgs=4, cfl=2.0, steps=2, amp=0.01,
+        bc={1: "sonicInflow", 2: "sonicOutflow", 3: "noSlip", 4: "sonicOutflow", 5: "symmetry", 6: "symmetry"},
+        twall={3: 1500.0}, reorder=1, chem="5speciesAir", temperature=3000.0, no_cvbc=1,
+        # mass fractions in the model's species order (N2, O2, NO, N, O: first appearance in the
+        # mechanism's reactions)
+        massfractions=[0.745, 0.2, 0.035, 0.01, 0.01]),
 }
+
+
+def write_chem_db(path, fixture):
+    """The species datasets Species::GetDBInfo reads (ucs/species.tcc:140),
+    from the fixture the reference's own database builder produced, as the
+    text the harness writes into the stand-in HDF5 store."""
+    import json
+    d = json.loads(Path(fixture).read_text())
+    lines = []
+    for sp in d["species"]:
+        lines.append("species %s" % sp["name"])
+        lines.append("MW %r" % (sp["MW"] * 1000.0))
+        lines.append("NASA7_burcat_coeff15 %r" % sp["hf298"])
+        for key, v in (("NASA7_burcat1", sp["lo"]), ("NASA7_burcat2", sp["hi"])):
+            lines.append("%s %d 1 %s" % (key, len(v), " ".join(repr(float(x)) for x in v)))
+        for key in ("mu", "k"):
+            rows = sp[key]
+            lines.append("%s %d %d %s" % (key, len(rows), len(rows[0]),
+                                          " ".join(repr(float(x)) for r in rows for x in r)))
+    Path(path).write_text("\n".join(lines) + "\n")
 
 
 def kuhn_box(nx, ny, nz, lx, ly, lz, jitter, seed, ramp_deg, ramp_x0, y_ratio):
@@ -171,7 +203,7 @@ def write_param(path, name, c):
         "flowDirection = [1.0, 0.0, 0.0]",
         "refPressure = 101325.0",
         "initialPressure = 101325.0",
-        "initialTemperature = 300.0",
+        "initialTemperature = %r" % c.get("temperature", 300.0),
         "refLength = 1.0",
         # laminar viscosity giving Re close to 1e5 on unit length (the
         # reference derives Re from it, ucs/compressible.tcc:86-89)
@@ -179,8 +211,13 @@ def write_param(path, name, c):
         "prandtlNumber = 0.72",
         "solutionWrite = 0",
         "turbulenceModel = 0",
-        "<<<END SPACE>>>",
     ]
+    if "chem" in c:
+        lines += ["chemicalDatabase = chemdb.h5",
+                  "massFractions = [%s]" % ", ".join(repr(float(v)) for v in c["massfractions"]),
+                  "reactionsOn = 1",
+                  "noCVBC = %d" % c.get("no_cvbc", 0)]
+    lines.append("<<<END SPACE>>>")
     Path(path).write_text("\n".join(lines) + "\n")
 
 
@@ -198,7 +235,7 @@ def write_bc(path, c):
     Path(path).write_text("\n".join(lines) + "\n")
 
 
-def run_case(exe, name, c, workdir):
+def run_case(exe, name, c, workdir, ref=None):
     nx, ny, nz = c["n"]
     xyz, tris, tags, tets = kuhn_box(nx, ny, nz, c["lx"], c["ly"], c["lz"], c["jitter"], c["seed"],
                                      c["ramp_deg"], c["ramp_x0"], c["y_ratio"])
@@ -207,6 +244,10 @@ def run_case(exe, name, c, workdir):
     write_ugrid(d / (name + ".ugrid"), xyz, tris, tags, tets)
     write_param(d / (name + ".param"), name, c)
     write_bc(d / (name + ".bc"), c)
+    if "chem" in c:
+        # the mechanism file beside the case (ChemModel reads <case>.rxn) and the species data
+        (d / (name + ".rxn")).write_text((Path(ref) / "chemModels" / (c["chem"] + ".rxn")).read_text())
+        write_chem_db(d / "chemdb.txt", HERE / "chem_5species_air.json")
     # freestream (non-dimensional: rho = gamma, p = 1, |u| = Mach) with a seeded perturbation
     rng = np.random.default_rng(1000 + c["seed"])
     out = d / "dump"
@@ -220,7 +261,12 @@ def run_case(exe, name, c, workdir):
     subprocess.run([str(exe), str(d), name, str(out), "1"], check=True, cwd=d,
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     qinf = np.fromfile(out / "qinf.bin", dtype="<f8")
-    q0 = np.tile(qinf[:5], (len(xyz), 1)) * (1.0 + rng.uniform(-c["amp"], c["amp"], size=(len(xyz), 5)))
+    neqn = int(np.fromfile(out / "neqn.bin", dtype="<i4")[0])
+    q0 = np.tile(qinf[:neqn], (len(xyz), 1)) * (1.0 + rng.uniform(-c["amp"], c["amp"], size=(len(xyz), neqn)))
+    if "chem" in c:
+        # native variables (rhoi, u, v, w, T): give v and w a seeded non-zero part too
+        ns = neqn - 4
+        q0[:, ns + 1:ns + 3] += c["amp"] * qinf[ns] * rng.uniform(-1.0, 1.0, size=(len(xyz), 2))
     q0.astype("<f8").tofile(d / (name + ".qinit"))
     for p in out.glob("*"):
         p.unlink()
@@ -262,7 +308,7 @@ def main():
     names = sys.argv[2:] if len(sys.argv) > 2 else list(CASES)
     with tempfile.TemporaryDirectory() as tmp:
         for name in names:
-            a = run_case(exe, name, CASES[name], tmp)
+            a = run_case(exe, name, CASES[name], tmp, ref)
             print(name, "nnode", int(a["nnode"][0]), "nedge", int(a["nedge"][0]), "norms", a["s1_norms"].ravel())
 
 
