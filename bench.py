@@ -185,7 +185,7 @@ def run_reference(args, rank, pg):
     """--impl reference: the reference's CPU path - the oracle port, which is
     bit-identical to the reference's own residual on its outputs (the
     reference itself needs HDF5/MPI/METIS and its source tree, absent on the
-    GPU machine) - on all host threads, rank 0 only, over a bounded sample of the
+    machines the benchmark runs on) - on all host threads, rank 0 only, over a bounded sample of the
     workload; the process loads nothing of the product."""
     if rank != 0:
         return

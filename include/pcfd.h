@@ -35,7 +35,7 @@ extern "C" {
 #define PCFD_ERR_CUDA 3        /* CUDA runtime error */
 #define PCFD_ERR_MESH 4        /* mesh preprocessing failed */
 #define PCFD_ERR_NOMEM 5       /* allocation failed */
-#define PCFD_ERR_UNSUPPORTED 6 /* option not available in this build */
+#define PCFD_ERR_UNSUPPORTED 6 /* option the library does not support */
 #define PCFD_ERR_NUMERIC 7     /* device reported a numerical failure (see pcfd_get_health) */
 
 /* ---- boundary condition types -------------------------------------------

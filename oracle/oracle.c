@@ -2,8 +2,8 @@
  * CPU ORACLE - test infrastructure only.
  *
  * A plain-C restatement of ProteusCFD's edge-based residual path, used by
- * tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py as
- * the checker for the CUDA implementation.  It is never linked into, called
+ * tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py to
+ * check the CUDA implementation against.  It is never linked into, called
  * by or shipped with the product library.
  *
  * Pinning: the reference solver itself is built from its own sources by

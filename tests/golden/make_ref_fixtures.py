@@ -35,13 +35,13 @@ ROOT = HERE.parent.parent
 
 # boundary types by name (ucs/bc_defines.h)
 CASES = {
-    # configs[0] family: Mach 2 Euler over a sheared ramp, first order
+    # the Euler ramp family: Mach 2 Euler over a sheared ramp, first order
     "euler_ramp": dict(
         n=(9, 6, 5), lx=2.0, ly=1.0, lz=1.0, jitter=0.2, seed=11, ramp_deg=15.0, ramp_x0=0.5, y_ratio=1.0,
         eqn="compressibleEuler", mach=2.0, sorder=1, limiter=0, nsgs=10, cfl=5.0, steps=3, amp=0.01,
         bc={1: "sonicInflow", 2: "sonicOutflow", 3: "impermeableWall", 4: "impermeableWall",
             5: "symmetry", 6: "symmetry"}),
-    # configs[1] family: Mach 0.8 laminar NS over an adiabatic no-slip wall, second order
+    # the flat-plate family: Mach 0.8 laminar NS over an adiabatic no-slip wall, second order
     "ns_plate": dict(
         n=(8, 7, 5), lx=7.0 / 6.0, ly=1.0, lz=1.0, jitter=0.2, seed=12, ramp_deg=0.0, ramp_x0=0.5, y_ratio=1.1,
         eqn="compressibleNS", mach=0.8, sorder=2, limiter=3, nsgs=10, cfl=5.0, steps=3, amp=0.01,
