@@ -715,7 +715,8 @@ def run_gb300(args, ws, rank, local, pg):
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": ms_per_step, "residual_evals_per_s": ws * 1e3 / ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": "ns_flatplate %dx%dx%d: 2nd-order laminar NS residual (BCs+LSQ grad+modified "
                                "Venkatakrishnan limiter K=%g+Roe+viscous), Mach 0.8, Re 1e5"
