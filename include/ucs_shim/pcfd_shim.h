@@ -208,6 +208,165 @@ Type NewtonIterate(SolutionSpace<Type>* space, pcfd_solver_t h, int linear_solve
   return r.res[0];
 }
 
+// ---- the reacting equation set (CompressibleFREqnSet) ----------------------
+// Include the reference's chem.h and compressibleFR.h too.
+
+// The chemistry the equation set owns (CompressibleFREqnSet::chem,
+// ucs/compressibleFR.tcc:39) as pcfd_chem_model: per species the molecular
+// weight (kg/mol after Species::GetDBInfo's division, ucs/species.tcc:162-167),
+// the NASA-7 fits below and above 1000 K (thermo_coeff[0], [1]; the third
+// range repeats the second) and the viscosity and conductivity fits; per
+// reaction its rate law and its species with their global indices,
+// stoichiometric coefficients and third-body efficiencies (ucs/reaction.h).
+template <class Type>
+void ChemModelFrom(const ChemModel<Type>* chem, pcfd_chem_model& m)
+{
+  m = pcfd_chem_model{};
+  if (chem->nspecies > PCFD_CHEM_MAX_SPECIES || chem->nreactions > PCFD_CHEM_MAX_REACTIONS) {
+    Abort << std::string("pcfd_shim::ChemModelFrom: mechanism larger than the library's limits");
+  }
+  m.nspecies = chem->nspecies;
+  for (Int k = 0; k < chem->nspecies; k++) {
+    const Species<Type>& s = chem->species[k];
+    m.mw[k] = s.MW;
+    for (int i = 0; i < 7; i++) {
+      m.nasa_lo[k][i] = s.thermo_coeff[0][i];
+      m.nasa_hi[k][i] = s.thermo_coeff[1][i];
+    }
+    m.nmu[k] = s.mu_coeff_curves;
+    m.nk[k] = s.k_coeff_curves;
+    for (Int r = 0; r < s.mu_coeff_curves; r++)
+      for (int i = 0; i < 6; i++) m.mu_fit[k][r][i] = s.mu_coeff[r][i];
+    for (Int r = 0; r < s.k_coeff_curves; r++)
+      for (int i = 0; i < 6; i++) m.k_fit[k][r][i] = s.k_coeff[r][i];
+  }
+  m.nreactions = chem->nreactions;
+  for (Int j = 0; j < chem->nreactions; j++) {
+    const Reaction<Type>& r = chem->reactions[j];
+    pcfd_chem_reaction& c = m.rx[j];
+    // the reaction's species, third bodies included (Reaction::GetNspecies)
+    const Int nloc = (Int)r.speciesSymbols.size();
+    if (nloc > PCFD_CHEM_MAX_LOCAL) {
+      Abort << std::string("pcfd_shim::ChemModelFrom: reaction with too many species");
+    }
+    c.type = r.rxnType;
+    c.A = r.A;
+    c.EA = r.EA;
+    c.n = r.n;
+    c.third_bodies = r.thirdBodiesPresent ? 1 : 0;
+    c.nlocal = nloc;
+    for (Int l = 0; l < nloc; l++) {
+      c.global[l] = r.globalIndx[l];
+      c.nup[l] = r.Nup[l];
+      c.nupp[l] = r.Nupp[l];
+      // TBEff is filled only for third-body reactions (Reaction::ParseThirdBodies)
+      c.tbeff[l] = (size_t)l < r.TBEff.size() ? r.TBEff[l] : 1.0;
+    }
+  }
+}
+
+// The reference scales the reacting set is non-dimensional in
+// (Param::PostCompute, ucs/param.tcc:355).
+template <class Type>
+pcfd_chem_ref ChemRefFrom(const Param<Type>* p)
+{
+  pcfd_chem_ref r;
+  r.density = p->ref_density;
+  r.pressure = p->ref_pressure;
+  r.temperature = p->ref_temperature;
+  r.specific_enthalpy = p->ref_specific_enthalpy;
+  r.velocity = p->ref_velocity;
+  r.viscosity = p->ref_viscosity;
+  r.conductivity = p->ref_k;
+  return r;
+}
+
+// A reacting handle with the space's mesh attached; keep `a` alive as long
+// as the handle is used with pcfd_chem_attach_mesh's arrays.
+template <class Type>
+pcfd_chem_t ChemCreate(SolutionSpace<Type>* space, CompressibleFREqnSet<Type>* eqn, MeshArrays& a)
+{
+  pcfd_chem_model m;
+  ChemModelFrom(eqn->chem, m);
+  pcfd_chem_t h = nullptr;
+  Check(pcfd_chem_create(&m, &h), "pcfd_chem_create");
+  GatherMesh(space->m, a);
+  Check(pcfd_chem_attach_mesh(h, &a.view), "pcfd_chem_attach_mesh");
+  return h;
+}
+
+// The boundary tables UpdateBCs reads, per face tag (BoundaryConditions,
+// ucs/bc.tcc:71,77; BCObj::Qref, which points at the equation set's Qinf
+// unless the .bc file gave one, ucs/bc.tcc:51-58).
+struct ChemBCTables {
+  std::vector<int> type, sym;
+  std::vector<double> twall, qref;
+};
+template <class Type>
+void ChemBCs(SolutionSpace<Type>* space, ChemBCTables& t)
+{
+  EqnSet<Type>* eqn = space->eqnset;
+  const int nvars = eqn->neqn + eqn->nauxvars;
+  const int ntags = space->bc->num_bcs + 1;
+  t.type.assign(ntags, -1);
+  t.twall.assign(ntags, 0.0);
+  t.qref.assign((size_t)ntags * nvars, 0.0);
+  t.sym.clear();
+  for (int tag = 0; tag < ntags; tag++) {
+    BCObj<Real>* o = space->bc->GetBCObj(tag);
+    t.type[tag] = space->bc->GetBCType(tag);
+    t.twall[tag] = o->twall;
+    std::vector<Real> q(nvars);
+    o->GetQref(q.data());
+    for (int i = 0; i < nvars; i++) t.qref[(size_t)tag * nvars + i] = q[i];
+    if (t.type[tag] == Proteus_Symmetry) t.sym.push_back(tag);
+  }
+}
+
+// SpatialResidual (ucs/residual.tcc:66) of the reacting set in the
+// reference's NewtonIterate order, with q, the gradient and the limiter on
+// the host arrays the reference reads: UpdateBCs, Gradient::Compute,
+// Limiter::Compute once past the first-order steps, the inviscid residual
+// (first order, or second order with the limiter) with the chemistry source,
+// plus the viscous residual (the directional correction once second order
+// is on).  b goes to crs->b.  The reference's own TemporalResidual and
+// boundary-row hook (ucs/residual.tcc:20-40) then run on crs->b as before.
+template <class Type>
+void ReactingSpatialResidual(SolutionSpace<Type>* space, CompressibleFREqnSet<Type>* eqn, pcfd_chem_t h)
+{
+  Param<Type>* p = space->param;
+  Mesh<Type>* m = space->m;
+  const int nnode = m->GetNumNodes();
+  const int neqn = eqn->neqn;
+  ChemBCTables t;
+  ChemBCs(space, t);
+  const pcfd_chem_ref ref = ChemRefFrom(p);
+  pcfd_chem_flux_opts o;
+  o.beta = 1.0;
+  o.pref = eqn->Pref;
+  o.symmetry2D = 0;
+  Check(pcfd_chem_update_bcs(h, &ref, (int)t.type.size(), t.type.data(), t.twall.data(), t.qref.data(), p->no_cvbc,
+                             space->q, 0), "pcfd_chem_update_bcs");
+  const bool second = p->sorder > 1 && space->iter > p->nFirstOrderSteps;
+  if (second || p->viscous)
+    Check(pcfd_chem_gradient(h, space->q, t.sym.data(), (int)t.sym.size(), space->qgrad, 0), "pcfd_chem_gradient");
+  if (second && p->limiter && space->iter % p->limiterRefresh == 0 && space->iter < p->limiterFreeze)
+    Check(pcfd_chem_limiter(h, p->chi, space->q, space->qgrad, space->limiter->l, 0), "pcfd_chem_limiter");
+  double norms[1 + PCFD_CHEM_MAX_SPECIES + 4];
+  if (second)
+    Check(pcfd_chem_residual_ho(h, &ref, &o, p->chi, p->ref_time, p->rxnOn ? 1 : 0, space->q, space->qgrad,
+                                space->limiter->l, space->crs->b, norms, 0), "pcfd_chem_residual_ho");
+  else
+    Check(pcfd_chem_residual(h, &ref, &o, p->ref_time, p->rxnOn ? 1 : 0, space->q, space->crs->b, norms, 0),
+          "pcfd_chem_residual");
+  if (p->viscous) {
+    std::vector<double> bv((size_t)nnode * neqn);
+    Check(pcfd_chem_viscous_residual(h, &ref, &o, p->Re, second ? 1 : 0, space->q, space->qgrad, bv.data(), 0),
+          "pcfd_chem_viscous_residual");
+    for (size_t i = 0; i < bv.size(); i++) space->crs->b[i] += bv[i];
+  }
+}
+
 }  // namespace pcfd_shim
 
 #endif

@@ -939,8 +939,8 @@ static void fr_aux_rec(const pcfd_chem_model* m, const pcfd_chem_ref* ref, doubl
  * unlimited extrapolation (ExtrapolateVariables, ucs/compressibleFR.tcc:734),
  * the running minimum, negatives clamped to 0 (:118-124).  The pressure clip
  * (Kernel_PressureClip, :737) is not restated.  lim [nnode][ns + 4]. */
-void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const double* grad,
-                         double chi, double* lim) {
+static void chem_limiter_raw(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const double* grad,
+                             double chi, double* lim) {
   const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
   const int nn = mv->nnode;
   double* qmin = (double*)calloc((size_t)nn * neqn, sizeof(double));
@@ -989,8 +989,80 @@ void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, con
       }
     }
   }
-  for (size_t i = 0; i < (size_t)nn * neqn; i++)
-    if (lim[i] < 0.0) lim[i] = 0.0;
   free(qmin);
   free(qmax);
+}
+
+/* the negative-limiter clamp at the end of Limiter<T>::Compute (:118-124) */
+static void chem_limiter_clamp(const pcfd_chem_model* m, const pcfd_mesh_view* mv, double* lim) {
+  const size_t n = (size_t)mv->nnode * (m->nspecies + 4);
+  for (size_t i = 0; i < n; i++)
+    if (lim[i] < 0.0) lim[i] = 0.0;
+}
+
+void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const double* grad,
+                         double chi, double* lim) {
+  chem_limiter_raw(m, mv, q, grad, chi, lim);
+  chem_limiter_clamp(m, mv, lim);
+}
+
+/* CompressibleFREqnSet::BadExtrapolation (ucs/compressibleFR.tcc:714) of a
+ * record whose auxiliary variables are current: a negative species density,
+ * a total energy (GetTotalEnergy, :1219) not above zero, a pressure or a
+ * temperature below 1e-10. */
+static int fr_bad_extrapolation(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q) {
+  const int ns = m->nspecies;
+  for (int i = 0; i < ns; i++)
+    if (Q[i] < 0.0) return 1;
+  const double T = Q[ns + 3], P = Q[ns + 4], rho = Q[ns + 5];
+  double X[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) X[i] = Q[i] / rho;
+  const double u = Q[ns], v = Q[ns + 1], w = Q[ns + 2];
+  const double v2 = u * u + v * v + w * w;
+  const double h = mix_h(m, X, T * ref->temperature) / ref->specific_enthalpy;
+  const double Et = (h * rho - P) + 0.5 * rho * v2;
+  if (Et <= 0.0) return 1;
+  if (P < 1.0e-10) return 1;
+  if (T < 1.0e-10) return 1;
+  return 0;
+}
+
+/* Limiter<T>::Compute (ucs/limiters.tcc:53) of the reacting set with its
+ * pressure clip: the raw modified Venkatakrishnan limiter as above, then
+ * Kernel_PressureClip (:737) edge by edge in edge order - each end's record
+ * extrapolated to the edge midpoint with its current limiter
+ * (ExtrapolateVariables, ucs/compressibleFR.tcc:734), its auxiliary
+ * variables recomputed, and the end's whole limiter zeroed when the state
+ * fails BadExtrapolation - then negatives clamped to 0.  lim [nnode][ns + 4]. */
+void oracle_chem_limiter_clip(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_mesh_view* mv,
+                              const double* q, const double* grad, double chi, double* lim) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns, nt = 2 * ns + 4;
+  chem_limiter_raw(m, mv, q, grad, chi, lim);
+  double Qe[6 + 3 * PCFD_CHEM_MAX_SPECIES], dQ[PCFD_CHEM_MAX_SPECIES + 4];
+  for (int e = 0; e < mv->nedge; e++) {
+    const int l = mv->edges[2 * e], r = mv->edges[2 * e + 1];
+    const double* xL = &mv->xyz[3 * (size_t)l];
+    const double* xR = &mv->xyz[3 * (size_t)r];
+    double dx[3] = {0.5 * (xR[0] - xL[0]), 0.5 * (xR[1] - xL[1]), 0.5 * (xR[2] - xL[2])};
+    for (int j = 0; j < neqn; j++) dQ[j] = q[(size_t)r * nv + j] - q[(size_t)l * nv + j];
+    for (int side = 0; side < 2; side++) {
+      const int a = side ? r : l;
+      if (side) {
+        for (int i = 0; i < 3; i++) dx[i] = -dx[i];
+        for (int j = 0; j < neqn; j++) dQ[j] = -dQ[j];
+      }
+      const double* qa = &q[(size_t)a * nv];
+      const double* g = &grad[(size_t)a * nt * 3];
+      double* la = &lim[(size_t)a * neqn];
+      for (int j = 0; j < neqn; j++) {
+        const double corr = 0.5 * chi * dQ[j] + (1.0 - chi) * (g[3 * j] * dx[0] + g[3 * j + 1] * dx[1] +
+                                                                 g[3 * j + 2] * dx[2]);
+        Qe[j] = qa[j] + corr * la[j];
+      }
+      fr_aux(m, ref, Qe);
+      if (fr_bad_extrapolation(m, ref, Qe))
+        for (int j = 0; j < neqn; j++) la[j] = 0.0;
+    }
+  }
+  chem_limiter_clamp(m, mv, lim);
 }

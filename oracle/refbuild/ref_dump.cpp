@@ -22,7 +22,7 @@
 // variables, in the file's node order) replaces the freestream initial state
 // before step 1, so the gradients, limiters and viscous terms are all active.
 // An optional <case>/chemdb.txt is written into <case>/chemdb.h5 first, the
-// species database a reacting case names (write_chem_db below).
+// species database a reacting case names (write_chem_db, chemdb_text.h).
 //
 // Usage: ref_dump <case directory> <case name> <output directory> <steps>
 // Output: one raw little-endian file per array plus index.txt
@@ -67,6 +67,7 @@
 #include "crs.h"
 #include "crsmatrix.h"
 #include "h5layer.h"
+#include "chemdb_text.h"
 
 #include <cmath>
 #include <cstdio>
@@ -179,44 +180,6 @@ void dump_forces(SolutionSpace<Real>* space, const std::string& pre) {
     v[3 + j] = real(f->bodies[1].vforces[j]);
   }
   dump(pre + "forces", v, 1, 6);
-}
-
-// The species database of a reacting case.  The reference reads it from an
-// HDF5 file (Species::GetDBInfo, ucs/species.tcc:140) that its Python
-// builder writes; here <case>/chemdb.txt carries the same datasets as text
-// (one per line: "species <name>", "<dataset> <value>" for scalars,
-// "<dataset> <rows> <cols> <values...>" for arrays) and is written through
-// the reference's own h5layer writers into <case>/chemdb.h5 (the stand-in
-// file store), which the case's chemicalDatabase names.
-int write_chem_db(const std::string& dir) {
-  std::ifstream in((dir + "chemdb.txt").c_str());
-  if (!in.is_open()) return 0;
-  hid_t f = HDF_CreateFile(dir + "chemdb.h5", 1);
-  if (f < 0) return -1;
-  std::string line, group;
-  while (std::getline(in, line)) {
-    std::istringstream ls(line);
-    std::string key;
-    if (!(ls >> key)) continue;
-    if (key == "species") {
-      std::string name;
-      ls >> name;
-      group = "/species/" + name;
-      continue;
-    }
-    std::vector<double> v;
-    double x;
-    while (ls >> x) v.push_back(x);
-    if (v.size() == 1) {
-      HDF_WriteScalar(f, group, key, &v[0]);
-    } else if (v.size() >= 2) {
-      const int rows = (int)v[0], cols = (int)v[1];
-      if ((size_t)rows * cols + 2 != v.size()) return -2;
-      HDF_WriteArray(f, group, key, &v[2], rows, cols);
-    }
-  }
-  HDF_CloseFile(f);
-  return 0;
 }
 
 }  // namespace

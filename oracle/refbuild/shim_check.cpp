@@ -20,6 +20,8 @@
 #include "solutionSpace.h"
 #include "limiters.h"
 #include "crs.h"
+#include "chem.h"
+#include "compressibleFR.h"
 #include "pcfd_shim.h"
 
 template void pcfd_shim::GatherMesh<double>(Mesh<double>*, pcfd_shim::MeshArrays&);
@@ -31,3 +33,10 @@ template void pcfd_shim::UpdateBCsGradientLimiter<double>(SolutionSpace<double>*
 template double pcfd_shim::ComputeTimesteps<double>(SolutionSpace<double>*, pcfd_solver_t, double*);
 template double pcfd_shim::JacobianAndSGS<double>(SolutionSpace<double>*, pcfd_solver_t);
 template double pcfd_shim::NewtonIterate<double>(SolutionSpace<double>*, pcfd_solver_t, int, int);
+template void pcfd_shim::ChemModelFrom<double>(const ChemModel<double>*, pcfd_chem_model&);
+template pcfd_chem_ref pcfd_shim::ChemRefFrom<double>(const Param<double>*);
+template pcfd_chem_t pcfd_shim::ChemCreate<double>(SolutionSpace<double>*, CompressibleFREqnSet<double>*,
+                                                   pcfd_shim::MeshArrays&);
+template void pcfd_shim::ChemBCs<double>(SolutionSpace<double>*, pcfd_shim::ChemBCTables&);
+template void pcfd_shim::ReactingSpatialResidual<double>(SolutionSpace<double>*, CompressibleFREqnSet<double>*,
+                                                         pcfd_chem_t);

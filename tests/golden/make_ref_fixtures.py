@@ -60,9 +60,9 @@ CASES = {
         eqn="compressibleNSFR", mach=2.0, sorder=2, limiter=3, nsgs=4, cfl=2.0, steps=2, amp=0.01,
         bc={1: "sonicInflow", 2: "sonicOutflow", 3: "noSlip", 4: "sonicOutflow", 5: "symmetry", 6: "symmetry"},
         twall={3: 1500.0}, reorder=1, chem="5speciesAir", temperature=3000.0, no_cvbc=1,
-        # mass fractions in the model's species order (N2, O2, NO, N, O: first appearance in the
-        # mechanism's reactions)
-        massfractions=[0.745, 0.2, 0.035, 0.01, 0.01]),
+        # mass fractions in the model's species order (O2, O, N, N2, NO: first appearance over the
+        # mechanism's reactions, ChemModel::BuildGlobalSpeciesList): partly dissociated air
+        massfractions=[0.2, 0.01, 0.01, 0.745, 0.035]),
 }
 
 

@@ -74,6 +74,8 @@ def lib():
                                                _DP]),
             "oracle_chem_limiter": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.MeshView), _DP, _DP, C.c_double,
                                            _DP]),
+            "oracle_chem_limiter_clip": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.MeshView),
+                                                _DP, _DP, C.c_double, _DP]),
             "oracle_chem_residual_ho": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
                                                C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), _DP, _DP, _DP,
                                                C.c_double, C.c_double, C.c_int, _DP, _DP]),
@@ -556,6 +558,15 @@ class OracleChemState:
         grad = np.ascontiguousarray(grad, np.float64)
         lim = np.empty((mesh.nnode, self.ns + 4))
         self.L.oracle_chem_limiter(C.byref(self.m), C.byref(mesh.view), dp(q), dp(grad), float(chi), dp(lim))
+        return lim
+
+    def limiter_clip(self, mesh, q, grad, chi):
+        """The limiter with the reacting pressure clip (Kernel_PressureClip)."""
+        q = np.ascontiguousarray(q, np.float64)
+        grad = np.ascontiguousarray(grad, np.float64)
+        lim = np.empty((mesh.nnode, self.ns + 4))
+        self.L.oracle_chem_limiter_clip(C.byref(self.m), C.byref(self.ref), C.byref(mesh.view), dp(q), dp(grad),
+                                        float(chi), dp(lim))
         return lim
 
     def residual_ho(self, opts, mesh, q, grad, lim, chi, ref_time, reactions):

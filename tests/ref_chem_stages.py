@@ -7,7 +7,9 @@ the CUDA path through the C ABI.
 Stages (ucs/solutionSpace.tcc:573-818): UpdateBCs as the reference runs it
 before a step's residual (the boundary pass of the step's set-up, then
 NewtonIterate's own); the LSQ gradient with the symmetry fix; the modified
-Venkatakrishnan limiter (step 2); ComputeResiduals (ucs/residual.tcc:13) -
+Venkatakrishnan limiter with the reacting pressure clip (step 2; the CUDA
+path has no clip, so its limiter is compared where the clip left a node
+alone); ComputeResiduals (ucs/residual.tcc:13) -
 inviscid HLLC (first order on step 1, second order with the limiter on step
 2), viscous (the directional correction once second order is on), the
 chemistry source, the temporal term a steady run still adds (Param::dt = -1:
@@ -70,6 +72,10 @@ class OracleEngine:
         return self.S.gradient(self.mesh, q, sym)
 
     def limiter(self, q, g, chi):
+        """with the reacting pressure clip, as Limiter::Compute runs it"""
+        return self.S.limiter_clip(self.mesh, q, g, chi)
+
+    def limiter_noclip(self, q, g, chi):
         return self.S.limiter(self.mesh, q, g, chi)
 
     def residual(self, opts, q, ref_time):

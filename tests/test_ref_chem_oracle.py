@@ -4,12 +4,15 @@ tests/golden/ref_fr_plate.npz is written by tests/golden/make_ref_fixtures.py
 from the reference itself (oracle/refbuild): the 5-species air mechanism of
 chemModels/5speciesAir.rxn with the species data of the reference's database
 builder, compressibleNSFR, second order with the modified Venkatakrishnan
-limiter, finite-rate chemistry on, on a jittered 7x6x5 box with sonic inflow,
+limiter, finite-rate chemistry on, partly dissociated air at 3000 K (mass
+fractions O2 0.2, O 0.01, N 0.01, N2 0.745, NO 0.035), on a jittered 7x6x5
+box with sonic inflow,
 outflow, an isothermal no-slip wall (1500 K) and mirror symmetry planes
 (noCVBC).  Each stage of the first two Newton steps is fed the reference's
 own input for that stage (tests/ref_chem_stages.py):
 
-* UpdateBCs, the reacting LSQ gradient and the limiter - bit-identical;
+* UpdateBCs, the reacting LSQ gradient and the limiter with its pressure
+  clip (Kernel_PressureClip zeroes 12 nodes' limiters here) - bit-identical;
 * ComputeResiduals (HLLC at first and second order, viscous, chemistry
   source, the steady temporal term, the no-slip rows) and its norms - to
   1e-13 of their scale: the oracle sums each node's edge contributions, the
@@ -62,7 +65,13 @@ def test_stages_match_reference(case):
             assert np.abs(got - want).max() <= RES_TOL * scale, (name, np.abs(got - want).max() / scale)
     assert {"s1_q_bc", "s1_qgrad", "s1_b", "s1_norms", "s2_q_bc", "s2_qgrad", "s2_limiter", "s2_b",
             "s2_norms"} <= seen
-    assert 0.0 < f["s2_limiter"].min() < 1.0  # the limiter is active somewhere
+    lim = f["s2_limiter"]
+    assert np.any((lim > 0.0) & (lim < 1.0))  # the limiter is active somewhere
+    # and the pressure clip zeroed some nodes whole, which the unclipped limiter does not
+    n, nt = E.mesh.nnode, 2 * E.ns + 4
+    raw = E.limiter_noclip(f["s2_q_bc"], f["s2_qgrad"].reshape(n, nt, 3), R.scalar(f, "chi"))
+    clipped = np.all(lim == 0.0, axis=1) & ~np.all(raw == 0.0, axis=1)
+    assert clipped.sum() > 0
 
 
 def test_boundary_update_is_idempotent_on_reference_state(case):
