@@ -250,6 +250,17 @@ PCFD_API int pcfd_coloring(pcfd_solver_t s, int* color_ptr, int* rows);
  * dnorm (|norm change of x over the last sweep|, the reference's return
  * value) optional. */
 PCFD_API int pcfd_sgs(pcfd_solver_t s, int nsweeps, double* x_out, double* dnorm);
+/* CRS<T>::GMRES's role (ucs/crs.tcc:176) for the Newton system: restarted
+ * flexible GMRES, right-preconditioned by nsgs block-SGS sweeps (>= 1), on
+ * the assembled matrix (pcfd_jacobian) with the residual of the last
+ * residual call as the right-hand side, from x = 0: m directions per restart
+ * (1..60), at most `restarts` restarts, until the relative residual falls
+ * below rtol.  x_out (optional) [nnode][5]; *relres (optional) the final
+ * relative residual estimate, *iters (optional) the Krylov iterations.  The
+ * Krylov vectors are FP32 when the matrix is stored in FP32 or BF16, FP64
+ * otherwise; x accumulates in FP64.  PCFD_ERR_STATE before a Jacobian. */
+PCFD_API int pcfd_fgmres(pcfd_solver_t s, int m, int restarts, double rtol, int nsgs, double* x_out, double* relres,
+                         int* iters);
 /* CRSMatrix::MatVecMultiply (ucs/crs.tcc:484): y = A x with the assembled
  * matrix, x and y host arrays [nnode][5].  vec_precision 0 multiplies FP64
  * vectors (the FGMRES solver of an FP64 system); 1 FP32 vectors (the FP32

@@ -167,6 +167,7 @@ PROTOTYPES = {
     "pcfd_nblocks": (C.c_longlong, [_P]),
     "pcfd_crs_structure": (C.c_int, [_P, _IP, _IP, _IP]),
     "pcfd_sgs": (C.c_int, [_P, C.c_int, _DP, _DP]),
+    "pcfd_fgmres": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, C.c_int, _DP, _DP, C.POINTER(C.c_int)]),
     "pcfd_matvec": (C.c_int, [_P, _DP, _DP, C.c_int]),
     "pcfd_sgs_rhs": (C.c_int, [_P, C.c_int, _DP, _DP, C.c_int]),
     "pcfd_coloring": (C.c_int, [_P, _IP, _IP]),

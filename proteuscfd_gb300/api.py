@@ -458,6 +458,17 @@ class SolutionSpace:
         N.check(self._lib.pcfd_sgs(self._h, int(nsweeps), N.dptr(x), C.byref(dn)), "pcfd_sgs")
         return x, dn.value
 
+    def fgmres(self, m=30, restarts=1, rtol=1e-3, nsgs=1):
+        """Flexible GMRES(m), right-preconditioned by nsgs SGS sweeps, on the
+        assembled system with the last residual as right-hand side, from
+        x = 0: returns (x, relative residual, Krylov iterations)."""
+        x = np.empty((self.mesh.nnode, NEQN), dtype=np.float64)
+        rel = C.c_double()
+        its = C.c_int()
+        N.check(self._lib.pcfd_fgmres(self._h, int(m), int(restarts), float(rtol), int(nsgs), N.dptr(x),
+                                      C.byref(rel), C.byref(its)), "pcfd_fgmres")
+        return x, rel.value, its.value
+
     def matvec(self, x, fp32=False):
         """y = A x with the assembled matrix (FP64 vectors, or FP32 vectors
         through the FP32 Krylov solver's product)."""

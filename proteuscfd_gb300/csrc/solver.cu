@@ -3552,6 +3552,31 @@ PCFD_API int pcfd_sgs(pcfd_solver_t h, int nsweeps, double* x_out, double* dnorm
   return check_sweeps(s);
 }
 
+PCFD_API int pcfd_fgmres(pcfd_solver_t h, int m, int restarts, double rtol, int nsgs, double* x_out, double* relres,
+                         int* iters) {
+  Solver* s = (Solver*)h;
+  if (!s || m < 1 || m > 60 || restarts < 1 || !(rtol > 0.0) || nsgs < 1)
+    return set_err(PCFD_ERR_ARG, "pcfd_fgmres: bad arguments");
+  if (!s->have_jac) return set_err(PCFD_ERR_STATE, "pcfd_fgmres: no Jacobian assembled");
+  pcfd_newton_opts o = {};
+  o.nsgs = nsgs;
+  o.fgmres_m = m;
+  o.fgmres_restarts = restarts;
+  o.fgmres_rtol = rtol;
+  CUDA_TRY(cudaMemsetAsync(s->d_x, 0, (size_t)s->nnode * NEQN * sizeof(double), s->stream));
+  double rel = 1.0;
+  int it = 0;
+  int rc = run_fgmres(s, &o, &rel, &it);
+  if (rc) return rc;
+  if (x_out)
+    CUDA_TRY(cudaMemcpyAsync(x_out, s->d_x, (size_t)s->nnode * NEQN * sizeof(double), cudaMemcpyDeviceToHost,
+                             s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (relres) *relres = rel;
+  if (iters) *iters = it;
+  return check_sweeps(s);
+}
+
 PCFD_API int pcfd_matvec(pcfd_solver_t h, const double* x, double* y, int vec_precision) {
   Solver* s = (Solver*)h;
   if (!s || !x || !y || vec_precision < 0 || vec_precision > 1) return set_err(PCFD_ERR_ARG, "pcfd_matvec: bad arguments");
