@@ -1006,6 +1006,76 @@ void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, con
   chem_limiter_clamp(m, mv, lim);
 }
 
+/* CompressibleFREqnSet::MaxEigenvalue (ucs/compressibleFR.tcc:1603) of a
+ * record with current auxiliary variables: the mixture's frozen speed of
+ * sound from GetFluidProperties (:1523; ChemModel::GetFluidProperties,
+ * ucs/chem.tcc:545: c^2 = (cp / cv) R T with Dalton's R and the mass-fraction
+ * weighted cp and cv = cp_i - R_i), and the acoustic eigenvalues modified by
+ * Gupta's preconditioning parameter beta. */
+static double fr_max_eigenvalue(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const double* Q,
+                                const double* avec, double vdotn, double beta) {
+  const int ns = m->nspecies;
+  const double T = Q[ns + 3];
+  double rhoiDim[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rhoiDim[i] = Q[i] * ref->density;
+  const double Tdim = T * ref->temperature;
+  double rho = 0.0, R = 0.0;
+  for (int i = 0; i < ns; i++) rho += rhoiDim[i];
+  for (int i = 0; i < ns; i++) R += rhoiDim[i] * (UNIV_R_ / m->mw[i]);
+  R /= rho;
+  double rhoX = 0.0, X[PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < ns; i++) rhoX += rhoiDim[i];
+  for (int i = 0; i < ns; i++) X[i] = rhoiDim[i] / rhoX;
+  double cp = 0.0, cv = 0.0;
+  for (int i = 0; i < ns; i++) cp += species_cp(m, i, Tdim) * X[i];
+  for (int i = 0; i < ns; i++) cv += X[i] * (species_cp(m, i, Tdim) - UNIV_R_ / m->mw[i]);
+  const double gamma = cp / cv;
+  const double c2 = (gamma * R * Tdim) / (ref->velocity * ref->velocity);
+  const double theta = Q[ns] * avec[0] + Q[ns + 1] * avec[1] + Q[ns + 2] * avec[2] + vdotn;
+  const double oneMBeta = 1.0 - beta;
+  const double thetaPrime = theta * (1.0 + beta) * 0.5;
+  const double cPrime = 0.5 * sqrt(theta * theta * (oneMBeta * oneMBeta) + 4.0 * beta * c2);
+  const double e4 = fabs(thetaPrime + cPrime), e5 = fabs(thetaPrime - cPrime);
+  return e4 > e5 ? e4 : e5;
+}
+
+/* ComputeTimesteps (ucs/timestep.tcc:7) of the reacting set with local time
+ * stepping on a static mesh: each edge's averaged record (its auxiliary
+ * variables recomputed) gives MaxEigenvalue x area to both ends
+ * (Kernel_Timestep, :80), each boundary half-edge its own to its node
+ * (Bkernel_Timestep, :115), summed in edge order, then half-edge order; dt =
+ * cfl vol / sum.  beta is the preconditioning parameter of every node (the
+ * reference fills its beta field with one value, ucs/solutionSpace.tcc:236-
+ * 248).  q [nnode + nbedge][6 + 3 ns] -> dt [nnode]; returns the smallest. */
+double oracle_chem_timestep(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_mesh_view* mv,
+                            const double* q, double beta, double cfl, double* dt) {
+  const int ns = m->nspecies, neqn = ns + 4, nv = 6 + 3 * ns;
+  double Qa[6 + 3 * PCFD_CHEM_MAX_SPECIES];
+  for (int i = 0; i < mv->nnode; i++) dt[i] = 0.0;
+  for (int e = 0; e < mv->nedge; e++) {
+    const int l = mv->edges[2 * e], r = mv->edges[2 * e + 1];
+    for (int j = 0; j < neqn; j++) Qa[j] = 0.5 * (q[(size_t)l * nv + j] + q[(size_t)r * nv + j]);
+    fr_aux(m, ref, Qa);
+    const double* a = &mv->edge_area[4 * (size_t)e];
+    const double v = fr_max_eigenvalue(m, ref, Qa, a, 0.0, 0.5 * (beta + beta)) * a[3];
+    dt[l] += v;
+    dt[r] += v;
+  }
+  for (int k = 0; k < mv->nbedge; k++) {
+    const int l = mv->bedges[2 * k], r = mv->bedges[2 * k + 1];
+    for (int j = 0; j < neqn; j++) Qa[j] = 0.5 * (q[(size_t)l * nv + j] + q[(size_t)r * nv + j]);
+    fr_aux(m, ref, Qa);
+    const double* a = &mv->bedge_area[4 * (size_t)k];
+    dt[l] += fr_max_eigenvalue(m, ref, Qa, a, 0.0, beta) * a[3];
+  }
+  double dtmin = 0.0;
+  for (int i = 0; i < mv->nnode; i++) {
+    dt[i] = cfl * (mv->vol[i] / dt[i]);
+    if (i == 0 || dt[i] < dtmin) dtmin = dt[i];
+  }
+  return dtmin;
+}
+
 /* CompressibleFREqnSet::BadExtrapolation (ucs/compressibleFR.tcc:714) of a
  * record whose auxiliary variables are current: a negative species density,
  * a total energy (GetTotalEnergy, :1219) not above zero, a pressure or a

@@ -114,6 +114,8 @@ void oracle_chem_residual_ho(const pcfd_chem_model* m, const pcfd_chem_ref* ref,
                              double chi, double ref_time, int reactions, double* b, double* norms);
 void oracle_chem_limiter(const pcfd_chem_model* m, const pcfd_mesh_view* mv, const double* q, const double* grad,
                          double chi, double* lim);
+double oracle_chem_timestep(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_mesh_view* mv,
+                            const double* q, double beta, double cfl, double* dt);
 void oracle_chem_limiter_clip(const pcfd_chem_model* m, const pcfd_chem_ref* ref, const pcfd_mesh_view* mv,
                               const double* q, const double* grad, double chi, double* lim);
 void oracle_chem_temporal_n(const pcfd_chem_model* m, const pcfd_chem_ref* ref, long long n, const double* q,

@@ -76,6 +76,8 @@ def lib():
                                            _DP]),
             "oracle_chem_limiter_clip": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef), C.POINTER(N.MeshView),
                                                 _DP, _DP, C.c_double, _DP]),
+            "oracle_chem_timestep": (C.c_double, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
+                                                  C.POINTER(N.MeshView), _DP, C.c_double, C.c_double, _DP]),
             "oracle_chem_residual_ho": (None, [C.POINTER(N.ChemModelC), C.POINTER(N.ChemRef),
                                                C.POINTER(N.ChemFluxOpts), C.POINTER(N.MeshView), _DP, _DP, _DP,
                                                C.c_double, C.c_double, C.c_int, _DP, _DP]),
@@ -559,6 +561,14 @@ class OracleChemState:
         lim = np.empty((mesh.nnode, self.ns + 4))
         self.L.oracle_chem_limiter(C.byref(self.m), C.byref(mesh.view), dp(q), dp(grad), float(chi), dp(lim))
         return lim
+
+    def timestep(self, mesh, q, beta, cfl):
+        """Local time steps of the reacting set -> (dt [nnode], smallest)."""
+        q = np.ascontiguousarray(q, np.float64)
+        dt = np.empty(mesh.nnode)
+        dtmin = self.L.oracle_chem_timestep(C.byref(self.m), C.byref(self.ref), C.byref(mesh.view), dp(q),
+                                            float(beta), float(cfl), dp(dt))
+        return dt, dtmin
 
     def limiter_clip(self, mesh, q, grad, chi):
         """The limiter with the reacting pressure clip (Kernel_PressureClip)."""

@@ -78,3 +78,18 @@ def test_boundary_update_is_idempotent_on_reference_state(case):
     f, bc, E = case
     for st in ("s1_", "s2_"):
         np.testing.assert_array_equal(E.update_bcs(f[st + "q_bc"], bc), f[st + "q_bc"], err_msg=st)
+
+
+def test_timestep_matches_reference(case):
+    """ComputeTimesteps of the reacting set (MaxEigenvalue with the mixture's
+    frozen speed of sound, beta = 1 above Mach 1) with local time stepping:
+    at PreIterate on the initial state, and at PreTimeAdvance on the state
+    after the set-up's boundary pass - bit-identical, with dtmin."""
+    f, bc, E = case
+    cfl = R.scalar(f, "case_cfl")
+    assert R.scalar(f, "velocity") > 1.0  # the reference's beta field is then 1 everywhere
+    dt0, _ = E.S.timestep(E.mesh, f["q_init"], 1.0, cfl)
+    np.testing.assert_array_equal(dt0, f["dt_preiterate"])
+    dt1, dtmin = E.S.timestep(E.mesh, E.update_bcs(f["q_init"], bc), 1.0, cfl)
+    np.testing.assert_array_equal(dt1, f["dt"])
+    assert dtmin == R.scalar(f, "dtmin")
