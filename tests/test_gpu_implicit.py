@@ -196,29 +196,6 @@ def test_fgmres_reduces_linear_residual():
         assert np.isfinite(rep["dqnorm"]) and rep["dqnorm"] > 0
 
 
-def test_fgmres_entry_point_solves_the_assembled_system():
-    """pcfd_fgmres on the system pcfd_jacobian and the residual left: the
-    library's own product of its solution meets the right-hand side to the
-    requested tolerance (FP64 storage), or to the FP32 Krylov solver's
-    accuracy (FP32 storage); and a call before any Jacobian is refused."""
-    m, S, O, q0 = setup(ns_case(3))
-    S.set_state(q0)
-    with pytest.raises(N.PcfdError):
-        S.fgmres(10, 1, 1e-3, 1)
-    for prec, rtol, bar in ((0, 1e-8, 1e-7), (1, 1e-4, 1e-3)):
-        S.set_state(q0)
-        S.set_jacobian_precision(prec)
-        S.compute_timesteps(5.0)
-        S.compute_jacobians()
-        S.residual_full()
-        b = S.compute_residuals()[0]
-        x, rel, its = S.fgmres(20, 10, rtol, 1)
-        assert rel < rtol and its > 0, (prec, rel, its)
-        true_rel = np.linalg.norm(S.matvec(x) - b) / np.linalg.norm(b)
-        assert true_rel < bar, (prec, true_rel)
-    S.set_jacobian_precision(0)
-
-
 def star_mesh(npts=40):
     """A ball of tets around one centre node joined to npts hull vertices:
     its Jacobian row has npts off-diagonal blocks, past the block counts the
